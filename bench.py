@@ -1,0 +1,299 @@
+"""Benchmark of the plain full step (bin, scan, stable sort with bond remap, density/pressure,
+diffusion + gene reaction, bond + fluid force, integration) at 1,048,576 particles.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is whole-job particle-steps/s with the state resident in HBM
+(CUDA events around K graph-replayed steps on the library's stream); `e2e` is the same metric
+through the public C-ABI with the per-step dynamic state (FPOS, FVEL, FVEVAL, FCONC) copied
+from pinned host buffers and back every step.  Multi-GPU runs are independent replicas
+(a single tissue instance has no data-parallel split here), so scaling is weak.
+`--impl reference` times the CPU restatement of the reference step (the reference itself
+does not build or run here) with every host thread on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s at 1M (plain vs MLP surrogate, conc err≤1e-3); % HBM roofline"
+UNIT = "particle-steps/s"
+DIMS = (128, 64, 128)          # 1,048,576 particles
+PARAM = "R"
+FALLBACK_HBM = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max/sum reductions across ranks (gloo on CPU tensors), no-ops at N=1."""
+
+    def __init__(self, world: int):
+        self.world = world
+        if world > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX if op == "max" else self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1])); smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if one exists."""
+    f = ROOT / "profiles" / "traffic.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        v = d.get(kernel)
+        if isinstance(v, dict):
+            return v.get("bytes_per_launch_full_size")
+    return None
+
+
+def cpu_reference(steps: int, warmup: int, threads: int):
+    """The oracle (CPU restatement of the reference step) on the same workload."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+    from morphogenesis_gb300 import demo
+
+    orc.build()
+    used = orc.set_threads(threads)
+    d = demo.make_block(DIMS, PARAM, seed=0)
+    o = orc.Oracle(d.params, d.genome, d.n)
+    o.upload_all(d.arrays)
+    if warmup:
+        o.step(warmup)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return d.n * steps / dt, used, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    steps = max(1, args.steps if args.steps <= 20 else 20)
+    warm = min(args.warmup, 1)
+    value, used, dt = cpu_reference(steps, warm, threads)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded jittered 128x64x128 lattice, 6 bonds/particle, 16 species, 16 gene bits",
+        "config": {"workload": "plain full step, 1,048,576 particles (128x64x128 lattice), grid 132^3, gsrch 3",
+                   "parameterisation": PARAM},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port",
+                         "sample": f"{steps} steps of the 1,048,576-particle workload after {warm} warm-up"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own compute path does not build or run here (OpenCL/CUDA hybrid; "
+                "no CL headers, ICD, jsoncpp or VTK); this is the oracle restatement of it",
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import morphogenesis_gb300 as mg
+    from morphogenesis_gb300 import _abi as A
+    from morphogenesis_gb300 import demo
+
+    dist = Dist(world)
+    d = demo.make_block(DIMS, PARAM, seed=rank)
+    fs = mg.FluidSystem(d.params, d.genome, d.n)
+    fs.TransferToCL(d.arrays)
+    flags = A.STEP_DEFAULT
+    fs.Run(max(args.warmup, 3), flags)
+    n = d.n
+    cells = int(d.params.grid_total)
+
+    # ---- timed region: K graph-replayed steps, state resident in HBM ----
+    clocks = Clocks(local if world > 1 else int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0))
+    launches0 = fs.kernel_launches()
+    dist.barrier()
+    fs.synchronize()
+    ms = fs.time_steps(args.steps, flags)
+    fs.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    launches = fs.kernel_launches() - launches0
+    ms_max = dist.reduce(ms, "max")
+    total_particle_steps = dist.reduce(float(n * args.steps), "sum")
+    value = total_particle_steps / (ms_max / 1e3)
+
+    # ---- per-kernel device times over K profiled steps (events around every launch) ----
+    fs.profile(True)
+    fs.Run(args.steps, flags)
+    prof = fs.profile_read()
+    fs.profile(False)
+    top = max(prof.items(), key=lambda kv: kv[1][1])
+    tot_ms = sum(v[1] for v in prof.values())
+    kname, (klaunch, kms) = top
+    bpp, bpc = fs.algorithmic_bytes(kname, flags)
+    kbytes = bpp * n + bpc * cells
+    achieved = kbytes / (kms / klaunch / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    sbpp, sbpc = fs.algorithmic_bytes(None, flags)
+    step_bytes = sbpp * n + sbpc * cells
+    traffic = ncu_traffic(kname)
+
+    # ---- end to end through the C-ABI with host buffers ----
+    e2e_bufs = [A.FPOS, A.FVEL, A.FVEVAL, A.FCONC]
+    host = {}
+    for b in e2e_bufs:
+        dt_, shape = mg._shape(b, n, cells)
+        host[b] = mg.pinned_empty(shape, dt_)
+        fs.download(b, host[b])
+    h2d = sum(host[b].nbytes for b in e2e_bufs)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        for b in e2e_bufs:
+            fs.upload(b, host[b])
+        fs.Run(1, flags)
+        for b in e2e_bufs:
+            fs.download(b, host[b])
+    e2e_s = time.perf_counter() - t0
+    e2e_s = dist.reduce(e2e_s, "max")
+    e2e_total = dist.reduce(float(n * args.e2e_steps), "sum")
+    e2e_value = e2e_total / e2e_s
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cval, used, cdt = cpu_reference(args.cpu_steps, 0, threads)
+        cpu = {"value": cval, "unit": UNIT, "cores": used, "kind": "port",
+               "sample": f"{args.cpu_steps} steps of the same 1,048,576-particle workload ({cdt:.1f} s)"}
+    fs.close()
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded jittered 128x64x128 lattice, 6 bonds/particle, 16 species, 16 gene bits",
+            "config": {"workload": "plain full step, 1,048,576 particles (128x64x128 lattice), grid 132^3, gsrch 3",
+                       "parameterisation": PARAM, "particles_per_gpu": n, "cells": cells,
+                       "l2": f"inputs larger than L2: step state {step_bytes / 1e9:.2f} GB/step",
+                       "parallelism": f"replicas x{world}"},
+            "clocks": clk,
+            "gpu_launches": int(launches),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                    "steps": args.e2e_steps},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "kernel": kname,
+                         "kernel_share": kms / tot_ms, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": kbytes},
+            "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
+                              "achieved_gbs": step_bytes / (ms_max / args.steps / 1e3) / 1e9,
+                              "frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak},
+            "kernels_ms_per_launch": {k: v[1] / v[0] for k, v in prof.items()},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,239 @@
+/*
+ * mg_abi.h - C-ABI of the GB300 per-timestep particle pipeline (Morphogenesis drop-in).
+ *
+ * This is the boundary a host program links against in place of the reference's
+ * FluidSystem compute backend (Morphogenesis src/host_CL.cpp, src/host_CUDA.cpp and the
+ * FluidSystem run/transfer methods in src/fluid_system.cpp).  Every entry point is plain C:
+ * host pointers and sizes in, an mg_status out.  No CUDA or torch types appear here.
+ *
+ * Ownership: a handle owns all device memory for its particles and grid (the reference's
+ * FluidSystem owns mgpu[] per buffer id, fluid.h:239-242).  Host pointers are borrowed for
+ * the duration of a call only.  Errors are returned, never exit()ed; mg_last_error() gives
+ * the text.  A handle is single-threaded (one CUDA stream, like the reference's one
+ * in-order queue, fluid_system.h:365); distinct handles may be used from distinct threads.
+ *
+ * Buffer ids are numerically equal to the reference's F* ids (fluid.h:138-206) and the bytes
+ * exchanged by mg_upload/mg_download use the reference's device element layouts:
+ *   FPOS/FVEL/FVEVAL/FFORCE  float[N][4]            (cl_float3, 16 bytes)
+ *   FPRESS/FDENSITY          float[N]               (FDENSITY holds 1/density)
+ *   FAGE/FCOLOR/FGCELL/FGNDX/FBIN/FPARTICLE_ID/FMASS_RADIUS/FNERVEIDX  uint32[N]
+ *   FELASTIDX                uint32[N][6][9]        (words 1-4 and 6-7 are float bits)
+ *   FPARTICLEIDX             uint32[N][12]          ((particle, bond) pairs of incoming bonds)
+ *   FCONC                    float[N][16]           (device layout used by the kernels)
+ *   FEPIGEN                  uint32[16][N]          ([gene][particle])
+ *   FBIN_COUNT/FBIN_OFFSET   uint32[grid_total]
+ *   FBIN_COUNT_ACTIVE_GENES/FBIN_OFFSET_ACTIVE_GENES  uint32[16][grid_total]
+ *   FDENSE_LIST_LENGTHS      uint32[16]
+ *   FDENSE_LISTS             uint32[16][N]          (list g padded with 0xFFFFFFFF)
+ * N is the max_points given to mg_create (the reference's mMaxPoints).
+ */
+#ifndef MG_ABI_H
+#define MG_ABI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- sizes (fluid.h:72-103) ---------------------------------------------------------- */
+#define MG_BONDS_PER_PARTICLE 6
+#define MG_DATA_PER_BOND 9
+#define MG_BOND_DATA (MG_BONDS_PER_PARTICLE * MG_DATA_PER_BOND)
+#define MG_NUM_TF 16
+#define MG_NUM_GENES 16
+#define MG_NUM_CHANGES 9
+#define MG_GRID_UNDEF 0xFFFFFFFFu   /* fluid_system_cuda.cuh:43 */
+/* "No bond" partner index.  The reference writes UINT_MAXSIZE=65535 (fluid_system.cpp:22),
+ * which is a valid particle index once N > 65535; any index >= N means "no bond" on input
+ * and the pipeline writes this value. */
+#define MG_NO_PARTNER 0xFFFFFFFFu
+#define MG_EPIGEN_ACTIVE 2147483647u /* INT_MAX, "fixedActive" (fluid_system.cpp:1110) */
+
+/* ---- buffer ids (fluid.h:138-206) ------------------------------------------------------- */
+enum mg_buf {
+    MG_FPOS = 0, MG_FVEL = 1, MG_FVEVAL = 2, MG_FFORCE = 3, MG_FPRESS = 4, MG_FDENSITY = 5,
+    MG_FAGE = 6, MG_FCOLOR = 7, MG_FGCELL = 8, MG_FGNDX = 9, MG_FGNEXT = 10, MG_FNBRNDX = 11,
+    MG_FNBRCNT = 12, MG_FCLUSTER = 13, MG_FELASTIDX = 14, MG_FNERVEIDX = 15, MG_FCONC = 16,
+    MG_FEPIGEN = 17, MG_FBIN = 18, MG_FBIN_COUNT = 19, MG_FBIN_OFFSET = 20, MG_FBIN_ACT = 21,
+    MG_FSTATE = 22, MG_FPARAMS = 24, MG_FAUXARRAY1 = 25, MG_FAUXSCAN1 = 26, MG_FAUXARRAY2 = 27,
+    MG_FAUXSCAN2 = 28, MG_FPARTICLEIDX = 29, MG_FPARTICLE_ID = 30, MG_FMASS_RADIUS = 31,
+    MG_FBIN_COUNT_ACTIVE_GENES = 32, MG_FBIN_OFFSET_ACTIVE_GENES = 33,
+    MG_FDENSE_LIST_LENGTHS = 34, MG_FDENSE_LISTS = 35, MG_FDENSE_BUF_LENGTHS = 36,
+    MG_FBIN_OFFSET_CHANGES = 37, MG_FBIN_COUNT_CHANGES = 38, MG_FDENSE_LIST_LENGTHS_CHANGES = 39,
+    MG_FDENSE_LISTS_CHANGES = 40, MG_FDENSE_BUF_LENGTHS_CHANGES = 41, MG_FCURAND_STATE = 42,
+    MG_FCURAND_SEED = 43, MG_MAX_BUF = 44
+};
+
+/* ---- scalar parameter ids for mg_set_param (fluid_system.h:77-103) --------------------- */
+enum mg_param {
+    MG_PSIMSCALE = 4, MG_PVISC = 7, MG_PRESTDENSITY = 8, MG_PMASS = 9, MG_PRADIUS = 10,
+    MG_PSMOOTHRADIUS = 12, MG_PINTSTIFF = 13, MG_PEXTSTIFF = 14, MG_PEXTDAMP = 15,
+    MG_PACCEL_LIMIT = 16, MG_PVEL_LIMIT = 17, MG_PGROUND_SLOPE = 19, MG_PFORCE_MIN = 20,
+    MG_PFORCE_MAX = 21, MG_PFORCE_FREQ = 23, MG_PSURFACE_TENSION = 24,
+    MG_PACTUATION_FACTOR = 25, MG_PACTUATION_PERIOD = 26,
+    /* run controls with no m_Param id in the reference (m_DT, m_Time, FParams.freeze) */
+    MG_PDT = 100, MG_PTIME = 101, MG_PFREEZE = 102
+};
+
+typedef enum mg_status {
+    MG_OK = 0,
+    MG_ERR_INVALID_ARG = 1,
+    MG_ERR_OOM = 2,
+    MG_ERR_GRID_OVERFLOW = 3,   /* a grid cell holds more particles than the sort supports */
+    MG_ERR_LIST_OVERFLOW = 4,
+    MG_ERR_DEVICE_TIMEOUT = 5,  /* a bounded device-side wait gave up */
+    MG_ERR_CUDA = 6,
+    MG_ERR_UNSUPPORTED = 7,
+    MG_ERR_INCONSISTENT = 8     /* uploaded state violates an invariant the pipeline needs */
+} mg_status;
+
+/* Flags for mg_step. */
+enum mg_step_flags {
+    MG_STEP_PHYSICS = 1u << 0,   /* pressure, force, advance */
+    MG_STEP_GENES = 1u << 1,     /* diffusion + gene reaction */
+    MG_STEP_REMODEL = 1u << 2,   /* bond break/re-form (heal) */
+    MG_STEP_FREEZE = 1u << 3,    /* bonds do not break this step (FParams.freeze) */
+    MG_STEP_SURROGATE = 1u << 4, /* learned reaction instead of the plain gene reaction */
+    MG_STEP_DEFAULT = MG_STEP_PHYSICS | MG_STEP_GENES
+};
+
+/*
+ * Simulation parameters: the arguments of FluidParamCL (fluid_system.cpp:521) and of
+ * FluidSetupCL (host_CL.cpp:39), plus the run controls m_DT, m_Time and freeze.
+ * Derived constants (r2, H, d2, rd2, AL2, VL2, Wendland normalisation, gridAdj, gridScanMax)
+ * are computed inside the library exactly as FluidParamCL/FluidSetupCL compute them.
+ */
+typedef struct mg_fparams {
+    float psimscale;         /* ss */
+    float psmoothradius;     /* sr, simulation units */
+    float pradius;           /* pr */
+    float pmass;
+    float prest_dens;
+    float pboundmin[3];
+    float pboundmax[3];
+    float pextstiff;
+    float pintstiff;
+    float pvisc;
+    float psurface_t;
+    float pdamp;
+    float pforce_min;
+    float pforce_max;
+    float pforce_freq;
+    float pground_slope;
+    float pgravity[3];
+    float paccel_limit;      /* al */
+    float pvel_limit;        /* vl */
+    float actuation_factor;  /* a_f */
+    float actuation_period;  /* a_p */
+    int32_t grid_res[3];
+    int32_t grid_srch;       /* gsrch: 1-D neighbour search width (2..4) */
+    float grid_size[3];
+    float grid_delta[3];
+    float grid_min[3];
+    float grid_max[3];
+    int32_t grid_total;
+    float dt;                /* m_DT */
+    float time;              /* m_Time */
+    int32_t freeze;          /* FParams.freeze */
+    int32_t debug;
+} mg_fparams;
+
+/*
+ * Genome (fluid.h:398-422) with the fields the gene kernel reads as fractions widened to
+ * float: sensitivity is a signed weight, diffusability and breakdown are rates, and the
+ * secrete/activate sparse lists hold (index, value) pairs with the count in entry [2*16];
+ * indices and counts are small exact integers stored as float.
+ */
+typedef struct mg_genome {
+    uint32_t mutability[MG_NUM_GENES];
+    uint32_t delay[MG_NUM_GENES];
+    float sensitivity[MG_NUM_GENES][MG_NUM_TF];
+    float tf_diffusability[MG_NUM_TF];
+    float tf_breakdown_rate[MG_NUM_TF];
+    float secrete[MG_NUM_GENES][2 * MG_NUM_TF + 1];
+    float activate[MG_NUM_GENES][2 * MG_NUM_GENES + 1];
+    float tanh_param[3][8];
+    float param[3][12];
+} mg_genome;
+
+typedef struct mg_system* mg_handle;
+
+/* ---- host-only helpers (no GPU needed) ------------------------------------------------- */
+
+/* SetupGrid (fluid_system.cpp:2073-2131): fills grid_res/size/delta/min/max/total/srch of p
+ * from the volume corners, the cell size in simulation units and p->psmoothradius /
+ * p->psimscale.  gsrch_override > 0 replaces the computed search width, as FluidSetupCL's
+ * own gsrch argument does (host_CL.cpp:39,55). */
+mg_status mg_setup_grid(mg_fparams* p, const float vol_min[3], const float vol_max[3],
+                        float cell_size, int32_t gsrch_override);
+
+/* Library version string. */
+const char* mg_version(void);
+
+/* Last error text of a handle (or of the calling thread when h is NULL). */
+const char* mg_last_error(mg_handle h);
+
+/* ---- lifetime (FluidSetupCL + AllocateParticles + AllocateGrid, host_CL.cpp:39-174) ---- */
+mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t max_points,
+                    mg_handle* out);
+mg_status mg_destroy(mg_handle h);
+
+/* UpdateParams / FluidParamCL (fluid_system.cpp:521-610): grid fields must match creation. */
+mg_status mg_update_params(mg_handle h, const mg_fparams* params);
+/* UpdateGenome (fluid_system.cpp:494). */
+mg_status mg_update_genome(mg_handle h, const mg_genome* genome);
+/* SetParam(id, value) on m_Param ids (fluid_system.h:77-103) plus MG_PDT/MG_PTIME/MG_PFREEZE. */
+mg_status mg_set_param(mg_handle h, int32_t param_id, float value);
+mg_status mg_get_params(mg_handle h, mg_fparams* out);
+
+/* ---- transfer (TransferToCL / TransferFromCL, host_CL.cpp:1608-1668) -------------------- */
+mg_status mg_buffer_bytes(mg_handle h, int32_t buf_id, size_t* bytes);
+mg_status mg_upload(mg_handle h, int32_t buf_id, const void* host, size_t bytes);
+mg_status mg_download(mg_handle h, int32_t buf_id, void* host, size_t bytes);
+/* Page-locked host buffers for mg_upload/mg_download (copies from them run at full link
+ * bandwidth).  Convenience with no counterpart in the reference. */
+mg_status mg_host_alloc(size_t bytes, void** out);
+mg_status mg_host_free(void* ptr);
+/* mNumPoints (particles in the grid after the last sort) and mActivePoints. */
+mg_status mg_get_counts(mg_handle h, uint32_t* num_points, uint32_t* active_points);
+
+/* ---- stages (the *CL wrappers of host_CL.cpp / host_CUDA.cpp) --------------------------- */
+mg_status mg_insert_particles(mg_handle h);     /* InsertParticlesCL, host_CL.cpp:228-426 */
+mg_status mg_prefix_sum_cells(mg_handle h);     /* PrefixSumCellsCL, host_CL.cpp:429-863 */
+mg_status mg_counting_sort_full(mg_handle h);   /* CountingSortFullCL, host_CL.cpp:1064-1413 */
+mg_status mg_compute_pressure(mg_handle h);     /* ComputePressureCL, host_CL.cpp:1918 */
+mg_status mg_compute_force(mg_handle h);        /* ComputeForceCL, host_CL.cpp:1950 */
+mg_status mg_compute_diffusion(mg_handle h);    /* ComputeDiffusionCL, host_CL.cpp:1936 */
+mg_status mg_compute_genes(mg_handle h);        /* ComputeGenesCL, host_CL.cpp:1965-2019 */
+mg_status mg_advance(mg_handle h);              /* AdvanceCL + AdvanceTime, host_CL.cpp:2182 */
+
+/* ---- run loop (fluid_system.cpp:1919-2014) ---------------------------------------------- */
+mg_status mg_run_physical_sort(mg_handle h);        /* Run2PhysicalSort */
+mg_status mg_run_inner_physical_loop(mg_handle h);  /* Run2InnerPhysicalLoop */
+mg_status mg_run_gene_action(mg_handle h);          /* Run2GeneAction */
+/* nsteps full steps in the legacy Run() order (fluid_system.cpp:1179-1349), one sort per
+ * step: insert, scan, sort, pressure, force, diffusion, genes, [remodel], advance, time. */
+mg_status mg_step(mg_handle h, uint32_t nsteps, uint32_t flags);
+mg_status mg_synchronize(mg_handle h);
+
+/* ---- measurement ------------------------------------------------------------------------- */
+/* Runs nsteps of mg_step and returns their device time (CUDA events on the handle's stream). */
+mg_status mg_time_steps(mg_handle h, uint32_t nsteps, uint32_t flags, float* ms);
+/* Per-kernel device time: when enabled, every stage kernel launch of mg_step is bracketed by
+ * CUDA events; mg_profile_read returns, per kernel slot, launches and total milliseconds. */
+mg_status mg_profile_enable(mg_handle h, int32_t enable);
+mg_status mg_profile_read(mg_handle h, int32_t max_slots, char* names /* max_slots*32 */,
+                          uint32_t* launches, double* total_ms, int32_t* nslots);
+/* Algorithmic DRAM bytes per particle and per cell of one kernel slot (by name) or of the
+ * whole step (name NULL), for the roofline. */
+mg_status mg_algorithmic_bytes(mg_handle h, const char* kernel, uint32_t flags,
+                               double* bytes_per_particle, double* bytes_per_cell);
+/* Number of GPU kernels mg_step/mg_time_steps have launched on this handle. */
+uint64_t mg_kernel_launches(mg_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MG_ABI_H */

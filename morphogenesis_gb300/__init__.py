@@ -1,0 +1,246 @@
+"""GB300-native per-timestep particle pipeline of the Morphogenesis simulator.
+
+``FluidSystem`` mirrors the reference's host API names (src/fluid_system.h) over the C-ABI
+of ``include/mg_abi.h``; every stage runs as a hand-written sm_103a kernel of the in-tree
+library ``_build/libmg_gb300.so``.  There is no CPU fallback: constructing a FluidSystem
+without the built library or without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from ._abi import MgError, load  # noqa: F401
+
+__all__ = ["FluidSystem", "MgError", "load", "A", "pinned_empty"]
+
+
+class _Pinned:
+    """Owner of one page-locked host allocation (freed with the last numpy view)."""
+
+    def __init__(self, nbytes: int):
+        self.lib = load()
+        self.ptr = C.c_void_p()
+        st = self.lib.mg_host_alloc(nbytes, C.byref(self.ptr))
+        if st != A.MG_OK:
+            raise MgError(st, (self.lib.mg_last_error(None) or b"").decode())
+        self.nbytes = nbytes
+
+    def __del__(self):
+        if self.ptr:
+            self.lib.mg_host_free(self.ptr)
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype) -> np.ndarray:
+    """numpy array in page-locked host memory (for full-bandwidth transfers)."""
+    dt = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dt.itemsize
+    owner = _Pinned(max(nbytes, 1))
+    buf = (C.c_char * nbytes).from_address(owner.ptr.value)
+    arr = np.frombuffer(buf, dtype=dt).reshape(shape)
+    return _PinnedArray(arr, owner)
+
+
+class _PinnedArray(np.ndarray):
+    def __new__(cls, arr, owner):
+        obj = arr.view(cls)
+        obj._owner = owner
+        return obj
+
+    def __array_finalize__(self, obj):
+        if obj is not None:
+            self._owner = getattr(obj, "_owner", None)
+
+
+def _shape(buf: int, n: int, cells: int):
+    f32, u32 = np.float32, np.uint32
+    if buf in (A.FPOS, A.FVEL, A.FVEVAL, A.FFORCE):
+        return f32, (n, 4)
+    if buf in (A.FPRESS, A.FDENSITY):
+        return f32, (n,)
+    if buf in (A.FAGE, A.FCOLOR, A.FGCELL, A.FGNDX, A.FBIN, A.FPARTICLE_ID, A.FMASS_RADIUS,
+               A.FNERVEIDX):
+        return u32, (n,)
+    if buf == A.FELASTIDX:
+        return u32, (n, A.BOND_DATA)
+    if buf == A.FPARTICLEIDX:
+        return u32, (n, 12)
+    if buf == A.FCONC:
+        return f32, (n, A.NUM_TF)
+    if buf == A.FEPIGEN:
+        return u32, (A.NUM_GENES, n)
+    if buf in (A.FBIN_COUNT, A.FBIN_OFFSET):
+        return u32, (cells,)
+    if buf in (A.FBIN_COUNT_ACTIVE_GENES, A.FBIN_OFFSET_ACTIVE_GENES):
+        return u32, (A.NUM_GENES, cells)
+    if buf == A.FDENSE_LIST_LENGTHS:
+        return u32, (A.NUM_GENES,)
+    if buf == A.FDENSE_LISTS:
+        return u32, (A.NUM_GENES, n)
+    raise ValueError(f"buffer id {buf} is not exchanged")
+
+
+class FluidSystem:
+    """Host object of one simulation (reference: class FluidSystem, fluid_system.h:357-766).
+
+    Setup mirrors FluidSetupCL + FluidParamCL + UpdateGenome + AllocateParticles/AllocateGrid;
+    TransferToCL/TransferFromCL move buffers in the reference layouts; the *CL stage methods
+    and Run2* loops launch the GPU kernels.
+    """
+
+    def __init__(self, params: A.FParams, genome: A.Genome, max_points: int):
+        self.lib = load()
+        self.params = params
+        self.genome = genome
+        self.max_points = int(max_points)
+        self.cells = int(params.grid_total)
+        h = C.c_void_p()
+        self._check(self.lib.mg_create(C.byref(params), C.byref(genome), self.max_points, C.byref(h)), None)
+        self.h = h
+
+    # -- lifetime -----------------------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.mg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, status: int, h=...) -> None:
+        if status != A.MG_OK:
+            handle = self.h if h is ... else h
+            msg = self.lib.mg_last_error(handle)
+            raise MgError(status, (msg or b"").decode())
+
+    # -- parameters -----------------------------------------------------------------------------
+    def UpdateParams(self, params: A.FParams | None = None) -> None:
+        if params is not None:
+            self.params = params
+        self._check(self.lib.mg_update_params(self.h, C.byref(self.params)))
+
+    def UpdateGenome(self, genome: A.Genome | None = None) -> None:
+        if genome is not None:
+            self.genome = genome
+        self._check(self.lib.mg_update_genome(self.h, C.byref(self.genome)))
+
+    def SetParam(self, param_id: int, value: float) -> None:
+        self._check(self.lib.mg_set_param(self.h, param_id, float(value)))
+
+    def GetParams(self) -> A.FParams:
+        p = A.FParams()
+        self._check(self.lib.mg_get_params(self.h, C.byref(p)))
+        return p
+
+    # -- transfer -------------------------------------------------------------------------------
+    def upload(self, buf: int, arr: np.ndarray) -> None:
+        dt, shape = _shape(buf, self.max_points, self.cells)
+        a = np.ascontiguousarray(arr, dtype=dt)
+        if a.shape != shape:
+            raise ValueError(f"buffer {buf}: expected shape {shape}, got {a.shape}")
+        self._check(self.lib.mg_upload(self.h, buf, a.ctypes.data, a.nbytes))
+
+    def download(self, buf: int, out: np.ndarray | None = None) -> np.ndarray:
+        dt, shape = _shape(buf, self.max_points, self.cells)
+        if out is None:
+            out = np.empty(shape, dt)
+        self._check(self.lib.mg_download(self.h, buf, out.ctypes.data, out.nbytes))
+        return out
+
+    def TransferToCL(self, arrays: dict) -> None:
+        for buf, arr in arrays.items():
+            self.upload(buf, arr)
+
+    def TransferFromCL(self, bufs=(A.FPOS, A.FVEL, A.FVEVAL, A.FFORCE, A.FPRESS, A.FDENSITY,
+                                   A.FELASTIDX, A.FPARTICLEIDX, A.FCONC, A.FEPIGEN,
+                                   A.FPARTICLE_ID)) -> dict:
+        return {b: self.download(b) for b in bufs}
+
+    def getPos(self) -> np.ndarray:
+        return self.download(A.FPOS)
+
+    def getVel(self) -> np.ndarray:
+        return self.download(A.FVEL)
+
+    def getElastIdx(self) -> np.ndarray:
+        return self.download(A.FELASTIDX)
+
+    def getParticle_Idx(self) -> np.ndarray:
+        return self.download(A.FPARTICLEIDX)
+
+    def getConc(self) -> np.ndarray:
+        return self.download(A.FCONC)
+
+    def getEpiGen(self) -> np.ndarray:
+        return self.download(A.FEPIGEN)
+
+    def counts(self) -> tuple[int, int]:
+        """(mNumPoints, mActivePoints) after the last sort."""
+        a, b = C.c_uint32(), C.c_uint32()
+        self._check(self.lib.mg_get_counts(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    # -- stages (host_CL.cpp *CL wrappers) --------------------------------------------------------
+    def InsertParticlesCL(self) -> None: self._check(self.lib.mg_insert_particles(self.h))
+    def PrefixSumCellsCL(self) -> None: self._check(self.lib.mg_prefix_sum_cells(self.h))
+    def CountingSortFullCL(self) -> None: self._check(self.lib.mg_counting_sort_full(self.h))
+    def ComputePressureCL(self) -> None: self._check(self.lib.mg_compute_pressure(self.h))
+    def ComputeForceCL(self) -> None: self._check(self.lib.mg_compute_force(self.h))
+    def ComputeDiffusionCL(self) -> None: self._check(self.lib.mg_compute_diffusion(self.h))
+    def ComputeGenesCL(self) -> None: self._check(self.lib.mg_compute_genes(self.h))
+    def AdvanceCL(self) -> None: self._check(self.lib.mg_advance(self.h))
+
+    # -- run loop (fluid_system.cpp Run2*) --------------------------------------------------------
+    def Run2PhysicalSort(self) -> None: self._check(self.lib.mg_run_physical_sort(self.h))
+    def Run2InnerPhysicalLoop(self) -> None: self._check(self.lib.mg_run_inner_physical_loop(self.h))
+    def Run2GeneAction(self) -> None: self._check(self.lib.mg_run_gene_action(self.h))
+
+    def Run(self, nsteps: int = 1, flags: int = A.STEP_DEFAULT) -> None:
+        """nsteps steps in the legacy Run() order (one sort per step), graph-captured."""
+        self._check(self.lib.mg_step(self.h, int(nsteps), int(flags)))
+
+    def time_steps(self, nsteps: int, flags: int = A.STEP_DEFAULT) -> float:
+        ms = C.c_float()
+        self._check(self.lib.mg_time_steps(self.h, int(nsteps), int(flags), C.byref(ms)))
+        return float(ms.value)
+
+    def synchronize(self) -> None:
+        self._check(self.lib.mg_synchronize(self.h))
+
+    def profile(self, enable: bool = True) -> None:
+        self._check(self.lib.mg_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        n = C.c_int32()
+        self._check(self.lib.mg_profile_read(self.h, 0, None, None, None, C.byref(n)))
+        k = n.value
+        names = C.create_string_buffer(32 * max(k, 1))
+        launches = (C.c_uint32 * max(k, 1))()
+        ms = (C.c_double * max(k, 1))()
+        self._check(self.lib.mg_profile_read(self.h, k, names, launches, ms, C.byref(n)))
+        out = {}
+        for i in range(k):
+            nm = names.raw[32 * i:32 * i + 32].split(b"\0", 1)[0].decode()
+            out[nm] = (int(launches[i]), float(ms[i]))
+        return out
+
+    def algorithmic_bytes(self, kernel: str | None = None, flags: int = A.STEP_DEFAULT):
+        bp, bc = C.c_double(), C.c_double()
+        self._check(self.lib.mg_algorithmic_bytes(self.h, kernel.encode() if kernel else None,
+                                                  flags, C.byref(bp), C.byref(bc)))
+        return bp.value, bc.value
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.mg_kernel_launches(self.h))

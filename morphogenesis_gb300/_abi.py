@@ -1,0 +1,133 @@
+"""ctypes mirror of include/mg_abi.h (structs, ids, flags) and the library loader."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libmg_gb300.so"
+
+BONDS_PER_PARTICLE = 6
+DATA_PER_BOND = 9
+BOND_DATA = BONDS_PER_PARTICLE * DATA_PER_BOND
+NUM_TF = 16
+NUM_GENES = 16
+GRID_UNDEF = 0xFFFFFFFF
+NO_PARTNER = 0xFFFFFFFF
+EPIGEN_ACTIVE = 2147483647
+
+# buffer ids (fluid.h:138-206)
+FPOS, FVEL, FVEVAL, FFORCE, FPRESS, FDENSITY, FAGE, FCOLOR, FGCELL, FGNDX = range(10)
+FELASTIDX, FNERVEIDX, FCONC, FEPIGEN, FBIN, FBIN_COUNT, FBIN_OFFSET = 14, 15, 16, 17, 18, 19, 20
+FPARTICLEIDX, FPARTICLE_ID, FMASS_RADIUS = 29, 30, 31
+FBIN_COUNT_ACTIVE_GENES, FBIN_OFFSET_ACTIVE_GENES, FDENSE_LIST_LENGTHS, FDENSE_LISTS = 32, 33, 34, 35
+
+# m_Param ids (fluid_system.h:77-103) + run controls
+PSIMSCALE, PVISC, PRESTDENSITY, PMASS, PRADIUS = 4, 7, 8, 9, 10
+PSMOOTHRADIUS, PINTSTIFF, PEXTSTIFF, PEXTDAMP, PACCEL_LIMIT, PVEL_LIMIT = 12, 13, 14, 15, 16, 17
+PGROUND_SLOPE, PFORCE_MIN, PFORCE_MAX, PFORCE_FREQ, PSURFACE_TENSION = 19, 20, 21, 23, 24
+PACTUATION_FACTOR, PACTUATION_PERIOD, PDT, PTIME, PFREEZE = 25, 26, 100, 101, 102
+
+STEP_PHYSICS, STEP_GENES, STEP_REMODEL, STEP_FREEZE, STEP_SURROGATE = 1, 2, 4, 8, 16
+STEP_DEFAULT = STEP_PHYSICS | STEP_GENES
+
+MG_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "GRID_OVERFLOW", 4: "LIST_OVERFLOW",
+                5: "DEVICE_TIMEOUT", 6: "CUDA_ERROR", 7: "UNSUPPORTED", 8: "INCONSISTENT"}
+
+F3 = C.c_float * 3
+I3 = C.c_int32 * 3
+
+
+class FParams(C.Structure):
+    _fields_ = [
+        ("psimscale", C.c_float), ("psmoothradius", C.c_float), ("pradius", C.c_float),
+        ("pmass", C.c_float), ("prest_dens", C.c_float), ("pboundmin", F3), ("pboundmax", F3),
+        ("pextstiff", C.c_float), ("pintstiff", C.c_float), ("pvisc", C.c_float),
+        ("psurface_t", C.c_float), ("pdamp", C.c_float), ("pforce_min", C.c_float),
+        ("pforce_max", C.c_float), ("pforce_freq", C.c_float), ("pground_slope", C.c_float),
+        ("pgravity", F3), ("paccel_limit", C.c_float), ("pvel_limit", C.c_float),
+        ("actuation_factor", C.c_float), ("actuation_period", C.c_float),
+        ("grid_res", I3), ("grid_srch", C.c_int32), ("grid_size", F3), ("grid_delta", F3),
+        ("grid_min", F3), ("grid_max", F3), ("grid_total", C.c_int32), ("dt", C.c_float),
+        ("time", C.c_float), ("freeze", C.c_int32), ("debug", C.c_int32),
+    ]
+
+
+class Genome(C.Structure):
+    _fields_ = [
+        ("mutability", C.c_uint32 * NUM_GENES), ("delay", C.c_uint32 * NUM_GENES),
+        ("sensitivity", (C.c_float * NUM_TF) * NUM_GENES),
+        ("tf_diffusability", C.c_float * NUM_TF), ("tf_breakdown_rate", C.c_float * NUM_TF),
+        ("secrete", (C.c_float * (2 * NUM_TF + 1)) * NUM_GENES),
+        ("activate", (C.c_float * (2 * NUM_GENES + 1)) * NUM_GENES),
+        ("tanh_param", (C.c_float * 8) * 3), ("param", (C.c_float * 12) * 3),
+    ]
+
+
+class MgError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+# (name, restype, argtypes) of every entry point declared in include/mg_abi.h
+H = C.c_void_p
+SIGNATURES = [
+    ("mg_setup_grid", C.c_int, [C.POINTER(FParams), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float, C.c_int32]),
+    ("mg_version", C.c_char_p, []),
+    ("mg_last_error", C.c_char_p, [H]),
+    ("mg_create", C.c_int, [C.POINTER(FParams), C.POINTER(Genome), C.c_uint32, C.POINTER(H)]),
+    ("mg_destroy", C.c_int, [H]),
+    ("mg_update_params", C.c_int, [H, C.POINTER(FParams)]),
+    ("mg_update_genome", C.c_int, [H, C.POINTER(Genome)]),
+    ("mg_set_param", C.c_int, [H, C.c_int32, C.c_float]),
+    ("mg_get_params", C.c_int, [H, C.POINTER(FParams)]),
+    ("mg_buffer_bytes", C.c_int, [H, C.c_int32, C.POINTER(C.c_size_t)]),
+    ("mg_upload", C.c_int, [H, C.c_int32, C.c_void_p, C.c_size_t]),
+    ("mg_download", C.c_int, [H, C.c_int32, C.c_void_p, C.c_size_t]),
+    ("mg_host_alloc", C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    ("mg_host_free", C.c_int, [C.c_void_p]),
+    ("mg_get_counts", C.c_int, [H, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    ("mg_insert_particles", C.c_int, [H]),
+    ("mg_prefix_sum_cells", C.c_int, [H]),
+    ("mg_counting_sort_full", C.c_int, [H]),
+    ("mg_compute_pressure", C.c_int, [H]),
+    ("mg_compute_force", C.c_int, [H]),
+    ("mg_compute_diffusion", C.c_int, [H]),
+    ("mg_compute_genes", C.c_int, [H]),
+    ("mg_advance", C.c_int, [H]),
+    ("mg_run_physical_sort", C.c_int, [H]),
+    ("mg_run_inner_physical_loop", C.c_int, [H]),
+    ("mg_run_gene_action", C.c_int, [H]),
+    ("mg_step", C.c_int, [H, C.c_uint32, C.c_uint32]),
+    ("mg_synchronize", C.c_int, [H]),
+    ("mg_time_steps", C.c_int, [H, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]),
+    ("mg_profile_enable", C.c_int, [H, C.c_int32]),
+    ("mg_profile_read", C.c_int, [H, C.c_int32, C.c_char_p, C.POINTER(C.c_uint32),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+    ("mg_algorithmic_bytes", C.c_int, [H, C.c_char_p, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("mg_kernel_launches", C.c_uint64, [H]),
+]
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Loads the CUDA extension; raises if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"CUDA extension {p} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(p))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib

@@ -1,0 +1,997 @@
+// mg_api.cu - the C-ABI (include/mg_abi.h): handle, device memory arena, transfers, stage
+// entry points and the CUDA-graph-captured step.
+//
+// Reference host side replaced here: FluidSetupCL / FluidParamCL / UpdateGenome
+// (host_CL.cpp:39-174, fluid_system.cpp:494-610), TransferToCL / TransferFromCL
+// (host_CL.cpp:1608-1668), the *CL stage wrappers (host_CL.cpp:228-2264) and the Run2* loop
+// (fluid_system.cpp:1919-2014).  Where the reference calls clFinish after every kernel and
+// reads counts back to the host every sort, the whole step here is one CUDA graph with the
+// active particle count kept on the device.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/mg_abi.h"
+#include "mg_internal.cuh"
+
+using namespace mg;
+
+namespace {
+
+thread_local std::string g_thread_error;
+
+constexpr int PHASE_UNSORTED = 0, PHASE_INSERTED = 1, PHASE_SORTED = 2;
+
+struct ProfSlot {
+    std::string name;
+    uint32_t launches = 0;
+    double ms = 0.0;
+};
+
+struct ProfMark {
+    int slot;
+    cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct mg_system {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    mg_fparams params{};
+    mg_genome genome{};
+    DevParams P{};
+    DevGenome* dG = nullptr;
+    uint32_t cap = 0;
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    Carried set[2]{};
+    int cur = 0;
+    int conc_cur = 0;
+    Cold cold{};
+    Scratch s{};
+    void* staging = nullptr;
+    size_t staging_bytes = 0;
+    uint32_t* dense = nullptr;  // gcount | goffset | lists | lens (allocated on demand)
+    int phase = PHASE_UNSORTED;
+    bool ever_sorted = false;
+    bool brk_pending = false;
+    float time = 0.f;
+    std::string err;
+    std::map<uint64_t, cudaGraphExec_t> graphs;
+    bool profile = false;
+    std::vector<ProfSlot> prof;
+    std::vector<ProfMark> marks;
+    uint64_t launches = 0;  // kernels launched by mg_step (one graph step counts its kernels)
+};
+
+namespace {
+
+mg_status fail(mg_system* h, mg_status st, const std::string& msg) {
+    if (h) h->err = msg;
+    g_thread_error = msg;
+    return st;
+}
+
+mg_status cuda_fail(mg_system* h, cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    return fail(h, MG_ERR_CUDA, m);
+}
+
+#define MG_CUDA(h, expr)                                          \
+    do {                                                          \
+        cudaError_t e_ = (expr);                                  \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #expr);  \
+    } while (0)
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Derived constants exactly as FluidParamCL (fluid_system.cpp:527-598) and FluidSetupCL
+// (host_CL.cpp:39-106) compute them, in float.
+void derive(DevParams& D, const mg_fparams& p, uint32_t cap) {
+    std::memset(&D, 0, sizeof(D));
+    for (int k = 0; k < 3; k++) {
+        D.gmin[k] = p.grid_min[k];
+        D.gdelta[k] = p.grid_delta[k];
+        D.res[k] = p.grid_res[k];
+        D.scanmax[k] = p.grid_res[k] - p.grid_srch;
+        D.bmin[k] = p.pboundmin[k];
+        D.bmax[k] = p.pboundmax[k];
+        D.grav[k] = p.pgravity[k];
+    }
+    int c = 0;
+    for (int y = 0; y < p.grid_srch; y++)
+        for (int z = 0; z < p.grid_srch; z++)
+            for (int x = 0; x < p.grid_srch; x++)
+                if (c < 64) D.adj[c++] = (y * p.grid_res[2] + z) * p.grid_res[0] + x;
+    D.adjcnt = p.grid_srch * p.grid_srch * p.grid_srch;
+    D.nadj = (1 * p.grid_res[2] + 1) * p.grid_res[0] + 1;
+    D.sr = p.psmoothradius;
+    D.r2 = p.psmoothradius * p.psmoothradius;
+    D.d2 = p.psimscale * p.psimscale;
+    D.r2diff = D.r2 / D.d2;  // computeDiffusion: r2 = fparam.r2 / d2 (cuda:3032)
+    D.pmass = p.pmass;
+    D.rest = p.prest_dens;
+    D.istiff = p.pintstiff;
+    D.wc2 = 21 / (2 * 3.141592f);
+    D.surf = p.psurface_t;
+    D.pr = p.pradius;
+    D.estiff = p.pextstiff;
+    D.damp = p.pdamp;
+    D.xmin_stiff = (p.pforce_min + 1) * p.pextstiff;
+    D.xmax_stiff = (p.pforce_max + 1) * p.pextstiff;
+    D.slope = p.pground_slope;
+    D.one_minus_slope = 1.0f - p.pground_slope;
+    D.AL = p.paccel_limit;
+    D.AL2 = p.paccel_limit * p.paccel_limit;
+    D.VL = p.pvel_limit;
+    D.VL2 = p.pvel_limit * p.pvel_limit;
+    D.vl_factor = D.VL / sqrtf(D.VL2);
+    D.dt = p.dt;
+    D.null_z = p.pboundmin[2] - (float)(2 * p.grid_res[2]);
+    D.freeze = p.freeze ? 1 : 0;
+    D.cap = cap;
+    D.cells = (uint32_t)p.grid_total;
+}
+
+mg_status check_params(mg_system* h, const mg_fparams* p) {
+    if (!p) return fail(h, MG_ERR_INVALID_ARG, "params is NULL");
+    if (p->grid_srch < 1 || p->grid_srch > 4)
+        return fail(h, MG_ERR_INVALID_ARG, "grid_srch must be 1..4 (gridAdj holds 64 cells)");
+    for (int k = 0; k < 3; k++)
+        if (p->grid_res[k] <= p->grid_srch)
+            return fail(h, MG_ERR_INVALID_ARG, "grid_res must exceed grid_srch on every axis");
+    long long tot = (long long)p->grid_res[0] * p->grid_res[1] * p->grid_res[2];
+    if (tot != p->grid_total || tot <= 0 || tot > 0x7fffffffLL)
+        return fail(h, MG_ERR_INVALID_ARG, "grid_total must equal res.x*res.y*res.z (< 2^31)");
+    if (!(p->psmoothradius > 0.f) || !(p->psimscale > 0.f) || !(p->pmass > 0.f))
+        return fail(h, MG_ERR_INVALID_ARG, "psmoothradius, psimscale and pmass must be > 0");
+    return MG_OK;
+}
+
+mg_status upload_genome(mg_system* h) {
+    DevGenome g;
+    std::memset(&g, 0, sizeof(g));
+    const mg_genome& G = h->genome;
+    for (int a = 0; a < NG; a++)
+        for (int t = 0; t < NTF; t++) g.sens[a][t] = G.sensitivity[a][t];
+    for (int t = 0; t < NTF; t++) {
+        g.diff[t] = G.tf_diffusability[t];
+        g.breakdown[t] = G.tf_breakdown_rate[t];
+    }
+    for (int a = 0; a < NG; a++) {
+        int ns = (int)G.secrete[a][2 * NTF];
+        if (ns < 0 || ns > NTF) return fail(h, MG_ERR_INVALID_ARG, "secrete list count out of range");
+        int k = 0;
+        for (int j = 0; j < ns; j++) {
+            int tf = (int)G.secrete[a][2 * j];
+            if (tf < 0 || tf >= NTF) return fail(h, MG_ERR_INVALID_ARG, "secrete list names a species out of range");
+            g.sec_tf[a][k] = tf;
+            g.sec_rate[a][k] = G.secrete[a][2 * j + 1];
+            k++;
+        }
+        g.nsec[a] = k;
+        int na = (int)G.activate[a][2 * NG];
+        if (na != 0)
+            return fail(h, MG_ERR_UNSUPPORTED,
+                        "genome activation lists need per-gene epigenetic counters; the GPU gene "
+                        "kernel holds gene state as a bitmask (FEPIGEN in {0, INT_MAX})");
+        g.nact[a] = 0;
+        g.delay[a] = G.delay[a];
+    }
+    MG_CUDA(h, cudaMemcpyAsync(h->dG, &g, sizeof(g), cudaMemcpyHostToDevice, h->stream));
+    MG_CUDA(h, cudaStreamSynchronize(h->stream));
+    return MG_OK;
+}
+
+void clear_graphs(mg_system* h) {
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+}
+
+uint32_t read_word(mg_system* h, const uint32_t* dptr, mg_status* st) {
+    uint32_t v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, dptr, 4, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) *st = cuda_fail(h, e, "read device word");
+    return v;
+}
+
+// Reads and clears the device error word; maps its bits to a status.
+mg_status check_device(mg_system* h) {
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamSynchronize");
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
+    mg_status st = MG_OK;
+    uint32_t err = read_word(h, h->s.counters + 2, &st);
+    if (st != MG_OK) return st;
+    if (err == 0) return MG_OK;
+    uint32_t zero = 0;
+    cudaMemcpy(h->s.counters + 2, &zero, 4, cudaMemcpyHostToDevice);
+    if (err & ERR_SCAN_TIMEOUT)
+        return fail(h, MG_ERR_DEVICE_TIMEOUT, "prefix-sum look-back gave up waiting (bounded spin)");
+    if (err & ERR_BIG_LIST_OVERFLOW)
+        return fail(h, MG_ERR_GRID_OVERFLOW, "more than 65536 grid cells hold over 256 particles");
+    if (err & ERR_EPIGEN_VALUE)
+        return fail(h, MG_ERR_UNSUPPORTED,
+                    "FEPIGEN values other than 0 and INT_MAX (epigenetic countdowns) are not "
+                    "supported by the GPU gene kernel");
+    return fail(h, MG_ERR_CUDA, "unknown device error word");
+}
+
+// ---- profiling marks ------------------------------------------------------------------------
+int prof_slot(mg_system* h, const char* name) {
+    for (size_t k = 0; k < h->prof.size(); k++)
+        if (h->prof[k].name == name) return (int)k;
+    h->prof.push_back(ProfSlot{name, 0, 0.0});
+    return (int)h->prof.size() - 1;
+}
+
+struct Mark {
+    mg_system* h;
+    bool on;
+    ProfMark m{};
+    Mark(mg_system* h_, bool on_, const char* name) : h(h_), on(on_) {
+        if (!on) return;
+        m.slot = prof_slot(h, name);
+        cudaEventCreate(&m.a);
+        cudaEventCreate(&m.b);
+        cudaEventRecord(m.a, h->stream);
+    }
+    ~Mark() {
+        if (!on) return;
+        cudaEventRecord(m.b, h->stream);
+        h->marks.push_back(m);
+    }
+};
+
+void prof_collect(mg_system* h) {
+    cudaStreamSynchronize(h->stream);
+    for (auto& m : h->marks) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, m.a, m.b);
+        h->prof[m.slot].launches++;
+        h->prof[m.slot].ms += ms;
+        cudaEventDestroy(m.a);
+        cudaEventDestroy(m.b);
+    }
+    h->marks.clear();
+}
+
+// ---- pipeline pieces -------------------------------------------------------------------------
+float* conc_of(mg_system* h, int k) { return h->set[k].conc; }
+
+void enqueue_insert_rank(mg_system* h, bool prof) {
+    const DevParams& P = h->P;
+    cudaStream_t st = h->stream;
+    cudaMemsetAsync(h->s.count, 0, sizeof(uint32_t) * P.cells, st);
+    cudaMemsetAsync(h->s.scan_status, 0, sizeof(unsigned long long) * scan_status_words(P.cells), st);
+    cudaMemsetAsync(h->s.counters, 0, 2 * sizeof(uint32_t), st);
+    { Mark m(h, prof, "insert"); launch_insert(P, h->set[h->cur], h->s, st); }
+    { Mark m(h, prof, "scan"); launch_scan(h->s.count, h->s.offset, P.cells, h->s.scan_status,
+                                           h->s.counters, h->s.counters + 3, h->s.counters + 2, st); }
+    { Mark m(h, prof, "place"); launch_place(P, h->s, st); }
+    { Mark m(h, prof, "cellsort"); launch_cellsort(P, h->s, h->num_sms, st); }
+}
+
+void enqueue_gather(mg_system* h, bool prof) {
+    int src = h->cur, dst = 1 - h->cur;
+    int csrc = h->conc_cur, cdst = 1 - h->conc_cur;
+    { Mark m(h, prof, "gather");
+      launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream); }
+    h->cur = dst;
+    h->conc_cur = cdst;
+}
+
+// dens flags: 1 density, 2 diffusion, 4 genes.  Any conc-writing variant flips conc_cur.
+void enqueue_dens(mg_system* h, int flags, bool prof) {
+    int cin = h->conc_cur, cout = 1 - h->conc_cur;
+    { Mark m(h, prof, flags == 1 ? "pressure" : flags == 7 ? "density_diffusion_genes" : "diffusion_genes");
+      launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, flags, h->stream); }
+    if (flags & 6) h->conc_cur = cout;
+}
+
+// One step in the legacy Run() order (fluid_system.cpp:1179-1349), one sort per step.
+void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
+    enqueue_insert_rank(h, prof);
+    enqueue_gather(h, prof);
+    int dflags = ((flags & MG_STEP_PHYSICS) ? 1 : 0) | ((flags & MG_STEP_GENES) ? 6 : 0);
+    if (dflags) enqueue_dens(h, dflags, prof);
+    if (flags & MG_STEP_PHYSICS) {
+        { Mark m(h, prof, "force"); launch_force(h->P, h->set[h->cur], h->s, h->stream); }
+        { Mark m(h, prof, "advance"); launch_advance(h->P, h->set[h->cur], h->s, true, h->stream); }
+    }
+}
+
+int kernels_per_step(uint32_t flags) {
+    int n = 6;  // insert, scan, place, cellsort, cellsort_big, gather
+    if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES)) n += 1;
+    if (flags & MG_STEP_PHYSICS) n += 2;
+    return n;
+}
+
+mg_status get_graph(mg_system* h, uint32_t flags, cudaGraphExec_t* out) {
+    uint64_t key = ((uint64_t)flags << 8) | ((uint64_t)h->cur << 1) | (uint64_t)h->conc_cur;
+    auto it = h->graphs.find(key);
+    int cur0 = h->cur, conc0 = h->conc_cur;
+    if (it != h->graphs.end()) {
+        *out = it->second;
+        // advance the buffer state exactly as enqueue_step would
+        h->cur = 1 - cur0;
+        h->conc_cur = 1 - conc0;
+        if (flags & MG_STEP_GENES) h->conc_cur = conc0;
+        return MG_OK;
+    }
+    DevParams saved = h->P;
+    if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
+    cudaGraph_t g = nullptr;
+    MG_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(h, flags, false);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    h->P = saved;
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+    cudaGraphExec_t ge = nullptr;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    h->graphs[key] = ge;
+    *out = ge;
+    return MG_OK;
+}
+
+mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
+    if (flags & (MG_STEP_REMODEL | MG_STEP_SURROGATE))
+        return fail(h, MG_ERR_UNSUPPORTED, "remodelling and surrogate steps are not built");
+    for (uint32_t s = 0; s < nsteps; s++) {
+        if (h->profile) {
+            DevParams saved = h->P;
+            if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
+            enqueue_step(h, flags, true);
+            h->P = saved;
+        } else {
+            cudaGraphExec_t ge = nullptr;
+            mg_status st = get_graph(h, flags, &ge);
+            if (st != MG_OK) return st;
+            MG_CUDA(h, cudaGraphLaunch(ge, h->stream));
+        }
+        h->launches += (uint64_t)kernels_per_step(flags);
+        if (flags & MG_STEP_PHYSICS) h->time = h->time + h->P.dt;
+    }
+    h->phase = PHASE_SORTED;
+    h->ever_sorted = true;
+    h->brk_pending = false;
+    if (h->profile) prof_collect(h);
+    return MG_OK;
+}
+
+size_t buf_bytes(const mg_system* h, int32_t id) {
+    size_t n = h->cap, C = (size_t)h->P.cells;
+    switch (id) {
+    case MG_FPOS: case MG_FVEL: case MG_FVEVAL: case MG_FFORCE: return 16 * n;
+    case MG_FPRESS: case MG_FDENSITY: case MG_FAGE: case MG_FCOLOR: case MG_FGCELL: case MG_FGNDX:
+    case MG_FBIN: case MG_FPARTICLE_ID: case MG_FMASS_RADIUS: case MG_FNERVEIDX: return 4 * n;
+    case MG_FELASTIDX: return 4 * n * MG_BOND_DATA;
+    case MG_FPARTICLEIDX: return 4 * n * 2 * NB;
+    case MG_FCONC: return 4 * n * NTF;
+    case MG_FEPIGEN: return 4 * n * NG;
+    case MG_FBIN_COUNT: case MG_FBIN_OFFSET: return 4 * C;
+    case MG_FBIN_COUNT_ACTIVE_GENES: case MG_FBIN_OFFSET_ACTIVE_GENES: return 4 * C * NG;
+    case MG_FDENSE_LIST_LENGTHS: return 4 * NG;
+    case MG_FDENSE_LISTS: return 4 * n * NG;
+    default: return 0;
+    }
+}
+
+mg_status ensure_staging(mg_system* h, size_t bytes) {
+    if (h->staging_bytes >= bytes) return MG_OK;
+    if (h->staging) cudaFree(h->staging);
+    h->staging = nullptr;
+    h->staging_bytes = 0;
+    cudaError_t e = cudaMalloc(&h->staging, bytes);
+    if (e != cudaSuccess) return fail(h, MG_ERR_OOM, "staging buffer allocation failed");
+    h->staging_bytes = bytes;
+    return MG_OK;
+}
+
+uint32_t* cold_field(mg_system* h, int32_t id) {
+    switch (id) {
+    case MG_FAGE: return h->cold.age;
+    case MG_FCOLOR: return h->cold.color;
+    case MG_FPARTICLE_ID: return h->cold.pid;
+    case MG_FMASS_RADIUS: return h->cold.mass_radius;
+    case MG_FNERVEIDX: return h->cold.nerve;
+    default: return nullptr;
+    }
+}
+
+// Per-gene cell counts, offsets, dense lists and lengths from the sorted gene bits.
+mg_status build_dense_lists(mg_system* h) {
+    size_t C = h->P.cells, n = h->cap;
+    if (!h->dense) {
+        cudaError_t e = cudaMalloc(&h->dense, 4 * (2 * C * NG + n * NG + NG));
+        if (e != cudaSuccess) return fail(h, MG_ERR_OOM, "dense-list buffers");
+    }
+    uint32_t* gcount = h->dense;
+    uint32_t* goffset = gcount + C * NG;
+    uint32_t* lists = goffset + C * NG;
+    uint32_t* lens = lists + n * NG;
+    cudaStream_t st = h->stream;
+    MG_CUDA(h, cudaMemsetAsync(gcount, 0, 4 * C * NG, st));
+    launch_gene_cell_counts(h->P, h->set[h->cur], h->s, gcount, st);
+    for (int g = 0; g < NG; g++) {
+        MG_CUDA(h, cudaMemsetAsync(h->s.scan_status, 0, sizeof(unsigned long long) * scan_status_words((uint32_t)C), st));
+        MG_CUDA(h, cudaMemsetAsync(h->s.counters, 0, 4, st));
+        launch_scan(gcount + g * C, goffset + g * C, (uint32_t)C, h->s.scan_status, h->s.counters,
+                    nullptr, h->s.counters + 2, st);
+    }
+    launch_fill_u32(lists, UNDEF, n * NG, st);
+    launch_gene_lists(h->P, h->set[h->cur], h->s, goffset, lists, st);
+    mg_status s2 = check_device(h);
+    if (s2 != MG_OK) return s2;
+    // tally_denselist_lengths: len = cnt[last] + off[last] (cuda:185-194)
+    std::vector<uint32_t> hl(NG);
+    for (int g = 0; g < NG; g++) {
+        uint32_t a = 0, b = 0;
+        MG_CUDA(h, cudaMemcpy(&a, gcount + g * C + C - 1, 4, cudaMemcpyDeviceToHost));
+        MG_CUDA(h, cudaMemcpy(&b, goffset + g * C + C - 1, 4, cudaMemcpyDeviceToHost));
+        hl[g] = a + b;
+    }
+    MG_CUDA(h, cudaMemcpy(lens, hl.data(), 4 * NG, cudaMemcpyHostToDevice));
+    return MG_OK;
+}
+
+}  // namespace
+
+// =============================================================================================
+extern "C" {
+
+const char* mg_version(void) { return "morphogenesis-gb300 0.1 (sm_103a)"; }
+
+const char* mg_last_error(mg_handle h) {
+    if (h) return h->err.c_str();
+    return g_thread_error.c_str();
+}
+
+mg_status mg_setup_grid(mg_fparams* p, const float vol_min[3], const float vol_max[3],
+                        float cell_size, int32_t gsrch_override) {
+    if (!p || !vol_min || !vol_max || !(cell_size > 0.f) || !(p->psimscale > 0.f))
+        return fail(nullptr, MG_ERR_INVALID_ARG, "mg_setup_grid: bad arguments");
+    // SetupGrid (fluid_system.cpp:2073-2131)
+    float ss = p->psimscale;
+    float world_cellsize = cell_size / ss;
+    long long total = 1;
+    for (int k = 0; k < 3; k++) {
+        p->grid_min[k] = vol_min[k];
+        p->grid_max[k] = vol_max[k];
+        float size = vol_max[k] - vol_min[k];
+        int res = (int)ceil(size / world_cellsize);
+        if (res < 1) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_setup_grid: empty volume");
+        p->grid_res[k] = res;
+        p->grid_size[k] = res * cell_size / ss;
+        p->grid_delta[k] = (float)res / p->grid_size[k];
+        total *= res;
+    }
+    if (total > 0x7fffffffLL) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_setup_grid: grid too large");
+    p->grid_total = (int32_t)total;
+    int srch = (int)(floor(2.0f * (p->psmoothradius / ss) / world_cellsize) + 1.0f);
+    if (srch < 2) srch = 2;
+    if (gsrch_override > 0) srch = gsrch_override;
+    p->grid_srch = srch;
+    return MG_OK;
+}
+
+mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t max_points,
+                    mg_handle* out) {
+    if (!out) return fail(nullptr, MG_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    mg_status st = check_params(nullptr, params);
+    if (st != MG_OK) return st;
+    if (!genome) return fail(nullptr, MG_ERR_INVALID_ARG, "genome is NULL");
+    if (max_points == 0 || max_points >= 0x80000000u)
+        return fail(nullptr, MG_ERR_INVALID_ARG, "max_points must be in [1, 2^31)");
+    mg_system* h = new mg_system();
+    h->params = *params;
+    h->genome = *genome;
+    h->cap = max_points;
+    h->time = params->time;
+    derive(h->P, *params, max_points);
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaGetDevice"); }
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+    if (h->num_sms <= 0) h->num_sms = 1;
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaStreamCreate"); }
+
+    // ---- one arena for everything the step touches ----
+    const size_t n = max_points, C = (size_t)params->grid_total;
+    const size_t tiles = scan_status_words((uint32_t)C);
+    std::vector<std::pair<void**, size_t>> plan;
+    for (int k = 0; k < 2; k++) {
+        Carried& c = h->set[k];
+        plan.push_back({(void**)&c.pos, 16 * n});
+        plan.push_back({(void**)&c.vel, 16 * n});
+        plan.push_back({(void**)&c.veval, 16 * n});
+        plan.push_back({(void**)&c.bond, 32 * NB * n});
+        plan.push_back({(void**)&c.pidx, 48 * n});
+        plan.push_back({(void**)&c.conc, 64 * n});
+        plan.push_back({(void**)&c.genes, 4 * n});
+        plan.push_back({(void**)&c.origin, 4 * n});
+    }
+    plan.push_back({(void**)&h->cold.age, 4 * n});
+    plan.push_back({(void**)&h->cold.color, 4 * n});
+    plan.push_back({(void**)&h->cold.pid, 4 * n});
+    plan.push_back({(void**)&h->cold.mass_radius, 4 * n});
+    plan.push_back({(void**)&h->cold.nerve, 4 * n});
+    plan.push_back({(void**)&h->cold.change, 4 * NB * n});
+    plan.push_back({(void**)&h->s.cell, 4 * n});
+    plan.push_back({(void**)&h->s.arank, 4 * n});
+    plan.push_back({(void**)&h->s.order, 4 * n});
+    plan.push_back({(void**)&h->s.newidx, 4 * n});
+    plan.push_back({(void**)&h->s.scell, 4 * n});
+    plan.push_back({(void**)&h->s.press, 4 * n});
+    plan.push_back({(void**)&h->s.invdens, 4 * n});
+    plan.push_back({(void**)&h->s.force, 16 * n});
+    plan.push_back({(void**)&h->s.brk, 4 * n});
+    plan.push_back({(void**)&h->s.count, 4 * C});
+    plan.push_back({(void**)&h->s.offset, 4 * C});
+    plan.push_back({(void**)&h->s.scan_status, 8 * (tiles + 1)});
+    plan.push_back({(void**)&h->s.counters, 64});
+    plan.push_back({(void**)&h->s.big_list, 4 * (size_t)BIG_LIST_CAP});
+    plan.push_back({(void**)&h->dG, sizeof(DevGenome)});
+    size_t total = 0;
+    for (auto& pr : plan) total += align_up(pr.second);
+    e = cudaMalloc(&h->arena, total);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(h->stream);
+        delete h;
+        return fail(nullptr, MG_ERR_OOM, "device arena allocation failed (" + std::to_string(total) + " bytes)");
+    }
+    h->arena_bytes = total;
+    char* base = (char*)h->arena;
+    for (auto& pr : plan) {
+        *pr.first = base;
+        base += align_up(pr.second);
+    }
+    cudaMemsetAsync(h->arena, 0, total, h->stream);
+    launch_init_set(max_points, h->set[0], h->stream);
+    launch_init_set(max_points, h->set[1], h->stream);
+    uint32_t init_counters[16] = {0};
+    init_counters[3] = max_points;  // every slot counts as active until the first sort
+    cudaMemcpyAsync(h->s.counters, init_counters, sizeof(init_counters), cudaMemcpyHostToDevice, h->stream);
+    launch_fill_u32(h->s.cell, UNDEF, n, h->stream);
+    launch_fill_u32(h->s.newidx, UNDEF, n, h->stream);
+    launch_fill_u32(h->s.scell, UNDEF, n, h->stream);
+    st = upload_genome(h);
+    if (st == MG_OK) st = check_device(h);
+    if (st != MG_OK) {
+        std::string m = h->err;
+        mg_destroy(h);
+        return fail(nullptr, st, m);
+    }
+    *out = h;
+    return MG_OK;
+}
+
+mg_status mg_destroy(mg_handle h) {
+    if (!h) return MG_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    clear_graphs(h);
+    for (auto& m : h->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
+    if (h->staging) cudaFree(h->staging);
+    if (h->dense) cudaFree(h->dense);
+    if (h->arena) cudaFree(h->arena);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return MG_OK;
+}
+
+mg_status mg_update_params(mg_handle h, const mg_fparams* p) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    mg_status st = check_params(h, p);
+    if (st != MG_OK) return st;
+    if (p->grid_total != h->params.grid_total)
+        return fail(h, MG_ERR_INVALID_ARG, "grid size is fixed at mg_create");
+    for (int k = 0; k < 3; k++)
+        if (p->grid_res[k] != h->params.grid_res[k])
+            return fail(h, MG_ERR_INVALID_ARG, "grid resolution is fixed at mg_create");
+    h->params = *p;
+    h->time = p->time;
+    derive(h->P, *p, h->cap);
+    clear_graphs(h);
+    return MG_OK;
+}
+
+mg_status mg_update_genome(mg_handle h, const mg_genome* g) {
+    if (!h || !g) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    mg_genome saved = h->genome;
+    h->genome = *g;
+    mg_status st = upload_genome(h);
+    if (st != MG_OK) {
+        h->genome = saved;
+        upload_genome(h);
+        return st;
+    }
+    return MG_OK;
+}
+
+mg_status mg_set_param(mg_handle h, int32_t id, float v) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    mg_fparams p = h->params;
+    p.time = h->time;
+    switch (id) {
+    case MG_PSIMSCALE: p.psimscale = v; break;
+    case MG_PVISC: p.pvisc = v; break;
+    case MG_PRESTDENSITY: p.prest_dens = v; break;
+    case MG_PMASS: p.pmass = v; break;
+    case MG_PRADIUS: p.pradius = v; break;
+    case MG_PSMOOTHRADIUS: p.psmoothradius = v; break;
+    case MG_PINTSTIFF: p.pintstiff = v; break;
+    case MG_PEXTSTIFF: p.pextstiff = v; break;
+    case MG_PEXTDAMP: p.pdamp = v; break;
+    case MG_PACCEL_LIMIT: p.paccel_limit = v; break;
+    case MG_PVEL_LIMIT: p.pvel_limit = v; break;
+    case MG_PGROUND_SLOPE: p.pground_slope = v; break;
+    case MG_PFORCE_MIN: p.pforce_min = v; break;
+    case MG_PFORCE_MAX: p.pforce_max = v; break;
+    case MG_PFORCE_FREQ: p.pforce_freq = v; break;
+    case MG_PSURFACE_TENSION: p.psurface_t = v; break;
+    case MG_PACTUATION_FACTOR: p.actuation_factor = v; break;
+    case MG_PACTUATION_PERIOD: p.actuation_period = v; break;
+    case MG_PDT: p.dt = v; break;
+    case MG_PTIME: p.time = v; break;
+    case MG_PFREEZE: p.freeze = v != 0.f; break;
+    default: return fail(h, MG_ERR_INVALID_ARG, "unknown parameter id " + std::to_string(id));
+    }
+    return mg_update_params(h, &p);
+}
+
+mg_status mg_get_params(mg_handle h, mg_fparams* out) {
+    if (!h || !out) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    *out = h->params;
+    out->time = h->time;
+    return MG_OK;
+}
+
+mg_status mg_buffer_bytes(mg_handle h, int32_t id, size_t* bytes) {
+    if (!h || !bytes) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    *bytes = buf_bytes(h, id);
+    if (*bytes == 0) return fail(h, MG_ERR_INVALID_ARG, "buffer id not exchanged by this pipeline");
+    return MG_OK;
+}
+
+mg_status mg_upload(mg_handle h, int32_t id, const void* host, size_t bytes) {
+    if (!h || !host) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    size_t want = buf_bytes(h, id);
+    if (want == 0 || id == MG_FBIN || id == MG_FBIN_COUNT || id == MG_FBIN_OFFSET ||
+        id == MG_FBIN_COUNT_ACTIVE_GENES || id == MG_FBIN_OFFSET_ACTIVE_GENES ||
+        id == MG_FDENSE_LIST_LENGTHS || id == MG_FDENSE_LISTS)
+        return fail(h, MG_ERR_INVALID_ARG, "buffer id " + std::to_string(id) + " cannot be uploaded");
+    if (bytes != want)
+        return fail(h, MG_ERR_INVALID_ARG, "buffer " + std::to_string(id) + ": expected " +
+                                               std::to_string(want) + " bytes, got " + std::to_string(bytes));
+    cudaStream_t st = h->stream;
+    Carried& c = h->set[h->cur];
+    void* dst = nullptr;
+    switch (id) {
+    case MG_FPOS: dst = c.pos; break;
+    case MG_FVEL: dst = c.vel; break;
+    case MG_FVEVAL: dst = c.veval; break;
+    case MG_FFORCE: dst = h->s.force; break;
+    case MG_FPRESS: dst = h->s.press; break;
+    case MG_FDENSITY: dst = h->s.invdens; break;
+    case MG_FPARTICLEIDX: dst = c.pidx; break;
+    case MG_FCONC: dst = conc_of(h, h->conc_cur); break;
+    case MG_FGCELL: case MG_FGNDX: return MG_OK;  // recomputed by insert
+    default: break;
+    }
+    if (dst) {
+        MG_CUDA(h, cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, st));
+        return check_device(h);
+    }
+    mg_status s2 = ensure_staging(h, bytes);
+    if (s2 != MG_OK) return s2;
+    MG_CUDA(h, cudaMemcpyAsync(h->staging, host, bytes, cudaMemcpyHostToDevice, st));
+    const uint32_t* sref = (const uint32_t*)h->staging;
+    if (id == MG_FELASTIDX) {
+        launch_import_bonds(h->P, sref, c, h->cold, st);
+        h->brk_pending = false;
+    } else if (id == MG_FEPIGEN) {
+        launch_import_epigen(h->P, sref, c, h->s.counters + 2, st);
+    } else if (uint32_t* f = cold_field(h, id)) {
+        launch_import_cold(h->P, sref, c, f, st);
+    } else {
+        return fail(h, MG_ERR_INVALID_ARG, "buffer id " + std::to_string(id) + " cannot be uploaded");
+    }
+    return check_device(h);
+}
+
+mg_status mg_download(mg_handle h, int32_t id, void* host, size_t bytes) {
+    if (!h || !host) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    size_t want = buf_bytes(h, id);
+    if (want == 0) return fail(h, MG_ERR_INVALID_ARG, "buffer id " + std::to_string(id) + " not exchanged");
+    if (bytes != want)
+        return fail(h, MG_ERR_INVALID_ARG, "buffer " + std::to_string(id) + ": expected " +
+                                               std::to_string(want) + " bytes, got " + std::to_string(bytes));
+    cudaStream_t st = h->stream;
+    Carried& c = h->set[h->cur];
+    const void* src = nullptr;
+    switch (id) {
+    case MG_FPOS: src = c.pos; break;
+    case MG_FVEL: src = c.vel; break;
+    case MG_FVEVAL: src = c.veval; break;
+    case MG_FFORCE: src = h->s.force; break;
+    case MG_FPRESS: src = h->s.press; break;
+    case MG_FDENSITY: src = h->s.invdens; break;
+    case MG_FPARTICLEIDX: src = c.pidx; break;
+    case MG_FCONC: src = conc_of(h, h->conc_cur); break;
+    case MG_FBIN_COUNT: src = h->s.count; break;
+    case MG_FBIN_OFFSET: src = h->s.offset; break;
+    default: break;
+    }
+    if (src) {
+        MG_CUDA(h, cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, st));
+        return check_device(h);
+    }
+    if (id == MG_FBIN_COUNT_ACTIVE_GENES || id == MG_FBIN_OFFSET_ACTIVE_GENES ||
+        id == MG_FDENSE_LIST_LENGTHS || id == MG_FDENSE_LISTS) {
+        if (!h->ever_sorted) return fail(h, MG_ERR_INVALID_ARG, "dense lists exist after a sort");
+        mg_status s2 = build_dense_lists(h);
+        if (s2 != MG_OK) return s2;
+        size_t C = h->P.cells, n = h->cap;
+        const uint32_t* base = h->dense;
+        const uint32_t* p = id == MG_FBIN_COUNT_ACTIVE_GENES ? base
+                          : id == MG_FBIN_OFFSET_ACTIVE_GENES ? base + C * NG
+                          : id == MG_FDENSE_LISTS ? base + 2 * C * NG
+                          : base + 2 * C * NG + n * NG;
+        MG_CUDA(h, cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, st));
+        return check_device(h);
+    }
+    mg_status s2 = ensure_staging(h, bytes);
+    if (s2 != MG_OK) return s2;
+    uint32_t* sref = (uint32_t*)h->staging;
+    if (id == MG_FELASTIDX) {
+        launch_export_bonds(h->P, c, h->cold, h->s, h->brk_pending, sref, st);
+    } else if (id == MG_FEPIGEN) {
+        launch_export_epigen(h->P, c, h->s, sref, st);
+    } else if (uint32_t* f = cold_field(h, id)) {
+        launch_export_cold(h->P, c, h->s, f, id == MG_FPARTICLE_ID ? NO_PARTNER : 0u, sref, st);
+    } else if (id == MG_FGCELL || id == MG_FGNDX || id == MG_FBIN) {
+        int which = id == MG_FGCELL ? 0 : id == MG_FGNDX ? 1 : 2;
+        if (h->phase == PHASE_UNSORTED && !h->ever_sorted && which != 2)
+            launch_fill_u32(sref, UNDEF, h->cap, st);
+        else
+            launch_export_grid_index(h->P, h->s, which, h->phase == PHASE_INSERTED ? 1 : 2, sref, st);
+    } else {
+        return fail(h, MG_ERR_INVALID_ARG, "buffer id " + std::to_string(id) + " not exchanged");
+    }
+    MG_CUDA(h, cudaMemcpyAsync(host, sref, bytes, cudaMemcpyDeviceToHost, st));
+    return check_device(h);
+}
+
+mg_status mg_host_alloc(size_t bytes, void** out) {
+    if (!out || bytes == 0) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_host_alloc: bad arguments");
+    cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaHostAlloc");
+    return MG_OK;
+}
+
+mg_status mg_host_free(void* ptr) {
+    if (!ptr) return MG_OK;
+    cudaError_t e = cudaFreeHost(ptr);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaFreeHost");
+    return MG_OK;
+}
+
+mg_status mg_get_counts(mg_handle h, uint32_t* num_points, uint32_t* active_points) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    mg_status st = check_device(h);
+    if (st != MG_OK) return st;
+    uint32_t n = read_word(h, h->s.counters + 3, &st);
+    if (st != MG_OK) return st;
+    uint32_t a = n;
+    if (h->ever_sorted || h->phase == PHASE_INSERTED) {
+        const DevParams& P = h->P;
+        long long corner = ((long long)P.scanmax[1] * P.res[2] + P.scanmax[2]) * P.res[0] + P.scanmax[0];
+        if (corner >= 0 && corner < (long long)P.cells) a = read_word(h, h->s.offset + corner, &st);
+    }
+    if (num_points) *num_points = n;
+    if (active_points) *active_points = a;
+    return st;
+}
+
+mg_status mg_insert_particles(mg_handle h) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    enqueue_insert_rank(h, false);
+    h->phase = PHASE_INSERTED;
+    return check_device(h);
+}
+
+mg_status mg_prefix_sum_cells(mg_handle h) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    if (h->phase != PHASE_INSERTED) return fail(h, MG_ERR_INVALID_ARG, "prefix sum needs mg_insert_particles first");
+    cudaStream_t st = h->stream;
+    cudaMemsetAsync(h->s.scan_status, 0, sizeof(unsigned long long) * scan_status_words(h->P.cells), st);
+    cudaMemsetAsync(h->s.counters, 0, 4, st);
+    launch_scan(h->s.count, h->s.offset, h->P.cells, h->s.scan_status, h->s.counters,
+                h->s.counters + 3, h->s.counters + 2, st);
+    return check_device(h);
+}
+
+mg_status mg_counting_sort_full(mg_handle h) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    if (h->phase != PHASE_INSERTED) return fail(h, MG_ERR_INVALID_ARG, "counting sort needs mg_insert_particles first");
+    enqueue_gather(h, false);
+    h->phase = PHASE_SORTED;
+    h->ever_sorted = true;
+    h->brk_pending = false;
+    return check_device(h);
+}
+
+static mg_status need_sorted(mg_handle h) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    if (!h->ever_sorted) return fail(h, MG_ERR_INVALID_ARG, "this stage needs a counting sort first");
+    return MG_OK;
+}
+
+mg_status mg_compute_pressure(mg_handle h) {
+    mg_status st = need_sorted(h);
+    if (st != MG_OK) return st;
+    enqueue_dens(h, 1, false);
+    return check_device(h);
+}
+
+mg_status mg_compute_force(mg_handle h) {
+    mg_status st = need_sorted(h);
+    if (st != MG_OK) return st;
+    launch_force(h->P, h->set[h->cur], h->s, h->stream);
+    launch_apply_breaks(h->P, h->set[h->cur], h->s, h->stream);
+    return check_device(h);
+}
+
+mg_status mg_compute_diffusion(mg_handle h) {
+    mg_status st = need_sorted(h);
+    if (st != MG_OK) return st;
+    enqueue_dens(h, 2, false);
+    return check_device(h);
+}
+
+mg_status mg_compute_genes(mg_handle h) {
+    mg_status st = need_sorted(h);
+    if (st != MG_OK) return st;
+    enqueue_dens(h, 4, false);
+    return check_device(h);
+}
+
+mg_status mg_advance(mg_handle h) {
+    mg_status st = need_sorted(h);
+    if (st != MG_OK) return st;
+    launch_advance(h->P, h->set[h->cur], h->s, false, h->stream);
+    h->time = h->time + h->P.dt;
+    return check_device(h);
+}
+
+mg_status mg_run_physical_sort(mg_handle h) {
+    mg_status st = mg_insert_particles(h);
+    if (st == MG_OK) st = mg_prefix_sum_cells(h);
+    if (st == MG_OK) st = mg_counting_sort_full(h);
+    return st;
+}
+
+mg_status mg_run_inner_physical_loop(mg_handle h) {
+    mg_status st = mg_compute_pressure(h);
+    if (st == MG_OK) st = mg_compute_force(h);
+    if (st == MG_OK) st = mg_advance(h);
+    return st;
+}
+
+mg_status mg_run_gene_action(mg_handle h) {
+    mg_status st = mg_compute_diffusion(h);
+    if (st == MG_OK) st = mg_compute_genes(h);
+    return st;
+}
+
+mg_status mg_step(mg_handle h, uint32_t nsteps, uint32_t flags) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    mg_status st = run_steps(h, nsteps, flags);
+    if (st != MG_OK) return st;
+    return check_device(h);
+}
+
+mg_status mg_synchronize(mg_handle h) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    return check_device(h);
+}
+
+mg_status mg_time_steps(mg_handle h, uint32_t nsteps, uint32_t flags, float* ms) {
+    if (!h || !ms) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    cudaEvent_t a, b;
+    MG_CUDA(h, cudaEventCreate(&a));
+    MG_CUDA(h, cudaEventCreate(&b));
+    MG_CUDA(h, cudaEventRecord(a, h->stream));
+    mg_status st = run_steps(h, nsteps, flags);
+    cudaEventRecord(b, h->stream);
+    cudaEventSynchronize(b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = t;
+    if (st != MG_OK) return st;
+    return check_device(h);
+}
+
+mg_status mg_profile_enable(mg_handle h, int32_t enable) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    h->profile = enable != 0;
+    if (enable) h->prof.clear();
+    return MG_OK;
+}
+
+mg_status mg_profile_read(mg_handle h, int32_t max_slots, char* names, uint32_t* launches,
+                          double* total_ms, int32_t* nslots) {
+    if (!h || !nslots) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    int n = (int)h->prof.size();
+    *nslots = n;
+    for (int k = 0; k < n && k < max_slots; k++) {
+        if (names) {
+            std::memset(names + 32 * k, 0, 32);
+            std::strncpy(names + 32 * k, h->prof[k].name.c_str(), 31);
+        }
+        if (launches) launches[k] = h->prof[k].launches;
+        if (total_ms) total_ms[k] = h->prof[k].ms;
+    }
+    return MG_OK;
+}
+
+// Compulsory DRAM bytes of each kernel (own-particle arrays read/written once; neighbour
+// reads are served from cache because the particles are sorted by cell).
+mg_status mg_algorithmic_bytes(mg_handle h, const char* kernel, uint32_t flags,
+                               double* bpp, double* bpc) {
+    if (!bpp || !bpc) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    struct K { const char* name; double per_particle, per_cell; };
+    const bool phys = flags & MG_STEP_PHYSICS, genes = flags & MG_STEP_GENES;
+    // carried state per particle: pos/vel/veval 48, bonds 192, incoming 48, conc 64, genes 4, origin 4
+    const double carried = 48 + 192 + 48 + 64 + 4 + 4;
+    const double dens = (phys ? 16 + 4 + 4 + 4 : 0) + (genes ? (phys ? 0 : 16 + 4) + 64 + 64 + 4 : 0);
+    const K table[] = {
+        {"insert", 16 + 4 + 4 + 4, 4 + 8},            // pos, cell, rank, newidx | memset, atomics
+        {"scan", 0, 8},                               // count read, offset write
+        {"place", 12, 0},                             // cell, rank, order
+        {"cellsort", 12, 8},                          // order r/w, newidx | count, offset
+        {"gather", 4 + carried + carried + 4 + 4, 0}, // order, read+write carried, cell, scell
+        {"pressure", phys ? 28.0 : 0.0, 0},
+        {"density_diffusion_genes", dens, 0},
+        {"diffusion_genes", genes ? 16 + 4 + 64 + 64 + 4 : 0.0, 0},
+        {"force", phys ? 16 + 16 + 4 + 4 + 4 + 192 + 48 + 48 + 16 + 4 : 0.0, 0},
+        {"advance", phys ? 48 + 48 + 16 + 4 : 0.0, 0},
+    };
+    if (kernel) {
+        for (const K& k : table)
+            if (std::strcmp(k.name, kernel) == 0) {
+                *bpp = k.per_particle;
+                *bpc = k.per_cell;
+                return MG_OK;
+            }
+        return fail(h, MG_ERR_INVALID_ARG, std::string("unknown kernel ") + kernel);
+    }
+    double p = 0, c = 0;
+    for (const K& k : table) {
+        if (!std::strcmp(k.name, "pressure") || !std::strcmp(k.name, "diffusion_genes")) continue;
+        if (!std::strcmp(k.name, "density_diffusion_genes")) { p += dens; continue; }
+        p += k.per_particle;
+        c += k.per_cell;
+    }
+    *bpp = p;
+    *bpc = c;
+    return MG_OK;
+}
+
+// Number of kernels launched by mg_step since the handle was created.
+uint64_t mg_kernel_launches(mg_handle h) { return h ? h->launches : 0; }
+
+}  // extern "C"

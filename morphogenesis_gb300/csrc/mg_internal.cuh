@@ -1,0 +1,154 @@
+// mg_internal.cuh - device-side data layout and kernel interfaces of the GB300 pipeline.
+//
+// HBM layout (structure of arrays, one "carried" set per sort direction):
+//   pos/vel/veval   float4[N]            (the reference's cl_float3 is 16 bytes too)
+//   bond            uint4[6][N][2]       per bond slot a, particle p: two 16-byte words
+//                     A = (partner, restlen, modulus, damping)
+//                     B = (elastlim, partner particle ID, strain^2 integrator, strain integrator)
+//                   i.e. FELASTIDX words (0,2,3,4 | 1,5,6,7); word 8 (change type) is cold.
+//                   The force kernel's gather of incoming bonds reads A and B.x of the
+//                   partner's record while the owner writes only B.z/B.w.
+//   pidx            uint32[N][12]        FPARTICLEIDX, the reference layout
+//   conc            float[N][16]         FCONC, the reference device layout
+//   genes           uint32[N]            bit g set <=> FEPIGEN[g][p] != 0
+//   origin          uint32[N]            slot of this particle in the cold arrays
+// Cold arrays (indexed by origin, never permuted): FAGE, FCOLOR, FPARTICLE_ID, FMASS_RADIUS,
+// FNERVEIDX and FELASTIDX word 8.
+// Per step: cell/arrival-rank/order/newidx/scell uint32[N], press/invdens float[N],
+// force float4[N], brk uint32[N], count/offset uint32[cells].
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mg {
+
+constexpr int NB = 6;
+constexpr int NTF = 16;
+constexpr int NG = 16;
+constexpr uint32_t UNDEF = 0xFFFFFFFFu;
+constexpr uint32_t NO_PARTNER = 0xFFFFFFFFu;
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;                      // per thread
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS; // 4096 cells per tile
+constexpr int WARP_CELL_MAX = 256;   // cells up to this size are ordered by one warp
+constexpr int BLOCK_CELL_MAX = 8192; // up to this by one block in shared memory
+constexpr uint32_t BIG_LIST_CAP = 1u << 16;
+constexpr uint32_t SPIN_LIMIT = 1u << 22; // bounded look-back polls
+
+// Error bits in the device error word.
+enum : uint32_t {
+    ERR_SCAN_TIMEOUT = 1u << 0,
+    ERR_BIG_LIST_OVERFLOW = 1u << 1,
+    ERR_EPIGEN_VALUE = 1u << 2,
+};
+
+// Simulation parameters passed by value to every kernel (constant bank).
+struct DevParams {
+    float gmin[3], gdelta[3];
+    int res[3], scanmax[3];
+    int adjcnt, nadj;
+    int adj[64];
+    float sr, r2, r2diff, d2, pmass, rest, istiff, wc2, surf;
+    float pr, bmin[3], bmax[3], estiff, damp, xmin_stiff, xmax_stiff, slope, one_minus_slope;
+    float grav[3], AL, AL2, VL, VL2, vl_factor, dt;
+    float null_z;
+    int freeze;
+    uint32_t cap;
+    uint32_t cells;
+};
+
+// Genome in device memory (float-widened, compacted sparse lists).
+struct DevGenome {
+    float sens[NG][NTF];
+    float diff[NTF];
+    float breakdown[NTF];
+    int nsec[NG];
+    int sec_tf[NG][NTF];
+    float sec_rate[NG][NTF];
+    int nact[NG];
+    int act_gene[NG][NG];
+    float act_thr[NG][NG];
+    uint32_t delay[NG];
+};
+
+struct Carried {
+    float4* pos;
+    float4* vel;
+    float4* veval;
+    uint4* bond;  // [NB][cap][2]
+    uint32_t* pidx;
+    float* conc;
+    uint32_t* genes;
+    uint32_t* origin;
+};
+
+struct Cold {
+    uint32_t* age;
+    uint32_t* color;
+    uint32_t* pid;
+    uint32_t* mass_radius;
+    uint32_t* nerve;
+    uint32_t* change;  // [cap][NB]
+};
+
+struct Scratch {
+    uint32_t* cell;     // unsorted cell of particle i (UNDEF outside the window)
+    uint32_t* arank;    // arrival rank within the cell (not deterministic)
+    uint32_t* order;    // order[p] = pre-sort index of the particle sorted to p
+    uint32_t* newidx;   // newidx[i] = sorted index of pre-sort particle i (UNDEF if dropped)
+    uint32_t* scell;    // cell of sorted particle p
+    float* press;
+    float* invdens;
+    float4* force;
+    uint32_t* brk;      // bonds that broke in the last force pass
+    uint32_t* count;    // [cells]
+    uint32_t* offset;   // [cells]
+    unsigned long long* scan_status;  // [tiles]
+    uint32_t* counters; // [0] scan tile ticket, [1] big-cell list length, [2] error word, [3] nactive
+    uint32_t* big_list; // [BIG_LIST_CAP] cells that need the block-level ordering
+};
+
+// ---- launchers (all on one stream; no host synchronisation inside) ----------------------
+void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
+void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long long* status,
+                 uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st);
+size_t scan_status_words(uint32_t n);
+void launch_place(const DevParams& P, const Scratch& s, cudaStream_t st);
+void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, cudaStream_t st);
+void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
+                   const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st);
+// flags: 1 density/pressure, 2 diffusion, 4 gene reaction
+void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
+                 float* conc_out, const Scratch& s, int flags, cudaStream_t st);
+void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
+void launch_apply_breaks(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
+void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_breaks,
+                    cudaStream_t st);
+
+// ---- import/export between the reference layouts and the device layout -------------------
+void launch_import_bonds(const DevParams& P, const uint32_t* ref, const Carried& cur,
+                         const Cold& cold, cudaStream_t st);
+void launch_export_bonds(const DevParams& P, const Carried& cur, const Cold& cold,
+                         const Scratch& s, bool apply_breaks, uint32_t* ref, cudaStream_t st);
+void launch_import_epigen(const DevParams& P, const uint32_t* ref, const Carried& cur,
+                          uint32_t* err, cudaStream_t st);
+void launch_export_epigen(const DevParams& P, const Carried& cur, const Scratch& s,
+                          uint32_t* ref, cudaStream_t st);
+void launch_import_cold(const DevParams& P, const uint32_t* ref, const Carried& cur,
+                        uint32_t* cold_field, cudaStream_t st);
+void launch_export_cold(const DevParams& P, const Carried& cur, const Scratch& s,
+                        const uint32_t* cold_field, uint32_t null_value, uint32_t* ref,
+                        cudaStream_t st);
+// FGCELL / FGNDX / FBIN views.  mode 1: after insert (pre-sort indices), 2: after sort.
+void launch_export_grid_index(const DevParams& P, const Scratch& s, int which, int mode,
+                              uint32_t* ref, cudaStream_t st);
+void launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st);
+void launch_identity(uint32_t* p, uint32_t n, cudaStream_t st);
+void launch_init_set(uint32_t cap, const Carried& c, cudaStream_t st);
+// dense per-gene lists from the sorted gene bits
+void launch_gene_cell_counts(const DevParams& P, const Carried& cur, const Scratch& s,
+                             uint32_t* gcount, cudaStream_t st);
+void launch_gene_lists(const DevParams& P, const Carried& cur, const Scratch& s,
+                       const uint32_t* goffset, uint32_t* lists, cudaStream_t st);
+
+}  // namespace mg

@@ -1,0 +1,380 @@
+// mg_sort.cu - grid binning, prefix sum and the stable counting sort (rows a2-a4).
+//
+// Reference: insertParticles (fluid_system_cuda.cu:53-100), prefixSum/prefixFixup
+// (cuda:136-183, host_CUDA.cpp:307-407), countingSortFull (cuda:196-296).
+//
+// The reference assigns each particle its rank in a cell with atomicAdd, so the sorted order
+// depends on the thread schedule.  Here the sorted order is the stable one (rank = number of
+// earlier-index particles in the same cell, i.e. a serial execution of insertParticles):
+//   insert   : cell of every particle, per-cell counts (warp-aggregated atomics) and an
+//              arrival rank that is only used to scatter indices into their cell's segment;
+//   scan     : single-pass exclusive scan with decoupled look-back -> per-cell offsets;
+//   place    : order[offset[cell] + arrival rank] = i;
+//   cellsort : each cell's segment of indices is put in ascending order (warp tier for
+//              cells <= 256 particles, block tier <= 8192, ordered stream compaction above),
+//              which yields order[] (sorted -> old) and newidx[] (old -> sorted);
+//   gather   : every carried field is gathered through order[], bond partners and incoming
+//              bond owners are remapped through newidx[].
+#include <cuda/atomic>
+#include <cfloat>
+#include "mg_internal.cuh"
+
+namespace mg {
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// Cell of a position (cuda:70-79): gcf = (pos - gridMin) * gridDelta truncated toward zero,
+// valid when 1 <= gc <= gridScanMax on every axis.  Written as float range tests so that NaN
+// and out-of-range values never go through a float->int conversion.
+__device__ __forceinline__ uint32_t cell_of(const DevParams& P, float4 p) {
+    float gx = (p.x - P.gmin[0]) * P.gdelta[0];
+    float gy = (p.y - P.gmin[1]) * P.gdelta[1];
+    float gz = (p.z - P.gmin[2]) * P.gdelta[2];
+    if (!(gx >= 1.0f && gx < (float)(P.scanmax[0] + 1))) return UNDEF;
+    if (!(gy >= 1.0f && gy < (float)(P.scanmax[1] + 1))) return UNDEF;
+    if (!(gz >= 1.0f && gz < (float)(P.scanmax[2] + 1))) return UNDEF;
+    int cx = (int)gx, cy = (int)gy, cz = (int)gz;
+    return (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
+}
+
+// ---- insert -------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __restrict__ pos,
+                                                uint32_t* __restrict__ cell,
+                                                uint32_t* __restrict__ arank,
+                                                uint32_t* __restrict__ newidx,
+                                                uint32_t* __restrict__ count) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool in = i < P.cap;
+    uint32_t c = UNDEF;
+    if (in) {
+        c = cell_of(P, pos[i]);
+        cell[i] = c;
+        newidx[i] = UNDEF;  // overwritten by the cell sort for particles inside the window
+    }
+    bool valid = in && c != UNDEF;
+    unsigned active = __ballot_sync(0xffffffffu, valid);
+    if (valid) {
+        unsigned peers = __match_any_sync(active, c);
+        int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if ((int)lane_id() == leader) base = atomicAdd(&count[c], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        unsigned lt = (1u << lane_id()) - 1u;
+        arank[i] = base + (uint32_t)__popc(peers & lt);
+    }
+}
+
+void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st) {
+    uint32_t blocks = (P.cap + 255) / 256;
+    k_insert<<<blocks, 256, 0, st>>>(P, cur.pos, s.cell, s.arank, s.newidx, s.count);
+}
+
+// ---- single-pass scan (decoupled look-back) ------------------------------------------------
+// Tile status word: high 32 bits = flag (0 not ready, 1 aggregate, 2 inclusive prefix),
+// low 32 bits = value.  Flag and value are published by one 64-bit atomic store, so a relaxed
+// load that sees the flag also sees its value.  Tiles take their index from a ticket counter,
+// so every tile a block waits on has already started; each wait is still bounded and sets
+// ERR_SCAN_TIMEOUT when it gives up.
+size_t scan_status_words(uint32_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restrict__ in,
+                                                       uint32_t* __restrict__ out, uint32_t n,
+                                                       unsigned long long* status,
+                                                       uint32_t* ticket, uint32_t* total,
+                                                       uint32_t* err) {
+    __shared__ uint32_t s_tile, s_prefix;
+    __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+    const uint32_t per_warp = SCAN_TILE / (SCAN_THREADS / 32);
+    const uint32_t wbase = tile * SCAN_TILE + warp * per_warp;
+    uint32_t vals[SCAN_ITEMS];
+    uint32_t run = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        uint32_t idx = wbase + k * 32 + lane;
+        uint32_t v = idx < n ? in[idx] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, x, d);
+            if ((int)lane >= d) x += t;
+        }
+        vals[k] = run + x - v;
+        run += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (lane == 0) s_warp[warp] = run;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = SCAN_THREADS / 32;
+        uint32_t w = (int)lane < nw ? s_warp[lane] : 0u;
+        uint32_t incl = w;
+#pragma unroll
+        for (int d = 1; d < nw; d <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+            if ((int)lane >= d) incl += t;
+        }
+        uint32_t agg = __shfl_sync(0xffffffffu, incl, nw - 1);
+        if ((int)lane < nw) s_warp[lane] = incl - w;
+        if (lane == 0) {
+            uint32_t excl = 0;
+            cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> me(status[tile]);
+            if (tile == 0) {
+                me.store((2ull << 32) | agg, cuda::memory_order_relaxed);
+            } else {
+                me.store((1ull << 32) | agg, cuda::memory_order_relaxed);
+                int64_t t = (int64_t)tile - 1;
+                uint32_t spins = 0;
+                while (t >= 0) {
+                    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> prev(status[t]);
+                    unsigned long long sw = prev.load(cuda::memory_order_relaxed);
+                    uint32_t flag = (uint32_t)(sw >> 32);
+                    if (flag == 0) {
+                        if (++spins > SPIN_LIMIT) {
+                            atomicOr(err, ERR_SCAN_TIMEOUT);
+                            break;
+                        }
+                        __nanosleep(32);
+                        continue;
+                    }
+                    excl += (uint32_t)sw;
+                    if (flag == 2) break;
+                    t--;
+                }
+                me.store((2ull << 32) | (uint32_t)(excl + agg), cuda::memory_order_relaxed);
+            }
+            s_prefix = excl;
+            if (tile == ntiles - 1 && total) *total = excl + agg;
+        }
+    }
+    __syncthreads();
+    const uint32_t pre = s_prefix + s_warp[warp];
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        uint32_t idx = wbase + k * 32 + lane;
+        if (idx < n) out[idx] = pre + vals[k];
+    }
+}
+
+void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long long* status,
+                 uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st) {
+    uint32_t tiles = (uint32_t)scan_status_words(n);
+    if (tiles == 0) return;
+    k_scan<<<tiles, SCAN_THREADS, 0, st>>>(in, out, n, status, ticket, total, err);
+}
+
+// ---- place ----------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_place(uint32_t cap, const uint32_t* __restrict__ cell,
+                                               const uint32_t* __restrict__ arank,
+                                               const uint32_t* __restrict__ offset,
+                                               uint32_t* __restrict__ order) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    uint32_t c = cell[i];
+    if (c == UNDEF) return;
+    order[offset[c] + arank[i]] = i;
+}
+
+void launch_place(const DevParams& P, const Scratch& s, cudaStream_t st) {
+    uint32_t blocks = (P.cap + 255) / 256;
+    k_place<<<blocks, 256, 0, st>>>(P.cap, s.cell, s.arank, s.offset, s.order);
+}
+
+// ---- cell sort ------------------------------------------------------------------------------
+constexpr int CS_WARPS = 8;
+
+__global__ void __launch_bounds__(CS_WARPS * 32) k_cellsort(uint32_t cells,
+                                                            const uint32_t* __restrict__ count,
+                                                            const uint32_t* __restrict__ offset,
+                                                            uint32_t* __restrict__ order,
+                                                            uint32_t* __restrict__ newidx,
+                                                            uint32_t* __restrict__ big_list,
+                                                            uint32_t* __restrict__ big_count,
+                                                            uint32_t* __restrict__ err) {
+    __shared__ uint32_t sbuf[CS_WARPS][WARP_CELL_MAX];
+    const uint32_t w = threadIdx.x >> 5, lane = lane_id();
+    const uint32_t gw = blockIdx.x * CS_WARPS + w;
+    const uint32_t nw = gridDim.x * CS_WARPS;
+    for (uint32_t c0 = gw * 32; c0 < cells; c0 += nw * 32) {
+        uint32_t c = c0 + lane;
+        uint32_t n = c < cells ? count[c] : 0u;
+        uint32_t off = n ? offset[c] : 0u;
+        if (n == 1) newidx[order[off]] = off;
+        if (n > (uint32_t)WARP_CELL_MAX) {
+            uint32_t k = atomicAdd(big_count, 1u);
+            if (k < BIG_LIST_CAP) big_list[k] = c;
+            else atomicOr(err, ERR_BIG_LIST_OVERFLOW);
+        }
+        unsigned multi = __ballot_sync(0xffffffffu, n > 1 && n <= (uint32_t)WARP_CELL_MAX);
+        while (multi) {
+            int src = __ffs(multi) - 1;
+            multi &= multi - 1;
+            uint32_t cn = __shfl_sync(0xffffffffu, n, src);
+            uint32_t co = __shfl_sync(0xffffffffu, off, src);
+            for (uint32_t k = lane; k < cn; k += 32) sbuf[w][k] = order[co + k];
+            __syncwarp();
+            for (uint32_t k = lane; k < cn; k += 32) {
+                uint32_t x = sbuf[w][k];
+                uint32_t r = 0;
+                for (uint32_t m = 0; m < cn; m++) r += sbuf[w][m] < x ? 1u : 0u;
+                order[co + r] = x;
+                newidx[x] = co + r;
+            }
+            __syncwarp();
+        }
+    }
+}
+
+constexpr int BIG_THREADS = 512;
+
+__global__ void __launch_bounds__(BIG_THREADS) k_cellsort_big(uint32_t cap,
+                                                              const uint32_t* __restrict__ cell,
+                                                              const uint32_t* __restrict__ count,
+                                                              const uint32_t* __restrict__ offset,
+                                                              uint32_t* __restrict__ order,
+                                                              uint32_t* __restrict__ newidx,
+                                                              const uint32_t* __restrict__ big_list,
+                                                              const uint32_t* __restrict__ big_count) {
+    extern __shared__ uint32_t sseg[];  // BLOCK_CELL_MAX entries
+    __shared__ uint32_t s_warp[BIG_THREADS / 32];
+    uint32_t nbig = *big_count;
+    if (nbig > BIG_LIST_CAP) nbig = BIG_LIST_CAP;
+    for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+        const uint32_t c = big_list[b];
+        const uint32_t n = count[c], off = offset[c];
+        if (n <= (uint32_t)BLOCK_CELL_MAX) {
+            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) sseg[k] = order[off + k];
+            __syncthreads();
+            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+                uint32_t x = sseg[k], r = 0;
+                for (uint32_t m = 0; m < n; m++) r += sseg[m] < x ? 1u : 0u;
+                order[off + r] = x;
+                newidx[x] = off + r;
+            }
+            __syncthreads();
+        } else {
+            // Ordered stream compaction over all particles: members of cell c in index order.
+            uint32_t running = 0;
+            const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+            for (uint32_t base = 0; base < cap; base += blockDim.x) {
+                uint32_t i = base + threadIdx.x;
+                bool m = i < cap && cell[i] == c;
+                unsigned bal = __ballot_sync(0xffffffffu, m);
+                if (lane == 0) s_warp[warp] = (uint32_t)__popc(bal);
+                __syncthreads();
+                uint32_t before = 0, tot = 0;
+                for (uint32_t q = 0; q < BIG_THREADS / 32; q++) {
+                    if (q < warp) before += s_warp[q];
+                    tot += s_warp[q];
+                }
+                if (m) {
+                    uint32_t r = running + before + (uint32_t)__popc(bal & ((1u << lane) - 1u));
+                    order[off + r] = i;
+                    newidx[i] = off + r;
+                }
+                running += tot;
+                __syncthreads();
+            }
+        }
+    }
+}
+
+void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, cudaStream_t st) {
+    uint32_t groups = (P.cells + 31) / 32;
+    uint32_t blocks = (groups + CS_WARPS - 1) / CS_WARPS;
+    uint32_t maxb = (uint32_t)num_sms * 8;
+    if (blocks > maxb) blocks = maxb;
+    if (blocks == 0) blocks = 1;
+    k_cellsort<<<blocks, CS_WARPS * 32, 0, st>>>(P.cells, s.count, s.offset, s.order, s.newidx,
+                                                  s.big_list, s.counters + 1, s.counters + 2);
+    k_cellsort_big<<<num_sms, BIG_THREADS, BLOCK_CELL_MAX * sizeof(uint32_t), st>>>(
+        P.cap, s.cell, s.count, s.offset, s.order, s.newidx, s.big_list, s.counters + 1);
+}
+
+// ---- gather ---------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t remap(uint32_t j, uint32_t cap, const uint32_t* newidx) {
+    return j < cap ? __ldg(newidx + j) : NO_PARTNER;
+}
+
+__global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
+                                                const float* __restrict__ sconc, Carried D,
+                                                float* __restrict__ dconc,
+                                                const uint32_t* __restrict__ order,
+                                                const uint32_t* __restrict__ newidx,
+                                                const uint32_t* __restrict__ cell,
+                                                uint32_t* __restrict__ scell,
+                                                float* __restrict__ press,
+                                                float* __restrict__ invdens,
+                                                float4* __restrict__ force,
+                                                const uint32_t* __restrict__ nactive_p) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t cap = P.cap;
+    if (p >= cap) return;
+    const uint32_t nact = *nactive_p;
+    if (p < nact) {
+        const uint32_t i = order[p];
+        D.pos[p] = __ldg(S.pos + i);
+        D.vel[p] = __ldg(S.vel + i);
+        D.veval[p] = __ldg(S.veval + i);
+#pragma unroll
+        for (int a = 0; a < NB; a++) {
+            const size_t src = ((size_t)a * cap + i) * 2, dst = ((size_t)a * cap + p) * 2;
+            uint4 A = __ldg(S.bond + src);
+            uint4 B = __ldg(S.bond + src + 1);
+            A.x = remap(A.x, cap, newidx);
+            D.bond[dst] = A;
+            D.bond[dst + 1] = B;
+        }
+        const uint4* pi = reinterpret_cast<const uint4*>(S.pidx + (size_t)i * 12);
+        uint4* po = reinterpret_cast<uint4*>(D.pidx + (size_t)p * 12);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            uint4 v = __ldg(pi + k);
+            v.x = remap(v.x, cap, newidx);
+            v.z = remap(v.z, cap, newidx);
+            po[k] = v;
+        }
+        const float4* ci = reinterpret_cast<const float4*>(sconc + (size_t)i * NTF);
+        float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
+#pragma unroll
+        for (int k = 0; k < 4; k++) co[k] = __ldg(ci + k);
+        D.genes[p] = __ldg(S.genes + i);
+        D.origin[p] = __ldg(S.origin + i);
+        scell[p] = __ldg(cell + i);
+    } else {
+        // parked null particle (out-of-grid parking of advanceParticles, cuda:3474-3477)
+        D.pos[p] = make_float4(P.bmin[0], P.bmin[1], P.null_z, 0.0f);
+        D.vel[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        D.veval[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int a = 0; a < NB; a++) {
+            const size_t dst = ((size_t)a * cap + p) * 2;
+            D.bond[dst] = make_uint4(NO_PARTNER, 0u, 0u, 0u);
+            D.bond[dst + 1] = make_uint4(0u, NO_PARTNER, 0u, 0u);
+        }
+        uint4* po = reinterpret_cast<uint4*>(D.pidx + (size_t)p * 12);
+#pragma unroll
+        for (int k = 0; k < 3; k++) po[k] = make_uint4(NO_PARTNER, NO_PARTNER, NO_PARTNER, NO_PARTNER);
+        float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
+#pragma unroll
+        for (int k = 0; k < 4; k++) co[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        D.genes[p] = 0u;
+        D.origin[p] = UNDEF;
+        scell[p] = UNDEF;
+        press[p] = 0.f;
+        invdens[p] = 0.f;
+        force[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
+                   const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st) {
+    uint32_t blocks = (P.cap + 255) / 256;
+    k_gather<<<blocks, 256, 0, st>>>(P, src, src_conc, dst, dst_conc, s.order, s.newidx, s.cell,
+                                      s.scell, s.press, s.invdens, s.force, s.counters + 3);
+}
+
+}  // namespace mg

@@ -1,0 +1,231 @@
+"""GPU pipeline vs the CPU oracle through the C-ABI (parity tests proper).
+
+Integer outputs (cells, ranks, counts, offsets, sorted order, bond remap, gene bits) must be
+bit-exact.  Float fields are compared with an explicit tolerance: FP_RTOL relative plus
+FP_ATOL absolute scaled by the field's magnitude.  The kernels evaluate the reference
+expressions in the oracle's order without fused multiply-adds, so the observed difference is
+zero; the tolerance is the contract, the bitwise check is reported.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as orc
+from helpers import box_centre, scene
+from morphogenesis_gb300 import _abi as A
+from morphogenesis_gb300 import demo
+
+pytestmark = pytest.mark.gpu
+
+FP_RTOL = 1e-5
+FP_ATOL = 1e-6
+KATS = json.loads((Path(__file__).parent / "golden" / "kats.json").read_text())
+C0 = box_centre()
+
+INT_BUFS = [A.FGCELL, A.FGNDX, A.FBIN, A.FPARTICLE_ID, A.FPARTICLEIDX, A.FEPIGEN, A.FAGE,
+            A.FCOLOR, A.FMASS_RADIUS, A.FNERVEIDX, A.FBIN_COUNT, A.FBIN_OFFSET]
+FLOAT_BUFS = [A.FPOS, A.FVEL, A.FVEVAL, A.FFORCE, A.FPRESS, A.FDENSITY, A.FCONC]
+
+
+def pair(d, n, bits=32):
+    import morphogenesis_gb300 as mg
+
+    g = mg.FluidSystem(d.params, d.genome, n)
+    o = orc.Oracle(d.params, d.genome, n, bits)
+    g.TransferToCL(d.arrays)
+    o.upload_all(d.arrays)
+    return g, o
+
+
+def close(a, b, what=""):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = max(1.0, float(np.nanmax(np.abs(b))) if b.size else 1.0)
+    ok = np.isclose(a, b, rtol=FP_RTOL, atol=FP_ATOL * scale, equal_nan=True)
+    assert ok.all(), f"{what}: {np.count_nonzero(~ok)} of {a.size} differ, max |d| {np.nanmax(np.abs(a - b))}"
+
+
+def compare(g, o, bufs_int=INT_BUFS, bufs_float=FLOAT_BUFS, elast=True):
+    for b in bufs_int:
+        x, y = g.download(b), o.download(b)
+        assert np.array_equal(x, y), f"integer buffer {b}: {np.count_nonzero(x != y)} words differ"
+    bitwise = True
+    for b in bufs_float:
+        x, y = g.download(b), o.download(b)
+        close(x, y, f"float buffer {b}")
+        bitwise &= np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    if elast:
+        x, y = g.download(A.FELASTIDX).reshape(-1, 6, 9), o.download(A.FELASTIDX).reshape(-1, 6, 9)
+        for w in (0, 5, 8):
+            assert np.array_equal(x[:, :, w], y[:, :, w]), f"FELASTIDX word {w}"
+        for w in (1, 2, 3, 4, 6, 7):
+            close(x[:, :, w].view(np.float32), y[:, :, w].view(np.float32), f"FELASTIDX word {w}")
+        bitwise &= np.array_equal(x, y)
+    return bitwise
+
+
+@pytest.fixture(scope="module")
+def cfg0():
+    return demo.make_block(16, "R", seed=0)
+
+
+def test_stage_by_stage_config0(built, cfg0):
+    g, o = pair(cfg0, cfg0.n)
+    g.InsertParticlesCL(); o.insert()
+    compare(g, o, [A.FGCELL, A.FGNDX, A.FBIN_COUNT], [], elast=False)
+    g.PrefixSumCellsCL(); o.prefix_sum()
+    compare(g, o, [A.FBIN_OFFSET], [], elast=False)
+    assert g.counts() == o.counts()
+    g.CountingSortFullCL(); o.sort()
+    compare(g, o, bufs_float=[A.FPOS, A.FVEL, A.FVEVAL, A.FCONC])
+    g.ComputePressureCL(); o.pressure()
+    compare(g, o, [], [A.FPRESS, A.FDENSITY], elast=False)
+    g.ComputeForceCL(); o.force()
+    compare(g, o, [], [A.FFORCE])
+    g.ComputeDiffusionCL(); o.diffusion()
+    compare(g, o, [], [A.FCONC], elast=False)
+    g.ComputeGenesCL(); o.genes()
+    compare(g, o, [A.FEPIGEN], [A.FCONC], elast=False)
+    g.AdvanceCL(); o.advance()
+    assert compare(g, o), "expected bitwise equality with the oracle"
+
+
+@pytest.mark.parametrize("param", ["R", "L"])
+def test_full_step_1_and_100_steps(built, param):
+    d = demo.make_block(16, param, seed=1)
+    g, o = pair(d, d.n)
+    g.Run(1); o.step(1)
+    assert compare(g, o)
+    g.Run(99); o.step(99)
+    assert compare(g, o), "100-step trajectories should stay bit-identical"
+    assert g.counts() == o.counts()
+
+
+def test_flags_physics_only_and_genes_only(built, cfg0):
+    for flags in (A.STEP_PHYSICS, A.STEP_GENES, A.STEP_PHYSICS | A.STEP_GENES | A.STEP_FREEZE):
+        g, o = pair(cfg0, cfg0.n)
+        g.Run(3, flags); o.step(3, flags)
+        compare(g, o)
+
+
+def test_breakable_bonds_break_identically(built):
+    d = demo.make_block(10, "R", seed=4, breakable=True, intstiff=50.0)
+    g, o = pair(d, d.n)
+    g.Run(30); o.step(30)
+    compare(g, o)
+    el = o.download(A.FELASTIDX).reshape(-1, 6, 9)
+    broken = (el[:, :, 0] != A.NO_PARTNER) & (el[:, :, 2] == 0)
+    assert broken.any(), "scenario should break some bonds"
+
+
+def test_kat_scenes_on_gpu(built):
+    k = KATS["bond_spring"]
+    d, n = scene([[C0, C0, C0], [C0 + k["d"], C0, C0]],
+                 bonds=[(0, 0, 1, k["L0"], k["modulus"], k["damping"], 1e30)])
+    g, o = pair(d, n)
+    g.Run2PhysicalSort(); g.ComputePressureCL(); g.ComputeForceCL()
+    f = g.download(A.FFORCE)[np.argsort(g.download(A.FPARTICLE_ID))]
+    np.testing.assert_allclose(f[:, 0], [k["force_owner_x"], k["force_partner_x"]], rtol=2e-6)
+    k = KATS["pair_density"]
+    d, n = scene([[C0, C0, C0], [C0 + k["r"], C0, C0]])
+    g, o = pair(d, n)
+    g.Run2PhysicalSort(); g.ComputePressureCL()
+    np.testing.assert_allclose(g.download(A.FPRESS), [k["press"]] * 2, rtol=2e-6)
+    np.testing.assert_allclose(g.download(A.FDENSITY), [k["invdens"]] * 2, rtol=2e-6)
+
+
+def test_stable_sort_hand_case_gpu(built):
+    cw = 4.0
+    x0, x1 = C0 + 0.5, C0 - cw + 0.5
+    d, n = scene([[x0, C0, C0], [x1, C0, C0], [x0 + 0.25, C0, C0], [x1 + 0.25, C0, C0]])
+    g, _ = pair(d, n)
+    g.InsertParticlesCL()
+    assert list(g.download(A.FGNDX)) == [0, 0, 1, 1]
+    g.PrefixSumCellsCL(); g.CountingSortFullCL()
+    assert list(g.download(A.FPARTICLE_ID)) == [2, 4, 1, 3]
+    assert list(g.download(A.FGNDX)) == [0, 1, 0, 1]
+
+
+def test_edge_empty_ragged_and_dropped(built):
+    # every particle outside the grid window
+    d, n = scene([[-1e6, 0, 0], [np.nan, 1, 1], [C0, -5.0, C0]])
+    g, o = pair(d, n)
+    g.Run(2); o.step(2)
+    assert g.counts()[0] == 0
+    compare(g, o)
+    # ragged: capacity larger than the particle count, spare slots parked outside the grid
+    d = demo.make_block(6, "R", seed=5, max_points=6 ** 3 + 37)
+    g, o = pair(d, 6 ** 3 + 37)
+    g.Run(3); o.step(3)
+    assert g.counts()[0] == 6 ** 3
+    compare(g, o)
+    # particles pushed out of the window mid-run are dropped identically
+    d = demo.make_block(6, "R", seed=6)
+    pos = d.arrays[A.FPOS]
+    pos[::7, 0] = -3.0
+    g, o = pair(d, d.n)
+    g.Run(2); o.step(2)
+    compare(g, o)
+
+
+@pytest.mark.parametrize("count", [300, 9000])
+def test_crowded_cell_orders(built, count):
+    """Cells above the warp tier (256) and above the block tier (8192) keep the stable order."""
+    rs = np.random.default_rng(count)
+    pts = C0 + rs.uniform(0.1, 3.9, (count, 3))
+    pts = np.concatenate([pts, C0 + 6 + rs.uniform(0, 8, (200, 3))])
+    d, n = scene(pts)
+    g, o = pair(d, n)
+    g.Run(1, A.STEP_GENES); o.step(1, A.STEP_GENES)
+    compare(g, o, bufs_float=[A.FPOS, A.FCONC])
+
+
+def test_dense_gene_lists(built, cfg0):
+    g, o = pair(cfg0, cfg0.n)
+    g.Run(2); o.step(2)
+    for b in (A.FBIN_COUNT_ACTIVE_GENES, A.FBIN_OFFSET_ACTIVE_GENES, A.FDENSE_LIST_LENGTHS,
+              A.FDENSE_LISTS):
+        assert np.array_equal(g.download(b), o.download(b)), f"dense-list buffer {b}"
+
+
+def test_rejects_what_it_cannot_hold(built, cfg0):
+    import morphogenesis_gb300 as mg
+
+    g = mg.FluidSystem(cfg0.params, cfg0.genome, cfg0.n)
+    ep = cfg0.arrays[A.FEPIGEN].copy()
+    ep[3, 10] = 5  # an epigenetic countdown value
+    with pytest.raises(mg.MgError) as e:
+        g.upload(A.FEPIGEN, ep)
+    assert e.value.status == 7
+    with pytest.raises(mg.MgError):
+        g.ComputePressureCL()  # no sort yet
+    with pytest.raises(ValueError):
+        g.upload(A.FPOS, cfg0.arrays[A.FPOS][:10])
+    gen = demo.make_genome()
+    gen.activate[0][32] = 1.0
+    with pytest.raises(mg.MgError):
+        g.UpdateGenome(gen)
+
+
+def test_deterministic_rerun(built):
+    d = demo.make_block(12, "R", seed=7)
+    outs = []
+    for _ in range(2):
+        g, _o = pair(d, d.n)
+        g.Run(5)
+        outs.append({b: g.download(b) for b in (A.FPOS, A.FCONC, A.FPARTICLE_ID, A.FELASTIDX)})
+    for b in outs[0]:
+        assert np.array_equal(outs[0][b], outs[1][b])
+
+
+def test_graph_cache_alternates_buffers(built, cfg0):
+    """Odd and even step counts, mixed with stage calls, give the oracle's result."""
+    g, o = pair(cfg0, cfg0.n)
+    g.Run(1); o.step(1)
+    g.Run2PhysicalSort(); o.insert(); o.prefix_sum(); o.sort()
+    g.Run2InnerPhysicalLoop(); o.pressure(); o.force(); o.advance()
+    g.Run2GeneAction(); o.diffusion(); o.genes()
+    g.Run(3); o.step(3)
+    compare(g, o)
