@@ -739,7 +739,7 @@ mg_status mg_download(mg_handle h, int32_t id, void* host, size_t bytes) {
     }
     if (id == MG_FBIN_COUNT_ACTIVE_GENES || id == MG_FBIN_OFFSET_ACTIVE_GENES ||
         id == MG_FDENSE_LIST_LENGTHS || id == MG_FDENSE_LISTS) {
-        if (!h->ever_sorted) return fail(h, MG_ERR_INVALID_ARG, "dense lists exist after a sort");
+        if (h->phase != PHASE_SORTED) return fail(h, MG_ERR_INVALID_ARG, "dense lists exist after a sort");
         mg_status s2 = build_dense_lists(h);
         if (s2 != MG_OK) return s2;
         size_t C = h->P.cells, n = h->cap;
@@ -834,7 +834,9 @@ mg_status mg_counting_sort_full(mg_handle h) {
 
 static mg_status need_sorted(mg_handle h) {
     if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
-    if (!h->ever_sorted) return fail(h, MG_ERR_INVALID_ARG, "this stage needs a counting sort first");
+    // Neighbour loops index cells through the sorted particles' cells; after an insert without
+    // the sort those no longer match the counts, so the sort must come first.
+    if (h->phase != PHASE_SORTED) return fail(h, MG_ERR_INVALID_ARG, "this stage needs a counting sort first");
     return MG_OK;
 }
 
