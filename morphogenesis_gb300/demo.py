@@ -10,7 +10,11 @@ four times the block extent.  Two parameterisations share positions, grid and me
 * ``"R"`` (reference-consistent): simulation scale 1, smoothing radius 2.0, spacing 1.0 --
   the same world-unit geometry with the scale the reference's own demos use
   (src/demo/SpecificationFile.txt), so that the kernels' mixed world/simulation-unit
-  comparisons (computePressure r2, computeForce dsq < 1) see neighbours.
+  comparisons (computePressure r2, computeForce dsq < 1) see neighbours.  computeDiffusion
+  weights each neighbour by (r2 - dsq) * simscale^2 (cuda:3053), so with simscale 1 the
+  diffusion rate is rescaled by 0.005^2 to keep the literal configuration's per-step
+  exchange (a rate of 0.1 with weights of order 1 over ~30 neighbours is an unstable
+  explicit scheme and overflows within 60 steps).
 
 The grid cell is 2h with a 27-cell (gsrch = 3) search window; the grid volume extends two
 cells beyond the walls on every side, as SetupSpacing places the walls (fluid_system.cpp:2536-2541).
@@ -115,6 +119,11 @@ def setup_grid(p: A.FParams, vmin, vmax, cell_size: float, gsrch: int) -> None:
     p.grid_srch = gsrch if gsrch > 0 else max(srch, 2)
 
 
+def diffusion_rate(parameterisation: str, rate: float = 0.1) -> float:
+    """Genome diffusability giving the literal configuration's per-step exchange."""
+    return rate if parameterisation == "L" else rate * 0.005 * 0.005
+
+
 def make_genome(seed: int = 1, diffusion: float = 0.1, decay: float = 0.01,
                 secretion: float = 0.004, density: float = 0.25) -> A.Genome:
     """Signed 16x16 regulatory table (25 % nonzero, U[-1,1]); gene g secretes species g."""
@@ -152,7 +161,7 @@ def make_block(n_side: int, parameterisation: str = "R", seed: int = 0, *,
     1.5 x rest length when ``breakable`` (bonds break at strain > 0.5), else 1e30.
     """
     p = make_params(n_side, parameterisation, intstiff=intstiff)
-    g = genome if genome is not None else make_genome(seed=1)
+    g = genome if genome is not None else make_genome(seed=1, diffusion=diffusion_rate(parameterisation))
     nx, ny, nz = dims_of(n_side)
     n = nx * ny * nz
     cap = max_points or n

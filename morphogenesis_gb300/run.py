@@ -1,0 +1,49 @@
+"""Demo driver (the role of the reference's make_demo2 / load_sim programs): builds a seeded
+tissue block, uploads it and runs steps on the GPU.
+
+    python -m morphogenesis_gb300.run --dims 128 64 128 --steps 10 [--param R|L] [--flags 3]
+
+Prints particle counts, the run's wall time and, with --profile, per-kernel device times.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+from . import FluidSystem
+from . import _abi as A
+from . import demo
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--dims", type=int, nargs=3, default=[16, 16, 16])
+    ap.add_argument("--param", default="R", choices=["R", "L"])
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=0)
+    ap.add_argument("--flags", type=int, default=A.STEP_DEFAULT)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--breakable", action="store_true")
+    ap.add_argument("--profile", action="store_true")
+    a = ap.parse_args(argv)
+    d = demo.make_block(tuple(a.dims), a.param, seed=a.seed, breakable=a.breakable)
+    fs = FluidSystem(d.params, d.genome, d.n)
+    fs.TransferToCL(d.arrays)
+    if a.warmup:
+        fs.Run(a.warmup, a.flags)
+    if a.profile:
+        fs.profile(True)
+    t0 = time.perf_counter()
+    fs.Run(a.steps, a.flags)
+    dt = time.perf_counter() - t0
+    out = {"particles": d.n, "steps": a.steps, "seconds": dt, "counts": fs.counts(),
+           "particle_steps_per_s": d.n * a.steps / dt}
+    if a.profile:
+        out["kernels"] = {k: {"launches": v[0], "ms": v[1]} for k, v in fs.profile_read().items()}
+    print(json.dumps(out))
+    fs.close()
+
+
+if __name__ == "__main__":
+    main()
