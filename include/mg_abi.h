@@ -218,6 +218,14 @@ mg_status mg_run_gene_action(mg_handle h);          /* Run2GeneAction */
 mg_status mg_step(mg_handle h, uint32_t nsteps, uint32_t flags);
 mg_status mg_synchronize(mg_handle h);
 
+/* ---- tuning ------------------------------------------------------------------------------ */
+enum mg_option {
+    /* neighbour search of the density/diffusion pass: 0 = one thread walks its 27 cells
+     * (the reference loop), 1 = warp-cooperative search (default).  Results are identical. */
+    MG_OPT_NEIGHBOR_SEARCH = 1
+};
+mg_status mg_set_option(mg_handle h, int32_t option, int32_t value);
+
 /* ---- measurement ------------------------------------------------------------------------- */
 /* Runs nsteps of mg_step and returns their device time (CUDA events on the handle's stream). */
 mg_status mg_time_steps(mg_handle h, uint32_t nsteps, uint32_t flags, float* ms);

@@ -219,6 +219,9 @@ class FluidSystem:
     def synchronize(self) -> None:
         self._check(self.lib.mg_synchronize(self.h))
 
+    def set_option(self, option: int, value: int) -> None:
+        self._check(self.lib.mg_set_option(self.h, int(option), int(value)))
+
     def profile(self, enable: bool = True) -> None:
         self._check(self.lib.mg_profile_enable(self.h, 1 if enable else 0))
 

@@ -32,6 +32,8 @@ PACTUATION_FACTOR, PACTUATION_PERIOD, PDT, PTIME, PFREEZE = 25, 26, 100, 101, 10
 STEP_PHYSICS, STEP_GENES, STEP_REMODEL, STEP_FREEZE, STEP_SURROGATE = 1, 2, 4, 8, 16
 STEP_DEFAULT = STEP_PHYSICS | STEP_GENES
 
+OPT_NEIGHBOR_SEARCH = 1
+
 MG_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "GRID_OVERFLOW", 4: "LIST_OVERFLOW",
                 5: "DEVICE_TIMEOUT", 6: "CUDA_ERROR", 7: "UNSUPPORTED", 8: "INCONSISTENT"}
@@ -104,6 +106,7 @@ SIGNATURES = [
     ("mg_step", C.c_int, [H, C.c_uint32, C.c_uint32]),
     ("mg_synchronize", C.c_int, [H]),
     ("mg_time_steps", C.c_int, [H, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]),
+    ("mg_set_option", C.c_int, [H, C.c_int32, C.c_int32]),
     ("mg_profile_enable", C.c_int, [H, C.c_int32]),
     ("mg_profile_read", C.c_int, [H, C.c_int32, C.c_char_p, C.POINTER(C.c_uint32),
                                   C.POINTER(C.c_double), C.POINTER(C.c_int32)]),

@@ -60,6 +60,8 @@ struct mg_system {
     int phase = PHASE_UNSORTED;
     bool ever_sorted = false;
     bool brk_pending = false;
+    bool flist_valid = false;   // fluid-force lists match the current positions and order
+    bool warp_search = true;    // density pass: warp-cooperative search (else direct walk)
     float time = 0.f;
     std::string err;
     std::map<uint64_t, cudaGraphExec_t> graphs;
@@ -110,6 +112,7 @@ void derive(DevParams& D, const mg_fparams& p, uint32_t cap) {
                 if (c < 64) D.adj[c++] = (y * p.grid_res[2] + z) * p.grid_res[0] + x;
     D.adjcnt = p.grid_srch * p.grid_srch * p.grid_srch;
     D.nadj = (1 * p.grid_res[2] + 1) * p.grid_res[0] + 1;
+    D.gsrch = p.grid_srch;
     D.sr = p.psmoothradius;
     D.r2 = p.psmoothradius * p.psmoothradius;
     D.d2 = p.psimscale * p.psimscale;
@@ -286,14 +289,17 @@ void enqueue_gather(mg_system* h, bool prof) {
       launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream); }
     h->cur = dst;
     h->conc_cur = cdst;
+    h->flist_valid = false;
 }
 
 // dens flags: 1 density, 2 diffusion, 4 genes.  Any conc-writing variant flips conc_cur.
 void enqueue_dens(mg_system* h, int flags, bool prof) {
     int cin = h->conc_cur, cout = 1 - h->conc_cur;
     { Mark m(h, prof, flags == 1 ? "pressure" : flags == 7 ? "density_diffusion_genes" : "diffusion_genes");
-      launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, flags, h->stream); }
+      launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, flags,
+                  h->warp_search, h->stream); }
     if (flags & 6) h->conc_cur = cout;
+    if (h->warp_search && (flags & 3)) h->flist_valid = true;
 }
 
 // One step in the legacy Run() order (fluid_system.cpp:1179-1349), one sort per step.
@@ -303,8 +309,9 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
     int dflags = ((flags & MG_STEP_PHYSICS) ? 1 : 0) | ((flags & MG_STEP_GENES) ? 6 : 0);
     if (dflags) enqueue_dens(h, dflags, prof);
     if (flags & MG_STEP_PHYSICS) {
-        { Mark m(h, prof, "force"); launch_force(h->P, h->set[h->cur], h->s, h->stream); }
+        { Mark m(h, prof, "force"); launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream); }
         { Mark m(h, prof, "advance"); launch_advance(h->P, h->set[h->cur], h->s, true, h->stream); }
+        h->flist_valid = false;
     }
 }
 
@@ -365,6 +372,7 @@ mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
     h->phase = PHASE_SORTED;
     h->ever_sorted = true;
     h->brk_pending = false;
+    h->flist_valid = (flags & MG_STEP_PHYSICS) ? false : (h->warp_search && (flags & MG_STEP_GENES));
     if (h->profile) prof_collect(h);
     return MG_OK;
 }
@@ -537,6 +545,8 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     plan.push_back({(void**)&h->s.invdens, 4 * n});
     plan.push_back({(void**)&h->s.force, 16 * n});
     plan.push_back({(void**)&h->s.brk, 4 * n});
+    plan.push_back({(void**)&h->s.flist, 4 * (size_t)FL_CAP * n});
+    plan.push_back({(void**)&h->s.fcount, 4 * n});
     plan.push_back({(void**)&h->s.count, 4 * C});
     plan.push_back({(void**)&h->s.offset, 4 * C});
     plan.push_back({(void**)&h->s.scan_status, 8 * (tiles + 1)});
@@ -677,6 +687,7 @@ mg_status mg_upload(mg_handle h, int32_t id, const void* host, size_t bytes) {
     cudaStream_t st = h->stream;
     Carried& c = h->set[h->cur];
     void* dst = nullptr;
+    h->flist_valid = false;
     switch (id) {
     case MG_FPOS: dst = c.pos; break;
     case MG_FVEL: dst = c.vel; break;
@@ -850,7 +861,7 @@ mg_status mg_compute_pressure(mg_handle h) {
 mg_status mg_compute_force(mg_handle h) {
     mg_status st = need_sorted(h);
     if (st != MG_OK) return st;
-    launch_force(h->P, h->set[h->cur], h->s, h->stream);
+    launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream);
     launch_apply_breaks(h->P, h->set[h->cur], h->s, h->stream);
     return check_device(h);
 }
@@ -873,6 +884,7 @@ mg_status mg_advance(mg_handle h) {
     mg_status st = need_sorted(h);
     if (st != MG_OK) return st;
     launch_advance(h->P, h->set[h->cur], h->s, false, h->stream);
+    h->flist_valid = false;
     h->time = h->time + h->P.dt;
     return check_device(h);
 }
@@ -925,6 +937,20 @@ mg_status mg_time_steps(mg_handle h, uint32_t nsteps, uint32_t flags, float* ms)
     *ms = t;
     if (st != MG_OK) return st;
     return check_device(h);
+}
+
+mg_status mg_set_option(mg_handle h, int32_t option, int32_t value) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    switch (option) {
+    case MG_OPT_NEIGHBOR_SEARCH:
+        if (value != 0 && value != 1) return fail(h, MG_ERR_INVALID_ARG, "neighbour search is 0 or 1");
+        h->warp_search = value == 1;
+        h->flist_valid = false;
+        clear_graphs(h);
+        return MG_OK;
+    default:
+        return fail(h, MG_ERR_INVALID_ARG, "unknown option " + std::to_string(option));
+    }
 }
 
 mg_status mg_profile_enable(mg_handle h, int32_t enable) {

@@ -34,6 +34,8 @@ constexpr int WARP_CELL_MAX = 256;   // cells up to this size are ordered by one
 constexpr int BLOCK_CELL_MAX = 8192; // up to this by one block in shared memory
 constexpr uint32_t BIG_LIST_CAP = 1u << 16;
 constexpr uint32_t SPIN_LIMIT = 1u << 22; // bounded look-back polls
+constexpr int NL_CAP = 48;  // per-lane neighbour list of the warp-cooperative density pass
+constexpr int FL_CAP = 12;  // fluid-force neighbours (dsq < 1) recorded per particle
 
 // Error bits in the device error word.
 enum : uint32_t {
@@ -46,7 +48,7 @@ enum : uint32_t {
 struct DevParams {
     float gmin[3], gdelta[3];
     int res[3], scanmax[3];
-    int adjcnt, nadj;
+    int adjcnt, nadj, gsrch;
     int adj[64];
     float sr, r2, r2diff, d2, pmass, rest, istiff, wc2, surf;
     float pr, bmin[3], bmax[3], estiff, damp, xmin_stiff, xmax_stiff, slope, one_minus_slope;
@@ -101,6 +103,8 @@ struct Scratch {
     float* invdens;
     float4* force;
     uint32_t* brk;      // bonds that broke in the last force pass
+    uint32_t* flist;    // [FL_CAP][cap] fluid-force neighbours found by the density pass
+    uint32_t* fcount;   // [cap] their number (> FL_CAP: search again)
     uint32_t* count;    // [cells]
     uint32_t* offset;   // [cells]
     unsigned long long* scan_status;  // [tiles]
@@ -119,8 +123,9 @@ void launch_gather(const DevParams& P, const Carried& src, const float* src_conc
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st);
 // flags: 1 density/pressure, 2 diffusion, 4 gene reaction
 void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
-                 float* conc_out, const Scratch& s, int flags, cudaStream_t st);
-void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
+                 float* conc_out, const Scratch& s, int flags, bool warp_search, cudaStream_t st);
+void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool use_list,
+                  cudaStream_t st);
 void launch_apply_breaks(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_breaks,
                     cudaStream_t st);

@@ -7,83 +7,106 @@
 // contributeDiffusion/computeDiffusion (cuda:3026-3105), computeGeneAction/tallyGeneAction
 // (cuda:714-772), contributeForce/computeForce (cuda:3167-3358), advanceParticles
 // (cuda:3470-3614).
+//
+// Summation order.  The reference visits the gridAdj cells in ascending linear cell index and
+// each cell's particles in sorted order, i.e. every neighbour sum runs over ascending sorted
+// index q, with per-cell partial sums for density and fluid force.  Both search paths below
+// keep exactly that order, so they give identical bits:
+//  * direct: one thread per particle walks its gridAdjCnt cells (the reference loop);
+//  * warp search: the 32 particles of a warp walk the union of their cell windows together.
+//    Each chunk of 32 candidates is loaded once (one candidate per lane) and tested against
+//    the warp's bounding box grown by the search radius; survivors are broadcast in ascending
+//    order and every lane appends the ones inside its own radius and window to a per-lane
+//    list in shared memory.  The neighbour terms are then evaluated lane by lane over these
+//    lists, so no lane idles through a neighbour that belongs to another lane.  A lane whose
+//    list overflows falls back to the direct walk.
+// The density pass also records each particle's fluid-force neighbours (dsq < 1) so the force
+// pass reads a short list instead of searching again.
 #include <cfloat>
 #include "mg_internal.cuh"
 
 namespace mg {
 
-// ---- density / pressure, diffusion, gene reaction ------------------------------------------
-// One thread per sorted particle.  The neighbour loop visits the gridAdjCnt cells in the
-// reference's gridAdj order and each cell's particles in sorted order; the density sum keeps
-// the reference's per-cell partial sums.  FLAGS: 1 density/pressure, 2 diffusion,
-// 4 gene reaction.  Diffusion reads conc_in for every neighbour and writes conc_out (Jacobi).
-template <int FLAGS>
-__global__ void __launch_bounds__(256) k_dens(DevParams P, const DevGenome* __restrict__ G,
-                                              const float4* __restrict__ pos,
-                                              const float* __restrict__ conc_in,
-                                              float* __restrict__ conc_out,
-                                              const uint32_t* __restrict__ genes,
-                                              const uint32_t* __restrict__ scell,
-                                              const uint32_t* __restrict__ count,
-                                              const uint32_t* __restrict__ offset,
-                                              float* __restrict__ press,
-                                              float* __restrict__ invdens,
-                                              const uint32_t* __restrict__ nactive_p) {
-    constexpr bool DENS = FLAGS & 1, DIFF = FLAGS & 2, GENE = FLAGS & 4;
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= *nactive_p) return;
-    const float4 ip = pos[p];
-    float cur[NTF], nc[NTF], dif[NTF];
-    if (DIFF || GENE) {
-        const float4* c4 = reinterpret_cast<const float4*>(conc_in + (size_t)p * NTF);
+constexpr int DENS_WARPS = 8;
+
+struct CellWin {
+    int x, y, z;  // window origin = own cell - (1,1,1)
+};
+
+__device__ __forceinline__ CellWin window_of(const DevParams& P, uint32_t cell) {
+    CellWin w;
+    w.x = (int)(cell % (uint32_t)P.res[0]) - 1;
+    w.z = (int)((cell / (uint32_t)P.res[0]) % (uint32_t)P.res[2]) - 1;
+    w.y = (int)(cell / ((uint32_t)P.res[0] * (uint32_t)P.res[2])) - 1;
+    return w;
+}
+
+// ---- per-neighbour terms ---------------------------------------------------------------
+__device__ __forceinline__ float wendland_term(float dsq, float sr) {
+    const float r = sqrtf(dsq);
+    const float qq = r / sr;
+    float b = 1.f - qq;
+    b *= b;
+    b *= b;
+    return b * (4.f * qq + 1.f);
+}
+
+template <bool DIFF>
+__device__ __forceinline__ void diffuse_add(float (&nc)[NTF], const float (&dif)[NTF],
+                                            const float (&cur)[NTF], const float* conc, uint32_t q,
+                                            float cc) {
+    if (!DIFF) return;
+    const float4* cj4 = reinterpret_cast<const float4*>(conc + (size_t)q * NTF);
+    float cj[NTF];
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            float4 v = c4[k];
-            cur[4 * k] = v.x; cur[4 * k + 1] = v.y; cur[4 * k + 2] = v.z; cur[4 * k + 3] = v.w;
-        }
+    for (int k = 0; k < 4; k++) {
+        float4 v = cj4[k];
+        cj[4 * k] = v.x; cj[4 * k + 1] = v.y; cj[4 * k + 2] = v.z; cj[4 * k + 3] = v.w;
     }
-    if (DIFF) {
 #pragma unroll
-        for (int t = 0; t < NTF; t++) { nc[t] = 0.f; dif[t] = G->diff[t]; }
-    }
+    for (int t = 0; t < NTF; t++)
+        if (dif[t] != 0.f) nc[t] += (dif[t] * cc) * (cj[t] - cur[t]);
+}
+
+// The reference neighbour walk for one particle: density sum and diffusion exchange.
+template <bool DENS, bool DIFF>
+__device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint32_t pcell,
+                                             const float4* __restrict__ pos,
+                                             const float* __restrict__ conc,
+                                             const uint32_t* __restrict__ count,
+                                             const uint32_t* __restrict__ offset,
+                                             float (&nc)[NTF], const float (&dif)[NTF],
+                                             const float (&cur)[NTF]) {
     float sum = 0.f;
-    if (DENS || DIFF) {
-        const uint32_t base = scell[p] - (uint32_t)P.nadj;
-        for (int c = 0; c < P.adjcnt; c++) {
-            const uint32_t cellc = base + (uint32_t)P.adj[c];
-            const uint32_t cnt = count[cellc];
-            if (cnt == 0) continue;
-            const uint32_t off = offset[cellc];
-            float part = 0.f;
-            for (uint32_t q = off; q < off + cnt; q++) {
-                const float4 jp = pos[q];
-                const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
-                const float dsq = dx * dx + dy * dy + dz * dz;
-                if (DENS && dsq < P.r2 && dsq > 0.f) {
-                    const float r = sqrtf(dsq);
-                    const float qq = r / P.sr;
-                    float b = 1.f - qq;
-                    b *= b;
-                    b *= b;
-                    part += b * (4.f * qq + 1.f);
-                }
-                if (DIFF && dsq < P.r2diff && dsq > 0.f) {
-                    const float cc = (P.r2diff - dsq) * P.d2;
-                    const float4* cj4 = reinterpret_cast<const float4*>(conc_in + (size_t)q * NTF);
-                    float cj[NTF];
-#pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        float4 v = cj4[k];
-                        cj[4 * k] = v.x; cj[4 * k + 1] = v.y; cj[4 * k + 2] = v.z; cj[4 * k + 3] = v.w;
-                    }
-#pragma unroll
-                    for (int t = 0; t < NTF; t++)
-                        if (dif[t] != 0.f) nc[t] += (dif[t] * cc) * (cj[t] - cur[t]);
-                }
-            }
-            if (DENS) sum += part;
+    const uint32_t base = pcell - (uint32_t)P.nadj;
+    for (int c = 0; c < P.adjcnt; c++) {
+        const uint32_t cellc = base + (uint32_t)P.adj[c];
+        const uint32_t cnt = count[cellc];
+        if (cnt == 0) continue;
+        const uint32_t off = offset[cellc];
+        float part = 0.f;
+        for (uint32_t q = off; q < off + cnt; q++) {
+            const float4 jp = pos[q];
+            const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+            const float dsq = dx * dx + dy * dy + dz * dz;
+            if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
+            if (DIFF && dsq < P.r2diff && dsq > 0.f) diffuse_add<DIFF>(nc, dif, cur, conc, q, (P.r2diff - dsq) * P.d2);
         }
+        if (DENS) sum += part;
     }
+    return sum;
+}
+
+// Density -> pressure and 1/density; diffusion result and the gene reaction; conc written.
+template <int FLAGS>
+__device__ __forceinline__ void dens_epilogue(const DevParams& P, const DevGenome* __restrict__ G,
+                                              uint32_t p, float sum, const float (&nc)[NTF],
+                                              const float (&cur)[NTF],
+                                              const uint32_t* __restrict__ genes,
+                                              float* __restrict__ conc_out,
+                                              float* __restrict__ press,
+                                              float* __restrict__ invdens) {
+    constexpr bool DENS = FLAGS & 1, DIFF = FLAGS & 2, GENE = FLAGS & 4;
     if (DENS) {
         sum = sum * P.pmass * P.wc2;
         if (sum == 0.f) sum = 1.f;
@@ -131,8 +154,204 @@ __global__ void __launch_bounds__(256) k_dens(DevParams P, const DevGenome* __re
     }
 }
 
+template <int FLAGS>
+__device__ __forceinline__ void load_conc(const DevGenome* __restrict__ G, const float* conc_in,
+                                          uint32_t p, float (&cur)[NTF], float (&nc)[NTF],
+                                          float (&dif)[NTF]) {
+    constexpr bool DIFF = FLAGS & 2, GENE = FLAGS & 4;
+    if (DIFF || GENE) {
+        const float4* c4 = reinterpret_cast<const float4*>(conc_in + (size_t)p * NTF);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            float4 v = c4[k];
+            cur[4 * k] = v.x; cur[4 * k + 1] = v.y; cur[4 * k + 2] = v.z; cur[4 * k + 3] = v.w;
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < NTF; t++) {
+        nc[t] = 0.f;
+        dif[t] = DIFF ? G->diff[t] : 0.f;
+    }
+}
+
+// ---- direct kernel (one thread per particle, the reference loop) ------------------------
+template <int FLAGS>
+__global__ void __launch_bounds__(256) k_dens(DevParams P, const DevGenome* __restrict__ G,
+                                              const float4* __restrict__ pos,
+                                              const float* __restrict__ conc_in,
+                                              float* __restrict__ conc_out,
+                                              const uint32_t* __restrict__ genes,
+                                              const uint32_t* __restrict__ scell,
+                                              const uint32_t* __restrict__ count,
+                                              const uint32_t* __restrict__ offset,
+                                              float* __restrict__ press,
+                                              float* __restrict__ invdens,
+                                              const uint32_t* __restrict__ nactive_p) {
+    constexpr bool DENS = FLAGS & 1, DIFF = FLAGS & 2;
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= *nactive_p) return;
+    float cur[NTF], nc[NTF], dif[NTF];
+    load_conc<FLAGS>(G, conc_in, p, cur, nc, dif);
+    float sum = 0.f;
+    if (DENS || DIFF)
+        sum = dens_direct<DENS, DIFF>(P, pos[p], scell[p], pos, conc_in, count, offset, nc, dif, cur);
+    dens_epilogue<FLAGS>(P, G, p, sum, nc, cur, genes, conc_out, press, invdens);
+}
+
+// ---- warp-cooperative kernel ----------------------------------------------------------------
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, d));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, d));
+    return v;
+}
+__device__ __forceinline__ int warp_mini(int v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, d));
+    return v;
+}
+__device__ __forceinline__ int warp_maxi(int v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, d));
+    return v;
+}
+
+template <int FLAGS>
+__global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
+    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
+    const float* __restrict__ conc_in, float* __restrict__ conc_out,
+    const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
+    const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
+    float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
+    uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p) {
+    constexpr bool DENS = FLAGS & 1, DIFF = FLAGS & 2;
+    extern __shared__ uint32_t s_list[];  // [DENS_WARPS][NL_CAP][32]
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    uint32_t* my = s_list + (size_t)w * NL_CAP * 32 + lane;
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nact = *nactive_p;
+    const bool act = p < nact;
+    if (!__any_sync(0xffffffffu, act)) return;
+
+    float cur[NTF], nc[NTF], dif[NTF];
+    load_conc<FLAGS>(G, conc_in, act ? p : 0u, cur, nc, dif);
+    const float4 ip = act ? pos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const uint32_t pcell = act ? scell[p] : 0u;
+    const CellWin win = window_of(P, pcell);
+    // search radius: the largest threshold any term of this pass (and the force list) uses
+    float R2 = 1.f;
+    if (DENS) R2 = fmaxf(R2, P.r2);
+    if (DIFF) R2 = fmaxf(R2, P.r2diff);
+    const float Rf = sqrtf(R2) * 1.0001f + 1e-3f;  // conservative prefilter radius
+    const float INF = __int_as_float(0x7f800000);
+    const float bx0 = warp_min(act ? ip.x : INF) - Rf, bx1 = warp_max(act ? ip.x : -INF) + Rf;
+    const float by0 = warp_min(act ? ip.y : INF) - Rf, by1 = warp_max(act ? ip.y : -INF) + Rf;
+    const float bz0 = warp_min(act ? ip.z : INF) - Rf, bz1 = warp_max(act ? ip.z : -INF) + Rf;
+    const int g = P.gsrch;
+    const int BIG = 1 << 30;
+    const int wx0 = warp_mini(act ? win.x : BIG), wx1 = warp_maxi(act ? win.x : -BIG) + g - 1;
+    const int wy0 = warp_mini(act ? win.y : BIG), wy1 = warp_maxi(act ? win.y : -BIG) + g - 1;
+    const int wz0 = warp_mini(act ? win.z : BIG), wz1 = warp_maxi(act ? win.z : -BIG) + g - 1;
+
+    uint32_t n = 0, nf = 0;
+    for (int cy = wy0; cy <= wy1; cy++) {
+        for (int cz = wz0; cz <= wz1; cz++) {
+            for (int cx = wx0; cx <= wx1; cx++) {
+                const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
+                const uint32_t cnt = count[cell];
+                if (cnt == 0) continue;
+                const bool inw = act && cx - win.x >= 0 && cx - win.x < g && cy - win.y >= 0 &&
+                                 cy - win.y < g && cz - win.z >= 0 && cz - win.z < g;
+                if (!__any_sync(0xffffffffu, inw)) continue;
+                const uint32_t off = offset[cell];
+                for (uint32_t base = 0; base < cnt; base += 32) {
+                    const uint32_t k = base + lane;
+                    const bool valid = k < cnt;
+                    const float4 qp = valid ? pos[off + k] : make_float4(INF, INF, INF, 0.f);
+                    const float ex = fmaxf(0.f, fmaxf(bx0 - qp.x, qp.x - bx1));
+                    const float ey = fmaxf(0.f, fmaxf(by0 - qp.y, qp.y - by1));
+                    const float ez = fmaxf(0.f, fmaxf(bz0 - qp.z, qp.z - bz1));
+                    const bool surv = valid && (ex == 0.f && ey == 0.f && ez == 0.f);
+                    unsigned ball = __ballot_sync(0xffffffffu, surv);
+                    while (ball) {
+                        const int s = __ffs(ball) - 1;
+                        ball &= ball - 1;
+                        const float qx = __shfl_sync(0xffffffffu, qp.x, s);
+                        const float qy = __shfl_sync(0xffffffffu, qp.y, s);
+                        const float qz = __shfl_sync(0xffffffffu, qp.z, s);
+                        if (inw) {
+                            const float dx = ip.x - qx, dy = ip.y - qy, dz = ip.z - qz;
+                            const float dsq = dx * dx + dy * dy + dz * dz;
+                            const uint32_t q = off + base + (uint32_t)s;
+                            if (dsq < R2 && dsq > 0.f) {
+                                if (n < (uint32_t)NL_CAP) my[n * 32] = q;
+                                n++;
+                            }
+                            if (dsq < 1.f && dsq > 0.f) {
+                                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
+                                nf++;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (!act) return;
+    fcount[p] = nf;
+    float sum = 0.f;
+    if (n <= (uint32_t)NL_CAP) {
+        float part = 0.f;
+        uint32_t curcell = UNDEF;
+        for (uint32_t k = 0; k < n; k++) {
+            const uint32_t q = my[k * 32];
+            if (DENS) {
+                const uint32_t qc = scell[q];
+                if (qc != curcell) {  // flush the partial sum of the previous cell
+                    sum += part;
+                    part = 0.f;
+                    curcell = qc;
+                }
+            }
+            const float4 jp = pos[q];
+            const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+            const float dsq = dx * dx + dy * dy + dz * dz;
+            if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
+            if (DIFF && dsq < P.r2diff && dsq > 0.f) diffuse_add<DIFF>(nc, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2);
+        }
+        if (DENS) sum += part;
+    } else {
+#pragma unroll
+        for (int t = 0; t < NTF; t++) nc[t] = 0.f;
+        sum = dens_direct<DENS, DIFF>(P, ip, pcell, pos, conc_in, count, offset, nc, dif, cur);
+    }
+    dens_epilogue<FLAGS>(P, G, p, sum, nc, cur, genes, conc_out, press, invdens);
+}
+
 void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
-                 float* conc_out, const Scratch& s, int flags, cudaStream_t st) {
+                 float* conc_out, const Scratch& s, int flags, bool warp_search, cudaStream_t st) {
+    const size_t smem = (size_t)DENS_WARPS * NL_CAP * 32 * sizeof(uint32_t);
+    if (warp_search && (flags & 3)) {
+        uint32_t blocks = (P.cap + DENS_WARPS * 32 - 1) / (DENS_WARPS * 32);
+#define MG_DENSW_CASE(F)                                                                          \
+    case F:                                                                                       \
+        k_dens_warp<F><<<blocks, DENS_WARPS * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,   \
+                                                             cur.genes, s.scell, s.count,         \
+                                                             s.offset, s.press, s.invdens,        \
+                                                             s.flist, s.fcount, s.counters + 3);  \
+        break;
+        switch (flags & 7) {
+            MG_DENSW_CASE(1) MG_DENSW_CASE(2) MG_DENSW_CASE(3) MG_DENSW_CASE(5) MG_DENSW_CASE(6)
+            MG_DENSW_CASE(7)
+            default: break;
+        }
+#undef MG_DENSW_CASE
+        return;
+    }
     uint32_t blocks = (P.cap + 255) / 256;
 #define MG_DENS_CASE(F)                                                                        \
     case F:                                                                                    \
@@ -179,12 +398,34 @@ __device__ __forceinline__ bool is_nan3(const BondTerm& t) {
     return t.ex != t.ex || t.ey != t.ey || t.ez != t.ez;
 }
 
+// Fluid pressure, surface and viscosity terms of one neighbour (contributeForce, cuda:3203-3221).
+__device__ __forceinline__ void fluid_term(const DevParams& P, float4 ip, float4 iv, float ipress,
+                                           float idens, float4 jp, float4 jv, float jpress,
+                                           float jdens, float dsq, float dx, float dy, float dz,
+                                           float& cx, float& cy, float& cz) {
+    const float r = sqrtf(dsq);
+    const float t = P.sr - r;
+    const float kern = t * t * t;
+    const float prs = 100.f * (ipress + jpress);
+    const float s = (idens * jdens) * 100.f;
+    const float term = prs * kern - P.surf * (t * t);
+    const float px = (s * (dx / r)) * term, py = (s * (dy / r)) * term, pz = (s * (dz / r)) * term;
+    const float vx = (100000.f * (jv.x - iv.x)) * kern;
+    const float vy = (100000.f * (jv.y - iv.y)) * kern;
+    const float vz = (100000.f * (jv.z - iv.z)) * kern;
+    cx = cx + (px + vx);
+    cy = cy + (py + vy);
+    cz = cz + (pz + vz);
+}
+
 __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
                                                const uint32_t* __restrict__ scell,
                                                const uint32_t* __restrict__ count,
                                                const uint32_t* __restrict__ offset,
                                                const float* __restrict__ press,
                                                const float* __restrict__ invdens,
+                                               const uint32_t* __restrict__ flist,
+                                               const uint32_t* __restrict__ fcount, int use_list,
                                                float4* __restrict__ force,
                                                uint32_t* __restrict__ brk,
                                                const uint32_t* __restrict__ nactive_p) {
@@ -219,40 +460,45 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
     }
     // fluid pressure, surface and viscosity terms (contributeForce, cuda:3167-3226)
     {
-        const uint32_t base = scell[p] - (uint32_t)P.nadj;
-        const float ipress = press[p], idens = invdens[p], sr = P.sr;
+        const float ipress = press[p], idens = invdens[p];
         float sx = 0.f, sy = 0.f, sz = 0.f;
-        for (int c = 0; c < P.adjcnt; c++) {
-            const uint32_t cellc = base + (uint32_t)P.adj[c];
-            const uint32_t cnt = count[cellc];
-            if (cnt == 0) continue;
-            const uint32_t off = offset[cellc];
+        const uint32_t nf = use_list ? fcount[p] : 0xFFFFFFFFu;
+        if (nf <= (uint32_t)FL_CAP) {
             float cx = 0.f, cy = 0.f, cz = 0.f;
-            for (uint32_t q = off; q < off + cnt; q++) {
+            uint32_t curcell = UNDEF;
+            for (uint32_t k = 0; k < nf; k++) {
+                const uint32_t q = flist[(size_t)k * cap + p];
+                const uint32_t qc = scell[q];
+                if (qc != curcell) {
+                    sx = sx + cx; sy = sy + cy; sz = sz + cz;
+                    cx = cy = cz = 0.f;
+                    curcell = qc;
+                }
                 const float4 jp = C.pos[q];
                 const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
                 const float dsq = dx * dx + dy * dy + dz * dz;
-                if (dsq < 1.f && dsq > 0.f) {
-                    const float r = sqrtf(dsq);
-                    const float t = sr - r;
-                    const float kern = t * t * t;
-                    const float prs = 100.f * (ipress + press[q]);
-                    const float s = (idens * invdens[q]) * 100.f;
-                    const float term = prs * kern - P.surf * (t * t);
-                    const float4 jv = C.veval[q];
-                    const float px = (s * (dx / r)) * term, py = (s * (dy / r)) * term,
-                                pz = (s * (dz / r)) * term;
-                    const float vx = (100000.f * (jv.x - iv.x)) * kern;
-                    const float vy = (100000.f * (jv.y - iv.y)) * kern;
-                    const float vz = (100000.f * (jv.z - iv.z)) * kern;
-                    cx = cx + (px + vx);
-                    cy = cy + (py + vy);
-                    cz = cz + (pz + vz);
-                }
+                fluid_term(P, ip, iv, ipress, idens, jp, C.veval[q], press[q], invdens[q], dsq, dx, dy,
+                           dz, cx, cy, cz);
             }
-            sx = sx + cx;
-            sy = sy + cy;
-            sz = sz + cz;
+            sx = sx + cx; sy = sy + cy; sz = sz + cz;
+        } else {
+            const uint32_t base = scell[p] - (uint32_t)P.nadj;
+            for (int c = 0; c < P.adjcnt; c++) {
+                const uint32_t cellc = base + (uint32_t)P.adj[c];
+                const uint32_t cnt = count[cellc];
+                if (cnt == 0) continue;
+                const uint32_t off = offset[cellc];
+                float cx = 0.f, cy = 0.f, cz = 0.f;
+                for (uint32_t q = off; q < off + cnt; q++) {
+                    const float4 jp = C.pos[q];
+                    const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+                    const float dsq = dx * dx + dy * dy + dz * dz;
+                    if (dsq < 1.f && dsq > 0.f)
+                        fluid_term(P, ip, iv, ipress, idens, jp, C.veval[q], press[q], invdens[q], dsq,
+                                   dx, dy, dz, cx, cy, cz);
+                }
+                sx = sx + cx; sy = sy + cy; sz = sz + cz;
+            }
         }
         fx = fx + sx * P.pmass;
         fy = fy + sy * P.pmass;
@@ -291,10 +537,11 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
     brk[p] = br;
 }
 
-void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st) {
+void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool use_list,
+                  cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
-    k_force<<<blocks, 256, 0, st>>>(P, cur, s.scell, s.count, s.offset, s.press, s.invdens,
-                                    s.force, s.brk, s.counters + 3);
+    k_force<<<blocks, 256, 0, st>>>(P, cur, s.scell, s.count, s.offset, s.press, s.invdens, s.flist,
+                                    s.fcount, use_list ? 1 : 0, s.force, s.brk, s.counters + 3);
 }
 
 // Broken bonds get rest length 0 (cuda:3315-3317).  The force kernel records the breaks in

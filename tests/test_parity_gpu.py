@@ -240,3 +240,21 @@ def test_graph_cache_alternates_buffers(built, cfg0):
     g.Run2GeneAction(); o.diffusion(); o.genes()
     g.Run(3); o.step(3)
     compare(g, o)
+
+
+@pytest.mark.parametrize("param", ["R", "L"])
+def test_warp_search_equals_direct_walk(built, param):
+    """The warp-cooperative neighbour search gives the direct walk's bits."""
+    import morphogenesis_gb300 as mg
+
+    d = demo.make_block((20, 12, 16), param, seed=8)
+    outs = []
+    for mode in (0, 1):
+        g = mg.FluidSystem(d.params, d.genome, d.n)
+        g.set_option(A.OPT_NEIGHBOR_SEARCH, mode)
+        g.TransferToCL(d.arrays)
+        g.Run(20)
+        outs.append({b: g.download(b) for b in (A.FPOS, A.FVEL, A.FCONC, A.FPRESS, A.FDENSITY,
+                                                 A.FFORCE, A.FELASTIDX, A.FPARTICLE_ID)})
+    for b in outs[0]:
+        assert same_bits(outs[0][b].view(np.float32), outs[1][b].view(np.float32)), f"buffer {b}"
