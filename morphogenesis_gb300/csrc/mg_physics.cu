@@ -257,7 +257,10 @@ __global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
     const int wy0 = warp_mini(act ? win.y : BIG), wy1 = warp_maxi(act ? win.y : -BIG) + g - 1;
     const int wz0 = warp_mini(act ? win.z : BIG), wz1 = warp_maxi(act ? win.z : -BIG) + g - 1;
 
-    uint32_t n = 0, nf = 0;
+    // survivors of one chunk: position and index, compacted in ascending candidate order
+    __shared__ float4 s_sp[DENS_WARPS][32];
+    __shared__ uint32_t s_sq[DENS_WARPS][32];
+    uint32_t n = 0;
     for (int cy = wy0; cy <= wy1; cy++) {
         for (int cz = wz0; cz <= wz1; cz++) {
             for (int cx = wx0; cx <= wx1; cx++) {
@@ -276,37 +279,35 @@ __global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
                     const float ey = fmaxf(0.f, fmaxf(by0 - qp.y, qp.y - by1));
                     const float ez = fmaxf(0.f, fmaxf(bz0 - qp.z, qp.z - bz1));
                     const bool surv = valid && (ex == 0.f && ey == 0.f && ez == 0.f);
-                    unsigned ball = __ballot_sync(0xffffffffu, surv);
-                    while (ball) {
-                        const int s = __ffs(ball) - 1;
-                        ball &= ball - 1;
-                        const float qx = __shfl_sync(0xffffffffu, qp.x, s);
-                        const float qy = __shfl_sync(0xffffffffu, qp.y, s);
-                        const float qz = __shfl_sync(0xffffffffu, qp.z, s);
-                        if (inw) {
-                            const float dx = ip.x - qx, dy = ip.y - qy, dz = ip.z - qz;
+                    const unsigned ball = __ballot_sync(0xffffffffu, surv);
+                    if (surv) {
+                        const uint32_t slot = (uint32_t)__popc(ball & ((1u << lane) - 1u));
+                        s_sp[w][slot] = qp;
+                        s_sq[w][slot] = off + k;
+                    }
+                    __syncwarp();
+                    const int ns = __popc(ball);
+                    if (inw) {
+                        for (int t = 0; t < ns; t++) {
+                            const float4 sp = s_sp[w][t];
+                            const float dx = ip.x - sp.x, dy = ip.y - sp.y, dz = ip.z - sp.z;
                             const float dsq = dx * dx + dy * dy + dz * dz;
-                            const uint32_t q = off + base + (uint32_t)s;
                             if (dsq < R2 && dsq > 0.f) {
-                                if (n < (uint32_t)NL_CAP) my[n * 32] = q;
+                                if (n < (uint32_t)NL_CAP) my[n * 32] = s_sq[w][t];
                                 n++;
-                            }
-                            if (dsq < 1.f && dsq > 0.f) {
-                                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
-                                nf++;
                             }
                         }
                     }
+                    __syncwarp();
                 }
             }
         }
     }
     if (!act) return;
-    fcount[p] = nf;
     float sum = 0.f;
     if (n <= (uint32_t)NL_CAP) {
         float part = 0.f;
-        uint32_t curcell = UNDEF;
+        uint32_t curcell = UNDEF, nf = 0;
         for (uint32_t k = 0; k < n; k++) {
             const uint32_t q = my[k * 32];
             if (DENS) {
@@ -320,14 +321,20 @@ __global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
             const float4 jp = pos[q];
             const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
             const float dsq = dx * dx + dy * dy + dz * dz;
+            if (dsq < 1.f && dsq > 0.f) {  // fluid-force neighbour, kept for the force pass
+                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
+                nf++;
+            }
             if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
             if (DIFF && dsq < P.r2diff && dsq > 0.f) diffuse_add<DIFF>(nc, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2);
         }
         if (DENS) sum += part;
+        fcount[p] = nf;
     } else {
 #pragma unroll
         for (int t = 0; t < NTF; t++) nc[t] = 0.f;
         sum = dens_direct<DENS, DIFF>(P, ip, pcell, pos, conc_in, count, offset, nc, dif, cur);
+        fcount[p] = FL_CAP + 1;  // the force pass searches again
     }
     dens_epilogue<FLAGS>(P, G, p, sum, nc, cur, genes, conc_out, press, invdens);
 }
