@@ -512,6 +512,8 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaGetDevice"); }
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
     if (h->num_sms <= 0) h->num_sms = 1;
+    e = physics_init();
+    if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "kernel attributes"); }
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaStreamCreate"); }
 

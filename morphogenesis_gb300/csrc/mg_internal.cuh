@@ -113,6 +113,7 @@ struct Scratch {
 };
 
 // ---- launchers (all on one stream; no host synchronisation inside) ----------------------
+cudaError_t physics_init();  // per-kernel attributes, once per device before the first launch
 void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
 void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long long* status,
                  uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st);

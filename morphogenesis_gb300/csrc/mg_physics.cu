@@ -339,6 +339,19 @@ __global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
     dens_epilogue<FLAGS>(P, G, p, sum, nc, cur, genes, conc_out, press, invdens);
 }
 
+// The per-lane lists take 48 KB of dynamic shared memory next to the static survivor buffers,
+// above the 48 KB a launch gets without opting in.
+cudaError_t physics_init() {
+    const int smem = DENS_WARPS * NL_CAP * 32 * (int)sizeof(uint32_t);
+    cudaError_t e = cudaSuccess;
+#define MG_ATTR(F)                                                                              \
+    if (e == cudaSuccess)                                                                       \
+        e = cudaFuncSetAttribute(k_dens_warp<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    MG_ATTR(1) MG_ATTR(2) MG_ATTR(3) MG_ATTR(5) MG_ATTR(6) MG_ATTR(7)
+#undef MG_ATTR
+    return e;
+}
+
 void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
                  float* conc_out, const Scratch& s, int flags, bool warp_search, cudaStream_t st) {
     const size_t smem = (size_t)DENS_WARPS * NL_CAP * 32 * sizeof(uint32_t);
