@@ -61,7 +61,7 @@ struct mg_system {
     bool ever_sorted = false;
     bool brk_pending = false;
     bool flist_valid = false;   // fluid-force lists match the current positions and order
-    bool warp_search = true;    // density pass: warp-cooperative search (else direct walk)
+    int search = 2;             // density pass search: 0 direct, 1 warp, 2 cell-aligned groups
     float time = 0.f;
     std::string err;
     std::map<uint64_t, cudaGraphExec_t> graphs;
@@ -275,11 +275,13 @@ void enqueue_insert_rank(mg_system* h, bool prof) {
     cudaMemsetAsync(h->s.count, 0, sizeof(uint32_t) * P.cells, st);
     cudaMemsetAsync(h->s.scan_status, 0, sizeof(unsigned long long) * scan_status_words(P.cells), st);
     cudaMemsetAsync(h->s.counters, 0, 2 * sizeof(uint32_t), st);
+    cudaMemsetAsync(h->s.counters + 4, 0, sizeof(uint32_t), st);
     { Mark m(h, prof, "insert"); launch_insert(P, h->set[h->cur], h->s, st); }
     { Mark m(h, prof, "scan"); launch_scan(h->s.count, h->s.offset, P.cells, h->s.scan_status,
                                            h->s.counters, h->s.counters + 3, h->s.counters + 2, st); }
     { Mark m(h, prof, "place"); launch_place(P, h->s, st); }
     { Mark m(h, prof, "cellsort"); launch_cellsort(P, h->s, h->num_sms, st); }
+    { Mark m(h, prof, "groups"); launch_groups(P, h->set[h->cur].pos, h->s, h->num_sms, st); }
 }
 
 void enqueue_gather(mg_system* h, bool prof) {
@@ -297,9 +299,9 @@ void enqueue_dens(mg_system* h, int flags, bool prof) {
     int cin = h->conc_cur, cout = 1 - h->conc_cur;
     { Mark m(h, prof, flags == 1 ? "pressure" : flags == 7 ? "density_diffusion_genes" : "diffusion_genes");
       launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, flags,
-                  h->warp_search, h->stream); }
+                  h->search, h->num_sms, h->stream); }
     if (flags & 6) h->conc_cur = cout;
-    if (h->warp_search && (flags & 3)) h->flist_valid = true;
+    if (h->search && (flags & 3)) h->flist_valid = true;
 }
 
 // One step in the legacy Run() order (fluid_system.cpp:1179-1349), one sort per step.
@@ -316,7 +318,7 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
 }
 
 int kernels_per_step(uint32_t flags) {
-    int n = 6;  // insert, scan, place, cellsort, cellsort_big, gather
+    int n = 7;  // insert, scan, place, cellsort, cellsort_big, groups, gather
     if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES)) n += 1;
     if (flags & MG_STEP_PHYSICS) n += 2;
     return n;
@@ -372,7 +374,7 @@ mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
     h->phase = PHASE_SORTED;
     h->ever_sorted = true;
     h->brk_pending = false;
-    h->flist_valid = (flags & MG_STEP_PHYSICS) ? false : (h->warp_search && (flags & MG_STEP_GENES));
+    h->flist_valid = (flags & MG_STEP_PHYSICS) ? false : (h->search && (flags & MG_STEP_GENES));
     if (h->profile) prof_collect(h);
     return MG_OK;
 }
@@ -548,6 +550,8 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     plan.push_back({(void**)&h->s.force, 16 * n});
     plan.push_back({(void**)&h->s.brk, 4 * n});
     plan.push_back({(void**)&h->s.flist, 4 * (size_t)FL_CAP * n});
+    plan.push_back({(void**)&h->s.porder, 4 * n});
+    plan.push_back({(void**)&h->s.groups, 8 * n});
     plan.push_back({(void**)&h->s.fcount, 4 * n});
     plan.push_back({(void**)&h->s.count, 4 * C});
     plan.push_back({(void**)&h->s.offset, 4 * C});
@@ -945,8 +949,8 @@ mg_status mg_set_option(mg_handle h, int32_t option, int32_t value) {
     if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
     switch (option) {
     case MG_OPT_NEIGHBOR_SEARCH:
-        if (value != 0 && value != 1) return fail(h, MG_ERR_INVALID_ARG, "neighbour search is 0 or 1");
-        h->warp_search = value == 1;
+        if (value < 0 || value > 2) return fail(h, MG_ERR_INVALID_ARG, "neighbour search is 0, 1 or 2");
+        h->search = value;
         h->flist_valid = false;
         clear_graphs(h);
         return MG_OK;

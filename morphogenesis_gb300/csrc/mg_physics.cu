@@ -220,22 +220,20 @@ __device__ __forceinline__ int warp_maxi(int v) {
     return v;
 }
 
+// One warp item: up to 32 particles (lane l holds particle p when act) searched together.
+// Every lane of the warp must call this (it uses warp collectives).
 template <int FLAGS>
-__global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
-    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
+__device__ __forceinline__ void dens_warp_item(
+    const DevParams& P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
     const float* __restrict__ conc_in, float* __restrict__ conc_out,
     const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
-    uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p) {
+    uint32_t* __restrict__ fcount, uint32_t p, bool act, uint32_t* s_list, float4 (*s_sp)[32],
+    uint32_t (*s_sq)[32]) {
     constexpr bool DENS = FLAGS & 1, DIFF = FLAGS & 2;
-    extern __shared__ uint32_t s_list[];  // [DENS_WARPS][NL_CAP][32]
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     uint32_t* my = s_list + (size_t)w * NL_CAP * 32 + lane;
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nact = *nactive_p;
-    const bool act = p < nact;
-    if (!__any_sync(0xffffffffu, act)) return;
 
     float cur[NTF], nc[NTF], dif[NTF];
     load_conc<FLAGS>(G, conc_in, act ? p : 0u, cur, nc, dif);
@@ -257,9 +255,6 @@ __global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
     const int wy0 = warp_mini(act ? win.y : BIG), wy1 = warp_maxi(act ? win.y : -BIG) + g - 1;
     const int wz0 = warp_mini(act ? win.z : BIG), wz1 = warp_maxi(act ? win.z : -BIG) + g - 1;
 
-    // survivors of one chunk: position and index, compacted in ascending candidate order
-    __shared__ float4 s_sp[DENS_WARPS][32];
-    __shared__ uint32_t s_sq[DENS_WARPS][32];
     uint32_t n = 0;
     for (int cy = wy0; cy <= wy1; cy++) {
         for (int cz = wz0; cz <= wz1; cz++) {
@@ -339,6 +334,52 @@ __global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
     dens_epilogue<FLAGS>(P, G, p, sum, nc, cur, genes, conc_out, press, invdens);
 }
 
+template <int FLAGS>
+__global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
+    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
+    const float* __restrict__ conc_in, float* __restrict__ conc_out,
+    const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
+    const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
+    float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
+    uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p) {
+    extern __shared__ uint32_t s_list[];  // [DENS_WARPS][NL_CAP][32]
+    __shared__ float4 s_sp[DENS_WARPS][32];
+    __shared__ uint32_t s_sq[DENS_WARPS][32];
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = p < *nactive_p;
+    if (!__any_sync(0xffffffffu, act)) return;
+    dens_warp_item<FLAGS>(P, G, pos, conc_in, conc_out, genes, scell, count, offset, press, invdens,
+                          flist, fcount, p, act, s_list, s_sp, s_sq);
+}
+
+// Cell-aligned groups: each warp takes groups of up to 32 particles of one cell, in the
+// octant order of k_groups, so its bounding box is a compact part of one cell.
+template <int FLAGS>
+__global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_grp(
+    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
+    const float* __restrict__ conc_in, float* __restrict__ conc_out,
+    const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
+    const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
+    float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
+    uint32_t* __restrict__ fcount, const uint2* __restrict__ groups,
+    const uint32_t* __restrict__ porder, const uint32_t* __restrict__ ngroups_p) {
+    extern __shared__ uint32_t s_list[];  // [DENS_WARPS][NL_CAP][32]
+    __shared__ float4 s_sp[DENS_WARPS][32];
+    __shared__ uint32_t s_sq[DENS_WARPS][32];
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t gw = blockIdx.x * DENS_WARPS + (threadIdx.x >> 5);
+    const uint32_t nw = gridDim.x * DENS_WARPS;
+    const uint32_t ng = *ngroups_p;
+    for (uint32_t grp = gw; grp < ng; grp += nw) {
+        const uint2 e = groups[grp];
+        const bool act = lane < e.y;
+        const uint32_t p = act ? porder[e.x + lane] : 0u;
+        dens_warp_item<FLAGS>(P, G, pos, conc_in, conc_out, genes, scell, count, offset, press,
+                              invdens, flist, fcount, p, act, s_list, s_sp, s_sq);
+        __syncwarp();
+    }
+}
+
 // The per-lane lists take 48 KB of dynamic shared memory next to the static survivor buffers,
 // above the 48 KB a launch gets without opting in.
 cudaError_t physics_init() {
@@ -349,13 +390,37 @@ cudaError_t physics_init() {
         e = cudaFuncSetAttribute(k_dens_warp<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     MG_ATTR(1) MG_ATTR(2) MG_ATTR(3) MG_ATTR(5) MG_ATTR(6) MG_ATTR(7)
 #undef MG_ATTR
+#define MG_ATTR(F)                                                                              \
+    if (e == cudaSuccess)                                                                       \
+        e = cudaFuncSetAttribute(k_dens_grp<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    MG_ATTR(1) MG_ATTR(2) MG_ATTR(3) MG_ATTR(5) MG_ATTR(6) MG_ATTR(7)
+#undef MG_ATTR
     return e;
 }
 
 void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
-                 float* conc_out, const Scratch& s, int flags, bool warp_search, cudaStream_t st) {
+                 float* conc_out, const Scratch& s, int flags, int search, int num_sms,
+                 cudaStream_t st) {
     const size_t smem = (size_t)DENS_WARPS * NL_CAP * 32 * sizeof(uint32_t);
-    if (warp_search && (flags & 3)) {
+    if (search == 2 && (flags & 3)) {
+        const uint32_t blocks = (uint32_t)num_sms * 4;
+#define MG_DENSG_CASE(F)                                                                          \
+    case F:                                                                                       \
+        k_dens_grp<F><<<blocks, DENS_WARPS * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,    \
+                                                            cur.genes, s.scell, s.count,          \
+                                                            s.offset, s.press, s.invdens,         \
+                                                            s.flist, s.fcount, s.groups,          \
+                                                            s.porder, s.counters + 4);            \
+        break;
+        switch (flags & 7) {
+            MG_DENSG_CASE(1) MG_DENSG_CASE(2) MG_DENSG_CASE(3) MG_DENSG_CASE(5) MG_DENSG_CASE(6)
+            MG_DENSG_CASE(7)
+            default: break;
+        }
+#undef MG_DENSG_CASE
+        return;
+    }
+    if (search == 1 && (flags & 3)) {
         uint32_t blocks = (P.cap + DENS_WARPS * 32 - 1) / (DENS_WARPS * 32);
 #define MG_DENSW_CASE(F)                                                                          \
     case F:                                                                                       \
