@@ -221,8 +221,7 @@ mg_status mg_synchronize(mg_handle h);
 /* ---- tuning ------------------------------------------------------------------------------ */
 enum mg_option {
     /* neighbour search of the density/diffusion pass: 0 = one thread walks its 27 cells
-     * (the reference loop), 1 = warp-cooperative search over consecutive particles,
-     * 2 = warp-cooperative search over cell-aligned groups (default).  Results are identical. */
+     * (the reference loop), 1 = warp-cooperative search (default).  Results are identical. */
     MG_OPT_NEIGHBOR_SEARCH = 1
 };
 mg_status mg_set_option(mg_handle h, int32_t option, int32_t value);

@@ -61,7 +61,7 @@ struct mg_system {
     bool ever_sorted = false;
     bool brk_pending = false;
     bool flist_valid = false;   // fluid-force lists match the current positions and order
-    int search = 2;             // density pass search: 0 direct, 1 warp, 2 cell-aligned groups
+    int search = 1;             // density pass search: 0 direct walk, 1 warp-cooperative
     float time = 0.f;
     std::string err;
     std::map<uint64_t, cudaGraphExec_t> graphs;
@@ -275,13 +275,11 @@ void enqueue_insert_rank(mg_system* h, bool prof) {
     cudaMemsetAsync(h->s.count, 0, sizeof(uint32_t) * P.cells, st);
     cudaMemsetAsync(h->s.scan_status, 0, sizeof(unsigned long long) * scan_status_words(P.cells), st);
     cudaMemsetAsync(h->s.counters, 0, 2 * sizeof(uint32_t), st);
-    cudaMemsetAsync(h->s.counters + 4, 0, sizeof(uint32_t), st);
     { Mark m(h, prof, "insert"); launch_insert(P, h->set[h->cur], h->s, st); }
     { Mark m(h, prof, "scan"); launch_scan(h->s.count, h->s.offset, P.cells, h->s.scan_status,
                                            h->s.counters, h->s.counters + 3, h->s.counters + 2, st); }
     { Mark m(h, prof, "place"); launch_place(P, h->s, st); }
     { Mark m(h, prof, "cellsort"); launch_cellsort(P, h->s, h->num_sms, st); }
-    { Mark m(h, prof, "groups"); launch_groups(P, h->set[h->cur].pos, h->s, h->num_sms, st); }
 }
 
 void enqueue_gather(mg_system* h, bool prof) {
@@ -318,7 +316,7 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
 }
 
 int kernels_per_step(uint32_t flags) {
-    int n = 7;  // insert, scan, place, cellsort, cellsort_big, groups, gather
+    int n = 6;  // insert, scan, place, cellsort, cellsort_big, gather
     if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES)) n += 1;
     if (flags & MG_STEP_PHYSICS) n += 2;
     return n;
@@ -550,8 +548,6 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     plan.push_back({(void**)&h->s.force, 16 * n});
     plan.push_back({(void**)&h->s.brk, 4 * n});
     plan.push_back({(void**)&h->s.flist, 4 * (size_t)FL_CAP * n});
-    plan.push_back({(void**)&h->s.porder, 4 * n});
-    plan.push_back({(void**)&h->s.groups, 8 * n});
     plan.push_back({(void**)&h->s.fcount, 4 * n});
     plan.push_back({(void**)&h->s.count, 4 * C});
     plan.push_back({(void**)&h->s.offset, 4 * C});
@@ -949,7 +945,7 @@ mg_status mg_set_option(mg_handle h, int32_t option, int32_t value) {
     if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
     switch (option) {
     case MG_OPT_NEIGHBOR_SEARCH:
-        if (value < 0 || value > 2) return fail(h, MG_ERR_INVALID_ARG, "neighbour search is 0, 1 or 2");
+        if (value < 0 || value > 1) return fail(h, MG_ERR_INVALID_ARG, "neighbour search is 0 or 1");
         h->search = value;
         h->flist_valid = false;
         clear_graphs(h);

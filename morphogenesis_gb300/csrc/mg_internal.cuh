@@ -34,8 +34,8 @@ constexpr int WARP_CELL_MAX = 256;   // cells up to this size are ordered by one
 constexpr int BLOCK_CELL_MAX = 8192; // up to this by one block in shared memory
 constexpr uint32_t BIG_LIST_CAP = 1u << 16;
 constexpr uint32_t SPIN_LIMIT = 1u << 22; // bounded look-back polls
-constexpr int NL_CAP = 48;  // per-lane neighbour list of the warp-cooperative density pass
-constexpr int FL_CAP = 12;  // fluid-force neighbours (dsq < 1) recorded per particle
+constexpr int NL_CAP = 64;  // per-lane neighbour list of the warp-cooperative density pass
+constexpr int FL_CAP = 32;  // fluid-force neighbours (dsq < 1) recorded per particle
 
 // Error bits in the device error word.
 enum : uint32_t {
@@ -108,10 +108,8 @@ struct Scratch {
     uint32_t* count;    // [cells]
     uint32_t* offset;   // [cells]
     unsigned long long* scan_status;  // [tiles]
-    uint32_t* porder;   // [cap] per-cell octant order of the sorted slots (processing order)
-    uint2* groups;      // [cap] (first porder slot, size <= 32) warp groups, one cell each
     uint32_t* counters; // [0] scan tile ticket, [1] big-cell list length, [2] error word,
-                        // [3] nactive, [4] number of warp groups
+                        // [3] nactive
     uint32_t* big_list; // [BIG_LIST_CAP] cells that need the block-level ordering
 };
 
@@ -126,13 +124,11 @@ void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, cudaStre
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st);
 // flags: 1 density/pressure, 2 diffusion, 4 gene reaction
-// search: 0 direct walk, 1 warp-cooperative over consecutive particles, 2 over cell groups
+// search: 0 direct walk, 1 warp-cooperative over consecutive particles
 void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
                  cudaStream_t st);
-// octant processing order and cell-aligned warp groups (after the cell sort, before gather)
-void launch_groups(const DevParams& P, const float4* src_pos, const Scratch& s, int num_sms,
-                   cudaStream_t st);
+
 void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool use_list,
                   cudaStream_t st);
 void launch_apply_breaks(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);

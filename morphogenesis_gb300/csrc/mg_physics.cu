@@ -255,82 +255,88 @@ __device__ __forceinline__ void dens_warp_item(
     const int wy0 = warp_mini(act ? win.y : BIG), wy1 = warp_maxi(act ? win.y : -BIG) + g - 1;
     const int wz0 = warp_mini(act ? win.z : BIG), wz1 = warp_maxi(act ? win.z : -BIG) + g - 1;
 
-    uint32_t n = 0;
-    for (int cy = wy0; cy <= wy1; cy++) {
-        for (int cz = wz0; cz <= wz1; cz++) {
-            for (int cx = wx0; cx <= wx1; cx++) {
-                const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
-                const uint32_t cnt = count[cell];
-                if (cnt == 0) continue;
-                const bool inw = act && cx - win.x >= 0 && cx - win.x < g && cy - win.y >= 0 &&
-                                 cy - win.y < g && cz - win.z >= 0 && cz - win.z < g;
-                if (!__any_sync(0xffffffffu, inw)) continue;
-                const uint32_t off = offset[cell];
-                for (uint32_t base = 0; base < cnt; base += 32) {
-                    const uint32_t k = base + lane;
-                    const bool valid = k < cnt;
-                    const float4 qp = valid ? pos[off + k] : make_float4(INF, INF, INF, 0.f);
-                    const float ex = fmaxf(0.f, fmaxf(bx0 - qp.x, qp.x - bx1));
-                    const float ey = fmaxf(0.f, fmaxf(by0 - qp.y, qp.y - by1));
-                    const float ez = fmaxf(0.f, fmaxf(bz0 - qp.z, qp.z - bz1));
-                    const bool surv = valid && (ex == 0.f && ey == 0.f && ez == 0.f);
-                    const unsigned ball = __ballot_sync(0xffffffffu, surv);
-                    if (surv) {
-                        const uint32_t slot = (uint32_t)__popc(ball & ((1u << lane) - 1u));
-                        s_sp[w][slot] = qp;
-                        s_sq[w][slot] = off + k;
-                    }
-                    __syncwarp();
-                    const int ns = __popc(ball);
-                    if (inw) {
-                        for (int t = 0; t < ns; t++) {
-                            const float4 sp = s_sp[w][t];
-                            const float dx = ip.x - sp.x, dy = ip.y - sp.y, dz = ip.z - sp.z;
-                            const float dsq = dx * dx + dy * dy + dz * dz;
-                            if (dsq < R2 && dsq > 0.f) {
-                                if (n < (uint32_t)NL_CAP) my[n * 32] = s_sq[w][t];
-                                n++;
+    // Passes: each collects, per lane, up to NL_CAP neighbours with index >= qmin in
+    // ascending order and consumes them; a lane with more neighbours asks for another pass.
+    // Every running sum (density partials, diffusion, force list) continues across passes,
+    // so the result is the single ascending walk whatever the number of passes.
+    float sum = 0.f, part = 0.f;
+    uint32_t curcell = UNDEF, nf = 0, qmin = 0;
+    bool more = act;
+    while (__any_sync(0xffffffffu, more)) {
+        uint32_t n = 0;
+        for (int cy = wy0; cy <= wy1; cy++) {
+            for (int cz = wz0; cz <= wz1; cz++) {
+                for (int cx = wx0; cx <= wx1; cx++) {
+                    const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
+                    const uint32_t cnt = count[cell];
+                    if (cnt == 0) continue;
+                    const bool inw = more && cx - win.x >= 0 && cx - win.x < g && cy - win.y >= 0 &&
+                                     cy - win.y < g && cz - win.z >= 0 && cz - win.z < g;
+                    if (!__any_sync(0xffffffffu, inw)) continue;
+                    const uint32_t off = offset[cell];
+                    for (uint32_t base = 0; base < cnt; base += 32) {
+                        const uint32_t k = base + lane;
+                        const bool valid = k < cnt;
+                        const float4 qp = valid ? pos[off + k] : make_float4(INF, INF, INF, 0.f);
+                        const float ex = fmaxf(0.f, fmaxf(bx0 - qp.x, qp.x - bx1));
+                        const float ey = fmaxf(0.f, fmaxf(by0 - qp.y, qp.y - by1));
+                        const float ez = fmaxf(0.f, fmaxf(bz0 - qp.z, qp.z - bz1));
+                        const bool surv = valid && (ex == 0.f && ey == 0.f && ez == 0.f);
+                        const unsigned ball = __ballot_sync(0xffffffffu, surv);
+                        if (surv) {
+                            const uint32_t slot = (uint32_t)__popc(ball & ((1u << lane) - 1u));
+                            s_sp[w][slot] = qp;
+                            s_sq[w][slot] = off + k;
+                        }
+                        __syncwarp();
+                        const int ns = __popc(ball);
+                        if (inw) {
+                            for (int t = 0; t < ns; t++) {
+                                const float4 sp = s_sp[w][t];
+                                const float dx = ip.x - sp.x, dy = ip.y - sp.y, dz = ip.z - sp.z;
+                                const float dsq = dx * dx + dy * dy + dz * dz;
+                                const uint32_t q = s_sq[w][t];
+                                if (dsq < R2 && dsq > 0.f && q >= qmin) {
+                                    if (n < (uint32_t)NL_CAP) my[n * 32] = q;
+                                    n++;
+                                }
                             }
                         }
+                        __syncwarp();
                     }
-                    __syncwarp();
                 }
             }
         }
+        if (more) {
+            const uint32_t take = n < (uint32_t)NL_CAP ? n : (uint32_t)NL_CAP;
+            for (uint32_t k = 0; k < take; k++) {
+                const uint32_t q = my[k * 32];
+                if (DENS) {
+                    const uint32_t qc = scell[q];
+                    if (qc != curcell) {  // flush the partial sum of the previous cell
+                        sum += part;
+                        part = 0.f;
+                        curcell = qc;
+                    }
+                }
+                const float4 jp = pos[q];
+                const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+                const float dsq = dx * dx + dy * dy + dz * dz;
+                if (dsq < 1.f && dsq > 0.f) {  // fluid-force neighbour, kept for the force pass
+                    if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
+                    nf++;
+                }
+                if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
+                if (DIFF && dsq < P.r2diff && dsq > 0.f) diffuse_add<DIFF>(nc, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2);
+            }
+            if (n > (uint32_t)NL_CAP) qmin = my[(NL_CAP - 1) * 32] + 1;
+            else more = false;
+        }
+        __syncwarp();
     }
     if (!act) return;
-    float sum = 0.f;
-    if (n <= (uint32_t)NL_CAP) {
-        float part = 0.f;
-        uint32_t curcell = UNDEF, nf = 0;
-        for (uint32_t k = 0; k < n; k++) {
-            const uint32_t q = my[k * 32];
-            if (DENS) {
-                const uint32_t qc = scell[q];
-                if (qc != curcell) {  // flush the partial sum of the previous cell
-                    sum += part;
-                    part = 0.f;
-                    curcell = qc;
-                }
-            }
-            const float4 jp = pos[q];
-            const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
-            const float dsq = dx * dx + dy * dy + dz * dz;
-            if (dsq < 1.f && dsq > 0.f) {  // fluid-force neighbour, kept for the force pass
-                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
-                nf++;
-            }
-            if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
-            if (DIFF && dsq < P.r2diff && dsq > 0.f) diffuse_add<DIFF>(nc, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2);
-        }
-        if (DENS) sum += part;
-        fcount[p] = nf;
-    } else {
-#pragma unroll
-        for (int t = 0; t < NTF; t++) nc[t] = 0.f;
-        sum = dens_direct<DENS, DIFF>(P, ip, pcell, pos, conc_in, count, offset, nc, dif, cur);
-        fcount[p] = FL_CAP + 1;  // the force pass searches again
-    }
+    if (DENS) sum += part;
+    fcount[p] = nf;  // > FL_CAP: the force pass searches again
     dens_epilogue<FLAGS>(P, G, p, sum, nc, cur, genes, conc_out, press, invdens);
 }
 
@@ -352,35 +358,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
                           flist, fcount, p, act, s_list, s_sp, s_sq);
 }
 
-// Cell-aligned groups: each warp takes groups of up to 32 particles of one cell, in the
-// octant order of k_groups, so its bounding box is a compact part of one cell.
-template <int FLAGS>
-__global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_grp(
-    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
-    const float* __restrict__ conc_in, float* __restrict__ conc_out,
-    const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
-    const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
-    float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
-    uint32_t* __restrict__ fcount, const uint2* __restrict__ groups,
-    const uint32_t* __restrict__ porder, const uint32_t* __restrict__ ngroups_p) {
-    extern __shared__ uint32_t s_list[];  // [DENS_WARPS][NL_CAP][32]
-    __shared__ float4 s_sp[DENS_WARPS][32];
-    __shared__ uint32_t s_sq[DENS_WARPS][32];
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t gw = blockIdx.x * DENS_WARPS + (threadIdx.x >> 5);
-    const uint32_t nw = gridDim.x * DENS_WARPS;
-    const uint32_t ng = *ngroups_p;
-    for (uint32_t grp = gw; grp < ng; grp += nw) {
-        const uint2 e = groups[grp];
-        const bool act = lane < e.y;
-        const uint32_t p = act ? porder[e.x + lane] : 0u;
-        dens_warp_item<FLAGS>(P, G, pos, conc_in, conc_out, genes, scell, count, offset, press,
-                              invdens, flist, fcount, p, act, s_list, s_sp, s_sq);
-        __syncwarp();
-    }
-}
-
-// The per-lane lists take 48 KB of dynamic shared memory next to the static survivor buffers,
+// The per-lane lists take 64 KB of dynamic shared memory next to the static survivor buffers,
 // above the 48 KB a launch gets without opting in.
 cudaError_t physics_init() {
     const int smem = DENS_WARPS * NL_CAP * 32 * (int)sizeof(uint32_t);
@@ -390,11 +368,6 @@ cudaError_t physics_init() {
         e = cudaFuncSetAttribute(k_dens_warp<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     MG_ATTR(1) MG_ATTR(2) MG_ATTR(3) MG_ATTR(5) MG_ATTR(6) MG_ATTR(7)
 #undef MG_ATTR
-#define MG_ATTR(F)                                                                              \
-    if (e == cudaSuccess)                                                                       \
-        e = cudaFuncSetAttribute(k_dens_grp<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    MG_ATTR(1) MG_ATTR(2) MG_ATTR(3) MG_ATTR(5) MG_ATTR(6) MG_ATTR(7)
-#undef MG_ATTR
     return e;
 }
 
@@ -402,24 +375,6 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
                  cudaStream_t st) {
     const size_t smem = (size_t)DENS_WARPS * NL_CAP * 32 * sizeof(uint32_t);
-    if (search == 2 && (flags & 3)) {
-        const uint32_t blocks = (uint32_t)num_sms * 4;
-#define MG_DENSG_CASE(F)                                                                          \
-    case F:                                                                                       \
-        k_dens_grp<F><<<blocks, DENS_WARPS * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,    \
-                                                            cur.genes, s.scell, s.count,          \
-                                                            s.offset, s.press, s.invdens,         \
-                                                            s.flist, s.fcount, s.groups,          \
-                                                            s.porder, s.counters + 4);            \
-        break;
-        switch (flags & 7) {
-            MG_DENSG_CASE(1) MG_DENSG_CASE(2) MG_DENSG_CASE(3) MG_DENSG_CASE(5) MG_DENSG_CASE(6)
-            MG_DENSG_CASE(7)
-            default: break;
-        }
-#undef MG_DENSG_CASE
-        return;
-    }
     if (search == 1 && (flags & 3)) {
         uint32_t blocks = (P.cap + DENS_WARPS * 32 - 1) / (DENS_WARPS * 32);
 #define MG_DENSW_CASE(F)                                                                          \
@@ -453,6 +408,10 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
 }
 
 // ---- force -------------------------------------------------------------------------------
+// computeForce skips a bond when `restlength < 0.000000001` with the float promoted to double
+// (cuda:3268).  For every float x that test equals x < REST_MIN, REST_MIN being the smallest
+// float not below 1e-9 (0x30897060 = 1.0000000604e-9), so it runs on the FP32 pipe.
+#define REST_MIN __int_as_float(0x30897060)
 // Elastic bond term of bond (owner o -> partner j) as computeForce evaluates it in the owner's
 // thread (cuda:3263-3307).  Returns the acceleration pushed onto the partner; the owner
 // subtracts it.
@@ -528,7 +487,7 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
         const uint4 A = rec[0];
         const uint32_t j = A.x;
         const float restlen = __uint_as_float(A.y);
-        if (j >= nact || (double)restlen < 0.000000001) continue;
+        if (j >= nact || restlen < REST_MIN) continue;
         const uint4 B = rec[1];
         const float elastlim = __uint_as_float(B.x);
         const BondTerm t = bond_term(ip, iv, C.pos[j], C.veval[j], restlen, __uint_as_float(A.z),
@@ -606,7 +565,7 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
             const uint4 A = rec[0];
             if (A.x != p) continue;
             const float restlen = __uint_as_float(A.y);
-            if ((double)restlen < 0.000000001) continue;
+            if (restlen < REST_MIN) continue;
             const float elastlim = __uint_as_float(reinterpret_cast<const uint32_t*>(rec + 1)[0]);
             const BondTerm t = bond_term(C.pos[k], C.veval[k], ip, iv, restlen,
                                          __uint_as_float(A.z), __uint_as_float(A.w), elastlim,

@@ -294,77 +294,6 @@ void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, cudaStre
         P.cap, s.cell, s.count, s.offset, s.order, s.newidx, s.big_list, s.counters + 1);
 }
 
-// ---- processing groups ------------------------------------------------------------------------
-// The neighbour passes take warps of up to 32 particles from one cell.  Inside each cell the
-// particles are ordered by octant (z half, then y half, then x half, then sorted index), so a
-// group of 32 from a cell of 64 is one half of the cell.  Group slots are claimed with an
-// atomic counter; their order does not matter because every particle is computed alone.
-constexpr int GR_WARPS = 8, GR_CELLS = 8;
-
-__global__ void __launch_bounds__(GR_WARPS * 32) k_groups(DevParams P, const float4* __restrict__ src_pos,
-                                                          const uint32_t* __restrict__ count,
-                                                          const uint32_t* __restrict__ offset,
-                                                          const uint32_t* __restrict__ order,
-                                                          uint32_t* __restrict__ porder,
-                                                          uint2* __restrict__ groups,
-                                                          uint32_t* __restrict__ ngroups) {
-    __shared__ uint32_t skey[GR_WARPS][WARP_CELL_MAX];
-    const uint32_t w = threadIdx.x >> 5, lane = lane_id();
-    const uint32_t gw = blockIdx.x * GR_WARPS + w, nw = gridDim.x * GR_WARPS;
-    for (uint32_t c0 = gw * GR_CELLS; c0 < P.cells; c0 += nw * GR_CELLS) {
-        const uint32_t c = c0 + lane;
-        const uint32_t n = (lane < (uint32_t)GR_CELLS && c < P.cells) ? count[c] : 0u;
-        unsigned todo = __ballot_sync(0xffffffffu, n > 0);
-        while (todo) {
-            const int src = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const uint32_t cell = c0 + (uint32_t)src;
-            const uint32_t cn = __shfl_sync(0xffffffffu, n, src);
-            const uint32_t co = offset[cell];
-            if (cn <= (uint32_t)WARP_CELL_MAX) {
-                const int cx = (int)(cell % (uint32_t)P.res[0]);
-                const int cz = (int)((cell / (uint32_t)P.res[0]) % (uint32_t)P.res[2]);
-                const int cy = (int)(cell / ((uint32_t)P.res[0] * (uint32_t)P.res[2]));
-                for (uint32_t k = lane; k < cn; k += 32) {
-                    const float4 q = src_pos[order[co + k]];
-                    const float fx = (q.x - P.gmin[0]) * P.gdelta[0] - (float)cx;
-                    const float fy = (q.y - P.gmin[1]) * P.gdelta[1] - (float)cy;
-                    const float fz = (q.z - P.gmin[2]) * P.gdelta[2] - (float)cz;
-                    const uint32_t oct = (fz >= 0.5f ? 4u : 0u) | (fy >= 0.5f ? 2u : 0u) | (fx >= 0.5f ? 1u : 0u);
-                    skey[w][k] = (oct << 16) | k;
-                }
-                __syncwarp();
-                for (uint32_t k = lane; k < cn; k += 32) {
-                    const uint32_t key = skey[w][k];
-                    uint32_t r = 0;
-                    for (uint32_t m = 0; m < cn; m++) r += skey[w][m] < key ? 1u : 0u;
-                    porder[co + r] = co + k;
-                }
-                __syncwarp();
-            } else {
-                for (uint32_t k = lane; k < cn; k += 32) porder[co + k] = co + k;
-            }
-            const uint32_t ng = (cn + 31) / 32;
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(ngroups, ng);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            for (uint32_t g = lane; g < ng; g += 32)
-                groups[base + g] = make_uint2(co + 32 * g, min(32u, cn - 32 * g));
-        }
-    }
-}
-
-void launch_groups(const DevParams& P, const float4* src_pos, const Scratch& s, int num_sms,
-                   cudaStream_t st) {
-    uint32_t units = (P.cells + GR_CELLS - 1) / GR_CELLS;
-    uint32_t blocks = (units + GR_WARPS - 1) / GR_WARPS;
-    uint32_t maxb = (uint32_t)num_sms * 16;
-    if (blocks > maxb) blocks = maxb;
-    if (blocks == 0) blocks = 1;
-    k_groups<<<blocks, GR_WARPS * 32, 0, st>>>(P, src_pos, s.count, s.offset, s.order, s.porder,
-                                                 s.groups, s.counters + 4);
-}
-
 // ---- gather ---------------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t remap(uint32_t j, uint32_t cap, const uint32_t* newidx) {
     return j < cap ? __ldg(newidx + j) : NO_PARTNER;

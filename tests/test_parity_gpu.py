@@ -249,7 +249,7 @@ def test_warp_search_equals_direct_walk(built, param):
 
     d = demo.make_block((20, 12, 16), param, seed=8)
     outs = []
-    for mode in (0, 1, 2):
+    for mode in (0, 1):
         g = mg.FluidSystem(d.params, d.genome, d.n)
         g.set_option(A.OPT_NEIGHBOR_SEARCH, mode)
         g.TransferToCL(d.arrays)
@@ -257,5 +257,5 @@ def test_warp_search_equals_direct_walk(built, param):
         outs.append({b: g.download(b) for b in (A.FPOS, A.FVEL, A.FCONC, A.FPRESS, A.FDENSITY,
                                                  A.FFORCE, A.FELASTIDX, A.FPARTICLE_ID)})
     for b in outs[0]:
-        for m in (1, 2):
+        for m in (1,):
             assert same_bits(outs[0][b].view(np.float32), outs[m][b].view(np.float32)), f"buffer {b} mode {m}"
