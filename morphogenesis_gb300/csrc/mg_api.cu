@@ -156,6 +156,8 @@ mg_status check_params(mg_system* h, const mg_fparams* p) {
     return MG_OK;
 }
 
+void clear_graphs(mg_system* h);
+
 mg_status upload_genome(mg_system* h) {
     DevGenome g;
     std::memset(&g, 0, sizeof(g));
@@ -186,6 +188,10 @@ mg_status upload_genome(mg_system* h) {
         g.nact[a] = 0;
         g.delay[a] = G.delay[a];
     }
+    int uniform = g.diff[0] != 0.f;
+    for (int t = 1; t < NTF; t++) uniform &= g.diff[t] == g.diff[0];
+    if (h->P.uniform_diff != uniform) clear_graphs(h);
+    h->P.uniform_diff = uniform;
     MG_CUDA(h, cudaMemcpyAsync(h->dG, &g, sizeof(g), cudaMemcpyHostToDevice, h->stream));
     MG_CUDA(h, cudaStreamSynchronize(h->stream));
     return MG_OK;
@@ -613,7 +619,9 @@ mg_status mg_update_params(mg_handle h, const mg_fparams* p) {
             return fail(h, MG_ERR_INVALID_ARG, "grid resolution is fixed at mg_create");
     h->params = *p;
     h->time = p->time;
+    const int uniform = h->P.uniform_diff;
     derive(h->P, *p, h->cap);
+    h->P.uniform_diff = uniform;
     clear_graphs(h);
     return MG_OK;
 }

@@ -55,6 +55,7 @@ struct DevParams {
     float grav[3], AL, AL2, VL, VL2, vl_factor, dt;
     float null_z;
     int freeze;
+    int uniform_diff;  // all 16 diffusion rates equal and nonzero (set from the genome)
     uint32_t cap;
     uint32_t cells;
 };

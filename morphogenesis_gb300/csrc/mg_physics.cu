@@ -19,7 +19,7 @@
 //    order and every lane appends the ones inside its own radius and window to a per-lane
 //    list in shared memory.  The neighbour terms are then evaluated lane by lane over these
 //    lists, so no lane idles through a neighbour that belongs to another lane.  A lane whose
-//    list overflows falls back to the direct walk.
+//    list overflows (more than NL_CAP neighbours) falls back to the direct walk.
 // The density pass also records each particle's fluid-force neighbours (dsq < 1) so the force
 // pass reads a short list instead of searching again.
 #include <cfloat>
@@ -54,8 +54,22 @@ __device__ __forceinline__ float wendland_term(float dsq, float sr) {
 template <bool DIFF>
 __device__ __forceinline__ void diffuse_add(float (&nc)[NTF], const float (&dif)[NTF],
                                             const float (&cur)[NTF], const float* conc, uint32_t q,
-                                            float cc) {
+                                            float cc, bool uniform) {
     if (!DIFF) return;
+    if (uniform) {
+        // every species has the same rate dif[0] != 0: (dif[t] * cc) is one value
+        const float a = dif[0] * cc;
+        const float4* cj4 = reinterpret_cast<const float4*>(conc + (size_t)q * NTF);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float4 v = cj4[k];
+            nc[4 * k] += a * (v.x - cur[4 * k]);
+            nc[4 * k + 1] += a * (v.y - cur[4 * k + 1]);
+            nc[4 * k + 2] += a * (v.z - cur[4 * k + 2]);
+            nc[4 * k + 3] += a * (v.w - cur[4 * k + 3]);
+        }
+        return;
+    }
     const float4* cj4 = reinterpret_cast<const float4*>(conc + (size_t)q * NTF);
     float cj[NTF];
 #pragma unroll
@@ -90,7 +104,7 @@ __device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint
             const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
             const float dsq = dx * dx + dy * dy + dz * dz;
             if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
-            if (DIFF && dsq < P.r2diff && dsq > 0.f) diffuse_add<DIFF>(nc, dif, cur, conc, q, (P.r2diff - dsq) * P.d2);
+            if (DIFF && dsq < P.r2diff && dsq > 0.f) diffuse_add<DIFF>(nc, dif, cur, conc, q, (P.r2diff - dsq) * P.d2, false);
         }
         if (DENS) sum += part;
     }
@@ -235,8 +249,9 @@ __device__ __forceinline__ void dens_warp_item(
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     uint32_t* my = s_list + (size_t)w * NL_CAP * 32 + lane;
 
-    float cur[NTF], nc[NTF], dif[NTF];
-    load_conc<FLAGS>(G, conc_in, act ? p : 0u, cur, nc, dif);
+    float nc[NTF];
+#pragma unroll
+    for (int t = 0; t < NTF; t++) nc[t] = 0.f;
     const float4 ip = act ? pos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
     const uint32_t pcell = act ? scell[p] : 0u;
     const CellWin win = window_of(P, pcell);
@@ -255,93 +270,91 @@ __device__ __forceinline__ void dens_warp_item(
     const int wy0 = warp_mini(act ? win.y : BIG), wy1 = warp_maxi(act ? win.y : -BIG) + g - 1;
     const int wz0 = warp_mini(act ? win.z : BIG), wz1 = warp_maxi(act ? win.z : -BIG) + g - 1;
 
-    // Passes: each collects, per lane, up to NL_CAP neighbours with index >= qmin in
-    // ascending order and consumes them; a lane with more neighbours asks for another pass.
-    // Every running sum (density partials, diffusion, force list) continues across passes,
-    // so the result is the single ascending walk whatever the number of passes.
-    float sum = 0.f, part = 0.f;
-    uint32_t curcell = UNDEF, nf = 0, qmin = 0;
-    bool more = act;
-    while (__any_sync(0xffffffffu, more)) {
-        uint32_t n = 0;
-        for (int cy = wy0; cy <= wy1; cy++) {
-            for (int cz = wz0; cz <= wz1; cz++) {
-                for (int cx = wx0; cx <= wx1; cx++) {
-                    const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
-                    const uint32_t cnt = count[cell];
-                    if (cnt == 0) continue;
-                    const bool inw = more && cx - win.x >= 0 && cx - win.x < g && cy - win.y >= 0 &&
-                                     cy - win.y < g && cz - win.z >= 0 && cz - win.z < g;
-                    if (!__any_sync(0xffffffffu, inw)) continue;
-                    const uint32_t off = offset[cell];
-                    for (uint32_t base = 0; base < cnt; base += 32) {
-                        const uint32_t k = base + lane;
-                        const bool valid = k < cnt;
-                        const float4 qp = valid ? pos[off + k] : make_float4(INF, INF, INF, 0.f);
-                        const float ex = fmaxf(0.f, fmaxf(bx0 - qp.x, qp.x - bx1));
-                        const float ey = fmaxf(0.f, fmaxf(by0 - qp.y, qp.y - by1));
-                        const float ez = fmaxf(0.f, fmaxf(bz0 - qp.z, qp.z - bz1));
-                        const bool surv = valid && (ex == 0.f && ey == 0.f && ez == 0.f);
-                        const unsigned ball = __ballot_sync(0xffffffffu, surv);
-                        if (surv) {
-                            const uint32_t slot = (uint32_t)__popc(ball & ((1u << lane) - 1u));
-                            s_sp[w][slot] = qp;
-                            s_sq[w][slot] = off + k;
-                        }
-                        __syncwarp();
-                        const int ns = __popc(ball);
-                        if (inw) {
-                            for (int t = 0; t < ns; t++) {
-                                const float4 sp = s_sp[w][t];
-                                const float dx = ip.x - sp.x, dy = ip.y - sp.y, dz = ip.z - sp.z;
-                                const float dsq = dx * dx + dy * dy + dz * dz;
-                                const uint32_t q = s_sq[w][t];
-                                if (dsq < R2 && dsq > 0.f && q >= qmin) {
-                                    if (n < (uint32_t)NL_CAP) my[n * 32] = q;
-                                    n++;
-                                }
+    uint32_t n = 0;
+    for (int cy = wy0; cy <= wy1; cy++) {
+        for (int cz = wz0; cz <= wz1; cz++) {
+            for (int cx = wx0; cx <= wx1; cx++) {
+                const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
+                const uint32_t cnt = count[cell];
+                if (cnt == 0) continue;
+                const bool inw = act && cx - win.x >= 0 && cx - win.x < g && cy - win.y >= 0 &&
+                                 cy - win.y < g && cz - win.z >= 0 && cz - win.z < g;
+                if (!__any_sync(0xffffffffu, inw)) continue;
+                const uint32_t off = offset[cell];
+                for (uint32_t base = 0; base < cnt; base += 32) {
+                    const uint32_t k = base + lane;
+                    const bool valid = k < cnt;
+                    const float4 qp = valid ? pos[off + k] : make_float4(INF, INF, INF, 0.f);
+                    const float ex = fmaxf(0.f, fmaxf(bx0 - qp.x, qp.x - bx1));
+                    const float ey = fmaxf(0.f, fmaxf(by0 - qp.y, qp.y - by1));
+                    const float ez = fmaxf(0.f, fmaxf(bz0 - qp.z, qp.z - bz1));
+                    const bool surv = valid && (ex == 0.f && ey == 0.f && ez == 0.f);
+                    const unsigned ball = __ballot_sync(0xffffffffu, surv);
+                    if (surv) {
+                        const uint32_t slot = (uint32_t)__popc(ball & ((1u << lane) - 1u));
+                        s_sp[w][slot] = qp;
+                        s_sq[w][slot] = off + k;
+                    }
+                    __syncwarp();
+                    const int ns = __popc(ball);
+                    if (inw) {
+                        for (int t = 0; t < ns; t++) {
+                            const float4 sp = s_sp[w][t];
+                            const float dx = ip.x - sp.x, dy = ip.y - sp.y, dz = ip.z - sp.z;
+                            const float dsq = dx * dx + dy * dy + dz * dz;
+                            if (dsq < R2 && dsq > 0.f) {
+                                if (n < (uint32_t)NL_CAP) my[n * 32] = s_sq[w][t];
+                                n++;
                             }
                         }
-                        __syncwarp();
                     }
+                    __syncwarp();
                 }
             }
         }
-        if (more) {
-            const uint32_t take = n < (uint32_t)NL_CAP ? n : (uint32_t)NL_CAP;
-            for (uint32_t k = 0; k < take; k++) {
-                const uint32_t q = my[k * 32];
-                if (DENS) {
-                    const uint32_t qc = scell[q];
-                    if (qc != curcell) {  // flush the partial sum of the previous cell
-                        sum += part;
-                        part = 0.f;
-                        curcell = qc;
-                    }
-                }
-                const float4 jp = pos[q];
-                const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
-                const float dsq = dx * dx + dy * dy + dz * dz;
-                if (dsq < 1.f && dsq > 0.f) {  // fluid-force neighbour, kept for the force pass
-                    if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
-                    nf++;
-                }
-                if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
-                if (DIFF && dsq < P.r2diff && dsq > 0.f) diffuse_add<DIFF>(nc, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2);
-            }
-            if (n > (uint32_t)NL_CAP) qmin = my[(NL_CAP - 1) * 32] + 1;
-            else more = false;
-        }
-        __syncwarp();
     }
     if (!act) return;
-    if (DENS) sum += part;
-    fcount[p] = nf;  // > FL_CAP: the force pass searches again
+    float cur[NTF], dif[NTF], scratch[NTF];
+    load_conc<FLAGS>(G, conc_in, p, cur, scratch, dif);
+    float sum = 0.f;
+    if (n <= (uint32_t)NL_CAP) {
+        float part = 0.f;
+        uint32_t curcell = UNDEF, nf = 0;
+        for (uint32_t k = 0; k < n; k++) {
+            const uint32_t q = my[k * 32];
+            if (DENS) {
+                const uint32_t qc = scell[q];
+                if (qc != curcell) {  // flush the partial sum of the previous cell
+                    sum += part;
+                    part = 0.f;
+                    curcell = qc;
+                }
+            }
+            const float4 jp = pos[q];
+            const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+            const float dsq = dx * dx + dy * dy + dz * dz;
+            if (dsq < 1.f && dsq > 0.f) {  // fluid-force neighbour, kept for the force pass
+                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
+                nf++;
+            }
+            if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
+            if (DIFF && dsq < P.r2diff && dsq > 0.f)
+                diffuse_add<DIFF>(nc, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2, P.uniform_diff != 0);
+        }
+        if (DENS) sum += part;
+        fcount[p] = nf;  // > FL_CAP: the force pass searches again
+    } else {
+        // more neighbours than the list holds (not seen at rest density): the reference walk
+#pragma unroll
+        for (int t = 0; t < NTF; t++) nc[t] = 0.f;
+        sum = dens_direct<DENS, DIFF>(P, ip, pcell, pos, conc_in, count, offset, nc, dif, cur);
+        fcount[p] = FL_CAP + 1;
+    }
     dens_epilogue<FLAGS>(P, G, p, sum, nc, cur, genes, conc_out, press, invdens);
 }
 
 template <int FLAGS>
-__global__ void __launch_bounds__(DENS_WARPS * 32) k_dens_warp(
+__global__ void __launch_bounds__(DENS_WARPS * 32, 2) k_dens_warp(
     DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
     const float* __restrict__ conc_in, float* __restrict__ conc_out,
     const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
