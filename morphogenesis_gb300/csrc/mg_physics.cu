@@ -354,7 +354,7 @@ __device__ __forceinline__ void dens_warp_item(
 }
 
 template <int FLAGS>
-__global__ void __launch_bounds__(DENS_WARPS * 32, 2) k_dens_warp(
+__global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
     DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
     const float* __restrict__ conc_in, float* __restrict__ conc_out,
     const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 2) k_dens_warp(
                           flist, fcount, p, act, s_list, s_sp, s_sq);
 }
 
-// The per-lane lists take 64 KB of dynamic shared memory next to the static survivor buffers,
+// The per-lane lists take 48 KB of dynamic shared memory next to the static survivor buffers,
 // above the 48 KB a launch gets without opting in.
 cudaError_t physics_init() {
     const int smem = DENS_WARPS * NL_CAP * 32 * (int)sizeof(uint32_t);
