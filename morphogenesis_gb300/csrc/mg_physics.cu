@@ -90,8 +90,12 @@ __device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint
                                              const uint32_t* __restrict__ count,
                                              const uint32_t* __restrict__ offset,
                                              float (&nc)[NTF], const float (&dif)[NTF],
-                                             const float (&cur)[NTF]) {
+                                             const float (&cur)[NTF],
+                                             uint32_t* __restrict__ flist = nullptr,
+                                             uint32_t* __restrict__ fcount = nullptr,
+                                             uint32_t p = 0) {
     float sum = 0.f;
+    uint32_t nf = 0;
     const uint32_t base = pcell - (uint32_t)P.nadj;
     for (int c = 0; c < P.adjcnt; c++) {
         const uint32_t cellc = base + (uint32_t)P.adj[c];
@@ -103,11 +107,16 @@ __device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint
             const float4 jp = pos[q];
             const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
             const float dsq = dx * dx + dy * dy + dz * dz;
+            if (flist && dsq < 1.f && dsq > 0.f) {
+                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
+                nf++;
+            }
             if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
             if (DIFF && dsq < P.r2diff && dsq > 0.f) diffuse_add<DIFF>(nc, dif, cur, conc, q, (P.r2diff - dsq) * P.d2, false);
         }
         if (DENS) sum += part;
     }
+    if (fcount) fcount[p] = nf;
     return sum;
 }
 
@@ -347,8 +356,8 @@ __device__ __forceinline__ void dens_warp_item(
         // more neighbours than the list holds (not seen at rest density): the reference walk
 #pragma unroll
         for (int t = 0; t < NTF; t++) nc[t] = 0.f;
-        sum = dens_direct<DENS, DIFF>(P, ip, pcell, pos, conc_in, count, offset, nc, dif, cur);
-        fcount[p] = FL_CAP + 1;
+        sum = dens_direct<DENS, DIFF>(P, ip, pcell, pos, conc_in, count, offset, nc, dif, cur,
+                                     flist, fcount, p);
     }
     dens_epilogue<FLAGS>(P, G, p, sum, nc, cur, genes, conc_out, press, invdens);
 }
@@ -371,7 +380,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
                           flist, fcount, p, act, s_list, s_sp, s_sq);
 }
 
-// The per-lane lists take 48 KB of dynamic shared memory next to the static survivor buffers,
+// The per-lane lists take 64 KB of dynamic shared memory next to the static survivor buffers,
 // above the 48 KB a launch gets without opting in.
 cudaError_t physics_init() {
     const int smem = DENS_WARPS * NL_CAP * 32 * (int)sizeof(uint32_t);
