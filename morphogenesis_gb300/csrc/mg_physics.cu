@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
                           flist, fcount, p, act, s_list, s_sp, s_sq);
 }
 
-// The per-lane lists take 64 KB of dynamic shared memory next to the static survivor buffers,
+// The per-lane lists take 48 KB of dynamic shared memory next to the static survivor buffers,
 // above the 48 KB a launch gets without opting in.
 cudaError_t physics_init() {
     const int smem = DENS_WARPS * NL_CAP * 32 * (int)sizeof(uint32_t);
