@@ -218,6 +218,49 @@ mg_status mg_run_gene_action(mg_handle h);          /* Run2GeneAction */
 mg_status mg_step(mg_handle h, uint32_t nsteps, uint32_t flags);
 mg_status mg_synchronize(mg_handle h);
 
+/* ---- learned morphogen surrogate ------------------------------------------------------------
+ * An MLP 48 -> 128 -> 128 -> 16 (GELU) maps a particle's 16 concentrations, the mean
+ * concentrations of its diffusion neighbours and its 16 gene bits to the increment of one
+ * morphogen stage (diffusion + gene reaction, computeDiffusion + computeGeneAction/tallyGene-
+ * Action in the reference).  BF16 weights and activations, FP32 accumulation; trained with
+ * Adam on (features, increment) pairs captured from plain steps.  In a step with
+ * MG_STEP_SURROGATE the plain update still runs, as judge, for every judge_stride-th particle
+ * every judge_period steps; a particle whose surrogate result is off by more than threshold
+ * (relative) is handed to the plain method for the rest of the run. */
+typedef struct mg_mlp_s* mg_mlp;
+typedef struct mg_dataset_s* mg_dataset;
+mg_status mg_mlp_create(uint64_t seed, mg_mlp* out);
+mg_status mg_mlp_destroy(mg_mlp m);
+/* Number of FP32 parameters (W1[128][48] b1 W2[128][128] b2 W3[16][128] b3, normalised
+ * network) and of normalisation values (mu_x[48] 1/sd_x[48] mu_y[16] 1/sd_y[16]). */
+mg_status mg_mlp_sizes(size_t* param_count, size_t* norm_count);
+mg_status mg_mlp_get_params(mg_mlp m, float* host, size_t count);
+mg_status mg_mlp_set_params(mg_mlp m, const float* host, size_t count);
+mg_status mg_mlp_get_norm(mg_mlp m, float* host, size_t count);
+mg_status mg_mlp_set_norm(mg_mlp m, const float* host, size_t count);
+/* Forward + backward on n given rows (raw features x[n][48], increments y[n][16]): gradients
+ * of the mean squared error of the normalised outputs, and the loss. */
+mg_status mg_mlp_gradients(mg_mlp m, const float* x, const float* y, uint32_t n, float* grads,
+                           double* loss);
+/* Increments predicted by the in-step (tensor-memory) inference kernel for raw features. */
+mg_status mg_mlp_infer(mg_mlp m, const float* x, uint32_t n, float* y);
+mg_status mg_mlp_fit_normalization(mg_mlp m, mg_dataset d);
+mg_status mg_mlp_train(mg_mlp m, mg_dataset d, uint32_t steps, uint32_t batch, float lr,
+                       uint64_t seed, float* loss_curve);
+mg_status mg_dataset_create(uint64_t capacity, mg_dataset* out);
+mg_status mg_dataset_destroy(mg_dataset d);
+/* Runs one plain step of h (flags: MG_STEP_PHYSICS or 0) and appends its particles'
+ * (features, morphogen increment) pairs. */
+mg_status mg_dataset_capture(mg_dataset d, mg_handle h, uint32_t flags);
+mg_status mg_dataset_size(mg_dataset d, uint64_t* n);
+mg_status mg_dataset_read(mg_dataset d, uint64_t first, uint32_t n, float* x, float* y);
+/* Attaches a network to a simulation (NULL detaches); the network must outlive the use. */
+mg_status mg_set_surrogate(mg_handle h, mg_mlp m, uint32_t judge_period, uint32_t judge_stride,
+                           float threshold);
+/* Particles judged, particles handed to the plain method, worst relative error seen. */
+mg_status mg_surrogate_stats(mg_handle h, uint64_t* judged, uint64_t* handed_over, float* worst,
+                             int32_t reset);
+
 /* ---- tuning ------------------------------------------------------------------------------ */
 enum mg_option {
     /* neighbour search of the density/diffusion pass: 0 = one thread walks its 27 cells

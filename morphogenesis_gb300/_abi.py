@@ -33,6 +33,15 @@ STEP_PHYSICS, STEP_GENES, STEP_REMODEL, STEP_FREEZE, STEP_SURROGATE = 1, 2, 4, 8
 STEP_DEFAULT = STEP_PHYSICS | STEP_GENES
 
 OPT_NEIGHBOR_SEARCH = 1
+MLP_IN, MLP_H, MLP_OUT = 48, 128, 16
+P_W1 = 0
+P_B1 = P_W1 + MLP_H * MLP_IN
+P_W2 = P_B1 + MLP_H
+P_B2 = P_W2 + MLP_H * MLP_H
+P_W3 = P_B2 + MLP_H
+P_B3 = P_W3 + MLP_OUT * MLP_H
+P_COUNT = P_B3 + MLP_OUT
+NORM_COUNT = 2 * MLP_IN + 2 * MLP_OUT
 
 MG_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "GRID_OVERFLOW", 4: "LIST_OVERFLOW",
@@ -107,6 +116,24 @@ SIGNATURES = [
     ("mg_synchronize", C.c_int, [H]),
     ("mg_time_steps", C.c_int, [H, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]),
     ("mg_set_option", C.c_int, [H, C.c_int32, C.c_int32]),
+    ("mg_mlp_create", C.c_int, [C.c_uint64, C.POINTER(H)]),
+    ("mg_mlp_destroy", C.c_int, [H]),
+    ("mg_mlp_sizes", C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    ("mg_mlp_get_params", C.c_int, [H, C.c_void_p, C.c_size_t]),
+    ("mg_mlp_set_params", C.c_int, [H, C.c_void_p, C.c_size_t]),
+    ("mg_mlp_get_norm", C.c_int, [H, C.c_void_p, C.c_size_t]),
+    ("mg_mlp_set_norm", C.c_int, [H, C.c_void_p, C.c_size_t]),
+    ("mg_mlp_gradients", C.c_int, [H, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_double)]),
+    ("mg_mlp_infer", C.c_int, [H, C.c_void_p, C.c_uint32, C.c_void_p]),
+    ("mg_mlp_fit_normalization", C.c_int, [H, H]),
+    ("mg_mlp_train", C.c_int, [H, H, C.c_uint32, C.c_uint32, C.c_float, C.c_uint64, C.c_void_p]),
+    ("mg_dataset_create", C.c_int, [C.c_uint64, C.POINTER(H)]),
+    ("mg_dataset_destroy", C.c_int, [H]),
+    ("mg_dataset_capture", C.c_int, [H, H, C.c_uint32]),
+    ("mg_dataset_size", C.c_int, [H, C.POINTER(C.c_uint64)]),
+    ("mg_dataset_read", C.c_int, [H, C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("mg_set_surrogate", C.c_int, [H, H, C.c_uint32, C.c_uint32, C.c_float]),
+    ("mg_surrogate_stats", C.c_int, [H, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.c_int32]),
     ("mg_profile_enable", C.c_int, [H, C.c_int32]),
     ("mg_profile_read", C.c_int, [H, C.c_int32, C.c_char_p, C.POINTER(C.c_uint32),
                                   C.POINTER(C.c_double), C.POINTER(C.c_int32)]),

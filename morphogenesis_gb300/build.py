@@ -26,6 +26,7 @@ UNITS = {
     "mg_sort.cu": ["-fmad=false"],
     "mg_physics.cu": ["-fmad=false"],
     "mg_io.cu": [],
+    "mg_mlp.cu": [],
     "mg_api.cu": [],
 }
 

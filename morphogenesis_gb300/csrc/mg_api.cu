@@ -16,6 +16,7 @@
 
 #include "../../include/mg_abi.h"
 #include "mg_internal.cuh"
+#include "mg_mlp.cuh"
 
 using namespace mg;
 
@@ -69,6 +70,24 @@ struct mg_system {
     std::vector<ProfSlot> prof;
     std::vector<ProfMark> marks;
     uint64_t launches = 0;  // kernels launched by mg_step (one graph step counts its kernels)
+    // learned morphogen surrogate (attached network is borrowed, not owned)
+    mg::Mlp* sur = nullptr;
+    __nv_bfloat16* feat = nullptr;   // [cap][48] surrogate inputs
+    float* conc_plain = nullptr;     // [cap][16] plain update of judged / handed-over particles
+    uint32_t* sur_stats = nullptr;   // [0] judged, [1] handed over, [2] worst relative error bits
+    uint32_t judge_period = 10, judge_stride = 64;
+    float judge_threshold = 1e-3f;
+};
+
+struct mg_mlp_s {
+    mg::Mlp m;
+    cudaStream_t st;
+};
+
+struct mg_dataset_s {
+    float* dx = nullptr;  // [capacity][48] raw features
+    float* dy = nullptr;  // [capacity][16] morphogen increments
+    uint64_t capacity = 0, size = 0;
 };
 
 namespace {
@@ -226,6 +245,8 @@ mg_status check_device(mg_system* h) {
         return fail(h, MG_ERR_DEVICE_TIMEOUT, "prefix-sum look-back gave up waiting (bounded spin)");
     if (err & ERR_BIG_LIST_OVERFLOW)
         return fail(h, MG_ERR_GRID_OVERFLOW, "more than 65536 grid cells hold over 256 particles");
+    if (err & mg::MLP_ERR_MBAR_TIMEOUT)
+        return fail(h, MG_ERR_DEVICE_TIMEOUT, "surrogate inference: tensor-core completion wait gave up (bounded spin)");
     if (err & ERR_EPIGEN_VALUE)
         return fail(h, MG_ERR_UNSUPPORTED,
                     "FEPIGEN values other than 0 and INT_MAX (epigenetic countdowns) are not "
@@ -309,9 +330,39 @@ void enqueue_dens(mg_system* h, int flags, bool prof) {
 }
 
 // One step in the legacy Run() order (fluid_system.cpp:1179-1349), one sort per step.
+void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof) {
+    DensExtra X{};
+    X.feat = h->feat;
+    X.conc_plain = h->conc_plain;
+    X.step = h->s.counters + 5;
+    X.judge_period = h->judge_period;
+    X.judge_stride = h->judge_stride;
+    const int cin = h->conc_cur, cout = 1 - h->conc_cur;
+    const int dflags = (density ? 1 : 0) | 2 | 4 | 8 | 32;
+    { Mark m(h, prof, density ? "density_features" : "features");
+      launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, dflags,
+                  h->search, h->num_sms, h->stream, &X); }
+    if (h->search) h->flist_valid = true;
+    { Mark m(h, prof, "mlp_infer");
+      launch_mlp_infer(h->sur, h->feat, conc_of(h, cin), h->conc_plain, conc_of(h, cout),
+                       h->set[h->cur].genes, h->s.counters + 3, 0, h->s.counters + 5, h->judge_period,
+                       h->judge_stride, h->judge_threshold, h->sur_stats, h->s.counters + 2,
+                       h->num_sms, h->stream); }
+    h->conc_cur = cout;
+}
+
 void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
     enqueue_insert_rank(h, prof);
     enqueue_gather(h, prof);
+    if (flags & MG_STEP_SURROGATE) {
+        enqueue_surrogate_morphogen(h, (flags & MG_STEP_PHYSICS) != 0, prof);
+        if (flags & MG_STEP_PHYSICS) {
+            { Mark m(h, prof, "force"); launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream); }
+            { Mark m(h, prof, "advance"); launch_advance(h->P, h->set[h->cur], h->s, true, h->stream); }
+            h->flist_valid = false;
+        }
+        return;
+    }
     int dflags = ((flags & MG_STEP_PHYSICS) ? 1 : 0) | ((flags & MG_STEP_GENES) ? 6 : 0);
     if (dflags) enqueue_dens(h, dflags, prof);
     if (flags & MG_STEP_PHYSICS) {
@@ -323,7 +374,8 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
 
 int kernels_per_step(uint32_t flags) {
     int n = 6;  // insert, scan, place, cellsort, cellsort_big, gather
-    if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES)) n += 1;
+    if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE)) n += 1;
+    if (flags & MG_STEP_SURROGATE) n += 1;
     if (flags & MG_STEP_PHYSICS) n += 2;
     return n;
 }
@@ -337,7 +389,7 @@ mg_status get_graph(mg_system* h, uint32_t flags, cudaGraphExec_t* out) {
         // advance the buffer state exactly as enqueue_step would
         h->cur = 1 - cur0;
         h->conc_cur = 1 - conc0;
-        if (flags & MG_STEP_GENES) h->conc_cur = conc0;
+        if (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)) h->conc_cur = conc0;
         return MG_OK;
     }
     DevParams saved = h->P;
@@ -358,8 +410,10 @@ mg_status get_graph(mg_system* h, uint32_t flags, cudaGraphExec_t* out) {
 }
 
 mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
-    if (flags & (MG_STEP_REMODEL | MG_STEP_SURROGATE))
-        return fail(h, MG_ERR_UNSUPPORTED, "remodelling and surrogate steps are not built");
+    if (flags & MG_STEP_REMODEL)
+        return fail(h, MG_ERR_UNSUPPORTED, "remodelling steps are not built");
+    if ((flags & MG_STEP_SURROGATE) && !h->sur)
+        return fail(h, MG_ERR_INVALID_ARG, "surrogate step without an attached network (mg_set_surrogate)");
     for (uint32_t s = 0; s < nsteps; s++) {
         if (h->profile) {
             DevParams saved = h->P;
@@ -378,7 +432,8 @@ mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
     h->phase = PHASE_SORTED;
     h->ever_sorted = true;
     h->brk_pending = false;
-    h->flist_valid = (flags & MG_STEP_PHYSICS) ? false : (h->search && (flags & MG_STEP_GENES));
+    h->flist_valid = (flags & MG_STEP_PHYSICS) ? false
+                     : (h->search && (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)));
     if (h->profile) prof_collect(h);
     return MG_OK;
 }
@@ -519,6 +574,7 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
     if (h->num_sms <= 0) h->num_sms = 1;
     e = physics_init();
+    if (e == cudaSuccess) e = mg::mlp_init_attributes();
     if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "kernel attributes"); }
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaStreamCreate"); }
@@ -602,6 +658,9 @@ mg_status mg_destroy(mg_handle h) {
     for (auto& m : h->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
     if (h->staging) cudaFree(h->staging);
     if (h->dense) cudaFree(h->dense);
+    if (h->feat) cudaFree(h->feat);
+    if (h->conc_plain) cudaFree(h->conc_plain);
+    if (h->sur_stats) cudaFree(h->sur_stats);
     if (h->arena) cudaFree(h->arena);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -1027,6 +1086,231 @@ mg_status mg_algorithmic_bytes(mg_handle h, const char* kernel, uint32_t flags,
     *bpp = p;
     *bpc = c;
     return MG_OK;
+}
+
+// ---- learned morphogen surrogate ------------------------------------------------------------
+static mg_status mlp_fail(cudaError_t e, const char* where) { return cuda_fail(nullptr, e, where); }
+
+mg_status mg_mlp_create(uint64_t seed, mg_mlp* out) {
+    if (!out) return fail(nullptr, MG_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    mg_mlp m = new mg_mlp_s();
+    cudaError_t e = cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = mg::mlp_init_attributes();
+    if (e == cudaSuccess) e = mg::mlp_alloc(&m->m, seed, m->st);
+    if (e != cudaSuccess) {
+        mg::mlp_free(&m->m);
+        if (m->st) cudaStreamDestroy(m->st);
+        delete m;
+        return mlp_fail(e, "mg_mlp_create");
+    }
+    *out = m;
+    return MG_OK;
+}
+
+mg_status mg_mlp_destroy(mg_mlp m) {
+    if (!m) return MG_OK;
+    cudaStreamSynchronize(m->st);
+    mg::mlp_free(&m->m);
+    cudaStreamDestroy(m->st);
+    delete m;
+    return MG_OK;
+}
+
+mg_status mg_mlp_sizes(size_t* param_count, size_t* norm_count) {
+    if (param_count) *param_count = mg::P_COUNT;
+    if (norm_count) *norm_count = mg::NORM_COUNT;
+    return MG_OK;
+}
+
+mg_status mg_mlp_get_params(mg_mlp m, float* host, size_t count) {
+    if (!m || !host || count != (size_t)mg::P_COUNT) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_mlp_get_params");
+    cudaError_t e = mg::mlp_get_params(&m->m, host);
+    return e == cudaSuccess ? MG_OK : mlp_fail(e, "mg_mlp_get_params");
+}
+
+mg_status mg_mlp_set_params(mg_mlp m, const float* host, size_t count) {
+    if (!m || !host || count != (size_t)mg::P_COUNT) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_mlp_set_params");
+    cudaError_t e = mg::mlp_set_params(&m->m, host);
+    if (e == cudaSuccess) e = mg::mlp_refresh_inference(&m->m);
+    return e == cudaSuccess ? MG_OK : mlp_fail(e, "mg_mlp_set_params");
+}
+
+mg_status mg_mlp_get_norm(mg_mlp m, float* host, size_t count) {
+    if (!m || !host || count != (size_t)mg::NORM_COUNT) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_mlp_get_norm");
+    cudaError_t e = mg::mlp_get_norm(&m->m, host);
+    return e == cudaSuccess ? MG_OK : mlp_fail(e, "mg_mlp_get_norm");
+}
+
+mg_status mg_mlp_set_norm(mg_mlp m, const float* host, size_t count) {
+    if (!m || !host || count != (size_t)mg::NORM_COUNT) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_mlp_set_norm");
+    cudaError_t e = mg::mlp_set_norm(&m->m, host);
+    if (e == cudaSuccess) e = mg::mlp_refresh_inference(&m->m);
+    return e == cudaSuccess ? MG_OK : mlp_fail(e, "mg_mlp_set_norm");
+}
+
+mg_status mg_mlp_gradients(mg_mlp m, const float* x, const float* y, uint32_t n, float* grads,
+                           double* loss) {
+    if (!m || !x || !y || !grads || n == 0) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_mlp_gradients");
+    float *dx = nullptr, *dy = nullptr;
+    cudaError_t e = cudaMalloc(&dx, 4ull * n * (mg::MLP_IN + mg::MLP_OUT));
+    if (e != cudaSuccess) return fail(nullptr, MG_ERR_OOM, "mg_mlp_gradients: device buffers");
+    dy = dx + (size_t)n * mg::MLP_IN;
+    e = cudaMemcpyAsync(dx, x, 4ull * n * mg::MLP_IN, cudaMemcpyHostToDevice, m->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y, 4ull * n * mg::MLP_OUT, cudaMemcpyHostToDevice, m->st);
+    if (e == cudaSuccess) e = mg::mlp_grad(&m->m, dx, dy, n, grads, loss);
+    cudaStreamSynchronize(m->st);
+    cudaFree(dx);
+    return e == cudaSuccess ? MG_OK : mlp_fail(e, "mg_mlp_gradients");
+}
+
+mg_status mg_mlp_infer(mg_mlp m, const float* x, uint32_t n, float* y) {
+    if (!m || !x || !y || n == 0) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_mlp_infer");
+    std::vector<__nv_bfloat16> xb((size_t)n * mg::MLP_IN);
+    for (size_t i = 0; i < xb.size(); i++) xb[i] = __float2bfloat16(x[i]);
+    void* mem = nullptr;
+    const size_t fb = sizeof(__nv_bfloat16) * xb.size(), cb = 4ull * n * mg::MLP_OUT;
+    cudaError_t e = cudaMalloc(&mem, fb + 2 * cb + 256);
+    if (e != cudaSuccess) return fail(nullptr, MG_ERR_OOM, "mg_mlp_infer: device buffers");
+    char* b = (char*)mem;
+    __nv_bfloat16* feat = (__nv_bfloat16*)b;
+    float* cin = (float*)(b + ((fb + 255) & ~(size_t)255));
+    float* cout = cin + (size_t)n * mg::MLP_OUT;
+    uint32_t* err = (uint32_t*)(cout + (size_t)n * mg::MLP_OUT);
+    e = cudaMemcpyAsync(feat, xb.data(), fb, cudaMemcpyHostToDevice, m->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cin, 0, cb + cb + 64, m->st);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) {
+        mg::launch_mlp_infer(&m->m, feat, cin, nullptr, cout, nullptr, nullptr, n, nullptr, 0, 0, 0.f,
+                             nullptr, err, sms, m->st);
+        e = cudaGetLastError();
+    }
+    uint32_t herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(y, cout, cb, cudaMemcpyDeviceToHost, m->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, m->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->st);
+    cudaFree(mem);
+    if (e != cudaSuccess) return mlp_fail(e, "mg_mlp_infer");
+    if (herr) return fail(nullptr, MG_ERR_DEVICE_TIMEOUT, "mg_mlp_infer: tensor-core completion wait gave up");
+    return MG_OK;
+}
+
+mg_status mg_dataset_create(uint64_t capacity, mg_dataset* out) {
+    if (!out || capacity == 0) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_dataset_create");
+    mg_dataset d = new mg_dataset_s();
+    cudaError_t e = cudaMalloc(&d->dx, 4ull * capacity * (mg::MLP_IN + mg::MLP_OUT));
+    if (e != cudaSuccess) {
+        delete d;
+        return fail(nullptr, MG_ERR_OOM, "mg_dataset_create: device buffers");
+    }
+    d->dy = d->dx + capacity * mg::MLP_IN;
+    d->capacity = capacity;
+    *out = d;
+    return MG_OK;
+}
+
+mg_status mg_dataset_destroy(mg_dataset d) {
+    if (!d) return MG_OK;
+    cudaDeviceSynchronize();
+    cudaFree(d->dx);
+    delete d;
+    return MG_OK;
+}
+
+mg_status mg_dataset_size(mg_dataset d, uint64_t* n) {
+    if (!d || !n) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_dataset_size");
+    *n = d->size;
+    return MG_OK;
+}
+
+mg_status mg_dataset_read(mg_dataset d, uint64_t first, uint32_t n, float* x, float* y) {
+    if (!d || first + n > d->size) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_dataset_read: range");
+    cudaError_t e = cudaSuccess;
+    if (x) e = cudaMemcpy(x, d->dx + first * mg::MLP_IN, 4ull * n * mg::MLP_IN, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && y) e = cudaMemcpy(y, d->dy + first * mg::MLP_OUT, 4ull * n * mg::MLP_OUT, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? MG_OK : mlp_fail(e, "mg_dataset_read");
+}
+
+mg_status mg_dataset_capture(mg_dataset d, mg_handle h, uint32_t flags) {
+    if (!d || !h) return fail(h, MG_ERR_INVALID_ARG, "mg_dataset_capture: NULL argument");
+    if (d->size + h->cap > d->capacity) return fail(h, MG_ERR_LIST_OVERFLOW, "mg_dataset_capture: dataset full");
+    enqueue_insert_rank(h, false);
+    enqueue_gather(h, false);
+    DensExtra X{};
+    X.cap_x = d->dx + d->size * mg::MLP_IN;
+    X.cap_y = d->dy + d->size * mg::MLP_OUT;
+    const int cin = h->conc_cur, cout = 1 - h->conc_cur;
+    launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, 1 | 2 | 4 | 16,
+                h->search, h->num_sms, h->stream, &X);
+    h->conc_cur = cout;
+    h->flist_valid = h->search != 0;
+    if (flags & MG_STEP_PHYSICS) {
+        launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream);
+        launch_advance(h->P, h->set[h->cur], h->s, true, h->stream);
+        h->flist_valid = false;
+        h->time = h->time + h->P.dt;
+    }
+    h->phase = PHASE_SORTED;
+    h->ever_sorted = true;
+    h->brk_pending = false;
+    mg_status st = check_device(h);
+    if (st != MG_OK) return st;
+    uint32_t n = read_word(h, h->s.counters + 3, &st);
+    if (st != MG_OK) return st;
+    d->size += n;
+    return MG_OK;
+}
+
+mg_status mg_mlp_fit_normalization(mg_mlp m, mg_dataset d) {
+    if (!m || !d || d->size == 0) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_mlp_fit_normalization");
+    cudaError_t e = mg::mlp_fit_norm(&m->m, d->dx, d->dy, d->size);
+    if (e == cudaSuccess) e = mg::mlp_refresh_inference(&m->m);
+    return e == cudaSuccess ? MG_OK : mlp_fail(e, "mg_mlp_fit_normalization");
+}
+
+mg_status mg_mlp_train(mg_mlp m, mg_dataset d, uint32_t steps, uint32_t batch, float lr,
+                       uint64_t seed, float* loss_curve) {
+    if (!m || !d || d->size == 0 || batch == 0) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_mlp_train");
+    cudaError_t e = mg::mlp_train(&m->m, d->dx, d->dy, d->size, steps, batch, lr, seed, loss_curve);
+    return e == cudaSuccess ? MG_OK : mlp_fail(e, "mg_mlp_train");
+}
+
+mg_status mg_set_surrogate(mg_handle h, mg_mlp m, uint32_t judge_period, uint32_t judge_stride,
+                           float threshold) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    clear_graphs(h);
+    if (!m) {
+        h->sur = nullptr;
+        return MG_OK;
+    }
+    if (!h->feat) {
+        cudaError_t e = cudaMalloc(&h->feat, sizeof(__nv_bfloat16) * (size_t)h->cap * mg::MLP_IN);
+        if (e == cudaSuccess) e = cudaMalloc(&h->conc_plain, 4ull * h->cap * NTF);
+        if (e == cudaSuccess) e = cudaMalloc(&h->sur_stats, 16);
+        if (e != cudaSuccess) return fail(h, MG_ERR_OOM, "surrogate buffers");
+    }
+    MG_CUDA(h, cudaMemsetAsync(h->sur_stats, 0, 16, h->stream));
+    cudaStreamSynchronize(m->st);
+    h->sur = &m->m;
+    h->judge_period = judge_period;
+    h->judge_stride = judge_stride;
+    h->judge_threshold = threshold;
+    return check_device(h);
+}
+
+mg_status mg_surrogate_stats(mg_handle h, uint64_t* judged, uint64_t* handed_over, float* worst,
+                             int32_t reset) {
+    if (!h || !h->sur_stats) return fail(h, MG_ERR_INVALID_ARG, "no surrogate attached");
+    uint32_t v[4] = {0, 0, 0, 0};
+    MG_CUDA(h, cudaMemcpyAsync(v, h->sur_stats, 16, cudaMemcpyDeviceToHost, h->stream));
+    MG_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (judged) *judged = v[0];
+    if (handed_over) *handed_over = v[1];
+    if (worst) std::memcpy(worst, &v[2], 4);
+    if (reset) MG_CUDA(h, cudaMemsetAsync(h->sur_stats, 0, 16, h->stream));
+    return check_device(h);
 }
 
 // Number of kernels launched by mg_step since the handle was created.

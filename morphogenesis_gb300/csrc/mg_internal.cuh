@@ -10,7 +10,8 @@
 //                   partner's record while the owner writes only B.z/B.w.
 //   pidx            uint32[N][12]        FPARTICLEIDX, the reference layout
 //   conc            float[N][16]         FCONC, the reference device layout
-//   genes           uint32[N]            bit g set <=> FEPIGEN[g][p] != 0
+//   genes           uint32[N]            bit g set <=> FEPIGEN[g][p] != 0; bit 31: the particle's
+//                                        morphogen update was handed to the plain method
 //   origin          uint32[N]            slot of this particle in the cold arrays
 // Cold arrays (indexed by origin, never permuted): FAGE, FCOLOR, FPARTICLE_ID, FMASS_RADIUS,
 // FNERVEIDX and FELASTIDX word 8.
@@ -18,6 +19,7 @@
 // force float4[N], brk uint32[N], count/offset uint32[cells].
 #pragma once
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace mg {
@@ -36,6 +38,7 @@ constexpr uint32_t BIG_LIST_CAP = 1u << 16;
 constexpr uint32_t SPIN_LIMIT = 1u << 22; // bounded look-back polls
 constexpr int NL_CAP = 48;  // per-lane neighbour list of the warp-cooperative density pass
 constexpr int FL_CAP = 32;  // fluid-force neighbours (dsq < 1) recorded per particle
+constexpr int MLP_FEATURES = 48;  // surrogate inputs: conc[16], neighbour-mean conc[16], gene bits[16]
 
 // Error bits in the device error word.
 enum : uint32_t {
@@ -110,7 +113,7 @@ struct Scratch {
     uint32_t* offset;   // [cells]
     unsigned long long* scan_status;  // [tiles]
     uint32_t* counters; // [0] scan tile ticket, [1] big-cell list length, [2] error word,
-                        // [3] nactive
+                        // [3] nactive, [5] step counter (incremented by insert)
     uint32_t* big_list; // [BIG_LIST_CAP] cells that need the block-level ordering
 };
 
@@ -125,10 +128,21 @@ void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, cudaStre
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st);
 // flags: 1 density/pressure, 2 diffusion, 4 gene reaction
-// search: 0 direct walk, 1 warp-cooperative over consecutive particles
+// flags: 1 density, 2 diffusion, 4 gene reaction, 8 surrogate features, 16 capture of
+// training pairs, 32 judge (plain update of sampled / handed-over particles into conc_plain).
+// search: 0 direct walk, 1 warp-cooperative.
+// Optional outputs of the density pass besides pressure/density/concentrations.
+struct DensExtra {
+    __nv_bfloat16* feat;       // FEATURES: surrogate inputs [cap][48] bf16
+    float* cap_x;              // CAPTURE: dataset features [..][48] for particle 0 of this pass
+    float* cap_y;              // CAPTURE: dataset targets (morphogen increment) [..][16]
+    float* conc_plain;         // JUDGE: plain update of judged / handed-over particles
+    const uint32_t* step;      // JUDGE: device step counter
+    uint32_t judge_period, judge_stride;
+};
 void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
-                 cudaStream_t st);
+                 cudaStream_t st, const DensExtra* extra = nullptr);
 
 void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool use_list,
                   cudaStream_t st);

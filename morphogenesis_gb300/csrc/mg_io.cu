@@ -179,7 +179,7 @@ __global__ void k_gene_cell_counts(uint32_t cap, uint32_t cells, const uint32_t*
                                    uint32_t* __restrict__ gcount) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= *nactive_p || p >= cap) return;
-    uint32_t bits = genes[p], c = scell[p];
+    uint32_t bits = genes[p] & 0xFFFFu, c = scell[p];
     while (bits) {
         int g = __ffs(bits) - 1;
         bits &= bits - 1;
@@ -197,7 +197,7 @@ __global__ void k_gene_lists(uint32_t cap, uint32_t cells, const uint32_t* __res
                              uint32_t* __restrict__ lists) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= *nactive_p || p >= cap) return;
-    uint32_t bits = genes[p];
+    uint32_t bits = genes[p] & 0xFFFFu;
     if (!bits) return;
     uint32_t c = scell[p], start = offset[c];
     uint32_t before[NG];

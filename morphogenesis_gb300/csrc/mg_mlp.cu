@@ -1,0 +1,866 @@
+// mg_mlp.cu - training and inference kernels of the learned reaction surrogate (row a12).
+//
+// Training: BF16 tensor-core GEMMs (mma.sync.m16n8k16, FP32 accumulate) for the forward and
+// backward products, elementwise bias/GELU/loss kernels and Adam on FP32 master weights.
+// Inference (inside the simulation step): one persistent kernel per SM that runs the three
+// layers on 5th-generation tensor cores -- tcgen05.mma with operands in shared memory
+// (K-major core-matrix layout, no swizzle) and FP32 accumulators in tensor memory, read back
+// with tcgen05.ld for the bias + GELU epilogue.  Every wait on the MMA-completion mbarrier is
+// bounded; on timeout the kernel records MLP_ERR_MBAR_TIMEOUT, frees its tensor memory and
+// returns.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "mg_internal.cuh"
+#include "mg_mlp.cuh"
+
+namespace mg {
+
+using bf16 = __nv_bfloat16;
+
+// =============================================================================================
+// Training GEMM: C (+)= A * B with mma.sync.m16n8k16 (bf16 in, fp32 accumulate)
+// =============================================================================================
+constexpr int GBM = 64, GBN = 64, GBK = 32, GPAD = 8;
+
+__device__ __forceinline__ uint32_t ld_pair(const bf16* p) {
+    return *reinterpret_cast<const uint32_t*>(p);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], const uint32_t (&a)[4],
+                                               const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf16* __restrict__ A,
+                                                   long sam, long sak, const bf16* __restrict__ B,
+                                                   long sbk, long sbn, float* __restrict__ C,
+                                                   long ldc, int split) {
+    __shared__ __align__(16) bf16 As[GBM][GBK + GPAD];
+    __shared__ __align__(16) bf16 Bs[GBN][GBK + GPAD];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    const int per = ((K + split - 1) / split + GBK - 1) / GBK * GBK;
+    const int kb = blockIdx.z * per, ke = min(K, kb + per);
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int r = 0; r < 4; r++) acc[i][j][r] = 0.f;
+    const bf16 zero = __float2bfloat16(0.f);
+    for (int k0 = kb; k0 < ke; k0 += GBK) {
+        for (int e = tid; e < GBM * GBK; e += 128) {
+            const int mm = e / GBK, kk = e % GBK, gm = m0 + mm, gk = k0 + kk;
+            As[mm][kk] = (gm < M && gk < ke) ? A[(long)gm * sam + (long)gk * sak] : zero;
+        }
+        for (int e = tid; e < GBN * GBK; e += 128) {
+            const int nn = e / GBK, kk = e % GBK, gn = n0 + nn, gk = k0 + kk;
+            Bs[nn][kk] = (gn < N && gk < ke) ? B[(long)gk * sbk + (long)gn * sbn] : zero;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GBK; kk += 16) {
+            uint32_t a[2][4], b[4][2];
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++) {
+                const int r = wm + mt * 16 + g;
+                a[mt][0] = ld_pair(&As[r][kk + 2 * t]);
+                a[mt][1] = ld_pair(&As[r + 8][kk + 2 * t]);
+                a[mt][2] = ld_pair(&As[r][kk + 2 * t + 8]);
+                a[mt][3] = ld_pair(&As[r + 8][kk + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {
+                const int c = wn + nt * 8 + g;
+                b[nt][0] = ld_pair(&Bs[c][kk + 2 * t]);
+                b[nt][1] = ld_pair(&Bs[c][kk + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int nt = 0; nt < 4; nt++) mma_bf16_16816(acc[mt][nt], a[mt], b[nt]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++) {
+            const int r = m0 + wm + mt * 16 + g, c = n0 + wn + nt * 8 + 2 * t;
+            const float v[4] = {acc[mt][nt][0], acc[mt][nt][1], acc[mt][nt][2], acc[mt][nt][3]};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int rr = r + (q >= 2 ? 8 : 0), cc = c + (q & 1);
+                if (rr < M && cc < N) {
+                    if (split > 1) atomicAdd(&C[(long)rr * ldc + cc], v[q]);
+                    else C[(long)rr * ldc + cc] = v[q];
+                }
+            }
+        }
+}
+
+void launch_gemm_bf16(int M, int N, int K, const bf16* A, long sam, long sak, const bf16* B,
+                      long sbk, long sbn, float* C, long ldc, int split, cudaStream_t st) {
+    dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM, split);
+    k_gemm_bf16<<<grid, 128, 0, st>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, split);
+}
+
+// =============================================================================================
+// Training elementwise kernels
+// =============================================================================================
+// Batch assembly: rows drawn uniformly (with replacement) from the dataset by a counter-based
+// hash of (seed, step, row); features and targets normalised; features rounded to bf16.
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27; x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+
+__global__ void k_make_batch(const float* __restrict__ dx, const float* __restrict__ dy,
+                             uint64_t nrows, uint32_t B, uint64_t seed, const float* __restrict__ norm,
+                             bf16* __restrict__ X, float* __restrict__ Y, int sequential) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const uint64_t row = sequential ? (uint64_t)b % nrows
+                                    : mix64(seed ^ (0x9e3779b97f4a7c15ull * (b + 1))) % nrows;
+    const float* mx = norm, *sx = norm + MLP_IN, *my = norm + 2 * MLP_IN, *sy = my + MLP_OUT;
+    for (int i = 0; i < MLP_IN; i++)
+        X[(size_t)b * MLP_IN + i] = __float2bfloat16((dx[row * MLP_IN + i] - mx[i]) * sx[i]);
+    for (int o = 0; o < MLP_OUT; o++)
+        Y[(size_t)b * MLP_OUT + o] = (dy[row * MLP_OUT + o] - my[o]) * sy[o];
+}
+
+// Z += bias; optionally H = bf16(gelu(Z)).
+__global__ void k_bias_act(float* __restrict__ Z, const float* __restrict__ bias, int O, size_t n,
+                           bf16* __restrict__ H) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const float z = Z[e] + bias[e % O];
+    Z[e] = z;
+    if (H) H[e] = __float2bfloat16(gelu(z));
+}
+
+// d(mean squared error)/dY and the loss sum.
+__global__ void k_out_grad(const float* __restrict__ Yp, const float* __restrict__ Y, size_t n,
+                           float scale, bf16* __restrict__ dY16, float* __restrict__ dY32,
+                           double* __restrict__ loss) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if (e < n) {
+        const float d = Yp[e] - Y[e];
+        const float gr = 2.f * d * scale;
+        dY16[e] = __float2bfloat16(gr);
+        dY32[e] = gr;
+        l = d * d;
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) l += __shfl_xor_sync(0xffffffffu, l, s);
+    if ((threadIdx.x & 31) == 0 && l != 0.f) atomicAdd(loss, (double)l);
+}
+
+// dZ = dH * gelu'(Z) (fp32 and bf16 copies).
+__global__ void k_act_grad(const float* __restrict__ dH, const float* __restrict__ Z, size_t n,
+                           bf16* __restrict__ dZ16, float* __restrict__ dZ32) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const float v = dH[e] * gelu_grad(Z[e]);
+    dZ16[e] = __float2bfloat16(v);
+    dZ32[e] = v;
+}
+
+// db[o] += sum_b dZ[b][o]
+__global__ void k_colsum(const float* __restrict__ dZ, int rows, int O, float* __restrict__ db) {
+    const int o = blockIdx.x;
+    float s = 0.f;
+    for (int r = threadIdx.x; r < rows; r += blockDim.x) s += dZ[(size_t)r * O + o];
+    __shared__ float red[256];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[o] = red[0];
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ gr, float* __restrict__ m,
+                       float* __restrict__ v, int n, float lr, float b1, float b2, float eps,
+                       float c1, float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float g = gr[i];
+    const float mi = b1 * m[i] + (1.f - b1) * g;
+    const float vi = b2 * v[i] + (1.f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+__global__ void k_to_bf16(const float* __restrict__ src, bf16* __restrict__ dst, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = __float2bfloat16(src[i]);
+}
+
+// Column statistics of the dataset for the normalisation: sums and sums of squares.
+__global__ void k_col_stats(const float* __restrict__ d, uint64_t rows, int cols,
+                            double* __restrict__ acc) {
+    const int c = blockIdx.y;
+    double s = 0.0, s2 = 0.0;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += (uint64_t)gridDim.x * blockDim.x) {
+        const double x = d[r * cols + c];
+        s += x;
+        s2 += x * x;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&acc[2 * c], s);
+        atomicAdd(&acc[2 * c + 1], s2);
+    }
+}
+
+// =============================================================================================
+// Inference on tcgen05
+// =============================================================================================
+constexpr int INF_THREADS = 128;  // four warps: warp w owns TMEM lanes 32w..32w+31 (tile rows)
+constexpr int INF_TMEM_COLS = 256;
+constexpr uint32_t MBAR_SPIN_LIMIT = 1u << 24;
+
+// Shared memory image of one inference CTA.
+struct InferSmem {
+    bf16 w1[MLP_H * MLP_IN];    // 12 KB  B operand layer 1 (N=128 x K=48)
+    bf16 w2[MLP_H * MLP_H];     // 32 KB  B operand layer 2 (N=128 x K=128)
+    bf16 w3[MLP_OUT * MLP_H];   //  4 KB  B operand layer 3 (N=16 x K=128)
+    bf16 a1[128 * MLP_IN];      // 12 KB  A operand layer 1 (M=128 x K=48)
+    bf16 a2[128 * MLP_H];       // 32 KB  A operand layers 2 and 3 (M=128 x K=128)
+    float b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
+    unsigned long long mbar;
+    uint32_t tmem_base;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading-dimension byte offset
+// (K direction: next core matrix along K), stride-dimension byte offset (M/N direction: next
+// group of 8 rows), version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;  // descriptor version for tcgen05
+    return d;                 // base offset 0, relative LBO, swizzle mode 0 (none)
+}
+
+// Instruction descriptor of kind::f16: D = F32, A = B = BF16, both K-major, dense.
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t M, uint32_t N) {
+    return (1u << 4)            // D format F32
+           | (1u << 7)          // A format BF16
+           | (1u << 10)         // B format BF16
+           | ((N >> 3) << 17)   // N / 8
+           | ((M >> 4) << 24);  // M / 16
+}
+
+__device__ __forceinline__ void mma_f16_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                           uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar_saddr) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                     mbar_saddr)
+                 : "memory");
+}
+
+// Bounded parity wait; returns false when the wait gave up.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar_saddr, uint32_t parity) {
+    for (uint32_t it = 0; it < MBAR_SPIN_LIMIT; it++) {
+        uint32_t done = 0;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar_saddr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// 32 consecutive fp32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+}
+
+// Writes 8 consecutive bf16 of row r, columns k..k+7, into a rows x K core-matrix tile.
+__device__ __forceinline__ void put8(bf16* tile, uint32_t r, uint32_t k, uint32_t K,
+                                     const float (&v)[8]) {
+    __nv_bfloat162 h[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+    *reinterpret_cast<uint4*>(tile + core_offset(r, k, K)) = *reinterpret_cast<uint4*>(h);
+}
+
+// Issues one layer: D[128 x N] = A[128 x K] * B[N x K]^T, K/16 MMAs (single thread).
+__device__ __forceinline__ void issue_layer(uint32_t d_tmem, const bf16* a, const bf16* b, uint32_t K,
+                                            uint32_t N) {
+    const uint32_t sa = smem_u32(a), sb = smem_u32(b);
+    const uint32_t sbo = (K >> 3) * 128u;  // next group of 8 rows
+    const uint32_t idesc = idesc_bf16(128, N);
+    for (uint32_t s = 0; s < K / 16; s++) {
+        const uint64_t ad = smem_desc(sa + s * 256u, 128u, sbo);
+        const uint64_t bd = smem_desc(sb + s * 256u, 128u, sbo);
+        mma_f16_ss(d_tmem, ad, bd, idesc, s > 0 ? 1u : 0u);
+    }
+}
+
+// Surrogate step: for each particle p < nactive, conc_out[p] = conc_in[p] + MLP(features[p]).
+// Particles under judgement (sampled this step) or already handed to the plain method
+// (bit 31 of their gene word) compare against / take the plain update in conc_plain.
+__global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
+    InferWeights W, const bf16* __restrict__ feat, const float* __restrict__ conc_in,
+    const float* __restrict__ conc_plain, float* __restrict__ conc_out, uint32_t* __restrict__ genes,
+    const uint32_t* __restrict__ nactive_p, uint32_t ntotal_override, const uint32_t* __restrict__ step_p,
+    uint32_t judge_period, uint32_t judge_stride, float threshold, uint32_t* __restrict__ stats,
+    uint32_t* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t n = nactive_p ? *nactive_p : ntotal_override;
+    const uint32_t step = step_p ? *step_p : 0u;
+    const bool judge_step = judge_period && judge_stride && (step % judge_period) == 0;
+    const uint32_t judge_phase = judge_step ? (step / judge_period) % judge_stride : 0u;
+
+    // weights and biases into shared memory (already in the core-matrix layout)
+    {
+        const uint4* s1 = reinterpret_cast<const uint4*>(W.w1);
+        uint4* d1 = reinterpret_cast<uint4*>(S.w1);
+        for (uint32_t i = tid; i < MLP_H * MLP_IN / 8; i += INF_THREADS) d1[i] = s1[i];
+        const uint4* s2 = reinterpret_cast<const uint4*>(W.w2);
+        uint4* d2 = reinterpret_cast<uint4*>(S.w2);
+        for (uint32_t i = tid; i < MLP_H * MLP_H / 8; i += INF_THREADS) d2[i] = s2[i];
+        const uint4* s3 = reinterpret_cast<const uint4*>(W.w3);
+        uint4* d3 = reinterpret_cast<uint4*>(S.w3);
+        for (uint32_t i = tid; i < MLP_OUT * MLP_H / 8; i += INF_THREADS) d3[i] = s3[i];
+        for (uint32_t i = tid; i < MLP_H; i += INF_THREADS) {
+            S.b1[i] = W.b1[i];
+            S.b2[i] = W.b2[i];
+        }
+        if (tid < MLP_OUT) S.b3[tid] = W.b3[tid];
+    }
+    const uint32_t mbar = smem_u32(&S.mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {  // one warp allocates the tensor memory of the CTA
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         smem_u32(&S.tmem_base)),
+                     "r"((uint32_t)INF_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+    const uint32_t lane_addr = tmem + ((warp * 32u) << 16);  // this warp's TMEM lanes
+    uint32_t phase = 0;
+    bool ok = true;
+
+    const uint32_t ntiles = (n + 127) / 128;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t row = tid;  // tile row = this thread's particle
+        const uint32_t p = tile * 128u + row;
+        const bool live = p < n;
+        // layer-1 operand: the particle's 48 bf16 features (zeros past the end)
+        {
+            const uint4* src = reinterpret_cast<const uint4*>(feat + (size_t)p * MLP_IN);
+#pragma unroll
+            for (uint32_t c = 0; c < MLP_IN / 8; c++) {
+                const uint4 v = live ? src[c] : make_uint4(0u, 0u, 0u, 0u);
+                *reinterpret_cast<uint4*>(S.a1 + core_offset(row, c * 8, MLP_IN)) = v;
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            issue_layer(tmem + 0, S.a1, S.w1, MLP_IN, MLP_H);
+            mma_commit(mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        phase ^= 1u;
+        if (!ok) break;
+        tc_fence_after();
+        // layer-1 epilogue: bias + GELU -> layer-2 operand
+#pragma unroll
+        for (uint32_t c0 = 0; c0 < MLP_H; c0 += 32) {
+            float v[32];
+            tmem_ld32(lane_addr + c0, v);
+#pragma unroll
+            for (int q = 0; q < 32; q += 8) {
+                float h[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) h[i] = gelu(v[q + i] + S.b1[c0 + q + i]);
+                put8(S.a2, row, c0 + q, MLP_H, h);
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            issue_layer(tmem + 128, S.a2, S.w2, MLP_H, MLP_H);
+            mma_commit(mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        phase ^= 1u;
+        if (!ok) break;
+        tc_fence_after();
+        // layer-2 epilogue -> layer-3 operand.  The barrier fired, so the layer-2 MMAs have
+        // finished reading a2 and it can be overwritten.
+#pragma unroll
+        for (uint32_t c0 = 0; c0 < MLP_H; c0 += 32) {
+            float v[32];
+            tmem_ld32(lane_addr + 128 + c0, v);
+#pragma unroll
+            for (int q = 0; q < 32; q += 8) {
+                float h[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) h[i] = gelu(v[q + i] + S.b2[c0 + q + i]);
+                put8(S.a2, row, c0 + q, MLP_H, h);
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            issue_layer(tmem + 0, S.a2, S.w3, MLP_H, MLP_OUT);
+            mma_commit(mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        phase ^= 1u;
+        if (!ok) break;
+        tc_fence_after();
+        {
+            float d[16];
+            tmem_ld16(lane_addr + 0, d);
+            if (live) {
+                const float4* ci = reinterpret_cast<const float4*>(conc_in + (size_t)p * NTF);
+                float c[16];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const float4 x = ci[k];
+                    c[4 * k] = x.x + (d[4 * k] + S.b3[4 * k]);
+                    c[4 * k + 1] = x.y + (d[4 * k + 1] + S.b3[4 * k + 1]);
+                    c[4 * k + 2] = x.z + (d[4 * k + 2] + S.b3[4 * k + 2]);
+                    c[4 * k + 3] = x.w + (d[4 * k + 3] + S.b3[4 * k + 3]);
+                }
+                if (genes) {
+                    const uint32_t gw = genes[p];
+                    const bool judged = judge_step && (p % judge_stride) == judge_phase;
+                    const bool fallback = (gw >> 31) & 1u;
+                    if (judged || fallback) {
+                        const float4* cp = reinterpret_cast<const float4*>(conc_plain + (size_t)p * NTF);
+                        float pl[16];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const float4 x = cp[k];
+                            pl[4 * k] = x.x; pl[4 * k + 1] = x.y; pl[4 * k + 2] = x.z; pl[4 * k + 3] = x.w;
+                        }
+                        bool take = fallback;
+                        if (judged && !fallback) {
+                            float worst = 0.f;
+#pragma unroll
+                            for (int t = 0; t < 16; t++) {
+                                const float e = fabsf(c[t] - pl[t]) / fmaxf(fabsf(pl[t]), 1e-6f);
+                                worst = fmaxf(worst, e);
+                            }
+                            atomicAdd(&stats[0], 1u);
+                            atomicMax(&stats[2], __float_as_uint(worst));
+                            if (!(worst <= threshold)) {  // hand the particle to the plain method
+                                genes[p] = gw | 0x80000000u;
+                                atomicAdd(&stats[1], 1u);
+                                take = true;
+                            }
+                        }
+                        if (take) {
+#pragma unroll
+                            for (int t = 0; t < 16; t++) c[t] = pl[t];
+                        }
+                    }
+                }
+                float4* co = reinterpret_cast<float4*>(conc_out + (size_t)p * NTF);
+#pragma unroll
+                for (int k = 0; k < 4; k++) co[k] = make_float4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
+    if (!ok) {
+        // a wait gave up: record it and give the MMAs in flight one more bounded wait before
+        // the tensor memory is released
+        if (tid == 0) {
+            atomicOr(err, MLP_ERR_MBAR_TIMEOUT);
+            mbar_wait(mbar, phase ^ 1u);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                     "r"((uint32_t)INF_TMEM_COLS)
+                     : "memory");
+}
+
+}  // namespace mg
+
+// =============================================================================================
+// Host side: parameters, training loop, normalisation, inference weights
+// =============================================================================================
+namespace mg {
+
+namespace {
+
+uint64_t splitmix(uint64_t& s) {
+    uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+inline uint32_t blocks(size_t n, int t = 256) { return (uint32_t)((n + t - 1) / t); }
+
+#define MLP_TRY(x)                             \
+    do {                                       \
+        cudaError_t e_ = (x);                  \
+        if (e_ != cudaSuccess) return e_;      \
+    } while (0)
+
+}  // namespace
+
+cudaError_t mlp_init_attributes() {
+    return cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(InferSmem));
+}
+
+cudaError_t mlp_alloc(Mlp* m, uint64_t seed, cudaStream_t st) {
+    std::memset(m, 0, sizeof(*m));
+    m->st = st;
+    MLP_TRY(cudaMalloc(&m->params, 4ull * P_COUNT * 4));
+    m->grads = m->params + P_COUNT;
+    m->adam_m = m->grads + P_COUNT;
+    m->adam_v = m->adam_m + P_COUNT;
+    MLP_TRY(cudaMalloc(&m->wb, sizeof(bf16) * P_COUNT));
+    MLP_TRY(cudaMalloc(&m->norm, sizeof(float) * NORM_COUNT));
+    const size_t inf_bytes = sizeof(bf16) * (MLP_H * MLP_IN + MLP_H * MLP_H + MLP_OUT * MLP_H) +
+                             sizeof(float) * (2 * MLP_H + MLP_OUT);
+    MLP_TRY(cudaMalloc(&m->inf_mem, inf_bytes));
+    char* b = (char*)m->inf_mem;
+    m->inf.w1 = (bf16*)b; b += sizeof(bf16) * MLP_H * MLP_IN;
+    m->inf.w2 = (bf16*)b; b += sizeof(bf16) * MLP_H * MLP_H;
+    m->inf.w3 = (bf16*)b; b += sizeof(bf16) * MLP_OUT * MLP_H;
+    m->inf.b1 = (float*)b; b += sizeof(float) * MLP_H;
+    m->inf.b2 = (float*)b; b += sizeof(float) * MLP_H;
+    m->inf.b3 = (float*)b;
+    // uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases
+    std::vector<float> p(P_COUNT, 0.f);
+    uint64_t s = seed * 0x632be59bd9b4e019ull + 12345;
+    auto fill = [&](int off, int rows, int cols, float gain) {
+        const float a = gain / std::sqrt((float)cols);
+        for (int i = 0; i < rows * cols; i++) {
+            const double u = (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0);
+            p[off + i] = (float)((2.0 * u - 1.0) * a);
+        }
+    };
+    fill(P_W1, MLP_H, MLP_IN, 1.f);
+    fill(P_W2, MLP_H, MLP_H, 1.f);
+    fill(P_W3, MLP_OUT, MLP_H, 0.1f);
+    std::vector<float> nrm(NORM_COUNT, 0.f);
+    for (int i = 0; i < MLP_IN; i++) nrm[MLP_IN + i] = 1.f;            // isd_x
+    for (int o = 0; o < MLP_OUT; o++) nrm[2 * MLP_IN + MLP_OUT + o] = 1.f;  // isd_y
+    MLP_TRY(mlp_set_params(m, p.data()));
+    MLP_TRY(cudaMemcpyAsync(m->norm, nrm.data(), sizeof(float) * NORM_COUNT, cudaMemcpyHostToDevice, st));
+    MLP_TRY(cudaMemsetAsync(m->adam_m, 0, 2ull * P_COUNT * 4, st));
+    m->adam_t = 0;
+    return mlp_refresh_inference(m);
+}
+
+void mlp_free(Mlp* m) {
+    cudaFree(m->params);
+    cudaFree(m->wb);
+    cudaFree(m->norm);
+    cudaFree(m->inf_mem);
+    cudaFree(m->ws);
+    std::memset(m, 0, sizeof(*m));
+}
+
+cudaError_t mlp_set_params(Mlp* m, const float* host) {
+    MLP_TRY(cudaMemcpyAsync(m->params, host, 4ull * P_COUNT, cudaMemcpyHostToDevice, m->st));
+    k_to_bf16<<<blocks(P_COUNT), 256, 0, m->st>>>(m->params, m->wb, P_COUNT);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_get_params(Mlp* m, float* host) {
+    MLP_TRY(cudaMemcpyAsync(host, m->params, 4ull * P_COUNT, cudaMemcpyDeviceToHost, m->st));
+    return cudaStreamSynchronize(m->st);
+}
+
+cudaError_t mlp_set_norm(Mlp* m, const float* host) {
+    MLP_TRY(cudaMemcpyAsync(m->norm, host, sizeof(float) * NORM_COUNT, cudaMemcpyHostToDevice, m->st));
+    return cudaStreamSynchronize(m->st);
+}
+
+cudaError_t mlp_get_norm(Mlp* m, float* host) {
+    MLP_TRY(cudaMemcpyAsync(host, m->norm, sizeof(float) * NORM_COUNT, cudaMemcpyDeviceToHost, m->st));
+    return cudaStreamSynchronize(m->st);
+}
+
+// Inference weights: input normalisation folded into layer 1, output scaling into layer 3,
+// matrices re-laid out as tcgen05 K-major core matrices.
+cudaError_t mlp_refresh_inference(Mlp* m) {
+    std::vector<float> p(P_COUNT), nrm(NORM_COUNT);
+    MLP_TRY(mlp_get_params(m, p.data()));
+    MLP_TRY(mlp_get_norm(m, nrm.data()));
+    const float* mx = nrm.data();
+    const float* sx = mx + MLP_IN;
+    const float* my = sx + MLP_IN;
+    const float* sy = my + MLP_OUT;
+    std::vector<bf16> w1(MLP_H * MLP_IN), w2(MLP_H * MLP_H), w3(MLP_OUT * MLP_H);
+    std::vector<float> b1(MLP_H), b2(MLP_H), b3(MLP_OUT);
+    for (int o = 0; o < MLP_H; o++) {
+        double bias = p[P_B1 + o];
+        for (int i = 0; i < MLP_IN; i++) {
+            const float w = p[P_W1 + o * MLP_IN + i] * sx[i];
+            w1[core_offset(o, i, MLP_IN)] = __float2bfloat16(w);
+            bias -= (double)w * mx[i];
+        }
+        b1[o] = (float)bias;
+        b2[o] = p[P_B2 + o];
+        for (int j = 0; j < MLP_H; j++) w2[core_offset(o, j, MLP_H)] = __float2bfloat16(p[P_W2 + o * MLP_H + j]);
+    }
+    for (int o = 0; o < MLP_OUT; o++) {
+        const float inv = 1.f / sy[o];
+        for (int j = 0; j < MLP_H; j++)
+            w3[core_offset(o, j, MLP_H)] = __float2bfloat16(p[P_W3 + o * MLP_H + j] * inv);
+        b3[o] = p[P_B3 + o] * inv + my[o];
+    }
+    MLP_TRY(cudaMemcpyAsync(m->inf.w1, w1.data(), sizeof(bf16) * w1.size(), cudaMemcpyHostToDevice, m->st));
+    MLP_TRY(cudaMemcpyAsync(m->inf.w2, w2.data(), sizeof(bf16) * w2.size(), cudaMemcpyHostToDevice, m->st));
+    MLP_TRY(cudaMemcpyAsync(m->inf.w3, w3.data(), sizeof(bf16) * w3.size(), cudaMemcpyHostToDevice, m->st));
+    MLP_TRY(cudaMemcpyAsync(m->inf.b1, b1.data(), sizeof(float) * MLP_H, cudaMemcpyHostToDevice, m->st));
+    MLP_TRY(cudaMemcpyAsync(m->inf.b2, b2.data(), sizeof(float) * MLP_H, cudaMemcpyHostToDevice, m->st));
+    MLP_TRY(cudaMemcpyAsync(m->inf.b3, b3.data(), sizeof(float) * MLP_OUT, cudaMemcpyHostToDevice, m->st));
+    return cudaStreamSynchronize(m->st);
+}
+
+// Per-column mean and inverse standard deviation of the dataset (constant columns get 1).
+cudaError_t mlp_fit_norm(Mlp* m, const float* dx, const float* dy, uint64_t rows) {
+    double* acc = nullptr;
+    MLP_TRY(cudaMalloc(&acc, sizeof(double) * 2 * (MLP_IN + MLP_OUT)));
+    MLP_TRY(cudaMemsetAsync(acc, 0, sizeof(double) * 2 * (MLP_IN + MLP_OUT), m->st));
+    k_col_stats<<<dim3(256, MLP_IN), 256, 0, m->st>>>(dx, rows, MLP_IN, acc);
+    k_col_stats<<<dim3(256, MLP_OUT), 256, 0, m->st>>>(dy, rows, MLP_OUT, acc + 2 * MLP_IN);
+    std::vector<double> h(2 * (MLP_IN + MLP_OUT));
+    cudaError_t e = cudaMemcpyAsync(h.data(), acc, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, m->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->st);
+    cudaFree(acc);
+    if (e != cudaSuccess) return e;
+    std::vector<float> nrm(NORM_COUNT);
+    auto put = [&](int col, int mu_at, int isd_at, const double* a) {
+        const double mean = a[0] / (double)rows;
+        const double var = a[1] / (double)rows - mean * mean;
+        const double sd = var > 1e-20 ? std::sqrt(var) : 0.0;
+        nrm[mu_at] = (float)mean;
+        nrm[isd_at] = sd > 0.0 ? (float)(1.0 / sd) : 1.f;
+        (void)col;
+    };
+    for (int i = 0; i < MLP_IN; i++) put(i, i, MLP_IN + i, &h[2 * i]);
+    for (int o = 0; o < MLP_OUT; o++) put(o, 2 * MLP_IN + o, 2 * MLP_IN + MLP_OUT + o, &h[2 * (MLP_IN + o)]);
+    return mlp_set_norm(m, nrm.data());
+}
+
+namespace {
+
+struct Workspace {
+    bf16 *X, *H1, *H2, *dY16, *dZ16;
+    float *Y, *Z1, *Z2, *Z3, *dY32, *dH, *dZ32;
+    double* loss;
+};
+
+cudaError_t workspace(Mlp* m, uint32_t B, Workspace* w) {
+    const size_t need = (size_t)B * (2 * MLP_IN + 2 * MLP_H * 3 + 2 * MLP_OUT) +  // bf16 arrays
+                        (size_t)B * 4 * (MLP_OUT * 3 + MLP_H * 4) + 64;
+    if (m->ws_batch < B) {
+        cudaFree(m->ws);
+        m->ws = nullptr;
+        m->ws_batch = 0;
+        MLP_TRY(cudaMalloc(&m->ws, need + 4096));
+        m->ws_batch = B;
+    }
+    char* p = (char*)m->ws;
+    auto take = [&](size_t bytes) { char* r = p; p += (bytes + 255) & ~(size_t)255; return r; };
+    w->loss = (double*)take(64);
+    w->X = (bf16*)take(2ull * B * MLP_IN);
+    w->H1 = (bf16*)take(2ull * B * MLP_H);
+    w->H2 = (bf16*)take(2ull * B * MLP_H);
+    w->dZ16 = (bf16*)take(2ull * B * MLP_H);
+    w->dY16 = (bf16*)take(2ull * B * MLP_OUT);
+    w->Y = (float*)take(4ull * B * MLP_OUT);
+    w->Z3 = (float*)take(4ull * B * MLP_OUT);
+    w->dY32 = (float*)take(4ull * B * MLP_OUT);
+    w->Z1 = (float*)take(4ull * B * MLP_H);
+    w->Z2 = (float*)take(4ull * B * MLP_H);
+    w->dH = (float*)take(4ull * B * MLP_H);
+    w->dZ32 = (float*)take(4ull * B * MLP_H);
+    return cudaSuccess;
+}
+
+// Forward and backward of one batch already in w->X / w->Y; gradients into m->grads.
+void fwd_bwd(Mlp* m, const Workspace& w, uint32_t B) {
+    cudaStream_t st = m->st;
+    const bf16* W1 = m->wb + P_W1;
+    const bf16* W2 = m->wb + P_W2;
+    const bf16* W3 = m->wb + P_W3;
+    const int split = (int)std::max<uint32_t>(1u, std::min<uint32_t>(64u, B / 1024u));
+    launch_gemm_bf16(B, MLP_H, MLP_IN, w.X, MLP_IN, 1, W1, 1, MLP_IN, w.Z1, MLP_H, 1, st);
+    k_bias_act<<<blocks((size_t)B * MLP_H), 256, 0, st>>>(w.Z1, m->params + P_B1, MLP_H, (size_t)B * MLP_H, w.H1);
+    launch_gemm_bf16(B, MLP_H, MLP_H, w.H1, MLP_H, 1, W2, 1, MLP_H, w.Z2, MLP_H, 1, st);
+    k_bias_act<<<blocks((size_t)B * MLP_H), 256, 0, st>>>(w.Z2, m->params + P_B2, MLP_H, (size_t)B * MLP_H, w.H2);
+    launch_gemm_bf16(B, MLP_OUT, MLP_H, w.H2, MLP_H, 1, W3, 1, MLP_H, w.Z3, MLP_OUT, 1, st);
+    k_bias_act<<<blocks((size_t)B * MLP_OUT), 256, 0, st>>>(w.Z3, m->params + P_B3, MLP_OUT, (size_t)B * MLP_OUT, nullptr);
+    cudaMemsetAsync(w.loss, 0, sizeof(double), st);
+    k_out_grad<<<blocks((size_t)B * MLP_OUT), 256, 0, st>>>(w.Z3, w.Y, (size_t)B * MLP_OUT,
+                                                          1.f / ((float)B * MLP_OUT), w.dY16, w.dY32, w.loss);
+    cudaMemsetAsync(m->grads, 0, 4ull * P_COUNT, st);
+    // layer 3
+    launch_gemm_bf16(MLP_OUT, MLP_H, B, w.dY16, 1, MLP_OUT, w.H2, MLP_H, 1, m->grads + P_W3, MLP_H, split, st);
+    k_colsum<<<MLP_OUT, 256, 0, st>>>(w.dY32, B, MLP_OUT, m->grads + P_B3);
+    launch_gemm_bf16(B, MLP_H, MLP_OUT, w.dY16, MLP_OUT, 1, W3, MLP_H, 1, w.dH, MLP_H, 1, st);
+    k_act_grad<<<blocks((size_t)B * MLP_H), 256, 0, st>>>(w.dH, w.Z2, (size_t)B * MLP_H, w.dZ16, w.dZ32);
+    // layer 2
+    launch_gemm_bf16(MLP_H, MLP_H, B, w.dZ16, 1, MLP_H, w.H1, MLP_H, 1, m->grads + P_W2, MLP_H, split, st);
+    k_colsum<<<MLP_H, 256, 0, st>>>(w.dZ32, B, MLP_H, m->grads + P_B2);
+    launch_gemm_bf16(B, MLP_H, MLP_H, w.dZ16, MLP_H, 1, W2, MLP_H, 1, w.dH, MLP_H, 1, st);
+    k_act_grad<<<blocks((size_t)B * MLP_H), 256, 0, st>>>(w.dH, w.Z1, (size_t)B * MLP_H, w.dZ16, w.dZ32);
+    // layer 1
+    launch_gemm_bf16(MLP_H, MLP_IN, B, w.dZ16, 1, MLP_H, w.X, MLP_IN, 1, m->grads + P_W1, MLP_IN, split, st);
+    k_colsum<<<MLP_H, 256, 0, st>>>(w.dZ32, B, MLP_H, m->grads + P_B1);
+}
+
+}  // namespace
+
+cudaError_t mlp_train(Mlp* m, const float* dx, const float* dy, uint64_t rows, uint32_t steps,
+                      uint32_t B, float lr, uint64_t seed, float* loss_host) {
+    if (rows == 0 || B == 0) return cudaErrorInvalidValue;
+    Workspace w;
+    MLP_TRY(workspace(m, B, &w));
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (uint32_t s = 0; s < steps; s++) {
+        k_make_batch<<<blocks(B), 256, 0, m->st>>>(dx, dy, rows, B, mix_seed(seed, m->adam_t), m->norm,
+                                                   w.X, w.Y, 0);
+        fwd_bwd(m, w, B);
+        m->adam_t++;
+        const float c1 = 1.f - std::pow(b1, (float)m->adam_t);
+        const float c2 = 1.f - std::pow(b2, (float)m->adam_t);
+        k_adam<<<blocks(P_COUNT), 256, 0, m->st>>>(m->params, m->grads, m->adam_m, m->adam_v, P_COUNT, lr,
+                                                   b1, b2, eps, c1, c2);
+        k_to_bf16<<<blocks(P_COUNT), 256, 0, m->st>>>(m->params, m->wb, P_COUNT);
+        if (loss_host) {
+            double l = 0;
+            MLP_TRY(cudaMemcpyAsync(&l, w.loss, sizeof(double), cudaMemcpyDeviceToHost, m->st));
+            MLP_TRY(cudaStreamSynchronize(m->st));
+            loss_host[s] = (float)(l / ((double)B * MLP_OUT));
+        }
+    }
+    MLP_TRY(cudaGetLastError());
+    return mlp_refresh_inference(m);
+}
+
+cudaError_t mlp_grad(Mlp* m, const float* dx, const float* dy, uint32_t n, float* grads_host,
+                     double* loss) {
+    Workspace w;
+    MLP_TRY(workspace(m, n, &w));
+    k_make_batch<<<blocks(n), 256, 0, m->st>>>(dx, dy, n, n, 0, m->norm, w.X, w.Y, 1);
+    fwd_bwd(m, w, n);
+    MLP_TRY(cudaGetLastError());
+    MLP_TRY(cudaMemcpyAsync(grads_host, m->grads, 4ull * P_COUNT, cudaMemcpyDeviceToHost, m->st));
+    double l = 0;
+    MLP_TRY(cudaMemcpyAsync(&l, w.loss, sizeof(double), cudaMemcpyDeviceToHost, m->st));
+    MLP_TRY(cudaStreamSynchronize(m->st));
+    if (loss) *loss = l / ((double)n * MLP_OUT);
+    return cudaSuccess;
+}
+
+void launch_mlp_infer(const Mlp* m, const bf16* feat, const float* conc_in, const float* conc_plain,
+                      float* conc_out, uint32_t* genes, const uint32_t* nactive, uint32_t n_override,
+                      const uint32_t* step, uint32_t period, uint32_t stride, float threshold,
+                      uint32_t* stats, uint32_t* err, int num_sms, cudaStream_t st) {
+    k_mlp_infer<<<num_sms, INF_THREADS, sizeof(InferSmem), st>>>(
+        m->inf, feat, conc_in, conc_plain, conc_out, genes, nactive, n_override, step, period, stride,
+        threshold, stats, err);
+}
+
+}  // namespace mg

@@ -23,6 +23,7 @@
 // The density pass also records each particle's fluid-force neighbours (dsq < 1) so the force
 // pass reads a short list instead of searching again.
 #include <cfloat>
+#include <cuda_bf16.h>
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -51,49 +52,69 @@ __device__ __forceinline__ float wendland_term(float dsq, float sr) {
     return b * (4.f * qq + 1.f);
 }
 
-template <bool DIFF>
-__device__ __forceinline__ void diffuse_add(float (&nc)[NTF], const float (&dif)[NTF],
-                                            const float (&cur)[NTF], const float* conc, uint32_t q,
-                                            float cc, bool uniform) {
-    if (!DIFF) return;
-    if (uniform) {
-        // every species has the same rate dif[0] != 0: (dif[t] * cc) is one value
-        const float a = dif[0] * cc;
-        const float4* cj4 = reinterpret_cast<const float4*>(conc + (size_t)q * NTF);
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const float4 v = cj4[k];
-            nc[4 * k] += a * (v.x - cur[4 * k]);
-            nc[4 * k + 1] += a * (v.y - cur[4 * k + 1]);
-            nc[4 * k + 2] += a * (v.z - cur[4 * k + 2]);
-            nc[4 * k + 3] += a * (v.w - cur[4 * k + 3]);
-        }
-        return;
-    }
+// Neighbour q's concentrations into the diffusion sums (nc, when `diffuse`) and into the plain
+// neighbour sum (ms, when MEAN).  (dif[t] * cc) * (cq[t] - cur[t]) is the reference term; with
+// one common nonzero rate the product dif[t] * cc is the same value for every species.
+template <bool DIFF, bool MEAN>
+__device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], const float (&dif)[NTF],
+                                           const float (&cur)[NTF], const float* conc, uint32_t q,
+                                           float cc, bool uniform, bool diffuse) {
+    if (!DIFF && !MEAN) return;
     const float4* cj4 = reinterpret_cast<const float4*>(conc + (size_t)q * NTF);
     float cj[NTF];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        float4 v = cj4[k];
+        const float4 v = cj4[k];
         cj[4 * k] = v.x; cj[4 * k + 1] = v.y; cj[4 * k + 2] = v.z; cj[4 * k + 3] = v.w;
     }
+    if (MEAN) {
 #pragma unroll
-    for (int t = 0; t < NTF; t++)
-        if (dif[t] != 0.f) nc[t] += (dif[t] * cc) * (cj[t] - cur[t]);
+        for (int t = 0; t < NTF; t++) ms[t] += cj[t];
+    }
+    if (DIFF && diffuse) {
+        if (uniform) {
+            const float a = dif[0] * cc;
+#pragma unroll
+            for (int t = 0; t < NTF; t++) nc[t] += a * (cj[t] - cur[t]);
+        } else {
+#pragma unroll
+            for (int t = 0; t < NTF; t++)
+                if (dif[t] != 0.f) nc[t] += (dif[t] * cc) * (cj[t] - cur[t]);
+        }
+    }
 }
 
-// The reference neighbour walk for one particle: density sum and diffusion exchange.
-template <bool DENS, bool DIFF>
+
+// FLAGS: 1 density/pressure, 2 diffusion, 4 gene reaction, 8 surrogate features,
+// 16 capture of (features, plain increment) pairs, 32 judge (plain update only for the
+// particles sampled this step or handed to the plain method; results go to conc_plain).
+template <int FLAGS>
+struct DF {
+    static constexpr bool DENS = FLAGS & 1, DIFF = FLAGS & 2, GENE = FLAGS & 4, FEAT = FLAGS & 8,
+                          CAPTURE = FLAGS & 16, JUDGE = FLAGS & 32, MEAN = FEAT || CAPTURE;
+};
+
+__device__ __forceinline__ bool judged_lane(const DensExtra& X, uint32_t p, uint32_t gene_word) {
+    if ((gene_word >> 31) & 1u) return true;  // handed to the plain method for good
+    if (!X.judge_period || !X.judge_stride) return false;
+    const uint32_t step = *X.step;
+    if (step % X.judge_period) return false;
+    return p % X.judge_stride == (step / X.judge_period) % X.judge_stride;
+}
+
+// The reference neighbour walk for one particle: density sum, diffusion and neighbour sums.
+template <int FLAGS>
 __device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint32_t pcell,
                                              const float4* __restrict__ pos,
                                              const float* __restrict__ conc,
                                              const uint32_t* __restrict__ count,
                                              const uint32_t* __restrict__ offset,
-                                             float (&nc)[NTF], const float (&dif)[NTF],
-                                             const float (&cur)[NTF],
-                                             uint32_t* __restrict__ flist = nullptr,
+                                             float (&nc)[NTF], float (&ms)[NTF], uint32_t& mcnt,
+                                             const float (&dif)[NTF], const float (&cur)[NTF],
+                                             bool diffuse, uint32_t* __restrict__ flist = nullptr,
                                              uint32_t* __restrict__ fcount = nullptr,
                                              uint32_t p = 0) {
+    using F = DF<FLAGS>;
     float sum = 0.f;
     uint32_t nf = 0;
     const uint32_t base = pcell - (uint32_t)P.nadj;
@@ -111,41 +132,68 @@ __device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint
                 if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
                 nf++;
             }
-            if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
-            if (DIFF && dsq < P.r2diff && dsq > 0.f) diffuse_add<DIFF>(nc, dif, cur, conc, q, (P.r2diff - dsq) * P.d2, false);
+            if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
+            if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
+                conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc, q, (P.r2diff - dsq) * P.d2,
+                                             false, diffuse);
+                mcnt++;
+            }
         }
-        if (DENS) sum += part;
+        if (F::DENS) sum += part;
     }
     if (fcount) fcount[p] = nf;
     return sum;
 }
 
-// Density -> pressure and 1/density; diffusion result and the gene reaction; conc written.
+// Density -> pressure and 1/density; diffusion + gene reaction (the plain update); surrogate
+// features and captured training pairs.
 template <int FLAGS>
 __device__ __forceinline__ void dens_epilogue(const DevParams& P, const DevGenome* __restrict__ G,
                                               uint32_t p, float sum, const float (&nc)[NTF],
-                                              const float (&cur)[NTF],
+                                              const float (&ms)[NTF], uint32_t mcnt,
+                                              const float (&cur)[NTF], bool plain,
                                               const uint32_t* __restrict__ genes,
                                               float* __restrict__ conc_out,
                                               float* __restrict__ press,
-                                              float* __restrict__ invdens) {
-    constexpr bool DENS = FLAGS & 1, DIFF = FLAGS & 2, GENE = FLAGS & 4;
-    if (DENS) {
+                                              float* __restrict__ invdens, const DensExtra& X) {
+    using F = DF<FLAGS>;
+    if (F::DENS) {
         sum = sum * P.pmass * P.wc2;
         if (sum == 0.f) sum = 1.f;
         press[p] = (sum - P.rest) * P.istiff;
         invdens[p] = 1.f / sum;
     }
-    if (DIFF || GENE) {
+    const uint32_t gene_word = (F::GENE || F::MEAN || F::JUDGE) ? genes[p] : 0u;
+    if (F::MEAN) {
+        float f[MLP_FEATURES];
+        const float inv = mcnt ? 1.f / (float)mcnt : 0.f;
+#pragma unroll
+        for (int t = 0; t < NTF; t++) {
+            f[t] = cur[t];
+            f[NTF + t] = mcnt ? ms[t] * inv : cur[t];
+            f[2 * NTF + t] = (float)((gene_word >> t) & 1u);
+        }
+        if (F::FEAT) {
+            __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(X.feat + (size_t)p * MLP_FEATURES);
+#pragma unroll
+            for (int t = 0; t < MLP_FEATURES / 2; t++) o[t] = __floats2bfloat162_rn(f[2 * t], f[2 * t + 1]);
+        }
+        if (F::CAPTURE) {
+            float4* o = reinterpret_cast<float4*>(X.cap_x + (size_t)p * MLP_FEATURES);
+#pragma unroll
+            for (int k = 0; k < MLP_FEATURES / 4; k++) o[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+        }
+    }
+    if ((F::DIFF || F::GENE) && plain) {
         float c[NTF];
 #pragma unroll
-        for (int t = 0; t < NTF; t++) c[t] = DIFF ? G->breakdown[t] * (cur[t] + nc[t]) : cur[t];
-        if (GENE) {
+        for (int t = 0; t < NTF; t++) c[t] = F::DIFF ? G->breakdown[t] * (cur[t] + nc[t]) : cur[t];
+        if (F::GENE) {
             // Gene bits are the sort-time dense-list membership (FEPIGEN > 0).  With every
             // FEPIGEN in {0, INT_MAX} and no activation lists the countdown never fires and
             // the reaction is: for each active gene g in order, activity = sum_tf sens*conc,
             // secretion accumulates rate*activity; living particles (gene 2) add it.
-            const uint32_t bits = genes[p];
+            const uint32_t bits = gene_word & 0xFFFFu;
             float dc[NTF];
 #pragma unroll
             for (int t = 0; t < NTF; t++) dc[t] = 0.f;
@@ -171,18 +219,25 @@ __device__ __forceinline__ void dens_epilogue(const DevParams& P, const DevGenom
                 for (int t = 0; t < NTF; t++) c[t] += dc[t];
             }
         }
-        float4* o4 = reinterpret_cast<float4*>(conc_out + (size_t)p * NTF);
+        float* dst = F::JUDGE ? X.conc_plain : conc_out;
+        float4* o4 = reinterpret_cast<float4*>(dst + (size_t)p * NTF);
 #pragma unroll
         for (int k = 0; k < 4; k++) o4[k] = make_float4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
+        if (F::CAPTURE) {
+            float4* y4 = reinterpret_cast<float4*>(X.cap_y + (size_t)p * NTF);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                y4[k] = make_float4(c[4 * k] - cur[4 * k], c[4 * k + 1] - cur[4 * k + 1],
+                                    c[4 * k + 2] - cur[4 * k + 2], c[4 * k + 3] - cur[4 * k + 3]);
+        }
     }
 }
 
 template <int FLAGS>
 __device__ __forceinline__ void load_conc(const DevGenome* __restrict__ G, const float* conc_in,
-                                          uint32_t p, float (&cur)[NTF], float (&nc)[NTF],
-                                          float (&dif)[NTF]) {
-    constexpr bool DIFF = FLAGS & 2, GENE = FLAGS & 4;
-    if (DIFF || GENE) {
+                                          uint32_t p, float (&cur)[NTF], float (&dif)[NTF]) {
+    using F = DF<FLAGS>;
+    if (F::DIFF || F::GENE || F::MEAN) {
         const float4* c4 = reinterpret_cast<const float4*>(conc_in + (size_t)p * NTF);
 #pragma unroll
         for (int k = 0; k < 4; k++) {
@@ -191,10 +246,7 @@ __device__ __forceinline__ void load_conc(const DevGenome* __restrict__ G, const
         }
     }
 #pragma unroll
-    for (int t = 0; t < NTF; t++) {
-        nc[t] = 0.f;
-        dif[t] = DIFF ? G->diff[t] : 0.f;
-    }
+    for (int t = 0; t < NTF; t++) dif[t] = F::DIFF ? G->diff[t] : 0.f;
 }
 
 // ---- direct kernel (one thread per particle, the reference loop) ------------------------
@@ -209,16 +261,21 @@ __global__ void __launch_bounds__(256) k_dens(DevParams P, const DevGenome* __re
                                               const uint32_t* __restrict__ offset,
                                               float* __restrict__ press,
                                               float* __restrict__ invdens,
-                                              const uint32_t* __restrict__ nactive_p) {
-    constexpr bool DENS = FLAGS & 1, DIFF = FLAGS & 2;
+                                              const uint32_t* __restrict__ nactive_p, DensExtra X) {
+    using F = DF<FLAGS>;
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= *nactive_p) return;
-    float cur[NTF], nc[NTF], dif[NTF];
-    load_conc<FLAGS>(G, conc_in, p, cur, nc, dif);
+    float cur[NTF], nc[NTF], ms[NTF], dif[NTF];
+    load_conc<FLAGS>(G, conc_in, p, cur, dif);
+#pragma unroll
+    for (int t = 0; t < NTF; t++) { nc[t] = 0.f; ms[t] = 0.f; }
+    const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
+    uint32_t mcnt = 0;
     float sum = 0.f;
-    if (DENS || DIFF)
-        sum = dens_direct<DENS, DIFF>(P, pos[p], scell[p], pos, conc_in, count, offset, nc, dif, cur);
-    dens_epilogue<FLAGS>(P, G, p, sum, nc, cur, genes, conc_out, press, invdens);
+    if (F::DENS || F::DIFF || F::MEAN)
+        sum = dens_direct<FLAGS>(P, pos[p], scell[p], pos, conc_in, count, offset, nc, ms, mcnt, dif,
+                                 cur, plain);
+    dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press, invdens, X);
 }
 
 // ---- warp-cooperative kernel ----------------------------------------------------------------
@@ -243,31 +300,31 @@ __device__ __forceinline__ int warp_maxi(int v) {
     return v;
 }
 
-// One warp item: up to 32 particles (lane l holds particle p when act) searched together.
-// Every lane of the warp must call this (it uses warp collectives).
 template <int FLAGS>
-__device__ __forceinline__ void dens_warp_item(
-    const DevParams& P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
+    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
     const float* __restrict__ conc_in, float* __restrict__ conc_out,
     const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
-    uint32_t* __restrict__ fcount, uint32_t p, bool act, uint32_t* s_list, float4 (*s_sp)[32],
-    uint32_t (*s_sq)[32]) {
-    constexpr bool DENS = FLAGS & 1, DIFF = FLAGS & 2;
+    uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p, DensExtra X) {
+    using F = DF<FLAGS>;
+    extern __shared__ uint32_t s_list[];  // [DENS_WARPS][NL_CAP][32]
+    __shared__ float4 s_sp[DENS_WARPS][32];
+    __shared__ uint32_t s_sq[DENS_WARPS][32];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     uint32_t* my = s_list + (size_t)w * NL_CAP * 32 + lane;
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = p < *nactive_p;
+    if (!__any_sync(0xffffffffu, act)) return;
 
-    float nc[NTF];
-#pragma unroll
-    for (int t = 0; t < NTF; t++) nc[t] = 0.f;
     const float4 ip = act ? pos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
     const uint32_t pcell = act ? scell[p] : 0u;
     const CellWin win = window_of(P, pcell);
     // search radius: the largest threshold any term of this pass (and the force list) uses
     float R2 = 1.f;
-    if (DENS) R2 = fmaxf(R2, P.r2);
-    if (DIFF) R2 = fmaxf(R2, P.r2diff);
+    if (F::DENS) R2 = fmaxf(R2, P.r2);
+    if (F::DIFF || F::MEAN) R2 = fmaxf(R2, P.r2diff);
     const float Rf = sqrtf(R2) * 1.0001f + 1e-3f;  // conservative prefilter radius
     const float INF = __int_as_float(0x7f800000);
     const float bx0 = warp_min(act ? ip.x : INF) - Rf, bx1 = warp_max(act ? ip.x : -INF) + Rf;
@@ -323,15 +380,19 @@ __device__ __forceinline__ void dens_warp_item(
         }
     }
     if (!act) return;
-    float cur[NTF], dif[NTF], scratch[NTF];
-    load_conc<FLAGS>(G, conc_in, p, cur, scratch, dif);
+    float cur[NTF], dif[NTF], nc[NTF], ms[NTF];
+    load_conc<FLAGS>(G, conc_in, p, cur, dif);
+#pragma unroll
+    for (int t = 0; t < NTF; t++) { nc[t] = 0.f; ms[t] = 0.f; }
+    const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
+    uint32_t mcnt = 0;
     float sum = 0.f;
     if (n <= (uint32_t)NL_CAP) {
         float part = 0.f;
         uint32_t curcell = UNDEF, nf = 0;
         for (uint32_t k = 0; k < n; k++) {
             const uint32_t q = my[k * 32];
-            if (DENS) {
+            if (F::DENS) {
                 const uint32_t qc = scell[q];
                 if (qc != curcell) {  // flush the partial sum of the previous cell
                     sum += part;
@@ -346,86 +407,64 @@ __device__ __forceinline__ void dens_warp_item(
                 if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
                 nf++;
             }
-            if (DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
-            if (DIFF && dsq < P.r2diff && dsq > 0.f)
-                diffuse_add<DIFF>(nc, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2, P.uniform_diff != 0);
+            if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
+            if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
+                conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2,
+                                             P.uniform_diff != 0, plain);
+                mcnt++;
+            }
         }
-        if (DENS) sum += part;
+        if (F::DENS) sum += part;
         fcount[p] = nf;  // > FL_CAP: the force pass searches again
     } else {
         // more neighbours than the list holds (not seen at rest density): the reference walk
-#pragma unroll
-        for (int t = 0; t < NTF; t++) nc[t] = 0.f;
-        sum = dens_direct<DENS, DIFF>(P, ip, pcell, pos, conc_in, count, offset, nc, dif, cur,
-                                     flist, fcount, p);
+        sum = dens_direct<FLAGS>(P, ip, pcell, pos, conc_in, count, offset, nc, ms, mcnt, dif, cur,
+                                 plain, flist, fcount, p);
     }
-    dens_epilogue<FLAGS>(P, G, p, sum, nc, cur, genes, conc_out, press, invdens);
-}
-
-template <int FLAGS>
-__global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
-    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
-    const float* __restrict__ conc_in, float* __restrict__ conc_out,
-    const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
-    const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
-    float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
-    uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p) {
-    extern __shared__ uint32_t s_list[];  // [DENS_WARPS][NL_CAP][32]
-    __shared__ float4 s_sp[DENS_WARPS][32];
-    __shared__ uint32_t s_sq[DENS_WARPS][32];
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool act = p < *nactive_p;
-    if (!__any_sync(0xffffffffu, act)) return;
-    dens_warp_item<FLAGS>(P, G, pos, conc_in, conc_out, genes, scell, count, offset, press, invdens,
-                          flist, fcount, p, act, s_list, s_sp, s_sq);
+    dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press, invdens, X);
 }
 
 // The per-lane lists take 48 KB of dynamic shared memory next to the static survivor buffers,
 // above the 48 KB a launch gets without opting in.
+#define MG_DENS_FLAG_SETS(M) M(1) M(2) M(3) M(5) M(6) M(7) M(9) M(23) M(46) M(47)
+
 cudaError_t physics_init() {
     const int smem = DENS_WARPS * NL_CAP * 32 * (int)sizeof(uint32_t);
     cudaError_t e = cudaSuccess;
 #define MG_ATTR(F)                                                                              \
     if (e == cudaSuccess)                                                                       \
         e = cudaFuncSetAttribute(k_dens_warp<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    MG_ATTR(1) MG_ATTR(2) MG_ATTR(3) MG_ATTR(5) MG_ATTR(6) MG_ATTR(7)
+    MG_DENS_FLAG_SETS(MG_ATTR)
 #undef MG_ATTR
     return e;
 }
 
 void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
-                 cudaStream_t st) {
+                 cudaStream_t st, const DensExtra* extra) {
+    (void)num_sms;
+    const DensExtra X = extra ? *extra : DensExtra{};
     const size_t smem = (size_t)DENS_WARPS * NL_CAP * 32 * sizeof(uint32_t);
-    if (search == 1 && (flags & 3)) {
+    if (search == 1 && (flags & (1 | 2 | 8 | 16))) {
         uint32_t blocks = (P.cap + DENS_WARPS * 32 - 1) / (DENS_WARPS * 32);
 #define MG_DENSW_CASE(F)                                                                          \
     case F:                                                                                       \
         k_dens_warp<F><<<blocks, DENS_WARPS * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,   \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
-                                                             s.flist, s.fcount, s.counters + 3);  \
-        break;
-        switch (flags & 7) {
-            MG_DENSW_CASE(1) MG_DENSW_CASE(2) MG_DENSW_CASE(3) MG_DENSW_CASE(5) MG_DENSW_CASE(6)
-            MG_DENSW_CASE(7)
-            default: break;
-        }
-#undef MG_DENSW_CASE
+                                                             s.flist, s.fcount, s.counters + 3, X); \
         return;
+        switch (flags) { MG_DENS_FLAG_SETS(MG_DENSW_CASE) default: break; }
+#undef MG_DENSW_CASE
     }
     uint32_t blocks = (P.cap + 255) / 256;
 #define MG_DENS_CASE(F)                                                                        \
     case F:                                                                                    \
         k_dens<F><<<blocks, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out, cur.genes, s.scell, \
                                           s.count, s.offset, s.press, s.invdens,              \
-                                          s.counters + 3);                                     \
-        break;
-    switch (flags & 7) {
-        MG_DENS_CASE(1) MG_DENS_CASE(2) MG_DENS_CASE(3) MG_DENS_CASE(4) MG_DENS_CASE(5)
-        MG_DENS_CASE(6) MG_DENS_CASE(7)
-        default: break;
-    }
+                                          s.counters + 3, X);                                  \
+        return;
+    switch (flags) { MG_DENS_FLAG_SETS(MG_DENS_CASE) MG_DENS_CASE(4) default: break; }
 #undef MG_DENS_CASE
 }
 

@@ -42,8 +42,10 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
                                                 uint32_t* __restrict__ cell,
                                                 uint32_t* __restrict__ arank,
                                                 uint32_t* __restrict__ newidx,
-                                                uint32_t* __restrict__ count) {
+                                                uint32_t* __restrict__ count,
+                                                uint32_t* __restrict__ step) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *step += 1u;  // step counter read by the later kernels of this step
     bool in = i < P.cap;
     uint32_t c = UNDEF;
     if (in) {
@@ -66,7 +68,7 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
 
 void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
-    k_insert<<<blocks, 256, 0, st>>>(P, cur.pos, s.cell, s.arank, s.newidx, s.count);
+    k_insert<<<blocks, 256, 0, st>>>(P, cur.pos, s.cell, s.arank, s.newidx, s.count, s.counters + 5);
 }
 
 // ---- single-pass scan (decoupled look-back) ------------------------------------------------
