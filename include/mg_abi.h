@@ -284,6 +284,30 @@ mg_status mg_algorithmic_bytes(mg_handle h, const char* kernel, uint32_t flags,
 /* Number of GPU kernels mg_step/mg_time_steps have launched on this handle. */
 uint64_t mg_kernel_launches(mg_handle h);
 
+/* ---- allocation-free prefix sum (no counterpart in the reference) ------------------------ */
+/* Largest n mg_prefix_sum_noalloc accepts: 16384 tiles of 4096 elements. */
+#define MG_NOALLOC_SCAN_MAX 67108864ull
+/* Exclusive prefix sum offsets[i] = counts[0] + ... + counts[i-1] (mod 2^32), the scan
+ * mg_prefix_sum_cells runs, over the caller's own device arrays, for callers that may not
+ * allocate device memory at that point (an application whose own pool owns all device memory,
+ * code inside an allocator callback, a loop that cannot take cudaFree's device-wide
+ * synchronisation).  It calls no allocating routine (a rejected call only records its error
+ * text): its scratch is a fixed 128 KiB device array per device inside the library, which it
+ * clears on the stream before each scan.
+ *   counts, offsets  device arrays of n uint32 (must not overlap)
+ *   n                0 .. MG_NOALLOC_SCAN_MAX; larger n is rejected with MG_ERR_INVALID_ARG
+ *   total            optional device uint32 receiving the sum of all n counts
+ *   error            optional device uint32 the caller has zeroed; bit 0 is set if a bounded
+ *                    look-back wait gave up (the offsets are then invalid)
+ *   stream           a cudaStream_t passed as void* (NULL: the default stream); the call is
+ *                    asynchronous on it and uses the current device
+ * The first call on each device looks up the scratch address (a one-time set-up); make that
+ * first call, with the device current, before any stream capture begins.  Calls on one device
+ * share the scratch: calls whose scans can overlap in time (different streams without
+ * ordering, or several host threads at once) race and give wrong offsets; order them. */
+mg_status mg_prefix_sum_noalloc(const uint32_t* counts, uint32_t* offsets, uint64_t n,
+                                uint32_t* total, uint32_t* error, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

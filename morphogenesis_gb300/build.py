@@ -28,6 +28,7 @@ UNITS = {
     "mg_io.cu": [],
     "mg_mlp.cu": [],
     "mg_api.cu": [],
+    "mg_noalloc.cu": [],
 }
 
 

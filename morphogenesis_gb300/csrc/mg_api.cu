@@ -1317,3 +1317,5 @@ mg_status mg_surrogate_stats(mg_handle h, uint64_t* judged, uint64_t* handed_ove
 uint64_t mg_kernel_launches(mg_handle h) { return h ? h->launches : 0; }
 
 }  // extern "C"
+
+mg_status mg::record_thread_error(mg_status st, const char* msg) { return fail(nullptr, st, msg); }

@@ -21,6 +21,7 @@
 #include <cstdint>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include "../../include/mg_abi.h"
 
 namespace mg {
 
@@ -175,5 +176,8 @@ void launch_gene_cell_counts(const DevParams& P, const Carried& cur, const Scrat
                              uint32_t* gcount, cudaStream_t st);
 void launch_gene_lists(const DevParams& P, const Carried& cur, const Scratch& s,
                        const uint32_t* goffset, uint32_t* lists, cudaStream_t st);
+
+// Records the calling thread's error text (what mg_last_error(NULL) returns) and gives st back.
+mg_status record_thread_error(mg_status st, const char* msg);
 
 }  // namespace mg
