@@ -38,12 +38,15 @@ FALLBACK_HBM = 6800.0
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate section")
+    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--sur-steps", type=int, default=1000, help="in-loop surrogate evaluation steps")
     return ap.parse_args()
 
 
@@ -133,6 +136,13 @@ def measured_peak():
     return FALLBACK_HBM, "fallback"
 
 
+def measured_tflops():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        return float(json.loads(f.read_text())["bf16_tflops"])
+    return 1900.0
+
+
 def ncu_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` from the committed ncu summary, if one exists."""
     f = ROOT / "profiles" / "traffic.json"
@@ -162,6 +172,110 @@ def cpu_reference(steps: int, warmup: int, threads: int):
     dt = time.perf_counter() - t0
     o.close()
     return d.n * steps / dt, used, dt
+
+
+def surrogate_section(args, peak_tflops):
+    """Learned morphogen surrogate at 1,048,576 particles: trained on 2^24 (state, increment)
+    pairs captured from plain runs under 8 seeds, then compared with the plain morphogen stage
+    (diffusion + gene reaction) for speed and for concentration error."""
+    import morphogenesis_gb300 as mg
+    from morphogenesis_gb300 import _abi as A
+    from morphogenesis_gb300 import demo
+    from morphogenesis_gb300 import surrogate as S
+
+    out = {}
+    seeds = 8
+    ds = S.Dataset(1 << 24)
+    t0 = time.perf_counter()
+    for k in range(seeds):
+        d = demo.make_block(DIMS, PARAM, seed=100 + k)
+        fs = mg.FluidSystem(d.params, d.genome, d.n)
+        fs.TransferToCL(d.arrays)
+        fs.Run(5)
+        ds.capture(fs, A.STEP_PHYSICS)
+        fs.Run(200 + 100 * k)
+        ds.capture(fs, A.STEP_PHYSICS)
+        fs.close()
+    out["pairs"] = len(ds)
+    out["capture_s"] = time.perf_counter() - t0
+    m = S.Mlp(seed=0)
+    m.fit_normalization(ds)
+    t0 = time.perf_counter()
+    curve = m.train(ds, args.train_steps, batch=65536, lr=1e-3, seed=1)
+    out["train"] = {"steps": args.train_steps, "batch": 65536, "lr": 1e-3,
+                    "seconds": time.perf_counter() - t0,
+                    "loss_first": float(curve[:10].mean()), "loss_last": float(curve[-50:].mean())}
+    ds.close()
+
+    d = demo.make_block(DIMS, PARAM, seed=0)
+    n = d.n
+    plain = mg.FluidSystem(d.params, d.genome, n)
+    sur = mg.FluidSystem(d.params, d.genome, n)
+    for fs in (plain, sur):
+        fs.TransferToCL(d.arrays)
+        fs.Run(5)
+
+    def rel_err(a, b):
+        r = np.abs(a - b) / np.maximum(np.abs(b), 1e-6)
+        return {"median": float(np.median(r)), "p99": float(np.quantile(r, 0.99)), "max": float(r.max())}
+
+    # one morphogen stage from the same state, surrogate alone (no judge)
+    S.attach(sur, m, judge_period=0, judge_stride=0, threshold=1e-3)
+    c_plain, c_sur = plain.download(A.FCONC), None
+    plain.Run(1, A.STEP_GENES)
+    sur.Run(1, A.STEP_GENES | A.STEP_SURROGATE)
+    c_plain, c_sur = plain.download(A.FCONC), sur.download(A.FCONC)
+    out["rel_err_one_stage"] = rel_err(c_sur, c_plain)
+
+    # stage timings: plain diffusion + reaction kernel vs features + tcgen05 inference
+    K = 50
+    for fs, fl, key in ((plain, A.STEP_GENES, "plain"), (sur, A.STEP_GENES | A.STEP_SURROGATE, "surrogate")):
+        fs.profile(True)
+        fs.Run(K, fl)
+        prof = fs.profile_read()
+        fs.profile(False)
+        out[f"kernels_ms_{key}"] = {k: v[1] / v[0] for k, v in prof.items()}
+    stage_plain = out["kernels_ms_plain"]["diffusion_genes"]
+    stage_sur = out["kernels_ms_surrogate"]["features"] + out["kernels_ms_surrogate"]["mlp_infer"]
+    out["morphogen_stage"] = {
+        "plain_particle_steps_s": n / (stage_plain / 1e3),
+        "surrogate_particle_steps_s": n / (stage_sur / 1e3),
+        "speedup": stage_plain / stage_sur,
+    }
+    mlp_ms = out["kernels_ms_surrogate"]["mlp_infer"]
+    tflops = 49152.0 * n / (mlp_ms / 1e3) / 1e12
+    out["mlp_infer_roofline"] = {"bound": "tensor", "achieved": tflops, "peak": peak_tflops,
+                                 "unit": "TFLOP/s", "frac": tflops / peak_tflops,
+                                 "flops_per_particle": 49152}
+
+    # whole steps (sort + density + morphogen + force + advance), graph-replayed
+    for fs in (plain, sur):
+        fs.synchronize()
+    ms_plain = plain.time_steps(K, A.STEP_DEFAULT)
+    ms_sur = sur.time_steps(K, A.STEP_DEFAULT | A.STEP_SURROGATE)
+    out["full_step"] = {"plain_particle_steps_s": n * K / (ms_plain / 1e3),
+                        "surrogate_particle_steps_s": n * K / (ms_sur / 1e3)}
+    plain.close()
+    sur.close()
+
+    # in loop: judge re-runs 1/64 of the particles every 10 steps and takes over any particle
+    # whose relative error exceeds 1e-3
+    plain = mg.FluidSystem(d.params, d.genome, n)
+    sur = mg.FluidSystem(d.params, d.genome, n)
+    for fs in (plain, sur):
+        fs.TransferToCL(d.arrays)
+    S.attach(sur, m, judge_period=10, judge_stride=64, threshold=1e-3)
+    plain.Run(args.sur_steps, A.STEP_DEFAULT)
+    sur.Run(args.sur_steps, A.STEP_DEFAULT | A.STEP_SURROGATE)
+    judged, handed, worst = S.stats(sur)
+    out["in_loop"] = {"steps": args.sur_steps, "judge_period": 10, "judge_stride": 64,
+                      "threshold": 1e-3, "judged": judged, "handed_over": handed,
+                      "worst_judged_rel_err": worst,
+                      "rel_err_vs_plain": rel_err(sur.download(A.FCONC), plain.download(A.FCONC))}
+    plain.close()
+    sur.close()
+    m.close()
+    return out
 
 
 def run_reference(args, rank, world):
@@ -267,6 +381,10 @@ def main():
                "sample": f"{args.cpu_steps} steps of the same 1,048,576-particle workload ({cdt:.1f} s)"}
     fs.close()
 
+    sur = None
+    if rank == 0 and not args.no_surrogate:
+        sur = surrogate_section(args, measured_tflops())
+
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -290,6 +408,7 @@ def main():
                               "frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak},
             "kernels_ms_per_launch": {k: v[1] / v[0] for k, v in prof.items()},
             "cpu_baseline": cpu,
+            "surrogate": sur,
         }
         print(json.dumps(out), flush=True)
     dist.close()
