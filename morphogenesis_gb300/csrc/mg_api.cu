@@ -372,9 +372,10 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
     }
 }
 
-int kernels_per_step(uint32_t flags) {
+int kernels_per_step(const mg_system* h, uint32_t flags) {
     int n = 6;  // insert, scan, place, cellsort, cellsort_big, gather
-    if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE)) n += 1;
+    // density pass (+ its overflow pass with the warp search)
+    if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE)) n += h->search ? 2 : 1;
     if (flags & MG_STEP_SURROGATE) n += 1;
     if (flags & MG_STEP_PHYSICS) n += 2;
     return n;
@@ -426,7 +427,7 @@ mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
             if (st != MG_OK) return st;
             MG_CUDA(h, cudaGraphLaunch(ge, h->stream));
         }
-        h->launches += (uint64_t)kernels_per_step(flags);
+        h->launches += (uint64_t)kernels_per_step(h, flags);
         if (flags & MG_STEP_PHYSICS) h->time = h->time + h->P.dt;
     }
     h->phase = PHASE_SORTED;
@@ -603,6 +604,10 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     plan.push_back({(void**)&h->s.cell, 4 * n});
     plan.push_back({(void**)&h->s.arank, 4 * n});
     plan.push_back({(void**)&h->s.order, 4 * n});
+    plan.push_back({(void**)&h->s.sorted, 4 * n});
+    plan.push_back({(void**)&h->s.work, 4 * n});
+    plan.push_back({(void**)&h->s.sub, n});
+    plan.push_back({(void**)&h->s.ovf, 4 * n});
     plan.push_back({(void**)&h->s.newidx, 4 * n});
     plan.push_back({(void**)&h->s.scell, 4 * n});
     plan.push_back({(void**)&h->s.press, 4 * n});
@@ -1054,16 +1059,17 @@ mg_status mg_algorithmic_bytes(mg_handle h, const char* kernel, uint32_t flags,
     const bool phys = flags & MG_STEP_PHYSICS, genes = flags & MG_STEP_GENES;
     // carried state per particle: pos/vel/veval 48, bonds 192, incoming 48, conc 64, genes 4, origin 4
     const double carried = 48 + 192 + 48 + 64 + 4 + 4;
-    const double dens = (phys ? 16 + 4 + 4 + 4 : 0) + (genes ? (phys ? 0 : 16 + 4) + 64 + 64 + 4 : 0);
+    // density pass: work-order entry 4, pos 16, scell 4, then press/invdens/fcount or conc
+    const double dens = 4 + (phys ? 16 + 4 + 4 + 4 : 0) + (genes ? (phys ? 0 : 16 + 4) + 64 + 64 + 4 : 0);
     const K table[] = {
-        {"insert", 16 + 4 + 4 + 4, 4 + 8},            // pos, cell, rank, newidx | memset, atomics
+        {"insert", 16 + 4 + 4 + 4 + 1, 4 + 8},        // pos, cell, rank, newidx, sub | memset, atomics
         {"scan", 0, 8},                               // count read, offset write
         {"place", 12, 0},                             // cell, rank, order
-        {"cellsort", 12, 8},                          // order r/w, newidx | count, offset
+        {"cellsort", 21, 0},                          // order, cell, sub | sorted, newidx, work
         {"gather", 4 + carried + carried + 4 + 4, 0}, // order, read+write carried, cell, scell
         {"pressure", phys ? 28.0 : 0.0, 0},
         {"density_diffusion_genes", dens, 0},
-        {"diffusion_genes", genes ? 16 + 4 + 64 + 64 + 4 : 0.0, 0},
+        {"diffusion_genes", genes ? 4 + 16 + 4 + 64 + 64 + 4 : 0.0, 0},
         {"force", phys ? 16 + 16 + 4 + 4 + 4 + 192 + 48 + 48 + 16 + 4 : 0.0, 0},
         {"advance", phys ? 48 + 48 + 16 + 4 : 0.0, 0},
     };

@@ -101,7 +101,11 @@ struct Cold {
 struct Scratch {
     uint32_t* cell;     // unsorted cell of particle i (UNDEF outside the window)
     uint32_t* arank;    // arrival rank within the cell (not deterministic)
-    uint32_t* order;    // order[p] = pre-sort index of the particle sorted to p
+    uint32_t* order;    // arrival order: order[offset[cell] + arank[i]] = i (not stable)
+    uint32_t* sorted;   // sorted[p] = pre-sort index of the particle sorted to p (stable)
+    uint32_t* work;     // density-pass processing order: sorted slots, cell by cell, each
+                        // cell's particles by sub-cell Morton code (a permutation of [0, nactive))
+    uint8_t* sub;       // Morton code of particle i's 4x4x4 sub-cell inside its cell
     uint32_t* newidx;   // newidx[i] = sorted index of pre-sort particle i (UNDEF if dropped)
     uint32_t* scell;    // cell of sorted particle p
     float* press;
@@ -114,7 +118,9 @@ struct Scratch {
     uint32_t* offset;   // [cells]
     unsigned long long* scan_status;  // [tiles]
     uint32_t* counters; // [0] scan tile ticket, [1] big-cell list length, [2] error word,
-                        // [3] nactive, [5] step counter (incremented by insert)
+                        // [3] nactive, [5] step counter (incremented by insert),
+                        // [6] density-pass overflow queue length
+    uint32_t* ovf;      // [cap] particles whose neighbours overflow a lane's list
     uint32_t* big_list; // [BIG_LIST_CAP] cells that need the block-level ordering
 };
 

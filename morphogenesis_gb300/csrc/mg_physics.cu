@@ -289,6 +289,19 @@ __device__ __forceinline__ float warp_max(float v) {
     for (int d = 16; d > 0; d >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, d));
     return v;
 }
+// Whether cell (cx, cy, cz) can hold a point of the box [b?0, b?1].  The cell's extent is
+// widened by 1% of a cell on each side, far more than the rounding of the cell hash, so a
+// point the hash put in this cell is never excluded.
+__device__ __forceinline__ bool cell_meets_box(const DevParams& P, int cx, int cy, int cz,
+                                               float bx0, float bx1, float by0, float by1,
+                                               float bz0, float bz1) {
+    const float sx = 1.f / P.gdelta[0], sy = 1.f / P.gdelta[1], sz = 1.f / P.gdelta[2];
+    const float x0 = P.gmin[0] + ((float)cx - 0.01f) * sx, x1 = P.gmin[0] + ((float)cx + 1.01f) * sx;
+    const float y0 = P.gmin[1] + ((float)cy - 0.01f) * sy, y1 = P.gmin[1] + ((float)cy + 1.01f) * sy;
+    const float z0 = P.gmin[2] + ((float)cz - 0.01f) * sz, z1 = P.gmin[2] + ((float)cz + 1.01f) * sz;
+    return x1 >= bx0 && x0 <= bx1 && y1 >= by0 && y0 <= by1 && z1 >= bz0 && z0 <= bz1;
+}
+
 __device__ __forceinline__ int warp_mini(int v) {
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, d));
@@ -307,16 +320,21 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
     const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
-    uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p, DensExtra X) {
+    uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p,
+    const uint32_t* __restrict__ work, uint32_t* __restrict__ ovf, uint32_t* __restrict__ ovf_count,
+    DensExtra X) {
     using F = DF<FLAGS>;
     extern __shared__ uint32_t s_list[];  // [DENS_WARPS][NL_CAP][32]
     __shared__ float4 s_sp[DENS_WARPS][32];
     __shared__ uint32_t s_sq[DENS_WARPS][32];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     uint32_t* my = s_list + (size_t)w * NL_CAP * 32 + lane;
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool act = p < *nactive_p;
+    // Lane k of the grid takes the k-th entry of the processing order, so a warp holds
+    // particles of one compact sub-region of a cell; results go to the particle's sorted slot.
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = k < *nactive_p;
     if (!__any_sync(0xffffffffu, act)) return;
+    const uint32_t p = act ? work[k] : 0u;
 
     const float4 ip = act ? pos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
     const uint32_t pcell = act ? scell[p] : 0u;
@@ -327,30 +345,58 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
     if (F::DIFF || F::MEAN) R2 = fmaxf(R2, P.r2diff);
     const float Rf = sqrtf(R2) * 1.0001f + 1e-3f;  // conservative prefilter radius
     const float INF = __int_as_float(0x7f800000);
-    const float bx0 = warp_min(act ? ip.x : INF) - Rf, bx1 = warp_max(act ? ip.x : -INF) + Rf;
-    const float by0 = warp_min(act ? ip.y : INF) - Rf, by1 = warp_max(act ? ip.y : -INF) + Rf;
-    const float bz0 = warp_min(act ? ip.z : INF) - Rf, bz1 = warp_max(act ? ip.z : -INF) + Rf;
     const int g = P.gsrch;
     const int BIG = 1 << 30;
-    const int wx0 = warp_mini(act ? win.x : BIG), wx1 = warp_maxi(act ? win.x : -BIG) + g - 1;
-    const int wy0 = warp_mini(act ? win.y : BIG), wy1 = warp_maxi(act ? win.y : -BIG) + g - 1;
-    const int wz0 = warp_mini(act ? win.z : BIG), wz1 = warp_maxi(act ? win.z : -BIG) + g - 1;
 
+    // The warp's lanes are searched in groups: a group is the lanes whose cell is the first
+    // remaining lane's cell or the next cell of its row (the lanes' cells ascend with the
+    // lane index).  In dense regions a warp is one or two such cells and this is one pass; in
+    // sparse regions a warp's particles can come from distant cells, and searching them
+    // apart keeps each box and window small.  Within a group the search is unchanged.
     uint32_t n = 0;
-    for (int cy = wy0; cy <= wy1; cy++) {
-        for (int cz = wz0; cz <= wz1; cz++) {
-            for (int cx = wx0; cx <= wx1; cx++) {
-                const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
-                const uint32_t cnt = count[cell];
-                if (cnt == 0) continue;
-                const bool inw = act && cx - win.x >= 0 && cx - win.x < g && cy - win.y >= 0 &&
+    unsigned remaining = __ballot_sync(0xffffffffu, act);
+    while (remaining) {
+        const int leader = __ffs(remaining) - 1;
+        const uint32_t lcell = __shfl_sync(0xffffffffu, pcell, leader);
+        const bool ing = act && ((remaining >> lane) & 1u) && (pcell == lcell || pcell == lcell + 1u);
+        remaining &= ~__ballot_sync(0xffffffffu, ing);
+        const float bx0 = warp_min(ing ? ip.x : INF) - Rf, bx1 = warp_max(ing ? ip.x : -INF) + Rf;
+        const float by0 = warp_min(ing ? ip.y : INF) - Rf, by1 = warp_max(ing ? ip.y : -INF) + Rf;
+        const float bz0 = warp_min(ing ? ip.z : INF) - Rf, bz1 = warp_max(ing ? ip.z : -INF) + Rf;
+        const int wx0 = warp_mini(ing ? win.x : BIG), wx1 = warp_maxi(ing ? win.x : -BIG) + g - 1;
+        const int wy0 = warp_mini(ing ? win.y : BIG), wy1 = warp_maxi(ing ? win.y : -BIG) + g - 1;
+        const int wz0 = warp_mini(ing ? win.z : BIG), wz1 = warp_maxi(ing ? win.z : -BIG) + g - 1;
+        // The group's window cells, in ascending linear index (y, then z, then x), are looked
+        // up 32 at a time, one per lane, skipping cells whose box misses the group's box; the
+        // non-empty ones are then taken in order.
+        const int ncx = wx1 - wx0 + 1, ncz = wz1 - wz0 + 1;
+        const int ncell = ncx * ncz * (wy1 - wy0 + 1);
+        for (int cb = 0; cb < ncell; cb += 32) {
+            const int t = cb + (int)lane;
+            uint32_t tcnt = 0, toff = 0;
+            if (t < ncell) {
+                const int cx = wx0 + t % ncx, cz = wz0 + (t / ncx) % ncz, cy = wy0 + t / (ncx * ncz);
+                if (cell_meets_box(P, cx, cy, cz, bx0, bx1, by0, by1, bz0, bz1)) {
+                    const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
+                    tcnt = count[cell];
+                    if (tcnt) toff = offset[cell];
+                }
+            }
+            unsigned ne = __ballot_sync(0xffffffffu, tcnt != 0);
+            while (ne) {
+                const int src = __ffs(ne) - 1;
+                ne &= ne - 1;
+                const uint32_t cnt = __shfl_sync(0xffffffffu, tcnt, src);
+                const uint32_t off = __shfl_sync(0xffffffffu, toff, src);
+                const int ts = cb + src;
+                const int cx = wx0 + ts % ncx, cz = wz0 + (ts / ncx) % ncz, cy = wy0 + ts / (ncx * ncz);
+                const bool inw = ing && cx - win.x >= 0 && cx - win.x < g && cy - win.y >= 0 &&
                                  cy - win.y < g && cz - win.z >= 0 && cz - win.z < g;
                 if (!__any_sync(0xffffffffu, inw)) continue;
-                const uint32_t off = offset[cell];
                 for (uint32_t base = 0; base < cnt; base += 32) {
-                    const uint32_t k = base + lane;
-                    const bool valid = k < cnt;
-                    const float4 qp = valid ? pos[off + k] : make_float4(INF, INF, INF, 0.f);
+                    const uint32_t kk = base + lane;
+                    const bool valid = kk < cnt;
+                    const float4 qp = valid ? pos[off + kk] : make_float4(INF, INF, INF, 0.f);
                     const float ex = fmaxf(0.f, fmaxf(bx0 - qp.x, qp.x - bx1));
                     const float ey = fmaxf(0.f, fmaxf(by0 - qp.y, qp.y - by1));
                     const float ez = fmaxf(0.f, fmaxf(bz0 - qp.z, qp.z - bz1));
@@ -359,17 +405,17 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
                     if (surv) {
                         const uint32_t slot = (uint32_t)__popc(ball & ((1u << lane) - 1u));
                         s_sp[w][slot] = qp;
-                        s_sq[w][slot] = off + k;
+                        s_sq[w][slot] = off + kk;
                     }
                     __syncwarp();
                     const int ns = __popc(ball);
                     if (inw) {
-                        for (int t = 0; t < ns; t++) {
-                            const float4 sp = s_sp[w][t];
+                        for (int tt = 0; tt < ns; tt++) {
+                            const float4 sp = s_sp[w][tt];
                             const float dx = ip.x - sp.x, dy = ip.y - sp.y, dz = ip.z - sp.z;
                             const float dsq = dx * dx + dy * dy + dz * dz;
                             if (dsq < R2 && dsq > 0.f) {
-                                if (n < (uint32_t)NL_CAP) my[n * 32] = s_sq[w][t];
+                                if (n < (uint32_t)NL_CAP) my[n * 32] = s_sq[w][tt];
                                 n++;
                             }
                         }
@@ -380,6 +426,11 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
         }
     }
     if (!act) return;
+    if (n > (uint32_t)NL_CAP) {
+        // more neighbours than the list holds (dense clumps): the overflow pass takes it
+        ovf[atomicAdd(ovf_count, 1u)] = p;
+        return;
+    }
     float cur[NTF], dif[NTF], nc[NTF], ms[NTF];
     load_conc<FLAGS>(G, conc_in, p, cur, dif);
 #pragma unroll
@@ -387,7 +438,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
     const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
     uint32_t mcnt = 0;
     float sum = 0.f;
-    if (n <= (uint32_t)NL_CAP) {
+    {
         float part = 0.f;
         uint32_t curcell = UNDEF, nf = 0;
         for (uint32_t k = 0; k < n; k++) {
@@ -416,12 +467,93 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
         }
         if (F::DENS) sum += part;
         fcount[p] = nf;  // > FL_CAP: the force pass searches again
-    } else {
-        // more neighbours than the list holds (not seen at rest density): the reference walk
-        sum = dens_direct<FLAGS>(P, ip, pcell, pos, conc_in, count, offset, nc, ms, mcnt, dif, cur,
-                                 plain, flist, fcount, p);
     }
     dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press, invdens, X);
+}
+
+// ---- overflow pass ----------------------------------------------------------------------------
+// Particles queued by the warp search (more neighbours than NL_CAP, only in dense clumps), one
+// warp per particle.  The window cells are walked in the reference order, 32 candidates at a
+// time; each neighbour is then taken in ascending sorted index by every lane: all lanes keep the
+// density partial sums, lane t (mod 16) accumulates species t with the same expression and order
+// as the one-thread walk, lane 0 records the force list.  Lane 0 then runs the common epilogue.
+template <int FLAGS>
+__global__ void __launch_bounds__(256) k_dens_ovf(
+    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
+    const float* __restrict__ conc_in, float* __restrict__ conc_out,
+    const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
+    const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
+    float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
+    uint32_t* __restrict__ fcount, const uint32_t* __restrict__ ovf,
+    const uint32_t* __restrict__ ovf_count, DensExtra X) {
+    using F = DF<FLAGS>;
+    const uint32_t lane = threadIdx.x & 31u, t = lane & 15u;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    uint32_t nq = *ovf_count;
+    if (nq > P.cap) nq = P.cap;
+    float R2 = 1.f;
+    if (F::DENS) R2 = fmaxf(R2, P.r2);
+    if (F::DIFF || F::MEAN) R2 = fmaxf(R2, P.r2diff);
+    for (uint32_t e = gw; e < nq; e += nw) {
+        const uint32_t p = ovf[e];
+        const float4 ip = pos[p];
+        const float cur_t = (F::DIFF || F::GENE || F::MEAN) ? conc_in[(size_t)p * NTF + t] : 0.f;
+        const float dif_t = F::DIFF ? G->diff[t] : 0.f;
+        const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
+        float nc_t = 0.f, ms_t = 0.f, sum = 0.f;
+        uint32_t mcnt = 0, nf = 0;
+        const uint32_t base = scell[p] - (uint32_t)P.nadj;
+        for (int c = 0; c < P.adjcnt; c++) {
+            const uint32_t cellc = base + (uint32_t)P.adj[c];
+            const uint32_t cnt = count[cellc];
+            if (cnt == 0) continue;
+            const uint32_t off = offset[cellc];
+            float part = 0.f;
+            for (uint32_t b = 0; b < cnt; b += 32) {
+                const bool valid = b + lane < cnt;
+                float dsq = 0.f;
+                if (valid) {
+                    const float4 jp = pos[off + b + lane];
+                    const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+                    dsq = dx * dx + dy * dy + dz * dz;
+                }
+                unsigned hits = __ballot_sync(0xffffffffu, valid && dsq < R2 && dsq > 0.f);
+                while (hits) {
+                    const int src = __ffs(hits) - 1;
+                    hits &= hits - 1;
+                    const float d = __shfl_sync(0xffffffffu, dsq, src);
+                    const uint32_t q = off + b + (uint32_t)src;
+                    if (d < 1.f) {
+                        if (lane == 0 && nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
+                        nf++;
+                    }
+                    if (F::DENS && d < P.r2) part += wendland_term(d, P.sr);
+                    if ((F::DIFF || F::MEAN) && d < P.r2diff) {
+                        const float cj = conc_in[(size_t)q * NTF + t];
+                        if (F::MEAN) ms_t += cj;
+                        if (F::DIFF && plain && dif_t != 0.f)
+                            nc_t += (dif_t * ((P.r2diff - d) * P.d2)) * (cj - cur_t);
+                        mcnt++;
+                    }
+                }
+            }
+            if (F::DENS) sum += part;
+        }
+        float cur[NTF], nc[NTF], ms[NTF];
+#pragma unroll
+        for (int k = 0; k < NTF; k++) {
+            cur[k] = __shfl_sync(0xffffffffu, cur_t, k);
+            nc[k] = __shfl_sync(0xffffffffu, nc_t, k);
+            ms[k] = __shfl_sync(0xffffffffu, ms_t, k);
+        }
+        if (lane == 0) {
+            fcount[p] = nf;
+            dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press,
+                                 invdens, X);
+        }
+        __syncwarp();
+    }
 }
 
 // The per-lane lists take 48 KB of dynamic shared memory next to the static survivor buffers,
@@ -442,7 +574,6 @@ cudaError_t physics_init() {
 void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
                  cudaStream_t st, const DensExtra* extra) {
-    (void)num_sms;
     const DensExtra X = extra ? *extra : DensExtra{};
     const size_t smem = (size_t)DENS_WARPS * NL_CAP * 32 * sizeof(uint32_t);
     if (search == 1 && (flags & (1 | 2 | 8 | 16))) {
@@ -452,8 +583,15 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
         k_dens_warp<F><<<blocks, DENS_WARPS * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,   \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
-                                                             s.flist, s.fcount, s.counters + 3, X); \
+                                                             s.flist, s.fcount, s.counters + 3,   \
+                                                             s.work, s.ovf, s.counters + 6, X);   \
+        k_dens_ovf<F><<<(uint32_t)num_sms * 2, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out,    \
+                                                             cur.genes, s.scell, s.count,         \
+                                                             s.offset, s.press, s.invdens,        \
+                                                             s.flist, s.fcount, s.ovf,            \
+                                                             s.counters + 6, X);                  \
         return;
+        cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
         switch (flags) { MG_DENS_FLAG_SETS(MG_DENSW_CASE) default: break; }
 #undef MG_DENSW_CASE
     }

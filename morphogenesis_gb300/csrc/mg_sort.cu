@@ -10,10 +10,11 @@
 //              arrival rank that is only used to scatter indices into their cell's segment;
 //   scan     : single-pass exclusive scan with decoupled look-back -> per-cell offsets;
 //   place    : order[offset[cell] + arrival rank] = i;
-//   cellsort : each cell's segment of indices is put in ascending order (warp tier for
-//              cells <= 256 particles, block tier <= 8192, ordered stream compaction above),
-//              which yields order[] (sorted -> old) and newidx[] (old -> sorted);
-//   gather   : every carried field is gathered through order[], bond partners and incoming
+//   cellsort : the stable rank of every particle in its cell (one thread per particle for
+//              cells <= 256 particles; block tier <= 8192, ordered stream compaction above),
+//              which yields sorted[] (sorted -> old) and newidx[] (old -> sorted), and the
+//              density pass's processing order work[];
+//   gather   : every carried field is gathered through sorted[], bond partners and incoming
 //              bond owners are remapped through newidx[].
 #include <cuda/atomic>
 #include <cfloat>
@@ -37,21 +38,40 @@ __device__ __forceinline__ uint32_t cell_of(const DevParams& P, float4 p) {
     return (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
 }
 
+// Morton code of the 4x4x4 sub-cell holding a position inside its cell (2 bits per axis from
+// the fractional part of the cell coordinate).  Only the density pass's processing order uses
+// it, never a result.
+__device__ __forceinline__ uint32_t sub_of(const DevParams& P, float4 p) {
+    const float g[3] = {(p.x - P.gmin[0]) * P.gdelta[0], (p.y - P.gmin[1]) * P.gdelta[1],
+                        (p.z - P.gmin[2]) * P.gdelta[2]};
+    uint32_t code = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        int q = (int)((g[a] - floorf(g[a])) * 4.f);
+        q = q < 0 ? 0 : (q > 3 ? 3 : q);
+        code |= ((uint32_t)(q & 1) << a) | ((uint32_t)(q >> 1) << (3 + a));
+    }
+    return code;
+}
+
 // ---- insert -------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __restrict__ pos,
                                                 uint32_t* __restrict__ cell,
                                                 uint32_t* __restrict__ arank,
                                                 uint32_t* __restrict__ newidx,
                                                 uint32_t* __restrict__ count,
+                                                uint8_t* __restrict__ sub,
                                                 uint32_t* __restrict__ step) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) *step += 1u;  // step counter read by the later kernels of this step
     bool in = i < P.cap;
     uint32_t c = UNDEF;
     if (in) {
-        c = cell_of(P, pos[i]);
+        const float4 pi = pos[i];
+        c = cell_of(P, pi);
         cell[i] = c;
         newidx[i] = UNDEF;  // overwritten by the cell sort for particles inside the window
+        if (c != UNDEF) sub[i] = (uint8_t)sub_of(P, pi);
     }
     bool valid = in && c != UNDEF;
     unsigned active = __ballot_sync(0xffffffffu, valid);
@@ -68,7 +88,8 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
 
 void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
-    k_insert<<<blocks, 256, 0, st>>>(P, cur.pos, s.cell, s.arank, s.newidx, s.count, s.counters + 5);
+    k_insert<<<blocks, 256, 0, st>>>(P, cur.pos, s.cell, s.arank, s.newidx, s.count, s.sub,
+                                      s.counters + 5);
 }
 
 // ---- single-pass scan (decoupled look-back) ------------------------------------------------
@@ -186,48 +207,48 @@ void launch_place(const DevParams& P, const Scratch& s, cudaStream_t st) {
 }
 
 // ---- cell sort ------------------------------------------------------------------------------
-constexpr int CS_WARPS = 8;
-
-__global__ void __launch_bounds__(CS_WARPS * 32) k_cellsort(uint32_t cells,
-                                                            const uint32_t* __restrict__ count,
-                                                            const uint32_t* __restrict__ offset,
-                                                            uint32_t* __restrict__ order,
-                                                            uint32_t* __restrict__ newidx,
-                                                            uint32_t* __restrict__ big_list,
-                                                            uint32_t* __restrict__ big_count,
-                                                            uint32_t* __restrict__ err) {
-    __shared__ uint32_t sbuf[CS_WARPS][WARP_CELL_MAX];
-    const uint32_t w = threadIdx.x >> 5, lane = lane_id();
-    const uint32_t gw = blockIdx.x * CS_WARPS + w;
-    const uint32_t nw = gridDim.x * CS_WARPS;
-    for (uint32_t c0 = gw * 32; c0 < cells; c0 += nw * 32) {
-        uint32_t c = c0 + lane;
-        uint32_t n = c < cells ? count[c] : 0u;
-        uint32_t off = n ? offset[c] : 0u;
-        if (n == 1) newidx[order[off]] = off;
-        if (n > (uint32_t)WARP_CELL_MAX) {
-            uint32_t k = atomicAdd(big_count, 1u);
+// One thread per arrival slot s < nactive: particle x = order[s] of cell c counts the members
+// of c with a smaller index (its stable rank r) and the members whose (sub-cell code, index)
+// key is smaller (its rank w in the processing order).  Members are read in the same order by
+// every lane of a warp that shares the cell, so the loads broadcast.  Cells above
+// WARP_CELL_MAX particles go to the block tier through the big-cell list.
+__global__ void __launch_bounds__(256) k_cellsort(const uint32_t* __restrict__ cell,
+                                                  const uint32_t* __restrict__ count,
+                                                  const uint32_t* __restrict__ offset,
+                                                  const uint32_t* __restrict__ order,
+                                                  const uint8_t* __restrict__ sub,
+                                                  uint32_t* __restrict__ sorted,
+                                                  uint32_t* __restrict__ newidx,
+                                                  uint32_t* __restrict__ work,
+                                                  uint32_t* __restrict__ big_list,
+                                                  uint32_t* __restrict__ big_count,
+                                                  uint32_t* __restrict__ err,
+                                                  const uint32_t* __restrict__ nactive_p) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= *nactive_p) return;
+    const uint32_t x = order[s];
+    const uint32_t c = cell[x];
+    const uint32_t off = offset[c], n = count[c];
+    if (n > (uint32_t)WARP_CELL_MAX) {
+        if (s == off) {
+            const uint32_t k = atomicAdd(big_count, 1u);
             if (k < BIG_LIST_CAP) big_list[k] = c;
             else atomicOr(err, ERR_BIG_LIST_OVERFLOW);
         }
-        unsigned multi = __ballot_sync(0xffffffffu, n > 1 && n <= (uint32_t)WARP_CELL_MAX);
-        while (multi) {
-            int src = __ffs(multi) - 1;
-            multi &= multi - 1;
-            uint32_t cn = __shfl_sync(0xffffffffu, n, src);
-            uint32_t co = __shfl_sync(0xffffffffu, off, src);
-            for (uint32_t k = lane; k < cn; k += 32) sbuf[w][k] = order[co + k];
-            __syncwarp();
-            for (uint32_t k = lane; k < cn; k += 32) {
-                uint32_t x = sbuf[w][k];
-                uint32_t r = 0;
-                for (uint32_t m = 0; m < cn; m++) r += sbuf[w][m] < x ? 1u : 0u;
-                order[co + r] = x;
-                newidx[x] = co + r;
-            }
-            __syncwarp();
-        }
+        return;
     }
+    const uint32_t kx = sub[x];
+    uint32_t r = 0, w = 0;
+#pragma unroll 4
+    for (uint32_t m = 0; m < n; m++) {
+        const uint32_t xm = __ldg(order + off + m);
+        const uint32_t km = __ldg(sub + xm);
+        r += xm < x ? 1u : 0u;
+        w += (km < kx || (km == kx && xm < x)) ? 1u : 0u;
+    }
+    sorted[off + r] = x;
+    newidx[x] = off + r;
+    work[off + w] = off + r;
 }
 
 constexpr int BIG_THREADS = 512;
@@ -236,8 +257,10 @@ __global__ void __launch_bounds__(BIG_THREADS) k_cellsort_big(uint32_t cap,
                                                               const uint32_t* __restrict__ cell,
                                                               const uint32_t* __restrict__ count,
                                                               const uint32_t* __restrict__ offset,
-                                                              uint32_t* __restrict__ order,
+                                                              const uint32_t* __restrict__ order,
+                                                              uint32_t* __restrict__ sorted,
                                                               uint32_t* __restrict__ newidx,
+                                                              uint32_t* __restrict__ work,
                                                               const uint32_t* __restrict__ big_list,
                                                               const uint32_t* __restrict__ big_count) {
     extern __shared__ uint32_t sseg[];  // BLOCK_CELL_MAX entries
@@ -247,13 +270,14 @@ __global__ void __launch_bounds__(BIG_THREADS) k_cellsort_big(uint32_t cap,
     for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
         const uint32_t c = big_list[b];
         const uint32_t n = count[c], off = offset[c];
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) work[off + k] = off + k;
         if (n <= (uint32_t)BLOCK_CELL_MAX) {
             for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) sseg[k] = order[off + k];
             __syncthreads();
             for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
                 uint32_t x = sseg[k], r = 0;
                 for (uint32_t m = 0; m < n; m++) r += sseg[m] < x ? 1u : 0u;
-                order[off + r] = x;
+                sorted[off + r] = x;
                 newidx[x] = off + r;
             }
             __syncthreads();
@@ -274,7 +298,7 @@ __global__ void __launch_bounds__(BIG_THREADS) k_cellsort_big(uint32_t cap,
                 }
                 if (m) {
                     uint32_t r = running + before + (uint32_t)__popc(bal & ((1u << lane) - 1u));
-                    order[off + r] = i;
+                    sorted[off + r] = i;
                     newidx[i] = off + r;
                 }
                 running += tot;
@@ -285,15 +309,13 @@ __global__ void __launch_bounds__(BIG_THREADS) k_cellsort_big(uint32_t cap,
 }
 
 void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, cudaStream_t st) {
-    uint32_t groups = (P.cells + 31) / 32;
-    uint32_t blocks = (groups + CS_WARPS - 1) / CS_WARPS;
-    uint32_t maxb = (uint32_t)num_sms * 8;
-    if (blocks > maxb) blocks = maxb;
-    if (blocks == 0) blocks = 1;
-    k_cellsort<<<blocks, CS_WARPS * 32, 0, st>>>(P.cells, s.count, s.offset, s.order, s.newidx,
-                                                  s.big_list, s.counters + 1, s.counters + 2);
+    const uint32_t blocks = (P.cap + 255) / 256;
+    k_cellsort<<<blocks, 256, 0, st>>>(s.cell, s.count, s.offset, s.order, s.sub, s.sorted,
+                                        s.newidx, s.work, s.big_list, s.counters + 1,
+                                        s.counters + 2, s.counters + 3);
     k_cellsort_big<<<num_sms, BIG_THREADS, BLOCK_CELL_MAX * sizeof(uint32_t), st>>>(
-        P.cap, s.cell, s.count, s.offset, s.order, s.newidx, s.big_list, s.counters + 1);
+        P.cap, s.cell, s.count, s.offset, s.order, s.sorted, s.newidx, s.work, s.big_list,
+        s.counters + 1);
 }
 
 // ---- gather ---------------------------------------------------------------------------------
@@ -304,7 +326,7 @@ __device__ __forceinline__ uint32_t remap(uint32_t j, uint32_t cap, const uint32
 __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
                                                 const float* __restrict__ sconc, Carried D,
                                                 float* __restrict__ dconc,
-                                                const uint32_t* __restrict__ order,
+                                                const uint32_t* __restrict__ sorted,
                                                 const uint32_t* __restrict__ newidx,
                                                 const uint32_t* __restrict__ cell,
                                                 uint32_t* __restrict__ scell,
@@ -317,7 +339,7 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
     if (p >= cap) return;
     const uint32_t nact = *nactive_p;
     if (p < nact) {
-        const uint32_t i = order[p];
+        const uint32_t i = sorted[p];
         D.pos[p] = __ldg(S.pos + i);
         D.vel[p] = __ldg(S.vel + i);
         D.veval[p] = __ldg(S.veval + i);
@@ -375,7 +397,7 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
-    k_gather<<<blocks, 256, 0, st>>>(P, src, src_conc, dst, dst_conc, s.order, s.newidx, s.cell,
+    k_gather<<<blocks, 256, 0, st>>>(P, src, src_conc, dst, dst_conc, s.sorted, s.newidx, s.cell,
                                       s.scell, s.press, s.invdens, s.force, s.counters + 3);
 }
 
