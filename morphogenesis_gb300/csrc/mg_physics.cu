@@ -289,6 +289,17 @@ __device__ __forceinline__ float warp_max(float v) {
     for (int d = 16; d > 0; d >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, d));
     return v;
 }
+// List entries are sorted particle indices (< 2^31); the top bit marks the first entry of a
+// lane's list that lies in a new grid cell, where the per-cell partial sum is flushed.
+constexpr uint32_t LIST_CELL_START = 0x80000000u;
+
+// Squared distance with fused multiply-adds: within a few ulps of the reference expression,
+// used only to choose list candidates.
+__device__ __forceinline__ float approx_dsq(float4 a, float4 b) {
+    const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
 // Whether cell (cx, cy, cz) can hold a point of the box [b?0, b?1].  The cell's extent is
 // widened by 1% of a cell on each side, far more than the rounding of the cell hash, so a
 // point the hash put in this cell is never excluded.
@@ -344,6 +355,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
     if (F::DENS) R2 = fmaxf(R2, P.r2);
     if (F::DIFF || F::MEAN) R2 = fmaxf(R2, P.r2diff);
     const float Rf = sqrtf(R2) * 1.0001f + 1e-3f;  // conservative prefilter radius
+    const float R2s = R2 * 1.000004f;               // list threshold for the fused distance
     const float INF = __int_as_float(0x7f800000);
     const int g = P.gsrch;
     const int BIG = 1 << 30;
@@ -393,6 +405,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
                 const bool inw = ing && cx - win.x >= 0 && cx - win.x < g && cy - win.y >= 0 &&
                                  cy - win.y < g && cz - win.z >= 0 && cz - win.z < g;
                 if (!__any_sync(0xffffffffu, inw)) continue;
+                uint32_t mark = LIST_CELL_START;  // flags a lane's first neighbour in this cell
                 for (uint32_t base = 0; base < cnt; base += 32) {
                     const uint32_t kk = base + lane;
                     const bool valid = kk < cnt;
@@ -410,12 +423,28 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
                     __syncwarp();
                     const int ns = __popc(ball);
                     if (inw) {
-                        for (int tt = 0; tt < ns; tt++) {
-                            const float4 sp = s_sp[w][tt];
-                            const float dx = ip.x - sp.x, dy = ip.y - sp.y, dz = ip.z - sp.z;
-                            const float dsq = dx * dx + dy * dy + dz * dz;
-                            if (dsq < R2 && dsq > 0.f) {
-                                if (n < (uint32_t)NL_CAP) my[n * 32] = s_sq[w][tt];
+                        // Membership uses a fused-multiply-add distance with a slack of a few
+                        // ulps, so the list is a superset of the neighbours; the exact test is
+                        // made again when the list is evaluated.  Four survivors per iteration
+                        // keep four independent dependency chains in flight.
+                        int tt = 0;
+                        for (; tt + 4 <= ns; tt += 4) {
+                            float d[4];
+#pragma unroll
+                            for (int u = 0; u < 4; u++) d[u] = approx_dsq(ip, s_sp[w][tt + u]);
+#pragma unroll
+                            for (int u = 0; u < 4; u++)
+                                if (d[u] < R2s && d[u] > 0.f) {
+                                    if (n < (uint32_t)NL_CAP) my[n * 32] = s_sq[w][tt + u] | mark;
+                                    mark = 0u;
+                                    n++;
+                                }
+                        }
+                        for (; tt < ns; tt++) {
+                            const float d = approx_dsq(ip, s_sp[w][tt]);
+                            if (d < R2s && d > 0.f) {
+                                if (n < (uint32_t)NL_CAP) my[n * 32] = s_sq[w][tt] | mark;
+                                mark = 0u;
                                 n++;
                             }
                         }
@@ -440,16 +469,13 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
     float sum = 0.f;
     {
         float part = 0.f;
-        uint32_t curcell = UNDEF, nf = 0;
+        uint32_t nf = 0;
         for (uint32_t k = 0; k < n; k++) {
-            const uint32_t q = my[k * 32];
-            if (F::DENS) {
-                const uint32_t qc = scell[q];
-                if (qc != curcell) {  // flush the partial sum of the previous cell
-                    sum += part;
-                    part = 0.f;
-                    curcell = qc;
-                }
+            const uint32_t e = my[k * 32];
+            const uint32_t q = e & ~LIST_CELL_START;
+            if (F::DENS && (e & LIST_CELL_START)) {  // first neighbour of the next cell:
+                sum += part;                         // flush the previous cell's partial sum
+                part = 0.f;
             }
             const float4 jp = pos[q];
             const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
@@ -487,7 +513,8 @@ __global__ void __launch_bounds__(256) k_dens_ovf(
     uint32_t* __restrict__ fcount, const uint32_t* __restrict__ ovf,
     const uint32_t* __restrict__ ovf_count, DensExtra X) {
     using F = DF<FLAGS>;
-    const uint32_t lane = threadIdx.x & 31u, t = lane & 15u;
+    __shared__ float4 s_cj[256 / 32][32][NTF / 4];  // concentrations of this batch's neighbours
+    const uint32_t lane = threadIdx.x & 31u, t = lane & 15u, wl = threadIdx.x >> 5;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     uint32_t nq = *ovf_count;
@@ -519,6 +546,12 @@ __global__ void __launch_bounds__(256) k_dens_ovf(
                     dsq = dx * dx + dy * dy + dz * dz;
                 }
                 unsigned hits = __ballot_sync(0xffffffffu, valid && dsq < R2 && dsq > 0.f);
+                if ((F::DIFF || F::MEAN) && ((hits >> lane) & 1u) && dsq < P.r2diff) {
+                    const float4* c4 = reinterpret_cast<const float4*>(conc_in + (size_t)(off + b + lane) * NTF);
+#pragma unroll
+                    for (int k = 0; k < NTF / 4; k++) s_cj[wl][lane][k] = c4[k];
+                }
+                __syncwarp();
                 while (hits) {
                     const int src = __ffs(hits) - 1;
                     hits &= hits - 1;
@@ -530,13 +563,14 @@ __global__ void __launch_bounds__(256) k_dens_ovf(
                     }
                     if (F::DENS && d < P.r2) part += wendland_term(d, P.sr);
                     if ((F::DIFF || F::MEAN) && d < P.r2diff) {
-                        const float cj = conc_in[(size_t)q * NTF + t];
+                        const float cj = reinterpret_cast<const float*>(s_cj[wl][src])[t];
                         if (F::MEAN) ms_t += cj;
                         if (F::DIFF && plain && dif_t != 0.f)
                             nc_t += (dif_t * ((P.r2diff - d) * P.d2)) * (cj - cur_t);
                         mcnt++;
                     }
                 }
+                __syncwarp();
             }
             if (F::DENS) sum += part;
         }
@@ -585,7 +619,7 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.counters + 3,   \
                                                              s.work, s.ovf, s.counters + 6, X);   \
-        k_dens_ovf<F><<<(uint32_t)num_sms * 2, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out,    \
+        k_dens_ovf<F><<<(uint32_t)num_sms * 4, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out,    \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.ovf,            \
