@@ -216,8 +216,13 @@ def surrogate_section(args, peak_tflops):
         fs.Run(5)
 
     def rel_err(a, b):
-        r = np.abs(a - b) / np.maximum(np.abs(b), 1e-6)
-        return {"median": float(np.median(r)), "p99": float(np.quantile(r, 0.99)), "max": float(r.max())}
+        # per particle: largest deviation over the largest plain concentration; and the
+        # relative L2 error over all particles and species
+        a = a.astype(np.float64)
+        b = b.astype(np.float64)
+        r = np.abs(a - b).max(1) / np.maximum(np.abs(b).max(1), 1e-30)
+        return {"median": float(np.median(r)), "p99": float(np.quantile(r, 0.99)), "max": float(r.max()),
+                "l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))}
 
     # one morphogen stage from the same state, surrogate alone (no judge)
     S.attach(sur, m, judge_period=0, judge_stride=0, threshold=1e-3)

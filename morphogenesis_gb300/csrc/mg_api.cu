@@ -73,6 +73,7 @@ struct mg_system {
     // learned morphogen surrogate (attached network is borrowed, not owned)
     mg::Mlp* sur = nullptr;
     __nv_bfloat16* feat = nullptr;   // [cap][48] surrogate inputs
+    float* feat_scale = nullptr;     // [cap] per-particle scale of the inputs
     float* conc_plain = nullptr;     // [cap][16] plain update of judged / handed-over particles
     uint32_t* sur_stats = nullptr;   // [0] judged, [1] handed over, [2] worst relative error bits
     uint32_t judge_period = 10, judge_stride = 64;
@@ -333,6 +334,7 @@ void enqueue_dens(mg_system* h, int flags, bool prof) {
 void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof) {
     DensExtra X{};
     X.feat = h->feat;
+    X.feat_scale = h->feat_scale;
     X.conc_plain = h->conc_plain;
     X.step = h->s.counters + 5;
     X.judge_period = h->judge_period;
@@ -344,7 +346,8 @@ void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof) {
                   h->search, h->num_sms, h->stream, &X); }
     if (h->search) h->flist_valid = true;
     { Mark m(h, prof, "mlp_infer");
-      launch_mlp_infer(h->sur, h->feat, conc_of(h, cin), h->conc_plain, conc_of(h, cout),
+      // conc_out holds the diffused concentrations; the network adds the reaction increment
+      launch_mlp_infer(h->sur, h->feat, h->feat_scale, conc_of(h, cout), h->conc_plain, conc_of(h, cout),
                        h->set[h->cur].genes, h->s.counters + 3, 0, h->s.counters + 5, h->judge_period,
                        h->judge_stride, h->judge_threshold, h->sur_stats, h->s.counters + 2,
                        h->num_sms, h->stream); }
@@ -664,6 +667,7 @@ mg_status mg_destroy(mg_handle h) {
     if (h->staging) cudaFree(h->staging);
     if (h->dense) cudaFree(h->dense);
     if (h->feat) cudaFree(h->feat);
+    if (h->feat_scale) cudaFree(h->feat_scale);
     if (h->conc_plain) cudaFree(h->conc_plain);
     if (h->sur_stats) cudaFree(h->sur_stats);
     if (h->arena) cudaFree(h->arena);
@@ -1189,7 +1193,7 @@ mg_status mg_mlp_infer(mg_mlp m, const float* x, uint32_t n, float* y) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess) {
-        mg::launch_mlp_infer(&m->m, feat, cin, nullptr, cout, nullptr, nullptr, n, nullptr, 0, 0, 0.f,
+        mg::launch_mlp_infer(&m->m, feat, nullptr, cin, nullptr, cout, nullptr, nullptr, n, nullptr, 0, 0, 0.f,
                              nullptr, err, sms, m->st);
         e = cudaGetLastError();
     }
@@ -1293,6 +1297,7 @@ mg_status mg_set_surrogate(mg_handle h, mg_mlp m, uint32_t judge_period, uint32_
     }
     if (!h->feat) {
         cudaError_t e = cudaMalloc(&h->feat, sizeof(__nv_bfloat16) * (size_t)h->cap * mg::MLP_IN);
+        if (e == cudaSuccess) e = cudaMalloc(&h->feat_scale, 4ull * h->cap);
         if (e == cudaSuccess) e = cudaMalloc(&h->conc_plain, 4ull * h->cap * NTF);
         if (e == cudaSuccess) e = cudaMalloc(&h->sur_stats, 16);
         if (e != cudaSuccess) return fail(h, MG_ERR_OOM, "surrogate buffers");

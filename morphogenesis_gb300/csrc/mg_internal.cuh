@@ -139,10 +139,15 @@ void launch_gather(const DevParams& P, const Carried& src, const float* src_conc
 // training pairs, 32 judge (plain update of sampled / handed-over particles into conc_plain).
 // search: 0 direct walk, 1 warp-cooperative.
 // Optional outputs of the density pass besides pressure/density/concentrations.
+// Surrogate inputs are scale-free: a particle's diffused and neighbour-mean concentrations are
+// divided by its scale s = max_t |c_t| (after diffusion), and the network predicts the reaction
+// increment divided by s.  The reaction is linear in the concentrations, so this keeps the
+// relative error of the prediction independent of how far the concentrations have decayed.
 struct DensExtra {
     __nv_bfloat16* feat;       // FEATURES: surrogate inputs [cap][48] bf16
+    float* feat_scale;         // FEATURES: the particle's scale s [cap]
     float* cap_x;              // CAPTURE: dataset features [..][48] for particle 0 of this pass
-    float* cap_y;              // CAPTURE: dataset targets (morphogen increment) [..][16]
+    float* cap_y;              // CAPTURE: dataset targets (reaction increment / s) [..][16]
     float* conc_plain;         // JUDGE: plain update of judged / handed-over particles
     const uint32_t* step;      // JUDGE: device step counter
     uint32_t judge_period, judge_stride;

@@ -237,7 +237,10 @@ __global__ void k_col_stats(const float* __restrict__ d, uint64_t rows, int cols
 // =============================================================================================
 // Inference on tcgen05
 // =============================================================================================
-constexpr int INF_THREADS = 128;  // four warps: warp w owns TMEM lanes 32w..32w+31 (tile rows)
+// Eight warps, two CTAs per SM.  Warp w reads TMEM lanes 32(w%4)..32(w%4)+31 (its tile rows)
+// and, in the hidden-layer epilogues, columns 64(w/4)..64(w/4)+63.
+constexpr int INF_THREADS = 256;
+constexpr int INF_CTAS_PER_SM = 2;
 constexpr int INF_TMEM_COLS = 256;
 constexpr uint32_t MBAR_SPIN_LIMIT = 1u << 24;
 
@@ -373,9 +376,10 @@ __device__ __forceinline__ void issue_layer(uint32_t d_tmem, const bf16* a, cons
 // Surrogate step: for each particle p < nactive, conc_out[p] = conc_in[p] + MLP(features[p]).
 // Particles under judgement (sampled this step) or already handed to the plain method
 // (bit 31 of their gene word) compare against / take the plain update in conc_plain.
-__global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
-    InferWeights W, const bf16* __restrict__ feat, const float* __restrict__ conc_in,
-    const float* __restrict__ conc_plain, float* __restrict__ conc_out, uint32_t* __restrict__ genes,
+__global__ void __launch_bounds__(INF_THREADS, INF_CTAS_PER_SM) k_mlp_infer(
+    InferWeights W, const bf16* __restrict__ feat, const float* __restrict__ feat_scale,
+    const float* conc_in,
+    const float* __restrict__ conc_plain, float* conc_out, uint32_t* __restrict__ genes,
     const uint32_t* __restrict__ nactive_p, uint32_t ntotal_override, const uint32_t* __restrict__ step_p,
     uint32_t judge_period, uint32_t judge_stride, float threshold, uint32_t* __restrict__ stats,
     uint32_t* __restrict__ err) {
@@ -421,20 +425,22 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = S.tmem_base;
-    const uint32_t lane_addr = tmem + ((warp * 32u) << 16);  // this warp's TMEM lanes
+    const uint32_t quad = warp & 3u, half = warp >> 2;
+    const uint32_t lane_addr = tmem + ((quad * 32u) << 16);  // this warp's TMEM lanes
+    const uint32_t row = quad * 32u + (tid & 31u);           // tile row = this thread's particle
     uint32_t phase = 0;
     bool ok = true;
 
     const uint32_t ntiles = (n + 127) / 128;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const uint32_t row = tid;  // tile row = this thread's particle
         const uint32_t p = tile * 128u + row;
         const bool live = p < n;
-        // layer-1 operand: the particle's 48 bf16 features (zeros past the end)
+        // layer-1 operand: the particle's 48 bf16 features (zeros past the end), three of the
+        // six 16-byte chunks per thread
         {
             const uint4* src = reinterpret_cast<const uint4*>(feat + (size_t)p * MLP_IN);
 #pragma unroll
-            for (uint32_t c = 0; c < MLP_IN / 8; c++) {
+            for (uint32_t c = half * 3; c < half * 3 + 3; c++) {
                 const uint4 v = live ? src[c] : make_uint4(0u, 0u, 0u, 0u);
                 *reinterpret_cast<uint4*>(S.a1 + core_offset(row, c * 8, MLP_IN)) = v;
             }
@@ -453,7 +459,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         tc_fence_after();
         // layer-1 epilogue: bias + GELU -> layer-2 operand
 #pragma unroll
-        for (uint32_t c0 = 0; c0 < MLP_H; c0 += 32) {
+        for (uint32_t c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
             float v[32];
             tmem_ld32(lane_addr + c0, v);
 #pragma unroll
@@ -479,7 +485,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         // layer-2 epilogue -> layer-3 operand.  The barrier fired, so the layer-2 MMAs have
         // finished reading a2 and it can be overwritten.
 #pragma unroll
-        for (uint32_t c0 = 0; c0 < MLP_H; c0 += 32) {
+        for (uint32_t c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
             float v[32];
             tmem_ld32(lane_addr + 128 + c0, v);
 #pragma unroll
@@ -502,19 +508,20 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         phase ^= 1u;
         if (!ok) break;
         tc_fence_after();
-        {
+        if (half == 0) {
             float d[16];
             tmem_ld16(lane_addr + 0, d);
             if (live) {
                 const float4* ci = reinterpret_cast<const float4*>(conc_in + (size_t)p * NTF);
+                const float sc = feat_scale ? feat_scale[p] : 1.f;  // inputs' per-particle scale
                 float c[16];
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     const float4 x = ci[k];
-                    c[4 * k] = x.x + (d[4 * k] + S.b3[4 * k]);
-                    c[4 * k + 1] = x.y + (d[4 * k + 1] + S.b3[4 * k + 1]);
-                    c[4 * k + 2] = x.z + (d[4 * k + 2] + S.b3[4 * k + 2]);
-                    c[4 * k + 3] = x.w + (d[4 * k + 3] + S.b3[4 * k + 3]);
+                    c[4 * k] = x.x + sc * (d[4 * k] + S.b3[4 * k]);
+                    c[4 * k + 1] = x.y + sc * (d[4 * k + 1] + S.b3[4 * k + 1]);
+                    c[4 * k + 2] = x.z + sc * (d[4 * k + 2] + S.b3[4 * k + 2]);
+                    c[4 * k + 3] = x.w + sc * (d[4 * k + 3] + S.b3[4 * k + 3]);
                 }
                 if (genes) {
                     const uint32_t gw = genes[p];
@@ -530,12 +537,15 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
                         }
                         bool take = fallback;
                         if (judged && !fallback) {
-                            float worst = 0.f;
+                            // relative error of the particle: largest deviation over the
+                            // largest plain concentration
+                            float dev = 0.f, mag = 0.f;
 #pragma unroll
                             for (int t = 0; t < 16; t++) {
-                                const float e = fabsf(c[t] - pl[t]) / fmaxf(fabsf(pl[t]), 1e-6f);
-                                worst = fmaxf(worst, e);
+                                dev = fmaxf(dev, fabsf(c[t] - pl[t]));
+                                mag = fmaxf(mag, fabsf(pl[t]));
                             }
+                            const float worst = dev / fmaxf(mag, 1e-30f);
                             atomicAdd(&stats[0], 1u);
                             atomicMax(&stats[2], __float_as_uint(worst));
                             if (!(worst <= threshold)) {  // hand the particle to the plain method
@@ -854,12 +864,14 @@ cudaError_t mlp_grad(Mlp* m, const float* dx, const float* dy, uint32_t n, float
     return cudaSuccess;
 }
 
-void launch_mlp_infer(const Mlp* m, const bf16* feat, const float* conc_in, const float* conc_plain,
+void launch_mlp_infer(const Mlp* m, const bf16* feat, const float* feat_scale, const float* conc_in,
+                      const float* conc_plain,
                       float* conc_out, uint32_t* genes, const uint32_t* nactive, uint32_t n_override,
                       const uint32_t* step, uint32_t period, uint32_t stride, float threshold,
                       uint32_t* stats, uint32_t* err, int num_sms, cudaStream_t st) {
-    k_mlp_infer<<<num_sms, INF_THREADS, sizeof(InferSmem), st>>>(
-        m->inf, feat, conc_in, conc_plain, conc_out, genes, nactive, n_override, step, period, stride,
+    k_mlp_infer<<<num_sms * INF_CTAS_PER_SM, INF_THREADS, sizeof(InferSmem), st>>>(
+        m->inf, feat, feat_scale, conc_in, conc_plain, conc_out, genes, nactive, n_override, step,
+        period, stride,
         threshold, stats, err);
 }
 

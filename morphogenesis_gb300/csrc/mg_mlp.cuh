@@ -40,13 +40,24 @@ __host__ __device__ __forceinline__ uint32_t core_offset(uint32_t row, uint32_t 
     return (((row >> 3) * (K >> 3) + (k >> 3)) << 6) + ((row & 7u) << 3) + (k & 7u);
 }
 
+// GELU in its tanh form (Hendrycks & Gimpel): 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))),
+// with the hardware tanh approximation (relative error below 2^-10, under the bf16 rounding
+// the activations get anyway).
+__device__ __forceinline__ float tanh_hw(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+constexpr float GELU_K0 = 0.7978845608028654f;  // sqrt(2/pi)
+constexpr float GELU_K1 = 0.044715f;
 __device__ __forceinline__ float gelu(float x) {
-    return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+    const float u = GELU_K0 * (x + GELU_K1 * x * x * x);
+    return 0.5f * x * (1.0f + tanh_hw(u));
 }
 __device__ __forceinline__ float gelu_grad(float x) {
-    const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
-    const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
-    return cdf + x * pdf;
+    const float u = GELU_K0 * (x + GELU_K1 * x * x * x);
+    const float t = tanh_hw(u);
+    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * GELU_K0 * (1.0f + 3.0f * GELU_K1 * x * x);
 }
 
 // ---- training (mma.sync) ----------------------------------------------------------------
@@ -98,7 +109,8 @@ cudaError_t mlp_train(Mlp* m, const float* dx, const float* dy, uint64_t rows, u
                       uint32_t batch, float lr, uint64_t seed, float* loss_host);
 cudaError_t mlp_grad(Mlp* m, const float* dx, const float* dy, uint32_t n, float* grads_host,
                      double* loss);
-void launch_mlp_infer(const Mlp* m, const __nv_bfloat16* feat, const float* conc_in,
+void launch_mlp_infer(const Mlp* m, const __nv_bfloat16* feat, const float* feat_scale,
+                      const float* conc_in,
                       const float* conc_plain, float* conc_out, uint32_t* genes,
                       const uint32_t* nactive, uint32_t n_override, const uint32_t* step,
                       uint32_t period, uint32_t stride, float threshold, uint32_t* stats,

@@ -85,9 +85,11 @@ __device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], c
 }
 
 
-// FLAGS: 1 density/pressure, 2 diffusion, 4 gene reaction, 8 surrogate features,
-// 16 capture of (features, plain increment) pairs, 32 judge (plain update only for the
-// particles sampled this step or handed to the plain method; results go to conc_plain).
+// FLAGS: 1 density/pressure, 2 diffusion (+ decay), 4 gene reaction, 8 surrogate features,
+// 16 capture of (features, reaction increment) pairs, 32 judge (the gene reaction runs only
+// for the particles sampled this step or handed to the plain method and its result goes to
+// conc_plain, while conc_out receives the diffused concentrations of every particle, to which
+// the surrogate adds its predicted reaction increment).
 template <int FLAGS>
 struct DF {
     static constexpr bool DENS = FLAGS & 1, DIFF = FLAGS & 2, GENE = FLAGS & 4, FEAT = FLAGS & 8,
@@ -164,19 +166,32 @@ __device__ __forceinline__ void dens_epilogue(const DevParams& P, const DevGenom
         invdens[p] = 1.f / sum;
     }
     const uint32_t gene_word = (F::GENE || F::MEAN || F::JUDGE) ? genes[p] : 0u;
+    if (!(F::DIFF || F::GENE || F::MEAN)) return;
+    // concentrations after diffusion and decay (the reaction's input)
+    float c[NTF];
+#pragma unroll
+    for (int t = 0; t < NTF; t++) c[t] = F::DIFF ? G->breakdown[t] * (cur[t] + nc[t]) : cur[t];
+    float inv_s = 0.f;
     if (F::MEAN) {
+        // surrogate inputs: the diffused concentrations and the neighbours' mean concentration,
+        // both divided by the particle's scale, and the gene bits
+        float sc = 0.f;
+#pragma unroll
+        for (int t = 0; t < NTF; t++) sc = fmaxf(sc, fabsf(c[t]));
+        inv_s = sc > 0.f ? 1.f / sc : 0.f;  // all-zero concentrations: zero inputs and increment
         float f[MLP_FEATURES];
         const float inv = mcnt ? 1.f / (float)mcnt : 0.f;
 #pragma unroll
         for (int t = 0; t < NTF; t++) {
-            f[t] = cur[t];
-            f[NTF + t] = mcnt ? ms[t] * inv : cur[t];
+            f[t] = c[t] * inv_s;
+            f[NTF + t] = (mcnt ? ms[t] * inv : cur[t]) * inv_s;
             f[2 * NTF + t] = (float)((gene_word >> t) & 1u);
         }
         if (F::FEAT) {
             __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(X.feat + (size_t)p * MLP_FEATURES);
 #pragma unroll
             for (int t = 0; t < MLP_FEATURES / 2; t++) o[t] = __floats2bfloat162_rn(f[2 * t], f[2 * t + 1]);
+            X.feat_scale[p] = sc;
         }
         if (F::CAPTURE) {
             float4* o = reinterpret_cast<float4*>(X.cap_x + (size_t)p * MLP_FEATURES);
@@ -184,51 +199,56 @@ __device__ __forceinline__ void dens_epilogue(const DevParams& P, const DevGenom
             for (int k = 0; k < MLP_FEATURES / 4; k++) o[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
         }
     }
-    if ((F::DIFF || F::GENE) && plain) {
-        float c[NTF];
+    if (F::JUDGE) {  // every particle: diffused concentrations, the surrogate adds the reaction
+        float4* o4 = reinterpret_cast<float4*>(conc_out + (size_t)p * NTF);
 #pragma unroll
-        for (int t = 0; t < NTF; t++) c[t] = F::DIFF ? G->breakdown[t] * (cur[t] + nc[t]) : cur[t];
-        if (F::GENE) {
-            // Gene bits are the sort-time dense-list membership (FEPIGEN > 0).  With every
-            // FEPIGEN in {0, INT_MAX} and no activation lists the countdown never fires and
-            // the reaction is: for each active gene g in order, activity = sum_tf sens*conc,
-            // secretion accumulates rate*activity; living particles (gene 2) add it.
-            const uint32_t bits = gene_word & 0xFFFFu;
-            float dc[NTF];
+        for (int k = 0; k < 4; k++) o4[k] = make_float4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
+    }
+    if (!F::GENE && !F::JUDGE) {  // diffusion only
+        float4* o4 = reinterpret_cast<float4*>(conc_out + (size_t)p * NTF);
 #pragma unroll
-            for (int t = 0; t < NTF; t++) dc[t] = 0.f;
-            for (int g = 0; g < NG; g++) {
-                if (!((bits >> g) & 1u)) continue;
-                float act = 0.f;
+        for (int k = 0; k < 4; k++) o4[k] = make_float4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
+    }
+    if (F::GENE && plain) {
+        // Gene bits are the sort-time dense-list membership (FEPIGEN > 0).  With every
+        // FEPIGEN in {0, INT_MAX} and no activation lists the countdown never fires and
+        // the reaction is: for each active gene g in order, activity = sum_tf sens*conc,
+        // secretion accumulates rate*activity; living particles (gene 2) add it.
+        const uint32_t bits = gene_word & 0xFFFFu;
+        float dc[NTF];
 #pragma unroll
-                for (int t = 0; t < NTF; t++) {
-                    const float s = G->sens[g][t];
-                    if (s != 0.f) act += s * c[t];
-                }
-                const int ns = G->nsec[g];
-                for (int k = 0; k < ns; k++) {
-                    const int tf = G->sec_tf[g][k];
-                    const float v = G->sec_rate[g][k] * act;
+        for (int t = 0; t < NTF; t++) dc[t] = 0.f;
+        for (int g = 0; g < NG; g++) {
+            if (!((bits >> g) & 1u)) continue;
+            float act = 0.f;
 #pragma unroll
-                    for (int t = 0; t < NTF; t++)
-                        if (t == tf) dc[t] += v;
-                }
+            for (int t = 0; t < NTF; t++) {
+                const float sv = G->sens[g][t];
+                if (sv != 0.f) act += sv * c[t];
             }
-            if (bits & 4u) {
+            const int ns = G->nsec[g];
+            for (int k = 0; k < ns; k++) {
+                const int tf = G->sec_tf[g][k];
+                const float v = G->sec_rate[g][k] * act;
 #pragma unroll
-                for (int t = 0; t < NTF; t++) c[t] += dc[t];
+                for (int t = 0; t < NTF; t++)
+                    if (t == tf) dc[t] += v;
             }
         }
+        float cf[NTF];
+#pragma unroll
+        for (int t = 0; t < NTF; t++) cf[t] = (bits & 4u) ? c[t] + dc[t] : c[t];
         float* dst = F::JUDGE ? X.conc_plain : conc_out;
         float4* o4 = reinterpret_cast<float4*>(dst + (size_t)p * NTF);
 #pragma unroll
-        for (int k = 0; k < 4; k++) o4[k] = make_float4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
+        for (int k = 0; k < 4; k++) o4[k] = make_float4(cf[4 * k], cf[4 * k + 1], cf[4 * k + 2], cf[4 * k + 3]);
         if (F::CAPTURE) {
             float4* y4 = reinterpret_cast<float4*>(X.cap_y + (size_t)p * NTF);
 #pragma unroll
             for (int k = 0; k < 4; k++)
-                y4[k] = make_float4(c[4 * k] - cur[4 * k], c[4 * k + 1] - cur[4 * k + 1],
-                                    c[4 * k + 2] - cur[4 * k + 2], c[4 * k + 3] - cur[4 * k + 3]);
+                y4[k] = make_float4((cf[4 * k] - c[4 * k]) * inv_s, (cf[4 * k + 1] - c[4 * k + 1]) * inv_s,
+                                    (cf[4 * k + 2] - c[4 * k + 2]) * inv_s,
+                                    (cf[4 * k + 3] - c[4 * k + 3]) * inv_s);
         }
     }
 }
@@ -274,7 +294,7 @@ __global__ void __launch_bounds__(256) k_dens(DevParams P, const DevGenome* __re
     float sum = 0.f;
     if (F::DENS || F::DIFF || F::MEAN)
         sum = dens_direct<FLAGS>(P, pos[p], scell[p], pos, conc_in, count, offset, nc, ms, mcnt, dif,
-                                 cur, plain);
+                                 cur, true);
     dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press, invdens, X);
 }
 
@@ -487,7 +507,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
             if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
             if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
                 conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2,
-                                             P.uniform_diff != 0, plain);
+                                             P.uniform_diff != 0, true);
                 mcnt++;
             }
         }
@@ -565,7 +585,7 @@ __global__ void __launch_bounds__(256) k_dens_ovf(
                     if ((F::DIFF || F::MEAN) && d < P.r2diff) {
                         const float cj = reinterpret_cast<const float*>(s_cj[wl][src])[t];
                         if (F::MEAN) ms_t += cj;
-                        if (F::DIFF && plain && dif_t != 0.f)
+                        if (F::DIFF && dif_t != 0.f)
                             nc_t += (dif_t * ((P.r2diff - d) * P.d2)) * (cj - cur_t);
                         mcnt++;
                     }

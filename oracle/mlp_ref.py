@@ -21,7 +21,6 @@ P_W3 = P_B2 + H
 P_B3 = P_W3 + OUT * H
 P_COUNT = P_B3 + OUT
 
-_erf = np.vectorize(math.erf)
 
 
 def bf16(x) -> np.ndarray:
@@ -34,14 +33,18 @@ def bf16(x) -> np.ndarray:
     return out.astype(np.float64)
 
 
+K0 = math.sqrt(2.0 / math.pi)
+K1 = 0.044715
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    """GELU, tanh form (the device evaluates tanh with the hardware approximation)."""
+    return 0.5 * z * (1.0 + np.tanh(K0 * (z + K1 * z ** 3)))
 
 
 def gelu_grad(z):
-    cdf = 0.5 * (1.0 + _erf(z / math.sqrt(2.0)))
-    pdf = np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
-    return cdf + z * pdf
+    t = np.tanh(K0 * (z + K1 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * K0 * (1.0 + 3.0 * K1 * z * z)
 
 
 def unpack(p):
