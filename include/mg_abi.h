@@ -213,6 +213,14 @@ mg_status mg_advance(mg_handle h);              /* AdvanceCL + AdvanceTime, host
 mg_status mg_run_physical_sort(mg_handle h);        /* Run2PhysicalSort */
 mg_status mg_run_inner_physical_loop(mg_handle h);  /* Run2InnerPhysicalLoop */
 mg_status mg_run_gene_action(mg_handle h);          /* Run2GeneAction */
+/* Run2Remodelling (fluid_system.cpp:2037): re-forms broken bonds on the sorted state, after a
+ * force pass and before integration.  Deterministic restatement of heal's bond-0 rule
+ * (fluid_system_cuda.cu:1938-1975, 2047-2105, makeBond :1573-1593): each particle with a broken
+ * bond proposes, for its lowest broken slot, the nearest particle within h that is not a
+ * boundary marker, not already its partner and has a free incoming slot (ties: lower index);
+ * proposals are accepted in (distance, index) order; the new bond has rest length = distance,
+ * elastic limit 1.5 x rest length, the broken slot's modulus and damping. */
+mg_status mg_run_remodelling(mg_handle h);
 /* nsteps full steps in the legacy Run() order (fluid_system.cpp:1179-1349), one sort per
  * step: insert, scan, sort, pressure, force, diffusion, genes, [remodel], advance, time. */
 mg_status mg_step(mg_handle h, uint32_t nsteps, uint32_t flags);

@@ -206,6 +206,7 @@ class FluidSystem:
     def Run2PhysicalSort(self) -> None: self._check(self.lib.mg_run_physical_sort(self.h))
     def Run2InnerPhysicalLoop(self) -> None: self._check(self.lib.mg_run_inner_physical_loop(self.h))
     def Run2GeneAction(self) -> None: self._check(self.lib.mg_run_gene_action(self.h))
+    def Run2Remodelling(self) -> None: self._check(self.lib.mg_run_remodelling(self.h))
 
     def Run(self, nsteps: int = 1, flags: int = A.STEP_DEFAULT) -> None:
         """nsteps steps in the legacy Run() order (one sort per step), graph-captured."""

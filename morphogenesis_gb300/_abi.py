@@ -139,6 +139,7 @@ SIGNATURES = [
                                   C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     ("mg_algorithmic_bytes", C.c_int, [H, C.c_char_p, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("mg_kernel_launches", C.c_uint64, [H]),
+    ("mg_run_remodelling", C.c_int, [H]),
     ("mg_prefix_sum_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
 

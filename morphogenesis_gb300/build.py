@@ -29,6 +29,7 @@ UNITS = {
     "mg_mlp.cu": [],
     "mg_api.cu": [],
     "mg_noalloc.cu": [],
+    "mg_remodel.cu": ["-fmad=false"],
 }
 
 

@@ -368,9 +368,17 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
     }
     int dflags = ((flags & MG_STEP_PHYSICS) ? 1 : 0) | ((flags & MG_STEP_GENES) ? 6 : 0);
     if (dflags) enqueue_dens(h, dflags, prof);
+    const bool remodel = (flags & MG_STEP_REMODEL) != 0;
     if (flags & MG_STEP_PHYSICS) {
         { Mark m(h, prof, "force"); launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream); }
-        { Mark m(h, prof, "advance"); launch_advance(h->P, h->set[h->cur], h->s, true, h->stream); }
+    }
+    if (remodel) {  // Run2Remodelling, after the gene action and before AdvanceCL
+        Mark m(h, prof, "remodel");
+        if (flags & MG_STEP_PHYSICS) launch_apply_breaks(h->P, h->set[h->cur], h->s, h->stream);
+        launch_remodel(h->P, h->set[h->cur], h->cold, h->s, h->stream);
+    }
+    if (flags & MG_STEP_PHYSICS) {
+        { Mark m(h, prof, "advance"); launch_advance(h->P, h->set[h->cur], h->s, !remodel, h->stream); }
         h->flist_valid = false;
     }
 }
@@ -381,6 +389,7 @@ int kernels_per_step(const mg_system* h, uint32_t flags) {
     if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE)) n += h->search ? 2 : 1;
     if (flags & MG_STEP_SURROGATE) n += 1;
     if (flags & MG_STEP_PHYSICS) n += 2;
+    if (flags & MG_STEP_REMODEL) n += (flags & MG_STEP_PHYSICS) ? 4 : 3;
     return n;
 }
 
@@ -414,8 +423,8 @@ mg_status get_graph(mg_system* h, uint32_t flags, cudaGraphExec_t* out) {
 }
 
 mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
-    if (flags & MG_STEP_REMODEL)
-        return fail(h, MG_ERR_UNSUPPORTED, "remodelling steps are not built");
+    if ((flags & MG_STEP_REMODEL) && (flags & MG_STEP_SURROGATE))
+        return fail(h, MG_ERR_UNSUPPORTED, "remodelling together with the surrogate step is not built");
     if ((flags & MG_STEP_SURROGATE) && !h->sur)
         return fail(h, MG_ERR_INVALID_ARG, "surrogate step without an attached network (mg_set_surrogate)");
     for (uint32_t s = 0; s < nsteps; s++) {
@@ -611,6 +620,9 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     plan.push_back({(void**)&h->s.work, 4 * n});
     plan.push_back({(void**)&h->s.sub, n});
     plan.push_back({(void**)&h->s.ovf, 4 * n});
+    plan.push_back({(void**)&h->s.freemask, n});
+    plan.push_back({(void**)&h->s.prop, 4 * n});
+    plan.push_back({(void**)&h->s.propd, 4 * n});
     plan.push_back({(void**)&h->s.newidx, 4 * n});
     plan.push_back({(void**)&h->s.scell, 4 * n});
     plan.push_back({(void**)&h->s.press, 4 * n});
@@ -964,6 +976,13 @@ mg_status mg_advance(mg_handle h) {
     launch_advance(h->P, h->set[h->cur], h->s, false, h->stream);
     h->flist_valid = false;
     h->time = h->time + h->P.dt;
+    return check_device(h);
+}
+
+mg_status mg_run_remodelling(mg_handle h) {
+    mg_status st = need_sorted(h);
+    if (st != MG_OK) return st;
+    launch_remodel(h->P, h->set[h->cur], h->cold, h->s, h->stream);
     return check_device(h);
 }
 

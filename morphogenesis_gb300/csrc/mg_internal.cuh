@@ -121,6 +121,9 @@ struct Scratch {
                         // [3] nactive, [5] step counter (incremented by insert),
                         // [6] density-pass overflow queue length
     uint32_t* ovf;      // [cap] particles whose neighbours overflow a lane's list
+    uint8_t* freemask;  // [cap] remodelling: free incoming slots
+    uint32_t* prop;     // [cap] remodelling: proposed partner
+    float* propd;       // [cap] remodelling: its squared distance
     uint32_t* big_list; // [BIG_LIST_CAP] cells that need the block-level ordering
 };
 
@@ -159,6 +162,9 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
 void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool use_list,
                   cudaStream_t st);
 void launch_apply_breaks(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
+// re-forming of broken bonds on the sorted state, breaks already applied (D5)
+void launch_remodel(const DevParams& P, const Carried& cur, const Cold& cold, const Scratch& s,
+                    cudaStream_t st);
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_breaks,
                     cudaStream_t st);
 

@@ -844,6 +844,111 @@ void mgo_advance(mgo_handle h) {
     h->P.time = h->P.time + dt; /* AdvanceTime (fluid_system.cpp:2016) */
 }
 
+/* ---- a11 (D5): re-forming of broken bonds ---------------------------------------------------
+ * Deterministic restatement of heal's bond-0 rule (contribFindBonds theta = dsq, cuda:1938-1975;
+ * heal cuda:2047-2105 without the curand jitter of cuda:2066-2071; makeBond cuda:1573-1593):
+ *  - a slot is broken when its partner is an active particle and its rest length failed the
+ *    computeForce rest-length test (cuda:3268; breaks set the rest length to 0, cuda:3316);
+ *  - each particle with a broken slot proposes, for its lowest broken slot, the nearest particle
+ *    j within h (dsq < rd2, dsq > 0) that is not a boundary marker (particle id 0, cuda:1950),
+ *    is not already the partner of any of its slots (cuda:1960) and has a free incoming slot
+ *    (fewer than six live incoming bonds); ties go to the lower sorted index;
+ *  - every particle accepts proposals in (distance, index) order into its free incoming slots,
+ *    in slot order; the others retry on a later step;
+ *  - the new bond: rest length = current distance, elastic limit 1.5 x rest length (strain
+ *    0.5), modulus and damping kept from the broken slot, integrators and change word 0,
+ *    word 5 = the partner's particle id (makeBond's [5]). */
+static int rest_is_small(real r) { return (double)r < 0.000000001; }
+
+static int lowest_broken_slot(const mgo_handle h, uint32_t i, uint32_t n) {
+    for (int a = 0; a < NB; a++) {
+        const bond_t* b = &h->bond[(size_t)i * NB + a];
+        if (b->partner < n && rest_is_small(b->restlen)) return a;
+    }
+    return -1;
+}
+
+void mgo_remodel(mgo_handle h) {
+    const params_t* P = &h->P;
+    const uint32_t n = h->nactive;
+    if (n == 0) return;
+    unsigned char* freemask = (unsigned char*)calloc(n, 1);
+    uint32_t* prop = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    real* propd = (real*)malloc(sizeof(real) * n);
+    for (uint32_t j = 0; j < n; j++) {
+        unsigned m = 0;
+        for (int s = 0; s < NB; s++) {
+            uint32_t k = h->pidx[(size_t)j * 2 * NB + 2 * s], bk = h->pidx[(size_t)j * 2 * NB + 2 * s + 1];
+            int live = k < n && bk < NB && h->bond[(size_t)k * NB + bk].partner == j &&
+                       !rest_is_small(h->bond[(size_t)k * NB + bk].restlen);
+            if (!live) m |= 1u << s;
+        }
+        freemask[j] = (unsigned char)m;
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        prop[i] = MG_GRID_UNDEF;
+        propd[i] = 0;
+        if (h->gcell[i] == MG_GRID_UNDEF || lowest_broken_slot(h, i, n) < 0) continue;
+        const r4 ip = h->pos[i];
+        const uint32_t gc = h->gcell[i] - (uint32_t)P->nadj;
+        real best = 0;
+        uint32_t bj = MG_GRID_UNDEF;
+        for (int c = 0; c < P->adjcnt; c++) {
+            uint32_t cell = gc + (uint32_t)P->adj[c];
+            uint32_t clast = h->offset[cell] + h->count[cell];
+            for (uint32_t j = h->offset[cell]; j < clast; j++) {
+                real dx = ip.x - h->pos[j].x, dy = ip.y - h->pos[j].y, dz = ip.z - h->pos[j].z;
+                real dsq = dx * dx + dy * dy + dz * dz;
+                if (!(dsq < P->rd2 && dsq > (real)0)) continue;
+                if (h->pid[j] == 0 || freemask[j] == 0) continue;
+                int bonded = 0;
+                for (int a = 0; a < NB; a++) bonded |= h->bond[(size_t)i * NB + a].partner == j;
+                if (bonded) continue;
+                if (bj == MG_GRID_UNDEF || dsq < best) { best = dsq; bj = j; }
+            }
+        }
+        prop[i] = bj;
+        propd[i] = best;
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t j = prop[i];
+        if (j == MG_GRID_UNDEF) continue;
+        const real d = propd[i];
+        uint32_t rank = 0;
+        const uint32_t gc = h->gcell[j] - (uint32_t)P->nadj;
+        for (int c = 0; c < P->adjcnt; c++) {
+            uint32_t cell = gc + (uint32_t)P->adj[c];
+            uint32_t clast = h->offset[cell] + h->count[cell];
+            for (uint32_t q = h->offset[cell]; q < clast; q++)
+                if (prop[q] == j && (propd[q] < d || (propd[q] == d && q < i))) rank++;
+        }
+        unsigned m = freemask[j];
+        uint32_t r = rank;
+        int slot = -1;
+        for (int s = 0; s < NB; s++)
+            if ((m >> s) & 1u) {
+                if (r == 0) { slot = s; break; }
+                r--;
+            }
+        if (slot < 0) continue;
+        const int b = lowest_broken_slot(h, i, n);
+        bond_t* nb = &h->bond[(size_t)i * NB + b];
+        const real rest = RSQRT(d);
+        nb->partner = j;
+        nb->restlen = rest;
+        nb->elastlim = (real)1.5f * rest;
+        nb->pid = h->pid[j];
+        nb->sqint = 0;
+        nb->sint = 0;
+        nb->change = 0;
+        h->pidx[(size_t)j * 2 * NB + 2 * slot] = i;
+        h->pidx[(size_t)j * 2 * NB + 2 * slot + 1] = (uint32_t)b;
+    }
+    free(freemask);
+    free(prop);
+    free(propd);
+}
+
 /* ---- D6: one step in the legacy Run() order --------------------------------------------- */
 void mgo_step(mgo_handle h, uint32_t nsteps, uint32_t flags) {
     int saved_freeze = h->P.freeze;
@@ -860,6 +965,7 @@ void mgo_step(mgo_handle h, uint32_t nsteps, uint32_t flags) {
             mgo_compute_diffusion(h);
             mgo_compute_genes(h);
         }
+        if (flags & MG_STEP_REMODEL) mgo_remodel(h); /* Run2Remodelling, before AdvanceCL */
         if (flags & MG_STEP_PHYSICS) mgo_advance(h);
     }
     h->P.freeze = saved_freeze;

@@ -65,6 +65,7 @@ void mgo_compute_force(mgo_handle h);
 void mgo_compute_diffusion(mgo_handle h);
 void mgo_compute_genes(mgo_handle h);
 void mgo_advance(mgo_handle h);
+void mgo_remodel(mgo_handle h); /* D5 re-forming of broken bonds (Run2Remodelling) */
 /* nsteps steps in the legacy Run() order, flags as mg_step. */
 void mgo_step(mgo_handle h, uint32_t nsteps, uint32_t flags);
 

@@ -68,6 +68,7 @@ def lib(bits: int = 32) -> C.CDLL:
         "mgo_compute_diffusion": (None, [H]),
         "mgo_compute_genes": (None, [H]),
         "mgo_advance": (None, [H]),
+        "mgo_remodel": (None, [H]),
         "mgo_step": (None, [H, C.c_uint32, C.c_uint32]),
         "mgo_set_threads": (C.c_int, [C.c_int]),
     }
@@ -164,6 +165,7 @@ class Oracle:
     def diffusion(self): self.L.mgo_compute_diffusion(self.h)
     def genes(self): self.L.mgo_compute_genes(self.h)
     def advance(self): self.L.mgo_advance(self.h)
+    def remodel(self): self.L.mgo_remodel(self.h)
 
     def step(self, nsteps: int = 1, flags: int = A.STEP_DEFAULT) -> None:
         self.L.mgo_step(self.h, nsteps, flags)

@@ -259,3 +259,47 @@ def test_warp_search_equals_direct_walk(built, param):
     for b in outs[0]:
         for m in (1,):
             assert same_bits(outs[0][b].view(np.float32), outs[m][b].view(np.float32)), f"buffer {b} mode {m}"
+
+
+def test_remodelling_reforms_identically(built):
+    d = demo.make_block(10, "R", seed=4, breakable=True)
+    v = np.random.default_rng(4).uniform(-30, 30, (d.n, 4)).astype(np.float32)
+    v[:, 3] = 0
+    d.arrays[A.FVEL] = v
+    d.arrays[A.FVEVAL] = v.copy()
+    g, o = pair(d, d.n)
+    flags = A.STEP_DEFAULT | A.STEP_REMODEL
+    g.Run(40, flags)
+    o.step(40, flags)
+    assert compare(g, o), "remodelling run is not bitwise equal to the oracle"
+    plain = orc.Oracle(d.params, d.genome, d.n)
+    plain.upload_all(d.arrays)
+    plain.step(40)
+
+    def broken(x):
+        el = x.download(A.FELASTIDX).reshape(-1, 6, 9)
+        return int(((el[:, :, 0] != A.NO_PARTNER) & (el[:, :, 2] == 0)).sum())
+
+    assert broken(o) < broken(plain), "re-forming should leave fewer broken bonds"
+    plain.close()
+
+
+def test_remodelling_stage_matches_oracle(built):
+    q, p1, p2 = [C0, C0, C0], [C0 + 1.0, C0, C0], [C0 - 1.2, C0, C0]
+    rs = [[C0, C0 + 3.0, C0], [C0, C0 - 3.0, C0], [C0, C0, C0 + 3.0], [C0, C0, C0 - 3.0],
+          [C0, C0 + 2.2, C0 + 2.2]]
+    bonds = [(1, 0, 2, 0.0, 1000.0, 10.0, 5.0), (2, 0, 1, 0.0, 1000.0, 10.0, 5.0)]
+    bonds += [(3 + k, 0, 0, 3.0, 1000.0, 10.0, 9.0) for k in range(5)]
+    d, n = scene([q, p1, p2] + rs, bonds=bonds)
+    pidx = d.arrays[A.FPARTICLEIDX]
+    pidx[0, :] = A.NO_PARTNER
+    for k in range(5):
+        pidx[0, 2 * k] = 3 + k
+        pidx[0, 2 * k + 1] = 0
+    g, o = pair(d, n)
+    for _ in range(2):
+        g.Run2PhysicalSort()
+        g.Run2Remodelling()
+        o.insert(); o.prefix_sum(); o.sort(); o.remodel()
+        for b in (A.FELASTIDX, A.FPARTICLEIDX, A.FPARTICLE_ID):
+            assert np.array_equal(g.download(b), o.download(b)), f"buffer {b}"
