@@ -292,6 +292,18 @@ mg_status mg_algorithmic_bytes(mg_handle h, const char* kernel, uint32_t flags,
 /* Number of GPU kernels mg_step/mg_time_steps have launched on this handle. */
 uint64_t mg_kernel_launches(mg_handle h);
 
+/* ---- batched instances (parameter sweeps) --------------------------------------------------- */
+/* A batch steps many independent systems together (each keeps its own particles, grid,
+ * parameters and genome): one CUDA graph launch per step advances every member, the members'
+ * kernels running concurrently.  Members must live on one device, must not be profiling, and
+ * must outlive the batch; their own streams wait for the batch's steps. */
+typedef struct mg_batch_s* mg_batch;
+mg_status mg_batch_create(const mg_handle* members, uint32_t count, mg_batch* out);
+mg_status mg_batch_destroy(mg_batch b);
+mg_status mg_batch_step(mg_batch b, uint32_t nsteps, uint32_t flags);
+/* nsteps batch steps, device time of the whole run (CUDA events on the batch stream) */
+mg_status mg_batch_time_steps(mg_batch b, uint32_t nsteps, uint32_t flags, float* ms);
+
 /* ---- allocation-free prefix sum (no counterpart in the reference) ------------------------ */
 /* Largest n mg_prefix_sum_noalloc accepts: 16384 tiles of 4096 elements. */
 #define MG_NOALLOC_SCAN_MAX 67108864ull

@@ -248,3 +248,42 @@ class FluidSystem:
 
     def kernel_launches(self) -> int:
         return int(self.lib.mg_kernel_launches(self.h))
+
+
+class Batch:
+    """Independent systems stepped together: one graph launch per step advances every member
+    (parameter sweeps over tissue instances of different sizes, parameters and genomes)."""
+
+    def __init__(self, members):
+        self.lib = A.load()
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.h for m in self.members])
+        h = C.c_void_p()
+        st = self.lib.mg_batch_create(arr, len(self.members), C.byref(h))
+        if st != A.MG_OK:
+            raise A.MgError(st, (self.lib.mg_last_error(None) or b"").decode())
+        self.h = h
+
+    def _check(self, st):
+        if st != A.MG_OK:
+            raise A.MgError(st, (self.lib.mg_last_error(None) or b"").decode())
+
+    def Run(self, nsteps: int = 1, flags: int = A.STEP_DEFAULT) -> None:
+        self._check(self.lib.mg_batch_step(self.h, nsteps, flags))
+
+    def time_steps(self, nsteps: int, flags: int = A.STEP_DEFAULT) -> float:
+        ms = C.c_float()
+        self._check(self.lib.mg_batch_time_steps(self.h, nsteps, flags, C.byref(ms)))
+        return ms.value
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.mg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

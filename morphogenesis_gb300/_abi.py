@@ -140,6 +140,10 @@ SIGNATURES = [
     ("mg_algorithmic_bytes", C.c_int, [H, C.c_char_p, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("mg_kernel_launches", C.c_uint64, [H]),
     ("mg_run_remodelling", C.c_int, [H]),
+    ("mg_batch_create", C.c_int, [C.POINTER(H), C.c_uint32, C.POINTER(H)]),
+    ("mg_batch_destroy", C.c_int, [H]),
+    ("mg_batch_step", C.c_int, [H, C.c_uint32, C.c_uint32]),
+    ("mg_batch_time_steps", C.c_int, [H, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]),
     ("mg_prefix_sum_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
 

@@ -85,6 +85,17 @@ struct mg_mlp_s {
     cudaStream_t st;
 };
 
+// A batch of independent systems stepped together: one CUDA graph per (flags, buffer states)
+// holds every member's captured step as an independent child graph, so one launch advances all
+// members and the GPU runs their kernels concurrently.
+struct mg_batch_s {
+    std::vector<mg_system*> hs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    std::map<std::string, cudaGraphExec_t> graphs;
+    std::string err;
+};
+
 struct mg_dataset_s {
     float* dx = nullptr;  // [capacity][48] raw features
     float* dy = nullptr;  // [capacity][16] morphogen increments
@@ -357,18 +368,13 @@ void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof) {
 void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
     enqueue_insert_rank(h, prof);
     enqueue_gather(h, prof);
+    const bool remodel = (flags & MG_STEP_REMODEL) != 0;
     if (flags & MG_STEP_SURROGATE) {
         enqueue_surrogate_morphogen(h, (flags & MG_STEP_PHYSICS) != 0, prof);
-        if (flags & MG_STEP_PHYSICS) {
-            { Mark m(h, prof, "force"); launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream); }
-            { Mark m(h, prof, "advance"); launch_advance(h->P, h->set[h->cur], h->s, true, h->stream); }
-            h->flist_valid = false;
-        }
-        return;
+    } else {
+        int dflags = ((flags & MG_STEP_PHYSICS) ? 1 : 0) | ((flags & MG_STEP_GENES) ? 6 : 0);
+        if (dflags) enqueue_dens(h, dflags, prof);
     }
-    int dflags = ((flags & MG_STEP_PHYSICS) ? 1 : 0) | ((flags & MG_STEP_GENES) ? 6 : 0);
-    if (dflags) enqueue_dens(h, dflags, prof);
-    const bool remodel = (flags & MG_STEP_REMODEL) != 0;
     if (flags & MG_STEP_PHYSICS) {
         { Mark m(h, prof, "force"); launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream); }
     }
@@ -422,9 +428,27 @@ mg_status get_graph(mg_system* h, uint32_t flags, cudaGraphExec_t* out) {
     return MG_OK;
 }
 
+// The buffer-state change one step makes (what enqueue_step does to cur / conc_cur).
+void advance_state(mg_system* h, uint32_t flags) {
+    const int conc0 = h->conc_cur;
+    h->cur = 1 - h->cur;
+    h->conc_cur = 1 - conc0;
+    if (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)) h->conc_cur = conc0;
+}
+
+// Bookkeeping of a handle after nsteps graph steps (the same as run_steps does).
+void after_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
+    h->launches += (uint64_t)kernels_per_step(h, flags) * nsteps;
+    if (flags & MG_STEP_PHYSICS)
+        for (uint32_t s = 0; s < nsteps; s++) h->time = h->time + h->P.dt;
+    h->phase = PHASE_SORTED;
+    h->ever_sorted = true;
+    h->brk_pending = false;
+    h->flist_valid = (flags & MG_STEP_PHYSICS) ? false
+                     : (h->search && (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)));
+}
+
 mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
-    if ((flags & MG_STEP_REMODEL) && (flags & MG_STEP_SURROGATE))
-        return fail(h, MG_ERR_UNSUPPORTED, "remodelling together with the surrogate step is not built");
     if ((flags & MG_STEP_SURROGATE) && !h->sur)
         return fail(h, MG_ERR_INVALID_ARG, "surrogate step without an attached network (mg_set_surrogate)");
     for (uint32_t s = 0; s < nsteps; s++) {
@@ -1345,6 +1369,132 @@ mg_status mg_surrogate_stats(mg_handle h, uint64_t* judged, uint64_t* handed_ove
 
 // Number of kernels launched by mg_step since the handle was created.
 uint64_t mg_kernel_launches(mg_handle h) { return h ? h->launches : 0; }
+
+// ---- batched instances -----------------------------------------------------------------------
+mg_status mg_batch_create(const mg_handle* hs, uint32_t count, mg_batch* out) {
+    if (!hs || !out || count == 0) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_batch_create: bad arguments");
+    for (uint32_t k = 0; k < count; k++) {
+        if (!hs[k]) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_batch_create: NULL member");
+        for (uint32_t q = 0; q < k; q++)
+            if (hs[q] == hs[k]) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_batch_create: a member appears twice");
+        if (hs[k]->device != hs[0]->device)
+            return fail(nullptr, MG_ERR_INVALID_ARG, "mg_batch_create: members on different devices");
+    }
+    mg_batch b = new mg_batch_s();
+    b->hs.assign(hs, hs + count);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        if (b->stream) cudaStreamDestroy(b->stream);
+        delete b;
+        return cuda_fail(nullptr, e, "mg_batch_create");
+    }
+    *out = b;
+    return MG_OK;
+}
+
+mg_status mg_batch_destroy(mg_batch b) {
+    if (!b) return MG_OK;
+    cudaStreamSynchronize(b->stream);
+    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    cudaEventDestroy(b->done);
+    cudaStreamDestroy(b->stream);
+    delete b;
+    return MG_OK;
+}
+
+static mg_status batch_graph(mg_batch b, uint32_t flags, cudaGraphExec_t* out) {
+    std::string key = std::to_string(flags) + ":";
+    for (mg_system* h : b->hs) key += (char)('0' + 2 * h->cur + h->conc_cur);
+    auto it = b->graphs.find(key);
+    if (it != b->graphs.end()) {
+        for (mg_system* h : b->hs) advance_state(h, flags);
+        *out = it->second;
+        return MG_OK;
+    }
+    cudaGraph_t bg = nullptr;
+    MG_CUDA(nullptr, cudaGraphCreate(&bg, 0));
+    for (mg_system* h : b->hs) {
+        DevParams saved = h->P;
+        if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            enqueue_step(h, flags, false);  // advances the member's buffer state
+            e = cudaStreamEndCapture(h->stream, &g);
+        }
+        h->P = saved;
+        cudaGraphNode_t node;
+        if (e == cudaSuccess) e = cudaGraphAddChildGraphNode(&node, bg, nullptr, 0, g);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(bg);
+            return cuda_fail(h, e, "batch step capture");
+        }
+    }
+    cudaGraphExec_t ge = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&ge, bg, 0);
+    cudaGraphDestroy(bg);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGraphInstantiate (batch)");
+    b->graphs[key] = ge;
+    *out = ge;
+    return MG_OK;
+}
+
+static mg_status batch_run(mg_batch b, uint32_t nsteps, uint32_t flags, float* ms) {
+    if (!b) return fail(nullptr, MG_ERR_INVALID_ARG, "batch is NULL");
+    for (mg_system* h : b->hs) {
+        if (h->profile) return fail(h, MG_ERR_INVALID_ARG, "batch members must not be profiling");
+        if ((flags & MG_STEP_SURROGATE) && !h->sur)
+            return fail(h, MG_ERR_INVALID_ARG, "surrogate step without an attached network (mg_set_surrogate)");
+        MG_CUDA(h, cudaStreamSynchronize(h->stream));  // members' earlier work first
+    }
+    cudaEvent_t a = nullptr, z = nullptr;
+    if (ms) {
+        MG_CUDA(nullptr, cudaEventCreate(&a));
+        MG_CUDA(nullptr, cudaEventCreate(&z));
+        MG_CUDA(nullptr, cudaEventRecord(a, b->stream));
+    }
+    mg_status st = MG_OK;
+    for (uint32_t s = 0; s < nsteps && st == MG_OK; s++) {
+        cudaGraphExec_t ge = nullptr;
+        st = batch_graph(b, flags, &ge);
+        if (st == MG_OK) {
+            cudaError_t e = cudaGraphLaunch(ge, b->stream);
+            if (e != cudaSuccess) st = cuda_fail(nullptr, e, "cudaGraphLaunch (batch)");
+        }
+    }
+    if (ms) {
+        cudaEventRecord(z, b->stream);
+        cudaEventSynchronize(z);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, a, z);
+        *ms = t;
+        cudaEventDestroy(a);
+        cudaEventDestroy(z);
+    }
+    // later work on a member's own stream waits for the batch
+    cudaEventRecord(b->done, b->stream);
+    for (mg_system* h : b->hs) {
+        cudaStreamWaitEvent(h->stream, b->done, 0);
+        after_steps(h, nsteps, flags);
+    }
+    if (st != MG_OK) return st;
+    for (mg_system* h : b->hs) {
+        mg_status s2 = check_device(h);
+        if (s2 != MG_OK) return s2;
+    }
+    return MG_OK;
+}
+
+mg_status mg_batch_step(mg_batch b, uint32_t nsteps, uint32_t flags) {
+    return batch_run(b, nsteps, flags, nullptr);
+}
+
+mg_status mg_batch_time_steps(mg_batch b, uint32_t nsteps, uint32_t flags, float* ms) {
+    if (!ms) return fail(nullptr, MG_ERR_INVALID_ARG, "NULL argument");
+    return batch_run(b, nsteps, flags, ms);
+}
 
 }  // extern "C"
 
