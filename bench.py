@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate section")
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--sur-steps", type=int, default=1000, help="in-loop surrogate evaluation steps")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-instances section")
+    ap.add_argument("--batch-steps", type=int, default=500)
+    ap.add_argument("--batch-instances", type=int, default=256)
     return ap.parse_args()
 
 
@@ -283,6 +286,51 @@ def surrogate_section(args, peak_tflops):
     return out
 
 
+def batch_section(args):
+    """Parameter sweep: independent instances (jittered cubic lattice blocks with particle
+    counts log-uniform in [1,024, 65,536], stiffness U[0.5, 2], diffusion U[0.05, 0.2], own
+    regulatory table) advanced together, one graph launch per step, against the same instances
+    run one after another."""
+    import morphogenesis_gb300 as mg
+    from morphogenesis_gb300 import demo
+
+    r = np.random.default_rng(2)
+    counts = np.exp(r.uniform(np.log(1024), np.log(65536), args.batch_instances))
+    members = []
+    total = 0
+    t0 = time.perf_counter()
+    for k, c in enumerate(counts):
+        side = max(2, int(round(float(c) ** (1.0 / 3.0))))
+        g = demo.make_genome(seed=1000 + k, diffusion=demo.diffusion_rate(PARAM, float(r.uniform(0.05, 0.2))))
+        d = demo.make_block(side, PARAM, seed=k, genome=g, intstiff=float(r.uniform(0.5, 2.0)))
+        fs = mg.FluidSystem(d.params, d.genome, d.n)
+        fs.TransferToCL(d.arrays)
+        members.append(fs)
+        total += d.n
+    build_s = time.perf_counter() - t0
+    for fs in members:  # warm: graphs captured, caches hot
+        fs.Run(3)
+    b = mg.Batch(members)
+    b.Run(3)
+    ms_batch = b.time_steps(args.batch_steps)
+    ms_seq = 0.0
+    for fs in members:
+        ms_seq += fs.time_steps(args.batch_steps)
+    out = {"instances": len(members), "particles": total, "steps": args.batch_steps,
+           "particles_min": int(min(m.max_points for m in members)),
+           "particles_max": int(max(m.max_points for m in members)),
+           "batched_ms": ms_batch, "sequential_ms": ms_seq,
+           "batched_particle_steps_s": total * args.batch_steps / (ms_batch / 1e3),
+           "sequential_particle_steps_s": total * args.batch_steps / (ms_seq / 1e3),
+           "speedup": ms_seq / ms_batch, "setup_s": build_s,
+           "design": "one CUDA graph launch per step holding every instance's step graph as an "
+                     "independent branch (instances keep their own arenas, grids and genomes)"}
+    b.close()
+    for fs in members:
+        fs.close()
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -389,6 +437,9 @@ def main():
     sur = None
     if rank == 0 and not args.no_surrogate:
         sur = surrogate_section(args, measured_tflops())
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = batch_section(args)
 
     if rank == 0:
         out = {
@@ -414,6 +465,7 @@ def main():
             "kernels_ms_per_launch": {k: v[1] / v[0] for k, v in prof.items()},
             "cpu_baseline": cpu,
             "surrogate": sur,
+            "batch": batch,
         }
         print(json.dumps(out), flush=True)
     dist.close()

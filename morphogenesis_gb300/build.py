@@ -48,8 +48,14 @@ def _sources_newer(target: Path, deps) -> bool:
 
 
 def build(verbose: bool = False, force: bool = False) -> Path:
+    """Compiles what changed.  MG_NVCC_EXTRA (environment) adds flags to every unit, e.g.
+    -DMG_NL_CAP=64 -DMG_DENS_WARPS=6 to try another density-pass configuration."""
     OUT.mkdir(exist_ok=True)
     headers = list(CSRC.glob("*.cuh")) + [ROOT / "include" / "mg_abi.h"]
+    user = os.environ.get("MG_NVCC_EXTRA", "").split()
+    stamp = OUT / "flags.txt"
+    if not stamp.exists() or stamp.read_text() != " ".join(user):
+        force = True
     objs = []
     jobs = []
     for unit, extra in UNITS.items():
@@ -57,7 +63,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         obj = OUT / (unit + ".o")
         objs.append(obj)
         if force or _sources_newer(obj, [src, *headers, Path(__file__)]):
-            cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", str(src), "-o", str(obj)]
+            cmd = [nvcc(), *ARCH, *COMMON, *extra, *user, "-c", str(src), "-o", str(obj)]
             jobs.append(cmd)
 
     def run(cmd):
@@ -72,6 +78,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     if force or jobs or _sources_newer(LIB, objs):
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
         run(cmd)
+    stamp.write_text(" ".join(user))
     return LIB
 
 

@@ -37,7 +37,10 @@ constexpr int WARP_CELL_MAX = 256;   // cells up to this size are ordered by one
 constexpr int BLOCK_CELL_MAX = 8192; // up to this by one block in shared memory
 constexpr uint32_t BIG_LIST_CAP = 1u << 16;
 constexpr uint32_t SPIN_LIMIT = 1u << 22; // bounded look-back polls
-constexpr int NL_CAP = 48;  // per-lane neighbour list of the warp-cooperative density pass
+#ifndef MG_NL_CAP
+#define MG_NL_CAP 56
+#endif
+constexpr int NL_CAP = MG_NL_CAP;  // per-lane neighbour list of the warp-cooperative density pass
 constexpr int FL_CAP = 32;  // fluid-force neighbours (dsq < 1) recorded per particle
 constexpr int MLP_FEATURES = 48;  // surrogate inputs: conc[16], neighbour-mean conc[16], gene bits[16]
 

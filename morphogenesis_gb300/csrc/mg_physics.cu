@@ -28,7 +28,13 @@
 
 namespace mg {
 
-constexpr int DENS_WARPS = 8;
+#ifndef MG_DENS_WARPS
+#define MG_DENS_WARPS 8
+#endif
+#ifndef MG_DENS_MIN_BLOCKS
+#define MG_DENS_MIN_BLOCKS 3
+#endif
+constexpr int DENS_WARPS = MG_DENS_WARPS;  // warps per block of the warp-cooperative pass
 
 struct CellWin {
     int x, y, z;  // window origin = own cell - (1,1,1)
@@ -345,7 +351,7 @@ __device__ __forceinline__ int warp_maxi(int v) {
 }
 
 template <int FLAGS>
-__global__ void __launch_bounds__(DENS_WARPS * 32, 3) k_dens_warp(
+__global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_warp(
     DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
     const float* __restrict__ conc_in, float* __restrict__ conc_out,
     const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
