@@ -372,6 +372,7 @@ def main():
     fs.TransferToCL(d.arrays)
     flags = A.STEP_DEFAULT
     fs.Run(max(args.warmup, 3), flags)
+    tune = fs.autotune(5, flags)  # launch shape of the density pass, state restored afterwards
     n = d.n
     cells = int(d.params.grid_total)
 
@@ -450,7 +451,8 @@ def main():
             "config": {"workload": "plain full step, 1,048,576 particles (128x64x128 lattice), grid 132^3, gsrch 3",
                        "parameterisation": PARAM, "particles_per_gpu": n, "cells": cells,
                        "l2": f"inputs larger than L2: step state {step_bytes / 1e9:.2f} GB/step",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}",
+                       "density_launch_shape": {k: tune[k] for k in ("dens_warps", "group_mode", "sub_bits")}},
             "clocks": clk,
             "gpu_launches": int(launches),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,

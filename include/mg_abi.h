@@ -277,6 +277,18 @@ enum mg_option {
 };
 mg_status mg_set_option(mg_handle h, int32_t option, int32_t value);
 
+/* ---- launch-shape autotuner ------------------------------------------------------------------ */
+/* Launch shape of the density pass: {warps per block (4 or 8), search groups (0: a cell and the
+ * next cell of its row, 1: one cell), sub-cell bits per axis of the processing order (1 or 2)}.
+ * Results are identical for every choice. */
+mg_status mg_get_tuning(mg_handle h, int32_t choice[3]);
+mg_status mg_set_tuning(mg_handle h, const int32_t choice[3]);
+/* Times every launch shape over `steps` plain steps (flags: physics/genes only) on the
+ * handle's current state, restoring the state after each trial, and keeps the fastest.
+ * Needs a free device allocation the size of the handle's arena for the snapshot. */
+mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t choice[3],
+                      float* ms_per_step);
+
 /* ---- measurement ------------------------------------------------------------------------- */
 /* Runs nsteps of mg_step and returns their device time (CUDA events on the handle's stream). */
 mg_status mg_time_steps(mg_handle h, uint32_t nsteps, uint32_t flags, float* ms);

@@ -223,6 +223,23 @@ class FluidSystem:
     def set_option(self, option: int, value: int) -> None:
         self._check(self.lib.mg_set_option(self.h, int(option), int(value)))
 
+    def autotune(self, steps: int = 5, flags: int = A.STEP_DEFAULT) -> dict:
+        """Times the density pass's launch shapes on the current state (restored after each
+        trial) and keeps the fastest; returns the choice and its ms per step."""
+        ch = (C.c_int32 * 3)()
+        ms = C.c_float()
+        self._check(self.lib.mg_autotune(self.h, steps, flags, ch, C.byref(ms)))
+        return {"dens_warps": ch[0], "group_mode": ch[1], "sub_bits": ch[2], "ms_per_step": ms.value}
+
+    def tuning(self) -> tuple[int, int, int]:
+        ch = (C.c_int32 * 3)()
+        self._check(self.lib.mg_get_tuning(self.h, ch))
+        return tuple(ch)
+
+    def set_tuning(self, dens_warps: int, group_mode: int, sub_bits: int) -> None:
+        ch = (C.c_int32 * 3)(dens_warps, group_mode, sub_bits)
+        self._check(self.lib.mg_set_tuning(self.h, ch))
+
     def profile(self, enable: bool = True) -> None:
         self._check(self.lib.mg_profile_enable(self.h, 1 if enable else 0))
 

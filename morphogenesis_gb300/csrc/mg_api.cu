@@ -169,6 +169,9 @@ void derive(DevParams& D, const mg_fparams& p, uint32_t cap) {
     D.null_z = p.pboundmin[2] - (float)(2 * p.grid_res[2]);
     D.freeze = p.freeze ? 1 : 0;
     D.cap = cap;
+    D.dens_warps = 8;
+    D.group_mode = 0;
+    D.sub_bits = 2;
     D.cells = (uint32_t)p.grid_total;
 }
 
@@ -1369,6 +1372,97 @@ mg_status mg_surrogate_stats(mg_handle h, uint64_t* judged, uint64_t* handed_ove
 
 // Number of kernels launched by mg_step since the handle was created.
 uint64_t mg_kernel_launches(mg_handle h) { return h ? h->launches : 0; }
+
+// ---- autotuner --------------------------------------------------------------------------------
+// Times the density pass's launch shapes on the handle's own state: each candidate runs
+// `steps` graph steps from a snapshot of the whole arena, which is restored afterwards, so
+// tuning leaves the simulation where it was.  Results do not depend on the choice.
+mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choice, float* ms_per_step) {
+    if (!h || steps == 0) return fail(h, MG_ERR_INVALID_ARG, "mg_autotune: bad arguments");
+    if (flags & (MG_STEP_SURROGATE | MG_STEP_REMODEL))
+        return fail(h, MG_ERR_INVALID_ARG, "mg_autotune times plain steps (physics and genes flags)");
+    if (h->profile) return fail(h, MG_ERR_INVALID_ARG, "mg_autotune: profiling is on");
+    if (h->search != 1) return fail(h, MG_ERR_INVALID_ARG, "mg_autotune tunes the warp-cooperative search");
+    void* snap = nullptr;
+    if (cudaMalloc(&snap, h->arena_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, MG_ERR_OOM, "mg_autotune: no room for a snapshot of the arena");
+    }
+    struct Host { int cur, conc_cur, phase; bool ever_sorted, brk_pending, flist_valid; float time; uint64_t launches; };
+    const Host saved{h->cur, h->conc_cur, h->phase, h->ever_sorted, h->brk_pending, h->flist_valid, h->time, h->launches};
+    const DevParams P0 = h->P;
+    auto restore = [&]() -> cudaError_t {
+        h->cur = saved.cur; h->conc_cur = saved.conc_cur; h->phase = saved.phase;
+        h->ever_sorted = saved.ever_sorted; h->brk_pending = saved.brk_pending;
+        h->flist_valid = saved.flist_valid; h->time = saved.time; h->launches = saved.launches;
+        return cudaMemcpyAsync(h->arena, snap, h->arena_bytes, cudaMemcpyDeviceToDevice, h->stream);
+    };
+    mg_status st = MG_OK;
+    cudaError_t e = cudaMemcpyAsync(snap, h->arena, h->arena_bytes, cudaMemcpyDeviceToDevice, h->stream);
+    if (e != cudaSuccess) st = cuda_fail(h, e, "mg_autotune snapshot");
+    struct Cand { int warps, group, sub; };
+    const Cand cands[] = {{8, 0, 2}, {8, 1, 2}, {8, 0, 1}, {8, 1, 1}, {4, 0, 2}, {4, 1, 2}, {4, 0, 1}, {4, 1, 1}};
+    float best = 0.f;
+    Cand pick = cands[0];
+    cudaEvent_t a = nullptr, z = nullptr;
+    if (st == MG_OK && (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&z) != cudaSuccess))
+        st = fail(h, MG_ERR_CUDA, "mg_autotune: events");
+    for (const Cand& c : cands) {
+        if (st != MG_OK) break;
+        h->P.dens_warps = c.warps;
+        h->P.group_mode = c.group;
+        h->P.sub_bits = c.sub;
+        clear_graphs(h);
+        // two warm steps capture the graphs of both buffer parities, then the timed run
+        if ((e = restore()) != cudaSuccess) { st = cuda_fail(h, e, "mg_autotune restore"); break; }
+        if ((st = run_steps(h, 2, flags)) != MG_OK) break;
+        if ((e = restore()) != cudaSuccess) { st = cuda_fail(h, e, "mg_autotune restore"); break; }
+        cudaEventRecord(a, h->stream);
+        if ((st = run_steps(h, steps, flags)) != MG_OK) break;
+        cudaEventRecord(z, h->stream);
+        cudaEventSynchronize(z);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, a, z);
+        if (&c == cands || t < best) { best = t; pick = c; }
+    }
+    if (a) cudaEventDestroy(a);
+    if (z) cudaEventDestroy(z);
+    h->P = P0;
+    if (st == MG_OK) {
+        h->P.dens_warps = pick.warps;
+        h->P.group_mode = pick.group;
+        h->P.sub_bits = pick.sub;
+    }
+    clear_graphs(h);
+    e = restore();
+    cudaStreamSynchronize(h->stream);
+    cudaFree(snap);
+    if (st != MG_OK) return st;
+    if (e != cudaSuccess) return cuda_fail(h, e, "mg_autotune restore");
+    if (choice) { choice[0] = pick.warps; choice[1] = pick.group; choice[2] = pick.sub; }
+    if (ms_per_step) *ms_per_step = best / (float)steps;
+    return check_device(h);
+}
+
+mg_status mg_get_tuning(mg_handle h, int32_t* choice) {
+    if (!h || !choice) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    choice[0] = h->P.dens_warps;
+    choice[1] = h->P.group_mode;
+    choice[2] = h->P.sub_bits;
+    return MG_OK;
+}
+
+mg_status mg_set_tuning(mg_handle h, const int32_t* choice) {
+    if (!h || !choice) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    if ((choice[0] != 4 && choice[0] != 8) || (choice[1] != 0 && choice[1] != 1) ||
+        (choice[2] != 1 && choice[2] != 2))
+        return fail(h, MG_ERR_INVALID_ARG, "tuning: warps 4 or 8, group mode 0 or 1, sub-cell bits 1 or 2");
+    h->P.dens_warps = choice[0];
+    h->P.group_mode = choice[1];
+    h->P.sub_bits = choice[2];
+    clear_graphs(h);
+    return MG_OK;
+}
 
 // ---- batched instances -----------------------------------------------------------------------
 mg_status mg_batch_create(const mg_handle* hs, uint32_t count, mg_batch* out) {

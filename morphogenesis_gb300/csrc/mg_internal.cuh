@@ -63,6 +63,10 @@ struct DevParams {
     float null_z;
     int freeze;
     int uniform_diff;  // all 16 diffusion rates equal and nonzero (set from the genome)
+    // launch-shape choices of the density pass (results do not depend on them; mg_autotune
+    // picks them by timing): warps per block, search groups (0: a cell and the next cell of
+    // its row, 1: one cell), sub-cell bits per axis of the processing order (1 or 2)
+    int dens_warps, group_mode, sub_bits;
     uint32_t cap;
     uint32_t cells;
 };

@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     const uint32_t* __restrict__ work, uint32_t* __restrict__ ovf, uint32_t* __restrict__ ovf_count,
     DensExtra X) {
     using F = DF<FLAGS>;
-    extern __shared__ uint32_t s_list[];  // [DENS_WARPS][NL_CAP][32]
+    extern __shared__ uint32_t s_list[];  // [warps of the block][NL_CAP][32]
     __shared__ float4 s_sp[DENS_WARPS][32];
     __shared__ uint32_t s_sq[DENS_WARPS][32];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
@@ -396,7 +396,8 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     while (remaining) {
         const int leader = __ffs(remaining) - 1;
         const uint32_t lcell = __shfl_sync(0xffffffffu, pcell, leader);
-        const bool ing = act && ((remaining >> lane) & 1u) && (pcell == lcell || pcell == lcell + 1u);
+        const bool ing = act && ((remaining >> lane) & 1u) &&
+                         (pcell == lcell || (P.group_mode == 0 && pcell == lcell + 1u));
         remaining &= ~__ballot_sync(0xffffffffu, ing);
         const float bx0 = warp_min(ing ? ip.x : INF) - Rf, bx1 = warp_max(ing ? ip.x : -INF) + Rf;
         const float by0 = warp_min(ing ? ip.y : INF) - Rf, by1 = warp_max(ing ? ip.y : -INF) + Rf;
@@ -635,12 +636,13 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
                  cudaStream_t st, const DensExtra* extra) {
     const DensExtra X = extra ? *extra : DensExtra{};
-    const size_t smem = (size_t)DENS_WARPS * NL_CAP * 32 * sizeof(uint32_t);
+    const int warps = (P.dens_warps >= 1 && P.dens_warps <= DENS_WARPS) ? P.dens_warps : DENS_WARPS;
+    const size_t smem = (size_t)warps * NL_CAP * 32 * sizeof(uint32_t);
     if (search == 1 && (flags & (1 | 2 | 8 | 16))) {
-        uint32_t blocks = (P.cap + DENS_WARPS * 32 - 1) / (DENS_WARPS * 32);
+        uint32_t blocks = (P.cap + warps * 32 - 1) / (warps * 32);
 #define MG_DENSW_CASE(F)                                                                          \
     case F:                                                                                       \
-        k_dens_warp<F><<<blocks, DENS_WARPS * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,   \
+        k_dens_warp<F><<<blocks, warps * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,        \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.counters + 3,   \

@@ -38,20 +38,21 @@ __device__ __forceinline__ uint32_t cell_of(const DevParams& P, float4 p) {
     return (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
 }
 
-// Morton code of the 4x4x4 sub-cell holding a position inside its cell (2 bits per axis from
-// the fractional part of the cell coordinate).  Only the density pass's processing order uses
-// it, never a result.
+// Morton code of the sub-cell holding a position inside its cell: 2^sub_bits sub-cells per axis
+// (sub_bits 1 or 2) from the fractional part of the cell coordinate.  Only the density pass's
+// processing order uses it, never a result.
 __device__ __forceinline__ uint32_t sub_of(const DevParams& P, float4 p) {
     const float g[3] = {(p.x - P.gmin[0]) * P.gdelta[0], (p.y - P.gmin[1]) * P.gdelta[1],
                         (p.z - P.gmin[2]) * P.gdelta[2]};
+    const int nsub = 1 << P.sub_bits;
     uint32_t code = 0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        int q = (int)((g[a] - floorf(g[a])) * 4.f);
-        q = q < 0 ? 0 : (q > 3 ? 3 : q);
-        code |= ((uint32_t)(q & 1) << a) | ((uint32_t)(q >> 1) << (3 + a));
+        int q = (int)((g[a] - floorf(g[a])) * (float)nsub);
+        q = q < 0 ? 0 : (q > nsub - 1 ? nsub - 1 : q);
+        code |= ((uint32_t)(q & 1) << a) | ((uint32_t)((q >> 1) & 1) << (3 + a));
     }
-    return code;
+    return P.sub_bits == 1 ? code & 7u : code;
 }
 
 // ---- insert -------------------------------------------------------------------------------

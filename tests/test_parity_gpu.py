@@ -303,3 +303,32 @@ def test_remodelling_stage_matches_oracle(built):
         o.insert(); o.prefix_sum(); o.sort(); o.remodel()
         for b in (A.FELASTIDX, A.FPARTICLEIDX, A.FPARTICLE_ID):
             assert np.array_equal(g.download(b), o.download(b)), f"buffer {b}"
+
+
+def test_launch_shapes_give_identical_results(built):
+    d = demo.make_block((24, 12, 24), "R", seed=6)
+    import morphogenesis_gb300 as mg
+
+    ref = mg.FluidSystem(d.params, d.genome, d.n)
+    ref.TransferToCL(d.arrays)
+    ref.Run(30)
+    want = {b: ref.download(b).view(np.uint32) for b in (A.FPOS, A.FVEL, A.FCONC, A.FELASTIDX, A.FPARTICLE_ID)}
+    for shape in ((4, 1, 1), (8, 1, 2), (4, 0, 2), (8, 0, 1)):
+        fs = mg.FluidSystem(d.params, d.genome, d.n)
+        fs.TransferToCL(d.arrays)
+        fs.set_tuning(*shape)
+        fs.Run(30)
+        for b, w in want.items():
+            assert np.array_equal(fs.download(b).view(np.uint32), w), f"shape {shape} buffer {b}"
+        fs.close()
+    # the autotuner restores the state it tunes on
+    fs = mg.FluidSystem(d.params, d.genome, d.n)
+    fs.TransferToCL(d.arrays)
+    fs.Run(10)
+    before = fs.download(A.FPOS).copy()
+    res = fs.autotune(3)
+    assert fs.tuning() == (res["dens_warps"], res["group_mode"], res["sub_bits"])
+    assert np.array_equal(fs.download(A.FPOS), before)
+    fs.Run(20)
+    for b, w in want.items():
+        assert np.array_equal(fs.download(b).view(np.uint32), w), f"after autotune, buffer {b}"
