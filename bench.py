@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--sur-steps", type=int, default=1000, help="in-loop surrogate evaluation steps")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-instances section")
+    ap.add_argument("--no-large", action="store_true", help="skip the 16.8M-particle section")
+    ap.add_argument("--large-steps", type=int, default=200)
     ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--batch-instances", type=int, default=256)
     return ap.parse_args()
@@ -282,7 +284,39 @@ def surrogate_section(args, peak_tflops):
                       "rel_err_vs_plain": rel_err(sur.download(A.FCONC), plain.download(A.FCONC))}
     plain.close()
     sur.close()
-    m.close()
+    return out, m
+
+
+def large_section(args, mlp):
+    """16,777,216 particles (256^3 lattice, grid 260^3), the surrogate of the surrogate section
+    and bond remodelling (breaks at strain > 0.5, deterministic re-forming), 200 steps; the
+    device footprint of the instance against the GB300's HBM."""
+    import morphogenesis_gb300 as mg
+    from morphogenesis_gb300 import _abi as A
+    from morphogenesis_gb300 import demo
+    from morphogenesis_gb300 import surrogate as S
+
+    t0 = time.perf_counter()
+    d = demo.make_block(256, PARAM, seed=0, breakable=True)
+    fs = mg.FluidSystem(d.params, d.genome, d.n)
+    fs.TransferToCL(d.arrays)
+    del d.arrays
+    S.attach(fs, mlp, judge_period=10, judge_stride=64, threshold=1e-3)
+    setup_s = time.perf_counter() - t0
+    flags = A.STEP_DEFAULT | A.STEP_SURROGATE | A.STEP_REMODEL
+    fs.Run(3, flags)
+    ms = fs.time_steps(args.large_steps, flags)
+    arena, total = fs.device_bytes()
+    judged, handed, _ = S.stats(fs)
+    n = d.n
+    out = {"particles": n, "cells": int(d.params.grid_total), "steps": args.large_steps,
+           "flags": "physics + surrogate morphogen stage + remodelling",
+           "ms_per_step": ms / args.large_steps,
+           "particle_steps_s": n * args.large_steps / (ms / 1e3),
+           "device_bytes": total, "arena_bytes": arena, "bytes_per_particle": total / n,
+           "hbm_fraction": total / (288e9), "judged": judged, "handed_over": handed,
+           "setup_s": setup_s}
+    fs.close()
     return out
 
 
@@ -436,8 +470,12 @@ def main():
     fs.close()
 
     sur = None
+    large = None
     if rank == 0 and not args.no_surrogate:
-        sur = surrogate_section(args, measured_tflops())
+        sur, mlp = surrogate_section(args, measured_tflops())
+        if not args.no_large:
+            large = large_section(args, mlp)
+        mlp.close()
     batch = None
     if rank == 0 and not args.no_batch:
         batch = batch_section(args)
@@ -468,6 +506,7 @@ def main():
             "cpu_baseline": cpu,
             "surrogate": sur,
             "batch": batch,
+            "large": large,
         }
         print(json.dumps(out), flush=True)
     dist.close()

@@ -303,6 +303,9 @@ mg_status mg_algorithmic_bytes(mg_handle h, const char* kernel, uint32_t flags,
                                double* bytes_per_particle, double* bytes_per_cell);
 /* Number of GPU kernels mg_step/mg_time_steps have launched on this handle. */
 uint64_t mg_kernel_launches(mg_handle h);
+/* Device memory of the handle: the arena made by mg_create, and everything it holds now
+ * (arena, upload staging, dense gene lists and surrogate buffers once made). */
+mg_status mg_device_bytes(mg_handle h, size_t* arena, size_t* total);
 
 /* ---- batched instances (parameter sweeps) --------------------------------------------------- */
 /* A batch steps many independent systems together (each keeps its own particles, grid,

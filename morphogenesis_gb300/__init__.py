@@ -231,6 +231,12 @@ class FluidSystem:
         self._check(self.lib.mg_autotune(self.h, steps, flags, ch, C.byref(ms)))
         return {"dens_warps": ch[0], "group_mode": ch[1], "sub_bits": ch[2], "ms_per_step": ms.value}
 
+    def device_bytes(self) -> tuple[int, int]:
+        """(arena bytes, all device bytes the handle holds now)."""
+        a, t = C.c_size_t(), C.c_size_t()
+        self._check(self.lib.mg_device_bytes(self.h, C.byref(a), C.byref(t)))
+        return a.value, t.value
+
     def tuning(self) -> tuple[int, int, int]:
         ch = (C.c_int32 * 3)()
         self._check(self.lib.mg_get_tuning(self.h, ch))

@@ -140,6 +140,7 @@ SIGNATURES = [
     ("mg_algorithmic_bytes", C.c_int, [H, C.c_char_p, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("mg_kernel_launches", C.c_uint64, [H]),
     ("mg_run_remodelling", C.c_int, [H]),
+    ("mg_device_bytes", C.c_int, [H, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     ("mg_get_tuning", C.c_int, [H, C.POINTER(C.c_int32)]),
     ("mg_set_tuning", C.c_int, [H, C.POINTER(C.c_int32)]),
     ("mg_autotune", C.c_int, [H, C.c_uint32, C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_float)]),

@@ -1373,6 +1373,17 @@ mg_status mg_surrogate_stats(mg_handle h, uint64_t* judged, uint64_t* handed_ove
 // Number of kernels launched by mg_step since the handle was created.
 uint64_t mg_kernel_launches(mg_handle h) { return h ? h->launches : 0; }
 
+mg_status mg_device_bytes(mg_handle h, size_t* arena, size_t* total) {
+    if (!h || !arena || !total) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    const size_t n = h->cap, C = (size_t)h->P.cells;
+    size_t t = h->arena_bytes + h->staging_bytes;
+    if (h->dense) t += 4 * (2 * C * NG + n * NG + NG);
+    if (h->feat) t += sizeof(__nv_bfloat16) * n * mg::MLP_IN + 4 * n + 4 * n * NTF + 16;
+    *arena = h->arena_bytes;
+    *total = t;
+    return MG_OK;
+}
+
 // ---- autotuner --------------------------------------------------------------------------------
 // Times the density pass's launch shapes on the handle's own state: each candidate runs
 // `steps` graph steps from a snapshot of the whole arena, which is restored afterwards, so
