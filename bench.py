@@ -490,7 +490,7 @@ def main():
                        "parameterisation": PARAM, "particles_per_gpu": n, "cells": cells,
                        "l2": f"inputs larger than L2: step state {step_bytes / 1e9:.2f} GB/step",
                        "parallelism": f"replicas x{world}",
-                       "density_launch_shape": {k: tune[k] for k in ("dens_warps", "group_mode", "sub_bits")}},
+                       "density_launch_shape": {k: tune[k] for k in ("dens_warps", "group_mode", "sub_bits", "search")}},
             "clocks": clk,
             "gpu_launches": int(launches),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,

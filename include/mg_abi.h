@@ -272,21 +272,23 @@ mg_status mg_surrogate_stats(mg_handle h, uint64_t* judged, uint64_t* handed_ove
 /* ---- tuning ------------------------------------------------------------------------------ */
 enum mg_option {
     /* neighbour search of the density/diffusion pass: 0 = one thread walks its 27 cells
-     * (the reference loop), 1 = warp-cooperative search (default).  Results are identical. */
+     * (the reference loop), 1 = warp-cooperative search (default), 2 = per-lane walk of the
+     * 2x2x2 sub-cells within the radius (needs gsrch 3).  Results are identical. */
     MG_OPT_NEIGHBOR_SEARCH = 1
 };
 mg_status mg_set_option(mg_handle h, int32_t option, int32_t value);
 
 /* ---- launch-shape autotuner ------------------------------------------------------------------ */
 /* Launch shape of the density pass: {warps per block (4 or 8), search groups (0: a cell and the
- * next cell of its row, 1: one cell), sub-cell bits per axis of the processing order (1 or 2)}.
+ * next cell of its row, 1: one cell), sub-cell bits per axis of the processing order (1 or 2),
+ * neighbour search (MG_OPT_NEIGHBOR_SEARCH: 0, 1 or 2; 2 needs sub-cell bits 1)}.
  * Results are identical for every choice. */
-mg_status mg_get_tuning(mg_handle h, int32_t choice[3]);
-mg_status mg_set_tuning(mg_handle h, const int32_t choice[3]);
+mg_status mg_get_tuning(mg_handle h, int32_t choice[4]);
+mg_status mg_set_tuning(mg_handle h, const int32_t choice[4]);
 /* Times every launch shape over `steps` plain steps (flags: physics/genes only) on the
  * handle's current state, restoring the state after each trial, and keeps the fastest.
  * Needs a free device allocation the size of the handle's arena for the snapshot. */
-mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t choice[3],
+mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t choice[4],
                       float* ms_per_step);
 
 /* ---- measurement ------------------------------------------------------------------------- */

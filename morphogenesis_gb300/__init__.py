@@ -226,10 +226,11 @@ class FluidSystem:
     def autotune(self, steps: int = 5, flags: int = A.STEP_DEFAULT) -> dict:
         """Times the density pass's launch shapes on the current state (restored after each
         trial) and keeps the fastest; returns the choice and its ms per step."""
-        ch = (C.c_int32 * 3)()
+        ch = (C.c_int32 * 4)()
         ms = C.c_float()
         self._check(self.lib.mg_autotune(self.h, steps, flags, ch, C.byref(ms)))
-        return {"dens_warps": ch[0], "group_mode": ch[1], "sub_bits": ch[2], "ms_per_step": ms.value}
+        return {"dens_warps": ch[0], "group_mode": ch[1], "sub_bits": ch[2], "search": ch[3],
+                "ms_per_step": ms.value}
 
     def device_bytes(self) -> tuple[int, int]:
         """(arena bytes, all device bytes the handle holds now)."""
@@ -237,13 +238,14 @@ class FluidSystem:
         self._check(self.lib.mg_device_bytes(self.h, C.byref(a), C.byref(t)))
         return a.value, t.value
 
-    def tuning(self) -> tuple[int, int, int]:
-        ch = (C.c_int32 * 3)()
+    def tuning(self) -> tuple[int, int, int, int]:
+        """(warps per block, search groups, sub-cell bits, neighbour search) of the density pass."""
+        ch = (C.c_int32 * 4)()
         self._check(self.lib.mg_get_tuning(self.h, ch))
         return tuple(ch)
 
-    def set_tuning(self, dens_warps: int, group_mode: int, sub_bits: int) -> None:
-        ch = (C.c_int32 * 3)(dens_warps, group_mode, sub_bits)
+    def set_tuning(self, dens_warps: int, group_mode: int, sub_bits: int, search: int = 1) -> None:
+        ch = (C.c_int32 * 4)(dens_warps, group_mode, sub_bits, search)
         self._check(self.lib.mg_set_tuning(self.h, ch))
 
     def profile(self, enable: bool = True) -> None:

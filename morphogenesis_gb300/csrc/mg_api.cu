@@ -321,7 +321,7 @@ void enqueue_insert_rank(mg_system* h, bool prof) {
     { Mark m(h, prof, "scan"); launch_scan(h->s.count, h->s.offset, P.cells, h->s.scan_status,
                                            h->s.counters, h->s.counters + 3, h->s.counters + 2, st); }
     { Mark m(h, prof, "place"); launch_place(P, h->s, st); }
-    { Mark m(h, prof, "cellsort"); launch_cellsort(P, h->s, h->num_sms, st); }
+    { Mark m(h, prof, "cellsort"); launch_cellsort(P, h->s, h->num_sms, h->search == 2, st); }
 }
 
 void enqueue_gather(mg_system* h, bool prof) {
@@ -646,6 +646,7 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     plan.push_back({(void**)&h->s.sorted, 4 * n});
     plan.push_back({(void**)&h->s.work, 4 * n});
     plan.push_back({(void**)&h->s.sub, n});
+    plan.push_back({(void**)&h->s.subcnt, 8 * C});
     plan.push_back({(void**)&h->s.ovf, 4 * n});
     plan.push_back({(void**)&h->s.freemask, n});
     plan.push_back({(void**)&h->s.prop, 4 * n});
@@ -1067,7 +1068,12 @@ mg_status mg_set_option(mg_handle h, int32_t option, int32_t value) {
     if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
     switch (option) {
     case MG_OPT_NEIGHBOR_SEARCH:
-        if (value < 0 || value > 1) return fail(h, MG_ERR_INVALID_ARG, "neighbour search is 0 or 1");
+        if (value < 0 || value > 2) return fail(h, MG_ERR_INVALID_ARG, "neighbour search is 0, 1 or 2");
+        if (value == 2 && h->P.gsrch != 3)
+            return fail(h, MG_ERR_UNSUPPORTED, "the fine-cell search needs the 27-cell window (gsrch 3)");
+        if (value == 2) h->P.sub_bits = 1;  // its sub-cells are the 2x2x2 halves of a cell
+        // the fine-cell search reads sub-cell tables that only a sort made for it writes
+        if (value == 2 && h->search != 2 && h->phase == PHASE_SORTED) h->phase = PHASE_UNSORTED;
         h->search = value;
         h->flist_valid = false;
         clear_graphs(h);
@@ -1393,7 +1399,8 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
     if (flags & (MG_STEP_SURROGATE | MG_STEP_REMODEL))
         return fail(h, MG_ERR_INVALID_ARG, "mg_autotune times plain steps (physics and genes flags)");
     if (h->profile) return fail(h, MG_ERR_INVALID_ARG, "mg_autotune: profiling is on");
-    if (h->search != 1) return fail(h, MG_ERR_INVALID_ARG, "mg_autotune tunes the warp-cooperative search");
+    if (h->search == 0) return fail(h, MG_ERR_INVALID_ARG, "mg_autotune tunes the warp searches (1, 2)");
+    const int search0 = h->search;
     void* snap = nullptr;
     if (cudaMalloc(&snap, h->arena_bytes) != cudaSuccess) {
         cudaGetLastError();
@@ -1411,8 +1418,10 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
     mg_status st = MG_OK;
     cudaError_t e = cudaMemcpyAsync(snap, h->arena, h->arena_bytes, cudaMemcpyDeviceToDevice, h->stream);
     if (e != cudaSuccess) st = cuda_fail(h, e, "mg_autotune snapshot");
-    struct Cand { int warps, group, sub; };
-    const Cand cands[] = {{8, 0, 2}, {8, 1, 2}, {8, 0, 1}, {8, 1, 1}, {4, 0, 2}, {4, 1, 2}, {4, 0, 1}, {4, 1, 1}};
+    struct Cand { int warps, group, sub, search; };
+    const bool fine_ok = h->P.gsrch == 3;
+    const Cand cands[] = {{8, 0, 2, 1}, {8, 1, 2, 1}, {8, 0, 1, 1}, {8, 1, 1, 1}, {4, 0, 2, 1},
+                          {4, 1, 2, 1}, {4, 0, 1, 1}, {4, 1, 1, 1}, {8, 0, 1, 2}, {4, 0, 1, 2}};
     float best = 0.f;
     Cand pick = cands[0];
     cudaEvent_t a = nullptr, z = nullptr;
@@ -1420,6 +1429,8 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
         st = fail(h, MG_ERR_CUDA, "mg_autotune: events");
     for (const Cand& c : cands) {
         if (st != MG_OK) break;
+        if (c.search == 2 && !fine_ok) continue;
+        h->search = c.search;
         h->P.dens_warps = c.warps;
         h->P.group_mode = c.group;
         h->P.sub_bits = c.sub;
@@ -1439,18 +1450,23 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
     if (a) cudaEventDestroy(a);
     if (z) cudaEventDestroy(z);
     h->P = P0;
+    h->search = search0;
     if (st == MG_OK) {
         h->P.dens_warps = pick.warps;
         h->P.group_mode = pick.group;
         h->P.sub_bits = pick.sub;
+        h->search = pick.search;
     }
     clear_graphs(h);
     e = restore();
+    h->flist_valid = false;
+    // the fine-cell search reads sub-cell tables that only a sort made for it writes
+    if (h->search == 2 && search0 != 2 && h->phase == PHASE_SORTED) h->phase = PHASE_UNSORTED;
     cudaStreamSynchronize(h->stream);
     cudaFree(snap);
     if (st != MG_OK) return st;
     if (e != cudaSuccess) return cuda_fail(h, e, "mg_autotune restore");
-    if (choice) { choice[0] = pick.warps; choice[1] = pick.group; choice[2] = pick.sub; }
+    if (choice) { choice[0] = pick.warps; choice[1] = pick.group; choice[2] = pick.sub; choice[3] = pick.search; }
     if (ms_per_step) *ms_per_step = best / (float)steps;
     return check_device(h);
 }
@@ -1460,17 +1476,25 @@ mg_status mg_get_tuning(mg_handle h, int32_t* choice) {
     choice[0] = h->P.dens_warps;
     choice[1] = h->P.group_mode;
     choice[2] = h->P.sub_bits;
+    choice[3] = h->search;
     return MG_OK;
 }
 
 mg_status mg_set_tuning(mg_handle h, const int32_t* choice) {
     if (!h || !choice) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
     if ((choice[0] != 4 && choice[0] != 8) || (choice[1] != 0 && choice[1] != 1) ||
-        (choice[2] != 1 && choice[2] != 2))
-        return fail(h, MG_ERR_INVALID_ARG, "tuning: warps 4 or 8, group mode 0 or 1, sub-cell bits 1 or 2");
+        (choice[2] != 1 && choice[2] != 2) || choice[3] < 0 || choice[3] > 2)
+        return fail(h, MG_ERR_INVALID_ARG,
+                    "tuning: warps 4 or 8, group mode 0 or 1, sub-cell bits 1 or 2, search 0-2");
+    if (choice[3] == 2 && (choice[2] != 1 || h->P.gsrch != 3))
+        return fail(h, MG_ERR_INVALID_ARG, "the fine-cell search needs sub-cell bits 1 and gsrch 3");
+    if (choice[3] == 2 && (h->search != 2 || h->P.sub_bits != 1) && h->phase == PHASE_SORTED)
+        h->phase = PHASE_UNSORTED;  // the fine-cell search needs a sort made for it
     h->P.dens_warps = choice[0];
     h->P.group_mode = choice[1];
     h->P.sub_bits = choice[2];
+    h->search = choice[3];
+    h->flist_valid = false;
     clear_graphs(h);
     return MG_OK;
 }

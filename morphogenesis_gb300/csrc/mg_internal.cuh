@@ -112,7 +112,9 @@ struct Scratch {
     uint32_t* sorted;   // sorted[p] = pre-sort index of the particle sorted to p (stable)
     uint32_t* work;     // density-pass processing order: sorted slots, cell by cell, each
                         // cell's particles by sub-cell Morton code (a permutation of [0, nactive))
-    uint8_t* sub;       // Morton code of particle i's 4x4x4 sub-cell inside its cell
+    uint8_t* sub;       // Morton code of particle i's sub-cell inside its cell
+    unsigned long long* subcnt;  // [cells] with 2x2x2 sub-cells: count of each sub-cell code
+                                 // (8 bits each) of cells below WARP_CELL_MAX particles
     uint32_t* newidx;   // newidx[i] = sorted index of pre-sort particle i (UNDEF if dropped)
     uint32_t* scell;    // cell of sorted particle p
     float* press;
@@ -141,7 +143,9 @@ void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long lo
                  uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st);
 size_t scan_status_words(uint32_t n);
 void launch_place(const DevParams& P, const Scratch& s, cudaStream_t st);
-void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, cudaStream_t st);
+// subcounts: also count each cell's 2x2x2 sub-cells (for the per-lane fine-cell search)
+void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, bool subcounts,
+                     cudaStream_t st);
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st);
 // flags: 1 density/pressure, 2 diffusion, 4 gene reaction

@@ -350,6 +350,54 @@ __device__ __forceinline__ int warp_maxi(int v) {
     return v;
 }
 
+// Evaluates a lane's neighbour list (ascending sorted index, first entry of each cell flagged)
+// with the reference expressions: density partial sums per cell, diffusion and neighbour sums,
+// the fluid-force list; then the common epilogue.
+template <int FLAGS>
+__device__ __forceinline__ void dens_list_finish(
+    const DevParams& P, const DevGenome* __restrict__ G, uint32_t p, float4 ip, uint32_t n,
+    const uint32_t* my, const float4* __restrict__ pos, const float* __restrict__ conc_in,
+    float* __restrict__ conc_out, const uint32_t* __restrict__ genes, float* __restrict__ press,
+    float* __restrict__ invdens, uint32_t* __restrict__ flist, uint32_t* __restrict__ fcount,
+    const DensExtra& X) {
+    using F = DF<FLAGS>;
+    float cur[NTF], dif[NTF], nc[NTF], ms[NTF];
+    load_conc<FLAGS>(G, conc_in, p, cur, dif);
+#pragma unroll
+    for (int t = 0; t < NTF; t++) { nc[t] = 0.f; ms[t] = 0.f; }
+    const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
+    uint32_t mcnt = 0;
+    float sum = 0.f;
+    {
+        float part = 0.f;
+        uint32_t nf = 0;
+        for (uint32_t k = 0; k < n; k++) {
+            const uint32_t e = my[k * 32];
+            const uint32_t q = e & ~LIST_CELL_START;
+            if (F::DENS && (e & LIST_CELL_START)) {  // first neighbour of the next cell:
+                sum += part;                         // flush the previous cell's partial sum
+                part = 0.f;
+            }
+            const float4 jp = pos[q];
+            const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+            const float dsq = dx * dx + dy * dy + dz * dz;
+            if (dsq < 1.f && dsq > 0.f) {  // fluid-force neighbour, kept for the force pass
+                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
+                nf++;
+            }
+            if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
+            if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
+                conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2,
+                                             P.uniform_diff != 0, true);
+                mcnt++;
+            }
+        }
+        if (F::DENS) sum += part;
+        fcount[p] = nf;  // > FL_CAP: the force pass searches again
+    }
+    dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press, invdens, X);
+}
+
 template <int FLAGS>
 __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_warp(
     DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
@@ -487,41 +535,110 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
         ovf[atomicAdd(ovf_count, 1u)] = p;
         return;
     }
-    float cur[NTF], dif[NTF], nc[NTF], ms[NTF];
-    load_conc<FLAGS>(G, conc_in, p, cur, dif);
-#pragma unroll
-    for (int t = 0; t < NTF; t++) { nc[t] = 0.f; ms[t] = 0.f; }
-    const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
-    uint32_t mcnt = 0;
-    float sum = 0.f;
+    dens_list_finish<FLAGS>(P, G, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,
+                            fcount, X);
+}
+
+// ---- per-lane fine-cell search ----------------------------------------------------------------
+// For search radii up to half a grid cell.  The processing order groups each cell's particles
+// by 2x2x2 sub-cell (sub_bits 1) and the cell sort records each cell's eight sub-cell counts, so
+// every lane walks only the sub-cells within its radius: the fine cells floor(2g - rf) ..
+// floor(2g + rf) per axis (g the particle's cell coordinate, rf the radius in fine cells with a
+// margin for the rounding of g), grouped by grid cell in ascending cell index.  Hits of one
+// cell are kept in ascending sorted index by insertion, so the list has the canonical order.
+template <int FLAGS>
+__global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_fine(
+    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
+    const float* __restrict__ conc_in, float* __restrict__ conc_out,
+    const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
+    const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
+    const unsigned long long* __restrict__ subcnt, float* __restrict__ press,
+    float* __restrict__ invdens, uint32_t* __restrict__ flist, uint32_t* __restrict__ fcount,
+    const uint32_t* __restrict__ nactive_p, const uint32_t* __restrict__ work,
+    uint32_t* __restrict__ ovf, uint32_t* __restrict__ ovf_count, DensExtra X) {
+    using F = DF<FLAGS>;
+    extern __shared__ uint32_t s_list[];  // [warps of the block][NL_CAP][32]
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    uint32_t* my = s_list + (size_t)w * NL_CAP * 32 + lane;
+    const uint32_t k0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k0 >= *nactive_p) return;
+    const uint32_t p = work[k0];
+    const float4 ip = pos[p];
+    float R2 = 1.f;
+    if (F::DENS) R2 = fmaxf(R2, P.r2);
+    if (F::DIFF || F::MEAN) R2 = fmaxf(R2, P.r2diff);
+    const float R2s = R2 * 1.000004f;  // list threshold for the fused distance (superset)
+    const float Rw = sqrtf(R2);
+    // fine-cell range per axis, clipped to the 27-cell window of the particle's own cell
+    int lo[3], hi[3];
     {
-        float part = 0.f;
-        uint32_t nf = 0;
-        for (uint32_t k = 0; k < n; k++) {
-            const uint32_t e = my[k * 32];
-            const uint32_t q = e & ~LIST_CELL_START;
-            if (F::DENS && (e & LIST_CELL_START)) {  // first neighbour of the next cell:
-                sum += part;                         // flush the previous cell's partial sum
-                part = 0.f;
-            }
-            const float4 jp = pos[q];
-            const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
-            const float dsq = dx * dx + dy * dy + dz * dz;
-            if (dsq < 1.f && dsq > 0.f) {  // fluid-force neighbour, kept for the force pass
-                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
-                nf++;
-            }
-            if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
-            if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
-                conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2,
-                                             P.uniform_diff != 0, true);
-                mcnt++;
+        const float c[3] = {ip.x, ip.y, ip.z};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const float g = (c[a] - P.gmin[a]) * P.gdelta[a];
+            const int own = (int)g;  // the cell hash of the insert pass
+            const float g2 = 2.f * g;
+            const float rf = 2.f * Rw * P.gdelta[a] * 1.0002f + 1e-3f;
+            lo[a] = max((int)floorf(g2 - rf), 2 * (own - 1));
+            hi[a] = min((int)floorf(g2 + rf), 2 * (own + 1) + 1);
+        }
+    }
+    uint32_t n = 0;
+    for (int cy = lo[1] >> 1; cy <= (hi[1] >> 1); cy++) {
+        for (int cz = lo[2] >> 1; cz <= (hi[2] >> 1); cz++) {
+            for (int cx = lo[0] >> 1; cx <= (hi[0] >> 1); cx++) {
+                const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
+                const uint32_t cnt = count[cell];
+                if (cnt == 0) continue;
+                const uint32_t off = offset[cell];
+                const uint32_t seg = n;  // this cell's hits start here
+                // sub-cell ranges of this cell inside the fine window
+                const int sx0 = max(lo[0] - 2 * cx, 0), sx1 = min(hi[0] - 2 * cx, 1);
+                const int sy0 = max(lo[1] - 2 * cy, 0), sy1 = min(hi[1] - 2 * cy, 1);
+                const int sz0 = max(lo[2] - 2 * cz, 0), sz1 = min(hi[2] - 2 * cz, 1);
+                uint32_t starts[9];
+                const bool whole = cnt >= (uint32_t)WARP_CELL_MAX;  // no sub-cell counts: scan it all
+                if (!whole) {
+                    const unsigned long long sc = subcnt[cell];
+                    uint32_t acc = 0;
+#pragma unroll
+                    for (int code = 0; code < 8; code++) {
+                        starts[code] = acc;
+                        acc += (uint32_t)((sc >> (8 * code)) & 0xFFu);
+                    }
+                    starts[8] = acc;
+                }
+                for (int sz = whole ? 0 : sz0; sz <= (whole ? 0 : sz1); sz++)
+                    for (int sy = whole ? 0 : sy0; sy <= (whole ? 0 : sy1); sy++)
+                        for (int sx = whole ? 0 : sx0; sx <= (whole ? 0 : sx1); sx++) {
+                            const int code = sx | (sy << 1) | (sz << 2);
+                            const uint32_t b = whole ? 0u : starts[code];
+                            const uint32_t e = whole ? cnt : starts[code + 1];
+                            for (uint32_t t = b; t < e; t++) {
+                                const uint32_t q = work[off + t];
+                                const float d = approx_dsq(ip, pos[q]);
+                                if (!(d < R2s && d > 0.f)) continue;
+                                if (n < (uint32_t)NL_CAP) {  // insert in ascending index
+                                    uint32_t i = n;
+                                    while (i > seg && my[(i - 1) * 32] > q) {
+                                        my[i * 32] = my[(i - 1) * 32];
+                                        i--;
+                                    }
+                                    my[i * 32] = q;
+                                }
+                                n++;
+                            }
+                        }
+                if (n > seg && seg < (uint32_t)NL_CAP) my[seg * 32] |= LIST_CELL_START;
             }
         }
-        if (F::DENS) sum += part;
-        fcount[p] = nf;  // > FL_CAP: the force pass searches again
     }
-    dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press, invdens, X);
+    if (n > (uint32_t)NL_CAP) {
+        ovf[atomicAdd(ovf_count, 1u)] = p;
+        return;
+    }
+    dens_list_finish<FLAGS>(P, G, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,
+                            fcount, X);
 }
 
 // ---- overflow pass ----------------------------------------------------------------------------
@@ -626,7 +743,9 @@ cudaError_t physics_init() {
     cudaError_t e = cudaSuccess;
 #define MG_ATTR(F)                                                                              \
     if (e == cudaSuccess)                                                                       \
-        e = cudaFuncSetAttribute(k_dens_warp<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = cudaFuncSetAttribute(k_dens_warp<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
+    if (e == cudaSuccess)                                                                       \
+        e = cudaFuncSetAttribute(k_dens_fine<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     MG_DENS_FLAG_SETS(MG_ATTR)
 #undef MG_ATTR
     return e;
@@ -656,6 +775,25 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
         cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
         switch (flags) { MG_DENS_FLAG_SETS(MG_DENSW_CASE) default: break; }
 #undef MG_DENSW_CASE
+    }
+    if (search == 2 && (flags & (1 | 2 | 8 | 16))) {
+        uint32_t blocks = (P.cap + warps * 32 - 1) / (warps * 32);
+#define MG_DENSF_CASE(F)                                                                          \
+    case F:                                                                                       \
+        k_dens_fine<F><<<blocks, warps * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,        \
+                                                         cur.genes, s.scell, s.count, s.offset,   \
+                                                         s.subcnt, s.press, s.invdens, s.flist,   \
+                                                         s.fcount, s.counters + 3, s.work, s.ovf, \
+                                                         s.counters + 6, X);                      \
+        k_dens_ovf<F><<<(uint32_t)num_sms * 4, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out,    \
+                                                             cur.genes, s.scell, s.count,         \
+                                                             s.offset, s.press, s.invdens,        \
+                                                             s.flist, s.fcount, s.ovf,            \
+                                                             s.counters + 6, X);                  \
+        return;
+        cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
+        switch (flags) { MG_DENS_FLAG_SETS(MG_DENSF_CASE) default: break; }
+#undef MG_DENSF_CASE
     }
     uint32_t blocks = (P.cap + 255) / 256;
 #define MG_DENS_CASE(F)                                                                        \

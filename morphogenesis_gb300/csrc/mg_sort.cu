@@ -221,6 +221,7 @@ __global__ void __launch_bounds__(256) k_cellsort(const uint32_t* __restrict__ c
                                                   uint32_t* __restrict__ sorted,
                                                   uint32_t* __restrict__ newidx,
                                                   uint32_t* __restrict__ work,
+                                                  unsigned long long* __restrict__ subcnt,
                                                   uint32_t* __restrict__ big_list,
                                                   uint32_t* __restrict__ big_count,
                                                   uint32_t* __restrict__ err,
@@ -250,6 +251,9 @@ __global__ void __launch_bounds__(256) k_cellsort(const uint32_t* __restrict__ c
     sorted[off + r] = x;
     newidx[x] = off + r;
     work[off + w] = off + r;
+    // per sub-cell code counts, 8 bits each (with 2x2x2 sub-cells the codes are 0..7; the
+    // table was zeroed before this pass)
+    if (subcnt && n < (uint32_t)WARP_CELL_MAX) atomicAdd(subcnt + c, 1ull << (8 * (kx & 7u)));
 }
 
 constexpr int BIG_THREADS = 512;
@@ -309,11 +313,13 @@ __global__ void __launch_bounds__(BIG_THREADS) k_cellsort_big(uint32_t cap,
     }
 }
 
-void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, cudaStream_t st) {
+void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, bool subcounts,
+                     cudaStream_t st) {
     const uint32_t blocks = (P.cap + 255) / 256;
+    if (subcounts) cudaMemsetAsync(s.subcnt, 0, sizeof(unsigned long long) * P.cells, st);
     k_cellsort<<<blocks, 256, 0, st>>>(s.cell, s.count, s.offset, s.order, s.sub, s.sorted,
-                                        s.newidx, s.work, s.big_list, s.counters + 1,
-                                        s.counters + 2, s.counters + 3);
+                                        s.newidx, s.work, subcounts ? s.subcnt : nullptr,
+                                        s.big_list, s.counters + 1, s.counters + 2, s.counters + 3);
     k_cellsort_big<<<num_sms, BIG_THREADS, BLOCK_CELL_MAX * sizeof(uint32_t), st>>>(
         P.cap, s.cell, s.count, s.offset, s.order, s.sorted, s.newidx, s.work, s.big_list,
         s.counters + 1);

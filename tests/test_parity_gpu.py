@@ -191,6 +191,11 @@ def test_crowded_cell_orders(built, count):
     g, o = pair(d, n)
     g.Run(1, A.STEP_GENES); o.step(1, A.STEP_GENES)
     compare(g, o, bufs_float=[A.FPOS, A.FCONC])
+    # the per-lane sub-cell search scans such cells whole
+    g2, _ = pair(d, n)
+    g2.set_option(A.OPT_NEIGHBOR_SEARCH, 2)
+    g2.Run(1, A.STEP_GENES)
+    assert same_bits(g2.download(A.FCONC), o.download(A.FCONC))
 
 
 def test_dense_gene_lists(built, cfg0):
@@ -249,7 +254,7 @@ def test_warp_search_equals_direct_walk(built, param):
 
     d = demo.make_block((20, 12, 16), param, seed=8)
     outs = []
-    for mode in (0, 1):
+    for mode in (0, 1, 2):
         g = mg.FluidSystem(d.params, d.genome, d.n)
         g.set_option(A.OPT_NEIGHBOR_SEARCH, mode)
         g.TransferToCL(d.arrays)
@@ -257,7 +262,7 @@ def test_warp_search_equals_direct_walk(built, param):
         outs.append({b: g.download(b) for b in (A.FPOS, A.FVEL, A.FCONC, A.FPRESS, A.FDENSITY,
                                                  A.FFORCE, A.FELASTIDX, A.FPARTICLE_ID)})
     for b in outs[0]:
-        for m in (1,):
+        for m in (1, 2):
             assert same_bits(outs[0][b].view(np.float32), outs[m][b].view(np.float32)), f"buffer {b} mode {m}"
 
 
@@ -313,7 +318,7 @@ def test_launch_shapes_give_identical_results(built):
     ref.TransferToCL(d.arrays)
     ref.Run(30)
     want = {b: ref.download(b).view(np.uint32) for b in (A.FPOS, A.FVEL, A.FCONC, A.FELASTIDX, A.FPARTICLE_ID)}
-    for shape in ((4, 1, 1), (8, 1, 2), (4, 0, 2), (8, 0, 1)):
+    for shape in ((4, 1, 1, 1), (8, 1, 2, 1), (4, 0, 2, 1), (8, 0, 1, 1), (8, 0, 1, 2), (4, 0, 1, 2)):
         fs = mg.FluidSystem(d.params, d.genome, d.n)
         fs.TransferToCL(d.arrays)
         fs.set_tuning(*shape)
@@ -327,7 +332,7 @@ def test_launch_shapes_give_identical_results(built):
     fs.Run(10)
     before = fs.download(A.FPOS).copy()
     res = fs.autotune(3)
-    assert fs.tuning() == (res["dens_warps"], res["group_mode"], res["sub_bits"])
+    assert fs.tuning() == (res["dens_warps"], res["group_mode"], res["sub_bits"], res["search"])
     assert np.array_equal(fs.download(A.FPOS), before)
     fs.Run(20)
     for b, w in want.items():
