@@ -194,6 +194,18 @@ mg_status mg_upload(mg_handle h, int32_t buf_id, const void* host, size_t bytes)
 mg_status mg_download(mg_handle h, int32_t buf_id, void* host, size_t bytes);
 /* Page-locked host buffers for mg_upload/mg_download (copies from them run at full link
  * bandwidth).  Convenience with no counterpart in the reference. */
+/* One host exchange cycle with a single synchronisation: uploads `in`, runs nsteps steps with
+ * `flags`, downloads `out` (same buffer ids, layouts and byte counts as mg_upload /
+ * mg_download), all queued in order on the handle's stream.  For a host that exchanges state
+ * every step (the reference's TransferToCL / Run / TransferFromCL cycle); pinned buffers from
+ * mg_host_alloc give the full host-link bandwidth. */
+typedef struct mg_io {
+    int32_t buf_id;
+    void* host;
+    size_t bytes;
+} mg_io;
+mg_status mg_step_io(mg_handle h, const mg_io* in, uint32_t nin, uint32_t nsteps, uint32_t flags,
+                     const mg_io* out, uint32_t nout);
 mg_status mg_host_alloc(size_t bytes, void** out);
 mg_status mg_host_free(void* ptr);
 /* mNumPoints (particles in the grid after the last sort) and mActivePoints. */

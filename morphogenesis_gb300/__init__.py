@@ -212,6 +212,24 @@ class FluidSystem:
         """nsteps steps in the legacy Run() order (one sort per step), graph-captured."""
         self._check(self.lib.mg_step(self.h, int(nsteps), int(flags)))
 
+    def step_io(self, inputs: dict, nsteps: int = 1, flags: int = A.STEP_DEFAULT,
+                outputs: dict | None = None) -> None:
+        """Uploads `inputs` ({buffer id: array}), runs nsteps steps and downloads into `outputs`
+        ({buffer id: array}) with one synchronisation (mg_step_io).  Arrays must be C-contiguous
+        with the buffer's exact byte size; pinned arrays (pinned_empty) transfer fastest."""
+        outputs = outputs or {}
+        def pack(d):
+            arr = (A.IO * max(1, len(d)))()
+            for k, (b, x) in enumerate(d.items()):
+                if not x.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"buffer {b}: array must be C-contiguous")
+                arr[k].buf_id = int(b)
+                arr[k].host = x.ctypes.data
+                arr[k].bytes = x.nbytes
+            return arr
+        i, o = pack(inputs), pack(outputs)
+        self._check(self.lib.mg_step_io(self.h, i, len(inputs), nsteps, flags, o, len(outputs)))
+
     def time_steps(self, nsteps: int, flags: int = A.STEP_DEFAULT) -> float:
         ms = C.c_float()
         self._check(self.lib.mg_time_steps(self.h, int(nsteps), int(flags), C.byref(ms)))
@@ -295,6 +313,24 @@ class Batch:
 
     def Run(self, nsteps: int = 1, flags: int = A.STEP_DEFAULT) -> None:
         self._check(self.lib.mg_batch_step(self.h, nsteps, flags))
+
+    def step_io(self, inputs: dict, nsteps: int = 1, flags: int = A.STEP_DEFAULT,
+                outputs: dict | None = None) -> None:
+        """Uploads `inputs` ({buffer id: array}), runs nsteps steps and downloads into `outputs`
+        ({buffer id: array}) with one synchronisation (mg_step_io).  Arrays must be C-contiguous
+        with the buffer's exact byte size; pinned arrays (pinned_empty) transfer fastest."""
+        outputs = outputs or {}
+        def pack(d):
+            arr = (A.IO * max(1, len(d)))()
+            for k, (b, x) in enumerate(d.items()):
+                if not x.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"buffer {b}: array must be C-contiguous")
+                arr[k].buf_id = int(b)
+                arr[k].host = x.ctypes.data
+                arr[k].bytes = x.nbytes
+            return arr
+        i, o = pack(inputs), pack(outputs)
+        self._check(self.lib.mg_step_io(self.h, i, len(inputs), nsteps, flags, o, len(outputs)))
 
     def time_steps(self, nsteps: int, flags: int = A.STEP_DEFAULT) -> float:
         ms = C.c_float()

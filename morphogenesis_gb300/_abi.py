@@ -83,6 +83,11 @@ class MgError(RuntimeError):
         self.status = status
 
 
+class IO(C.Structure):
+    """mg_io: one buffer of an mg_step_io exchange."""
+    _fields_ = [("buf_id", C.c_int32), ("host", C.c_void_p), ("bytes", C.c_size_t)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/mg_abi.h
 H = C.c_void_p
 SIGNATURES = [
@@ -140,6 +145,7 @@ SIGNATURES = [
     ("mg_algorithmic_bytes", C.c_int, [H, C.c_char_p, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("mg_kernel_launches", C.c_uint64, [H]),
     ("mg_run_remodelling", C.c_int, [H]),
+    ("mg_step_io", C.c_int, [H, C.POINTER(IO), C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(IO), C.c_uint32]),
     ("mg_device_bytes", C.c_int, [H, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     ("mg_get_tuning", C.c_int, [H, C.POINTER(C.c_int32)]),
     ("mg_set_tuning", C.c_int, [H, C.POINTER(C.c_int32)]),

@@ -792,7 +792,7 @@ mg_status mg_buffer_bytes(mg_handle h, int32_t id, size_t* bytes) {
     return MG_OK;
 }
 
-mg_status mg_upload(mg_handle h, int32_t id, const void* host, size_t bytes) {
+static mg_status enqueue_upload(mg_handle h, int32_t id, const void* host, size_t bytes) {
     if (!h || !host) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
     size_t want = buf_bytes(h, id);
     if (want == 0 || id == MG_FBIN || id == MG_FBIN_COUNT || id == MG_FBIN_OFFSET ||
@@ -820,7 +820,7 @@ mg_status mg_upload(mg_handle h, int32_t id, const void* host, size_t bytes) {
     }
     if (dst) {
         MG_CUDA(h, cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, st));
-        return check_device(h);
+        return MG_OK;
     }
     mg_status s2 = ensure_staging(h, bytes);
     if (s2 != MG_OK) return s2;
@@ -836,10 +836,15 @@ mg_status mg_upload(mg_handle h, int32_t id, const void* host, size_t bytes) {
     } else {
         return fail(h, MG_ERR_INVALID_ARG, "buffer id " + std::to_string(id) + " cannot be uploaded");
     }
-    return check_device(h);
+    return MG_OK;
 }
 
-mg_status mg_download(mg_handle h, int32_t id, void* host, size_t bytes) {
+mg_status mg_upload(mg_handle h, int32_t id, const void* host, size_t bytes) {
+    mg_status st = enqueue_upload(h, id, host, bytes);
+    return st != MG_OK ? st : check_device(h);
+}
+
+static mg_status enqueue_download(mg_handle h, int32_t id, void* host, size_t bytes) {
     if (!h || !host) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
     size_t want = buf_bytes(h, id);
     if (want == 0) return fail(h, MG_ERR_INVALID_ARG, "buffer id " + std::to_string(id) + " not exchanged");
@@ -864,7 +869,7 @@ mg_status mg_download(mg_handle h, int32_t id, void* host, size_t bytes) {
     }
     if (src) {
         MG_CUDA(h, cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, st));
-        return check_device(h);
+        return MG_OK;
     }
     if (id == MG_FBIN_COUNT_ACTIVE_GENES || id == MG_FBIN_OFFSET_ACTIVE_GENES ||
         id == MG_FDENSE_LIST_LENGTHS || id == MG_FDENSE_LISTS) {
@@ -878,7 +883,7 @@ mg_status mg_download(mg_handle h, int32_t id, void* host, size_t bytes) {
                           : id == MG_FDENSE_LISTS ? base + 2 * C * NG
                           : base + 2 * C * NG + n * NG;
         MG_CUDA(h, cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, st));
-        return check_device(h);
+        return MG_OK;
     }
     mg_status s2 = ensure_staging(h, bytes);
     if (s2 != MG_OK) return s2;
@@ -899,6 +904,32 @@ mg_status mg_download(mg_handle h, int32_t id, void* host, size_t bytes) {
         return fail(h, MG_ERR_INVALID_ARG, "buffer id " + std::to_string(id) + " not exchanged");
     }
     MG_CUDA(h, cudaMemcpyAsync(host, sref, bytes, cudaMemcpyDeviceToHost, st));
+    return MG_OK;
+}
+
+mg_status mg_download(mg_handle h, int32_t id, void* host, size_t bytes) {
+    mg_status st = enqueue_download(h, id, host, bytes);
+    return st != MG_OK ? st : check_device(h);
+}
+
+// One host exchange cycle with a single synchronisation: uploads, steps, downloads, all
+// enqueued in order on the handle's stream.
+mg_status mg_step_io(mg_handle h, const mg_io* in, uint32_t nin, uint32_t nsteps, uint32_t flags,
+                     const mg_io* out, uint32_t nout) {
+    if (!h || (nin && !in) || (nout && !out)) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    if (h->profile) return fail(h, MG_ERR_INVALID_ARG, "mg_step_io: profiling is on");
+    for (uint32_t k = 0; k < nin; k++) {
+        mg_status st = enqueue_upload(h, in[k].buf_id, in[k].host, in[k].bytes);
+        if (st != MG_OK) return st;
+    }
+    if (nsteps) {
+        mg_status st = run_steps(h, nsteps, flags);
+        if (st != MG_OK) return st;
+    }
+    for (uint32_t k = 0; k < nout; k++) {
+        mg_status st = enqueue_download(h, out[k].buf_id, out[k].host, out[k].bytes);
+        if (st != MG_OK) return st;
+    }
     return check_device(h);
 }
 

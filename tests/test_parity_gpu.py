@@ -337,3 +337,23 @@ def test_launch_shapes_give_identical_results(built):
     fs.Run(20)
     for b, w in want.items():
         assert np.array_equal(fs.download(b).view(np.uint32), w), f"after autotune, buffer {b}"
+
+
+def test_step_io_equals_separate_calls(built, cfg0):
+    import morphogenesis_gb300 as mg
+
+    bufs = (A.FPOS, A.FVEL, A.FVEVAL, A.FCONC, A.FELASTIDX)
+    a = mg.FluidSystem(cfg0.params, cfg0.genome, cfg0.n)
+    b = mg.FluidSystem(cfg0.params, cfg0.genome, cfg0.n)
+    for fs in (a, b):
+        fs.TransferToCL(cfg0.arrays)
+        fs.Run(3)
+    host = {k: a.download(k) for k in bufs}
+    host[A.FVEL] = (host[A.FVEL] * np.float32(0.5)).astype(np.float32)  # the host edits state
+    out_a = {k: np.empty_like(v) for k, v in host.items()}
+    for k, v in host.items():
+        b.upload(k, v)
+    b.Run(2)
+    a.step_io(host, 2, A.STEP_DEFAULT, out_a)
+    for k in bufs:
+        assert np.array_equal(out_a[k].view(np.uint32), b.download(k).view(np.uint32)), f"buffer {k}"
