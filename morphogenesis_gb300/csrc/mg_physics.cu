@@ -642,13 +642,54 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_fi
 }
 
 // ---- overflow pass ----------------------------------------------------------------------------
-// Particles queued by the warp search (more neighbours than NL_CAP, only in dense clumps), one
-// warp per particle.  The window cells are walked in the reference order, 32 candidates at a
-// time; each neighbour is then taken in ascending sorted index by every lane: all lanes keep the
-// density partial sums, lane t (mod 16) accumulates species t with the same expression and order
-// as the one-thread walk, lane 0 records the force list.  Lane 0 then runs the common epilogue.
+// Particles queued by the searches (more neighbours than NL_CAP, only in dense clumps), one
+// warp per particle, in two phases that repeat over segments of OVF_SEG hits:
+//  collect : the window cells (in the reference order, 32 at a time, one per lane) form one
+//            stream of candidates; each lane takes one candidate per chunk (its cell found by a
+//            binary search over the cells' running counts), several chunks in flight, and the
+//            hits are compacted in order into shared memory with their distance, window-cell
+//            index and concentrations;
+//  apply   : the hits are taken in that order by every lane: the density partial sum of each
+//            cell, species t (mod 16) of the diffusion and neighbour sums in lane t with the
+//            one-thread walk's expression and order, the force list in lane 0.
+// Lane 0 then runs the common epilogue.
+constexpr int OVF_SEG = 64;
+
+// Takes a segment's hits in order (the apply phase of the overflow pass).
 template <int FLAGS>
-__global__ void __launch_bounds__(256) k_dens_ovf(
+__device__ __forceinline__ void ovf_apply(const DevParams& P, uint32_t p, uint32_t lane, uint32_t t,
+                                          uint32_t* __restrict__ flist, const float* sd,
+                                          const uint32_t* sq, const uint8_t* sc, const float4 (*scj)[NTF / 4],
+                                          uint32_t nh, int& lastcell, float& sum, float& part,
+                                          uint32_t& nf, float& nc_t, float& ms_t, uint32_t& mcnt,
+                                          float dif_t, float cur_t) {
+    using F = DF<FLAGS>;
+    __syncwarp();
+    for (uint32_t h = 0; h < nh; h++) {
+        const float d = sd[h];
+        const int c = sc[h];
+        if (c != lastcell) {  // first hit of the next cell: flush the previous partial
+            sum += part;
+            part = 0.f;
+            lastcell = c;
+        }
+        if (d < 1.f) {
+            if (lane == 0 && nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = sq[h];
+            nf++;
+        }
+        if (F::DENS && d < P.r2) part += wendland_term(d, P.sr);
+        if ((F::DIFF || F::MEAN) && d < P.r2diff) {
+            const float cj = reinterpret_cast<const float*>(scj[h])[t];
+            if (F::MEAN) ms_t += cj;
+            if (F::DIFF && dif_t != 0.f) nc_t += (dif_t * ((P.r2diff - d) * P.d2)) * (cj - cur_t);
+            mcnt++;
+        }
+    }
+    __syncwarp();
+}
+
+template <int FLAGS>
+__global__ void __launch_bounds__(256, 1) k_dens_ovf(
     DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
     const float* __restrict__ conc_in, float* __restrict__ conc_out,
     const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
@@ -657,7 +698,11 @@ __global__ void __launch_bounds__(256) k_dens_ovf(
     uint32_t* __restrict__ fcount, const uint32_t* __restrict__ ovf,
     const uint32_t* __restrict__ ovf_count, DensExtra X) {
     using F = DF<FLAGS>;
-    __shared__ float4 s_cj[256 / 32][32][NTF / 4];  // concentrations of this batch's neighbours
+    constexpr bool CONC = F::DIFF || F::MEAN;
+    __shared__ float4 s_cj[256 / 32][OVF_SEG][NTF / 4];  // concentrations of the segment's hits
+    __shared__ float s_d[256 / 32][OVF_SEG];
+    __shared__ uint32_t s_q[256 / 32][OVF_SEG];
+    __shared__ uint8_t s_c[256 / 32][OVF_SEG];
     const uint32_t lane = threadIdx.x & 31u, t = lane & 15u, wl = threadIdx.x >> 5;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -665,59 +710,101 @@ __global__ void __launch_bounds__(256) k_dens_ovf(
     if (nq > P.cap) nq = P.cap;
     float R2 = 1.f;
     if (F::DENS) R2 = fmaxf(R2, P.r2);
-    if (F::DIFF || F::MEAN) R2 = fmaxf(R2, P.r2diff);
+    if (CONC) R2 = fmaxf(R2, P.r2diff);
     for (uint32_t e = gw; e < nq; e += nw) {
         const uint32_t p = ovf[e];
         const float4 ip = pos[p];
         const float cur_t = (F::DIFF || F::GENE || F::MEAN) ? conc_in[(size_t)p * NTF + t] : 0.f;
         const float dif_t = F::DIFF ? G->diff[t] : 0.f;
         const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
-        float nc_t = 0.f, ms_t = 0.f, sum = 0.f;
+        float nc_t = 0.f, ms_t = 0.f, sum = 0.f, part = 0.f;
         uint32_t mcnt = 0, nf = 0;
+        int lastcell = -1;
         const uint32_t base = scell[p] - (uint32_t)P.nadj;
-        for (int c = 0; c < P.adjcnt; c++) {
-            const uint32_t cellc = base + (uint32_t)P.adj[c];
-            const uint32_t cnt = count[cellc];
-            if (cnt == 0) continue;
-            const uint32_t off = offset[cellc];
-            float part = 0.f;
-            for (uint32_t b = 0; b < cnt; b += 32) {
-                const bool valid = b + lane < cnt;
-                float dsq = 0.f;
-                if (valid) {
-                    const float4 jp = pos[off + b + lane];
-                    const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
-                    dsq = dx * dx + dy * dy + dz * dz;
-                }
-                unsigned hits = __ballot_sync(0xffffffffu, valid && dsq < R2 && dsq > 0.f);
-                if ((F::DIFF || F::MEAN) && ((hits >> lane) & 1u) && dsq < P.r2diff) {
-                    const float4* c4 = reinterpret_cast<const float4*>(conc_in + (size_t)(off + b + lane) * NTF);
-#pragma unroll
-                    for (int k = 0; k < NTF / 4; k++) s_cj[wl][lane][k] = c4[k];
-                }
-                __syncwarp();
-                while (hits) {
-                    const int src = __ffs(hits) - 1;
-                    hits &= hits - 1;
-                    const float d = __shfl_sync(0xffffffffu, dsq, src);
-                    const uint32_t q = off + b + (uint32_t)src;
-                    if (d < 1.f) {
-                        if (lane == 0 && nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
-                        nf++;
-                    }
-                    if (F::DENS && d < P.r2) part += wendland_term(d, P.sr);
-                    if ((F::DIFF || F::MEAN) && d < P.r2diff) {
-                        const float cj = reinterpret_cast<const float*>(s_cj[wl][src])[t];
-                        if (F::MEAN) ms_t += cj;
-                        if (F::DIFF && dif_t != 0.f)
-                            nc_t += (dif_t * ((P.r2diff - d) * P.d2)) * (cj - cur_t);
-                        mcnt++;
-                    }
-                }
-                __syncwarp();
+        uint32_t nh = 0;  // hits of the current segment
+        for (int cg = 0; cg < P.adjcnt; cg += 32) {
+            // this group's window cells: count, offset and running start, one per lane
+            const int ci = cg + (int)lane;
+            uint32_t cnt = 0, off = 0;
+            if (ci < P.adjcnt) {
+                const uint32_t cellc = base + (uint32_t)P.adj[ci];
+                cnt = count[cellc];
+                if (cnt) off = offset[cellc];
             }
-            if (F::DENS) sum += part;
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int dd = 1; dd < 32; dd <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, dd);
+                if ((int)lane >= dd) incl += v;
+            }
+            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            const uint32_t start = incl - cnt;
+            for (uint32_t b0 = 0; b0 < total; b0 += 128) {
+                // four chunks of 32 candidates in flight
+                float dq[4];
+                uint32_t qq[4], cc[4];
+                bool hit[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const uint32_t k = b0 + (uint32_t)u * 32u + lane;
+                    hit[u] = false;
+                    dq[u] = 0.f;
+                    qq[u] = 0u;
+                    cc[u] = 0u;
+                    // the cell holding candidate k: the last lane whose start is <= k
+                    uint32_t lo = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const uint32_t st = __shfl_sync(0xffffffffu, start, (int)(lo + step) & 31);
+                        if (lo + step < 32 && st <= k) lo += step;
+                    }
+                    if (k < total) {
+                        const uint32_t sl = __shfl_sync(0xffffffffu, start, (int)lo);
+                        const uint32_t ol = __shfl_sync(0xffffffffu, off, (int)lo);
+                        qq[u] = ol + (k - sl);
+                        cc[u] = (uint32_t)cg + lo;
+                    } else {
+                        __shfl_sync(0xffffffffu, start, (int)lo);
+                        __shfl_sync(0xffffffffu, off, (int)lo);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const uint32_t k = b0 + (uint32_t)u * 32u + lane;
+                    if (k < total) {
+                        const float4 jp = pos[qq[u]];
+                        const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+                        dq[u] = dx * dx + dy * dy + dz * dz;
+                        hit[u] = dq[u] < R2 && dq[u] > 0.f;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const unsigned ball = __ballot_sync(0xffffffffu, hit[u]);
+                    const uint32_t nb = (uint32_t)__popc(ball);
+                    if (nh + nb > (uint32_t)OVF_SEG) {  // segment full: take what it holds
+                        ovf_apply<FLAGS>(P, p, lane, t, flist, s_d[wl], s_q[wl], s_c[wl], s_cj[wl], nh,
+                                         lastcell, sum, part, nf, nc_t, ms_t, mcnt, dif_t, cur_t);
+                        nh = 0;
+                    }
+                    if (hit[u]) {
+                        const uint32_t slot = nh + (uint32_t)__popc(ball & ((1u << lane) - 1u));
+                        s_d[wl][slot] = dq[u];
+                        s_q[wl][slot] = qq[u];
+                        s_c[wl][slot] = (uint8_t)cc[u];
+                        if (CONC && dq[u] < P.r2diff) {
+                            const float4* c4 = reinterpret_cast<const float4*>(conc_in + (size_t)qq[u] * NTF);
+#pragma unroll
+                            for (int k4 = 0; k4 < NTF / 4; k4++) s_cj[wl][slot][k4] = c4[k4];
+                        }
+                    }
+                    nh += nb;
+                }
+            }
         }
+        ovf_apply<FLAGS>(P, p, lane, t, flist, s_d[wl], s_q[wl], s_c[wl], s_cj[wl], nh, lastcell,
+                         sum, part, nf, nc_t, ms_t, mcnt, dif_t, cur_t);
+        if (F::DENS) sum += part;
         float cur[NTF], nc[NTF], ms[NTF];
 #pragma unroll
         for (int k = 0; k < NTF; k++) {
