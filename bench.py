@@ -91,6 +91,14 @@ class Dist:
             self.td.destroy_process_group()
 
 
+def whole_job_rate(dist, n_local: int, steps: int, ms_local: float):
+    """Particle-steps/s of the whole job: all ranks' particle-steps over the slowest rank's
+    time (replicas: weak scaling).  Returns (rate, max ms)."""
+    ms_max = dist.reduce(ms_local, "max")
+    total = dist.reduce(float(n_local * steps), "sum")
+    return total / (ms_max / 1e3), ms_max
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -420,9 +428,7 @@ def main():
     dist.barrier()
     clk = clocks.stop()
     launches = fs.kernel_launches() - launches0
-    ms_max = dist.reduce(ms, "max")
-    total_particle_steps = dist.reduce(float(n * args.steps), "sum")
-    value = total_particle_steps / (ms_max / 1e3)
+    value, ms_max = whole_job_rate(dist, n, args.steps, ms)
 
     # ---- per-kernel device times over K profiled steps (events around every launch) ----
     fs.profile(True)
