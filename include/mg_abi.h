@@ -321,6 +321,49 @@ uint64_t mg_kernel_launches(mg_handle h);
  * (arena, upload staging, dense gene lists and surrogate buffers once made). */
 mg_status mg_device_bytes(mg_handle h, size_t* arena, size_t* total);
 
+/* ---- files (fileCL_IO.cpp formats) ------------------------------------------------------------ */
+/* SimParams.txt fields (ReadSimParams / WriteSimParams, fileCL_IO.cpp:471-600). */
+typedef struct mg_simparams {
+    float time, dt, simscale, grid_density, visc, surface_tension, rest_density, spacing, mass,
+        radius, dist, smooth_radius, intstiff, extstiff, extdamp, accel_limit, vel_limit, grav,
+        ground_slope, force_min, force_max, force_freq;
+    float plane_grav_dir[3];
+    float grid_size;
+    float volmin[3], volmax[3], initmin[3], initmax[3];
+} mg_simparams;
+mg_status mg_read_simparams(const char* path, mg_simparams* out);
+mg_status mg_write_simparams(const char* dir, const mg_simparams* sp); /* writes dir/SimParams.txt */
+/* The set-up ReadPointsCSV2 performs before allocating (fileCL_IO.cpp:353-361): grid cell
+ * 2 * smooth radius / grid density, SetupSpacing's density from spacing and particle bounds
+ * (fluid_system.cpp:2521-2546), SetupGrid, gravity = plane direction * gravity
+ * (UpdateParams, fluid_system.cpp:617).  gsrch_override 0 keeps SetupGrid's own gsrch. */
+mg_status mg_fparams_from_simparams(const mg_simparams* sp, int32_t gsrch_override, mg_fparams* out);
+/* genome.csv (ReadGenome / WriteGenome, fileCL_IO.cpp:71-249).  The reference's integer fields
+ * are read as floats; integer_fields = 1 writes them as integers (the reference format, values
+ * rounded), 0 writes the floats in the same layout. */
+mg_status mg_read_genome(const char* path, mg_genome* out);
+mg_status mg_write_genome(const char* dir, const mg_genome* g, int32_t integer_fields); /* dir/genome.csv */
+/* Particle CSV of SavePointsCSV2 / ReadPointsCSV2 (fileCL_IO.cpp:250-469) over host arrays in
+ * the mg_upload layouts (n particles; epigen is [16][n]). */
+typedef struct mg_points {
+    uint32_t n;
+    float* pos;            /* [n][4] */
+    float* vel;            /* [n][4] */
+    uint32_t* age;         /* [n] */
+    uint32_t* color;       /* [n] */
+    uint32_t* elastidx;    /* [n][54] */
+    uint32_t* particle_id; /* [n] */
+    uint32_t* mass_radius; /* [n] mass | radius << 16 */
+    uint32_t* nerve;       /* [n] */
+    uint32_t* pidx;        /* [n][12] */
+    float* conc;           /* [n][16] */
+    uint32_t* epigen;      /* [16][n] */
+} mg_points;
+mg_status mg_count_points_csv(const char* path, uint32_t* n); /* lines - 1 */
+mg_status mg_read_points_csv(const char* path, mg_points* pts);
+/* writes dir/particles_pos_vel_color%04d.csv with frame + 100000 (SavePointsCSV2's naming) */
+mg_status mg_write_points_csv(const char* dir, int32_t frame, const mg_points* pts);
+
 /* ---- batched instances (parameter sweeps) --------------------------------------------------- */
 /* A batch steps many independent systems together (each keeps its own particles, grid,
  * parameters and genome): one CUDA graph launch per step advances every member, the members'

@@ -83,6 +83,24 @@ class MgError(RuntimeError):
         self.status = status
 
 
+class SimParams(C.Structure):
+    """mg_simparams: the fields of SimParams.txt."""
+    _fields_ = [(n, C.c_float) for n in (
+        "time", "dt", "simscale", "grid_density", "visc", "surface_tension", "rest_density", "spacing",
+        "mass", "radius", "dist", "smooth_radius", "intstiff", "extstiff", "extdamp", "accel_limit",
+        "vel_limit", "grav", "ground_slope", "force_min", "force_max", "force_freq")] + [
+        ("plane_grav_dir", C.c_float * 3), ("grid_size", C.c_float), ("volmin", C.c_float * 3),
+        ("volmax", C.c_float * 3), ("initmin", C.c_float * 3), ("initmax", C.c_float * 3)]
+
+
+class Points(C.Structure):
+    """mg_points: host arrays of a particle CSV."""
+    _fields_ = [("n", C.c_uint32), ("pos", C.c_void_p), ("vel", C.c_void_p), ("age", C.c_void_p),
+                ("color", C.c_void_p), ("elastidx", C.c_void_p), ("particle_id", C.c_void_p),
+                ("mass_radius", C.c_void_p), ("nerve", C.c_void_p), ("pidx", C.c_void_p),
+                ("conc", C.c_void_p), ("epigen", C.c_void_p)]
+
+
 class IO(C.Structure):
     """mg_io: one buffer of an mg_step_io exchange."""
     _fields_ = [("buf_id", C.c_int32), ("host", C.c_void_p), ("bytes", C.c_size_t)]
@@ -145,6 +163,14 @@ SIGNATURES = [
     ("mg_algorithmic_bytes", C.c_int, [H, C.c_char_p, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("mg_kernel_launches", C.c_uint64, [H]),
     ("mg_run_remodelling", C.c_int, [H]),
+    ("mg_read_simparams", C.c_int, [C.c_char_p, C.POINTER(SimParams)]),
+    ("mg_write_simparams", C.c_int, [C.c_char_p, C.POINTER(SimParams)]),
+    ("mg_fparams_from_simparams", C.c_int, [C.POINTER(SimParams), C.c_int32, C.POINTER(FParams)]),
+    ("mg_read_genome", C.c_int, [C.c_char_p, C.POINTER(Genome)]),
+    ("mg_write_genome", C.c_int, [C.c_char_p, C.POINTER(Genome), C.c_int32]),
+    ("mg_count_points_csv", C.c_int, [C.c_char_p, C.POINTER(C.c_uint32)]),
+    ("mg_read_points_csv", C.c_int, [C.c_char_p, C.POINTER(Points)]),
+    ("mg_write_points_csv", C.c_int, [C.c_char_p, C.c_int32, C.POINTER(Points)]),
     ("mg_step_io", C.c_int, [H, C.POINTER(IO), C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(IO), C.c_uint32]),
     ("mg_device_bytes", C.c_int, [H, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     ("mg_get_tuning", C.c_int, [H, C.POINTER(C.c_int32)]),

@@ -30,6 +30,7 @@ UNITS = {
     "mg_api.cu": [],
     "mg_noalloc.cu": [],
     "mg_remodel.cu": ["-fmad=false"],
+    "mg_files.cpp": [],
 }
 
 
