@@ -237,22 +237,26 @@ __global__ void k_col_stats(const float* __restrict__ d, uint64_t rows, int cols
 // =============================================================================================
 // Inference on tcgen05
 // =============================================================================================
-// Eight warps, two CTAs per SM.  Warp w reads TMEM lanes 32(w%4)..32(w%4)+31 (its tile rows)
-// and, in the hidden-layer epilogues, columns 64(w/4)..64(w/4)+63.
-constexpr int INF_THREADS = 256;
-constexpr int INF_CTAS_PER_SM = 2;
-constexpr int INF_TMEM_COLS = 256;
+// One CTA per SM holding the weights once, with INF_GROUPS independent groups of eight warps,
+// each with its own 128-particle tile in flight (activation buffer, TMEM columns, mbarrier):
+// while one group runs its GELU epilogue the tensor core works on another group's layer.  In a
+// group, warp w reads TMEM lanes 32(w%4)..32(w%4)+31 (its tile rows) and, in the hidden-layer
+// epilogues, columns 64(w/4)..64(w/4)+63 of its group's 128.
+constexpr int INF_GROUPS = 3;
+constexpr int INF_GROUP_THREADS = 256;
+constexpr int INF_THREADS = INF_GROUPS * INF_GROUP_THREADS;
+constexpr int INF_TMEM_COLS = 512;  // allocation (power of two); groups use 128 columns each
 constexpr uint32_t MBAR_SPIN_LIMIT = 1u << 24;
 
-// Shared memory image of one inference CTA.
 struct InferSmem {
     bf16 w1[MLP_H * MLP_IN];    // 12 KB  B operand layer 1 (N=128 x K=48)
     bf16 w2[MLP_H * MLP_H];     // 32 KB  B operand layer 2 (N=128 x K=128)
     bf16 w3[MLP_OUT * MLP_H];   //  4 KB  B operand layer 3 (N=16 x K=128)
-    bf16 a1[128 * MLP_IN];      // 12 KB  A operand layer 1 (M=128 x K=48)
-    bf16 a2[128 * MLP_H];       // 32 KB  A operand layers 2 and 3 (M=128 x K=128)
+    // per group: A operand of layer 1 (128 x 48, the first 12 KB) and of layers 2 and 3
+    // (128 x 128); layer 1 has finished reading its operand before the epilogue overwrites it
+    bf16 act[INF_GROUPS][128 * MLP_H];
     float b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
-    unsigned long long mbar;
+    unsigned long long mbar[INF_GROUPS];
     uint32_t tmem_base;
 };
 
@@ -373,10 +377,27 @@ __device__ __forceinline__ void issue_layer(uint32_t d_tmem, const bf16* a, cons
     }
 }
 
-// Surrogate step: for each particle p < nactive, conc_out[p] = conc_in[p] + MLP(features[p]).
-// Particles under judgement (sampled this step) or already handed to the plain method
-// (bit 31 of their gene word) compare against / take the plain update in conc_plain.
-__global__ void __launch_bounds__(INF_THREADS, INF_CTAS_PER_SM) k_mlp_infer(
+// Named barrier of one warp group (ids 1..INF_GROUPS; 0 is __syncthreads).
+__device__ __forceinline__ void group_sync(uint32_t g) {
+    asm volatile("bar.sync %0, %1;\n" ::"r"(g + 1u), "r"((uint32_t)INF_GROUP_THREADS) : "memory");
+}
+// AND of a predicate over one warp group (a barrier too).
+__device__ __forceinline__ bool group_and(uint32_t g, bool v) {
+    uint32_t out;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.and.pred p, %2, %3, q;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(out)
+        : "r"((uint32_t)v), "r"(g + 1u), "r"((uint32_t)INF_GROUP_THREADS)
+        : "memory");
+    return out != 0;
+}
+
+// Surrogate step: for each particle p < nactive, conc_out[p] = conc_in[p] + s_p * MLP(features[p])
+// (s_p the particle's input scale, 1 without feat_scale).  Particles under judgement (sampled
+// this step) or already handed to the plain method (bit 31 of their gene word) compare against /
+// take the plain update in conc_plain.
+__global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
     InferWeights W, const bf16* __restrict__ feat, const float* __restrict__ feat_scale,
     const float* conc_in,
     const float* __restrict__ conc_plain, float* conc_out, uint32_t* __restrict__ genes,
@@ -386,6 +407,9 @@ __global__ void __launch_bounds__(INF_THREADS, INF_CTAS_PER_SM) k_mlp_infer(
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t g = tid / INF_GROUP_THREADS;            // warp group
+    const uint32_t gtid = tid % INF_GROUP_THREADS;         // thread in the group
+    const uint32_t gwarp = gtid >> 5;
     const uint32_t n = nactive_p ? *nactive_p : ntotal_override;
     const uint32_t step = step_p ? *step_p : 0u;
     const bool judge_step = judge_period && judge_stride && (step % judge_period) == 0;
@@ -408,9 +432,8 @@ __global__ void __launch_bounds__(INF_THREADS, INF_CTAS_PER_SM) k_mlp_infer(
         }
         if (tid < MLP_OUT) S.b3[tid] = W.b3[tid];
     }
-    const uint32_t mbar = smem_u32(&S.mbar);
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+    if (tid < INF_GROUPS) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&S.mbar[tid])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     if (warp == 0) {  // one warp allocates the tensor memory of the CTA
@@ -424,15 +447,17 @@ __global__ void __launch_bounds__(INF_THREADS, INF_CTAS_PER_SM) k_mlp_infer(
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = S.tmem_base;
-    const uint32_t quad = warp & 3u, half = warp >> 2;
+    const uint32_t mbar = smem_u32(&S.mbar[g]);
+    const uint32_t tmem = S.tmem_base + g * 128u;        // this group's 128 columns
+    bf16* act = S.act[g];
+    const uint32_t quad = gwarp & 3u, half = gwarp >> 2;
     const uint32_t lane_addr = tmem + ((quad * 32u) << 16);  // this warp's TMEM lanes
-    const uint32_t row = quad * 32u + (tid & 31u);           // tile row = this thread's particle
+    const uint32_t row = quad * 32u + (gtid & 31u);          // tile row = this thread's particle
     uint32_t phase = 0;
     bool ok = true;
 
     const uint32_t ntiles = (n + 127) / 128;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (uint32_t tile = blockIdx.x * INF_GROUPS + g; tile < ntiles; tile += gridDim.x * INF_GROUPS) {
         const uint32_t p = tile * 128u + row;
         const bool live = p < n;
         // layer-1 operand: the particle's 48 bf16 features (zeros past the end), three of the
@@ -442,22 +467,22 @@ __global__ void __launch_bounds__(INF_THREADS, INF_CTAS_PER_SM) k_mlp_infer(
 #pragma unroll
             for (uint32_t c = half * 3; c < half * 3 + 3; c++) {
                 const uint4 v = live ? src[c] : make_uint4(0u, 0u, 0u, 0u);
-                *reinterpret_cast<uint4*>(S.a1 + core_offset(row, c * 8, MLP_IN)) = v;
+                *reinterpret_cast<uint4*>(act + core_offset(row, c * 8, MLP_IN)) = v;
             }
         }
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
+        group_sync(g);
         tc_fence_after();
-        if (tid == 0) {
-            issue_layer(tmem + 0, S.a1, S.w1, MLP_IN, MLP_H);
+        if (gtid == 0) {
+            issue_layer(tmem, act, S.w1, MLP_IN, MLP_H);
             mma_commit(mbar);
         }
-        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        ok = group_and(g, mbar_wait(mbar, phase));
         phase ^= 1u;
         if (!ok) break;
         tc_fence_after();
-        // layer-1 epilogue: bias + GELU -> layer-2 operand
+        // layer-1 epilogue: bias + GELU -> layer-2 operand (layer 1 has finished with `act`)
 #pragma unroll
         for (uint32_t c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
             float v[32];
@@ -467,44 +492,44 @@ __global__ void __launch_bounds__(INF_THREADS, INF_CTAS_PER_SM) k_mlp_infer(
                 float h[8];
 #pragma unroll
                 for (int i = 0; i < 8; i++) h[i] = gelu(v[q + i] + S.b1[c0 + q + i]);
-                put8(S.a2, row, c0 + q, MLP_H, h);
+                put8(act, row, c0 + q, MLP_H, h);
             }
         }
+        // the accumulator columns are read: layer 2 may overwrite them
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
+        group_sync(g);
         tc_fence_after();
-        if (tid == 0) {
-            issue_layer(tmem + 128, S.a2, S.w2, MLP_H, MLP_H);
+        if (gtid == 0) {
+            issue_layer(tmem, act, S.w2, MLP_H, MLP_H);
             mma_commit(mbar);
         }
-        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        ok = group_and(g, mbar_wait(mbar, phase));
         phase ^= 1u;
         if (!ok) break;
         tc_fence_after();
-        // layer-2 epilogue -> layer-3 operand.  The barrier fired, so the layer-2 MMAs have
-        // finished reading a2 and it can be overwritten.
+        // layer-2 epilogue -> layer-3 operand (layer 2 has finished reading `act`)
 #pragma unroll
         for (uint32_t c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
             float v[32];
-            tmem_ld32(lane_addr + 128 + c0, v);
+            tmem_ld32(lane_addr + c0, v);
 #pragma unroll
             for (int q = 0; q < 32; q += 8) {
                 float h[8];
 #pragma unroll
                 for (int i = 0; i < 8; i++) h[i] = gelu(v[q + i] + S.b2[c0 + q + i]);
-                put8(S.a2, row, c0 + q, MLP_H, h);
+                put8(act, row, c0 + q, MLP_H, h);
             }
         }
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
+        group_sync(g);
         tc_fence_after();
-        if (tid == 0) {
-            issue_layer(tmem + 0, S.a2, S.w3, MLP_H, MLP_OUT);
+        if (gtid == 0) {
+            issue_layer(tmem, act, S.w3, MLP_H, MLP_OUT);
             mma_commit(mbar);
         }
-        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        ok = group_and(g, mbar_wait(mbar, phase));
         phase ^= 1u;
         if (!ok) break;
         tc_fence_after();
@@ -565,14 +590,15 @@ __global__ void __launch_bounds__(INF_THREADS, INF_CTAS_PER_SM) k_mlp_infer(
                 for (int k = 0; k < 4; k++) co[k] = make_float4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
             }
         }
+        // the output columns are read before the next tile's layer 1 overwrites them
         tc_fence_before();
-        __syncthreads();
+        group_sync(g);
         tc_fence_after();
     }
     if (!ok) {
-        // a wait gave up: record it and give the MMAs in flight one more bounded wait before
-        // the tensor memory is released
-        if (tid == 0) {
+        // a wait gave up: record it and give the group's MMAs in flight one more bounded wait
+        // before the tensor memory is released
+        if (gtid == 0) {
             atomicOr(err, MLP_ERR_MBAR_TIMEOUT);
             mbar_wait(mbar, phase ^ 1u);
         }
@@ -580,7 +606,7 @@ __global__ void __launch_bounds__(INF_THREADS, INF_CTAS_PER_SM) k_mlp_infer(
     tc_fence_before();
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(S.tmem_base),
                      "r"((uint32_t)INF_TMEM_COLS)
                      : "memory");
 }
@@ -869,7 +895,7 @@ void launch_mlp_infer(const Mlp* m, const bf16* feat, const float* feat_scale, c
                       float* conc_out, uint32_t* genes, const uint32_t* nactive, uint32_t n_override,
                       const uint32_t* step, uint32_t period, uint32_t stride, float threshold,
                       uint32_t* stats, uint32_t* err, int num_sms, cudaStream_t st) {
-    k_mlp_infer<<<num_sms * INF_CTAS_PER_SM, INF_THREADS, sizeof(InferSmem), st>>>(
+    k_mlp_infer<<<num_sms, INF_THREADS, sizeof(InferSmem), st>>>(
         m->inf, feat, feat_scale, conc_in, conc_plain, conc_out, genes, nactive, n_override, step,
         period, stride,
         threshold, stats, err);

@@ -51,11 +51,13 @@ __device__ __forceinline__ float tanh_hw(float x) {
 constexpr float GELU_K0 = 0.7978845608028654f;  // sqrt(2/pi)
 constexpr float GELU_K1 = 0.044715f;
 __device__ __forceinline__ float gelu(float x) {
-    const float u = GELU_K0 * (x + GELU_K1 * x * x * x);
-    return 0.5f * x * (1.0f + tanh_hw(u));
+    // 0.5 x (1 + tanh(x (k0 + k0 k1 x^2))) as four fused operations around the tanh
+    const float u = x * __fmaf_rn(GELU_K0 * GELU_K1, x * x, GELU_K0);
+    const float hx = 0.5f * x;
+    return __fmaf_rn(hx, tanh_hw(u), hx);
 }
 __device__ __forceinline__ float gelu_grad(float x) {
-    const float u = GELU_K0 * (x + GELU_K1 * x * x * x);
+    const float u = x * __fmaf_rn(GELU_K0 * GELU_K1, x * x, GELU_K0);
     const float t = tanh_hw(u);
     return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * GELU_K0 * (1.0f + 3.0f * GELU_K1 * x * x);
 }
