@@ -96,6 +96,9 @@ enum mg_step_flags {
     MG_STEP_REMODEL = 1u << 2,   /* bond break/re-form (heal) */
     MG_STEP_FREEZE = 1u << 3,    /* bonds do not break this step (FParams.freeze) */
     MG_STEP_SURROGATE = 1u << 4, /* learned reaction instead of the plain gene reaction */
+    MG_STEP_SPECIAL = 1u << 5,   /* SpecialParticlesCL after the integration: gene 12 particles are
+                                    actuated (externalActuation), gene 11 particles stay fixed
+                                    (fixedParticles), fluid_system_cuda.cu:3617-3705 */
     MG_STEP_DEFAULT = MG_STEP_PHYSICS | MG_STEP_GENES
 };
 

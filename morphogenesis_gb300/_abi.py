@@ -29,7 +29,7 @@ PSMOOTHRADIUS, PINTSTIFF, PEXTSTIFF, PEXTDAMP, PACCEL_LIMIT, PVEL_LIMIT = 12, 13
 PGROUND_SLOPE, PFORCE_MIN, PFORCE_MAX, PFORCE_FREQ, PSURFACE_TENSION = 19, 20, 21, 23, 24
 PACTUATION_FACTOR, PACTUATION_PERIOD, PDT, PTIME, PFREEZE = 25, 26, 100, 101, 102
 
-STEP_PHYSICS, STEP_GENES, STEP_REMODEL, STEP_FREEZE, STEP_SURROGATE = 1, 2, 4, 8, 16
+STEP_PHYSICS, STEP_GENES, STEP_REMODEL, STEP_FREEZE, STEP_SURROGATE, STEP_SPECIAL = 1, 2, 4, 8, 16, 32
 STEP_DEFAULT = STEP_PHYSICS | STEP_GENES
 
 OPT_NEIGHBOR_SEARCH = 1

@@ -166,6 +166,8 @@ void derive(DevParams& D, const mg_fparams& p, uint32_t cap) {
     D.VL2 = p.pvel_limit * p.pvel_limit;
     D.vl_factor = D.VL / sqrtf(D.VL2);
     D.dt = p.dt;
+    D.actuation_factor = p.actuation_factor;
+    D.actuation_period = p.actuation_period;
     D.null_z = p.pboundmin[2] - (float)(2 * p.grid_res[2]);
     D.freeze = p.freeze ? 1 : 0;
     D.cap = cap;
@@ -387,7 +389,8 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
         launch_remodel(h->P, h->set[h->cur], h->cold, h->s, h->stream);
     }
     if (flags & MG_STEP_PHYSICS) {
-        { Mark m(h, prof, "advance"); launch_advance(h->P, h->set[h->cur], h->s, !remodel, h->stream); }
+        { Mark m(h, prof, "advance");
+          launch_advance(h->P, h->set[h->cur], h->s, !remodel, h->stream, (flags & MG_STEP_SPECIAL) != 0); }
         h->flist_valid = false;
     }
 }
@@ -684,6 +687,8 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     launch_init_set(max_points, h->set[1], h->stream);
     uint32_t init_counters[16] = {0};
     init_counters[3] = max_points;  // every slot counts as active until the first sort
+    std::memcpy(&init_counters[7], &params->time, 4);  // device time, both parity slots
+    std::memcpy(&init_counters[8], &params->time, 4);
     cudaMemcpyAsync(h->s.counters, init_counters, sizeof(init_counters), cudaMemcpyHostToDevice, h->stream);
     launch_fill_u32(h->s.cell, UNDEF, n, h->stream);
     launch_fill_u32(h->s.newidx, UNDEF, n, h->stream);
@@ -728,9 +733,17 @@ mg_status mg_update_params(mg_handle h, const mg_fparams* p) {
     h->params = *p;
     h->time = p->time;
     const int uniform = h->P.uniform_diff;
+    const int w = h->P.dens_warps, gm = h->P.group_mode, sb = h->P.sub_bits;
     derive(h->P, *p, h->cap);
     h->P.uniform_diff = uniform;
+    h->P.dens_warps = w;
+    h->P.group_mode = gm;
+    h->P.sub_bits = sb;
     clear_graphs(h);
+    // the device copy of the time (both parity slots)
+    const uint32_t t2[2] = {*reinterpret_cast<const uint32_t*>(&p->time), *reinterpret_cast<const uint32_t*>(&p->time)};
+    MG_CUDA(h, cudaStreamSynchronize(h->stream));
+    MG_CUDA(h, cudaMemcpy(h->s.counters + 7, t2, sizeof(t2), cudaMemcpyHostToDevice));
     return MG_OK;
 }
 

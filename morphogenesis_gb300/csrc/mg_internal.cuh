@@ -60,6 +60,7 @@ struct DevParams {
     float sr, r2, r2diff, d2, pmass, rest, istiff, wc2, surf;
     float pr, bmin[3], bmax[3], estiff, damp, xmin_stiff, xmax_stiff, slope, one_minus_slope;
     float grav[3], AL, AL2, VL, VL2, vl_factor, dt;
+    float actuation_factor, actuation_period;
     float null_z;
     int freeze;
     int uniform_diff;  // all 16 diffusion rates equal and nonzero (set from the genome)
@@ -128,7 +129,8 @@ struct Scratch {
     unsigned long long* scan_status;  // [tiles]
     uint32_t* counters; // [0] scan tile ticket, [1] big-cell list length, [2] error word,
                         // [3] nactive, [5] step counter (incremented by insert),
-                        // [6] density-pass overflow queue length
+                        // [6] density-pass overflow queue length, [7], [8] simulation time
+                        // (float bits, slot = step counter parity)
     uint32_t* ovf;      // [cap] particles whose neighbours overflow a lane's list
     uint8_t* freemask;  // [cap] remodelling: free incoming slots
     uint32_t* prop;     // [cap] remodelling: proposed partner
@@ -176,8 +178,9 @@ void launch_apply_breaks(const DevParams& P, const Carried& cur, const Scratch& 
 // re-forming of broken bonds on the sorted state, breaks already applied (D5)
 void launch_remodel(const DevParams& P, const Carried& cur, const Cold& cold, const Scratch& s,
                     cudaStream_t st);
+// special: externalActuation / fixedParticles for genes 12 / 11 (SpecialParticlesCL)
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_breaks,
-                    cudaStream_t st);
+                    cudaStream_t st, bool special = false);
 
 // ---- import/export between the reference layouts and the device layout -------------------
 void launch_import_bonds(const DevParams& P, const uint32_t* ref, const Carried& cur,

@@ -1108,13 +1108,39 @@ __device__ __forceinline__ void wall(float& ax, float& ay, float& az, float diff
     }
 }
 
-template <bool APPLY_BRK>
+// sin(x) by Cody-Waite reduction to [-pi/4, pi/4] (pi/2 split in three floats, the first two
+// with 12 significant bits so k * part is exact for |k| < 2^12) and Taylor polynomials of degree
+// 9 (sine) and 8 (cosine); written as separate multiplies and adds so the oracle's C copy gives
+// the same bits.
+__device__ __forceinline__ float mg_sin_cw(float x) {
+    const float P1 = 1.5703125f, P2 = __int_as_float(0x39fda000), P3 = __int_as_float(0x33a22169);
+    if (x - x != 0.0f) return x - x;  // NaN or infinity: NaN
+    const float k = rintf(x * 0.636619772f);
+    const float r = ((x - k * P1) - k * P2) - k * P3;
+    const int q = (int)k & 3;
+    const float s = r * r;
+    const float sn = r + r * s * ((-1.0f / 6.0f) + s * ((1.0f / 120.0f) + s * ((-1.0f / 5040.0f) + s * (1.0f / 362880.0f))));
+    const float cs = 1.0f + s * (-0.5f + s * ((1.0f / 24.0f) + s * ((-1.0f / 720.0f) + s * (1.0f / 40320.0f))));
+    return q == 0 ? sn : q == 1 ? cs : q == 2 ? -sn : -cs;
+}
+
+// Device copy of the simulation time: two slots alternating with the step counter's parity
+// (counters[5], advanced by the insert pass), so the advance pass reads this step's time and
+// writes the next one without a race.
+__device__ __forceinline__ float* time_slot(uint32_t* counters, uint32_t step) {
+    return reinterpret_cast<float*>(counters + 7 + (step & 1u));
+}
+
+template <bool APPLY_BRK, bool SPECIAL>
 __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
                                                  const float4* __restrict__ force,
                                                  const uint32_t* __restrict__ brk,
-                                                 const uint32_t* __restrict__ nactive_p) {
+                                                 uint32_t* __restrict__ counters) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= *nactive_p) return;
+    const uint32_t step = counters[5];
+    const float time = *time_slot(counters, step);
+    if (p == 0) *time_slot(counters, step + 1u) = time + P.dt;  // AdvanceTime (fluid_system.cpp:2016)
+    if (p >= counters[3]) return;
     const float4 pos = C.pos[p], ve = C.veval[p], f = force[p];
     float ax = f.x, ay = f.y, az = f.z;
     float diff;
@@ -1150,9 +1176,18 @@ __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
     }
     const float dt = P.dt;
     const float vnx = ax * dt + vel.x, vny = ay * dt + vel.y, vnz = az * dt + vel.z;
-    C.veval[p] = make_float4((vel.x + vnx) * 0.5f, (vel.y + vny) * 0.5f, (vel.z + vnz) * 0.5f, ve.w);
-    C.vel[p] = make_float4(vnx, vny, vnz, vel.w);
-    C.pos[p] = make_float4(pos.x + vnx * dt, pos.y + vny * dt, pos.z + vnz * dt, pos.w);
+    const uint32_t special = SPECIAL ? (C.genes[p] >> 11) & 3u : 0u;  // bit 0: gene 11, bit 1: gene 12
+    if (special == 0) {
+        C.veval[p] = make_float4((vel.x + vnx) * 0.5f, (vel.y + vny) * 0.5f, (vel.z + vnz) * 0.5f, ve.w);
+        C.vel[p] = make_float4(vnx, vny, vnz, vel.w);
+        C.pos[p] = make_float4(pos.x + vnx * dt, pos.y + vny * dt, pos.z + vnz * dt, pos.w);
+    } else if (special == 2u) {
+        // externalActuation (cuda:3617-3691): the previous state, z displaced by
+        // actuation_factor * sin(time / (actuation_period * dt))
+        const float ph = time / (P.actuation_period * dt);
+        C.pos[p] = make_float4(pos.x, pos.y, pos.z + P.actuation_factor * mg_sin_cw(ph), pos.w);
+    }
+    // fixedParticles (cuda:3694-3705, after the actuation): the previous state is kept
     if (APPLY_BRK) {
         const uint32_t br = brk[p];
         if (br) apply_breaks(C.bond, P.cap, p, br);
@@ -1160,12 +1195,16 @@ __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
 }
 
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_brk,
-                    cudaStream_t st) {
+                    cudaStream_t st, bool special) {
     uint32_t blocks = (P.cap + 255) / 256;
-    if (apply_brk)
-        k_advance<true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters + 3);
+    if (apply_brk && special)
+        k_advance<true, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+    else if (apply_brk)
+        k_advance<true, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+    else if (special)
+        k_advance<false, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
     else
-        k_advance<false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters + 3);
+        k_advance<false, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
 }
 
 }  // namespace mg

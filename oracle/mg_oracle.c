@@ -949,6 +949,44 @@ void mgo_remodel(mgo_handle h) {
     free(propd);
 }
 
+/* ---- SpecialParticlesCL (host_CUDA.cpp:869-900): externalActuation (cuda:3617-3691) for gene
+ * 12, then fixedParticles (cuda:3694-3705) for gene 11, applied to the integrated state ------
+ * The sine is a Cody-Waite reduction (pi/2 in three float parts, the first two with 12
+ * significant bits) with Taylor polynomials of degree 9 / 8, in separate float operations, the
+ * same expression the GPU kernel evaluates. */
+static float sin_cw(float x) {
+    const float P1 = 1.5703125f;
+    union { uint32_t u; float f; } p2 = {0x39fda000u}, p3 = {0x33a22169u};
+    if (x - x != 0.0f) return x - x; /* NaN or infinity: NaN */
+    const float k = rintf(x * 0.636619772f);
+    const float r = ((x - k * P1) - k * p2.f) - k * p3.f;
+    const int q = (int)k & 3;
+    const float s = r * r;
+    const float sn = r + r * s * ((-1.0f / 6.0f) + s * ((1.0f / 120.0f) + s * ((-1.0f / 5040.0f) + s * (1.0f / 362880.0f))));
+    const float cs = 1.0f + s * (-0.5f + s * ((1.0f / 24.0f) + s * ((-1.0f / 720.0f) + s * (1.0f / 40320.0f))));
+    return q == 0 ? sn : q == 1 ? cs : q == 2 ? -sn : -cs;
+}
+
+static void special_particles(mgo_handle h, const r4* pos0, const r4* vel0, const r4* veval0,
+                              real time) {
+    const params_t* P = &h->P;
+    for (uint32_t i = 0; i < h->nactive; i++) {
+        const int act = h->epigen[(size_t)12 * h->cap + i] != 0, fixed = h->epigen[(size_t)11 * h->cap + i] != 0;
+        if (act) {
+            const float ph = (float)time / ((float)P->a_p * (float)P->dt);
+            h->pos[i] = pos0[i];
+            h->pos[i].z = pos0[i].z + P->a_f * (real)sin_cw(ph);
+            h->vel[i] = vel0[i];
+            h->veval[i] = veval0[i];
+        }
+        if (fixed) {
+            h->pos[i] = pos0[i];
+            h->vel[i] = vel0[i];
+            h->veval[i] = veval0[i];
+        }
+    }
+}
+
 /* ---- D6: one step in the legacy Run() order --------------------------------------------- */
 void mgo_step(mgo_handle h, uint32_t nsteps, uint32_t flags) {
     int saved_freeze = h->P.freeze;
@@ -966,7 +1004,23 @@ void mgo_step(mgo_handle h, uint32_t nsteps, uint32_t flags) {
             mgo_compute_genes(h);
         }
         if (flags & MG_STEP_REMODEL) mgo_remodel(h); /* Run2Remodelling, before AdvanceCL */
-        if (flags & MG_STEP_PHYSICS) mgo_advance(h);
+        if (flags & MG_STEP_PHYSICS) {
+            r4 *p0 = NULL, *v0 = NULL, *e0 = NULL;
+            const real t = h->P.time;
+            if (flags & MG_STEP_SPECIAL) {
+                p0 = (r4*)malloc(sizeof(r4) * (h->nactive + 1));
+                v0 = (r4*)malloc(sizeof(r4) * (h->nactive + 1));
+                e0 = (r4*)malloc(sizeof(r4) * (h->nactive + 1));
+                memcpy(p0, h->pos, sizeof(r4) * h->nactive);
+                memcpy(v0, h->vel, sizeof(r4) * h->nactive);
+                memcpy(e0, h->veval, sizeof(r4) * h->nactive);
+            }
+            mgo_advance(h);
+            if (flags & MG_STEP_SPECIAL) {
+                special_particles(h, p0, v0, e0, t);
+                free(p0); free(v0); free(e0);
+            }
+        }
     }
     h->P.freeze = saved_freeze;
 }

@@ -357,3 +357,25 @@ def test_step_io_equals_separate_calls(built, cfg0):
     a.step_io(host, 2, A.STEP_DEFAULT, out_a)
     for k in bufs:
         assert np.array_equal(out_a[k].view(np.uint32), b.download(k).view(np.uint32)), f"buffer {k}"
+
+
+def test_special_particles_match_oracle(built):
+    d = demo.make_block(10, "R", seed=9)
+    d.params.actuation_factor = 0.05
+    d.params.actuation_period = 10.0
+    g, o = pair(d, d.n)
+    flags = A.STEP_DEFAULT | A.STEP_SPECIAL
+    g.Run(20, flags)
+    o.step(20, flags)
+    assert compare(g, o), "special-particle steps are not bitwise equal to the oracle"
+    # gene 11 particles keep their initial position; gene 12 (not 11) particles move in z only
+    ids = g.download(A.FPARTICLE_ID).astype(np.int64) - 1
+    pos = g.download(A.FPOS)
+    ep = d.arrays[A.FEPIGEN]
+    p0 = d.arrays[A.FPOS]
+    fixed = ep[11, ids] != 0
+    act = (ep[12, ids] != 0) & ~fixed
+    assert fixed.any() and act.any()
+    assert np.array_equal(pos[fixed, :3], p0[ids[fixed], :3])
+    assert np.array_equal(pos[act, :2], p0[ids[act], :2])
+    assert not np.array_equal(pos[act, 2], p0[ids[act], 2])
