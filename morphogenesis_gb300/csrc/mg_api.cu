@@ -58,6 +58,7 @@ struct mg_system {
     void* staging = nullptr;
     size_t staging_bytes = 0;
     uint32_t* dense = nullptr;  // gcount | goffset | lists | lens (allocated on demand)
+    uint32_t* epi_mem = nullptr;  // full epigenetic state of both sets (allocated on demand)
     int phase = PHASE_UNSORTED;
     bool ever_sorted = false;
     bool brk_pending = false;
@@ -194,6 +195,26 @@ mg_status check_params(mg_system* h, const mg_fparams* p) {
 
 void clear_graphs(mg_system* h);
 
+// Switches to the full epigenetic state: per-gene FEPIGEN words carried with the particles
+// (countdowns and activation lists), initialised from the current gene bits.
+mg_status enable_full_epi(mg_system* h) {
+    if (h->P.full_epi) return MG_OK;
+    const size_t words = (size_t)NG * h->cap;
+    cudaError_t e = cudaMalloc(&h->epi_mem, 2 * words * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        h->epi_mem = nullptr;
+        return fail(h, MG_ERR_OOM, "full epigenetic state");
+    }
+    h->set[0].epi = h->epi_mem;
+    h->set[1].epi = h->epi_mem + words;
+    MG_CUDA(h, cudaMemsetAsync(h->epi_mem, 0, 2 * words * sizeof(uint32_t), h->stream));
+    launch_bits_to_words(h->cap, h->set[h->cur], h->stream);
+    h->P.full_epi = 1;
+    clear_graphs(h);
+    return MG_OK;
+}
+
 mg_status upload_genome(mg_system* h) {
     DevGenome g;
     std::memset(&g, 0, sizeof(g));
@@ -216,13 +237,25 @@ mg_status upload_genome(mg_system* h) {
             k++;
         }
         g.nsec[a] = k;
-        int na = (int)G.activate[a][2 * NG];
-        if (na != 0)
-            return fail(h, MG_ERR_UNSUPPORTED,
-                        "genome activation lists need per-gene epigenetic counters; the GPU gene "
-                        "kernel holds gene state as a bitmask (FEPIGEN in {0, INT_MAX})");
-        g.nact[a] = 0;
+        // activation list (computeGeneAction cuda:752-757): entries naming a gene out of range
+        // are skipped, at most 16 are read
+        const int na = (int)G.activate[a][2 * NG];
+        int m = 0;
+        for (int j = 0; j < na && j < NG; j++) {
+            const int og = (int)G.activate[a][2 * j];
+            if (og < 0 || og >= NG) continue;
+            g.act_gene[a][m] = og;
+            g.act_thr[a][m] = G.activate[a][2 * j + 1];
+            m++;
+        }
+        g.nact[a] = m;
         g.delay[a] = G.delay[a];
+    }
+    bool activations = false;
+    for (int a = 0; a < NG; a++) activations |= g.nact[a] > 0;
+    if (activations) {  // activations change FEPIGEN words: keep the full state
+        mg_status st = enable_full_epi(h);
+        if (st != MG_OK) return st;
     }
     int uniform = g.diff[0] != 0.f;
     for (int t = 1; t < NTF; t++) uniform &= g.diff[t] == g.diff[0];
@@ -457,6 +490,10 @@ void after_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
 mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
     if ((flags & MG_STEP_SURROGATE) && !h->sur)
         return fail(h, MG_ERR_INVALID_ARG, "surrogate step without an attached network (mg_set_surrogate)");
+    if ((flags & MG_STEP_SURROGATE) && h->P.full_epi)
+        return fail(h, MG_ERR_UNSUPPORTED,
+                    "the surrogate step needs gene states 0 / INT_MAX without activation lists "
+                    "(the network replaces the reaction and would skip the epigenetic countdowns)");
     for (uint32_t s = 0; s < nsteps; s++) {
         if (h->profile) {
             DevParams saved = h->P;
@@ -711,6 +748,7 @@ mg_status mg_destroy(mg_handle h) {
     for (auto& m : h->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
     if (h->staging) cudaFree(h->staging);
     if (h->dense) cudaFree(h->dense);
+    if (h->epi_mem) cudaFree(h->epi_mem);
     if (h->feat) cudaFree(h->feat);
     if (h->feat_scale) cudaFree(h->feat_scale);
     if (h->conc_plain) cudaFree(h->conc_plain);
@@ -831,6 +869,22 @@ static mg_status enqueue_upload(mg_handle h, int32_t id, const void* host, size_
     case MG_FGCELL: case MG_FGNDX: return MG_OK;  // recomputed by insert
     default: break;
     }
+    if (id == MG_FEPIGEN) {
+        // values other than 0 and INT_MAX are epigenetic countdowns: keep the full state
+        const uint32_t* w = (const uint32_t*)host;
+        bool countdown = false;
+        for (size_t k = 0; k < (size_t)NG * h->cap && !countdown; k++)
+            countdown = w[k] != 0u && w[k] != MG_EPIGEN_ACTIVE;
+        if (countdown) {
+            mg_status s2 = enable_full_epi(h);
+            if (s2 != MG_OK) return s2;
+        }
+        if (h->P.full_epi) {
+            MG_CUDA(h, cudaMemcpyAsync(c.epi, host, bytes, cudaMemcpyHostToDevice, st));
+            launch_words_to_bits(h->cap, c, st);
+            return MG_OK;
+        }
+    }
     if (dst) {
         MG_CUDA(h, cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, st));
         return MG_OK;
@@ -880,6 +934,7 @@ static mg_status enqueue_download(mg_handle h, int32_t id, void* host, size_t by
     case MG_FBIN_OFFSET: src = h->s.offset; break;
     default: break;
     }
+    if (id == MG_FEPIGEN && h->P.full_epi) src = c.epi;
     if (src) {
         MG_CUDA(h, cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, st));
         return MG_OK;

@@ -68,6 +68,7 @@ struct DevParams {
     // picks them by timing): warps per block, search groups (0: a cell and the next cell of
     // its row, 1: one cell), sub-cell bits per axis of the processing order (1 or 2)
     int dens_warps, group_mode, sub_bits;
+    int full_epi;  // per-gene FEPIGEN words carried (countdowns, activation lists) instead of bits
     uint32_t cap;
     uint32_t cells;
 };
@@ -95,6 +96,7 @@ struct Carried {
     float* conc;
     uint32_t* genes;
     uint32_t* origin;
+    uint32_t* epi;  // [16][cap] FEPIGEN words when the full epigenetic state is kept, else null
 };
 
 struct Cold {
@@ -165,6 +167,7 @@ struct DensExtra {
     float* cap_x;              // CAPTURE: dataset features [..][48] for particle 0 of this pass
     float* cap_y;              // CAPTURE: dataset targets (reaction increment / s) [..][16]
     float* conc_plain;         // JUDGE: plain update of judged / handed-over particles
+    uint32_t* epi;             // full epigenetic state of the current set ([16][cap]) or null
     const uint32_t* step;      // JUDGE: device step counter
     uint32_t judge_period, judge_stride;
 };
@@ -202,6 +205,9 @@ void launch_export_grid_index(const DevParams& P, const Scratch& s, int which, i
 void launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st);
 void launch_identity(uint32_t* p, uint32_t n, cudaStream_t st);
 void launch_init_set(uint32_t cap, const Carried& c, cudaStream_t st);
+// full epigenetic state: words from the gene bits (INT_MAX / 0), bits from the words
+void launch_bits_to_words(uint32_t cap, const Carried& c, cudaStream_t st);
+void launch_words_to_bits(uint32_t cap, const Carried& c, cudaStream_t st);
 // dense per-gene lists from the sorted gene bits
 void launch_gene_cell_counts(const DevParams& P, const Carried& cur, const Scratch& s,
                              uint32_t* gcount, cudaStream_t st);

@@ -81,6 +81,31 @@ __global__ void k_export_epigen(uint32_t cap, const uint32_t* __restrict__ genes
     ref[k] = ((genes[p] >> g) & 1u) ? EPIGEN_ACTIVE : 0u;
 }
 
+__global__ void k_bits_to_words(uint32_t cap, const uint32_t* __restrict__ genes, uint32_t* __restrict__ epi) {
+    size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (size_t)cap * NG) return;
+    uint32_t g = (uint32_t)(k / cap), p = (uint32_t)(k % cap);
+    epi[k] = ((genes[p] >> g) & 1u) ? EPIGEN_ACTIVE : 0u;
+}
+
+// Gene bits (dense-list membership, FEPIGEN > 0) from the words; bit 31 is kept.
+__global__ void k_words_to_bits(uint32_t cap, const uint32_t* __restrict__ epi, uint32_t* __restrict__ genes) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= cap) return;
+    uint32_t bits = genes[p] & 0x80000000u;
+    for (int g = 0; g < NG; g++)
+        if (epi[(size_t)g * cap + p] != 0u) bits |= 1u << g;
+    genes[p] = bits;
+}
+
+void launch_bits_to_words(uint32_t cap, const Carried& c, cudaStream_t st) {
+    k_bits_to_words<<<blocks_for((size_t)cap * NG), 256, 0, st>>>(cap, c.genes, c.epi);
+}
+
+void launch_words_to_bits(uint32_t cap, const Carried& c, cudaStream_t st) {
+    k_words_to_bits<<<blocks_for(cap), 256, 0, st>>>(cap, c.epi, c.genes);
+}
+
 void launch_import_epigen(const DevParams& P, const uint32_t* ref, const Carried& cur,
                           uint32_t* err, cudaStream_t st) {
     k_import_epigen<<<blocks_for(P.cap), 256, 0, st>>>(P.cap, ref, cur.genes, err);

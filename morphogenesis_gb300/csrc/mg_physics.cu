@@ -153,6 +153,44 @@ __device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint
     return sum;
 }
 
+// The gene action with the full epigenetic state (computeGeneAction + tallyGeneAction,
+// fluid_system_cuda.cu:714-772, with D3): for each gene in the particle's sort-time dense lists,
+// in gene order, a counting-down word (0 < w < INT_MAX) is decremented and, when it reaches 0,
+// starts the next active gene's countdown at its genome delay; the activity (sensitivity .
+// concentrations) adds secretion and, above each activation threshold, one activation of the
+// other gene.  Living particles (gene 2) add the secretion and the activations.  Kept out of
+// line so it does not weigh on the registers of the common path.
+__device__ __noinline__ void gene_action_full(const DevParams& P, const DevGenome* __restrict__ G,
+                                              uint32_t p, uint32_t bits, const float (&c)[NTF],
+                                              float (&cf)[NTF], uint32_t* __restrict__ epi) {
+    const size_t cap = P.cap;
+    uint32_t E[NG], dE[NG];
+    float dc[NTF];
+    for (int g = 0; g < NG; g++) { E[g] = epi[(size_t)g * cap + p]; dE[g] = 0u; }
+    for (int t = 0; t < NTF; t++) dc[t] = 0.f;
+    for (int g = 0; g < NG; g++) {
+        if (!((bits >> g) & 1u)) continue;
+        const int delay = (int)E[g];
+        if (0 < delay && delay < 0x7FFFFFFF) {
+            E[g]--;
+            if (delay == 1 && g + 1 < NG && E[g + 1] != 0u) E[g + 1] = G->delay[g + 1];
+        }
+        float act = 0.f;
+        for (int t = 0; t < NTF; t++) {
+            const float sv = G->sens[g][t];
+            if (sv != 0.f) act += sv * c[t];
+        }
+        const int ns = G->nsec[g];
+        for (int k = 0; k < ns; k++) dc[G->sec_tf[g][k]] += G->sec_rate[g][k] * act;
+        const int na = G->nact[g];
+        for (int k = 0; k < na; k++)
+            if (G->act_thr[g][k] < act) dE[G->act_gene[g][k]] += 1u;
+    }
+    const bool living = (bits & 4u) != 0u;
+    for (int t = 0; t < NTF; t++) cf[t] = living ? c[t] + dc[t] : c[t];
+    for (int g = 0; g < NG; g++) epi[(size_t)g * cap + p] = living ? E[g] + dE[g] : E[g];
+}
+
 // Density -> pressure and 1/density; diffusion + gene reaction (the plain update); surrogate
 // features and captured training pairs.
 template <int FLAGS>
@@ -215,7 +253,22 @@ __device__ __forceinline__ void dens_epilogue(const DevParams& P, const DevGenom
 #pragma unroll
         for (int k = 0; k < 4; k++) o4[k] = make_float4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
     }
-    if (F::GENE && plain) {
+    if (F::GENE && plain && P.full_epi && X.epi) {
+        float cf[NTF];
+        gene_action_full(P, G, p, gene_word & 0xFFFFu, c, cf, X.epi);
+        float* dst = F::JUDGE ? X.conc_plain : conc_out;
+        float4* o4 = reinterpret_cast<float4*>(dst + (size_t)p * NTF);
+#pragma unroll
+        for (int k = 0; k < 4; k++) o4[k] = make_float4(cf[4 * k], cf[4 * k + 1], cf[4 * k + 2], cf[4 * k + 3]);
+        if (F::CAPTURE) {
+            float4* y4 = reinterpret_cast<float4*>(X.cap_y + (size_t)p * NTF);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                y4[k] = make_float4((cf[4 * k] - c[4 * k]) * inv_s, (cf[4 * k + 1] - c[4 * k + 1]) * inv_s,
+                                    (cf[4 * k + 2] - c[4 * k + 2]) * inv_s,
+                                    (cf[4 * k + 3] - c[4 * k + 3]) * inv_s);
+        }
+    } else if (F::GENE && plain) {
         // Gene bits are the sort-time dense-list membership (FEPIGEN > 0).  With every
         // FEPIGEN in {0, INT_MAX} and no activation lists the countdown never fires and
         // the reaction is: for each active gene g in order, activity = sum_tf sens*conc,
@@ -841,7 +894,8 @@ cudaError_t physics_init() {
 void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
                  cudaStream_t st, const DensExtra* extra) {
-    const DensExtra X = extra ? *extra : DensExtra{};
+    DensExtra X = extra ? *extra : DensExtra{};
+    X.epi = P.full_epi ? cur.epi : nullptr;
     const int warps = (P.dens_warps >= 1 && P.dens_warps <= DENS_WARPS) ? P.dens_warps : DENS_WARPS;
     const size_t smem = (size_t)warps * NL_CAP * 32 * sizeof(uint32_t);
     if (search == 1 && (flags & (1 | 2 | 8 | 16))) {

@@ -372,7 +372,20 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
         float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
 #pragma unroll
         for (int k = 0; k < 4; k++) co[k] = __ldg(ci + k);
-        D.genes[p] = __ldg(S.genes + i);
+        if (P.full_epi) {
+            // per-gene words move with the particle; the bits (dense-list membership at sort
+            // time, FEPIGEN > 0) are taken from them
+            uint32_t bits = __ldg(S.genes + i) & 0x80000000u;
+#pragma unroll
+            for (int g = 0; g < NG; g++) {
+                const uint32_t wv = __ldg(S.epi + (size_t)g * cap + i);
+                D.epi[(size_t)g * cap + p] = wv;
+                if (wv != 0u) bits |= 1u << g;
+            }
+            D.genes[p] = bits;
+        } else {
+            D.genes[p] = __ldg(S.genes + i);
+        }
         D.origin[p] = __ldg(S.origin + i);
         scell[p] = __ldg(cell + i);
     } else {
@@ -393,6 +406,8 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
 #pragma unroll
         for (int k = 0; k < 4; k++) co[k] = make_float4(0.f, 0.f, 0.f, 0.f);
         D.genes[p] = 0u;
+        if (P.full_epi)
+            for (int g = 0; g < NG; g++) D.epi[(size_t)g * cap + p] = 0u;
         D.origin[p] = UNDEF;
         scell[p] = UNDEF;
         press[p] = 0.f;

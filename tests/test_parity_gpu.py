@@ -210,19 +210,47 @@ def test_rejects_what_it_cannot_hold(built, cfg0):
     import morphogenesis_gb300 as mg
 
     g = mg.FluidSystem(cfg0.params, cfg0.genome, cfg0.n)
-    ep = cfg0.arrays[A.FEPIGEN].copy()
-    ep[3, 10] = 5  # an epigenetic countdown value
-    with pytest.raises(mg.MgError) as e:
-        g.upload(A.FEPIGEN, ep)
-    assert e.value.status == 7
     with pytest.raises(mg.MgError):
         g.ComputePressureCL()  # no sort yet
     with pytest.raises(ValueError):
         g.upload(A.FPOS, cfg0.arrays[A.FPOS][:10])
-    gen = demo.make_genome()
-    gen.activate[0][32] = 1.0
+
+
+def epigenetic_scene(seed):
+    """A block whose FEPIGEN words hold countdowns and whose genome has delays and activation
+    lists (the full epigenetic state of computeGeneAction)."""
+    d = demo.make_block(8, "R", seed=seed)
+    r = np.random.default_rng(seed)
+    ep = d.arrays[A.FEPIGEN].copy()
+    pick = r.random(ep.shape)
+    ep[pick < 0.15] = r.integers(1, 6, ep.shape)[pick < 0.15].astype(np.uint32)
+    ep[2, :] = np.where(r.random(ep.shape[1]) < 0.8, np.uint32(A.EPIGEN_ACTIVE), ep[2, :])  # mostly living
+    d.arrays[A.FEPIGEN] = ep
+    g = d.genome
+    for a in range(A.NUM_GENES):
+        g.delay[a] = int(r.integers(1, 5))
+        na = int(r.integers(0, 3))
+        for k in range(na):
+            g.activate[a][2 * k] = float(r.integers(0, A.NUM_GENES))
+            g.activate[a][2 * k + 1] = float(r.uniform(-0.2, 0.2))
+        g.activate[a][2 * A.NUM_GENES] = float(na)
+    return d
+
+
+def test_full_epigenetic_state_matches_oracle(built):
+    d = epigenetic_scene(5)
+    gsys, o = pair(d, d.n)
+    gsys.Run(12)
+    o.step(12)
+    assert compare(gsys, o), "full epigenetic steps are not bitwise equal to the oracle"
+    ep = gsys.download(A.FEPIGEN)
+    assert ((ep != 0) & (ep != A.EPIGEN_ACTIVE)).any(), "countdowns should remain in the state"
+    # the surrogate step needs binary gene states
+    import morphogenesis_gb300 as mg
+    from morphogenesis_gb300 import surrogate as S
+    S.attach(gsys, S.Mlp(seed=1), 0, 0, 1e-3)
     with pytest.raises(mg.MgError):
-        g.UpdateGenome(gen)
+        gsys.Run(1, A.STEP_DEFAULT | A.STEP_SURROGATE)
 
 
 def test_deterministic_rerun(built):
