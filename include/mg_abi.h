@@ -347,7 +347,11 @@ mg_status mg_fparams_from_simparams(const mg_simparams* sp, int32_t gsrch_overri
 mg_status mg_read_genome(const char* path, mg_genome* out);
 mg_status mg_write_genome(const char* dir, const mg_genome* g, int32_t integer_fields); /* dir/genome.csv */
 /* Particle CSV of SavePointsCSV2 / ReadPointsCSV2 (fileCL_IO.cpp:250-469) over host arrays in
- * the mg_upload layouts (n particles; epigen is [16][n]). */
+ * the mg_upload layouts (n particles; epigen is [16][n]).  Each CSV line holds one particle's
+ * 16 concentrations.  conc is [n][16], the layout the kernels read (FCONC[p*16+tf], cuda:739,
+ * 3097); conc_species_major = 1 takes conc as [16][n] instead, the reference host's getConc
+ * layout (FCONC[tf*maxPoints+p], fluid_system.h:574) that SavePointsCSV2 indexes
+ * (fileCL_IO.cpp:323-326), for hosts that keep their buffers that way. */
 typedef struct mg_points {
     uint32_t n;
     float* pos;            /* [n][4] */
@@ -359,8 +363,9 @@ typedef struct mg_points {
     uint32_t* mass_radius; /* [n] mass | radius << 16 */
     uint32_t* nerve;       /* [n] */
     uint32_t* pidx;        /* [n][12] */
-    float* conc;           /* [n][16] */
+    float* conc;           /* [n][16], or [16][n] with conc_species_major */
     uint32_t* epigen;      /* [16][n] */
+    uint32_t conc_species_major;
 } mg_points;
 mg_status mg_count_points_csv(const char* path, uint32_t* n); /* lines - 1 */
 mg_status mg_read_points_csv(const char* path, mg_points* pts);

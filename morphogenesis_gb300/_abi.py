@@ -98,7 +98,7 @@ class Points(C.Structure):
     _fields_ = [("n", C.c_uint32), ("pos", C.c_void_p), ("vel", C.c_void_p), ("age", C.c_void_p),
                 ("color", C.c_void_p), ("elastidx", C.c_void_p), ("particle_id", C.c_void_p),
                 ("mass_radius", C.c_void_p), ("nerve", C.c_void_p), ("pidx", C.c_void_p),
-                ("conc", C.c_void_p), ("epigen", C.c_void_p)]
+                ("conc", C.c_void_p), ("epigen", C.c_void_p), ("conc_species_major", C.c_uint32)]
 
 
 class IO(C.Structure):

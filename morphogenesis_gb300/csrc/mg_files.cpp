@@ -303,6 +303,11 @@ mg_status mg_count_points_csv(const char* path, uint32_t* n) {
     return MG_OK;
 }
 
+// index of (particle i, species j) in the points' conc array
+static size_t conc_at(const mg_points* p, uint32_t i, int j) {
+    return p->conc_species_major ? (size_t)j * p->n + i : (size_t)i * MG_NUM_TF + j;
+}
+
 static bool points_ok(const mg_points* p) {
     return p && p->pos && p->vel && p->age && p->color && p->elastidx && p->particle_id &&
            p->mass_radius && p->nerve && p->pidx && p->conc && p->epigen;
@@ -347,7 +352,7 @@ mg_status mg_write_points_csv(const char* dir, int32_t frame, const mg_points* p
         const uint32_t* pi = p->pidx + (size_t)i * 2 * MG_BONDS_PER_PARTICLE;
         for (int j = 0; j < 2 * MG_BONDS_PER_PARTICLE; j += 2) std::fprintf(fp, "%u, %u,, ", pi[j], pi[j + 1]);
         std::fprintf(fp, "\t\t");
-        for (int j = 0; j < MG_NUM_TF; j++) std::fprintf(fp, "%f, ", p->conc[(size_t)i * MG_NUM_TF + j]);
+        for (int j = 0; j < MG_NUM_TF; j++) std::fprintf(fp, "%f, ", p->conc[conc_at(p, i, j)]);
         std::fprintf(fp, "\t\t");
         for (int j = 0; j < MG_NUM_GENES; j++) std::fprintf(fp, "%u, ", p->epigen[(size_t)j * n + i]);
         std::fprintf(fp, " \n");
@@ -403,7 +408,7 @@ mg_status mg_read_points_csv(const char* path, mg_points* p) {
         ret += std::fscanf(f, " \t%u, %u, %u, %u, \t\t", &id, &mass, &radius, &nerve);
         uint32_t* pi = p->pidx + (size_t)i * 2 * MG_BONDS_PER_PARTICLE;
         for (int j = 0; j < 2 * MG_BONDS_PER_PARTICLE; j += 2) ret += std::fscanf(f, "%u, %u,, ", &pi[j], &pi[j + 1]);
-        for (int j = 0; j < MG_NUM_TF; j++) ret += std::fscanf(f, "%f, ", &p->conc[(size_t)i * MG_NUM_TF + j]);
+        for (int j = 0; j < MG_NUM_TF; j++) ret += std::fscanf(f, "%f, ", &p->conc[conc_at(p, i, j)]);
         skip(std::fscanf(f, "\t"));
         for (int j = 0; j < MG_NUM_GENES; j++) ret += std::fscanf(f, "%u, ", &p->epigen[(size_t)j * n + i]);
         skip(std::fscanf(f, " \n"));

@@ -100,6 +100,31 @@ def test_points_csv_round_trip(built, tmp_path):
         np.testing.assert_allclose(eb[:, :, w].view(np.float32), el[:, :, w].view(np.float32), atol=6e-7)
 
 
+def test_points_csv_species_major_concentrations(built, tmp_path):
+    """conc_species_major reads and writes FCONC as [16][n] (the reference host's getConc layout):
+    the file is the same as from the [n][16] layout."""
+    import ctypes as C
+    d = demo.make_block(4, "R", seed=2)
+    arrays = {b: np.ascontiguousarray(v) for b, v in d.arrays.items()}
+    for b in (A.FAGE, A.FCOLOR, A.FMASS_RADIUS, A.FNERVEIDX):
+        arrays[b] = np.arange(d.n, dtype=np.uint32)
+    lib = A.load()
+    (tmp_path / "pm").mkdir()
+    (tmp_path / "sm").mkdir()
+    pts = F._points(arrays, d.n)
+    assert lib.mg_write_points_csv(str(tmp_path / "pm").encode(), 0, C.byref(pts)) == 0
+    species_major = np.ascontiguousarray(arrays[A.FCONC].T)
+    pts.conc = species_major.ctypes.data
+    pts.conc_species_major = 1
+    assert lib.mg_write_points_csv(str(tmp_path / "sm").encode(), 0, C.byref(pts)) == 0
+    name = "particles_pos_vel_color100000.csv"
+    assert (tmp_path / "pm" / name).read_text() == (tmp_path / "sm" / name).read_text()
+    back = np.zeros_like(species_major)
+    pts.conc = back.ctypes.data
+    assert lib.mg_read_points_csv(str(tmp_path / "pm" / name).encode(), C.byref(pts)) == 0
+    np.testing.assert_allclose(back, species_major, atol=6e-7)
+
+
 def test_file_errors_are_returned(built, tmp_path):
     (tmp_path / "bad.txt").write_text("not a simparams file\n")
     with pytest.raises(A.MgError):
