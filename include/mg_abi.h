@@ -99,6 +99,9 @@ enum mg_step_flags {
     MG_STEP_SPECIAL = 1u << 5,   /* SpecialParticlesCL after the integration: gene 12 particles are
                                     actuated (externalActuation), gene 11 particles stay fixed
                                     (fixedParticles), fluid_system_cuda.cu:3617-3705 */
+    MG_STEP_BOND_CHANGES = 1u << 6, /* computeBondChanges (steps_per_InnerPhysicalLoop 1) before
+                                       the heal, which then heals the slots it flagged; implies
+                                       MG_STEP_REMODEL (legacy Run(), fluid_system.cpp:1256) */
     MG_STEP_DEFAULT = MG_STEP_PHYSICS | MG_STEP_GENES
 };
 
@@ -236,6 +239,19 @@ mg_status mg_run_gene_action(mg_handle h);          /* Run2GeneAction */
  * proposals are accepted in (distance, index) order; the new bond has rest length = distance,
  * elastic limit 1.5 x rest length, the broken slot's modulus and damping. */
 mg_status mg_run_remodelling(mg_handle h);
+/* ComputeBondChangesCL(steps_per_InnerPhysicalLoop) (host_CUDA.cpp:744-761, kernel
+ * computeBondChanges fluid_system_cuda.cu:1065-1331) over the living particles (gene 2): bonds
+ * with rest length > 0 average their strain integrators over the steps, zero them, and scale
+ * rest length and modulus by the genome's shifted tanh (tanh_param of the bond type the tissue
+ * genes give); the first bond with rest length 0 or no partner gets change word 1 (heal) and
+ * ends the particle's loop.  Until the next sort, mg_run_remodelling heals those slots, and the
+ * change-list buffers (FBIN_COUNT_CHANGES, FBIN_OFFSET_CHANGES [9][cells],
+ * FDENSE_LIST_LENGTHS_CHANGES [9], FDENSE_LISTS_CHANGES [9][2][N]: particle row then bond
+ * row) download what PrefixSumChangesCL / CountingSortChangesCL (cuda:406-618) build. */
+mg_status mg_compute_bond_changes(mg_handle h, uint32_t steps_per_inner_loop);
+/* Run2Remodelling(steps_per_InnerPhysicalLoop) (fluid_system.cpp:2037-2071): computeBondChanges,
+ * then heal of the slots it flagged. */
+mg_status mg_run_remodelling_steps(mg_handle h, uint32_t steps_per_inner_loop);
 /* nsteps full steps in the legacy Run() order (fluid_system.cpp:1179-1349), one sort per
  * step: insert, scan, sort, pressure, force, diffusion, genes, [remodel], advance, time. */
 mg_status mg_step(mg_handle h, uint32_t nsteps, uint32_t flags);
@@ -289,7 +305,12 @@ enum mg_option {
     /* neighbour search of the density/diffusion pass: 0 = one thread walks its 27 cells
      * (the reference loop), 1 = warp-cooperative search (default), 2 = per-lane walk of the
      * 2x2x2 sub-cells within the radius (needs gsrch 3).  Results are identical. */
-    MG_OPT_NEIGHBOR_SEARCH = 1
+    MG_OPT_NEIGHBOR_SEARCH = 1,
+    /* parameters of a healed bond: 0 = rest length = current distance, elastic limit 1.5 x rest
+     * length, modulus and damping kept from the slot (default); 1 = makeBond's elastin defaults
+     * from the genome (param[0]: elastLim, default rest length, modulus, damping,
+     * fluid_system_cuda.cu:1573-1593) */
+    MG_OPT_HEAL_PARAMS = 2
 };
 mg_status mg_set_option(mg_handle h, int32_t option, int32_t value);
 

@@ -80,6 +80,12 @@ def _shape(buf: int, n: int, cells: int):
         return u32, (A.NUM_GENES,)
     if buf == A.FDENSE_LISTS:
         return u32, (A.NUM_GENES, n)
+    if buf in (A.FBIN_COUNT_CHANGES, A.FBIN_OFFSET_CHANGES):
+        return u32, (A.NUM_CHANGES, cells)
+    if buf == A.FDENSE_LIST_LENGTHS_CHANGES:
+        return u32, (A.NUM_CHANGES,)
+    if buf == A.FDENSE_LISTS_CHANGES:
+        return u32, (A.NUM_CHANGES, 2, n)
     raise ValueError(f"buffer id {buf} is not exchanged")
 
 
@@ -201,12 +207,21 @@ class FluidSystem:
     def ComputeDiffusionCL(self) -> None: self._check(self.lib.mg_compute_diffusion(self.h))
     def ComputeGenesCL(self) -> None: self._check(self.lib.mg_compute_genes(self.h))
     def AdvanceCL(self) -> None: self._check(self.lib.mg_advance(self.h))
+    def ComputeBondChangesCL(self, steps_per_InnerPhysicalLoop: int = 1) -> None:
+        self._check(self.lib.mg_compute_bond_changes(self.h, int(steps_per_InnerPhysicalLoop)))
+    def ComputeParticleChangesCL(self) -> None: self._check(self.lib.mg_run_remodelling(self.h))
 
     # -- run loop (fluid_system.cpp Run2*) --------------------------------------------------------
     def Run2PhysicalSort(self) -> None: self._check(self.lib.mg_run_physical_sort(self.h))
     def Run2InnerPhysicalLoop(self) -> None: self._check(self.lib.mg_run_inner_physical_loop(self.h))
     def Run2GeneAction(self) -> None: self._check(self.lib.mg_run_gene_action(self.h))
-    def Run2Remodelling(self) -> None: self._check(self.lib.mg_run_remodelling(self.h))
+    def Run2Remodelling(self, steps_per_InnerPhysicalLoop: int | None = None) -> None:
+        """With a step count: computeBondChanges over that many inner-loop steps, then heal of
+        the slots it flagged (the reference's Run2Remodelling).  Without: heal only (D5 rule)."""
+        if steps_per_InnerPhysicalLoop is None:
+            self._check(self.lib.mg_run_remodelling(self.h))
+        else:
+            self._check(self.lib.mg_run_remodelling_steps(self.h, int(steps_per_InnerPhysicalLoop)))
 
     def Run(self, nsteps: int = 1, flags: int = A.STEP_DEFAULT) -> None:
         """nsteps steps in the legacy Run() order (one sort per step), graph-captured."""

@@ -22,6 +22,8 @@ FPOS, FVEL, FVEVAL, FFORCE, FPRESS, FDENSITY, FAGE, FCOLOR, FGCELL, FGNDX = rang
 FELASTIDX, FNERVEIDX, FCONC, FEPIGEN, FBIN, FBIN_COUNT, FBIN_OFFSET = 14, 15, 16, 17, 18, 19, 20
 FPARTICLEIDX, FPARTICLE_ID, FMASS_RADIUS = 29, 30, 31
 FBIN_COUNT_ACTIVE_GENES, FBIN_OFFSET_ACTIVE_GENES, FDENSE_LIST_LENGTHS, FDENSE_LISTS = 32, 33, 34, 35
+FBIN_OFFSET_CHANGES, FBIN_COUNT_CHANGES, FDENSE_LIST_LENGTHS_CHANGES, FDENSE_LISTS_CHANGES = 37, 38, 39, 40
+NUM_CHANGES = 9
 
 # m_Param ids (fluid_system.h:77-103) + run controls
 PSIMSCALE, PVISC, PRESTDENSITY, PMASS, PRADIUS = 4, 7, 8, 9, 10
@@ -30,9 +32,11 @@ PGROUND_SLOPE, PFORCE_MIN, PFORCE_MAX, PFORCE_FREQ, PSURFACE_TENSION = 19, 20, 2
 PACTUATION_FACTOR, PACTUATION_PERIOD, PDT, PTIME, PFREEZE = 25, 26, 100, 101, 102
 
 STEP_PHYSICS, STEP_GENES, STEP_REMODEL, STEP_FREEZE, STEP_SURROGATE, STEP_SPECIAL = 1, 2, 4, 8, 16, 32
+STEP_BOND_CHANGES = 64
 STEP_DEFAULT = STEP_PHYSICS | STEP_GENES
 
 OPT_NEIGHBOR_SEARCH = 1
+OPT_HEAL_PARAMS = 2
 MLP_IN, MLP_H, MLP_OUT = 48, 128, 16
 P_W1 = 0
 P_B1 = P_W1 + MLP_H * MLP_IN
@@ -163,6 +167,8 @@ SIGNATURES = [
     ("mg_algorithmic_bytes", C.c_int, [H, C.c_char_p, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("mg_kernel_launches", C.c_uint64, [H]),
     ("mg_run_remodelling", C.c_int, [H]),
+    ("mg_compute_bond_changes", C.c_int, [H, C.c_uint32]),
+    ("mg_run_remodelling_steps", C.c_int, [H, C.c_uint32]),
     ("mg_read_simparams", C.c_int, [C.c_char_p, C.POINTER(SimParams)]),
     ("mg_write_simparams", C.c_int, [C.c_char_p, C.POINTER(SimParams)]),
     ("mg_fparams_from_simparams", C.c_int, [C.POINTER(SimParams), C.c_int32, C.POINTER(FParams)]),

@@ -58,6 +58,8 @@ struct mg_system {
     void* staging = nullptr;
     size_t staging_bytes = 0;
     uint32_t* dense = nullptr;  // gcount | goffset | lists | lens (allocated on demand)
+    uint32_t* changes = nullptr;  // change lists: ccount | coffset | lists | lens (on demand)
+    bool changes_valid = false;   // computeBondChanges ran since the last sort (heal uses it)
     uint32_t* epi_mem = nullptr;  // full epigenetic state of both sets (allocated on demand)
     int phase = PHASE_UNSORTED;
     bool ever_sorted = false;
@@ -251,6 +253,10 @@ mg_status upload_genome(mg_system* h) {
         g.nact[a] = m;
         g.delay[a] = G.delay[a];
     }
+    for (int t = 0; t < 3; t++) {
+        for (int k = 0; k < 8; k++) g.tanh_p[t][k] = G.tanh_param[t][k];
+        for (int k = 0; k < 12; k++) g.bparam[t][k] = G.param[t][k];
+    }
     bool activations = false;
     for (int a = 0; a < NG; a++) activations |= g.nact[a] > 0;
     if (activations) {  // activations change FEPIGEN words: keep the full state
@@ -367,6 +373,7 @@ void enqueue_gather(mg_system* h, bool prof) {
     h->cur = dst;
     h->conc_cur = cdst;
     h->flist_valid = false;
+    h->changes_valid = false;
 }
 
 // dens flags: 1 density, 2 diffusion, 4 genes.  Any conc-writing variant flips conc_cur.
@@ -406,7 +413,7 @@ void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof) {
 void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
     enqueue_insert_rank(h, prof);
     enqueue_gather(h, prof);
-    const bool remodel = (flags & MG_STEP_REMODEL) != 0;
+    const bool remodel = (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) != 0;
     if (flags & MG_STEP_SURROGATE) {
         enqueue_surrogate_morphogen(h, (flags & MG_STEP_PHYSICS) != 0, prof);
     } else {
@@ -419,7 +426,10 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
     if (remodel) {  // Run2Remodelling, after the gene action and before AdvanceCL
         Mark m(h, prof, "remodel");
         if (flags & MG_STEP_PHYSICS) launch_apply_breaks(h->P, h->set[h->cur], h->s, h->stream);
-        launch_remodel(h->P, h->set[h->cur], h->cold, h->s, h->stream);
+        const bool changes = (flags & MG_STEP_BOND_CHANGES) != 0;
+        if (changes) launch_bond_changes(h->P, h->dG, h->set[h->cur], h->cold, h->s, 1.0f, h->stream);
+        launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, changes, h->stream);
+        h->changes_valid = changes;
     }
     if (flags & MG_STEP_PHYSICS) {
         { Mark m(h, prof, "advance");
@@ -434,7 +444,8 @@ int kernels_per_step(const mg_system* h, uint32_t flags) {
     if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE)) n += h->search ? 2 : 1;
     if (flags & MG_STEP_SURROGATE) n += 1;
     if (flags & MG_STEP_PHYSICS) n += 2;
-    if (flags & MG_STEP_REMODEL) n += (flags & MG_STEP_PHYSICS) ? 4 : 3;
+    if (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) n += (flags & MG_STEP_PHYSICS) ? 4 : 3;
+    if (flags & MG_STEP_BOND_CHANGES) n += 1;
     return n;
 }
 
@@ -485,6 +496,7 @@ void after_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
     h->brk_pending = false;
     h->flist_valid = (flags & MG_STEP_PHYSICS) ? false
                      : (h->search && (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)));
+    h->changes_valid = (flags & MG_STEP_BOND_CHANGES) != 0;
 }
 
 mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
@@ -514,6 +526,7 @@ mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
     h->brk_pending = false;
     h->flist_valid = (flags & MG_STEP_PHYSICS) ? false
                      : (h->search && (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)));
+    h->changes_valid = (flags & MG_STEP_BOND_CHANGES) != 0;
     if (h->profile) prof_collect(h);
     return MG_OK;
 }
@@ -532,6 +545,9 @@ size_t buf_bytes(const mg_system* h, int32_t id) {
     case MG_FBIN_COUNT_ACTIVE_GENES: case MG_FBIN_OFFSET_ACTIVE_GENES: return 4 * C * NG;
     case MG_FDENSE_LIST_LENGTHS: return 4 * NG;
     case MG_FDENSE_LISTS: return 4 * n * NG;
+    case MG_FBIN_COUNT_CHANGES: case MG_FBIN_OFFSET_CHANGES: return 4 * C * MG_NUM_CHANGES;
+    case MG_FDENSE_LIST_LENGTHS_CHANGES: return 4 * MG_NUM_CHANGES;
+    case MG_FDENSE_LISTS_CHANGES: return 8 * n * MG_NUM_CHANGES;
     default: return 0;
     }
 }
@@ -591,6 +607,45 @@ mg_status build_dense_lists(mg_system* h) {
         hl[g] = a + b;
     }
     MG_CUDA(h, cudaMemcpy(lens, hl.data(), 4 * NG, cudaMemcpyHostToDevice));
+    return MG_OK;
+}
+
+// countingSortChanges (cuda:406-618) + PrefixSumChangesCL from the bonds' change words.
+mg_status build_change_lists(mg_system* h) {
+    const size_t C = h->P.cells, n = h->cap, K = MG_NUM_CHANGES;
+    if (!h->changes) {
+        cudaError_t e = cudaMalloc(&h->changes, 4 * (2 * C * K + 2 * n * K + K));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            h->changes = nullptr;
+            return fail(h, MG_ERR_OOM, "change-list buffers");
+        }
+    }
+    uint32_t* ccount = h->changes;
+    uint32_t* coffset = ccount + C * K;
+    uint32_t* lists = coffset + C * K;
+    uint32_t* lens = lists + 2 * n * K;
+    cudaStream_t st = h->stream;
+    MG_CUDA(h, cudaMemsetAsync(ccount, 0, 4 * C * K, st));
+    launch_change_cell_counts(h->P, h->set[h->cur], h->cold, h->s, ccount, st);
+    for (size_t k = 0; k < K; k++) {
+        MG_CUDA(h, cudaMemsetAsync(h->s.scan_status, 0, sizeof(unsigned long long) * scan_status_words((uint32_t)C), st));
+        MG_CUDA(h, cudaMemsetAsync(h->s.counters, 0, 4, st));
+        launch_scan(ccount + k * C, coffset + k * C, (uint32_t)C, h->s.scan_status, h->s.counters,
+                    nullptr, h->s.counters + 2, st);
+    }
+    launch_fill_u32(lists, UNDEF, 2 * n * K, st);
+    launch_change_lists(h->P, h->set[h->cur], h->cold, h->s, coffset, lists, st);
+    mg_status s2 = check_device(h);
+    if (s2 != MG_OK) return s2;
+    std::vector<uint32_t> hl(K);
+    for (size_t k = 0; k < K; k++) {
+        uint32_t a = 0, b = 0;
+        MG_CUDA(h, cudaMemcpy(&a, ccount + k * C + C - 1, 4, cudaMemcpyDeviceToHost));
+        MG_CUDA(h, cudaMemcpy(&b, coffset + k * C + C - 1, 4, cudaMemcpyDeviceToHost));
+        hl[k] = a + b;
+    }
+    MG_CUDA(h, cudaMemcpy(lens, hl.data(), 4 * K, cudaMemcpyHostToDevice));
     return MG_OK;
 }
 
@@ -748,6 +803,7 @@ mg_status mg_destroy(mg_handle h) {
     for (auto& m : h->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
     if (h->staging) cudaFree(h->staging);
     if (h->dense) cudaFree(h->dense);
+    if (h->changes) cudaFree(h->changes);
     if (h->epi_mem) cudaFree(h->epi_mem);
     if (h->feat) cudaFree(h->feat);
     if (h->feat_scale) cudaFree(h->feat_scale);
@@ -770,13 +826,15 @@ mg_status mg_update_params(mg_handle h, const mg_fparams* p) {
             return fail(h, MG_ERR_INVALID_ARG, "grid resolution is fixed at mg_create");
     h->params = *p;
     h->time = p->time;
-    const int uniform = h->P.uniform_diff;
-    const int w = h->P.dens_warps, gm = h->P.group_mode, sb = h->P.sub_bits;
+    // state derive() does not compute: genome-derived flags, modes and the launch shape
+    const DevParams old = h->P;
     derive(h->P, *p, h->cap);
-    h->P.uniform_diff = uniform;
-    h->P.dens_warps = w;
-    h->P.group_mode = gm;
-    h->P.sub_bits = sb;
+    h->P.uniform_diff = old.uniform_diff;
+    h->P.full_epi = old.full_epi;
+    h->P.heal_params = old.heal_params;
+    h->P.dens_warps = old.dens_warps;
+    h->P.group_mode = old.group_mode;
+    h->P.sub_bits = old.sub_bits;
     clear_graphs(h);
     // the device copy of the time (both parity slots)
     const uint32_t t2[2] = {*reinterpret_cast<const uint32_t*>(&p->time), *reinterpret_cast<const uint32_t*>(&p->time)};
@@ -953,6 +1011,20 @@ static mg_status enqueue_download(mg_handle h, int32_t id, void* host, size_t by
         MG_CUDA(h, cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, st));
         return MG_OK;
     }
+    if (id == MG_FBIN_COUNT_CHANGES || id == MG_FBIN_OFFSET_CHANGES ||
+        id == MG_FDENSE_LIST_LENGTHS_CHANGES || id == MG_FDENSE_LISTS_CHANGES) {
+        if (h->phase != PHASE_SORTED) return fail(h, MG_ERR_INVALID_ARG, "change lists exist after a sort");
+        mg_status s2 = build_change_lists(h);
+        if (s2 != MG_OK) return s2;
+        const size_t C = h->P.cells, n = h->cap, K = MG_NUM_CHANGES;
+        const uint32_t* base = h->changes;
+        const uint32_t* p = id == MG_FBIN_COUNT_CHANGES ? base
+                          : id == MG_FBIN_OFFSET_CHANGES ? base + C * K
+                          : id == MG_FDENSE_LISTS_CHANGES ? base + 2 * C * K
+                          : base + 2 * C * K + 2 * n * K;
+        MG_CUDA(h, cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, st));
+        return MG_OK;
+    }
     mg_status s2 = ensure_staging(h, bytes);
     if (s2 != MG_OK) return s2;
     uint32_t* sref = (uint32_t*)h->staging;
@@ -1109,8 +1181,23 @@ mg_status mg_advance(mg_handle h) {
 mg_status mg_run_remodelling(mg_handle h) {
     mg_status st = need_sorted(h);
     if (st != MG_OK) return st;
-    launch_remodel(h->P, h->set[h->cur], h->cold, h->s, h->stream);
+    launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, h->changes_valid, h->stream);
     return check_device(h);
+}
+
+mg_status mg_compute_bond_changes(mg_handle h, uint32_t steps_per_inner_loop) {
+    mg_status st = need_sorted(h);
+    if (st != MG_OK) return st;
+    if (steps_per_inner_loop == 0) return fail(h, MG_ERR_INVALID_ARG, "steps_per_InnerPhysicalLoop is 0");
+    launch_bond_changes(h->P, h->dG, h->set[h->cur], h->cold, h->s, (float)steps_per_inner_loop, h->stream);
+    h->changes_valid = true;
+    return check_device(h);
+}
+
+mg_status mg_run_remodelling_steps(mg_handle h, uint32_t steps_per_inner_loop) {
+    mg_status st = mg_compute_bond_changes(h, steps_per_inner_loop);
+    if (st == MG_OK) st = mg_run_remodelling(h);
+    return st;
 }
 
 mg_status mg_run_physical_sort(mg_handle h) {
@@ -1175,6 +1262,11 @@ mg_status mg_set_option(mg_handle h, int32_t option, int32_t value) {
         if (value == 2 && h->search != 2 && h->phase == PHASE_SORTED) h->phase = PHASE_UNSORTED;
         h->search = value;
         h->flist_valid = false;
+        clear_graphs(h);
+        return MG_OK;
+    case MG_OPT_HEAL_PARAMS:
+        if (value < 0 || value > 1) return fail(h, MG_ERR_INVALID_ARG, "heal parameters are 0 or 1");
+        h->P.heal_params = value;
         clear_graphs(h);
         return MG_OK;
     default:

@@ -69,6 +69,7 @@ struct DevParams {
     // its row, 1: one cell), sub-cell bits per axis of the processing order (1 or 2)
     int dens_warps, group_mode, sub_bits;
     int full_epi;  // per-gene FEPIGEN words carried (countdowns, activation lists) instead of bits
+    int heal_params;  // healed bonds: 0 rest length = distance (D5), 1 makeBond's genome defaults
     uint32_t cap;
     uint32_t cells;
 };
@@ -85,6 +86,9 @@ struct DevGenome {
     int act_gene[NG][NG];
     float act_thr[NG][NG];
     uint32_t delay[NG];
+    float tanh_p[3][8];   // bond remodelling tanh parameters per bond type (l_a..l_d, s_a..s_d)
+    float bparam[3][12];  // bond parameters per bond type (elastLim = 8, default rest length,
+                          // modulus, damping = 9, 10, 11)
 };
 
 struct Carried {
@@ -179,8 +183,19 @@ void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool
                   cudaStream_t st);
 void launch_apply_breaks(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
 // re-forming of broken bonds on the sorted state, breaks already applied (D5)
-void launch_remodel(const DevParams& P, const Carried& cur, const Cold& cold, const Scratch& s,
-                    cudaStream_t st);
+// computeBondChanges over the living particles; steps = steps_per_InnerPhysicalLoop
+void launch_bond_changes(const DevParams& P, const DevGenome* G, const Carried& cur,
+                         const Cold& cold, const Scratch& s, float steps, cudaStream_t st);
+// change lists from the bonds' change words: counts / offsets [9][cells], lists [9][2][cap]
+void launch_change_cell_counts(const DevParams& P, const Carried& cur, const Cold& cold,
+                               const Scratch& s, uint32_t* ccount, cudaStream_t st);
+void launch_change_lists(const DevParams& P, const Carried& cur, const Cold& cold,
+                         const Scratch& s, const uint32_t* coffset, uint32_t* lists,
+                         cudaStream_t st);
+// heal: from_changes takes the slots computeBondChanges flagged (change word bit 0), else the
+// D5 rule (lowest slot with an active partner and a failed rest-length test)
+void launch_remodel(const DevParams& P, const DevGenome* G, const Carried& cur, const Cold& cold,
+                    const Scratch& s, bool from_changes, cudaStream_t st);
 // special: externalActuation / fixedParticles for genes 12 / 11 (SpecialParticlesCL)
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_breaks,
                     cudaStream_t st, bool special = false);

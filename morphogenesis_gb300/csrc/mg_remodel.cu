@@ -1,4 +1,21 @@
-// mg_remodel.cu - re-forming of broken bonds (row a11, Run2Remodelling).
+// mg_remodel.cu - bond remodelling (row a11, Run2Remodelling): computeBondChanges, the change
+// lists and the re-forming of broken bonds (heal).
+//
+// computeBondChanges (fluid_system_cuda.cu:1065-1331), over the living particles (gene 2, the
+// dense list it is launched on): bond types from the tissue genes (bone 9: bonds 0-3 apatite;
+// tendon 6 / muscle 7 / elastic ligament 10: bond 0 collagen; the cartilage branch tests gene 6
+// again and is never taken, cuda:1127-1132); per bond in slot order, a bond with rest length > 0
+// averages its strain integrators over the inner-loop steps, zeroes them and scales rest length
+// and modulus by the genome's shifted tanh (cuda:1156-1207); its change word is zeroed; the first
+// bond with rest length 0 or no partner is flagged for heal (change word 1) and ends the loop
+// (cuda:1214-1244).  The lengthen / shorten / strengthen / weaken flags are never set by the
+// reference (their insertion is commented out, cuda:1245-1285), so change lists 1-8 stay empty.
+// tanh is mg_tanh_cw below, written from its definition so the oracle evaluates the same float
+// operations.
+//
+// Change lists (countingSortChanges, cuda:406-618): bin by bin, the bin's particles in sorted
+// order, each particle's bonds in slot order, one entry (particle, bond) per set bit of the
+// bond's change word; built on demand for downloads.
 //
 // Reference: heal (fluid_system_cuda.cu:2047-2105) with contribFindBonds' bond-0 rule
 // (theta = dsq, cuda:1938-1975) and makeBond (cuda:1573-1593); breaks happen in computeForce
@@ -14,7 +31,11 @@
 //   accept   : each proposed-to particle takes proposals in (distance, index) order into its
 //              free incoming slots in slot order; a taken proposal writes the new bond (rest
 //              length = distance, elastic limit 1.5 x rest length, modulus and damping kept,
-//              integrators 0, word 5 = partner's particle id) and the incoming entry.
+//              integrators 0, word 5 = partner's particle id; or, with heal_params 1,
+//              makeBond's elastin defaults from the genome) and the incoming entry.
+// After computeBondChanges the slot a particle heals is its lowest slot in change list 0 that
+// still needs a bond (rest length 0 or no active partner); otherwise its lowest slot whose
+// partner is active and whose rest length failed the rest-length test.
 // Compiled with -fmad=false: distances are the reference expression, bit for bit.
 #include "mg_internal.cuh"
 
@@ -32,14 +53,168 @@ __device__ __forceinline__ uint4 bond_a(const uint4* bond, uint32_t cap, uint32_
     return bond[((size_t)a * cap + p) * 2];
 }
 
-__device__ __forceinline__ int lowest_broken_slot(const uint4* bond, uint32_t cap, uint32_t p,
-                                                  uint32_t nact) {
+__device__ __forceinline__ int heal_slot(const uint4* bond, uint32_t cap, uint32_t p, uint32_t nact,
+                                         const uint32_t* origin, const uint32_t* change,
+                                         bool from_changes) {
+    const uint32_t o = from_changes ? origin[p] : UNDEF;
 #pragma unroll
     for (int a = 0; a < NB; a++) {
         const uint4 A = bond_a(bond, cap, p, a);
-        if (A.x < nact && rest_is_small(A.y)) return a;
+        if (from_changes) {
+            const uint32_t w = o != UNDEF ? change[(size_t)o * NB + a] : 0u;
+            if ((w & 1u) && (__uint_as_float(A.y) == 0.f || A.x >= nact)) return a;
+        } else if (A.x < nact && rest_is_small(A.y)) {
+            return a;
+        }
     }
     return -1;
+}
+
+__device__ __forceinline__ float fbits(uint32_t u) { return __uint_as_float(u); }
+
+// tanh from its definition: |x| < 0.5, odd Taylor polynomial through x^15 (Horner in x^2);
+// 0.5 <= |x| < 9, 1 - 2 / (exp(2|x|) + 1) with exp by Cody-Waite reduction (ln 2 split in a
+// 16-bit head and a tail) and a degree-8 Taylor polynomial scaled by 2^k; beyond, +-1.
+// Within 2 ulp of tanh; separate float operations (-fmad=false), as the oracle evaluates them.
+__device__ float mg_tanh_cw(float x) {
+    if (x != x) return x + x;
+    const float ax = x < 0.0f ? -x : x;
+    if (ax < 0.5f) {
+        const float z = x * x;
+        float t = fbits(0xbabed1b2u);
+        t = t * z + fbits(0x3b6b69e8u);
+        t = t * z + fbits(0xbc11371bu);
+        t = t * z + fbits(0x3cb327a4u);
+        t = t * z + fbits(0xbd5d0dd1u);
+        t = t * z + fbits(0x3e088889u);
+        t = t * z + fbits(0xbeaaaaabu);
+        return x + x * (z * t);
+    }
+    if (ax < 9.0f) {
+        const float y = ax + ax;
+        const float k = rintf(y * fbits(0x3fb8aa3bu));
+        const float r = (y - k * fbits(0x3f317200u)) - k * fbits(0x35bfbe8eu);
+        float e = fbits(0x37d00d01u);
+        e = e * r + fbits(0x39500d01u);
+        e = e * r + fbits(0x3ab60b61u);
+        e = e * r + fbits(0x3c088889u);
+        e = e * r + fbits(0x3d2aaaabu);
+        e = e * r + fbits(0x3e2aaaabu);
+        e = e * r + 0.5f;
+        e = e * r + 1.0f;
+        e = e * r + 1.0f;
+        e = e * fbits((uint32_t)((int)k + 127) << 23);
+        const float t = 1.0f - 2.0f / (e + 1.0f);
+        return x < 0.0f ? -t : t;
+    }
+    return x < 0.0f ? -1.0f : 1.0f;
+}
+
+__global__ void __launch_bounds__(256) k_bond_changes(DevParams P, const DevGenome* __restrict__ G,
+                                                      Carried C, uint32_t* __restrict__ change_cold,
+                                                      float steps,
+                                                      const uint32_t* __restrict__ nactive_p) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = *nactive_p;
+    if (p >= n) return;
+    const uint32_t bits = C.genes[p];
+    if (!((bits >> 2) & 1u)) return;  // the living list (gene 2 at the sort)
+    const size_t cap = P.cap;
+    bool bone, fibre;
+    if (C.epi) {  // the current words, as computeBondChanges reads FEPIGEN
+        bone = C.epi[9 * cap + p] > 0u;
+        fibre = C.epi[6 * cap + p] > 0u || C.epi[7 * cap + p] > 0u || C.epi[10 * cap + p] > 0u;
+    } else {
+        bone = (bits >> 9) & 1u;
+        fibre = ((bits >> 6) & 1u) || ((bits >> 7) & 1u) || ((bits >> 10) & 1u);
+    }
+    const uint32_t o = C.origin[p];
+    for (int b = 0; b < NB; b++) {
+        const int type = bone && b < 4 ? 2 : (fibre && b == 0 ? 1 : 0);
+        const size_t r0 = ((size_t)b * cap + p) * 2;
+        uint4 A = C.bond[r0];
+        float rest = __uint_as_float(A.y);
+        if (rest > 0.f) {
+            uint4 B = C.bond[r0 + 1];
+            const float si = __uint_as_float(B.w) / steps, sq = __uint_as_float(B.z) / steps;
+            const float* T = G->tanh_p[type];
+            rest = rest * (T[0] + T[1] * mg_tanh_cw(T[2] * si - T[3]));
+            const float mod = __uint_as_float(A.z) * (T[4] + T[5] * mg_tanh_cw(T[6] * sq - T[7]));
+            A.y = __float_as_uint(rest);
+            A.z = __float_as_uint(mod);
+            B.z = 0u;
+            B.w = 0u;
+            C.bond[r0] = A;
+            C.bond[r0 + 1] = B;
+        }
+        const bool heal = rest == 0.f || A.x >= n;
+        if (o != UNDEF) change_cold[(size_t)o * NB + b] = heal ? 1u : 0u;
+        if (heal) break;
+    }
+}
+
+// Per cell and change list, the number of change-word bits set on its particles' bonds.
+__global__ void __launch_bounds__(256) k_change_cell_counts(uint32_t cap, uint32_t cells,
+                                                            const uint32_t* __restrict__ origin,
+                                                            const uint32_t* __restrict__ change,
+                                                            const uint32_t* __restrict__ scell,
+                                                            const uint32_t* __restrict__ nactive_p,
+                                                            uint32_t* __restrict__ ccount) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= *nactive_p || p >= cap) return;
+    const uint32_t o = origin[p];
+    if (o == UNDEF) return;
+    const uint32_t c = scell[p];
+    for (int b = 0; b < NB; b++) {
+        uint32_t w = change[(size_t)o * NB + b] & ((1u << MG_NUM_CHANGES) - 1u);
+        while (w) {
+            const int k = __ffs(w) - 1;
+            w &= w - 1;
+            atomicAdd(&ccount[(size_t)k * cells + c], 1u);
+        }
+    }
+}
+
+// Entries of particle p: after those of the earlier particles of its cell, in bond order.
+__global__ void __launch_bounds__(256) k_change_lists(uint32_t cap, uint32_t cells,
+                                                      const uint32_t* __restrict__ origin,
+                                                      const uint32_t* __restrict__ change,
+                                                      const uint32_t* __restrict__ scell,
+                                                      const uint32_t* __restrict__ offset,
+                                                      const uint32_t* __restrict__ coffset,
+                                                      const uint32_t* __restrict__ nactive_p,
+                                                      uint32_t* __restrict__ lists) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= *nactive_p || p >= cap) return;
+    const uint32_t o = origin[p];
+    if (o == UNDEF) return;
+    const uint32_t mask = (1u << MG_NUM_CHANGES) - 1u;
+    uint32_t any = 0;
+    for (int b = 0; b < NB; b++) any |= change[(size_t)o * NB + b] & mask;
+    if (!any) return;
+    const uint32_t c = scell[p];
+    uint32_t before[MG_NUM_CHANGES];
+#pragma unroll
+    for (int k = 0; k < MG_NUM_CHANGES; k++) before[k] = 0;
+    for (uint32_t q = offset[c]; q < p; q++) {
+        const uint32_t oq = origin[q];
+        if (oq == UNDEF) continue;
+        for (int b = 0; b < NB; b++) {
+            const uint32_t w = change[(size_t)oq * NB + b];
+#pragma unroll
+            for (int k = 0; k < MG_NUM_CHANGES; k++) before[k] += (w >> k) & 1u;
+        }
+    }
+    for (int b = 0; b < NB; b++) {
+        const uint32_t w = change[(size_t)o * NB + b] & mask;
+#pragma unroll
+        for (int k = 0; k < MG_NUM_CHANGES; k++)
+            if ((w >> k) & 1u) {
+                const size_t at = coffset[(size_t)k * cells + c] + before[k]++;
+                lists[(size_t)k * 2 * cap + at] = p;
+                lists[(size_t)k * 2 * cap + cap + at] = (uint32_t)b;
+            }
+    }
 }
 
 __global__ void __launch_bounds__(256) k_free_slots(uint32_t cap, const uint4* __restrict__ bond,
@@ -72,6 +247,8 @@ __global__ void __launch_bounds__(256) k_propose(DevParams P, const float4* __re
                                                  const uint32_t* __restrict__ offset,
                                                  const uint8_t* __restrict__ freemask,
                                                  const uint32_t* __restrict__ nactive_p,
+                                                 const uint32_t* __restrict__ change,
+                                                 bool from_changes,
                                                  uint32_t* __restrict__ prop,
                                                  float* __restrict__ propd) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -80,7 +257,7 @@ __global__ void __launch_bounds__(256) k_propose(DevParams P, const float4* __re
     const uint32_t cap = P.cap;
     prop[i] = UNDEF;
     propd[i] = 0.f;
-    if (lowest_broken_slot(bond, cap, i, n) < 0) return;
+    if (heal_slot(bond, cap, i, n, origin, change, from_changes) < 0) return;
     uint32_t partners[NB];
 #pragma unroll
     for (int a = 0; a < NB; a++) partners[a] = bond_a(bond, cap, i, a).x;
@@ -115,7 +292,8 @@ __global__ void __launch_bounds__(256) k_propose(DevParams P, const float4* __re
     propd[i] = best;
 }
 
-__global__ void __launch_bounds__(256) k_accept(DevParams P, uint4* __restrict__ bond,
+__global__ void __launch_bounds__(256) k_accept(DevParams P, const DevGenome* __restrict__ G,
+                                                uint4* __restrict__ bond,
                                                 uint32_t* __restrict__ pidx,
                                                 const uint32_t* __restrict__ origin,
                                                 const uint32_t* __restrict__ pid_cold,
@@ -126,7 +304,8 @@ __global__ void __launch_bounds__(256) k_accept(DevParams P, uint4* __restrict__
                                                 const uint8_t* __restrict__ freemask,
                                                 const uint32_t* __restrict__ prop,
                                                 const float* __restrict__ propd,
-                                                const uint32_t* __restrict__ nactive_p) {
+                                                const uint32_t* __restrict__ nactive_p,
+                                                bool from_changes) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = *nactive_p;
     if (i >= n) return;
@@ -156,14 +335,21 @@ __global__ void __launch_bounds__(256) k_accept(DevParams P, uint4* __restrict__
             else r--;
         }
     if (slot < 0) return;  // no free incoming slot left for this proposal: retry next step
-    const int b = lowest_broken_slot(bond, cap, i, n);
+    const int b = heal_slot(bond, cap, i, n, origin, change_cold, from_changes);
     if (b < 0) return;
     const size_t r0 = ((size_t)b * cap + i) * 2;
     const uint4 A = bond[r0];
-    const float rest = sqrtf(d);
     const uint32_t oj = origin[j];
-    bond[r0] = make_uint4(j, __float_as_uint(rest), A.z, A.w);
-    bond[r0 + 1] = make_uint4(__float_as_uint(1.5f * rest), oj != UNDEF ? pid_cold[oj] : UNDEF, 0u, 0u);
+    const uint32_t pj = oj != UNDEF ? pid_cold[oj] : UNDEF;
+    if (P.heal_params) {  // makeBond(i, j, b, slot, elastin) (cuda:1573-1593)
+        const float* E = G->bparam[0];
+        bond[r0] = make_uint4(j, __float_as_uint(E[9]), __float_as_uint(E[10]), __float_as_uint(E[11]));
+        bond[r0 + 1] = make_uint4(__float_as_uint(E[8]), pj, 0u, 0u);
+    } else {
+        const float rest = sqrtf(d);
+        bond[r0] = make_uint4(j, __float_as_uint(rest), A.z, A.w);
+        bond[r0 + 1] = make_uint4(__float_as_uint(1.5f * rest), pj, 0u, 0u);
+    }
     const uint32_t oi = origin[i];
     if (oi != UNDEF) change_cold[(size_t)oi * NB + b] = 0u;
     pidx[(size_t)j * 12 + 2 * slot] = i;
@@ -172,15 +358,35 @@ __global__ void __launch_bounds__(256) k_accept(DevParams P, uint4* __restrict__
 
 }  // namespace
 
-void launch_remodel(const DevParams& P, const Carried& cur, const Cold& cold, const Scratch& s,
-                    cudaStream_t st) {
+void launch_remodel(const DevParams& P, const DevGenome* G, const Carried& cur, const Cold& cold,
+                    const Scratch& s, bool from_changes, cudaStream_t st) {
     const uint32_t blocks = (P.cap + 255) / 256;
     k_free_slots<<<blocks, 256, 0, st>>>(P.cap, cur.bond, cur.pidx, s.counters + 3, s.freemask);
     k_propose<<<blocks, 256, 0, st>>>(P, cur.pos, cur.bond, cur.origin, cold.pid, s.scell, s.count,
-                                      s.offset, s.freemask, s.counters + 3, s.prop, s.propd);
-    k_accept<<<blocks, 256, 0, st>>>(P, cur.bond, cur.pidx, cur.origin, cold.pid, cold.change,
+                                      s.offset, s.freemask, s.counters + 3, cold.change,
+                                      from_changes, s.prop, s.propd);
+    k_accept<<<blocks, 256, 0, st>>>(P, G, cur.bond, cur.pidx, cur.origin, cold.pid, cold.change,
                                      s.scell, s.count, s.offset, s.freemask, s.prop, s.propd,
-                                     s.counters + 3);
+                                     s.counters + 3, from_changes);
+}
+
+void launch_bond_changes(const DevParams& P, const DevGenome* G, const Carried& cur,
+                         const Cold& cold, const Scratch& s, float steps, cudaStream_t st) {
+    k_bond_changes<<<(P.cap + 255) / 256, 256, 0, st>>>(P, G, cur, cold.change, steps, s.counters + 3);
+}
+
+void launch_change_cell_counts(const DevParams& P, const Carried& cur, const Cold& cold,
+                               const Scratch& s, uint32_t* ccount, cudaStream_t st) {
+    k_change_cell_counts<<<(P.cap + 255) / 256, 256, 0, st>>>(P.cap, P.cells, cur.origin, cold.change,
+                                                              s.scell, s.counters + 3, ccount);
+}
+
+void launch_change_lists(const DevParams& P, const Carried& cur, const Cold& cold,
+                         const Scratch& s, const uint32_t* coffset, uint32_t* lists,
+                         cudaStream_t st) {
+    k_change_lists<<<(P.cap + 255) / 256, 256, 0, st>>>(P.cap, P.cells, cur.origin, cold.change,
+                                                        s.scell, s.offset, coffset, s.counters + 3,
+                                                        lists);
 }
 
 }  // namespace mg

@@ -149,6 +149,12 @@ def make_genome(seed: int = 1, diffusion: float = 0.1, decay: float = 0.01,
         g.param[k][9] = 1.0
         g.param[k][10] = 1000.0
         g.param[k][11] = 10.0
+    # computeBondChanges' shifted tanh per bond type (elastin, collagen, apatite):
+    # rest length *= l_a + l_b tanh(l_c strain - l_d), modulus *= s_a + s_b tanh(s_c strain^2 - s_d)
+    for k, (lb, lc, ld, sb, sc, sd) in enumerate(((0.01, 10.0, 0.7, 0.02, 5.0, 0.5),
+                                                  (0.005, 8.0, 1.0, 0.03, 4.0, 0.25),
+                                                  (0.002, 6.0, 2.0, 0.01, 3.0, 1.0))):
+        g.tanh_param[k][:] = [1.0, lb, lc, ld, 1.0, sb, sc, sd]
     return g
 
 

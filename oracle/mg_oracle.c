@@ -104,6 +104,10 @@ struct mgo_system {
     real* conc_new;
     r4* eterm;          /* [cap][6] outgoing eterm, w = 1 if it was applied */
     unsigned char* brk; /* [cap] bonds that broke this step */
+    /* changes_valid: computeBondChanges ran since the last sort, so heal takes its slots from
+     * the change words (change list 0); heal_params 0 = D5 bond parameters, 1 = makeBond's
+     * genome defaults */
+    int changes_valid, heal_params;
 };
 
 static int g_threads = 0;
@@ -327,6 +331,39 @@ int mgo_import(mgo_handle h, int32_t id, const void* data, size_t bytes) {
     }
 }
 
+/* Change lists (countingSortChanges, cuda:406-618) from the bonds' change words: bin by bin,
+ * the bin's particles in sorted order, each particle's bonds in slot order, one entry
+ * (particle, bond) in list k for bit k of the change word.  counts / offsets are [9][cells],
+ * lists [9][2][cap] (particle row, then bond row; unused entries 0xFFFFFFFF), lengths [9]. */
+static void change_lists(mgo_handle h, uint32_t* counts, uint32_t* offsets, uint32_t* lists,
+                         uint32_t* lengths) {
+    const size_t C = (size_t)h->P.total, cap = h->cap;
+    const uint32_t n = h->nactive;
+    if (counts) memset(counts, 0, 4 * C * MG_NUM_CHANGES);
+    if (offsets) memset(offsets, 0, 4 * C * MG_NUM_CHANGES);
+    if (lists) memset(lists, 0xFF, 8 * cap * MG_NUM_CHANGES);
+    uint32_t len[MG_NUM_CHANGES] = {0};
+    for (size_t c = 0; c < C; c++) {
+        for (int k = 0; k < MG_NUM_CHANGES; k++)
+            if (offsets) offsets[k * C + c] = len[k];
+        const uint32_t last = h->offset[c] + h->count[c];
+        for (uint32_t p = h->offset[c]; p < last && p < n; p++)
+            for (int b = 0; b < NB; b++) {
+                const uint32_t w = h->bond[(size_t)p * NB + b].change;
+                for (int k = 0; k < MG_NUM_CHANGES; k++)
+                    if ((w >> k) & 1u) {
+                        if (counts) counts[k * C + c]++;
+                        if (lists) {
+                            lists[(size_t)k * 2 * cap + len[k]] = p;
+                            lists[(size_t)k * 2 * cap + cap + len[k]] = (uint32_t)b;
+                        }
+                        len[k]++;
+                    }
+            }
+    }
+    if (lengths) memcpy(lengths, len, sizeof len);
+}
+
 int mgo_export(mgo_handle h, int32_t id, void* data, size_t bytes) {
     uint32_t n = h->cap;
     size_t C = (size_t)h->P.total;
@@ -383,6 +420,10 @@ int mgo_export(mgo_handle h, int32_t id, void* data, size_t bytes) {
     case MG_FBIN_OFFSET_ACTIVE_GENES: if (bytes != 4 * C * NG) return 1; memcpy(data, h->goffset, bytes); return 0;
     case MG_FDENSE_LIST_LENGTHS: if (bytes != 4 * NG) return 1; memcpy(data, h->lens, bytes); return 0;
     case MG_FDENSE_LISTS: if (bytes != 4ull * n * NG) return 1; memcpy(data, h->lists, bytes); return 0;
+    case MG_FBIN_COUNT_CHANGES: if (bytes != 4 * C * MG_NUM_CHANGES) return 1; change_lists(h, (uint32_t*)data, NULL, NULL, NULL); return 0;
+    case MG_FBIN_OFFSET_CHANGES: if (bytes != 4 * C * MG_NUM_CHANGES) return 1; change_lists(h, NULL, (uint32_t*)data, NULL, NULL); return 0;
+    case MG_FDENSE_LIST_LENGTHS_CHANGES: if (bytes != 4 * MG_NUM_CHANGES) return 1; change_lists(h, NULL, NULL, NULL, (uint32_t*)data); return 0;
+    case MG_FDENSE_LISTS_CHANGES: if (bytes != 8ull * n * MG_NUM_CHANGES) return 1; change_lists(h, NULL, NULL, (uint32_t*)data, NULL); return 0;
     default: return 2;
     }
 }
@@ -485,6 +526,7 @@ void mgo_prefix_sum_cells(mgo_handle h) {
 
 void mgo_counting_sort_full(mgo_handle h) {
     const params_t* P = &h->P;
+    h->changes_valid = 0;
     uint32_t cap = h->cap;
     size_t C = (size_t)P->total;
     /* sort_ndx = FBIN_OFFSET[icell] + FGNDX (cuda:210-211) */
@@ -860,13 +902,110 @@ void mgo_advance(mgo_handle h) {
  *    word 5 = the partner's particle id (makeBond's [5]). */
 static int rest_is_small(real r) { return (double)r < 0.000000001; }
 
-static int lowest_broken_slot(const mgo_handle h, uint32_t i, uint32_t n) {
+/* The slot a particle heals this call, or -1.  Without bond changes (D5): its lowest slot
+ * whose partner is active and whose rest length failed the rest-length test.  After
+ * computeBondChanges: its lowest slot in change list 0 (change word bit 0, the order
+ * countingSortChanges lists them, cuda:470-490) that still needs a bond (rest length 0 or no
+ * active partner: a bond made since is not replaced). */
+static int heal_slot(const mgo_handle h, uint32_t i, uint32_t n) {
     for (int a = 0; a < NB; a++) {
         const bond_t* b = &h->bond[(size_t)i * NB + a];
-        if (b->partner < n && rest_is_small(b->restlen)) return a;
+        if (h->changes_valid) {
+            if ((b->change & 1u) && (b->restlen == (real)0 || b->partner >= n)) return a;
+        } else if (b->partner < n && rest_is_small(b->restlen)) {
+            return a;
+        }
     }
     return -1;
 }
+
+/* Deterministic tanh for computeBondChanges, the same float operations as the GPU kernel:
+ * |x| < 0.5: odd Taylor polynomial through x^15 (Horner in x^2); 0.5 <= |x| < 9:
+ * 1 - 2 / (exp(2|x|) + 1) with exp by Cody-Waite reduction (ln 2 split in a 16-bit head and a
+ * tail) and a degree-8 Taylor polynomial scaled by 2^k; beyond 9, +-1.  Error <= 2 ulp. */
+static float fbits(uint32_t u) { union { uint32_t u; float f; } v = {u}; return v.f; }
+float mgo_tanh_cw(float x) {
+    if (x != x) return x + x;
+    const float ax = x < 0.0f ? -x : x;
+    if (ax < 0.5f) {
+        const float z = x * x;
+        float t = fbits(0xbabed1b2u);
+        t = t * z + fbits(0x3b6b69e8u);
+        t = t * z + fbits(0xbc11371bu);
+        t = t * z + fbits(0x3cb327a4u);
+        t = t * z + fbits(0xbd5d0dd1u);
+        t = t * z + fbits(0x3e088889u);
+        t = t * z + fbits(0xbeaaaaabu);
+        return x + x * (z * t);
+    }
+    if (ax < 9.0f) {
+        const float y = ax + ax;
+        const float k = rintf(y * fbits(0x3fb8aa3bu));
+        const float r = (y - k * fbits(0x3f317200u)) - k * fbits(0x35bfbe8eu);
+        float e = fbits(0x37d00d01u);
+        e = e * r + fbits(0x39500d01u);
+        e = e * r + fbits(0x3ab60b61u);
+        e = e * r + fbits(0x3c088889u);
+        e = e * r + fbits(0x3d2aaaabu);
+        e = e * r + fbits(0x3e2aaaabu);
+        e = e * r + 0.5f;
+        e = e * r + 1.0f;
+        e = e * r + 1.0f;
+        e = e * fbits((uint32_t)((int)k + 127) << 23);
+        const float t = 1.0f - 2.0f / (e + 1.0f);
+        return x < 0.0f ? -t : t;
+    }
+    return x < 0.0f ? -1.0f : 1.0f;
+}
+
+#ifdef MGO_DOUBLE
+#define RTANH(x) tanh(x)
+#else
+#define RTANH(x) mgo_tanh_cw(x)
+#endif
+
+/* ---- a11: computeBondChanges (cuda:1065-1331) over the living list (dense list 2) ----------
+ * Bond types from the tissue genes (cuda:1127-1132; the cartilage branch tests gene 6 again
+ * and is never taken); per bond in slot order: a bond with rest length > 0 averages its strain
+ * integrators over the inner-loop steps, zeroes them, and scales rest length and modulus by
+ * the genome's shifted tanh (l_a + l_b tanh(l_c s - l_d), s_a + s_b tanh(s_c s2 - s_d),
+ * cuda:1156-1207); its change word is zeroed; the first bond with rest length 0 or no partner
+ * (any index outside the active particles) is flagged for heal (change word 1) and ends the
+ * particle's loop (cuda:1214-1244).  Lengthen/shorten/strengthen/weaken flags are never set by
+ * the reference (their insertion is commented out, cuda:1245-1285), so lists 1-8 stay empty. */
+void mgo_compute_bond_changes(mgo_handle h, uint32_t steps) {
+    const uint32_t n = h->nactive, cap = h->cap;
+    const mg_genome* G = &h->G;
+    const real fsteps = (real)(float)steps;
+    const uint32_t len = h->lens[2];
+    for (uint32_t li = 0; li < len; li++) {
+        const uint32_t i = h->lists[(size_t)2 * cap + li];
+        if (i >= n) continue;
+        int type[NB] = {0, 0, 0, 0, 0, 0};
+        const uint32_t* E = h->epigen;
+        if (E[(size_t)9 * cap + i] > 0) { type[0] = type[1] = type[2] = type[3] = 2; }
+        else if (E[(size_t)6 * cap + i] > 0 || E[(size_t)7 * cap + i] > 0 || E[(size_t)10 * cap + i] > 0) type[0] = 1;
+        for (int b = 0; b < NB; b++) {
+            bond_t* B = &h->bond[(size_t)i * NB + b];
+            if (B->restlen > (real)0) {
+                const real si = B->sint / fsteps, sq = B->sqint / fsteps;
+                B->sint = 0;
+                B->sqint = 0;
+                const float* T = G->tanh_param[type[b]];
+                B->restlen *= (real)T[0] + (real)T[1] * RTANH((real)T[2] * si - (real)T[3]);
+                B->modulus *= (real)T[4] + (real)T[5] * RTANH((real)T[6] * sq - (real)T[7]);
+            }
+            B->change = 0;
+            if (B->restlen == (real)0 || B->partner >= n) {
+                B->change += 1;
+                break;
+            }
+        }
+    }
+    h->changes_valid = 1;
+}
+
+void mgo_set_heal_params(mgo_handle h, int mode) { h->heal_params = mode; }
 
 void mgo_remodel(mgo_handle h) {
     const params_t* P = &h->P;
@@ -888,7 +1027,7 @@ void mgo_remodel(mgo_handle h) {
     for (uint32_t i = 0; i < n; i++) {
         prop[i] = MG_GRID_UNDEF;
         propd[i] = 0;
-        if (h->gcell[i] == MG_GRID_UNDEF || lowest_broken_slot(h, i, n) < 0) continue;
+        if (h->gcell[i] == MG_GRID_UNDEF || heal_slot(h, i, n) < 0) continue;
         const r4 ip = h->pos[i];
         const uint32_t gc = h->gcell[i] - (uint32_t)P->nadj;
         real best = 0;
@@ -931,12 +1070,20 @@ void mgo_remodel(mgo_handle h) {
                 r--;
             }
         if (slot < 0) continue;
-        const int b = lowest_broken_slot(h, i, n);
+        const int b = heal_slot(h, i, n);
         bond_t* nb = &h->bond[(size_t)i * NB + b];
-        const real rest = RSQRT(d);
         nb->partner = j;
-        nb->restlen = rest;
-        nb->elastlim = (real)1.5f * rest;
+        if (h->heal_params) { /* makeBond(i, j, b, slot, elastin) (cuda:1573-1593) */
+            const float* E = h->G.param[0];
+            nb->elastlim = (real)E[8];
+            nb->restlen = (real)E[9];
+            nb->modulus = (real)E[10];
+            nb->damping = (real)E[11];
+        } else {
+            const real rest = RSQRT(d);
+            nb->restlen = rest;
+            nb->elastlim = (real)1.5f * rest;
+        }
         nb->pid = h->pid[j];
         nb->sqint = 0;
         nb->sint = 0;
@@ -1003,7 +1150,8 @@ void mgo_step(mgo_handle h, uint32_t nsteps, uint32_t flags) {
             mgo_compute_diffusion(h);
             mgo_compute_genes(h);
         }
-        if (flags & MG_STEP_REMODEL) mgo_remodel(h); /* Run2Remodelling, before AdvanceCL */
+        if (flags & MG_STEP_BOND_CHANGES) mgo_compute_bond_changes(h, 1); /* ComputeBondChangesCL */
+        if (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) mgo_remodel(h); /* heal, before AdvanceCL */
         if (flags & MG_STEP_PHYSICS) {
             r4 *p0 = NULL, *v0 = NULL, *e0 = NULL;
             const real t = h->P.time;

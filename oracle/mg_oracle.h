@@ -66,6 +66,13 @@ void mgo_compute_diffusion(mgo_handle h);
 void mgo_compute_genes(mgo_handle h);
 void mgo_advance(mgo_handle h);
 void mgo_remodel(mgo_handle h); /* D5 re-forming of broken bonds (Run2Remodelling) */
+/* computeBondChanges over the living list with steps_per_InnerPhysicalLoop = steps; the next
+ * mgo_remodel heals the slots it flagged */
+void mgo_compute_bond_changes(mgo_handle h, uint32_t steps);
+/* bond parameters of healed bonds: 0 = D5 (rest length = distance, elastic limit 1.5 x rest,
+ * modulus and damping kept), 1 = makeBond's elastin defaults from the genome */
+void mgo_set_heal_params(mgo_handle h, int mode);
+float mgo_tanh_cw(float x); /* the deterministic tanh computeBondChanges uses */
 /* nsteps steps in the legacy Run() order, flags as mg_step. */
 void mgo_step(mgo_handle h, uint32_t nsteps, uint32_t flags);
 

@@ -69,6 +69,9 @@ def lib(bits: int = 32) -> C.CDLL:
         "mgo_compute_genes": (None, [H]),
         "mgo_advance": (None, [H]),
         "mgo_remodel": (None, [H]),
+        "mgo_compute_bond_changes": (None, [H, C.c_uint32]),
+        "mgo_set_heal_params": (None, [H, C.c_int]),
+        "mgo_tanh_cw": (C.c_float, [C.c_float]),
         "mgo_step": (None, [H, C.c_uint32, C.c_uint32]),
         "mgo_set_threads": (C.c_int, [C.c_int]),
     }
@@ -94,6 +97,9 @@ def buffer_shape(buf: int, n: int, cells: int):
         A.FBIN_OFFSET: (u32, (cells,)), A.FBIN_COUNT_ACTIVE_GENES: (u32, (A.NUM_GENES, cells)),
         A.FBIN_OFFSET_ACTIVE_GENES: (u32, (A.NUM_GENES, cells)),
         A.FDENSE_LIST_LENGTHS: (u32, (A.NUM_GENES,)), A.FDENSE_LISTS: (u32, (A.NUM_GENES, n)),
+        A.FBIN_COUNT_CHANGES: (u32, (A.NUM_CHANGES, cells)), A.FBIN_OFFSET_CHANGES: (u32, (A.NUM_CHANGES, cells)),
+        A.FDENSE_LIST_LENGTHS_CHANGES: (u32, (A.NUM_CHANGES,)),
+        A.FDENSE_LISTS_CHANGES: (u32, (A.NUM_CHANGES, 2, n)),
     }
     return table[buf]
 
@@ -166,6 +172,8 @@ class Oracle:
     def genes(self): self.L.mgo_compute_genes(self.h)
     def advance(self): self.L.mgo_advance(self.h)
     def remodel(self): self.L.mgo_remodel(self.h)
+    def bond_changes(self, steps: int = 1): self.L.mgo_compute_bond_changes(self.h, int(steps))
+    def set_heal_params(self, mode: int): self.L.mgo_set_heal_params(self.h, int(mode))
 
     def step(self, nsteps: int = 1, flags: int = A.STEP_DEFAULT) -> None:
         self.L.mgo_step(self.h, nsteps, flags)

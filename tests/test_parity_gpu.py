@@ -338,6 +338,66 @@ def test_remodelling_stage_matches_oracle(built):
             assert np.array_equal(g.download(b), o.download(b)), f"buffer {b}"
 
 
+CHANGE_BUFS = [A.FBIN_COUNT_CHANGES, A.FBIN_OFFSET_CHANGES, A.FDENSE_LIST_LENGTHS_CHANGES,
+               A.FDENSE_LISTS_CHANGES]
+
+
+def bond_change_block(seed):
+    """A breakable 10^3 block, moving, 80 % living, tissue genes (tendon, muscle, bone,
+    elastic ligament) at random, genome with the shifted-tanh remodel parameters."""
+    d = demo.make_block(10, "R", seed=seed, breakable=True)
+    r = np.random.default_rng(seed)
+    v = r.uniform(-30, 30, (d.n, 4)).astype(np.float32)
+    v[:, 3] = 0
+    d.arrays[A.FVEL] = v
+    d.arrays[A.FVEVAL] = v.copy()
+    ep = d.arrays[A.FEPIGEN]
+    ep[2] = np.where(r.random(d.n) < 0.8, A.EPIGEN_ACTIVE, 0)
+    for gene, share in ((6, 0.2), (7, 0.2), (9, 0.2), (10, 0.1)):
+        ep[gene] = np.where(r.random(d.n) < share, A.EPIGEN_ACTIVE, 0)
+    return d
+
+
+def test_bond_changes_step_matches_oracle(built):
+    """computeBondChanges + heal of the flagged slots inside the step, both heal-parameter
+    modes: bitwise equal to the oracle, change lists equal."""
+    for heal_params in (0, 1):
+        d = bond_change_block(7)
+        g, o = pair(d, d.n)
+        g.set_option(A.OPT_HEAL_PARAMS, heal_params)
+        o.set_heal_params(heal_params)
+        flags = A.STEP_DEFAULT | A.STEP_BOND_CHANGES
+        g.Run(30, flags)
+        o.step(30, flags)
+        assert compare(g, o), f"bond-change run (heal parameters {heal_params}) is not bitwise equal"
+        for b in CHANGE_BUFS:
+            x, y = g.download(b), o.download(b)
+            assert np.array_equal(x, y), f"change buffer {b}"
+        assert g.download(A.FDENSE_LIST_LENGTHS_CHANGES)[0] > 0, "no slot flagged for heal"
+        g.close()
+        o.close()
+
+
+def test_run2_remodelling_matches_oracle(built):
+    """The reference's Run2 loop: sort, 4 inner physical steps, Run2Remodelling(4)."""
+    d = bond_change_block(8)
+    g, o = pair(d, d.n)
+    for _ in range(3):
+        g.Run2PhysicalSort()
+        o.insert(); o.prefix_sum(); o.sort()
+        for _ in range(4):
+            g.Run2InnerPhysicalLoop()
+            o.pressure(); o.force(); o.advance()
+        g.Run2Remodelling(4)
+        o.bond_changes(4)
+        o.remodel()
+        assert compare(g, o), "Run2Remodelling(4) is not bitwise equal to the oracle"
+        for b in CHANGE_BUFS:
+            assert np.array_equal(g.download(b), o.download(b)), f"change buffer {b}"
+    g.close()
+    o.close()
+
+
 def test_launch_shapes_give_identical_results(built):
     d = demo.make_block((24, 12, 24), "R", seed=6)
     import morphogenesis_gb300 as mg
