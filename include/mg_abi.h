@@ -252,6 +252,12 @@ mg_status mg_compute_bond_changes(mg_handle h, uint32_t steps_per_inner_loop);
 /* Run2Remodelling(steps_per_InnerPhysicalLoop) (fluid_system.cpp:2037-2071): computeBondChanges,
  * then heal of the slots it flagged. */
 mg_status mg_run_remodelling_steps(mg_handle h, uint32_t steps_per_inner_loop);
+/* ZeroVelCL (host_CUDA.cpp:851-857): velocity and evaluated velocity of every particle set to 0
+ * (the freeze phase removes kinetic energy after each sort).  The reference's memset covers
+ * mMaxPoints 32-bit words, a quarter of the float4 buffers; here all of them are cleared. */
+mg_status mg_zero_vel(mg_handle h);
+/* m_Time: the simulation time after the steps issued so far (AdvanceTime, fluid_system.cpp:2016) */
+mg_status mg_get_time(mg_handle h, float* time);
 /* nsteps full steps in the legacy Run() order (fluid_system.cpp:1179-1349), one sort per
  * step: insert, scan, sort, pressure, force, diffusion, genes, [remodel], advance, time. */
 mg_status mg_step(mg_handle h, uint32_t nsteps, uint32_t flags);
@@ -392,6 +398,45 @@ mg_status mg_count_points_csv(const char* path, uint32_t* n); /* lines - 1 */
 mg_status mg_read_points_csv(const char* path, mg_points* pts);
 /* writes dir/particles_pos_vel_color%04d.csv with frame + 100000 (SavePointsCSV2's naming) */
 mg_status mg_write_points_csv(const char* dir, int32_t frame, const mg_points* pts);
+
+/* SpecificationFile.txt (ReadSpecificationFile / WriteSpecificationFile_fromLaunchParams,
+ * fileCL_IO.cpp:742-879, 1006-1114): the run description of the reference's drivers.  Paths
+ * are at most 255 characters without spaces (read with %s); the y/n switches are characters. */
+typedef struct mg_spec {
+    uint32_t num_particles, demo_type, sim_space;
+    float time, dt, gridsize, spacing, simscale, smooth_radius, visc, surface_tension, mass, radius,
+        intstiff, extstiff, extdamp, accel_limit, vel_limit, grav, ground_slope, force_min,
+        force_max, force_freq;
+    float dim[3], pos[3], volmin[3], volmax[3], initmin[3], initmax[3];
+    char params_path[256], points_path[256], genome_path[256], out_path[256];
+    uint32_t num_files, steps_per_inner_loop, steps_per_file, freeze_steps, debug, file_num;
+    char save_ply, save_csv, save_vtp, gene_activity, remodelling, read_genome;
+    float actuation_factor, actuation_period;
+} mg_spec;
+mg_status mg_read_specification(const char* dir, mg_spec* out);        /* dir/SpecificationFile.txt */
+mg_status mg_write_specification(const char* dir, const mg_spec* spec); /* dir/SpecificationFile.txt */
+/* results.csv (WriteResultsCSV, fileCL_IO.cpp:1117-1142): one line of run totals.  timesteps =
+ * (num_files / 100) * steps_per_inner_loop * steps_per_file of spec; num_bonds_end counts the
+ * bonds of elastidx ([n][54], the FELASTIDX layout) with rest length > 0; the reference writes
+ * its 65535 marker for num_bonds_start, which the caller passes. */
+mg_status mg_write_results_csv(const char* input_folder, const char* output_folder,
+                               const mg_spec* spec, uint32_t num_particles_start,
+                               uint32_t num_particles_end, uint32_t num_bonds_start,
+                               const uint32_t* elastidx, uint32_t n);
+/* VTK XML PolyData (ASCII) of a sorted state, SavePointsVTP2's content (fileCL_IO.cpp:1223-1655)
+ * written without VTK: the first `active` particles and the 8 corners of [volmin, volmax] as
+ * points; per particle 6 lines, one per bond slot, to its partner (to itself when the slot has
+ * no partner or a rest length below 1e-6), and 6 self-lines per corner, so the bond arrays
+ * (cell data: parent index, parent id, partner index, partner id, slot, 0; elastic limit, rest
+ * length, modulus, damping, both strain integrators) have one tuple per line; point data FAGE,
+ * FCLR, FPARTICLE_ID, FMASS_RADIUS (mass, radius), FNERVEIDX, FVEL, FVEVAL, FFORCE, FPRESS,
+ * "FDENSITY,(1/density,density)", FCONC_0..15, FEPIGEN_0..15, F_TISSUE_TYPE.  The reference
+ * builds the line cells but no longer attaches them; here they are written.  File:
+ * dir/particles_pos_vel_color%04d.vtp with frame + 100000.  veval, force: [n][4]; press,
+ * invdens: [n] (FDENSITY holds 1/density). */
+mg_status mg_write_points_vtp(const char* dir, int32_t frame, const mg_points* pts, uint32_t active,
+                              const float* veval, const float* force, const float* press,
+                              const float* invdens, const float volmin[3], const float volmax[3]);
 
 /* ---- batched instances (parameter sweeps) --------------------------------------------------- */
 /* A batch steps many independent systems together (each keeps its own particles, grid,

@@ -210,6 +210,13 @@ class FluidSystem:
     def ComputeBondChangesCL(self, steps_per_InnerPhysicalLoop: int = 1) -> None:
         self._check(self.lib.mg_compute_bond_changes(self.h, int(steps_per_InnerPhysicalLoop)))
     def ComputeParticleChangesCL(self) -> None: self._check(self.lib.mg_run_remodelling(self.h))
+    def ZeroVelCL(self) -> None: self._check(self.lib.mg_zero_vel(self.h))
+
+    def time(self) -> float:
+        """m_Time after the steps issued so far."""
+        t = C.c_float()
+        self._check(self.lib.mg_get_time(self.h, C.byref(t)))
+        return t.value
 
     # -- run loop (fluid_system.cpp Run2*) --------------------------------------------------------
     def Run2PhysicalSort(self) -> None: self._check(self.lib.mg_run_physical_sort(self.h))

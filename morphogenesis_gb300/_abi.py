@@ -97,6 +97,22 @@ class SimParams(C.Structure):
         ("volmax", C.c_float * 3), ("initmin", C.c_float * 3), ("initmax", C.c_float * 3)]
 
 
+class Spec(C.Structure):
+    """mg_spec: the fields of SpecificationFile.txt."""
+    _fields_ = [(n, C.c_uint32) for n in ("num_particles", "demo_type", "sim_space")] + [
+        (n, C.c_float) for n in (
+            "time", "dt", "gridsize", "spacing", "simscale", "smooth_radius", "visc", "surface_tension",
+            "mass", "radius", "intstiff", "extstiff", "extdamp", "accel_limit", "vel_limit", "grav",
+            "ground_slope", "force_min", "force_max", "force_freq")] + [
+        (n, C.c_float * 3) for n in ("dim", "pos", "volmin", "volmax", "initmin", "initmax")] + [
+        (n, C.c_char * 256) for n in ("params_path", "points_path", "genome_path", "out_path")] + [
+        (n, C.c_uint32) for n in ("num_files", "steps_per_inner_loop", "steps_per_file", "freeze_steps",
+                                  "debug", "file_num")] + [
+        (n, C.c_char) for n in ("save_ply", "save_csv", "save_vtp", "gene_activity", "remodelling",
+                                "read_genome")] + [
+        ("actuation_factor", C.c_float), ("actuation_period", C.c_float)]
+
+
 class Points(C.Structure):
     """mg_points: host arrays of a particle CSV."""
     _fields_ = [("n", C.c_uint32), ("pos", C.c_void_p), ("vel", C.c_void_p), ("age", C.c_void_p),
@@ -169,6 +185,8 @@ SIGNATURES = [
     ("mg_run_remodelling", C.c_int, [H]),
     ("mg_compute_bond_changes", C.c_int, [H, C.c_uint32]),
     ("mg_run_remodelling_steps", C.c_int, [H, C.c_uint32]),
+    ("mg_zero_vel", C.c_int, [H]),
+    ("mg_get_time", C.c_int, [H, C.POINTER(C.c_float)]),
     ("mg_read_simparams", C.c_int, [C.c_char_p, C.POINTER(SimParams)]),
     ("mg_write_simparams", C.c_int, [C.c_char_p, C.POINTER(SimParams)]),
     ("mg_fparams_from_simparams", C.c_int, [C.POINTER(SimParams), C.c_int32, C.POINTER(FParams)]),
@@ -177,6 +195,13 @@ SIGNATURES = [
     ("mg_count_points_csv", C.c_int, [C.c_char_p, C.POINTER(C.c_uint32)]),
     ("mg_read_points_csv", C.c_int, [C.c_char_p, C.POINTER(Points)]),
     ("mg_write_points_csv", C.c_int, [C.c_char_p, C.c_int32, C.POINTER(Points)]),
+    ("mg_read_specification", C.c_int, [C.c_char_p, C.POINTER(Spec)]),
+    ("mg_write_specification", C.c_int, [C.c_char_p, C.POINTER(Spec)]),
+    ("mg_write_results_csv", C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(Spec), C.c_uint32, C.c_uint32,
+                                       C.c_uint32, C.c_void_p, C.c_uint32]),
+    ("mg_write_points_vtp", C.c_int, [C.c_char_p, C.c_int32, C.POINTER(Points), C.c_uint32, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_float),
+                                      C.POINTER(C.c_float)]),
     ("mg_step_io", C.c_int, [H, C.POINTER(IO), C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(IO), C.c_uint32]),
     ("mg_device_bytes", C.c_int, [H, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     ("mg_get_tuning", C.c_int, [H, C.POINTER(C.c_int32)]),

@@ -1194,6 +1194,20 @@ mg_status mg_compute_bond_changes(mg_handle h, uint32_t steps_per_inner_loop) {
     return check_device(h);
 }
 
+mg_status mg_get_time(mg_handle h, float* time) {
+    if (!h || !time) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    *time = h->time;
+    return MG_OK;
+}
+
+mg_status mg_zero_vel(mg_handle h) {
+    if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    const Carried& c = h->set[h->cur];
+    MG_CUDA(h, cudaMemsetAsync(c.vel, 0, sizeof(float4) * h->cap, h->stream));
+    MG_CUDA(h, cudaMemsetAsync(c.veval, 0, sizeof(float4) * h->cap, h->stream));
+    return check_device(h);
+}
+
 mg_status mg_run_remodelling_steps(mg_handle h, uint32_t steps_per_inner_loop) {
     mg_status st = mg_compute_bond_changes(h, steps_per_inner_loop);
     if (st == MG_OK) st = mg_run_remodelling(h);

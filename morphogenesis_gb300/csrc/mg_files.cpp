@@ -1,5 +1,6 @@
-// mg_files.cpp - the reference's text file formats: SimParams.txt, genome.csv and the particle
-// CSV written by SavePointsCSV2, with the parameter set-up ReadPointsCSV2 performs.
+// mg_files.cpp - the reference's file formats: SimParams.txt, genome.csv, the particle CSV written
+// by SavePointsCSV2 (with the parameter set-up ReadPointsCSV2 performs), SpecificationFile.txt,
+// results.csv and the VTP frames of SavePointsVTP2 (written as VTK XML without VTK).
 //
 // Reference: ReadSimParams / WriteSimParams (fileCL_IO.cpp:471-600), ReadGenome / WriteGenome
 // (fileCL_IO.cpp:71-249), SavePointsCSV2 / ReadPointsCSV2 (fileCL_IO.cpp:250-469), SetupSpacing
@@ -425,6 +426,296 @@ mg_status mg_read_points_csv(const char* path, mg_points* p) {
         p->mass_radius[i] = mass + (radius << 16);  // two 16-bit halves (ReadPointsCSV2)
         p->nerve[i] = nerve;
     }
+    return MG_OK;
+}
+
+// ---- SpecificationFile.txt (ReadSpecificationFile fileCL_IO.cpp:742-879,
+//      WriteSpecificationFile_fromLaunchParams :1006-1114) ----------------------------------
+mg_status mg_read_specification(const char* dir, mg_spec* out) {
+    if (!dir || !out) return bad("mg_read_specification: NULL argument");
+    const std::string path = std::string(dir) + "/SpecificationFile.txt";
+    File fh(path.c_str(), "rb");
+    if (!fh.f) return bad("mg_read_specification: cannot open " + path);
+    FILE* f = fh.f;
+    mg_spec s{};
+    int ret = 0;
+    ret += std::fscanf(f, "num_particles = %u\n ", &s.num_particles);
+    ret += std::fscanf(f, "demoType = %u\n ", &s.demo_type);
+    ret += std::fscanf(f, "simSpace = %u\n ", &s.sim_space);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "m_Time = %f\n ", &s.time);
+    ret += std::fscanf(f, "m_DT = %f\n ", &s.dt);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "gridsize = %f\n ", &s.gridsize);
+    ret += std::fscanf(f, "spacing = %f\n ", &s.spacing);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "simscale = %f\n ", &s.simscale);
+    ret += std::fscanf(f, "smooth_radius = %f\n ", &s.smooth_radius);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "visc = %f\n ", &s.visc);
+    ret += std::fscanf(f, "surface_t = %f\n ", &s.surface_tension);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "mass = %f\n ", &s.mass);
+    ret += std::fscanf(f, "radius = %f\n ", &s.radius);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "int_stiff = %f\n ", &s.intstiff);
+    ret += std::fscanf(f, "ext_stiff = %f\n ", &s.extstiff);
+    ret += std::fscanf(f, "ext_damp = %f\n ", &s.extdamp);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "accel_limit = %f\n ", &s.accel_limit);
+    ret += std::fscanf(f, "vel_limit = %f\n ", &s.vel_limit);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "grav = %f\n ", &s.grav);
+    ret += std::fscanf(f, "slope = %f\n ", &s.ground_slope);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "force_min = %f\n ", &s.force_min);
+    ret += std::fscanf(f, "force_max = %f\n ", &s.force_max);
+    ret += std::fscanf(f, "force_freq = %f\n ", &s.force_freq);
+    skip(std::fscanf(f, "\n"));
+    static const char* const vec_names[6] = {"%s_dim", "pos_%s", "volmin_%s", "volmax_%s", "initmin_%s", "initmax_%s"};
+    float* vecs[6] = {s.dim, s.pos, s.volmin, s.volmax, s.initmin, s.initmax};
+    static const char* const axis[3] = {"x", "y", "z"};
+    for (int v = 0; v < 6; v++) {
+        for (int k = 0; k < 3; k++) {
+            char name[32], fmt[64];
+            std::snprintf(name, sizeof name, vec_names[v], axis[k]);
+            std::snprintf(fmt, sizeof fmt, "%s = %%f\n ", name);
+            ret += std::fscanf(f, fmt, &vecs[v][k]);
+        }
+        skip(std::fscanf(f, "\n"));
+    }
+    ret += std::fscanf(f, "paramsPath = %255s\n ", s.params_path);
+    ret += std::fscanf(f, "pointsPath = %255s\n ", s.points_path);
+    ret += std::fscanf(f, "genomePath = %255s\n ", s.genome_path);
+    ret += std::fscanf(f, "outPath = %255s\n ", s.out_path);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "num_files = %u\n ", &s.num_files);
+    ret += std::fscanf(f, "steps_per_InnerPhysicalLoop = %u\n ", &s.steps_per_inner_loop);
+    ret += std::fscanf(f, "steps_per_file = %u\n ", &s.steps_per_file);
+    ret += std::fscanf(f, "freeze_steps = %u\n ", &s.freeze_steps);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "debug = %u\n ", &s.debug);
+    ret += std::fscanf(f, "file_num = %u\n ", &s.file_num);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "save_ply = %c\n ", &s.save_ply);
+    ret += std::fscanf(f, "save_csv = %c\n ", &s.save_csv);
+    ret += std::fscanf(f, "save_vtp = %c\n ", &s.save_vtp);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "gene_activity = %c\n ", &s.gene_activity);
+    ret += std::fscanf(f, "remodelling = %c\n ", &s.remodelling);
+    ret += std::fscanf(f, "read_genome = %c\n ", &s.read_genome);
+    skip(std::fscanf(f, "\n"));
+    ret += std::fscanf(f, "actuation_factor = %f\n ", &s.actuation_factor);
+    ret += std::fscanf(f, "actuation_period = %f\n ", &s.actuation_period);
+    if (ret != 59) return bad("mg_read_specification: " + std::to_string(ret) + " of 59 fields read from " + path);
+    *out = s;
+    return MG_OK;
+}
+
+mg_status mg_write_specification(const char* dir, const mg_spec* s) {
+    if (!dir || !s) return bad("mg_write_specification: NULL argument");
+    for (const char* p : {s->params_path, s->points_path, s->genome_path, s->out_path})
+        if (std::memchr(p, 0, 256) == nullptr) return bad("mg_write_specification: a path is not terminated");
+    const std::string path = std::string(dir) + "/SpecificationFile.txt";
+    File fh(path.c_str(), "w");
+    if (!fh.f) return bad("mg_write_specification: cannot open " + path);
+    FILE* f = fh.f;
+    int ret = 0;
+    auto chk = [&](int r) { if (r < 0) ret = -1; };
+    chk(std::fprintf(f, "num_particles = %u\n demoType = %u\n simSpace = %u\n \n", s->num_particles, s->demo_type, s->sim_space));
+    chk(std::fprintf(f, "m_Time = %f\n m_DT = %f\n \n", s->time, s->dt));
+    chk(std::fprintf(f, "gridsize = %f\n spacing = %f\n \n", s->gridsize, s->spacing));
+    chk(std::fprintf(f, "simscale = %f\n smooth_radius = %f\n \n", s->simscale, s->smooth_radius));
+    chk(std::fprintf(f, "visc = %f\n surface_t = %f\n \n", s->visc, s->surface_tension));
+    chk(std::fprintf(f, "mass = %f\n radius = %f\n \n", s->mass, s->radius));
+    chk(std::fprintf(f, "int_stiff = %f\n ext_stiff = %f\n ext_damp = %f\n \n", s->intstiff, s->extstiff, s->extdamp));
+    chk(std::fprintf(f, "accel_limit = %f\n vel_limit = %f\n \n", s->accel_limit, s->vel_limit));
+    chk(std::fprintf(f, "grav = %f\n slope = %f\n \n", s->grav, s->ground_slope));
+    chk(std::fprintf(f, "force_min = %f\n force_max = %f\n force_freq = %f\n \n", s->force_min, s->force_max, s->force_freq));
+    chk(std::fprintf(f, "x_dim = %f\n y_dim = %f\n z_dim = %f\n \n", s->dim[0], s->dim[1], s->dim[2]));
+    chk(std::fprintf(f, "pos_x = %f\n pos_y = %f\n pos_z = %f\n \n", s->pos[0], s->pos[1], s->pos[2]));
+    const char* const names[4] = {"volmin", "volmax", "initmin", "initmax"};
+    const float* const vecs[4] = {s->volmin, s->volmax, s->initmin, s->initmax};
+    for (int v = 0; v < 4; v++)
+        chk(std::fprintf(f, "%s_x = %f\n %s_y = %f\n %s_z = %f\n \n", names[v], vecs[v][0], names[v], vecs[v][1],
+                         names[v], vecs[v][2]));
+    chk(std::fprintf(f, "paramsPath = %s\n pointsPath = %s\n genomePath = %s\n outPath = %s\n \n", s->params_path,
+                     s->points_path, s->genome_path, s->out_path));
+    chk(std::fprintf(f, "num_files = %u\n steps_per_InnerPhysicalLoop = %u\n steps_per_file = %u\n freeze_steps = %u\n \n",
+                     s->num_files, s->steps_per_inner_loop, s->steps_per_file, s->freeze_steps));
+    chk(std::fprintf(f, "debug = %u\n file_num = %u\n \n", s->debug, s->file_num));
+    chk(std::fprintf(f, "save_ply = %c\n save_csv = %c\n save_vtp = %c\n \n", s->save_ply, s->save_csv, s->save_vtp));
+    chk(std::fprintf(f, "gene_activity = %c\n remodelling = %c\n read_genome = %c\n \n", s->gene_activity,
+                     s->remodelling, s->read_genome));
+    chk(std::fprintf(f, "actuation_factor = %f\n actuation_period = %f\n \n", s->actuation_factor, s->actuation_period));
+    if (ret < 0) return bad("mg_write_specification: write failed for " + path);
+    return MG_OK;
+}
+
+// ---- results.csv (WriteResultsCSV, fileCL_IO.cpp:1117-1142) ----------------------------------
+mg_status mg_write_results_csv(const char* input_folder, const char* output_folder, const mg_spec* spec,
+                               uint32_t num_particles_start, uint32_t num_particles_end,
+                               uint32_t num_bonds_start, const uint32_t* elastidx, uint32_t n) {
+    if (!input_folder || !output_folder || !spec || (!elastidx && n)) return bad("mg_write_results_csv: NULL argument");
+    uint32_t bonds = 0;
+    for (size_t k = 0; k < (size_t)n * MG_BONDS_PER_PARTICLE; k++) {
+        float rest;
+        std::memcpy(&rest, &elastidx[k * MG_DATA_PER_BOND + 2], 4);
+        if (rest > 0.f) bonds++;
+    }
+    const uint32_t timesteps = (spec->num_files / 100) * spec->steps_per_inner_loop * spec->steps_per_file;
+    const std::string path = std::string(output_folder) + "/results.csv";
+    File fh(path.c_str(), "w");
+    if (!fh.f) return bad("mg_write_results_csv: cannot open " + path);
+    const int r = std::fprintf(fh.f,
+                               "input_folder=,%s,\toutput_folder=,%s,\tfreeze_steps=,%u,\ttimesteps=,%u,\t"
+                               "num_particles_start=,%u,\tnum_particles_end=,%u,\tnum_bonds_start=,%u,\t"
+                               "num_bonds_end=,%u,\t\n",
+                               input_folder, output_folder, spec->freeze_steps, timesteps, num_particles_start,
+                               num_particles_end, num_bonds_start, bonds);
+    if (r < 0) return bad("mg_write_results_csv: write failed for " + path);
+    return MG_OK;
+}
+
+}  // extern "C"
+
+// ---- VTP frames (SavePointsVTP2, fileCL_IO.cpp:1223-1655), VTK XML PolyData in ASCII ----------
+namespace {
+struct Xml {
+    FILE* f;
+    bool ok = true;
+    void put(const char* s) { ok &= std::fputs(s, f) >= 0; }
+    template <class... T> void fmt(const char* s, T... v) { ok &= std::fprintf(f, s, v...) >= 0; }
+    void open_array(const char* type, const char* name, int comps) {
+        fmt("        <DataArray type=\"%s\" Name=\"%s\" NumberOfComponents=\"%d\" format=\"ascii\">\n", type, name,
+            comps);
+    }
+    void close_array() { put("\n        </DataArray>\n"); }
+};
+}  // namespace
+
+extern "C" {
+
+mg_status mg_write_points_vtp(const char* dir, int32_t frame, const mg_points* p, uint32_t active,
+                              const float* veval, const float* force, const float* press, const float* invdens,
+                              const float volmin[3], const float volmax[3]) {
+    if (!dir || !points_ok(p) || !veval || !force || !press || !invdens || !volmin || !volmax)
+        return bad("mg_write_points_vtp: NULL argument");
+    if (active > p->n) return bad("mg_write_points_vtp: active exceeds the particle count");
+    char buf[1024];
+    std::snprintf(buf, sizeof buf, "%s/particles_pos_vel_color%04d.vtp", dir, frame + 100000);
+    File fh(buf, "w");
+    if (!fh.f) return bad(std::string("mg_write_points_vtp: cannot open ") + buf);
+    Xml x{fh.f};
+    const uint32_t n = p->n, np = active + 8, B = MG_BONDS_PER_PARTICLE;
+    const uint64_t nlines = (uint64_t)np * B;
+    auto bond_word = [&](uint32_t i, int b, int w) { return p->elastidx[(size_t)i * MG_BOND_DATA + b * MG_DATA_PER_BOND + w]; };
+    auto bond_float = [&](uint32_t i, int b, int w) {
+        float v;
+        const uint32_t u = bond_word(i, b, w);
+        std::memcpy(&v, &u, 4);
+        return v;
+    };
+    x.put("<?xml version=\"1.0\"?>\n<VTKFile type=\"PolyData\" version=\"0.1\" byte_order=\"LittleEndian\">\n"
+          "  <PolyData>\n");
+    x.fmt("    <Piece NumberOfPoints=\"%u\" NumberOfVerts=\"0\" NumberOfLines=\"%llu\" NumberOfStrips=\"0\" "
+          "NumberOfPolys=\"0\">\n", np, (unsigned long long)nlines);
+    // point data: particles, then the 8 corners with zeros
+    x.put("      <PointData>\n");
+    auto u32_points = [&](const char* name, const uint32_t* a) {
+        x.open_array("UInt32", name, 1);
+        for (uint32_t i = 0; i < active; i++) x.fmt("%u ", a[i]);
+        for (int c = 0; c < 8; c++) x.put("0 ");
+        x.close_array();
+    };
+    u32_points("FAGE", p->age);
+    u32_points("FCLR", p->color);
+    u32_points("FPARTICLE_ID", p->particle_id);
+    x.open_array("UInt32", "FMASS_RADIUS", 2);
+    for (uint32_t i = 0; i < active; i++) x.fmt("%u %u ", p->mass_radius[i] & 0xFFFFu, p->mass_radius[i] >> 16);
+    for (int c = 0; c < 8; c++) x.put("0 0 ");
+    x.close_array();
+    u32_points("FNERVEIDX", p->nerve);
+    auto vec_points = [&](const char* name, const float* a) {
+        x.open_array("Float32", name, 3);
+        for (uint32_t i = 0; i < active; i++) x.fmt("%.9g %.9g %.9g ", a[4 * i], a[4 * i + 1], a[4 * i + 2]);
+        for (int c = 0; c < 8; c++) x.put("0 0 0 ");
+        x.close_array();
+    };
+    vec_points("FVEL", p->vel);
+    vec_points("FVEVAL", veval);
+    vec_points("FFORCE", force);
+    x.open_array("Float32", "FPRESS", 1);
+    for (uint32_t i = 0; i < active; i++) x.fmt("%.9g ", press[i]);
+    for (int c = 0; c < 8; c++) x.put("0 ");
+    x.close_array();
+    x.open_array("Float32", "FDENSITY,(1/density,density)", 2);
+    for (uint32_t i = 0; i < active; i++) x.fmt("%.9g %.9g ", invdens[i], invdens[i] == 0.f ? 0.f : 1.f / invdens[i]);
+    for (int c = 0; c < 8; c++) x.put("0 0 ");
+    x.close_array();
+    for (int t = 0; t < MG_NUM_TF; t++) {
+        char name[32];
+        std::snprintf(name, sizeof name, "FCONC_%d", t);
+        x.open_array("Float32", name, 1);
+        for (uint32_t i = 0; i < active; i++) x.fmt("%.9g ", p->conc[conc_at(p, i, t)]);
+        for (int c = 0; c < 8; c++) x.put("0 ");
+        x.close_array();
+    }
+    for (int g = 0; g < MG_NUM_GENES; g++) {
+        char name[32];
+        std::snprintf(name, sizeof name, "FEPIGEN_%d", g);
+        u32_points(name, p->epigen + (size_t)g * n);
+    }
+    x.open_array("UInt32", "F_TISSUE_TYPE", 1);
+    for (uint32_t i = 0; i < active; i++) {
+        auto on = [&](int g) { return p->epigen[(size_t)g * n + i] > 0u; };
+        const unsigned t = on(9) ? 9 : on(6) ? 6 : on(7) ? 7 : on(10) ? 10 : on(8) ? 8 : 0;
+        x.fmt("%u ", t);
+    }
+    for (int c = 0; c < 8; c++) x.put("0 ");
+    x.close_array();
+    x.put("      </PointData>\n      <CellData>\n");
+    // cell data: one tuple per line (bond slot); the corners' lines carry zeros
+    x.open_array("UInt32", "parent_idx, parent_ID, curr_idx, particle ID, bond index", 6);
+    for (uint32_t i = 0; i < active; i++)
+        for (int b = 0; b < (int)B; b++)
+            x.fmt("%u %u %u %u %d 0 ", i, p->particle_id[i], bond_word(i, b, 0), bond_word(i, b, 5), b);
+    for (uint32_t c = 0; c < 8 * B; c++) x.put("0 0 0 0 0 0 ");
+    x.close_array();
+    static const char* const fnames[6] = {"elastic_limit", "restlength", "modulus", "damping_coeff",
+                                          "strain_integrator", "strain_sq_integrator"};
+    static const int fwords[6] = {1, 2, 3, 4, 7, 6};
+    for (int a = 0; a < 6; a++) {
+        x.open_array("Float32", fnames[a], 1);
+        for (uint32_t i = 0; i < active; i++)
+            for (int b = 0; b < (int)B; b++) x.fmt("%.9g ", bond_float(i, b, fwords[a]));
+        for (uint32_t c = 0; c < 8 * B; c++) x.put("0 ");
+        x.close_array();
+    }
+    x.put("      </CellData>\n      <Points>\n");
+    x.open_array("Float32", "Points", 3);
+    for (uint32_t i = 0; i < active; i++) x.fmt("%.9g %.9g %.9g ", p->pos[4 * i], p->pos[4 * i + 1], p->pos[4 * i + 2]);
+    for (int c = 0; c < 8; c++)
+        x.fmt("%.9g %.9g %.9g ", (c & 1) ? volmax[0] : volmin[0], (c & 2) ? volmax[1] : volmin[1],
+              (c & 4) ? volmax[2] : volmin[2]);
+    x.close_array();
+    x.put("      </Points>\n      <Lines>\n");
+    x.put("        <DataArray type=\"Int64\" Name=\"connectivity\" format=\"ascii\">\n");
+    for (uint32_t i = 0; i < np; i++)
+        for (int b = 0; b < (int)B; b++) {
+            uint32_t j = i;
+            if (i < active) {
+                const uint32_t partner = bond_word(i, b, 0);
+                if (!(bond_float(i, b, 2) < 0.000001f) && partner < active) j = partner;
+            }
+            x.fmt("%u %u ", i, j);
+        }
+    x.close_array();
+    x.put("        <DataArray type=\"Int64\" Name=\"offsets\" format=\"ascii\">\n");
+    for (uint64_t l = 1; l <= nlines; l++) x.fmt("%llu ", (unsigned long long)(2 * l));
+    x.close_array();
+    x.put("      </Lines>\n    </Piece>\n  </PolyData>\n</VTKFile>\n");
+    if (!x.ok) return bad(std::string("mg_write_points_vtp: write failed for ") + buf);
     return MG_OK;
 }
 

@@ -1,5 +1,6 @@
-"""The reference's text files: SimParams.txt, genome.csv and the particle CSV of SavePointsCSV2
-(C++ readers and writers in the library, include/mg_abi.h).
+"""The reference's files: SimParams.txt, genome.csv, the particle CSV of SavePointsCSV2,
+SpecificationFile.txt, results.csv and the VTP frames of SavePointsVTP2 (C++ readers and writers
+in the library, include/mg_abi.h).
 
     sp = read_simparams("demo/SimParams.txt"); params = fparams_from_simparams(sp)
     genome = read_genome("demo/genome.csv")
@@ -104,3 +105,51 @@ def write_points_csv(directory: str | os.PathLike, frame: int, source) -> None:
         n = len(arrays[A.FPOS])
     pts = _points(arrays, n)
     _check(lib, lib.mg_write_points_csv(os.fsencode(directory), int(frame), C.byref(pts)), "write_points_csv")
+
+
+def read_specification(directory: str | os.PathLike) -> A.Spec:
+    """directory/SpecificationFile.txt (ReadSpecificationFile)."""
+    lib = load()
+    sp = A.Spec()
+    _check(lib, lib.mg_read_specification(os.fsencode(directory), C.byref(sp)), "read_specification")
+    return sp
+
+
+def write_specification(directory: str | os.PathLike, spec: A.Spec) -> None:
+    lib = load()
+    _check(lib, lib.mg_write_specification(os.fsencode(directory), C.byref(spec)), "write_specification")
+
+
+def write_results_csv(input_folder: str, output_folder: str | os.PathLike, spec: A.Spec,
+                      num_particles_start: int, num_particles_end: int, elastidx: np.ndarray,
+                      num_bonds_start: int = 65535) -> None:
+    """output_folder/results.csv (WriteResultsCSV); bonds with rest length > 0 are counted from
+    elastidx (FELASTIDX layout).  65535 is the reference's marker for the unknown start count."""
+    lib = load()
+    el = np.ascontiguousarray(elastidx, np.uint32).reshape(-1, A.BOND_DATA)
+    _check(lib, lib.mg_write_results_csv(os.fsencode(input_folder), os.fsencode(output_folder), C.byref(spec),
+                                         int(num_particles_start), int(num_particles_end), int(num_bonds_start),
+                                         el.ctypes.data, len(el)), "write_results_csv")
+
+
+def write_points_vtp(directory: str | os.PathLike, frame: int, source, volmin, volmax,
+                     active: int | None = None) -> None:
+    """directory/particles_pos_vel_color{frame+100000}.vtp (SavePointsVTP2's content, VTK XML).
+    source: a FluidSystem (downloaded; active = its active count) or {buffer id: array} with the
+    point buffers plus FVEVAL, FFORCE, FPRESS, FDENSITY."""
+    lib = load()
+    bufs = [b for b, *_ in _POINT_BUFS] + [A.FEPIGEN, A.FVEVAL, A.FFORCE, A.FPRESS, A.FDENSITY]
+    if hasattr(source, "download"):
+        arrays = {b: source.download(b) for b in bufs}
+        if active is None:
+            active = source.counts()[1]
+    else:
+        arrays = source
+    n = len(arrays[A.FPOS])
+    active = n if active is None else int(active)
+    pts = _points(arrays, n)
+    extra = [np.ascontiguousarray(arrays[b], np.float32) for b in (A.FVEVAL, A.FFORCE, A.FPRESS, A.FDENSITY)]
+    lo = (C.c_float * 3)(*volmin)
+    hi = (C.c_float * 3)(*volmax)
+    _check(lib, lib.mg_write_points_vtp(os.fsencode(directory), int(frame), C.byref(pts), active,
+                                        *[e.ctypes.data for e in extra], lo, hi), "write_points_vtp")

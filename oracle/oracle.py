@@ -173,6 +173,9 @@ class Oracle:
     def advance(self): self.L.mgo_advance(self.h)
     def remodel(self): self.L.mgo_remodel(self.h)
     def bond_changes(self, steps: int = 1): self.L.mgo_compute_bond_changes(self.h, int(steps))
+    def update_params(self, params: A.FParams):
+        if self.L.mgo_update_params(self.h, C.byref(params)):
+            raise RuntimeError("mgo_update_params failed")
     def set_heal_params(self, mode: int): self.L.mgo_set_heal_params(self.h, int(mode))
 
     def step(self, nsteps: int = 1, flags: int = A.STEP_DEFAULT) -> None:

@@ -131,3 +131,99 @@ def test_file_errors_are_returned(built, tmp_path):
         F.read_simparams(tmp_path / "bad.txt")
     with pytest.raises(A.MgError):
         F.read_genome(tmp_path / "missing.csv")
+
+
+def make_spec():
+    s = A.Spec()
+    s.num_particles, s.demo_type, s.sim_space = 4096, 1, 0
+    for k, v in dict(time=0.0, dt=0.001, gridsize=64.0, spacing=1.0, simscale=1.0, smooth_radius=2.0, visc=0.1,
+                     surface_tension=0.25, mass=0.0005, radius=0.5, intstiff=1.0, extstiff=10000.0,
+                     extdamp=256.0, accel_limit=100.0, vel_limit=50.0, grav=9.8, ground_slope=0.0,
+                     force_min=0.0, force_max=0.0, force_freq=8.0, actuation_factor=0.5,
+                     actuation_period=400.0).items():
+        setattr(s, k, v)
+    for k, v in (("dim", (16, 16, 16)), ("pos", (8, 8, 8)), ("volmin", (0, 0, 0)), ("volmax", (64, 64, 64)),
+                 ("initmin", (8, 8, 8)), ("initmax", (24, 24, 24))):
+        getattr(s, k)[:] = v
+    s.params_path, s.points_path = b"demo/SimParams.txt", b"demo/particles_pos_vel_color100001.csv"
+    s.genome_path, s.out_path = b"demo/genome.csv", b"out"
+    s.num_files, s.steps_per_inner_loop, s.steps_per_file, s.freeze_steps = 400, 3, 6, 1
+    s.debug, s.file_num = 0, 0
+    s.save_ply, s.save_csv, s.save_vtp = b"n", b"y", b"y"
+    s.gene_activity, s.remodelling, s.read_genome = b"y", b"y", b"n"
+    return s
+
+
+def test_specification_round_trip_and_layout(built, tmp_path):
+    s = make_spec()
+    F.write_specification(tmp_path, s)
+    text = (tmp_path / "SpecificationFile.txt").read_text()
+    assert text.startswith("num_particles = 4096\n demoType = 1\n simSpace = 0\n \nm_Time = 0.000000\n m_DT = 0.001000\n")
+    assert " \nvolmin_x = 0.000000\n volmin_y = 0.000000\n" in text
+    assert "steps_per_InnerPhysicalLoop = 3\n" in text and "remodelling = y\n" in text
+    back = F.read_specification(tmp_path)
+    for name, _ in A.Spec._fields_:
+        a, b = getattr(s, name), getattr(back, name)
+        if isinstance(a, float):
+            assert b == pytest.approx(a, abs=5e-7), name
+        elif isinstance(a, (int, bytes)):
+            assert a == b, name
+        else:
+            assert list(b) == pytest.approx(list(a), abs=5e-7), name
+
+
+def test_results_csv(built, tmp_path):
+    d = demo.make_block(4, "R", seed=1)
+    el = d.arrays[A.FELASTIDX].reshape(-1, 6, 9).copy()
+    rest = el.view(np.float32)[:, :, 2]
+    bonds = int((rest > 0).sum())
+    F.write_results_csv("in", tmp_path, make_spec(), d.n, d.n - 3, el)
+    text = (tmp_path / "results.csv").read_text()
+    # timesteps = (num_files / 100) * steps_per_InnerPhysicalLoop * steps_per_file = 4 * 3 * 6
+    assert text == (f"input_folder=,in,\toutput_folder=,{tmp_path},\tfreeze_steps=,1,\ttimesteps=,72,\t"
+                    f"num_particles_start=,{d.n},\tnum_particles_end=,{d.n - 3},\tnum_bonds_start=,65535,\t"
+                    f"num_bonds_end=,{bonds},\t\n")
+
+
+def test_points_vtp(built, tmp_path):
+    import xml.etree.ElementTree as ET
+    d = demo.make_block(4, "R", seed=3)
+    n = d.n
+    arrays = {b: np.ascontiguousarray(v) for b, v in d.arrays.items()}
+    for b in (A.FAGE, A.FCOLOR, A.FMASS_RADIUS, A.FNERVEIDX):
+        arrays[b] = np.arange(n, dtype=np.uint32)
+    arrays[A.FFORCE] = np.ones((n, 4), np.float32)
+    arrays[A.FPRESS] = np.full(n, 2.0, np.float32)
+    arrays[A.FDENSITY] = np.full(n, 0.25, np.float32)
+    el = arrays[A.FELASTIDX].reshape(n, 6, 9)
+    el.view(np.float32)[0, 1, 2] = 0.0  # a broken bond is drawn to the particle itself
+    p = d.params
+    F.write_points_vtp(tmp_path, 3, arrays, p.pboundmin, p.pboundmax, active=n)
+    root = ET.parse(tmp_path / "particles_pos_vel_color100003.vtp").getroot()
+    piece = root.find("PolyData/Piece")
+    assert int(piece.get("NumberOfPoints")) == n + 8 and int(piece.get("NumberOfLines")) == 6 * (n + 8)
+
+    def arr(parent, name):
+        for a in piece.find(parent):
+            if a.get("Name") == name:
+                return np.array(a.text.split(), np.float64)
+        raise KeyError(name)
+
+    pts = arr("Points", "Points").reshape(-1, 3)
+    assert np.allclose(pts[:n], arrays[A.FPOS][:, :3]) and np.allclose(pts[n], list(p.pboundmin))
+    assert np.allclose(pts[n + 7], list(p.pboundmax))
+    conn = arr("Lines", "connectivity").astype(np.int64).reshape(-1, 6, 2)
+    partners = el[:, :, 0].astype(np.int64)
+    rest = el.view(np.float32)[:, :, 2]
+    want = np.where((rest >= 1e-6) & (partners < n), partners, np.arange(n)[:, None])
+    assert np.array_equal(conn[:n, :, 1], want) and conn[0, 1, 1] == 0
+    assert np.array_equal(conn[n:, :, 0], conn[n:, :, 1])
+    assert len(arr("CellData", "restlength")) == 6 * (n + 8)
+    assert np.allclose(arr("CellData", "restlength")[: 6 * n], rest.ravel())
+    dens = arr("PointData", "FDENSITY,(1/density,density)").reshape(-1, 2)
+    assert np.allclose(dens[:n], [0.25, 4.0]) and np.allclose(dens[n:], 0)
+    assert np.allclose(arr("PointData", "FCONC_5")[:n], arrays[A.FCONC][:, 5], atol=1e-6)
+    tissue = arr("PointData", "F_TISSUE_TYPE")[:n]
+    ep = arrays[A.FEPIGEN] > 0
+    want_t = np.select([ep[9], ep[6], ep[7], ep[10], ep[8]], [9, 6, 7, 10, 8], 0)
+    assert np.array_equal(tissue, want_t)
