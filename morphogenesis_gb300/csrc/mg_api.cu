@@ -69,6 +69,11 @@ struct mg_system {
     float time = 0.f;
     std::string err;
     std::map<uint64_t, cudaGraphExec_t> graphs;
+    // steps with their host exchange overlapped (mg_step_io): graphs keyed by the step's flags,
+    // buffer state and exchange list; side streams and fork / join events used in capture
+    std::map<std::string, cudaGraphExec_t> io_graphs;
+    cudaStream_t io_st[2] = {nullptr, nullptr};
+    cudaEvent_t io_ev[6] = {};
     bool profile = false;
     std::vector<ProfSlot> prof;
     std::vector<ProfMark> marks;
@@ -275,6 +280,8 @@ mg_status upload_genome(mg_system* h) {
 void clear_graphs(mg_system* h) {
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
+    for (auto& kv : h->io_graphs) cudaGraphExecDestroy(kv.second);
+    h->io_graphs.clear();
 }
 
 uint32_t read_word(mg_system* h, const uint32_t* dptr, mg_status* st) {
@@ -386,7 +393,41 @@ void enqueue_dens(mg_system* h, int flags, bool prof) {
     if (h->search && (flags & 3)) h->flist_valid = true;
 }
 
+// Host exchange folded into a step (mg_step_io): uploads before it, downloads after it, each a
+// plain copy between a host buffer and a device buffer of the reference layout.
+struct IoPlan {
+    const mg_io* in = nullptr;
+    uint32_t nin = 0;
+    const mg_io* out = nullptr;
+    uint32_t nout = 0;
+};
+
+// Device buffer that a plain copy exchanges with the host for buffer id (the mapping of
+// mg_upload / mg_download for those ids), in the handle's current buffer state; null when the
+// buffer needs a layout conversion.
+void* direct_buffer(mg_system* h, int32_t id, bool upload) {
+    Carried& c = h->set[h->cur];
+    switch (id) {
+    case MG_FPOS: return c.pos;
+    case MG_FVEL: return c.vel;
+    case MG_FVEVAL: return c.veval;
+    case MG_FFORCE: return h->s.force;
+    case MG_FPRESS: return h->s.press;
+    case MG_FDENSITY: return h->s.invdens;
+    case MG_FPARTICLEIDX: return c.pidx;
+    case MG_FCONC: return conc_of(h, h->conc_cur);
+    case MG_FBIN_COUNT: return upload ? nullptr : h->s.count;
+    case MG_FBIN_OFFSET: return upload ? nullptr : h->s.offset;
+    default: return nullptr;
+    }
+}
+
 // One step in the legacy Run() order (fluid_system.cpp:1179-1349), one sort per step.
+// With an exchange plan (captured into the step's graph): FPOS is uploaded first on a side
+// stream and the bin / scan / sort kernels start when it has arrived, while the other uploads
+// continue on a second side stream that the gather waits for; FCONC is downloaded on a side
+// stream as soon as the morphogen stage has written it, under the force and integration
+// kernels; the other downloads follow the step, and the step ends when every copy has.
 void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof) {
     DensExtra X{};
     X.feat = h->feat;
@@ -410,8 +451,24 @@ void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof) {
     h->conc_cur = cout;
 }
 
-void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
+void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nullptr) {
+    cudaStream_t st = h->stream;
+    cudaStream_t A = io ? h->io_st[0] : nullptr, B = io ? h->io_st[1] : nullptr;
+    cudaEvent_t* ev = h->io_ev;
+    const bool up = io && io->nin;
+    if (up) {
+        cudaEventRecord(ev[0], st);
+        cudaStreamWaitEvent(A, ev[0], 0);
+        cudaStreamWaitEvent(B, ev[0], 0);
+        for (uint32_t k = 0; k < io->nin; k++)
+            cudaMemcpyAsync(direct_buffer(h, io->in[k].buf_id, true), io->in[k].host, io->in[k].bytes,
+                            cudaMemcpyHostToDevice, io->in[k].buf_id == MG_FPOS ? A : B);
+        cudaEventRecord(ev[1], A);
+        cudaEventRecord(ev[2], B);
+        cudaStreamWaitEvent(st, ev[1], 0);
+    }
     enqueue_insert_rank(h, prof);
+    if (up) cudaStreamWaitEvent(st, ev[2], 0);
     enqueue_gather(h, prof);
     const bool remodel = (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) != 0;
     if (flags & MG_STEP_SURROGATE) {
@@ -420,6 +477,19 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
         int dflags = ((flags & MG_STEP_PHYSICS) ? 1 : 0) | ((flags & MG_STEP_GENES) ? 6 : 0);
         if (dflags) enqueue_dens(h, dflags, prof);
     }
+    bool early = false;  // FCONC is final once the morphogen stage has run
+    if (io)
+        for (uint32_t k = 0; k < io->nout; k++)
+            if (io->out[k].buf_id == MG_FCONC) {
+                if (!early) {
+                    cudaEventRecord(ev[3], st);
+                    cudaStreamWaitEvent(A, ev[3], 0);
+                    early = true;
+                }
+                cudaMemcpyAsync(io->out[k].host, direct_buffer(h, MG_FCONC, false), io->out[k].bytes,
+                                cudaMemcpyDeviceToHost, A);
+            }
+    if (early) cudaEventRecord(ev[4], A);
     if (flags & MG_STEP_PHYSICS) {
         { Mark m(h, prof, "force"); launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream); }
     }
@@ -435,6 +505,13 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof) {
         { Mark m(h, prof, "advance");
           launch_advance(h->P, h->set[h->cur], h->s, !remodel, h->stream, (flags & MG_STEP_SPECIAL) != 0); }
         h->flist_valid = false;
+    }
+    if (io) {
+        for (uint32_t k = 0; k < io->nout; k++)
+            if (io->out[k].buf_id != MG_FCONC)
+                cudaMemcpyAsync(io->out[k].host, direct_buffer(h, io->out[k].buf_id, false), io->out[k].bytes,
+                                cudaMemcpyDeviceToHost, st);
+        if (early) cudaStreamWaitEvent(st, ev[4], 0);
     }
 }
 
@@ -474,6 +551,67 @@ mg_status get_graph(mg_system* h, uint32_t flags, cudaGraphExec_t* out) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
     h->graphs[key] = ge;
+    *out = ge;
+    return MG_OK;
+}
+
+void advance_state(mg_system* h, uint32_t flags);
+
+// Whether a host buffer is page-locked (only those copies are captured into graphs).
+bool host_pinned(const void* ptr) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// Graph of one step with its host exchange folded in (cached by flags, buffer state and the
+// exchange list: host addresses are part of the captured copies).
+mg_status get_io_graph(mg_system* h, uint32_t flags, const IoPlan& io, cudaGraphExec_t* out) {
+    std::string key = std::to_string(flags) + "/" + std::to_string(h->cur) + "/" + std::to_string(h->conc_cur);
+    char buf[96];
+    for (uint32_t k = 0; k < io.nin; k++) {
+        std::snprintf(buf, sizeof buf, "/i%d:%p:%zu", io.in[k].buf_id, io.in[k].host, io.in[k].bytes);
+        key += buf;
+    }
+    for (uint32_t k = 0; k < io.nout; k++) {
+        std::snprintf(buf, sizeof buf, "/o%d:%p:%zu", io.out[k].buf_id, io.out[k].host, io.out[k].bytes);
+        key += buf;
+    }
+    const int cur0 = h->cur, conc0 = h->conc_cur;
+    auto it = h->io_graphs.find(key);
+    if (it != h->io_graphs.end()) {
+        *out = it->second;
+        advance_state(h, flags);
+        return MG_OK;
+    }
+    for (auto& x : h->io_st)
+        if (!x) MG_CUDA(h, cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+    for (auto& x : h->io_ev)
+        if (!x) MG_CUDA(h, cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    DevParams saved = h->P;
+    if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
+    cudaGraph_t g = nullptr;
+    MG_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(h, flags, false, &io);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    h->P = saved;
+    if (e != cudaSuccess) {
+        h->cur = cur0;
+        h->conc_cur = conc0;
+        return cuda_fail(h, e, "cudaStreamEndCapture (exchange step)");
+    }
+    cudaGraphExec_t ge = nullptr;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        h->cur = cur0;
+        h->conc_cur = conc0;
+        return cuda_fail(h, e, "cudaGraphInstantiate (exchange step)");
+    }
+    h->io_graphs[key] = ge;
     *out = ge;
     return MG_OK;
 }
@@ -801,6 +939,8 @@ mg_status mg_destroy(mg_handle h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     clear_graphs(h);
     for (auto& m : h->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
+    for (cudaStream_t x : h->io_st) if (x) cudaStreamDestroy(x);
+    for (cudaEvent_t x : h->io_ev) if (x) cudaEventDestroy(x);
     if (h->staging) cudaFree(h->staging);
     if (h->dense) cudaFree(h->dense);
     if (h->changes) cudaFree(h->changes);
@@ -1058,6 +1198,31 @@ mg_status mg_step_io(mg_handle h, const mg_io* in, uint32_t nin, uint32_t nsteps
                      const mg_io* out, uint32_t nout) {
     if (!h || (nin && !in) || (nout && !out)) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
     if (h->profile) return fail(h, MG_ERR_INVALID_ARG, "mg_step_io: profiling is on");
+    // Plain-copy buffers with the right sizes in page-locked host memory: the copies go into the
+    // steps' graphs, overlapped with the first step (uploads) and the last (downloads).
+    // Anything else goes the sequential way below.
+    bool direct = nsteps > 0 && (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE)) != 0;
+    for (uint32_t k = 0; direct && k < nin; k++)
+        direct = in[k].host && direct_buffer(h, in[k].buf_id, true) &&
+                 in[k].bytes == buf_bytes(h, in[k].buf_id) && host_pinned(in[k].host);
+    for (uint32_t k = 0; direct && k < nout; k++)
+        direct = out[k].host && direct_buffer(h, out[k].buf_id, false) &&
+                 out[k].bytes == buf_bytes(h, out[k].buf_id) && host_pinned(out[k].host);
+    if (direct) {
+        if ((flags & MG_STEP_SURROGATE) && (!h->sur || h->P.full_epi)) return run_steps(h, nsteps, flags);
+        if (nin) h->flist_valid = false;
+        for (uint32_t s = 0; s < nsteps; s++) {
+            IoPlan plan;
+            if (s == 0) { plan.in = in; plan.nin = nin; }
+            if (s + 1 == nsteps) { plan.out = out; plan.nout = nout; }
+            cudaGraphExec_t ge = nullptr;
+            mg_status st = (plan.nin || plan.nout) ? get_io_graph(h, flags, plan, &ge) : get_graph(h, flags, &ge);
+            if (st != MG_OK) return st;
+            MG_CUDA(h, cudaGraphLaunch(ge, h->stream));
+        }
+        after_steps(h, nsteps, flags);
+        return check_device(h);
+    }
     for (uint32_t k = 0; k < nin; k++) {
         mg_status st = enqueue_upload(h, in[k].buf_id, in[k].host, in[k].bytes);
         if (st != MG_OK) return st;

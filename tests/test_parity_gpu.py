@@ -447,6 +447,43 @@ def test_step_io_equals_separate_calls(built, cfg0):
         assert np.array_equal(out_a[k].view(np.uint32), b.download(k).view(np.uint32)), f"buffer {k}"
 
 
+def test_step_io_overlapped_exchange(built, cfg0):
+    """Page-locked plain-copy buffers take the graph path (uploads and downloads captured with
+    the first and last step, FCONC downloaded under the force pass): same results as uploads,
+    steps and downloads issued one after another."""
+    import morphogenesis_gb300 as mg
+
+    bufs = (A.FPOS, A.FVEL, A.FVEVAL, A.FCONC)
+    for nsteps, flags in ((1, A.STEP_DEFAULT), (3, A.STEP_DEFAULT | A.STEP_REMODEL), (2, A.STEP_GENES)):
+        a = mg.FluidSystem(cfg0.params, cfg0.genome, cfg0.n)
+        b = mg.FluidSystem(cfg0.params, cfg0.genome, cfg0.n)
+        for fs in (a, b):
+            fs.TransferToCL(cfg0.arrays)
+            fs.Run(2)
+        host = {k: mg.pinned_empty(*_shape_of(a, k)) for k in bufs}
+        outs = {k: mg.pinned_empty(*_shape_of(a, k)) for k in bufs}
+        for k in bufs:
+            host[k][...] = a.download(k)
+        host[A.FVEL][...] = host[A.FVEL] * np.float32(0.5)
+        for rep in range(2):  # the second call replays the cached exchange graphs
+            for k in bufs:
+                b.upload(k, np.ascontiguousarray(host[k]))
+            b.Run(nsteps, flags)
+            a.step_io(host, nsteps, flags, outs)
+            for k in bufs:
+                assert np.array_equal(outs[k].view(np.uint32), b.download(k).view(np.uint32)), (nsteps, flags, k)
+            for k in bufs:
+                host[k][...] = outs[k]
+        a.close()
+        b.close()
+
+
+def _shape_of(fs, buf):
+    import morphogenesis_gb300 as mg
+    dt, shape = mg._shape(buf, fs.max_points, fs.cells)
+    return shape, dt
+
+
 def test_special_particles_match_oracle(built):
     d = demo.make_block(10, "R", seed=9)
     d.params.actuation_factor = 0.05
