@@ -35,6 +35,15 @@ namespace mg {
 #define MG_DENS_MIN_BLOCKS 3
 #endif
 constexpr int DENS_WARPS = MG_DENS_WARPS;  // warps per block of the warp-cooperative pass
+#ifndef MG_DENS_UNROLL
+#define MG_DENS_UNROLL 4
+#endif
+// survivors tested per iteration of the list-building loop
+constexpr int DENS_UNROLL = MG_DENS_UNROLL;
+// rows of a lane's neighbour list in shared memory: the list appends are branch-free (every
+// survivor is written at the next free row, only hits advance it), so one spare row takes the
+// writes past a full list
+constexpr int NL_ROWS = NL_CAP + 1;
 
 struct CellWin {
     int x, y, z;  // window origin = own cell - (1,1,1)
@@ -427,11 +436,11 @@ __device__ __forceinline__ void dens_list_finish(
         for (uint32_t k = 0; k < n; k++) {
             const uint32_t e = my[k * 32];
             const uint32_t q = e & ~LIST_CELL_START;
+            const float4 jp = pos[q];
             if (F::DENS && (e & LIST_CELL_START)) {  // first neighbour of the next cell:
                 sum += part;                         // flush the previous cell's partial sum
                 part = 0.f;
             }
-            const float4 jp = pos[q];
             const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
             const float dsq = dx * dx + dy * dy + dz * dz;
             if (dsq < 1.f && dsq > 0.f) {  // fluid-force neighbour, kept for the force pass
@@ -466,7 +475,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     __shared__ float4 s_sp[DENS_WARPS][32];
     __shared__ uint32_t s_sq[DENS_WARPS][32];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
-    uint32_t* my = s_list + (size_t)w * NL_CAP * 32 + lane;
+    uint32_t* my = s_list + (size_t)w * NL_ROWS * 32 + lane;
     // Lane k of the grid takes the k-th entry of the processing order, so a warp holds
     // particles of one compact sub-region of a cell; results go to the particle's sorted slot.
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -553,29 +562,31 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                     if (inw) {
                         // Membership uses a fused-multiply-add distance with a slack of a few
                         // ulps, so the list is a superset of the neighbours; the exact test is
-                        // made again when the list is evaluated.  Four survivors per iteration
-                        // keep four independent dependency chains in flight.
+                        // made again when the list is evaluated.  DENS_UNROLL survivors per
+                        // iteration keep independent dependency chains in flight; every
+                        // survivor is written at the lane's next free row and only hits advance
+                        // it (no divergent branch; a full list writes to the spare row).
                         int tt = 0;
-                        for (; tt + 4 <= ns; tt += 4) {
-                            float d[4];
+                        for (; tt + DENS_UNROLL <= ns; tt += DENS_UNROLL) {
+                            float d[DENS_UNROLL];
 #pragma unroll
-                            for (int u = 0; u < 4; u++) d[u] = approx_dsq(ip, s_sp[w][tt + u]);
+                            for (int u = 0; u < DENS_UNROLL; u++) d[u] = approx_dsq(ip, s_sp[w][tt + u]);
 #pragma unroll
-                            for (int u = 0; u < 4; u++)
-                                if (d[u] < R2s && d[u] > 0.f) {
-                                    if (n < (uint32_t)NL_CAP) my[n * 32] = s_sq[w][tt + u] | mark;
-                                    mark = 0u;
-                                    n++;
-                                }
+                            for (int u = 0; u < DENS_UNROLL; u++) {
+                                const bool hit = d[u] < R2s && d[u] > 0.f;
+                                my[min(n, (uint32_t)NL_CAP) * 32] = s_sq[w][tt + u] | mark;
+                                mark = hit ? 0u : mark;
+                                n += hit ? 1u : 0u;
+                            }
                         }
                         for (; tt < ns; tt++) {
                             const float d = approx_dsq(ip, s_sp[w][tt]);
-                            if (d < R2s && d > 0.f) {
-                                if (n < (uint32_t)NL_CAP) my[n * 32] = s_sq[w][tt] | mark;
-                                mark = 0u;
-                                n++;
-                            }
+                            const bool hit = d < R2s && d > 0.f;
+                            my[min(n, (uint32_t)NL_CAP) * 32] = s_sq[w][tt] | mark;
+                            mark = hit ? 0u : mark;
+                            n += hit ? 1u : 0u;
                         }
+
                     }
                     __syncwarp();
                 }
@@ -879,7 +890,7 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
 #define MG_DENS_FLAG_SETS(M) M(1) M(2) M(3) M(5) M(6) M(7) M(9) M(23) M(46) M(47)
 
 cudaError_t physics_init() {
-    const int smem = DENS_WARPS * NL_CAP * 32 * (int)sizeof(uint32_t);
+    const int smem = DENS_WARPS * NL_ROWS * 32 * (int)sizeof(uint32_t);
     cudaError_t e = cudaSuccess;
 #define MG_ATTR(F)                                                                              \
     if (e == cudaSuccess)                                                                       \
@@ -897,7 +908,7 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
     DensExtra X = extra ? *extra : DensExtra{};
     X.epi = P.full_epi ? cur.epi : nullptr;
     const int warps = (P.dens_warps >= 1 && P.dens_warps <= DENS_WARPS) ? P.dens_warps : DENS_WARPS;
-    const size_t smem = (size_t)warps * NL_CAP * 32 * sizeof(uint32_t);
+    const size_t smem = (size_t)warps * NL_ROWS * 32 * sizeof(uint32_t);
     if (search == 1 && (flags & (1 | 2 | 8 | 16))) {
         uint32_t blocks = (P.cap + warps * 32 - 1) / (warps * 32);
 #define MG_DENSW_CASE(F)                                                                          \
