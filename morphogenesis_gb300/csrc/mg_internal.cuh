@@ -146,7 +146,10 @@ struct Scratch {
 
 // ---- launchers (all on one stream; no host synchronisation inside) ----------------------
 cudaError_t physics_init();  // per-kernel attributes, once per device before the first launch
-void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
+// mirror: the processing order's sub-cell codes mirrored in y and z in odd-x cells (not for
+// the per-lane fine-cell search, which reads the codes as positions)
+void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, bool mirror,
+                   cudaStream_t st);
 void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long long* status,
                  uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st);
 size_t scan_status_words(uint32_t n);

@@ -506,8 +506,13 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     while (remaining) {
         const int leader = __ffs(remaining) - 1;
         const uint32_t lcell = __shfl_sync(0xffffffffu, pcell, leader);
-        const bool ing = act && ((remaining >> lane) & 1u) &&
-                         (pcell == lcell || (P.group_mode == 0 && pcell == lcell + 1u));
+        // group: the lanes whose cell is the leader's cell or (group mode 0) the next cell of its
+        // row (any lanes may share a search: each takes its own window cells in ascending
+        // index, its adjacency order; the rule only keeps the group's box compact)
+        const uint32_t span = P.group_mode == 0 ? 1u : 0u;
+        const uint32_t rowx = (uint32_t)P.res[0];
+        const bool ing = act && ((remaining >> lane) & 1u) && pcell >= lcell && pcell - lcell <= span &&
+                         pcell / rowx == lcell / rowx;
         remaining &= ~__ballot_sync(0xffffffffu, ing);
         const float bx0 = warp_min(ing ? ip.x : INF) - Rf, bx1 = warp_max(ing ? ip.x : -INF) + Rf;
         const float by0 = warp_min(ing ? ip.y : INF) - Rf, by1 = warp_max(ing ? ip.y : -INF) + Rf;

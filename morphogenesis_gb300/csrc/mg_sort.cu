@@ -41,15 +41,21 @@ __device__ __forceinline__ uint32_t cell_of(const DevParams& P, float4 p) {
 // Morton code of the sub-cell holding a position inside its cell: 2^sub_bits sub-cells per axis
 // (sub_bits 1 or 2) from the fractional part of the cell coordinate.  Only the density pass's
 // processing order uses it, never a result.
-__device__ __forceinline__ uint32_t sub_of(const DevParams& P, float4 p) {
+// With `mirror`, cells with an odd x index take their y and z sub-cell coordinates mirrored:
+// cells are ordered along x, and the last sub-cells of one cell (high y, z) then meet the first
+// sub-cells of the next one (also high y, z, now at its low-x side), so a warp that takes the
+// tail of one cell and the head of the next still covers a compact region.
+__device__ __forceinline__ uint32_t sub_of(const DevParams& P, float4 p, bool mirror) {
     const float g[3] = {(p.x - P.gmin[0]) * P.gdelta[0], (p.y - P.gmin[1]) * P.gdelta[1],
                         (p.z - P.gmin[2]) * P.gdelta[2]};
     const int nsub = 1 << P.sub_bits;
+    const bool flip = mirror && (((int)floorf(g[0])) & 1);
     uint32_t code = 0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         int q = (int)((g[a] - floorf(g[a])) * (float)nsub);
         q = q < 0 ? 0 : (q > nsub - 1 ? nsub - 1 : q);
+        if (flip && a > 0) q = nsub - 1 - q;
         code |= ((uint32_t)(q & 1) << a) | ((uint32_t)((q >> 1) & 1) << (3 + a));
     }
     return P.sub_bits == 1 ? code & 7u : code;
@@ -62,7 +68,7 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
                                                 uint32_t* __restrict__ newidx,
                                                 uint32_t* __restrict__ count,
                                                 uint8_t* __restrict__ sub,
-                                                uint32_t* __restrict__ step) {
+                                                uint32_t* __restrict__ step, bool mirror) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) *step += 1u;  // step counter read by the later kernels of this step
     bool in = i < P.cap;
@@ -72,7 +78,7 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
         c = cell_of(P, pi);
         cell[i] = c;
         newidx[i] = UNDEF;  // overwritten by the cell sort for particles inside the window
-        if (c != UNDEF) sub[i] = (uint8_t)sub_of(P, pi);
+        if (c != UNDEF) sub[i] = (uint8_t)sub_of(P, pi, mirror);
     }
     bool valid = in && c != UNDEF;
     unsigned active = __ballot_sync(0xffffffffu, valid);
@@ -87,10 +93,11 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
     }
 }
 
-void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st) {
+void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, bool mirror,
+                   cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
     k_insert<<<blocks, 256, 0, st>>>(P, cur.pos, s.cell, s.arank, s.newidx, s.count, s.sub,
-                                      s.counters + 5);
+                                      s.counters + 5, mirror);
 }
 
 // ---- single-pass scan (decoupled look-back) ------------------------------------------------

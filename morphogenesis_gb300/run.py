@@ -31,6 +31,8 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--breakable", action="store_true")
     ap.add_argument("--profile", action="store_true")
+    ap.add_argument("--tuning", type=int, nargs=4, default=None, metavar=("WARPS", "GROUP", "SUB", "SEARCH"),
+                    help="density-pass launch shape (mg_set_tuning)")
     ap.add_argument("--surrogate-train", type=int, default=0,
                     help="train a reaction surrogate for this many Adam steps on pairs captured "
                          "from the block and run the steps with it")
@@ -44,6 +46,8 @@ def main(argv=None):
         fs.TransferToCL({int(k): z[k] for k in z.files})
     else:
         fs.TransferToCL(d.arrays)
+    if a.tuning:
+        fs.set_tuning(*a.tuning)
     if a.surrogate_train:
         from . import surrogate as S
         ds = S.Dataset(2 * d.n)
