@@ -69,6 +69,7 @@ struct mg_system {
     bool ever_sorted = false;
     bool brk_pending = false;
     bool flist_valid = false;   // fluid-force lists match the current positions and order
+    bool drifted = false;       // positions changed since the last sort (cells no longer bound them)
     int search = 1;             // density pass search: 0 direct walk, 1 warp-cooperative
     float time = 0.f;
     std::string err;
@@ -385,6 +386,7 @@ void enqueue_gather(mg_system* h, bool prof) {
     h->conc_cur = cdst;
     h->flist_valid = false;
     h->changes_valid = false;
+    h->drifted = false;
 }
 
 // dens flags: 1 density, 2 diffusion, 4 genes.  Any conc-writing variant flips conc_cur.
@@ -392,7 +394,7 @@ void enqueue_dens(mg_system* h, int flags, bool prof) {
     int cin = h->conc_cur, cout = 1 - h->conc_cur;
     { Mark m(h, prof, flags == 1 ? "pressure" : flags == 7 ? "density_diffusion_genes" : "diffusion_genes");
       launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, flags,
-                  h->search, h->num_sms, h->stream); }
+                  h->drifted && h->search ? 3 : h->search, h->num_sms, h->stream); }
     if (flags & 6) h->conc_cur = cout;
     if (h->search && (flags & 3)) h->flist_valid = true;
 }
@@ -502,7 +504,7 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
         if (flags & MG_STEP_PHYSICS) launch_apply_breaks(h->P, h->set[h->cur], h->s, h->stream);
         const bool changes = (flags & MG_STEP_BOND_CHANGES) != 0;
         if (changes) launch_bond_changes(h->P, h->dG, h->set[h->cur], h->cold, h->s, 1.0f, h->stream);
-        launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, changes, h->stream);
+        launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, changes, !h->drifted, h->stream);
         h->changes_valid = changes;
     }
     if (flags & MG_STEP_PHYSICS) {
@@ -639,6 +641,7 @@ void after_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
     h->flist_valid = (flags & MG_STEP_PHYSICS) ? false
                      : (h->search && (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)));
     h->changes_valid = (flags & MG_STEP_BOND_CHANGES) != 0;
+    h->drifted = (flags & MG_STEP_PHYSICS) != 0;
 }
 
 mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
@@ -669,6 +672,7 @@ mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
     h->flist_valid = (flags & MG_STEP_PHYSICS) ? false
                      : (h->search && (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)));
     h->changes_valid = (flags & MG_STEP_BOND_CHANGES) != 0;
+    h->drifted = (flags & MG_STEP_PHYSICS) != 0;
     if (h->profile) prof_collect(h);
     return MG_OK;
 }
@@ -886,6 +890,8 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     plan.push_back({(void**)&h->s.subcnt, 8 * C});
     plan.push_back({(void**)&h->s.ovf, 4 * n});
     plan.push_back({(void**)&h->s.freemask, n});
+    plan.push_back({(void**)&h->s.prop_cnt, 4 * n});
+    plan.push_back({(void**)&h->s.prop_list, 4 * n * PROP_K});
     plan.push_back({(void**)&h->s.prop, 4 * n});
     plan.push_back({(void**)&h->s.propd, 4 * n});
     plan.push_back({(void**)&h->s.newidx, 4 * n});
@@ -1059,6 +1065,7 @@ static mg_status enqueue_upload(mg_handle h, int32_t id, const void* host, size_
     Carried& c = h->set[h->cur];
     void* dst = nullptr;
     h->flist_valid = false;
+    if (id == MG_FPOS) h->drifted = true;  // positions no longer those the cells were built from
     switch (id) {
     case MG_FPOS: dst = c.pos; break;
     case MG_FVEL: dst = c.vel; break;
@@ -1343,6 +1350,7 @@ mg_status mg_advance(mg_handle h) {
     if (st != MG_OK) return st;
     launch_advance(h->P, h->set[h->cur], h->s, false, h->stream);
     h->flist_valid = false;
+    h->drifted = true;
     h->time = h->time + h->P.dt;
     return check_device(h);
 }
@@ -1350,7 +1358,7 @@ mg_status mg_advance(mg_handle h) {
 mg_status mg_run_remodelling(mg_handle h) {
     mg_status st = need_sorted(h);
     if (st != MG_OK) return st;
-    launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, h->changes_valid, h->stream);
+    launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, h->changes_valid, !h->drifted, h->stream);
     return check_device(h);
 }
 
@@ -1686,6 +1694,7 @@ mg_status mg_dataset_capture(mg_dataset d, mg_handle h, uint32_t flags) {
         launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream);
         launch_advance(h->P, h->set[h->cur], h->s, true, h->stream);
         h->flist_valid = false;
+        h->drifted = true;
         h->time = h->time + h->P.dt;
     }
     h->phase = PHASE_SORTED;

@@ -42,7 +42,8 @@ constexpr uint32_t SPIN_LIMIT = 1u << 22; // bounded look-back polls
 #endif
 constexpr int NL_CAP = MG_NL_CAP;  // per-lane neighbour list of the warp-cooperative density pass
 constexpr int FL_CAP = 32;  // fluid-force neighbours (dsq < 1) recorded per particle
-constexpr int MLP_FEATURES = 48;  // surrogate inputs: conc[16], neighbour-mean conc[16], gene bits[16]
+constexpr int MLP_FEATURES = 48;
+constexpr int PROP_K = 8;  // proposals a particle keeps for ranking (more: it walks its window)  // surrogate inputs: conc[16], neighbour-mean conc[16], gene bits[16]
 
 // Error bits in the device error word.
 enum : uint32_t {
@@ -139,6 +140,8 @@ struct Scratch {
                         // (float bits, slot = step counter parity)
     uint32_t* ovf;      // [cap] particles whose neighbours overflow a lane's list
     uint8_t* freemask;  // [cap] remodelling: free incoming slots
+    uint32_t* prop_cnt;   // [cap] remodelling: proposals received
+    uint32_t* prop_list;  // [cap][PROP_K] remodelling: the first PROP_K proposers
     uint32_t* prop;     // [cap] remodelling: proposed partner
     float* propd;       // [cap] remodelling: its squared distance
     uint32_t* big_list; // [BIG_LIST_CAP] cells that need the block-level ordering
@@ -162,7 +165,8 @@ void launch_gather(const DevParams& P, const Carried& src, const float* src_conc
 // flags: 1 density/pressure, 2 diffusion, 4 gene reaction
 // flags: 1 density, 2 diffusion, 4 gene reaction, 8 surrogate features, 16 capture of
 // training pairs, 32 judge (plain update of sampled / handed-over particles into conc_plain).
-// search: 0 direct walk, 1 warp-cooperative.
+// search: 0 direct walk, 1 warp-cooperative, 2 per-lane fine cells, 3 warp-cooperative for
+// positions that moved since the last sort (no window cell is skipped by its geometric box).
 // Optional outputs of the density pass besides pressure/density/concentrations.
 // Surrogate inputs are scale-free: a particle's diffused and neighbour-mean concentrations are
 // divided by its scale s = max_t |c_t| (after diffusion), and the network predicts the reaction
@@ -196,9 +200,10 @@ void launch_change_lists(const DevParams& P, const Carried& cur, const Cold& col
                          const Scratch& s, const uint32_t* coffset, uint32_t* lists,
                          cudaStream_t st);
 // heal: from_changes takes the slots computeBondChanges flagged (change word bit 0), else the
-// D5 rule (lowest slot with an active partner and a failed rest-length test)
+// D5 rule (lowest slot with an active partner and a failed rest-length test).  prune: positions
+// are those of the last sort, so window cells may be skipped by their geometric box
 void launch_remodel(const DevParams& P, const DevGenome* G, const Carried& cur, const Cold& cold,
-                    const Scratch& s, bool from_changes, cudaStream_t st);
+                    const Scratch& s, bool from_changes, bool prune, cudaStream_t st);
 // special: externalActuation / fixedParticles for genes 12 / 11 (SpecialParticlesCL)
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_breaks,
                     cudaStream_t st, bool special = false);

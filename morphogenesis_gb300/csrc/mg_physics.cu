@@ -25,6 +25,7 @@
 #include <cfloat>
 #include <cuda_bf16.h>
 #include "mg_internal.cuh"
+#include "mg_search.cuh"
 
 namespace mg {
 
@@ -44,18 +45,6 @@ constexpr int DENS_UNROLL = MG_DENS_UNROLL;
 // survivor is written at the next free row, only hits advance it), so one spare row takes the
 // writes past a full list
 constexpr int NL_ROWS = NL_CAP + 1;
-
-struct CellWin {
-    int x, y, z;  // window origin = own cell - (1,1,1)
-};
-
-__device__ __forceinline__ CellWin window_of(const DevParams& P, uint32_t cell) {
-    CellWin w;
-    w.x = (int)(cell % (uint32_t)P.res[0]) - 1;
-    w.z = (int)((cell / (uint32_t)P.res[0]) % (uint32_t)P.res[2]) - 1;
-    w.y = (int)(cell / ((uint32_t)P.res[0] * (uint32_t)P.res[2])) - 1;
-    return w;
-}
 
 // ---- per-neighbour terms ---------------------------------------------------------------
 __device__ __forceinline__ float wendland_term(float dsq, float sr) {
@@ -367,50 +356,9 @@ __global__ void __launch_bounds__(256) k_dens(DevParams P, const DevGenome* __re
 }
 
 // ---- warp-cooperative kernel ----------------------------------------------------------------
-__device__ __forceinline__ float warp_min(float v) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, d));
-    return v;
-}
-__device__ __forceinline__ float warp_max(float v) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, d));
-    return v;
-}
 // List entries are sorted particle indices (< 2^31); the top bit marks the first entry of a
 // lane's list that lies in a new grid cell, where the per-cell partial sum is flushed.
 constexpr uint32_t LIST_CELL_START = 0x80000000u;
-
-// Squared distance with fused multiply-adds: within a few ulps of the reference expression,
-// used only to choose list candidates.
-__device__ __forceinline__ float approx_dsq(float4 a, float4 b) {
-    const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
-    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-}
-
-// Whether cell (cx, cy, cz) can hold a point of the box [b?0, b?1].  The cell's extent is
-// widened by 1% of a cell on each side, far more than the rounding of the cell hash, so a
-// point the hash put in this cell is never excluded.
-__device__ __forceinline__ bool cell_meets_box(const DevParams& P, int cx, int cy, int cz,
-                                               float bx0, float bx1, float by0, float by1,
-                                               float bz0, float bz1) {
-    const float sx = 1.f / P.gdelta[0], sy = 1.f / P.gdelta[1], sz = 1.f / P.gdelta[2];
-    const float x0 = P.gmin[0] + ((float)cx - 0.01f) * sx, x1 = P.gmin[0] + ((float)cx + 1.01f) * sx;
-    const float y0 = P.gmin[1] + ((float)cy - 0.01f) * sy, y1 = P.gmin[1] + ((float)cy + 1.01f) * sy;
-    const float z0 = P.gmin[2] + ((float)cz - 0.01f) * sz, z1 = P.gmin[2] + ((float)cz + 1.01f) * sz;
-    return x1 >= bx0 && x0 <= bx1 && y1 >= by0 && y0 <= by1 && z1 >= bz0 && z0 <= bz1;
-}
-
-__device__ __forceinline__ int warp_mini(int v) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, d));
-    return v;
-}
-__device__ __forceinline__ int warp_maxi(int v) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, d));
-    return v;
-}
 
 // Evaluates a lane's neighbour list (ascending sorted index, first entry of each cell flagged)
 // with the reference expressions: density partial sums per cell, diffusion and neighbour sums,
@@ -469,7 +417,9 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
     uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p,
     const uint32_t* __restrict__ work, uint32_t* __restrict__ ovf, uint32_t* __restrict__ ovf_count,
-    DensExtra X) {
+    DensExtra X, bool prune) {
+    // prune: the positions are those of the last sort, so a window cell whose geometric box
+    // misses the group's box holds no candidate; after positions moved, every cell is walked
     using F = DF<FLAGS>;
     extern __shared__ uint32_t s_list[];  // [warps of the block][NL_CAP][32]
     __shared__ float4 s_sp[DENS_WARPS][32];
@@ -530,7 +480,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
             uint32_t tcnt = 0, toff = 0;
             if (t < ncell) {
                 const int cx = wx0 + t % ncx, cz = wz0 + (t / ncx) % ncz, cy = wy0 + t / (ncx * ncz);
-                if (cell_meets_box(P, cx, cy, cz, bx0, bx1, by0, by1, bz0, bz1)) {
+                if (!prune || cell_meets_box(P, cx, cy, cz, bx0, bx1, by0, by1, bz0, bz1)) {
                     const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
                     tcnt = count[cell];
                     if (tcnt) toff = offset[cell];
@@ -914,15 +864,17 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
     X.epi = P.full_epi ? cur.epi : nullptr;
     const int warps = (P.dens_warps >= 1 && P.dens_warps <= DENS_WARPS) ? P.dens_warps : DENS_WARPS;
     const size_t smem = (size_t)warps * NL_ROWS * 32 * sizeof(uint32_t);
-    if (search == 1 && (flags & (1 | 2 | 8 | 16))) {
+    if ((search == 1 || search == 3) && (flags & (1 | 2 | 8 | 16))) {
         uint32_t blocks = (P.cap + warps * 32 - 1) / (warps * 32);
+        const bool prune = search == 1;
 #define MG_DENSW_CASE(F)                                                                          \
     case F:                                                                                       \
         k_dens_warp<F><<<blocks, warps * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,        \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.counters + 3,   \
-                                                             s.work, s.ovf, s.counters + 6, X);   \
+                                                             s.work, s.ovf, s.counters + 6, X,    \
+                                                             prune);                              \
         k_dens_ovf<F><<<(uint32_t)num_sms * 4, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out,    \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \

@@ -38,6 +38,7 @@
 // partner is active and whose rest length failed the rest-length test.
 // Compiled with -fmad=false: distances are the reference expression, bit for bit.
 #include "mg_internal.cuh"
+#include "mg_search.cuh"
 
 namespace mg {
 
@@ -238,58 +239,134 @@ __global__ void __launch_bounds__(256) k_free_slots(uint32_t cap, const uint4* _
     freemask[j] = (uint8_t)m;
 }
 
-__global__ void __launch_bounds__(256) k_propose(DevParams P, const float4* __restrict__ pos,
-                                                 const uint4* __restrict__ bond,
-                                                 const uint32_t* __restrict__ origin,
-                                                 const uint32_t* __restrict__ pid_cold,
-                                                 const uint32_t* __restrict__ scell,
-                                                 const uint32_t* __restrict__ count,
-                                                 const uint32_t* __restrict__ offset,
-                                                 const uint8_t* __restrict__ freemask,
-                                                 const uint32_t* __restrict__ nactive_p,
-                                                 const uint32_t* __restrict__ change,
-                                                 bool from_changes,
-                                                 uint32_t* __restrict__ prop,
-                                                 float* __restrict__ propd) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// Proposals (the propose pass above), found by the warp-cooperative search of the density pass: a warp takes
+// 32 entries of the processing order (compact in space); the lanes that propose are searched in
+// groups (a cell and the next of its row), each group's window cells are walked in ascending
+// index, their particles loaded coalesced and kept when inside the group's box grown by h, and
+// each proposing lane tests the kept ones of its own window cells with the exact distance
+// expression, keeping the nearest eligible one (ties to the lower sorted index, as the serial
+// walk in ascending index keeps the first).  A proposal is counted at its target and the first
+// PROP_K proposers are listed there for the ranking in k_accept.
+constexpr int PROPOSE_WARPS = 8;
+__global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
+    DevParams P, const float4* __restrict__ pos, const uint4* __restrict__ bond,
+    const uint32_t* __restrict__ origin, const uint32_t* __restrict__ pid_cold,
+    const uint32_t* __restrict__ scell, const uint32_t* __restrict__ count,
+    const uint32_t* __restrict__ offset, const uint8_t* __restrict__ freemask,
+    const uint32_t* __restrict__ nactive_p, const uint32_t* __restrict__ change, bool from_changes,
+    const uint32_t* __restrict__ work, bool prune, uint32_t* __restrict__ prop,
+    float* __restrict__ propd, uint32_t* __restrict__ prop_cnt, uint32_t* __restrict__ prop_list) {
+    __shared__ float4 s_sp[PROPOSE_WARPS][32];
+    __shared__ uint32_t s_sq[PROPOSE_WARPS][32];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = *nactive_p;
-    if (i >= n) return;
+    const bool act = k < n;
     const uint32_t cap = P.cap;
-    prop[i] = UNDEF;
-    propd[i] = 0.f;
-    if (heal_slot(bond, cap, i, n, origin, change, from_changes) < 0) return;
+    const uint32_t i = act ? work[k] : 0u;
+    if (act) {
+        prop[i] = UNDEF;
+        propd[i] = 0.f;
+    }
+    const bool need = act && heal_slot(bond, cap, i, n, origin, change, from_changes) >= 0;
+    if (!__any_sync(0xffffffffu, need)) return;
     uint32_t partners[NB];
 #pragma unroll
-    for (int a = 0; a < NB; a++) partners[a] = bond_a(bond, cap, i, a).x;
-    const float4 ip = pos[i];
-    const uint32_t base = scell[i] - (uint32_t)P.nadj;
+    for (int a = 0; a < NB; a++) partners[a] = need ? bond_a(bond, cap, i, a).x : UNDEF;
+    const float INF = __int_as_float(0x7f800000);
+    const float4 ip = need ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const uint32_t pcell = need ? scell[i] : 0u;
+    const CellWin win = window_of(P, pcell);
+    const float Rf = sqrtf(P.r2diff) * 1.0001f + 1e-3f;
+    const int g = P.gsrch;
+    const int BIG = 1 << 30;
+    const uint32_t rowx = (uint32_t)P.res[0];
     float best = 0.f;
     uint32_t bj = UNDEF;
-    for (int c = 0; c < P.adjcnt; c++) {
-        const uint32_t cell = base + (uint32_t)P.adj[c];
-        const uint32_t cnt = count[cell];
-        if (cnt == 0) continue;
-        const uint32_t off = offset[cell];
-        for (uint32_t j = off; j < off + cnt; j++) {
-            const float4 jp = pos[j];
-            const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
-            const float dsq = dx * dx + dy * dy + dz * dz;
-            if (!(dsq < P.r2diff && dsq > 0.f)) continue;
-            if (freemask[j] == 0) continue;
-            bool bonded = false;
+    unsigned remaining = __ballot_sync(0xffffffffu, need);
+    while (remaining) {
+        const int leader = __ffs(remaining) - 1;
+        const uint32_t lcell = __shfl_sync(0xffffffffu, pcell, leader);
+        const bool ing = need && ((remaining >> lane) & 1u) && pcell >= lcell && pcell - lcell <= 1u &&
+                         pcell / rowx == lcell / rowx;
+        remaining &= ~__ballot_sync(0xffffffffu, ing);
+        const float bx0 = warp_min(ing ? ip.x : INF) - Rf, bx1 = warp_max(ing ? ip.x : -INF) + Rf;
+        const float by0 = warp_min(ing ? ip.y : INF) - Rf, by1 = warp_max(ing ? ip.y : -INF) + Rf;
+        const float bz0 = warp_min(ing ? ip.z : INF) - Rf, bz1 = warp_max(ing ? ip.z : -INF) + Rf;
+        const int wx0 = warp_mini(ing ? win.x : BIG), wx1 = warp_maxi(ing ? win.x : -BIG) + g - 1;
+        const int wy0 = warp_mini(ing ? win.y : BIG), wy1 = warp_maxi(ing ? win.y : -BIG) + g - 1;
+        const int wz0 = warp_mini(ing ? win.z : BIG), wz1 = warp_maxi(ing ? win.z : -BIG) + g - 1;
+        const int ncx = wx1 - wx0 + 1, ncz = wz1 - wz0 + 1;
+        const int ncell = ncx * ncz * (wy1 - wy0 + 1);
+        for (int cb = 0; cb < ncell; cb += 32) {
+            const int t = cb + (int)lane;
+            uint32_t tcnt = 0, toff = 0;
+            if (t < ncell) {
+                const int cx = wx0 + t % ncx, cz = wz0 + (t / ncx) % ncz, cy = wy0 + t / (ncx * ncz);
+                if (cx >= 0 && cy >= 0 && cz >= 0 && cx < P.res[0] && cy < P.res[1] && cz < P.res[2] &&
+                    (!prune || cell_meets_box(P, cx, cy, cz, bx0, bx1, by0, by1, bz0, bz1))) {
+                    const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
+                    tcnt = count[cell];
+                    if (tcnt) toff = offset[cell];
+                }
+            }
+            unsigned ne = __ballot_sync(0xffffffffu, tcnt != 0);
+            while (ne) {
+                const int src = __ffs(ne) - 1;
+                ne &= ne - 1;
+                const uint32_t cnt = __shfl_sync(0xffffffffu, tcnt, src);
+                const uint32_t off = __shfl_sync(0xffffffffu, toff, src);
+                const int ts = cb + src;
+                const int cx = wx0 + ts % ncx, cz = wz0 + (ts / ncx) % ncz, cy = wy0 + ts / (ncx * ncz);
+                const bool inw = ing && cx - win.x >= 0 && cx - win.x < g && cy - win.y >= 0 &&
+                                 cy - win.y < g && cz - win.z >= 0 && cz - win.z < g;
+                if (!__any_sync(0xffffffffu, inw)) continue;
+                for (uint32_t base = 0; base < cnt; base += 32) {
+                    const uint32_t kk = base + lane;
+                    const bool valid = kk < cnt;
+                    const float4 qp = valid ? pos[off + kk] : make_float4(INF, INF, INF, 0.f);
+                    const bool surv = valid && qp.x >= bx0 && qp.x <= bx1 && qp.y >= by0 &&
+                                      qp.y <= by1 && qp.z >= bz0 && qp.z <= bz1;
+                    const unsigned ball = __ballot_sync(0xffffffffu, surv);
+                    if (surv) {
+                        const uint32_t slot = (uint32_t)__popc(ball & ((1u << lane) - 1u));
+                        s_sp[w][slot] = qp;
+                        s_sq[w][slot] = off + kk;
+                    }
+                    __syncwarp();
+                    const int ns = __popc(ball);
+                    if (inw) {
+                        for (int tt = 0; tt < ns; tt++) {
+                            const float4 jp = s_sp[w][tt];
+                            const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+                            const float dsq = dx * dx + dy * dy + dz * dz;
+                            if (!(dsq < P.r2diff && dsq > 0.f)) continue;
+                            const uint32_t j = s_sq[w][tt];
+                            if (bj != UNDEF && (dsq > best || (dsq == best && j > bj))) continue;
+                            if (freemask[j] == 0) continue;
+                            bool bonded = false;
 #pragma unroll
-            for (int a = 0; a < NB; a++) bonded |= partners[a] == j;
-            if (bonded) continue;
-            const uint32_t o = origin[j];
-            if (o == UNDEF || pid_cold[o] == 0u) continue;  // boundary marker particles
-            if (bj == UNDEF || dsq < best) {
-                best = dsq;
-                bj = j;
+                            for (int a = 0; a < NB; a++) bonded |= partners[a] == j;
+                            if (bonded) continue;
+                            const uint32_t o = origin[j];
+                            if (o == UNDEF || pid_cold[o] == 0u) continue;  // boundary markers
+                            best = dsq;
+                            bj = j;
+                        }
+                    }
+                    __syncwarp();
+                }
             }
         }
     }
-    prop[i] = bj;
-    propd[i] = best;
+    if (need) {
+        prop[i] = bj;
+        propd[i] = best;
+        if (bj != UNDEF) {
+            const uint32_t slot = atomicAdd(&prop_cnt[bj], 1u);
+            if (slot < (uint32_t)PROP_K) prop_list[(size_t)bj * PROP_K + slot] = i;
+        }
+    }
 }
 
 __global__ void __launch_bounds__(256) k_accept(DevParams P, const DevGenome* __restrict__ G,
@@ -305,7 +382,9 @@ __global__ void __launch_bounds__(256) k_accept(DevParams P, const DevGenome* __
                                                 const uint32_t* __restrict__ prop,
                                                 const float* __restrict__ propd,
                                                 const uint32_t* __restrict__ nactive_p,
-                                                bool from_changes) {
+                                                bool from_changes,
+                                                const uint32_t* __restrict__ prop_cnt,
+                                                const uint32_t* __restrict__ prop_list) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = *nactive_p;
     if (i >= n) return;
@@ -314,16 +393,25 @@ __global__ void __launch_bounds__(256) k_accept(DevParams P, const DevGenome* __
     const float d = propd[i];
     const uint32_t cap = P.cap;
     uint32_t rank = 0;
-    const uint32_t base = scell[j] - (uint32_t)P.nadj;
-    for (int c = 0; c < P.adjcnt; c++) {
-        const uint32_t cell = base + (uint32_t)P.adj[c];
-        const uint32_t cnt = count[cell];
-        const uint32_t off = cnt ? offset[cell] : 0u;
-        for (uint32_t q = off; q < off + cnt; q++)
-            if (prop[q] == j) {
-                const float dq = propd[q];
-                if (dq < d || (dq == d && q < i)) rank++;
-            }
+    const uint32_t np = prop_cnt[j];
+    if (np <= (uint32_t)PROP_K) {  // every proposer of j is listed
+        for (uint32_t t = 0; t < np; t++) {
+            const uint32_t q = prop_list[(size_t)j * PROP_K + t];
+            const float dq = propd[q];
+            if (dq < d || (dq == d && q < i)) rank++;
+        }
+    } else {  // more proposers than listed: the ones within h of j, found in its window
+        const uint32_t base = scell[j] - (uint32_t)P.nadj;
+        for (int c = 0; c < P.adjcnt; c++) {
+            const uint32_t cell = base + (uint32_t)P.adj[c];
+            const uint32_t cnt = count[cell];
+            const uint32_t off = cnt ? offset[cell] : 0u;
+            for (uint32_t q = off; q < off + cnt; q++)
+                if (prop[q] == j) {
+                    const float dq = propd[q];
+                    if (dq < d || (dq == d && q < i)) rank++;
+                }
+        }
     }
     const uint32_t m = freemask[j];
     int slot = -1;
@@ -359,15 +447,18 @@ __global__ void __launch_bounds__(256) k_accept(DevParams P, const DevGenome* __
 }  // namespace
 
 void launch_remodel(const DevParams& P, const DevGenome* G, const Carried& cur, const Cold& cold,
-                    const Scratch& s, bool from_changes, cudaStream_t st) {
+                    const Scratch& s, bool from_changes, bool prune, cudaStream_t st) {
     const uint32_t blocks = (P.cap + 255) / 256;
     k_free_slots<<<blocks, 256, 0, st>>>(P.cap, cur.bond, cur.pidx, s.counters + 3, s.freemask);
-    k_propose<<<blocks, 256, 0, st>>>(P, cur.pos, cur.bond, cur.origin, cold.pid, s.scell, s.count,
-                                      s.offset, s.freemask, s.counters + 3, cold.change,
-                                      from_changes, s.prop, s.propd);
+    cudaMemsetAsync(s.prop_cnt, 0, sizeof(uint32_t) * P.cap, st);
+    const uint32_t wblocks = (P.cap + PROPOSE_WARPS * 32 - 1) / (PROPOSE_WARPS * 32);
+    k_propose_warp<<<wblocks, PROPOSE_WARPS * 32, 0, st>>>(
+        P, cur.pos, cur.bond, cur.origin, cold.pid, s.scell, s.count, s.offset, s.freemask,
+        s.counters + 3, cold.change, from_changes, s.work, prune, s.prop, s.propd, s.prop_cnt,
+        s.prop_list);
     k_accept<<<blocks, 256, 0, st>>>(P, G, cur.bond, cur.pidx, cur.origin, cold.pid, cold.change,
                                      s.scell, s.count, s.offset, s.freemask, s.prop, s.propd,
-                                     s.counters + 3, from_changes);
+                                     s.counters + 3, from_changes, s.prop_cnt, s.prop_list);
 }
 
 void launch_bond_changes(const DevParams& P, const DevGenome* G, const Carried& cur,

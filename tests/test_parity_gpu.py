@@ -398,6 +398,35 @@ def test_run2_remodelling_matches_oracle(built):
     o.close()
 
 
+def test_drifted_positions_between_sorts(built):
+    """The reference's Run2 loop sorts once per several inner steps, so positions move away from
+    the cells they were binned in (here about an eighth of a cell per step).  The neighbour
+    searches then must not skip window cells by their geometric box: pressure, force, diffusion
+    and the re-forming search stay bitwise equal to the oracle, which walks all 27 cells."""
+    d = demo.make_block(10, "R", seed=12, breakable=True)
+    d.params.pvel_limit = 1000.0
+    d.params.paccel_limit = 1e6
+    r = np.random.default_rng(12)
+    v = r.uniform(-500, 500, (d.n, 4)).astype(np.float32)
+    v[:, 3] = 0
+    d.arrays[A.FVEL] = v
+    d.arrays[A.FVEVAL] = v.copy()
+    g, o = pair(d, d.n)
+    for _ in range(3):
+        g.Run2PhysicalSort()
+        o.insert(); o.prefix_sum(); o.sort()
+        for _ in range(4):
+            g.Run2InnerPhysicalLoop()
+            o.pressure(); o.force(); o.advance()
+        g.Run2GeneAction()
+        o.diffusion(); o.genes()
+        g.Run2Remodelling()
+        o.remodel()
+        assert compare(g, o), "drifted positions: not bitwise equal to the oracle"
+    g.close()
+    o.close()
+
+
 def test_launch_shapes_give_identical_results(built):
     d = demo.make_block((24, 12, 24), "R", seed=6)
     import morphogenesis_gb300 as mg
