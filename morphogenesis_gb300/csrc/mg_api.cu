@@ -70,6 +70,8 @@ struct mg_system {
     bool brk_pending = false;
     bool flist_valid = false;   // fluid-force lists match the current positions and order
     bool drifted = false;       // positions changed since the last sort (cells no longer bound them)
+    uint32_t* hmem = nullptr;   // re-forming candidates recorded by the density pass: count [cap]
+                                // then list [NL_CAP][cap] (allocated with the first remodelling step)
     int search = 1;             // density pass search: 0 direct walk, 1 warp-cooperative
     float time = 0.f;
     std::string err;
@@ -390,11 +392,16 @@ void enqueue_gather(mg_system* h, bool prof) {
 }
 
 // dens flags: 1 density, 2 diffusion, 4 genes.  Any conc-writing variant flips conc_cur.
-void enqueue_dens(mg_system* h, int flags, bool prof) {
+void enqueue_dens(mg_system* h, int flags, bool prof, bool heal_list = false) {
     int cin = h->conc_cur, cout = 1 - h->conc_cur;
+    DensExtra X{};
+    if (heal_list) {
+        X.hcount = h->hmem;
+        X.hlist = h->hmem + h->cap;
+    }
     { Mark m(h, prof, flags == 1 ? "pressure" : flags == 7 ? "density_diffusion_genes" : "diffusion_genes");
       launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, flags,
-                  h->drifted && h->search ? 3 : h->search, h->num_sms, h->stream); }
+                  h->drifted && h->search ? 3 : h->search, h->num_sms, h->stream, &X); }
     if (flags & 6) h->conc_cur = cout;
     if (h->search && (flags & 3)) h->flist_valid = true;
 }
@@ -434,8 +441,30 @@ void* direct_buffer(mg_system* h, int32_t id, bool upload) {
 // continue on a second side stream that the gather waits for; FCONC is downloaded on a side
 // stream as soon as the morphogen stage has written it, under the force and integration
 // kernels; the other downloads follow the step, and the step ends when every copy has.
-void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof) {
+// Whether a step with these flags takes its re-forming candidates from the density pass: the
+// pass runs the diffusion (or surrogate) neighbour sums at the positions the re-forming search
+// sees, with a list-building search, and the record's memory exists.
+bool heal_from_density(const mg_system* h, uint32_t flags) {
+    return (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) && (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)) &&
+           (h->search == 1 || h->search == 2) && h->hmem;
+}
+
+// Allocates the candidate record for a remodelling step (before any capture); without memory
+// the step searches instead.
+void prepare_step(mg_system* h, uint32_t flags) {
+    if (!(flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) || h->hmem) return;
+    if (cudaMalloc(&h->hmem, sizeof(uint32_t) * (size_t)h->cap * (1 + NL_CAP)) != cudaSuccess) {
+        cudaGetLastError();
+        h->hmem = nullptr;
+    }
+}
+
+void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof, bool heal_list = false) {
     DensExtra X{};
+    if (heal_list) {
+        X.hcount = h->hmem;
+        X.hlist = h->hmem + h->cap;
+    }
     X.feat = h->feat;
     X.feat_scale = h->feat_scale;
     X.conc_plain = h->conc_plain;
@@ -477,11 +506,12 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
     if (up) cudaStreamWaitEvent(st, ev[2], 0);
     enqueue_gather(h, prof);
     const bool remodel = (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) != 0;
+    const bool heal_list = heal_from_density(h, flags);
     if (flags & MG_STEP_SURROGATE) {
-        enqueue_surrogate_morphogen(h, (flags & MG_STEP_PHYSICS) != 0, prof);
+        enqueue_surrogate_morphogen(h, (flags & MG_STEP_PHYSICS) != 0, prof, heal_list);
     } else {
         int dflags = ((flags & MG_STEP_PHYSICS) ? 1 : 0) | ((flags & MG_STEP_GENES) ? 6 : 0);
-        if (dflags) enqueue_dens(h, dflags, prof);
+        if (dflags) enqueue_dens(h, dflags, prof, heal_list);
     }
     bool early = false;  // FCONC is final once the morphogen stage has run
     if (io)
@@ -504,7 +534,8 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
         if (flags & MG_STEP_PHYSICS) launch_apply_breaks(h->P, h->set[h->cur], h->s, h->stream);
         const bool changes = (flags & MG_STEP_BOND_CHANGES) != 0;
         if (changes) launch_bond_changes(h->P, h->dG, h->set[h->cur], h->cold, h->s, 1.0f, h->stream);
-        launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, changes, !h->drifted, h->stream);
+        launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, changes, !h->drifted,
+                       heal_list ? h->hmem : nullptr, heal_list ? h->hmem + h->cap : nullptr, h->stream);
         h->changes_valid = changes;
     }
     if (flags & MG_STEP_PHYSICS) {
@@ -547,6 +578,7 @@ mg_status get_graph(mg_system* h, uint32_t flags, cudaGraphExec_t* out) {
     DevParams saved = h->P;
     if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
     cudaGraph_t g = nullptr;
+    prepare_step(h, flags);
     MG_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     enqueue_step(h, flags, false);
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
@@ -600,6 +632,7 @@ mg_status get_io_graph(mg_system* h, uint32_t flags, const IoPlan& io, cudaGraph
     DevParams saved = h->P;
     if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
     cudaGraph_t g = nullptr;
+    prepare_step(h, flags);
     MG_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     enqueue_step(h, flags, false, &io);
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
@@ -655,6 +688,7 @@ mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
         if (h->profile) {
             DevParams saved = h->P;
             if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
+            prepare_step(h, flags);
             enqueue_step(h, flags, true);
             h->P = saved;
         } else {
@@ -954,6 +988,7 @@ mg_status mg_destroy(mg_handle h) {
     if (h->staging) cudaFree(h->staging);
     if (h->dense) cudaFree(h->dense);
     if (h->changes) cudaFree(h->changes);
+    if (h->hmem) cudaFree(h->hmem);
     if (h->epi_mem) cudaFree(h->epi_mem);
     if (h->feat) cudaFree(h->feat);
     if (h->feat_scale) cudaFree(h->feat_scale);
@@ -1358,7 +1393,8 @@ mg_status mg_advance(mg_handle h) {
 mg_status mg_run_remodelling(mg_handle h) {
     mg_status st = need_sorted(h);
     if (st != MG_OK) return st;
-    launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, h->changes_valid, !h->drifted, h->stream);
+    launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, h->changes_valid, !h->drifted, nullptr,
+                   nullptr, h->stream);
     return check_device(h);
 }
 
@@ -1930,6 +1966,7 @@ static mg_status batch_graph(mg_batch b, uint32_t flags, cudaGraphExec_t* out) {
         DevParams saved = h->P;
         if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
         cudaGraph_t g = nullptr;
+        prepare_step(h, flags);
         cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
             enqueue_step(h, flags, false);  // advances the member's buffer state

@@ -181,6 +181,10 @@ struct DensExtra {
     uint32_t* epi;             // full epigenetic state of the current set ([16][cap]) or null
     const uint32_t* step;      // JUDGE: device step counter
     uint32_t judge_period, judge_stride;
+    // re-forming candidates: the neighbours within h of each particle, in canonical order
+    // ([NL_CAP][cap]), with their number (0xFFFFFFFF: not recorded, the particle overflowed)
+    uint32_t* hlist;
+    uint32_t* hcount;
 };
 void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
@@ -202,8 +206,11 @@ void launch_change_lists(const DevParams& P, const Carried& cur, const Cold& col
 // heal: from_changes takes the slots computeBondChanges flagged (change word bit 0), else the
 // D5 rule (lowest slot with an active partner and a failed rest-length test).  prune: positions
 // are those of the last sort, so window cells may be skipped by their geometric box
+// hcount / hlist: the density pass's record of each particle's neighbours within h, taken
+// instead of a new search (null: search)
 void launch_remodel(const DevParams& P, const DevGenome* G, const Carried& cur, const Cold& cold,
-                    const Scratch& s, bool from_changes, bool prune, cudaStream_t st);
+                    const Scratch& s, bool from_changes, bool prune, const uint32_t* hcount,
+                    const uint32_t* hlist, cudaStream_t st);
 // special: externalActuation / fixedParticles for genes 12 / 11 (SpecialParticlesCL)
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_breaks,
                     cudaStream_t st, bool special = false);

@@ -380,7 +380,7 @@ __device__ __forceinline__ void dens_list_finish(
     float sum = 0.f;
     {
         float part = 0.f;
-        uint32_t nf = 0;
+        uint32_t nf = 0, nh = 0;
         for (uint32_t k = 0; k < n; k++) {
             const uint32_t e = my[k * 32];
             const uint32_t q = e & ~LIST_CELL_START;
@@ -400,10 +400,12 @@ __device__ __forceinline__ void dens_list_finish(
                 conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2,
                                              P.uniform_diff != 0, true);
                 mcnt++;
+                if (X.hlist) X.hlist[(size_t)nh++ * P.cap + p] = q;  // nh <= n <= NL_CAP
             }
         }
         if (F::DENS) sum += part;
         fcount[p] = nf;  // > FL_CAP: the force pass searches again
+        if (X.hlist) X.hcount[p] = nh;
     }
     dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press, invdens, X);
 }
@@ -552,6 +554,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     if (n > (uint32_t)NL_CAP) {
         // more neighbours than the list holds (dense clumps): the overflow pass takes it
         ovf[atomicAdd(ovf_count, 1u)] = p;
+        if (X.hlist) X.hcount[p] = UNDEF;
         return;
     }
     dens_list_finish<FLAGS>(P, G, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,
@@ -654,6 +657,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_fi
     }
     if (n > (uint32_t)NL_CAP) {
         ovf[atomicAdd(ovf_count, 1u)] = p;
+        if (X.hlist) X.hcount[p] = UNDEF;
         return;
     }
     dens_list_finish<FLAGS>(P, G, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,

@@ -254,8 +254,9 @@ __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
     const uint32_t* __restrict__ scell, const uint32_t* __restrict__ count,
     const uint32_t* __restrict__ offset, const uint8_t* __restrict__ freemask,
     const uint32_t* __restrict__ nactive_p, const uint32_t* __restrict__ change, bool from_changes,
-    const uint32_t* __restrict__ work, bool prune, uint32_t* __restrict__ prop,
-    float* __restrict__ propd, uint32_t* __restrict__ prop_cnt, uint32_t* __restrict__ prop_list) {
+    const uint32_t* __restrict__ work, bool prune, const uint32_t* __restrict__ hcount,
+    const uint32_t* __restrict__ hlist, uint32_t* __restrict__ prop, float* __restrict__ propd,
+    uint32_t* __restrict__ prop_cnt, uint32_t* __restrict__ prop_list) {
     __shared__ float4 s_sp[PROPOSE_WARPS][32];
     __shared__ uint32_t s_sq[PROPOSE_WARPS][32];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
@@ -268,21 +269,43 @@ __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
         prop[i] = UNDEF;
         propd[i] = 0.f;
     }
-    const bool need = act && heal_slot(bond, cap, i, n, origin, change, from_changes) >= 0;
-    if (!__any_sync(0xffffffffu, need)) return;
+    const bool wants = act && heal_slot(bond, cap, i, n, origin, change, from_changes) >= 0;
+    if (!__any_sync(0xffffffffu, wants)) return;
     uint32_t partners[NB];
 #pragma unroll
-    for (int a = 0; a < NB; a++) partners[a] = need ? bond_a(bond, cap, i, a).x : UNDEF;
+    for (int a = 0; a < NB; a++) partners[a] = wants ? bond_a(bond, cap, i, a).x : UNDEF;
     const float INF = __int_as_float(0x7f800000);
-    const float4 ip = need ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 ip = wants ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float best = 0.f;
+    uint32_t bj = UNDEF;
+    // a particle whose neighbours within h the density pass recorded takes them from there
+    const uint32_t nh = wants && hcount ? hcount[i] : UNDEF;
+    const bool need = wants && nh == UNDEF;
+    if (wants && nh != UNDEF) {
+        for (uint32_t t = 0; t < nh; t++) {
+            const uint32_t j = hlist[(size_t)t * cap + i];
+            const float4 jp = pos[j];
+            const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+            const float dsq = dx * dx + dy * dy + dz * dz;
+            if (!(dsq < P.r2diff && dsq > 0.f)) continue;
+            if (bj != UNDEF && (dsq > best || (dsq == best && j > bj))) continue;
+            if (freemask[j] == 0) continue;
+            bool bonded = false;
+#pragma unroll
+            for (int a = 0; a < NB; a++) bonded |= partners[a] == j;
+            if (bonded) continue;
+            const uint32_t o = origin[j];
+            if (o == UNDEF || pid_cold[o] == 0u) continue;  // boundary markers
+            best = dsq;
+            bj = j;
+        }
+    }
     const uint32_t pcell = need ? scell[i] : 0u;
     const CellWin win = window_of(P, pcell);
     const float Rf = sqrtf(P.r2diff) * 1.0001f + 1e-3f;
     const int g = P.gsrch;
     const int BIG = 1 << 30;
     const uint32_t rowx = (uint32_t)P.res[0];
-    float best = 0.f;
-    uint32_t bj = UNDEF;
     unsigned remaining = __ballot_sync(0xffffffffu, need);
     while (remaining) {
         const int leader = __ffs(remaining) - 1;
@@ -359,7 +382,7 @@ __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
             }
         }
     }
-    if (need) {
+    if (wants) {
         prop[i] = bj;
         propd[i] = best;
         if (bj != UNDEF) {
@@ -447,15 +470,16 @@ __global__ void __launch_bounds__(256) k_accept(DevParams P, const DevGenome* __
 }  // namespace
 
 void launch_remodel(const DevParams& P, const DevGenome* G, const Carried& cur, const Cold& cold,
-                    const Scratch& s, bool from_changes, bool prune, cudaStream_t st) {
+                    const Scratch& s, bool from_changes, bool prune, const uint32_t* hcount,
+                    const uint32_t* hlist, cudaStream_t st) {
     const uint32_t blocks = (P.cap + 255) / 256;
     k_free_slots<<<blocks, 256, 0, st>>>(P.cap, cur.bond, cur.pidx, s.counters + 3, s.freemask);
     cudaMemsetAsync(s.prop_cnt, 0, sizeof(uint32_t) * P.cap, st);
     const uint32_t wblocks = (P.cap + PROPOSE_WARPS * 32 - 1) / (PROPOSE_WARPS * 32);
     k_propose_warp<<<wblocks, PROPOSE_WARPS * 32, 0, st>>>(
         P, cur.pos, cur.bond, cur.origin, cold.pid, s.scell, s.count, s.offset, s.freemask,
-        s.counters + 3, cold.change, from_changes, s.work, prune, s.prop, s.propd, s.prop_cnt,
-        s.prop_list);
+        s.counters + 3, cold.change, from_changes, s.work, prune, hcount, hlist, s.prop, s.propd,
+        s.prop_cnt, s.prop_list);
     k_accept<<<blocks, 256, 0, st>>>(P, G, cur.bond, cur.pidx, cur.origin, cold.pid, cold.change,
                                      s.scell, s.count, s.offset, s.freemask, s.prop, s.propd,
                                      s.counters + 3, from_changes, s.prop_cnt, s.prop_list);
