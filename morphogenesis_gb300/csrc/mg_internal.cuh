@@ -181,8 +181,9 @@ struct DensExtra {
     uint32_t* epi;             // full epigenetic state of the current set ([16][cap]) or null
     const uint32_t* step;      // JUDGE: device step counter
     uint32_t judge_period, judge_stride;
-    // re-forming candidates: the neighbours within h of each particle, in canonical order
-    // ([NL_CAP][cap]), with their number (0xFFFFFFFF: not recorded, the particle overflowed)
+    // re-forming candidates: the neighbours within h of each particle, in canonical order,
+    // indexed by the particle's position in the processing order ([NL_CAP][cap]), with their
+    // number (0xFFFFFFFF: not recorded, the particle overflowed)
     uint32_t* hlist;
     uint32_t* hcount;
 };

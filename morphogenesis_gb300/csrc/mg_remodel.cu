@@ -220,11 +220,18 @@ __global__ void __launch_bounds__(256) k_change_lists(uint32_t cap, uint32_t cel
 
 __global__ void __launch_bounds__(256) k_free_slots(uint32_t cap, const uint4* __restrict__ bond,
                                                     const uint32_t* __restrict__ pidx,
+                                                    const uint32_t* __restrict__ origin,
+                                                    const uint32_t* __restrict__ pid_cold,
                                                     const uint32_t* __restrict__ nactive_p,
                                                     uint8_t* __restrict__ freemask) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = *nactive_p;
     if (j >= n) return;
+    const uint32_t o = origin[j];
+    if (o == UNDEF || pid_cold[o] == 0u) {  // boundary markers (particle id 0) take no bond
+        freemask[j] = 0;
+        return;
+    }
     uint32_t m = 0;
 #pragma unroll
     for (int s = 0; s < NB; s++) {
@@ -279,23 +286,21 @@ __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
     float best = 0.f;
     uint32_t bj = UNDEF;
     // a particle whose neighbours within h the density pass recorded takes them from there
-    const uint32_t nh = wants && hcount ? hcount[i] : UNDEF;
+    const uint32_t nh = wants && hcount ? hcount[k] : UNDEF;
     const bool need = wants && nh == UNDEF;
     if (wants && nh != UNDEF) {
         for (uint32_t t = 0; t < nh; t++) {
-            const uint32_t j = hlist[(size_t)t * cap + i];
+            const uint32_t j = hlist[(size_t)t * cap + k];
             const float4 jp = pos[j];
             const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
             const float dsq = dx * dx + dy * dy + dz * dz;
             if (!(dsq < P.r2diff && dsq > 0.f)) continue;
             if (bj != UNDEF && (dsq > best || (dsq == best && j > bj))) continue;
-            if (freemask[j] == 0) continue;
+            if (freemask[j] == 0) continue;  // no free incoming slot, or a boundary marker
             bool bonded = false;
 #pragma unroll
             for (int a = 0; a < NB; a++) bonded |= partners[a] == j;
             if (bonded) continue;
-            const uint32_t o = origin[j];
-            if (o == UNDEF || pid_cold[o] == 0u) continue;  // boundary markers
             best = dsq;
             bj = j;
         }
@@ -366,13 +371,11 @@ __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
                             if (!(dsq < P.r2diff && dsq > 0.f)) continue;
                             const uint32_t j = s_sq[w][tt];
                             if (bj != UNDEF && (dsq > best || (dsq == best && j > bj))) continue;
-                            if (freemask[j] == 0) continue;
+                            if (freemask[j] == 0) continue;  // no free slot, or a boundary marker
                             bool bonded = false;
 #pragma unroll
                             for (int a = 0; a < NB; a++) bonded |= partners[a] == j;
                             if (bonded) continue;
-                            const uint32_t o = origin[j];
-                            if (o == UNDEF || pid_cold[o] == 0u) continue;  // boundary markers
                             best = dsq;
                             bj = j;
                         }
@@ -473,7 +476,8 @@ void launch_remodel(const DevParams& P, const DevGenome* G, const Carried& cur, 
                     const Scratch& s, bool from_changes, bool prune, const uint32_t* hcount,
                     const uint32_t* hlist, cudaStream_t st) {
     const uint32_t blocks = (P.cap + 255) / 256;
-    k_free_slots<<<blocks, 256, 0, st>>>(P.cap, cur.bond, cur.pidx, s.counters + 3, s.freemask);
+    k_free_slots<<<blocks, 256, 0, st>>>(P.cap, cur.bond, cur.pidx, cur.origin, cold.pid, s.counters + 3,
+                                         s.freemask);
     cudaMemsetAsync(s.prop_cnt, 0, sizeof(uint32_t) * P.cap, st);
     const uint32_t wblocks = (P.cap + PROPOSE_WARPS * 32 - 1) / (PROPOSE_WARPS * 32);
     k_propose_warp<<<wblocks, PROPOSE_WARPS * 32, 0, st>>>(
