@@ -369,8 +369,8 @@ __device__ __forceinline__ void dens_list_finish(
     const uint32_t* my, const float4* __restrict__ pos, const float* __restrict__ conc_in,
     float* __restrict__ conc_out, const uint32_t* __restrict__ genes, float* __restrict__ press,
     float* __restrict__ invdens, uint32_t* __restrict__ flist, uint32_t* __restrict__ fcount,
-    const DensExtra& X, uint32_t k) {
-    // k: the particle's position in the processing order (where its re-forming candidates go)
+    const DensExtra& X, uint32_t slot) {
+    // slot: the particle's position in the processing order (where its re-forming candidates go)
     using F = DF<FLAGS>;
     float cur[NTF], dif[NTF], nc[NTF], ms[NTF];
     load_conc<FLAGS>(G, conc_in, p, cur, dif);
@@ -401,12 +401,12 @@ __device__ __forceinline__ void dens_list_finish(
                 conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2,
                                              P.uniform_diff != 0, true);
                 mcnt++;
-                if (X.hlist) X.hlist[(size_t)nh++ * P.cap + k] = q;  // nh <= n <= NL_CAP
+                if (X.hlist) X.hlist[(size_t)nh++ * P.cap + slot] = q;  // nh <= n <= NL_CAP
             }
         }
         if (F::DENS) sum += part;
         fcount[p] = nf;  // > FL_CAP: the force pass searches again
-        if (X.hlist) X.hcount[k] = nh;
+        if (X.hlist) X.hcount[slot] = nh;
     }
     dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press, invdens, X);
 }
