@@ -18,6 +18,9 @@
 #include "mg_internal.cuh"
 #include "mg_mlp.cuh"
 
+#ifndef MG_BATCH_GROUP
+#define MG_BATCH_GROUP 32
+#endif
 #ifndef MG_SUB_MIRROR
 #define MG_SUB_MIRROR 1
 #endif
@@ -1962,7 +1965,25 @@ static mg_status batch_graph(mg_batch b, uint32_t flags, cudaGraphExec_t* out) {
     }
     cudaGraph_t bg = nullptr;
     MG_CUDA(nullptr, cudaGraphCreate(&bg, 0));
+    // Members run in groups of MG_BATCH_GROUP (32): a group's steps are independent branches, and an
+    // empty node joins each group before the next starts.  One flat level of hundreds of
+    // branches schedules far worse than a few levels of tens (measured: 256 members of 1,000
+    // particles take 11x the time of 64; groups of 32 were fastest among 16-256).
+    cudaGraphNode_t join = nullptr;
+    std::vector<cudaGraphNode_t> group;
+    size_t m = 0;
     for (mg_system* h : b->hs) {
+        if (group.size() == (size_t)MG_BATCH_GROUP) {
+            cudaGraphNode_t j = nullptr;
+            cudaError_t e = cudaGraphAddEmptyNode(&j, bg, group.data(), group.size());
+            if (e != cudaSuccess) {
+                cudaGraphDestroy(bg);
+                return cuda_fail(nullptr, e, "batch group join");
+            }
+            join = j;
+            group.clear();
+        }
+        m++;
         DevParams saved = h->P;
         if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
         cudaGraph_t g = nullptr;
@@ -1974,7 +1995,8 @@ static mg_status batch_graph(mg_batch b, uint32_t flags, cudaGraphExec_t* out) {
         }
         h->P = saved;
         cudaGraphNode_t node;
-        if (e == cudaSuccess) e = cudaGraphAddChildGraphNode(&node, bg, nullptr, 0, g);
+        if (e == cudaSuccess) e = cudaGraphAddChildGraphNode(&node, bg, join ? &join : nullptr, join ? 1 : 0, g);
+        if (e == cudaSuccess) group.push_back(node);
         if (g) cudaGraphDestroy(g);
         if (e != cudaSuccess) {
             cudaGraphDestroy(bg);
