@@ -365,8 +365,9 @@ def batch_section(args):
            "batched_particle_steps_s": total * args.batch_steps / (ms_batch / 1e3),
            "sequential_particle_steps_s": total * args.batch_steps / (ms_seq / 1e3),
            "speedup": ms_seq / ms_batch, "setup_s": build_s,
-           "design": "one CUDA graph launch per step holding every instance's step graph as an "
-                     "independent branch (instances keep their own arenas, grids and genomes)"}
+           "design": "one CUDA graph launch per step holding every instance's step graph, in "
+                     "groups of 32 independent branches joined before the next group (instances "
+                     "keep their own arenas, grids and genomes)"}
     b.close()
     for fs in members:
         fs.close()
