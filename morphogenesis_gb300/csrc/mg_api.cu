@@ -382,11 +382,20 @@ void enqueue_insert_rank(mg_system* h, bool prof) {
     { Mark m(h, prof, "cellsort"); launch_cellsort(P, h->s, h->num_sms, h->search == 2, st); }
 }
 
-void enqueue_gather(mg_system* h, bool prof) {
+// conc_ready: the concentrations arrive later (an upload still in flight); everything else is
+// moved first and the concentrations after the stream has waited for that event.
+void enqueue_gather(mg_system* h, bool prof, cudaEvent_t conc_ready = nullptr) {
     int src = h->cur, dst = 1 - h->cur;
     int csrc = h->conc_cur, cdst = 1 - h->conc_cur;
     { Mark m(h, prof, "gather");
-      launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream); }
+      if (conc_ready) {
+          launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream, 1);
+          cudaStreamWaitEvent(h->stream, conc_ready, 0);
+          launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream, 2);
+      } else {
+          launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream);
+      }
+    }
     h->cur = dst;
     h->conc_cur = cdst;
     h->flist_valid = false;
@@ -441,7 +450,8 @@ void* direct_buffer(mg_system* h, int32_t id, bool upload) {
 // One step in the legacy Run() order (fluid_system.cpp:1179-1349), one sort per step.
 // With an exchange plan (captured into the step's graph): FPOS is uploaded first on a side
 // stream and the bin / scan / sort kernels start when it has arrived, while the other uploads
-// continue on a second side stream that the gather waits for; FCONC is downloaded on a side
+// continue on a second side stream that the gather waits for (the concentrations, uploaded
+// last, are moved by a second gather kernel once they have arrived); FCONC is downloaded on a side
 // stream as soon as the morphogen stage has written it, under the force and integration
 // kernels; the other downloads follow the step, and the step ends when every copy has.
 // Whether a step with these flags takes its re-forming candidates from the density pass: the
@@ -494,20 +504,30 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
     cudaStream_t A = io ? h->io_st[0] : nullptr, B = io ? h->io_st[1] : nullptr;
     cudaEvent_t* ev = h->io_ev;
     const bool up = io && io->nin;
+    bool conc_up = false;
     if (up) {
         cudaEventRecord(ev[0], st);
         cudaStreamWaitEvent(A, ev[0], 0);
         cudaStreamWaitEvent(B, ev[0], 0);
+        // FPOS on A; the others on B, FCONC (the largest) last
         for (uint32_t k = 0; k < io->nin; k++)
-            cudaMemcpyAsync(direct_buffer(h, io->in[k].buf_id, true), io->in[k].host, io->in[k].bytes,
-                            cudaMemcpyHostToDevice, io->in[k].buf_id == MG_FPOS ? A : B);
+            if (io->in[k].buf_id != MG_FCONC)
+                cudaMemcpyAsync(direct_buffer(h, io->in[k].buf_id, true), io->in[k].host, io->in[k].bytes,
+                                cudaMemcpyHostToDevice, io->in[k].buf_id == MG_FPOS ? A : B);
         cudaEventRecord(ev[1], A);
         cudaEventRecord(ev[2], B);
+        for (uint32_t k = 0; k < io->nin; k++)
+            if (io->in[k].buf_id == MG_FCONC) {
+                cudaMemcpyAsync(direct_buffer(h, MG_FCONC, true), io->in[k].host, io->in[k].bytes,
+                                cudaMemcpyHostToDevice, B);
+                conc_up = true;
+            }
+        if (conc_up) cudaEventRecord(ev[5], B);
         cudaStreamWaitEvent(st, ev[1], 0);
     }
     enqueue_insert_rank(h, prof);
     if (up) cudaStreamWaitEvent(st, ev[2], 0);
-    enqueue_gather(h, prof);
+    enqueue_gather(h, prof, conc_up ? ev[5] : nullptr);
     const bool remodel = (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) != 0;
     const bool heal_list = heal_from_density(h, flags);
     if (flags & MG_STEP_SURROGATE) {
@@ -1270,6 +1290,8 @@ mg_status mg_step_io(mg_handle h, const mg_io* in, uint32_t nin, uint32_t nsteps
             MG_CUDA(h, cudaGraphLaunch(ge, h->stream));
         }
         after_steps(h, nsteps, flags);
+        for (uint32_t k = 0; k < nin; k++)
+            if (in[k].buf_id == MG_FCONC) h->launches += 1;  // the first step's gather in two parts
         return check_device(h);
     }
     for (uint32_t k = 0; k < nin; k++) {

@@ -347,11 +347,25 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
                                                 float* __restrict__ press,
                                                 float* __restrict__ invdens,
                                                 float4* __restrict__ force,
-                                                const uint32_t* __restrict__ nactive_p) {
+                                                const uint32_t* __restrict__ nactive_p,
+                                                int part) {
+    // part: 0 everything, 1 everything but the concentrations, 2 the concentrations only
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t cap = P.cap;
     if (p >= cap) return;
     const uint32_t nact = *nactive_p;
+    if (part == 2) {
+        float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
+        if (p < nact) {
+            const float4* ci = reinterpret_cast<const float4*>(sconc + (size_t)sorted[p] * NTF);
+#pragma unroll
+            for (int k = 0; k < 4; k++) co[k] = __ldg(ci + k);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) co[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        return;
+    }
     if (p < nact) {
         const uint32_t i = sorted[p];
         D.pos[p] = __ldg(S.pos + i);
@@ -375,10 +389,12 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
             v.z = remap(v.z, cap, newidx);
             po[k] = v;
         }
-        const float4* ci = reinterpret_cast<const float4*>(sconc + (size_t)i * NTF);
-        float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
+        if (part == 0) {
+            const float4* ci = reinterpret_cast<const float4*>(sconc + (size_t)i * NTF);
+            float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
 #pragma unroll
-        for (int k = 0; k < 4; k++) co[k] = __ldg(ci + k);
+            for (int k = 0; k < 4; k++) co[k] = __ldg(ci + k);
+        }
         if (P.full_epi) {
             // per-gene words move with the particle; the bits (dense-list membership at sort
             // time, FEPIGEN > 0) are taken from them
@@ -409,9 +425,11 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
         uint4* po = reinterpret_cast<uint4*>(D.pidx + (size_t)p * 12);
 #pragma unroll
         for (int k = 0; k < 3; k++) po[k] = make_uint4(NO_PARTNER, NO_PARTNER, NO_PARTNER, NO_PARTNER);
-        float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
+        if (part == 0) {
+            float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
 #pragma unroll
-        for (int k = 0; k < 4; k++) co[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int k = 0; k < 4; k++) co[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         D.genes[p] = 0u;
         if (P.full_epi)
             for (int g = 0; g < NG; g++) D.epi[(size_t)g * cap + p] = 0u;
@@ -424,10 +442,11 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
 }
 
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
-                   const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st) {
+                   const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st,
+                   int part) {
     uint32_t blocks = (P.cap + 255) / 256;
     k_gather<<<blocks, 256, 0, st>>>(P, src, src_conc, dst, dst_conc, s.sorted, s.newidx, s.cell,
-                                      s.scell, s.press, s.invdens, s.force, s.counters + 3);
+                                      s.scell, s.press, s.invdens, s.force, s.counters + 3, part);
 }
 
 }  // namespace mg
