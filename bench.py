@@ -415,7 +415,7 @@ def main():
     fs.TransferToCL(d.arrays)
     flags = A.STEP_DEFAULT
     fs.Run(max(args.warmup, 3), flags)
-    tune = fs.autotune(5, flags)  # launch shape of the density pass, state restored afterwards
+    tune = fs.autotune(20, flags)  # launch shape of the density pass, state restored afterwards
     n = d.n
     cells = int(d.params.grid_total)
 

@@ -328,7 +328,8 @@ mg_status mg_set_option(mg_handle h, int32_t option, int32_t value);
 mg_status mg_get_tuning(mg_handle h, int32_t choice[4]);
 mg_status mg_set_tuning(mg_handle h, const int32_t choice[4]);
 /* Times every launch shape over `steps` plain steps (flags: physics/genes only) on the
- * handle's current state, restoring the state after each trial, and keeps the fastest.
+ * handle's current state, restoring the state after each trial, and keeps the fastest (the
+ * default shape unless another is more than 3% faster).
  * Needs a free device allocation the size of the handle's arena for the snapshot. */
 mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t choice[4],
                       float* ms_per_step);
