@@ -427,6 +427,28 @@ def test_drifted_positions_between_sorts(built):
     o.close()
 
 
+def test_time_and_zero_vel(built, cfg0):
+    """m_Time advances by dt per integrating step (AdvanceTime) and is kept across SetParam;
+    ZeroVelCL clears the velocities of every particle."""
+    import morphogenesis_gb300 as mg
+
+    fs = mg.FluidSystem(cfg0.params, cfg0.genome, cfg0.n)
+    o = orc.Oracle(cfg0.params, cfg0.genome, cfg0.n)
+    fs.TransferToCL(cfg0.arrays)
+    o.upload_all(cfg0.arrays)
+    fs.Run(5)
+    o.step(5)
+    assert fs.time() == o.time()
+    fs.SetParam(A.PFREEZE, 1.0)
+    assert fs.time() == o.time(), "SetParam must not rewind m_Time"
+    fs.Run(1, A.STEP_GENES)  # no integration: time unchanged
+    assert fs.time() == o.time()
+    fs.ZeroVelCL()
+    assert not fs.download(A.FVEL).any() and not fs.download(A.FVEVAL).any()
+    fs.close()
+    o.close()
+
+
 def test_launch_shapes_give_identical_results(built):
     d = demo.make_block((24, 12, 24), "R", seed=6)
     import morphogenesis_gb300 as mg
