@@ -20,6 +20,10 @@
 #include <cfloat>
 #include "mg_internal.cuh"
 
+#ifndef MG_SUB_ORDER
+#define MG_SUB_ORDER 1  // in-cell processing order: 1 x-major slabs, 0 mirrored Morton
+#endif
+
 namespace mg {
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -41,22 +45,29 @@ __device__ __forceinline__ uint32_t cell_of(const DevParams& P, float4 p) {
 // Morton code of the sub-cell holding a position inside its cell: 2^sub_bits sub-cells per axis
 // (sub_bits 1 or 2) from the fractional part of the cell coordinate.  Only the density pass's
 // processing order uses it, never a result.
-// With `mirror`, cells with an odd x index take their y and z sub-cell coordinates mirrored:
-// cells are ordered along x, and the last sub-cells of one cell (high y, z) then meet the first
-// sub-cells of the next one (also high y, z, now at its low-x side), so a warp that takes the
-// tail of one cell and the head of the next still covers a compact region.
+// With `mirror` (the order for the warp-cooperative searches), the code sorts x first: the
+// cells are ordered along x, so a warp that takes the tail of one cell and the head of the next
+// covers a thin slab on both sides of their shared face, and a warp inside one cell a slab as
+// compact as a Morton half-cell (MG_SUB_ORDER 0 keeps Morton codes with the y and z
+// coordinates mirrored in odd-x cells).  Without it, Morton codes (bit a = level-0 half of axis
+// a, bit 3 + a = level-1), which the per-lane fine-cell search reads as positions.
 __device__ __forceinline__ uint32_t sub_of(const DevParams& P, float4 p, bool mirror) {
     const float g[3] = {(p.x - P.gmin[0]) * P.gdelta[0], (p.y - P.gmin[1]) * P.gdelta[1],
                         (p.z - P.gmin[2]) * P.gdelta[2]};
     const int nsub = 1 << P.sub_bits;
+    int q[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int v = (int)((g[a] - floorf(g[a])) * (float)nsub);
+        q[a] = v < 0 ? 0 : (v > nsub - 1 ? nsub - 1 : v);
+    }
+    if (mirror && MG_SUB_ORDER == 1) return (uint32_t)((q[0] * nsub + q[1]) * nsub + q[2]);
     const bool flip = mirror && (((int)floorf(g[0])) & 1);
     uint32_t code = 0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        int q = (int)((g[a] - floorf(g[a])) * (float)nsub);
-        q = q < 0 ? 0 : (q > nsub - 1 ? nsub - 1 : q);
-        if (flip && a > 0) q = nsub - 1 - q;
-        code |= ((uint32_t)(q & 1) << a) | ((uint32_t)((q >> 1) & 1) << (3 + a));
+        const int qa = (flip && a > 0) ? nsub - 1 - q[a] : q[a];
+        code |= ((uint32_t)(qa & 1) << a) | ((uint32_t)((qa >> 1) & 1) << (3 + a));
     }
     return P.sub_bits == 1 ? code & 7u : code;
 }
