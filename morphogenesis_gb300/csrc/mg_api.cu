@@ -21,9 +21,6 @@
 #ifndef MG_BATCH_GROUP
 #define MG_BATCH_GROUP 32
 #endif
-#ifndef MG_SUB_MIRROR
-#define MG_SUB_MIRROR 1
-#endif
 
 using namespace mg;
 
@@ -375,7 +372,7 @@ void enqueue_insert_rank(mg_system* h, bool prof) {
     cudaMemsetAsync(h->s.count, 0, sizeof(uint32_t) * P.cells, st);
     cudaMemsetAsync(h->s.scan_status, 0, sizeof(unsigned long long) * scan_status_words(P.cells), st);
     cudaMemsetAsync(h->s.counters, 0, 2 * sizeof(uint32_t), st);
-    { Mark m(h, prof, "insert"); launch_insert(P, h->set[h->cur], h->s, h->search != 2 && MG_SUB_MIRROR, st); }
+    { Mark m(h, prof, "insert"); launch_insert(P, h->set[h->cur], h->s, h->search != 2, st); }
     { Mark m(h, prof, "scan"); launch_scan(h->s.count, h->s.offset, P.cells, h->s.scan_status,
                                            h->s.counters, h->s.counters + 3, h->s.counters + 2, st); }
     { Mark m(h, prof, "place"); launch_place(P, h->s, st); }

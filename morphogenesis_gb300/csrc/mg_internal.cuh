@@ -149,9 +149,9 @@ struct Scratch {
 
 // ---- launchers (all on one stream; no host synchronisation inside) ----------------------
 cudaError_t physics_init();  // per-kernel attributes, once per device before the first launch
-// mirror: the processing order's sub-cell codes mirrored in y and z in odd-x cells (not for
-// the per-lane fine-cell search, which reads the codes as positions)
-void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, bool mirror,
+// warp_order: sub-cell codes ordered for the warp-cooperative searches (x-first slabs); false
+// gives the Morton codes the per-lane fine-cell search reads as positions
+void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, bool warp_order,
                    cudaStream_t st);
 void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long long* status,
                  uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st);

@@ -45,13 +45,13 @@ __device__ __forceinline__ uint32_t cell_of(const DevParams& P, float4 p) {
 // Morton code of the sub-cell holding a position inside its cell: 2^sub_bits sub-cells per axis
 // (sub_bits 1 or 2) from the fractional part of the cell coordinate.  Only the density pass's
 // processing order uses it, never a result.
-// With `mirror` (the order for the warp-cooperative searches), the code sorts x first: the
+// With `warp_order` (the order for the warp-cooperative searches), the code sorts x first: the
 // cells are ordered along x, so a warp that takes the tail of one cell and the head of the next
 // covers a thin slab on both sides of their shared face, and a warp inside one cell a slab as
 // compact as a Morton half-cell (MG_SUB_ORDER 0 keeps Morton codes with the y and z
 // coordinates mirrored in odd-x cells).  Without it, Morton codes (bit a = level-0 half of axis
 // a, bit 3 + a = level-1), which the per-lane fine-cell search reads as positions.
-__device__ __forceinline__ uint32_t sub_of(const DevParams& P, float4 p, bool mirror) {
+__device__ __forceinline__ uint32_t sub_of(const DevParams& P, float4 p, bool warp_order) {
     const float g[3] = {(p.x - P.gmin[0]) * P.gdelta[0], (p.y - P.gmin[1]) * P.gdelta[1],
                         (p.z - P.gmin[2]) * P.gdelta[2]};
     const int nsub = 1 << P.sub_bits;
@@ -61,8 +61,8 @@ __device__ __forceinline__ uint32_t sub_of(const DevParams& P, float4 p, bool mi
         const int v = (int)((g[a] - floorf(g[a])) * (float)nsub);
         q[a] = v < 0 ? 0 : (v > nsub - 1 ? nsub - 1 : v);
     }
-    if (mirror && MG_SUB_ORDER == 1) return (uint32_t)((q[0] * nsub + q[1]) * nsub + q[2]);
-    const bool flip = mirror && (((int)floorf(g[0])) & 1);
+    if (warp_order && MG_SUB_ORDER == 1) return (uint32_t)((q[0] * nsub + q[1]) * nsub + q[2]);
+    const bool flip = warp_order && (((int)floorf(g[0])) & 1);
     uint32_t code = 0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
                                                 uint32_t* __restrict__ newidx,
                                                 uint32_t* __restrict__ count,
                                                 uint8_t* __restrict__ sub,
-                                                uint32_t* __restrict__ step, bool mirror) {
+                                                uint32_t* __restrict__ step, bool warp_order) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) *step += 1u;  // step counter read by the later kernels of this step
     bool in = i < P.cap;
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
         c = cell_of(P, pi);
         cell[i] = c;
         newidx[i] = UNDEF;  // overwritten by the cell sort for particles inside the window
-        if (c != UNDEF) sub[i] = (uint8_t)sub_of(P, pi, mirror);
+        if (c != UNDEF) sub[i] = (uint8_t)sub_of(P, pi, warp_order);
     }
     bool valid = in && c != UNDEF;
     unsigned active = __ballot_sync(0xffffffffu, valid);
@@ -104,11 +104,11 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
     }
 }
 
-void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, bool mirror,
+void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, bool warp_order,
                    cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
     k_insert<<<blocks, 256, 0, st>>>(P, cur.pos, s.cell, s.arank, s.newidx, s.count, s.sub,
-                                      s.counters + 5, mirror);
+                                      s.counters + 5, warp_order);
 }
 
 // ---- single-pass scan (decoupled look-back) ------------------------------------------------
