@@ -467,9 +467,10 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
         const bool ing = act && ((remaining >> lane) & 1u) && pcell >= lcell && pcell - lcell <= span &&
                          pcell / rowx == lcell / rowx;
         remaining &= ~__ballot_sync(0xffffffffu, ing);
-        const float bx0 = warp_min(ing ? ip.x : INF) - Rf, bx1 = warp_max(ing ? ip.x : -INF) + Rf;
-        const float by0 = warp_min(ing ? ip.y : INF) - Rf, by1 = warp_max(ing ? ip.y : -INF) + Rf;
-        const float bz0 = warp_min(ing ? ip.z : INF) - Rf, bz1 = warp_max(ing ? ip.z : -INF) + Rf;
+        // the group's particles span [t?0, t?1]; the search box is that span widened by Rf
+        const float tx0 = warp_min(ing ? ip.x : INF), tx1 = warp_max(ing ? ip.x : -INF);
+        const float ty0 = warp_min(ing ? ip.y : INF), ty1 = warp_max(ing ? ip.y : -INF);
+        const float tz0 = warp_min(ing ? ip.z : INF), tz1 = warp_max(ing ? ip.z : -INF);
         const int wx0 = warp_mini(ing ? win.x : BIG), wx1 = warp_maxi(ing ? win.x : -BIG) + g - 1;
         const int wy0 = warp_mini(ing ? win.y : BIG), wy1 = warp_maxi(ing ? win.y : -BIG) + g - 1;
         const int wz0 = warp_mini(ing ? win.z : BIG), wz1 = warp_maxi(ing ? win.z : -BIG) + g - 1;
@@ -483,7 +484,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
             uint32_t tcnt = 0, toff = 0;
             if (t < ncell) {
                 const int cx = wx0 + t % ncx, cz = wz0 + (t / ncx) % ncz, cy = wy0 + t / (ncx * ncz);
-                if (!prune || cell_meets_box(P, cx, cy, cz, bx0, bx1, by0, by1, bz0, bz1)) {
+                if (!prune || cell_meets_box(P, cx, cy, cz, tx0 - Rf, tx1 + Rf, ty0 - Rf, ty1 + Rf, tz0 - Rf, tz1 + Rf)) {
                     const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
                     tcnt = count[cell];
                     if (tcnt) toff = offset[cell];
@@ -505,10 +506,12 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                     const uint32_t kk = base + lane;
                     const bool valid = kk < cnt;
                     const float4 qp = valid ? pos[off + kk] : make_float4(INF, INF, INF, 0.f);
-                    const float ex = fmaxf(0.f, fmaxf(bx0 - qp.x, qp.x - bx1));
-                    const float ey = fmaxf(0.f, fmaxf(by0 - qp.y, qp.y - by1));
-                    const float ez = fmaxf(0.f, fmaxf(bz0 - qp.z, qp.z - bz1));
-                    const bool surv = valid && (ex == 0.f && ey == 0.f && ez == 0.f);
+                    // survivors: candidates within Rf of the span (the span's box with rounded
+                    // edges and corners); every lane's neighbour is one, as the lane lies in it
+                    const float ex = fmaxf(0.f, fmaxf(tx0 - qp.x, qp.x - tx1));
+                    const float ey = fmaxf(0.f, fmaxf(ty0 - qp.y, qp.y - ty1));
+                    const float ez = fmaxf(0.f, fmaxf(tz0 - qp.z, qp.z - tz1));
+                    const bool surv = valid && ex * ex + ey * ey + ez * ez <= Rf * Rf;
                     const unsigned ball = __ballot_sync(0xffffffffu, surv);
                     if (surv) {
                         const uint32_t slot = (uint32_t)__popc(ball & ((1u << lane) - 1u));
