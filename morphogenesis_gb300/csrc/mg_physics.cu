@@ -56,6 +56,47 @@ __device__ __forceinline__ float wendland_term(float dsq, float sr) {
     return b * (4.f * qq + 1.f);
 }
 
+#ifndef MG_ROW_V8
+#define MG_ROW_V8 1
+#endif
+// A particle's 16 concentrations as two 256-bit loads: a gather of rows from 32 lanes then
+// costs the L1 two accesses per row instead of four.  Rows are 64 bytes in buffers aligned to
+// 256 bytes, so both halves are 32-byte aligned.
+__device__ __forceinline__ void load_row16(const float* row, float (&v)[NTF]) {
+    static_assert(NTF == 16, "rows of 16 concentrations");
+#if MG_ROW_V8
+    asm("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(row));
+    asm("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8+32];"
+        : "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15])
+        : "l"(row));
+#else
+    const float4* r4 = reinterpret_cast<const float4*>(row);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float4 x = r4[k];
+        v[4 * k] = x.x; v[4 * k + 1] = x.y; v[4 * k + 2] = x.z; v[4 * k + 3] = x.w;
+    }
+#endif
+}
+
+// ... and stored as two 256-bit stores
+__device__ __forceinline__ void store_row16(float* row, const float (&v)[NTF]) {
+#if MG_ROW_V8
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+                 :: "l"(row), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+                 : "memory");
+    asm volatile("st.global.v8.f32 [%0+32], {%1, %2, %3, %4, %5, %6, %7, %8};"
+                 :: "l"(row), "f"(v[8]), "f"(v[9]), "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
+                 : "memory");
+#else
+    float4* r4 = reinterpret_cast<float4*>(row);
+#pragma unroll
+    for (int k = 0; k < 4; k++) r4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+#endif
+}
+
 // Neighbour q's concentrations into the diffusion sums (nc, when `diffuse`) and into the plain
 // neighbour sum (ms, when MEAN).  (dif[t] * cc) * (cq[t] - cur[t]) is the reference term; with
 // one common nonzero rate the product dif[t] * cc is the same value for every species.
@@ -64,13 +105,8 @@ __device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], c
                                            const float (&cur)[NTF], const float* conc, uint32_t q,
                                            float cc, bool uniform, bool diffuse) {
     if (!DIFF && !MEAN) return;
-    const float4* cj4 = reinterpret_cast<const float4*>(conc + (size_t)q * NTF);
     float cj[NTF];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const float4 v = cj4[k];
-        cj[4 * k] = v.x; cj[4 * k + 1] = v.y; cj[4 * k + 2] = v.z; cj[4 * k + 3] = v.w;
-    }
+    load_row16(conc + (size_t)q * NTF, cj);
     if (MEAN) {
 #pragma unroll
         for (int t = 0; t < NTF; t++) ms[t] += cj[t];
@@ -242,22 +278,16 @@ __device__ __forceinline__ void dens_epilogue(const DevParams& P, const DevGenom
         }
     }
     if (F::JUDGE) {  // every particle: diffused concentrations, the surrogate adds the reaction
-        float4* o4 = reinterpret_cast<float4*>(conc_out + (size_t)p * NTF);
-#pragma unroll
-        for (int k = 0; k < 4; k++) o4[k] = make_float4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
+        store_row16(conc_out + (size_t)p * NTF, c);
     }
     if (!F::GENE && !F::JUDGE) {  // diffusion only
-        float4* o4 = reinterpret_cast<float4*>(conc_out + (size_t)p * NTF);
-#pragma unroll
-        for (int k = 0; k < 4; k++) o4[k] = make_float4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
+        store_row16(conc_out + (size_t)p * NTF, c);
     }
     if (F::GENE && plain && P.full_epi && X.epi) {
         float cf[NTF];
         gene_action_full(P, G, p, gene_word & 0xFFFFu, c, cf, X.epi);
         float* dst = F::JUDGE ? X.conc_plain : conc_out;
-        float4* o4 = reinterpret_cast<float4*>(dst + (size_t)p * NTF);
-#pragma unroll
-        for (int k = 0; k < 4; k++) o4[k] = make_float4(cf[4 * k], cf[4 * k + 1], cf[4 * k + 2], cf[4 * k + 3]);
+        store_row16(dst + (size_t)p * NTF, cf);
         if (F::CAPTURE) {
             float4* y4 = reinterpret_cast<float4*>(X.cap_y + (size_t)p * NTF);
 #pragma unroll
@@ -296,9 +326,7 @@ __device__ __forceinline__ void dens_epilogue(const DevParams& P, const DevGenom
 #pragma unroll
         for (int t = 0; t < NTF; t++) cf[t] = (bits & 4u) ? c[t] + dc[t] : c[t];
         float* dst = F::JUDGE ? X.conc_plain : conc_out;
-        float4* o4 = reinterpret_cast<float4*>(dst + (size_t)p * NTF);
-#pragma unroll
-        for (int k = 0; k < 4; k++) o4[k] = make_float4(cf[4 * k], cf[4 * k + 1], cf[4 * k + 2], cf[4 * k + 3]);
+        store_row16(dst + (size_t)p * NTF, cf);
         if (F::CAPTURE) {
             float4* y4 = reinterpret_cast<float4*>(X.cap_y + (size_t)p * NTF);
 #pragma unroll
@@ -315,12 +343,7 @@ __device__ __forceinline__ void load_conc(const DevGenome* __restrict__ G, const
                                           uint32_t p, float (&cur)[NTF], float (&dif)[NTF]) {
     using F = DF<FLAGS>;
     if (F::DIFF || F::GENE || F::MEAN) {
-        const float4* c4 = reinterpret_cast<const float4*>(conc_in + (size_t)p * NTF);
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            float4 v = c4[k];
-            cur[4 * k] = v.x; cur[4 * k + 1] = v.y; cur[4 * k + 2] = v.z; cur[4 * k + 3] = v.w;
-        }
+        load_row16(conc_in + (size_t)p * NTF, cur);
     }
 #pragma unroll
     for (int t = 0; t < NTF; t++) dif[t] = F::DIFF ? G->diff[t] : 0.f;
