@@ -59,6 +59,9 @@ __device__ __forceinline__ float wendland_term(float dsq, float sr) {
 #ifndef MG_ROW_V8
 #define MG_ROW_V8 1
 #endif
+#ifndef MG_F32X2
+#define MG_F32X2 1
+#endif
 // A particle's 16 concentrations as two 256-bit loads: a gather of rows from 32 lanes then
 // costs the L1 two accesses per row instead of four.  Rows are 64 bytes in buffers aligned to
 // 256 bytes, so both halves are 32-byte aligned.
@@ -107,15 +110,40 @@ __device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], c
     if (!DIFF && !MEAN) return;
     float cj[NTF];
     load_row16(conc + (size_t)q * NTF, cj);
+#if MG_F32X2
+    // Packed pairs of species (f32x2: two IEEE single operations, each rounded as the scalar
+    // one) where no product feeds a sum: the compiler may fuse a packed multiply into the packed
+    // add that consumes it, one rounding instead of the reference's two, so products and the
+    // sums they feed stay scalar.
+    if (MEAN) {
+#pragma unroll
+        for (int t = 0; t < NTF; t += 2) {
+            const float2 r = __fadd2_rn(make_float2(ms[t], ms[t + 1]), make_float2(cj[t], cj[t + 1]));
+            ms[t] = r.x; ms[t + 1] = r.y;
+        }
+    }
+#else
     if (MEAN) {
 #pragma unroll
         for (int t = 0; t < NTF; t++) ms[t] += cj[t];
     }
+#endif
     if (DIFF && diffuse) {
         if (uniform) {
             const float a = dif[0] * cc;
+#if MG_F32X2
+            // cj - cur as cj + (-1) * cur: one rounding of the exact difference, as the subtraction
+            const float2 m1 = make_float2(-1.f, -1.f);
+#pragma unroll
+            for (int t = 0; t < NTF; t += 2) {
+                const float2 d = __ffma2_rn(make_float2(cur[t], cur[t + 1]), m1, make_float2(cj[t], cj[t + 1]));
+                nc[t] += a * d.x;
+                nc[t + 1] += a * d.y;
+            }
+#else
 #pragma unroll
             for (int t = 0; t < NTF; t++) nc[t] += a * (cj[t] - cur[t]);
+#endif
         } else {
 #pragma unroll
             for (int t = 0; t < NTF; t++)
