@@ -104,7 +104,7 @@ __device__ __forceinline__ void store_row16(float* row, const float (&v)[NTF]) {
 // neighbour sum (ms, when MEAN).  (dif[t] * cc) * (cq[t] - cur[t]) is the reference term; with
 // one common nonzero rate the product dif[t] * cc is the same value for every species.
 template <bool DIFF, bool MEAN>
-__device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], const float (&dif)[NTF],
+__device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], const float* __restrict__ dif,
                                            const float (&cur)[NTF], const float* conc, uint32_t q,
                                            float cc, bool uniform, bool diffuse) {
     if (!DIFF && !MEAN) return;
@@ -180,7 +180,7 @@ __device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint
                                              const uint32_t* __restrict__ count,
                                              const uint32_t* __restrict__ offset,
                                              float (&nc)[NTF], float (&ms)[NTF], uint32_t& mcnt,
-                                             const float (&dif)[NTF], const float (&cur)[NTF],
+                                             const float* __restrict__ dif, const float (&cur)[NTF],
                                              bool diffuse, uint32_t* __restrict__ flist = nullptr,
                                              uint32_t* __restrict__ fcount = nullptr,
                                              uint32_t p = 0) {
@@ -368,13 +368,11 @@ __device__ __forceinline__ void dens_epilogue(const DevParams& P, const DevGenom
 
 template <int FLAGS>
 __device__ __forceinline__ void load_conc(const DevGenome* __restrict__ G, const float* conc_in,
-                                          uint32_t p, float (&cur)[NTF], float (&dif)[NTF]) {
+                                          uint32_t p, float (&cur)[NTF]) {
     using F = DF<FLAGS>;
     if (F::DIFF || F::GENE || F::MEAN) {
         load_row16(conc_in + (size_t)p * NTF, cur);
     }
-#pragma unroll
-    for (int t = 0; t < NTF; t++) dif[t] = F::DIFF ? G->diff[t] : 0.f;
 }
 
 // ---- direct kernel (one thread per particle, the reference loop) ------------------------
@@ -393,8 +391,9 @@ __global__ void __launch_bounds__(256) k_dens(DevParams P, const DevGenome* __re
     using F = DF<FLAGS>;
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= *nactive_p) return;
-    float cur[NTF], nc[NTF], ms[NTF], dif[NTF];
-    load_conc<FLAGS>(G, conc_in, p, cur, dif);
+    float cur[NTF], nc[NTF], ms[NTF];
+    load_conc<FLAGS>(G, conc_in, p, cur);
+    const float* dif = G->diff;  // the species' rates, read from the genome where used
 #pragma unroll
     for (int t = 0; t < NTF; t++) { nc[t] = 0.f; ms[t] = 0.f; }
     const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
@@ -423,8 +422,9 @@ __device__ __forceinline__ void dens_list_finish(
     const DensExtra& X, uint32_t slot) {
     // slot: the particle's position in the processing order (where its re-forming candidates go)
     using F = DF<FLAGS>;
-    float cur[NTF], dif[NTF], nc[NTF], ms[NTF];
-    load_conc<FLAGS>(G, conc_in, p, cur, dif);
+    float cur[NTF], nc[NTF], ms[NTF];
+    load_conc<FLAGS>(G, conc_in, p, cur);
+    const float* dif = G->diff;  // the species' rates, read from the genome where used
 #pragma unroll
     for (int t = 0; t < NTF; t++) { nc[t] = 0.f; ms[t] = 0.f; }
     const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
