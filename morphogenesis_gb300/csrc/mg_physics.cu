@@ -59,6 +59,9 @@ __device__ __forceinline__ float wendland_term(float dsq, float sr) {
 #ifndef MG_ROW_V8
 #define MG_ROW_V8 1
 #endif
+// Fluid-force list entries ([FL_CAP][cap], sorted particle indices < 2^31): the top bit marks
+// the first entry of each grid cell, where the force pass flushes its per-cell partial sum.
+constexpr uint32_t FLIST_CELL_START = 0x80000000u;
 #ifndef MG_F32X2
 #define MG_F32X2 1
 #endif
@@ -194,12 +197,14 @@ __device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint
         if (cnt == 0) continue;
         const uint32_t off = offset[cellc];
         float part = 0.f;
+        uint32_t fmark = FLIST_CELL_START;  // on this cell's first fluid-force neighbour
         for (uint32_t q = off; q < off + cnt; q++) {
             const float4 jp = pos[q];
             const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
             const float dsq = dx * dx + dy * dy + dz * dz;
             if (flist && dsq < 1.f && dsq > 0.f) {
-                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
+                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q | fmark;
+                fmark = 0u;
                 nf++;
             }
             if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
@@ -432,19 +437,23 @@ __device__ __forceinline__ void dens_list_finish(
     float sum = 0.f;
     {
         float part = 0.f;
-        uint32_t nf = 0, nh = 0;
+        uint32_t nf = 0, nh = 0, fmark = 0u;
         for (uint32_t k = 0; k < n; k++) {
             const uint32_t e = my[k * 32];
             const uint32_t q = e & ~LIST_CELL_START;
             const float4 jp = pos[q];
-            if (F::DENS && (e & LIST_CELL_START)) {  // first neighbour of the next cell:
-                sum += part;                         // flush the previous cell's partial sum
-                part = 0.f;
+            if (e & LIST_CELL_START) {  // first neighbour of the next cell:
+                if (F::DENS) {          // flush the previous cell's partial sum
+                    sum += part;
+                    part = 0.f;
+                }
+                fmark = FLIST_CELL_START;
             }
             const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
             const float dsq = dx * dx + dy * dy + dz * dz;
             if (dsq < 1.f && dsq > 0.f) {  // fluid-force neighbour, kept for the force pass
-                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q;
+                if (nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = q | fmark;
+                fmark = 0u;
                 nf++;
             }
             if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
@@ -738,7 +747,7 @@ template <int FLAGS>
 __device__ __forceinline__ void ovf_apply(const DevParams& P, uint32_t p, uint32_t lane, uint32_t t,
                                           uint32_t* __restrict__ flist, const float* sd,
                                           const uint32_t* sq, const uint8_t* sc, const float4 (*scj)[NTF / 4],
-                                          uint32_t nh, int& lastcell, float& sum, float& part,
+                                          uint32_t nh, int& lastcell, uint32_t& fmark, float& sum, float& part,
                                           uint32_t& nf, float& nc_t, float& ms_t, uint32_t& mcnt,
                                           float dif_t, float cur_t) {
     using F = DF<FLAGS>;
@@ -750,9 +759,11 @@ __device__ __forceinline__ void ovf_apply(const DevParams& P, uint32_t p, uint32
             sum += part;
             part = 0.f;
             lastcell = c;
+            fmark = FLIST_CELL_START;
         }
         if (d < 1.f) {
-            if (lane == 0 && nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = sq[h];
+            if (lane == 0 && nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = sq[h] | fmark;
+            fmark = 0u;
             nf++;
         }
         if (F::DENS && d < P.r2) part += wendland_term(d, P.sr);
@@ -798,6 +809,7 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
         float nc_t = 0.f, ms_t = 0.f, sum = 0.f, part = 0.f;
         uint32_t mcnt = 0, nf = 0;
         int lastcell = -1;
+        uint32_t fmark = 0u;
         const uint32_t base = scell[p] - (uint32_t)P.nadj;
         uint32_t nh = 0;  // hits of the current segment
         for (int cg = 0; cg < P.adjcnt; cg += 32) {
@@ -862,7 +874,7 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
                     const uint32_t nb = (uint32_t)__popc(ball);
                     if (nh + nb > (uint32_t)OVF_SEG) {  // segment full: take what it holds
                         ovf_apply<FLAGS>(P, p, lane, t, flist, s_d[wl], s_q[wl], s_c[wl], s_cj[wl], nh,
-                                         lastcell, sum, part, nf, nc_t, ms_t, mcnt, dif_t, cur_t);
+                                         lastcell, fmark, sum, part, nf, nc_t, ms_t, mcnt, dif_t, cur_t);
                         nh = 0;
                     }
                     if (hit[u]) {
@@ -881,7 +893,7 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
             }
         }
         ovf_apply<FLAGS>(P, p, lane, t, flist, s_d[wl], s_q[wl], s_c[wl], s_cj[wl], nh, lastcell,
-                         sum, part, nf, nc_t, ms_t, mcnt, dif_t, cur_t);
+                         fmark, sum, part, nf, nc_t, ms_t, mcnt, dif_t, cur_t);
         if (F::DENS) sum += part;
         float cur[NTF], nc[NTF], ms[NTF];
 #pragma unroll
@@ -1076,20 +1088,30 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
         const uint32_t nf = use_list ? fcount[p] : 0xFFFFFFFFu;
         if (nf <= (uint32_t)FL_CAP) {
             float cx = 0.f, cy = 0.f, cz = 0.f;
-            uint32_t curcell = UNDEF;
-            for (uint32_t k = 0; k < nf; k++) {
-                const uint32_t q = flist[(size_t)k * cap + p];
-                const uint32_t qc = scell[q];
-                if (qc != curcell) {
+            // One neighbour's term; its list entry flags the first neighbour of each cell,
+            // where the previous cell's partial sum is flushed.
+            auto term = [&](uint32_t e, float4 jp, float4 jv, float jpress, float jdens) {
+                if (e & FLIST_CELL_START) {
                     sx = sx + cx; sy = sy + cy; sz = sz + cz;
                     cx = cy = cz = 0.f;
-                    curcell = qc;
                 }
-                const float4 jp = C.pos[q];
                 const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
                 const float dsq = dx * dx + dy * dy + dz * dz;
-                fluid_term(P, ip, iv, ipress, idens, jp, C.veval[q], press[q], invdens[q], dsq, dx, dy,
-                           dz, cx, cy, cz);
+                fluid_term(P, ip, iv, ipress, idens, jp, jv, jpress, jdens, dsq, dx, dy, dz, cx, cy, cz);
+            };
+            uint32_t k = 0;
+            // two neighbours per iteration, so their gathers are in flight together
+            for (; k + 2 <= nf; k += 2) {
+                const uint32_t e0 = flist[(size_t)k * cap + p], e1 = flist[(size_t)(k + 1) * cap + p];
+                const uint32_t q0 = e0 & ~FLIST_CELL_START, q1 = e1 & ~FLIST_CELL_START;
+                const float4 jp0 = C.pos[q0], jp1 = C.pos[q1], jv0 = C.veval[q0], jv1 = C.veval[q1];
+                const float pr0 = press[q0], pr1 = press[q1], dn0 = invdens[q0], dn1 = invdens[q1];
+                term(e0, jp0, jv0, pr0, dn0);
+                term(e1, jp1, jv1, pr1, dn1);
+            }
+            if (k < nf) {
+                const uint32_t e = flist[(size_t)k * cap + p], q = e & ~FLIST_CELL_START;
+                term(e, C.pos[q], C.veval[q], press[q], invdens[q]);
             }
             sx = sx + cx; sy = sy + cy; sz = sz + cz;
         } else {
