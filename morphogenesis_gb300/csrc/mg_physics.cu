@@ -485,8 +485,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     // misses the group's box holds no candidate; after positions moved, every cell is walked
     using F = DF<FLAGS>;
     extern __shared__ uint32_t s_list[];  // [warps of the block][NL_CAP][32]
-    __shared__ float4 s_sp[DENS_WARPS][32];
-    __shared__ uint32_t s_sq[DENS_WARPS][32];
+    __shared__ float4 s_sp[DENS_WARPS][32];  // staged survivors: x, y, z, sorted index (bits)
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     uint32_t* my = s_list + (size_t)w * NL_ROWS * 32 + lane;
     // Lane k of the grid takes the k-th entry of the processing order, so a warp holds
@@ -575,8 +574,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                     const unsigned ball = __ballot_sync(0xffffffffu, surv);
                     if (surv) {
                         const uint32_t slot = (uint32_t)__popc(ball & ((1u << lane) - 1u));
-                        s_sp[w][slot] = qp;
-                        s_sq[w][slot] = off + kk;
+                        s_sp[w][slot] = make_float4(qp.x, qp.y, qp.z, __uint_as_float(off + kk));
                     }
                     __syncwarp();
                     const int ns = __popc(ball);
@@ -590,20 +588,26 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                         int tt = 0;
                         for (; tt + DENS_UNROLL <= ns; tt += DENS_UNROLL) {
                             float d[DENS_UNROLL];
+                            uint32_t qi[DENS_UNROLL];
 #pragma unroll
-                            for (int u = 0; u < DENS_UNROLL; u++) d[u] = approx_dsq(ip, s_sp[w][tt + u]);
+                            for (int u = 0; u < DENS_UNROLL; u++) {
+                                const float4 sp = s_sp[w][tt + u];
+                                d[u] = approx_dsq(ip, sp);
+                                qi[u] = __float_as_uint(sp.w);
+                            }
 #pragma unroll
                             for (int u = 0; u < DENS_UNROLL; u++) {
                                 const bool hit = d[u] < R2s && d[u] > 0.f;
-                                my[min(n, (uint32_t)NL_CAP) * 32] = s_sq[w][tt + u] | mark;
+                                my[min(n, (uint32_t)NL_CAP) * 32] = qi[u] | mark;
                                 mark = hit ? 0u : mark;
                                 n += hit ? 1u : 0u;
                             }
                         }
                         for (; tt < ns; tt++) {
-                            const float d = approx_dsq(ip, s_sp[w][tt]);
+                            const float4 sp = s_sp[w][tt];
+                            const float d = approx_dsq(ip, sp);
                             const bool hit = d < R2s && d > 0.f;
-                            my[min(n, (uint32_t)NL_CAP) * 32] = s_sq[w][tt] | mark;
+                            my[min(n, (uint32_t)NL_CAP) * 32] = __float_as_uint(sp.w) | mark;
                             mark = hit ? 0u : mark;
                             n += hit ? 1u : 0u;
                         }
