@@ -344,6 +344,41 @@ void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, bool sub
 }
 
 // ---- gather ---------------------------------------------------------------------------------
+#ifndef MG_GATHER_V8
+#define MG_GATHER_V8 1
+#endif
+// 32 bytes through one 256-bit access (both addresses 32-byte aligned: bond records are 32 bytes
+// and concentration rows 64 bytes, in buffers aligned to 256 bytes).  The source set is not
+// written by the gather, so its loads take the read-only path.
+__device__ __forceinline__ void ld32(const void* src, uint4& a, uint4& b) {
+#if MG_GATHER_V8
+    asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
+        : "l"(src));
+#else
+    a = __ldg(reinterpret_cast<const uint4*>(src));
+    b = __ldg(reinterpret_cast<const uint4*>(src) + 1);
+#endif
+}
+__device__ __forceinline__ void st32(void* dst, const uint4& a, const uint4& b) {
+#if MG_GATHER_V8
+    asm volatile("st.global.v8.u32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+                 ::"l"(dst), "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
+                 : "memory");
+#else
+    reinterpret_cast<uint4*>(dst)[0] = a;
+    reinterpret_cast<uint4*>(dst)[1] = b;
+#endif
+}
+// a 64-byte concentration row
+__device__ __forceinline__ void copy_row64(const float* src, float* dst) {
+    uint4 a, b, c, d;
+    ld32(src, a, b);
+    ld32(src + 8, c, d);
+    st32(dst, a, b);
+    st32(dst + 8, c, d);
+}
+
 __device__ __forceinline__ uint32_t remap(uint32_t j, uint32_t cap, const uint32_t* newidx) {
     return j < cap ? __ldg(newidx + j) : NO_PARTNER;
 }
@@ -368,9 +403,7 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
     if (part == 2) {
         float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
         if (p < nact) {
-            const float4* ci = reinterpret_cast<const float4*>(sconc + (size_t)sorted[p] * NTF);
-#pragma unroll
-            for (int k = 0; k < 4; k++) co[k] = __ldg(ci + k);
+            copy_row64(sconc + (size_t)sorted[p] * NTF, dconc + (size_t)p * NTF);
         } else {
 #pragma unroll
             for (int k = 0; k < 4; k++) co[k] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -385,11 +418,10 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
 #pragma unroll
         for (int a = 0; a < NB; a++) {
             const size_t src = ((size_t)a * cap + i) * 2, dst = ((size_t)a * cap + p) * 2;
-            uint4 A = __ldg(S.bond + src);
-            uint4 B = __ldg(S.bond + src + 1);
+            uint4 A, B;
+            ld32(S.bond + src, A, B);
             A.x = remap(A.x, cap, newidx);
-            D.bond[dst] = A;
-            D.bond[dst + 1] = B;
+            st32(D.bond + dst, A, B);
         }
         const uint4* pi = reinterpret_cast<const uint4*>(S.pidx + (size_t)i * 12);
         uint4* po = reinterpret_cast<uint4*>(D.pidx + (size_t)p * 12);
@@ -400,12 +432,7 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
             v.z = remap(v.z, cap, newidx);
             po[k] = v;
         }
-        if (part == 0) {
-            const float4* ci = reinterpret_cast<const float4*>(sconc + (size_t)i * NTF);
-            float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
-#pragma unroll
-            for (int k = 0; k < 4; k++) co[k] = __ldg(ci + k);
-        }
+        if (part == 0) copy_row64(sconc + (size_t)i * NTF, dconc + (size_t)p * NTF);
         if (P.full_epi) {
             // per-gene words move with the particle; the bits (dense-list membership at sort
             // time, FEPIGEN > 0) are taken from them
