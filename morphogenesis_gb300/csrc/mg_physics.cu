@@ -1021,6 +1021,14 @@ __device__ __forceinline__ BondTerm bond_term(float4 po, float4 vo, float4 pj, f
     return t;
 }
 
+// A bond record (32 bytes: partner, rest length, modulus, damping | elastic limit, -, the two
+// strain integrators) as one 256-bit load; records are 32-byte aligned.
+__device__ __forceinline__ void load_record(const uint4* rec, uint4& A, uint4& B) {
+    asm("ld.global.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(A.x), "=r"(A.y), "=r"(A.z), "=r"(A.w), "=r"(B.x), "=r"(B.y), "=r"(B.z), "=r"(B.w)
+        : "l"(rec));
+}
+
 __device__ __forceinline__ bool is_nan3(const BondTerm& t) {
     return t.ex != t.ex || t.ey != t.ey || t.ez != t.ez;
 }
@@ -1067,11 +1075,11 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
 #pragma unroll
     for (int a = 0; a < NB; a++) {
         uint4* rec = C.bond + ((size_t)a * cap + p) * 2;
-        const uint4 A = rec[0];
+        uint4 A, B;
+        load_record(rec, A, B);
         const uint32_t j = A.x;
         const float restlen = __uint_as_float(A.y);
         if (j >= nact || restlen < REST_MIN) continue;
-        const uint4 B = rec[1];
         const float elastlim = __uint_as_float(B.x);
         const BondTerm t = bond_term(ip, iv, C.pos[j], C.veval[j], restlen, __uint_as_float(A.z),
                                      __uint_as_float(A.w), elastlim, P.pmass);
@@ -1154,12 +1162,14 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
         for (int b = 0; b < NB; b++) {
             const uint32_t k = in[2 * b], bk = in[2 * b + 1];
             if (k >= nact || bk >= (uint32_t)NB) continue;
-            const uint4* rec = C.bond + ((size_t)bk * cap + k) * 2;
-            const uint4 A = rec[0];
+            // the owner's record (its integrator words, which the owner's thread rewrites in
+            // this pass, are not used)
+            uint4 A, B;
+            load_record(C.bond + ((size_t)bk * cap + k) * 2, A, B);
             if (A.x != p) continue;
             const float restlen = __uint_as_float(A.y);
             if (restlen < REST_MIN) continue;
-            const float elastlim = __uint_as_float(reinterpret_cast<const uint32_t*>(rec + 1)[0]);
+            const float elastlim = __uint_as_float(B.x);
             const BondTerm t = bond_term(C.pos[k], C.veval[k], ip, iv, restlen,
                                          __uint_as_float(A.z), __uint_as_float(A.w), elastlim,
                                          P.pmass);
