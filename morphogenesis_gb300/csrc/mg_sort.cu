@@ -161,33 +161,45 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
         }
         uint32_t agg = __shfl_sync(0xffffffffu, incl, nw - 1);
         if ((int)lane < nw) s_warp[lane] = incl - w;
-        if (lane == 0) {
-            uint32_t excl = 0;
-            cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> me(status[tile]);
-            if (tile == 0) {
-                me.store((2ull << 32) | agg, cuda::memory_order_relaxed);
-            } else {
-                me.store((1ull << 32) | agg, cuda::memory_order_relaxed);
-                int64_t t = (int64_t)tile - 1;
-                uint32_t spins = 0;
-                while (t >= 0) {
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> me(status[tile]);
+        if (lane == 0) me.store(((tile == 0 ? 2ull : 1ull) << 32) | agg, cuda::memory_order_relaxed);
+        // Look-back by the whole warp: lane i reads the status of tile (end - i), 32 tiles per
+        // round.  A round completes when every tile from end down to the nearest one holding
+        // an inclusive prefix has published; their values sum to this tile's exclusive prefix.
+        uint32_t excl = 0;
+        if (tile > 0) {
+            int64_t end = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            while (true) {
+                const int64_t t = end - (int64_t)lane;
+                unsigned long long sw = 2ull << 32;  // before tile 0: an inclusive prefix of 0
+                if (t >= 0) {
                     cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> prev(status[t]);
-                    unsigned long long sw = prev.load(cuda::memory_order_relaxed);
-                    uint32_t flag = (uint32_t)(sw >> 32);
-                    if (flag == 0) {
-                        if (++spins > SPIN_LIMIT) {
-                            atomicOr(err, ERR_SCAN_TIMEOUT);
-                            break;
-                        }
-                        __nanosleep(32);
-                        continue;
-                    }
-                    excl += (uint32_t)sw;
-                    if (flag == 2) break;
-                    t--;
+                    sw = prev.load(cuda::memory_order_relaxed);
                 }
-                me.store((2ull << 32) | (uint32_t)(excl + agg), cuda::memory_order_relaxed);
+                const uint32_t flag = (uint32_t)(sw >> 32);
+                const unsigned inclusive = __ballot_sync(0xffffffffu, flag == 2);
+                const unsigned unready = __ballot_sync(0xffffffffu, flag == 0);
+                const int stop = inclusive ? __ffs(inclusive) - 1 : 31;  // last lane to sum
+                const unsigned needed = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
+                if (unready & needed) {
+                    if (++spins > SPIN_LIMIT) {
+                        if (lane == 0) atomicOr(err, ERR_SCAN_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                uint32_t v = (int)lane <= stop ? (uint32_t)sw : 0u;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+                excl += v;
+                if (inclusive) break;
+                end -= 32;
             }
+            if (lane == 0) me.store((2ull << 32) | (uint32_t)(excl + agg), cuda::memory_order_relaxed);
+        }
+        if (lane == 0) {
             s_prefix = excl;
             if (tile == ntiles - 1 && total) *total = excl + agg;
         }
