@@ -80,7 +80,10 @@ struct mg_system {
     // buffer state and exchange list; side streams and fork / join events used in capture
     std::map<std::string, cudaGraphExec_t> io_graphs;
     cudaStream_t io_st[2] = {nullptr, nullptr};
-    cudaEvent_t io_ev[6] = {};
+    cudaEvent_t io_ev[7] = {};
+    // the velocities / incoming-bond table of the last gather still to move (their upload was in
+    // flight): moved after this event, before the force pass reads them
+    cudaEvent_t motion_ready = nullptr;
     bool profile = false;
     std::vector<ProfSlot> prof;
     std::vector<ProfMark> marks;
@@ -379,20 +382,24 @@ void enqueue_insert_rank(mg_system* h, bool prof) {
     { Mark m(h, prof, "cellsort"); launch_cellsort(P, h->s, h->num_sms, h->search == 2, st); }
 }
 
-// conc_ready: the concentrations arrive later (an upload still in flight); everything else is
-// moved first and the concentrations after the stream has waited for that event.
-void enqueue_gather(mg_system* h, bool prof, cudaEvent_t conc_ready = nullptr) {
+// conc_ready / motion_ready: the concentrations / the velocities and incoming-bond table arrive
+// later (uploads still in flight).  The rest is moved first, the concentrations after the
+// stream has waited for conc_ready; the motion part is left to flush_motion, which the step
+// calls before its force pass (nothing before it reads those fields).
+void enqueue_gather(mg_system* h, bool prof, cudaEvent_t conc_ready = nullptr,
+                    cudaEvent_t motion_ready = nullptr) {
     int src = h->cur, dst = 1 - h->cur;
     int csrc = h->conc_cur, cdst = 1 - h->conc_cur;
     { Mark m(h, prof, "gather");
+      const int first = GATHER_CORE | (conc_ready ? 0 : GATHER_CONC) | (motion_ready ? 0 : GATHER_MOTION);
+      launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream, first);
       if (conc_ready) {
-          launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream, 1);
           cudaStreamWaitEvent(h->stream, conc_ready, 0);
-          launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream, 2);
-      } else {
-          launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream);
+          launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream,
+                        GATHER_CONC);
       }
     }
+    h->motion_ready = motion_ready;
     h->cur = dst;
     h->conc_cur = cdst;
     h->flist_valid = false;
@@ -496,35 +503,59 @@ void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof, bool hea
     h->conc_cur = cout;
 }
 
+// The motion part of a gather whose upload was in flight (see enqueue_gather).
+void flush_motion(mg_system* h, bool prof) {
+    if (!h->motion_ready) return;
+    Mark m(h, prof, "gather");
+    cudaStreamWaitEvent(h->stream, h->motion_ready, 0);
+    launch_gather(h->P, h->set[1 - h->cur], nullptr, h->set[h->cur], nullptr, h->s, h->stream, GATHER_MOTION);
+    h->motion_ready = nullptr;
+}
+
+// Uploads the force pass reads first (the gather moves them last).
+bool motion_buffer(int32_t id) { return id == MG_FVEL || id == MG_FVEVAL || id == MG_FPARTICLEIDX; }
+
 void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nullptr) {
     cudaStream_t st = h->stream;
     cudaStream_t A = io ? h->io_st[0] : nullptr, B = io ? h->io_st[1] : nullptr;
     cudaEvent_t* ev = h->io_ev;
     const bool up = io && io->nin;
-    bool conc_up = false;
+    bool conc_up = false, motion_up = false;
     if (up) {
         cudaEventRecord(ev[0], st);
         cudaStreamWaitEvent(A, ev[0], 0);
         cudaStreamWaitEvent(B, ev[0], 0);
-        // FPOS on A; the others on B, FCONC (the largest) last
+        // FPOS on A (the sort needs it first); on B the other buffers the gather's first part
+        // moves, then FCONC (the density pass's input), then the velocities and the incoming-
+        // bond table, which nothing reads before the force pass
+        auto upload = [&](uint32_t k, cudaStream_t s) {
+            cudaMemcpyAsync(direct_buffer(h, io->in[k].buf_id, true), io->in[k].host, io->in[k].bytes,
+                            cudaMemcpyHostToDevice, s);
+        };
         for (uint32_t k = 0; k < io->nin; k++)
-            if (io->in[k].buf_id != MG_FCONC)
-                cudaMemcpyAsync(direct_buffer(h, io->in[k].buf_id, true), io->in[k].host, io->in[k].bytes,
-                                cudaMemcpyHostToDevice, io->in[k].buf_id == MG_FPOS ? A : B);
+            if (io->in[k].buf_id == MG_FPOS) upload(k, A);
+        for (uint32_t k = 0; k < io->nin; k++)
+            if (io->in[k].buf_id != MG_FPOS && io->in[k].buf_id != MG_FCONC && !motion_buffer(io->in[k].buf_id))
+                upload(k, B);
         cudaEventRecord(ev[1], A);
         cudaEventRecord(ev[2], B);
         for (uint32_t k = 0; k < io->nin; k++)
             if (io->in[k].buf_id == MG_FCONC) {
-                cudaMemcpyAsync(direct_buffer(h, MG_FCONC, true), io->in[k].host, io->in[k].bytes,
-                                cudaMemcpyHostToDevice, B);
+                upload(k, B);
                 conc_up = true;
             }
         if (conc_up) cudaEventRecord(ev[5], B);
+        for (uint32_t k = 0; k < io->nin; k++)
+            if (motion_buffer(io->in[k].buf_id)) {
+                upload(k, B);
+                motion_up = true;
+            }
+        if (motion_up) cudaEventRecord(ev[6], B);
         cudaStreamWaitEvent(st, ev[1], 0);
     }
     enqueue_insert_rank(h, prof);
     if (up) cudaStreamWaitEvent(st, ev[2], 0);
-    enqueue_gather(h, prof, conc_up ? ev[5] : nullptr);
+    enqueue_gather(h, prof, conc_up ? ev[5] : nullptr, motion_up ? ev[6] : nullptr);
     const bool remodel = (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) != 0;
     const bool heal_list = heal_from_density(h, flags);
     if (flags & MG_STEP_SURROGATE) {
@@ -546,6 +577,7 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
                                 cudaMemcpyDeviceToHost, A);
             }
     if (early) cudaEventRecord(ev[4], A);
+    flush_motion(h, prof);
     if (flags & MG_STEP_PHYSICS) {
         { Mark m(h, prof, "force"); launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream); }
     }
@@ -1287,8 +1319,14 @@ mg_status mg_step_io(mg_handle h, const mg_io* in, uint32_t nin, uint32_t nsteps
             MG_CUDA(h, cudaGraphLaunch(ge, h->stream));
         }
         after_steps(h, nsteps, flags);
-        for (uint32_t k = 0; k < nin; k++)
-            if (in[k].buf_id == MG_FCONC) h->launches += 1;  // the first step's gather in two parts
+        // the first step's gather in parts: the concentrations and the motion fields after
+        // their uploads
+        bool conc_in = false, motion_in = false;
+        for (uint32_t k = 0; k < nin; k++) {
+            conc_in |= in[k].buf_id == MG_FCONC;
+            motion_in |= motion_buffer(in[k].buf_id);
+        }
+        h->launches += (conc_in ? 1 : 0) + (motion_in ? 1 : 0);
         return check_device(h);
     }
     for (uint32_t k = 0; k < nin; k++) {

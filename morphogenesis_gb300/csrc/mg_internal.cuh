@@ -160,10 +160,12 @@ void launch_place(const DevParams& P, const Scratch& s, cudaStream_t st);
 // subcounts: also count each cell's 2x2x2 sub-cells (for the per-lane fine-cell search)
 void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, bool subcounts,
                      cudaStream_t st);
-// part: 0 the whole carried state, 1 all but the concentrations, 2 the concentrations only
+// parts of the carried state a gather moves (the three make the whole state): positions,
+// bonds, genes, origins and cells; concentrations; velocities and the incoming-bond table
+enum : int { GATHER_CORE = 1, GATHER_CONC = 2, GATHER_MOTION = 4, GATHER_ALL = 7 };
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st,
-                   int part = 0);
+                   int parts = GATHER_ALL);
 // flags: 1 density/pressure, 2 diffusion, 4 gene reaction
 // flags: 1 density, 2 diffusion, 4 gene reaction, 8 surrogate features, 16 capture of
 // training pairs, 32 judge (plain update of sampled / handed-over particles into conc_plain).

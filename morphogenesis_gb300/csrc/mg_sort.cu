@@ -406,97 +406,96 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
                                                 float* __restrict__ invdens,
                                                 float4* __restrict__ force,
                                                 const uint32_t* __restrict__ nactive_p,
-                                                int part) {
-    // part: 0 everything, 1 everything but the concentrations, 2 the concentrations only
+                                                int parts) {
+    // parts: GATHER_CORE (positions, bonds, genes, origins, cells; the scratch of parked slots),
+    // GATHER_CONC (concentrations), GATHER_MOTION (velocities, incoming-bond table)
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t cap = P.cap;
     if (p >= cap) return;
     const uint32_t nact = *nactive_p;
-    if (part == 2) {
-        float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
-        if (p < nact) {
-            copy_row64(sconc + (size_t)sorted[p] * NTF, dconc + (size_t)p * NTF);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 4; k++) co[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        return;
-    }
     if (p < nact) {
         const uint32_t i = sorted[p];
-        D.pos[p] = __ldg(S.pos + i);
-        D.vel[p] = __ldg(S.vel + i);
-        D.veval[p] = __ldg(S.veval + i);
+        if (parts & GATHER_CORE) {
+            D.pos[p] = __ldg(S.pos + i);
 #pragma unroll
-        for (int a = 0; a < NB; a++) {
-            const size_t src = ((size_t)a * cap + i) * 2, dst = ((size_t)a * cap + p) * 2;
-            uint4 A, B;
-            ld32(S.bond + src, A, B);
-            A.x = remap(A.x, cap, newidx);
-            st32(D.bond + dst, A, B);
-        }
-        const uint4* pi = reinterpret_cast<const uint4*>(S.pidx + (size_t)i * 12);
-        uint4* po = reinterpret_cast<uint4*>(D.pidx + (size_t)p * 12);
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            uint4 v = __ldg(pi + k);
-            v.x = remap(v.x, cap, newidx);
-            v.z = remap(v.z, cap, newidx);
-            po[k] = v;
-        }
-        if (part == 0) copy_row64(sconc + (size_t)i * NTF, dconc + (size_t)p * NTF);
-        if (P.full_epi) {
-            // per-gene words move with the particle; the bits (dense-list membership at sort
-            // time, FEPIGEN > 0) are taken from them
-            uint32_t bits = __ldg(S.genes + i) & 0x80000000u;
-#pragma unroll
-            for (int g = 0; g < NG; g++) {
-                const uint32_t wv = __ldg(S.epi + (size_t)g * cap + i);
-                D.epi[(size_t)g * cap + p] = wv;
-                if (wv != 0u) bits |= 1u << g;
+            for (int a = 0; a < NB; a++) {
+                const size_t src = ((size_t)a * cap + i) * 2, dst = ((size_t)a * cap + p) * 2;
+                uint4 A, B;
+                ld32(S.bond + src, A, B);
+                A.x = remap(A.x, cap, newidx);
+                st32(D.bond + dst, A, B);
             }
-            D.genes[p] = bits;
-        } else {
-            D.genes[p] = __ldg(S.genes + i);
+            if (P.full_epi) {
+                // per-gene words move with the particle; the bits (dense-list membership at sort
+                // time, FEPIGEN > 0) are taken from them
+                uint32_t bits = __ldg(S.genes + i) & 0x80000000u;
+#pragma unroll
+                for (int g = 0; g < NG; g++) {
+                    const uint32_t wv = __ldg(S.epi + (size_t)g * cap + i);
+                    D.epi[(size_t)g * cap + p] = wv;
+                    if (wv != 0u) bits |= 1u << g;
+                }
+                D.genes[p] = bits;
+            } else {
+                D.genes[p] = __ldg(S.genes + i);
+            }
+            D.origin[p] = __ldg(S.origin + i);
+            scell[p] = __ldg(cell + i);
         }
-        D.origin[p] = __ldg(S.origin + i);
-        scell[p] = __ldg(cell + i);
+        if (parts & GATHER_MOTION) {
+            D.vel[p] = __ldg(S.vel + i);
+            D.veval[p] = __ldg(S.veval + i);
+            const uint4* pi = reinterpret_cast<const uint4*>(S.pidx + (size_t)i * 12);
+            uint4* po = reinterpret_cast<uint4*>(D.pidx + (size_t)p * 12);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                uint4 v = __ldg(pi + k);
+                v.x = remap(v.x, cap, newidx);
+                v.z = remap(v.z, cap, newidx);
+                po[k] = v;
+            }
+        }
+        if (parts & GATHER_CONC) copy_row64(sconc + (size_t)i * NTF, dconc + (size_t)p * NTF);
     } else {
         // parked null particle (out-of-grid parking of advanceParticles, cuda:3474-3477)
-        D.pos[p] = make_float4(P.bmin[0], P.bmin[1], P.null_z, 0.0f);
-        D.vel[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-        D.veval[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (parts & GATHER_CORE) {
+            D.pos[p] = make_float4(P.bmin[0], P.bmin[1], P.null_z, 0.0f);
 #pragma unroll
-        for (int a = 0; a < NB; a++) {
-            const size_t dst = ((size_t)a * cap + p) * 2;
-            D.bond[dst] = make_uint4(NO_PARTNER, 0u, 0u, 0u);
-            D.bond[dst + 1] = make_uint4(0u, NO_PARTNER, 0u, 0u);
+            for (int a = 0; a < NB; a++) {
+                const size_t dst = ((size_t)a * cap + p) * 2;
+                D.bond[dst] = make_uint4(NO_PARTNER, 0u, 0u, 0u);
+                D.bond[dst + 1] = make_uint4(0u, NO_PARTNER, 0u, 0u);
+            }
+            D.genes[p] = 0u;
+            if (P.full_epi)
+                for (int g = 0; g < NG; g++) D.epi[(size_t)g * cap + p] = 0u;
+            D.origin[p] = UNDEF;
+            scell[p] = UNDEF;
+            press[p] = 0.f;
+            invdens[p] = 0.f;
+            force[p] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        uint4* po = reinterpret_cast<uint4*>(D.pidx + (size_t)p * 12);
+        if (parts & GATHER_MOTION) {
+            D.vel[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+            D.veval[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+            uint4* po = reinterpret_cast<uint4*>(D.pidx + (size_t)p * 12);
 #pragma unroll
-        for (int k = 0; k < 3; k++) po[k] = make_uint4(NO_PARTNER, NO_PARTNER, NO_PARTNER, NO_PARTNER);
-        if (part == 0) {
+            for (int k = 0; k < 3; k++) po[k] = make_uint4(NO_PARTNER, NO_PARTNER, NO_PARTNER, NO_PARTNER);
+        }
+        if (parts & GATHER_CONC) {
             float4* co = reinterpret_cast<float4*>(dconc + (size_t)p * NTF);
 #pragma unroll
             for (int k = 0; k < 4; k++) co[k] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        D.genes[p] = 0u;
-        if (P.full_epi)
-            for (int g = 0; g < NG; g++) D.epi[(size_t)g * cap + p] = 0u;
-        D.origin[p] = UNDEF;
-        scell[p] = UNDEF;
-        press[p] = 0.f;
-        invdens[p] = 0.f;
-        force[p] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st,
-                   int part) {
+                   int parts) {
     uint32_t blocks = (P.cap + 255) / 256;
     k_gather<<<blocks, 256, 0, st>>>(P, src, src_conc, dst, dst_conc, s.sorted, s.newidx, s.cell,
-                                      s.scell, s.press, s.invdens, s.force, s.counters + 3, part);
+                                      s.scell, s.press, s.invdens, s.force, s.counters + 3, parts);
 }
 
 }  // namespace mg
