@@ -970,6 +970,7 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     plan.push_back({(void**)&h->s.cell, 4 * n});
     plan.push_back({(void**)&h->s.arank, 4 * n});
     plan.push_back({(void**)&h->s.order, 4 * n});
+    plan.push_back({(void**)&h->s.okey, 8 * n});
     plan.push_back({(void**)&h->s.sorted, 4 * n});
     plan.push_back({(void**)&h->s.work, 4 * n});
     plan.push_back({(void**)&h->s.sub, n});

@@ -117,6 +117,7 @@ struct Scratch {
     uint32_t* cell;     // unsorted cell of particle i (UNDEF outside the window)
     uint32_t* arank;    // arrival rank within the cell (not deterministic)
     uint32_t* order;    // arrival order: order[offset[cell] + arank[i]] = i (not stable)
+    unsigned long long* okey;  // the same slots' keys (sub-cell code << 32 | i)
     uint32_t* sorted;   // sorted[p] = pre-sort index of the particle sorted to p (stable)
     uint32_t* work;     // density-pass processing order: sorted slots, cell by cell, each
                         // cell's particles by sub-cell Morton code (a permutation of [0, nactive))

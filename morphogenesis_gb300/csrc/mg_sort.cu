@@ -224,30 +224,33 @@ void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long lo
 __global__ void __launch_bounds__(256) k_place(uint32_t cap, const uint32_t* __restrict__ cell,
                                                const uint32_t* __restrict__ arank,
                                                const uint32_t* __restrict__ offset,
-                                               uint32_t* __restrict__ order) {
+                                               const uint8_t* __restrict__ sub,
+                                               uint32_t* __restrict__ order,
+                                               unsigned long long* __restrict__ okey) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap) return;
     uint32_t c = cell[i];
     if (c == UNDEF) return;
-    order[offset[c] + arank[i]] = i;
+    const uint32_t slot = offset[c] + arank[i];
+    order[slot] = i;
+    okey[slot] = ((unsigned long long)sub[i] << 32) | i;
 }
 
 void launch_place(const DevParams& P, const Scratch& s, cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
-    k_place<<<blocks, 256, 0, st>>>(P.cap, s.cell, s.arank, s.offset, s.order);
+    k_place<<<blocks, 256, 0, st>>>(P.cap, s.cell, s.arank, s.offset, s.sub, s.order, s.okey);
 }
 
 // ---- cell sort ------------------------------------------------------------------------------
 // One thread per arrival slot s < nactive: particle x = order[s] of cell c counts the members
 // of c with a smaller index (its stable rank r) and the members whose (sub-cell code, index)
-// key is smaller (its rank w in the processing order).  Members are read in the same order by
-// every lane of a warp that shares the cell, so the loads broadcast.  Cells above
+// key is smaller (its rank w in the processing order), one 64-bit key per member.  Members are
+// read in the same order by every lane of a warp that shares the cell, so the loads broadcast.  Cells above
 // WARP_CELL_MAX particles go to the block tier through the big-cell list.
 __global__ void __launch_bounds__(256) k_cellsort(const uint32_t* __restrict__ cell,
                                                   const uint32_t* __restrict__ count,
                                                   const uint32_t* __restrict__ offset,
-                                                  const uint32_t* __restrict__ order,
-                                                  const uint8_t* __restrict__ sub,
+                                                  const unsigned long long* __restrict__ okey,
                                                   uint32_t* __restrict__ sorted,
                                                   uint32_t* __restrict__ newidx,
                                                   uint32_t* __restrict__ work,
@@ -258,7 +261,8 @@ __global__ void __launch_bounds__(256) k_cellsort(const uint32_t* __restrict__ c
                                                   const uint32_t* __restrict__ nactive_p) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= *nactive_p) return;
-    const uint32_t x = order[s];
+    const unsigned long long kx = okey[s];
+    const uint32_t x = (uint32_t)kx;
     const uint32_t c = cell[x];
     const uint32_t off = offset[c], n = count[c];
     if (n > (uint32_t)WARP_CELL_MAX) {
@@ -269,21 +273,19 @@ __global__ void __launch_bounds__(256) k_cellsort(const uint32_t* __restrict__ c
         }
         return;
     }
-    const uint32_t kx = sub[x];
     uint32_t r = 0, w = 0;
 #pragma unroll 4
     for (uint32_t m = 0; m < n; m++) {
-        const uint32_t xm = __ldg(order + off + m);
-        const uint32_t km = __ldg(sub + xm);
-        r += xm < x ? 1u : 0u;
-        w += (km < kx || (km == kx && xm < x)) ? 1u : 0u;
+        const unsigned long long km = __ldg(okey + off + m);
+        r += (uint32_t)km < x ? 1u : 0u;
+        w += km < kx ? 1u : 0u;
     }
     sorted[off + r] = x;
     newidx[x] = off + r;
     work[off + w] = off + r;
     // per sub-cell code counts, 8 bits each (with 2x2x2 sub-cells the codes are 0..7; the
     // table was zeroed before this pass)
-    if (subcnt && n < (uint32_t)WARP_CELL_MAX) atomicAdd(subcnt + c, 1ull << (8 * (kx & 7u)));
+    if (subcnt && n < (uint32_t)WARP_CELL_MAX) atomicAdd(subcnt + c, 1ull << (8 * ((uint32_t)(kx >> 32) & 7u)));
 }
 
 constexpr int BIG_THREADS = 512;
@@ -347,7 +349,7 @@ void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, bool sub
                      cudaStream_t st) {
     const uint32_t blocks = (P.cap + 255) / 256;
     if (subcounts) cudaMemsetAsync(s.subcnt, 0, sizeof(unsigned long long) * P.cells, st);
-    k_cellsort<<<blocks, 256, 0, st>>>(s.cell, s.count, s.offset, s.order, s.sub, s.sorted,
+    k_cellsort<<<blocks, 256, 0, st>>>(s.cell, s.count, s.offset, s.okey, s.sorted,
                                         s.newidx, s.work, subcounts ? s.subcnt : nullptr,
                                         s.big_list, s.counters + 1, s.counters + 2, s.counters + 3);
     k_cellsort_big<<<num_sms, BIG_THREADS, BLOCK_CELL_MAX * sizeof(uint32_t), st>>>(
