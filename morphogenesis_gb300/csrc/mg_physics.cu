@@ -56,12 +56,15 @@ __device__ __forceinline__ float wendland_term(float dsq, float sr) {
     return b * (4.f * qq + 1.f);
 }
 
-#ifndef MG_ROW_V8
-#define MG_ROW_V8 1
-#endif
 // Fluid-force list entries ([FL_CAP][cap], sorted particle indices < 2^31): the top bit marks
 // the first entry of each grid cell, where the force pass flushes its per-cell partial sum.
 constexpr uint32_t FLIST_CELL_START = 0x80000000u;
+
+// Build switches kept for measuring each choice against its plain form (both forms give the
+// same bits): 256-bit concentration rows, packed f32x2 species differences.
+#ifndef MG_ROW_V8
+#define MG_ROW_V8 1
+#endif
 #ifndef MG_F32X2
 #define MG_F32X2 1
 #endif
