@@ -255,7 +255,9 @@ struct InferSmem {
     // per group: A operand of layer 1 (128 x 48, the first 12 KB) and of layers 2 and 3
     // (128 x 128); layer 1 has finished reading its operand before the epilogue overwrites it
     bf16 act[INF_GROUPS][128 * MLP_H];
-    float b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
+    alignas(16) float b1[MLP_H];
+    alignas(16) float b2[MLP_H];
+    alignas(16) float b3[MLP_OUT];
     unsigned long long mbar[INF_GROUPS];
     uint32_t tmem_base;
 };
@@ -362,6 +364,32 @@ __device__ __forceinline__ void put8(bf16* tile, uint32_t r, uint32_t k, uint32_
 #pragma unroll
     for (int i = 0; i < 4; i++) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
     *reinterpret_cast<uint4*>(tile + core_offset(r, k, K)) = *reinterpret_cast<uint4*>(h);
+}
+
+#ifndef MG_MLP_PACKED
+#define MG_MLP_PACKED 1
+#endif
+// bias + GELU of eight accumulator columns (biases b[0..7], 16-byte aligned in shared memory):
+// the gelu() expression with two columns per packed f32x2 operation, the tanh per column
+__device__ __forceinline__ void bias_gelu8(const float* v, const float* b, float (&h)[8]) {
+#if MG_MLP_PACKED
+    const float4 b0 = *reinterpret_cast<const float4*>(b), b4 = *reinterpret_cast<const float4*>(b + 4);
+    const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b4.x, b4.y, b4.z, b4.w};
+    const float2 k01 = make_float2(GELU_K0 * GELU_K1, GELU_K0 * GELU_K1), k0 = make_float2(GELU_K0, GELU_K0);
+    const float2 half = make_float2(0.5f, 0.5f);
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+        const float2 x = __fadd2_rn(make_float2(v[i], v[i + 1]), make_float2(bb[i], bb[i + 1]));
+        const float2 u = __fmul2_rn(x, __ffma2_rn(k01, __fmul2_rn(x, x), k0));
+        const float2 hx = __fmul2_rn(half, x);
+        const float2 r = __ffma2_rn(hx, make_float2(tanh_hw(u.x), tanh_hw(u.y)), hx);
+        h[i] = r.x;
+        h[i + 1] = r.y;
+    }
+#else
+#pragma unroll
+    for (int i = 0; i < 8; i++) h[i] = gelu(v[i] + b[i]);
+#endif
 }
 
 // Issues one layer: D[128 x N] = A[128 x K] * B[N x K]^T, K/16 MMAs (single thread).
@@ -490,8 +518,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
 #pragma unroll
             for (int q = 0; q < 32; q += 8) {
                 float h[8];
-#pragma unroll
-                for (int i = 0; i < 8; i++) h[i] = gelu(v[q + i] + S.b1[c0 + q + i]);
+                bias_gelu8(v + q, S.b1 + c0 + q, h);
                 put8(act, row, c0 + q, MLP_H, h);
             }
         }
@@ -516,8 +543,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
 #pragma unroll
             for (int q = 0; q < 32; q += 8) {
                 float h[8];
-#pragma unroll
-                for (int i = 0; i < 8; i++) h[i] = gelu(v[q + i] + S.b2[c0 + q + i]);
+                bias_gelu8(v + q, S.b2 + c0 + q, h);
                 put8(act, row, c0 + q, MLP_H, h);
             }
         }
