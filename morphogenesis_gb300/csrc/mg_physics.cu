@@ -792,7 +792,9 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
     uint32_t* __restrict__ fcount, const uint32_t* __restrict__ ovf,
-    const uint32_t* __restrict__ ovf_count, DensExtra X) {
+    const uint32_t* __restrict__ ovf_count, DensExtra X, bool prune) {
+    // prune: positions are those of the last sort, so a window cell whose geometric box misses
+    // the particle's search box holds no neighbour
     using F = DF<FLAGS>;
     constexpr bool CONC = F::DIFF || F::MEAN;
     __shared__ float4 s_cj[256 / 32][OVF_SEG][NTF / 4];  // concentrations of the segment's hits
@@ -807,6 +809,7 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
     float R2 = 1.f;
     if (F::DENS) R2 = fmaxf(R2, P.r2);
     if (CONC) R2 = fmaxf(R2, P.r2diff);
+    const float Rf = sqrtf(R2) * 1.0001f + 1e-3f;  // conservative search-box half width
     for (uint32_t e = gw; e < nq; e += nw) {
         const uint32_t p = ovf[e];
         const float4 ip = pos[p];
@@ -825,8 +828,14 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
             uint32_t cnt = 0, off = 0;
             if (ci < P.adjcnt) {
                 const uint32_t cellc = base + (uint32_t)P.adj[ci];
-                cnt = count[cellc];
-                if (cnt) off = offset[cellc];
+                const int cx = (int)(cellc % (uint32_t)P.res[0]);
+                const int cz = (int)((cellc / (uint32_t)P.res[0]) % (uint32_t)P.res[2]);
+                const int cy = (int)(cellc / ((uint32_t)P.res[0] * (uint32_t)P.res[2]));
+                if (!prune || cell_meets_box(P, cx, cy, cz, ip.x - Rf, ip.x + Rf, ip.y - Rf, ip.y + Rf,
+                                             ip.z - Rf, ip.z + Rf)) {
+                    cnt = count[cellc];
+                    if (cnt) off = offset[cellc];
+                }
             }
             uint32_t incl = cnt;
 #pragma unroll
@@ -957,7 +966,7 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.ovf,            \
-                                                             s.counters + 6, X);                  \
+                                                             s.counters + 6, X, prune);           \
         return;
         cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
         switch (flags) { MG_DENS_FLAG_SETS(MG_DENSW_CASE) default: break; }
@@ -976,7 +985,7 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.ovf,            \
-                                                             s.counters + 6, X);                  \
+                                                             s.counters + 6, X, true);            \
         return;
         cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
         switch (flags) { MG_DENS_FLAG_SETS(MG_DENSF_CASE) default: break; }
