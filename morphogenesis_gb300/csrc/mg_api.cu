@@ -609,7 +609,7 @@ int kernels_per_step(const mg_system* h, uint32_t flags) {
     // density pass (+ its overflow pass with the warp search)
     if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE)) n += h->search ? 2 : 1;
     if (flags & MG_STEP_SURROGATE) n += 1;
-    if (flags & MG_STEP_PHYSICS) n += 2;
+    if (flags & MG_STEP_PHYSICS) n += 3;  // force (two kernels), advance
     if (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) n += (flags & MG_STEP_PHYSICS) ? 4 : 3;
     if (flags & MG_STEP_BOND_CHANGES) n += 1;
     return n;
@@ -986,6 +986,7 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     plan.push_back({(void**)&h->s.press, 4 * n});
     plan.push_back({(void**)&h->s.invdens, 4 * n});
     plan.push_back({(void**)&h->s.force, 16 * n});
+    plan.push_back({(void**)&h->s.bterm, 16 * (size_t)NB * n});
     plan.push_back({(void**)&h->s.brk, 4 * n});
     plan.push_back({(void**)&h->s.flist, 4 * (size_t)FL_CAP * n});
     plan.push_back({(void**)&h->s.fcount, 4 * n});

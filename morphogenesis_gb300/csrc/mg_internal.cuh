@@ -129,6 +129,8 @@ struct Scratch {
     float* press;
     float* invdens;
     float4* force;
+    float4* bterm;      // [NB][cap] each own bond's acceleration on its partner in the last force
+                        // pass (x, y, z; w = the partner's index bits, UNDEF when not evaluated)
     uint32_t* brk;      // bonds that broke in the last force pass
     uint32_t* flist;    // [FL_CAP][cap] fluid-force neighbours found by the density pass
     uint32_t* fcount;   // [cap] their number (> FL_CAP: search again)

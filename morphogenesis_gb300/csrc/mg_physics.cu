@@ -1074,8 +1074,12 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
                                                const uint32_t* __restrict__ flist,
                                                const uint32_t* __restrict__ fcount, int use_list,
                                                float4* __restrict__ force,
+                                               float4* __restrict__ bterm,
                                                uint32_t* __restrict__ brk,
                                                const uint32_t* __restrict__ nactive_p) {
+    // First of the two force kernels: own bonds and fluid terms.  Each own bond's acceleration
+    // on its partner goes to bterm, where the second kernel gathers the partner's incoming
+    // reactions once every owner has written them.
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nact = *nactive_p;
     if (p >= nact) return;
@@ -1091,13 +1095,17 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
         load_record(rec, A, B);
         const uint32_t j = A.x;
         const float restlen = __uint_as_float(A.y);
-        if (j >= nact || restlen < REST_MIN) continue;
+        if (j >= nact || restlen < REST_MIN) {
+            bterm[(size_t)a * cap + p] = make_float4(0.f, 0.f, 0.f, __uint_as_float(UNDEF));
+            continue;
+        }
         const float elastlim = __uint_as_float(B.x);
         const BondTerm t = bond_term(ip, iv, C.pos[j], C.veval[j], restlen, __uint_as_float(A.z),
                                      __uint_as_float(A.w), elastlim, P.pmass);
         const float sq = __uint_as_float(B.z) + t.strain * t.strain;
         const float si = __uint_as_float(B.w) + t.strain;
         *reinterpret_cast<uint2*>(&rec[1].z) = make_uint2(__float_as_uint(sq), __float_as_uint(si));
+        bterm[(size_t)a * cap + p] = make_float4(t.ex, t.ey, t.ez, __uint_as_float(j));
         if (!is_nan3(t)) {
             fx = fx - t.ex;
             fy = fy - t.ey;
@@ -1161,46 +1169,53 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
         fy = fy + sy * P.pmass;
         fz = fz + sz * P.pmass;
     }
-    // reactions of incoming bonds, slot order (gather form of the atomicAdd at cuda:3311-3313)
-    {
-        const uint4* pi = reinterpret_cast<const uint4*>(C.pidx + (size_t)p * 12);
-        uint32_t in[12];
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            uint4 v = pi[k];
-            in[4 * k] = v.x; in[4 * k + 1] = v.y; in[4 * k + 2] = v.z; in[4 * k + 3] = v.w;
-        }
-#pragma unroll
-        for (int b = 0; b < NB; b++) {
-            const uint32_t k = in[2 * b], bk = in[2 * b + 1];
-            if (k >= nact || bk >= (uint32_t)NB) continue;
-            // the owner's record (its integrator words, which the owner's thread rewrites in
-            // this pass, are not used)
-            uint4 A, B;
-            load_record(C.bond + ((size_t)bk * cap + k) * 2, A, B);
-            if (A.x != p) continue;
-            const float restlen = __uint_as_float(A.y);
-            if (restlen < REST_MIN) continue;
-            const float elastlim = __uint_as_float(B.x);
-            const BondTerm t = bond_term(C.pos[k], C.veval[k], ip, iv, restlen,
-                                         __uint_as_float(A.z), __uint_as_float(A.w), elastlim,
-                                         P.pmass);
-            if (!is_nan3(t)) {
-                fx = fx + t.ex;
-                fy = fy + t.ey;
-                fz = fz + t.ez;
-            }
-        }
-    }
     force[p] = make_float4(fx, fy, fz, 0.f);
     brk[p] = br;
+}
+
+// Second force kernel: the reactions of incoming bonds, in slot order (the gather form of the
+// atomicAdd at cuda:3311-3313), added to the first kernel's sum.  An owner's stored term is the
+// one its own-bond loop evaluated for this particle as partner: the same arguments, the same
+// bits as evaluating it here.
+__global__ void __launch_bounds__(256) k_force_in(uint32_t cap, const uint32_t* __restrict__ pidx,
+                                                  const float4* __restrict__ bterm,
+                                                  float4* __restrict__ force,
+                                                  const uint32_t* __restrict__ nactive_p) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nact = *nactive_p;
+    if (p >= nact) return;
+    const uint4* pi = reinterpret_cast<const uint4*>(pidx + (size_t)p * 12);
+    uint32_t in[12];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const uint4 v = pi[k];
+        in[4 * k] = v.x; in[4 * k + 1] = v.y; in[4 * k + 2] = v.z; in[4 * k + 3] = v.w;
+    }
+    float4 t[NB];
+#pragma unroll
+    for (int b = 0; b < NB; b++) {  // all gathers in flight before the sums
+        const uint32_t k = in[2 * b], bk = in[2 * b + 1];
+        t[b] = (k < nact && bk < (uint32_t)NB) ? bterm[(size_t)bk * cap + k]
+                                                 : make_float4(0.f, 0.f, 0.f, __uint_as_float(UNDEF));
+    }
+    float4 f = force[p];
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+        if (__float_as_uint(t[b].w) != p) continue;  // the owner's slot no longer bonds to p
+        if (t[b].x != t[b].x || t[b].y != t[b].y || t[b].z != t[b].z) continue;
+        f.x = f.x + t[b].x;
+        f.y = f.y + t[b].y;
+        f.z = f.z + t[b].z;
+    }
+    force[p] = f;
 }
 
 void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool use_list,
                   cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
     k_force<<<blocks, 256, 0, st>>>(P, cur, s.scell, s.count, s.offset, s.press, s.invdens, s.flist,
-                                    s.fcount, use_list ? 1 : 0, s.force, s.brk, s.counters + 3);
+                                    s.fcount, use_list ? 1 : 0, s.force, s.bterm, s.brk, s.counters + 3);
+    k_force_in<<<blocks, 256, 0, st>>>(P.cap, cur.pidx, s.bterm, s.force, s.counters + 3);
 }
 
 // Broken bonds get rest length 0 (cuda:3315-3317).  The force kernel records the breaks in
