@@ -237,14 +237,23 @@ __global__ void k_col_stats(const float* __restrict__ d, uint64_t rows, int cols
 // =============================================================================================
 // Inference on tcgen05
 // =============================================================================================
-// One CTA per SM holding the weights once, with INF_GROUPS independent groups of eight warps,
-// each with its own 128-particle tile in flight (activation buffer, TMEM columns, mbarrier):
-// while one group runs its GELU epilogue the tensor core works on another group's layer.  In a
-// group, warp w reads TMEM lanes 32(w%4)..32(w%4)+31 (its tile rows) and, in the hidden-layer
-// epilogues, columns 64(w/4)..64(w/4)+63 of its group's 128.
-constexpr int INF_GROUPS = 3;
-constexpr int INF_GROUP_THREADS = 256;
+// One CTA per SM holding the weights once, with INF_GROUPS independent groups of warps, each
+// with its own 128-particle tile in flight (activation buffer, TMEM columns, mbarrier): while
+// one group runs its GELU epilogue the tensor core works on another group's layer.  In a group,
+// warp w reads TMEM lanes 32(w%4)..32(w%4)+31 (its tile rows) and, in the hidden-layer
+// epilogues, the w/4-th of the INF_SPLIT column ranges of its group's 128.
+#ifndef MG_INF_GROUPS
+#define MG_INF_GROUPS 4
+#endif
+#ifndef MG_INF_SPLIT
+#define MG_INF_SPLIT 2
+#endif
+constexpr int INF_GROUPS = MG_INF_GROUPS;
+constexpr int INF_SPLIT = MG_INF_SPLIT;                // threads per tile row (1 or 2)
+constexpr int INF_GROUP_THREADS = 128 * INF_SPLIT;
 constexpr int INF_THREADS = INF_GROUPS * INF_GROUP_THREADS;
+constexpr uint32_t INF_COLS = MLP_H / INF_SPLIT;       // hidden columns per thread
+static_assert(INF_GROUPS * 128 <= 512, "TMEM columns of the groups");
 constexpr int INF_TMEM_COLS = 512;  // allocation (power of two); groups use 128 columns each
 constexpr uint32_t MBAR_SPIN_LIMIT = 1u << 24;
 
@@ -488,12 +497,12 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
     for (uint32_t tile = blockIdx.x * INF_GROUPS + g; tile < ntiles; tile += gridDim.x * INF_GROUPS) {
         const uint32_t p = tile * 128u + row;
         const bool live = p < n;
-        // layer-1 operand: the particle's 48 bf16 features (zeros past the end), three of the
-        // six 16-byte chunks per thread
+        // layer-1 operand: the particle's 48 bf16 features (zeros past the end), 6 / INF_SPLIT
+        // of the six 16-byte chunks per thread
         {
             const uint4* src = reinterpret_cast<const uint4*>(feat + (size_t)p * MLP_IN);
 #pragma unroll
-            for (uint32_t c = half * 3; c < half * 3 + 3; c++) {
+            for (uint32_t c = half * (6 / INF_SPLIT); c < (half + 1) * (6 / INF_SPLIT); c++) {
                 const uint4 v = live ? src[c] : make_uint4(0u, 0u, 0u, 0u);
                 *reinterpret_cast<uint4*>(act + core_offset(row, c * 8, MLP_IN)) = v;
             }
@@ -512,7 +521,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         tc_fence_after();
         // layer-1 epilogue: bias + GELU -> layer-2 operand (layer 1 has finished with `act`)
 #pragma unroll
-        for (uint32_t c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
+        for (uint32_t c0 = half * INF_COLS; c0 < (half + 1) * INF_COLS; c0 += 32) {
             float v[32];
             tmem_ld32(lane_addr + c0, v);
 #pragma unroll
@@ -537,7 +546,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         tc_fence_after();
         // layer-2 epilogue -> layer-3 operand (layer 2 has finished reading `act`)
 #pragma unroll
-        for (uint32_t c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
+        for (uint32_t c0 = half * INF_COLS; c0 < (half + 1) * INF_COLS; c0 += 32) {
             float v[32];
             tmem_ld32(lane_addr + c0, v);
 #pragma unroll
