@@ -548,6 +548,19 @@ def _shape_of(fs, buf):
     return shape, dt
 
 
+def test_eight_cell_window_matches_oracle(built):
+    """gsrch 2 (the reference's own grid-search formula for a cell of 2h: offsets -1..0 per
+    axis): the warp search and the direct walk give the oracle's bits."""
+    d = demo.make_block(12, "R", seed=4)
+    d.params.grid_srch = 2
+    for mode in (1, 0):
+        g, o = pair(d, d.n)
+        g.set_option(A.OPT_NEIGHBOR_SEARCH, mode)
+        g.Run(5)
+        o.step(5)
+        assert compare(g, o), f"gsrch 2, search mode {mode}: not bitwise equal to the oracle"
+
+
 def test_special_particles_match_oracle(built):
     d = demo.make_block(10, "R", seed=9)
     d.params.actuation_factor = 0.05
