@@ -14,12 +14,13 @@
 // keep exactly that order, so they give identical bits:
 //  * direct: one thread per particle walks its gridAdjCnt cells (the reference loop);
 //  * warp search: the 32 particles of a warp walk the union of their cell windows together.
-//    Each chunk of 32 candidates is loaded once (one candidate per lane) and tested against
-//    the warp's bounding box grown by the search radius; survivors are broadcast in ascending
-//    order and every lane appends the ones inside its own radius and window to a per-lane
-//    list in shared memory.  The neighbour terms are then evaluated lane by lane over these
-//    lists, so no lane idles through a neighbour that belongs to another lane.  A lane whose
-//    list overflows (more than NL_CAP neighbours) falls back to the direct walk.
+//    Each chunk of 32 candidates is loaded once (one candidate per lane) and kept when it lies
+//    within the search radius of the box spanned by the group's particles; survivors are
+//    broadcast in ascending order and every lane appends the ones inside its own radius and
+//    window to a per-lane list in shared memory.  The neighbour terms are then evaluated lane
+//    by lane over these lists, so no lane idles through a neighbour that belongs to another
+//    lane.  A lane whose list overflows (more than NL_CAP neighbours) is queued for the
+//    overflow pass, one warp per queued particle.
 // The density pass also records each particle's fluid-force neighbours (dsq < 1) so the force
 // pass reads a short list instead of searching again.
 #include <cfloat>
