@@ -8,14 +8,16 @@
 // earlier-index particles in the same cell, i.e. a serial execution of insertParticles):
 //   insert   : cell of every particle, per-cell counts (warp-aggregated atomics) and an
 //              arrival rank that is only used to scatter indices into their cell's segment;
-//   scan     : single-pass exclusive scan with decoupled look-back -> per-cell offsets;
-//   place    : order[offset[cell] + arrival rank] = i;
+//   scan     : single-pass exclusive scan with decoupled look-back (a warp reads 32
+//              predecessor tiles per round) -> per-cell offsets;
+//   place    : order[offset[cell] + arrival rank] = i, with the (sub-cell code, i) key;
 //   cellsort : the stable rank of every particle in its cell (one thread per particle for
 //              cells <= 256 particles; block tier <= 8192, ordered stream compaction above),
 //              which yields sorted[] (sorted -> old) and newidx[] (old -> sorted), and the
 //              density pass's processing order work[];
 //   gather   : every carried field is gathered through sorted[], bond partners and incoming
-//              bond owners are remapped through newidx[].
+//              bond owners are remapped through newidx[] (in up to three kernels when parts
+//              of the state are still being uploaded).
 #include <cuda/atomic>
 #include <cfloat>
 #include "mg_internal.cuh"
