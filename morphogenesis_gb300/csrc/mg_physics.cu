@@ -525,10 +525,11 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
         // group: the lanes whose cell is the leader's cell or (group mode 0) the next cell of its
         // row (any lanes may share a search: each takes its own window cells in ascending
         // index, its adjacency order; the rule only keeps the group's box compact)
+        // (the next cell is in the leader's row unless the leader's cell ends the row: x = res - 1)
         const uint32_t span = P.group_mode == 0 ? 1u : 0u;
-        const uint32_t rowx = (uint32_t)P.res[0];
+        const bool row_next = __shfl_sync(0xffffffffu, win.x, leader) + 2 < P.res[0];
         const bool ing = act && ((remaining >> lane) & 1u) && pcell >= lcell && pcell - lcell <= span &&
-                         pcell / rowx == lcell / rowx;
+                         (pcell == lcell || row_next);
         remaining &= ~__ballot_sync(0xffffffffu, ing);
         // the group's particles span [t?0, t?1]; the search box is that span widened by Rf
         const float tx0 = warp_min(ing ? ip.x : INF), tx1 = warp_max(ing ? ip.x : -INF);

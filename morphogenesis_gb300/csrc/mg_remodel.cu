@@ -328,9 +328,11 @@ __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
         const int ncell = ncx * ncz * (wy1 - wy0 + 1);
         for (int cb = 0; cb < ncell; cb += 32) {
             const int t = cb + (int)lane;
-            uint32_t tcnt = 0, toff = 0;
+            uint32_t tcnt = 0, toff = 0, tpos = 0;  // tpos: the cell's offsets in the window
             if (t < ncell) {
-                const int cx = wx0 + t % ncx, cz = wz0 + (t / ncx) % ncz, cy = wy0 + t / (ncx * ncz);
+                const int ox = t % ncx, oz = (t / ncx) % ncz, oy = t / (ncx * ncz);
+                tpos = (uint32_t)ox | ((uint32_t)oy << 8) | ((uint32_t)oz << 16);
+                const int cx = wx0 + ox, cz = wz0 + oz, cy = wy0 + oy;
                 if (cx >= 0 && cy >= 0 && cz >= 0 && cx < P.res[0] && cy < P.res[1] && cz < P.res[2] &&
                     (!prune || cell_meets_box(P, cx, cy, cz, bx0, bx1, by0, by1, bz0, bz1))) {
                     const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
@@ -344,8 +346,9 @@ __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
                 ne &= ne - 1;
                 const uint32_t cnt = __shfl_sync(0xffffffffu, tcnt, src);
                 const uint32_t off = __shfl_sync(0xffffffffu, toff, src);
-                const int ts = cb + src;
-                const int cx = wx0 + ts % ncx, cz = wz0 + (ts / ncx) % ncz, cy = wy0 + ts / (ncx * ncz);
+                const uint32_t pos3 = __shfl_sync(0xffffffffu, tpos, src);
+                const int cx = wx0 + (int)(pos3 & 0xFFu), cy = wy0 + (int)((pos3 >> 8) & 0xFFu),
+                          cz = wz0 + (int)(pos3 >> 16);
                 const bool inw = ing && cx - win.x >= 0 && cx - win.x < g && cy - win.y >= 0 &&
                                  cy - win.y < g && cz - win.z >= 0 && cz - win.z < g;
                 if (!__any_sync(0xffffffffu, inw)) continue;
