@@ -148,6 +148,7 @@ void derive(DevParams& D, const mg_fparams& p, uint32_t cap) {
     for (int k = 0; k < 3; k++) {
         D.gmin[k] = p.grid_min[k];
         D.gdelta[k] = p.grid_delta[k];
+        D.gcell[k] = 1.f / p.grid_delta[k];
         D.res[k] = p.grid_res[k];
         D.scanmax[k] = p.grid_res[k] - p.grid_srch;
         D.bmin[k] = p.pboundmin[k];

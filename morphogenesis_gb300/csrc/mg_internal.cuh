@@ -55,6 +55,7 @@ enum : uint32_t {
 // Simulation parameters passed by value to every kernel (constant bank).
 struct DevParams {
     float gmin[3], gdelta[3];
+    float gcell[3];  // 1 / gdelta: a grid cell's extent per axis
     int res[3], scanmax[3];
     int adjcnt, nadj, gsrch;
     int adj[64];

@@ -310,13 +310,14 @@ __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
     const float Rf = sqrtf(P.r2diff) * 1.0001f + 1e-3f;
     const int g = P.gsrch;
     const int BIG = 1 << 30;
-    const uint32_t rowx = (uint32_t)P.res[0];
     unsigned remaining = __ballot_sync(0xffffffffu, need);
     while (remaining) {
         const int leader = __ffs(remaining) - 1;
         const uint32_t lcell = __shfl_sync(0xffffffffu, pcell, leader);
+        // the next cell is in the leader's row unless the leader's cell ends the row
+        const bool row_next = __shfl_sync(0xffffffffu, win.x, leader) + 2 < P.res[0];
         const bool ing = need && ((remaining >> lane) & 1u) && pcell >= lcell && pcell - lcell <= 1u &&
-                         pcell / rowx == lcell / rowx;
+                         (pcell == lcell || row_next);
         remaining &= ~__ballot_sync(0xffffffffu, ing);
         const float bx0 = warp_min(ing ? ip.x : INF) - Rf, bx1 = warp_max(ing ? ip.x : -INF) + Rf;
         const float by0 = warp_min(ing ? ip.y : INF) - Rf, by1 = warp_max(ing ? ip.y : -INF) + Rf;

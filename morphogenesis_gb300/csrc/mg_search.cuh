@@ -43,7 +43,7 @@ __device__ __forceinline__ float approx_dsq(float4 a, float4 b) {
 __device__ __forceinline__ bool cell_meets_box(const DevParams& P, int cx, int cy, int cz,
                                                float bx0, float bx1, float by0, float by1,
                                                float bz0, float bz1) {
-    const float sx = 1.f / P.gdelta[0], sy = 1.f / P.gdelta[1], sz = 1.f / P.gdelta[2];
+    const float sx = P.gcell[0], sy = P.gcell[1], sz = P.gcell[2];
     const float x0 = P.gmin[0] + ((float)cx - 0.01f) * sx, x1 = P.gmin[0] + ((float)cx + 1.01f) * sx;
     const float y0 = P.gmin[1] + ((float)cy - 0.01f) * sy, y1 = P.gmin[1] + ((float)cy + 1.01f) * sy;
     const float z0 = P.gmin[2] + ((float)cz - 0.01f) * sz, z1 = P.gmin[2] + ((float)cz + 1.01f) * sz;
