@@ -51,6 +51,7 @@ struct mg_system {
     mg_genome genome{};
     DevParams P{};
     DevGenome* dG = nullptr;
+    DevGenome hG{};  // host copy of *dG (the warp density pass takes the genome as a parameter)
     uint32_t cap = 0;
     void* arena = nullptr;
     size_t arena_bytes = 0;
@@ -283,6 +284,8 @@ mg_status upload_genome(mg_system* h) {
     for (int t = 1; t < NTF; t++) uniform &= g.diff[t] == g.diff[0];
     if (h->P.uniform_diff != uniform) clear_graphs(h);
     h->P.uniform_diff = uniform;
+    h->hG = g;
+    clear_graphs(h);  // captured density launches hold the genome by value
     MG_CUDA(h, cudaMemcpyAsync(h->dG, &g, sizeof(g), cudaMemcpyHostToDevice, h->stream));
     MG_CUDA(h, cudaStreamSynchronize(h->stream));
     return MG_OK;
@@ -417,7 +420,7 @@ void enqueue_dens(mg_system* h, int flags, bool prof, bool heal_list = false) {
         X.hlist = h->hmem + h->cap;
     }
     { Mark m(h, prof, flags == 1 ? "pressure" : flags == 7 ? "density_diffusion_genes" : "diffusion_genes");
-      launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, flags,
+      launch_dens(h->P, h->dG, h->hG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, flags,
                   h->drifted && h->search ? 3 : h->search, h->num_sms, h->stream, &X); }
     if (flags & 6) h->conc_cur = cout;
     if (h->search && (flags & 3)) h->flist_valid = true;
@@ -492,7 +495,7 @@ void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof, bool hea
     const int cin = h->conc_cur, cout = 1 - h->conc_cur;
     const int dflags = (density ? 1 : 0) | 2 | 4 | 8 | 32;
     { Mark m(h, prof, density ? "density_features" : "features");
-      launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, dflags,
+      launch_dens(h->P, h->dG, h->hG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, dflags,
                   h->search, h->num_sms, h->stream, &X); }
     if (h->search) h->flist_valid = true;
     { Mark m(h, prof, "mlp_infer");
@@ -1785,7 +1788,7 @@ mg_status mg_dataset_capture(mg_dataset d, mg_handle h, uint32_t flags) {
     X.cap_x = d->dx + d->size * mg::MLP_IN;
     X.cap_y = d->dy + d->size * mg::MLP_OUT;
     const int cin = h->conc_cur, cout = 1 - h->conc_cur;
-    launch_dens(h->P, h->dG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, 1 | 2 | 4 | 16,
+    launch_dens(h->P, h->dG, h->hG, h->set[h->cur], conc_of(h, cin), conc_of(h, cout), h->s, 1 | 2 | 4 | 16,
                 h->search, h->num_sms, h->stream, &X);
     h->conc_cur = cout;
     h->flist_valid = h->search != 0;

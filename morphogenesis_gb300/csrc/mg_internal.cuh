@@ -195,7 +195,9 @@ struct DensExtra {
     uint32_t* hlist;
     uint32_t* hcount;
 };
-void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
+// G: the genome in device memory; Gh: its host copy, passed by value to the warp search so
+// its uniform reads go through the constant cache
+void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, const Carried& cur, const float* conc_in,
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
                  cudaStream_t st, const DensExtra* extra = nullptr);
 

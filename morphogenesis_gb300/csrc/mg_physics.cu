@@ -66,6 +66,16 @@ constexpr uint32_t FLIST_CELL_START = 0x80000000u;
 #ifndef MG_ROW_V8
 #define MG_ROW_V8 1
 #endif
+#ifndef MG_DENS_GENOME_BY_VALUE
+#define MG_DENS_GENOME_BY_VALUE 1
+#endif
+#if MG_DENS_GENOME_BY_VALUE
+#define MG_DENS_GENOME_PARAM const __grid_constant__ DevGenome Gv
+#define MG_DENS_GENOME_ARG Gh
+#else
+#define MG_DENS_GENOME_PARAM const DevGenome* __restrict__ G
+#define MG_DENS_GENOME_ARG G
+#endif
 #ifndef MG_F32X2
 #define MG_F32X2 1
 #endif
@@ -477,7 +487,7 @@ __device__ __forceinline__ void dens_list_finish(
 
 template <int FLAGS>
 __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_warp(
-    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
+    DevParams P, MG_DENS_GENOME_PARAM, const float4* __restrict__ pos,
     const float* __restrict__ conc_in, float* __restrict__ conc_out,
     const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
@@ -488,6 +498,9 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     // prune: the positions are those of the last sort, so a window cell whose geometric box
     // misses the group's box holds no candidate; after positions moved, every cell is walked
     using F = DF<FLAGS>;
+#if MG_DENS_GENOME_BY_VALUE
+    const DevGenome* __restrict__ G = &Gv;  // the parameter itself: reads go to the constant bank
+#endif
     extern __shared__ uint32_t s_list[];  // [warps of the block][NL_CAP][32]
     __shared__ float4 s_sp[DENS_WARPS][32];  // staged survivors: x, y, z, sorted index (bits)
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
@@ -949,7 +962,7 @@ cudaError_t physics_init() {
     return e;
 }
 
-void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, const float* conc_in,
+void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, const Carried& cur, const float* conc_in,
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
                  cudaStream_t st, const DensExtra* extra) {
     DensExtra X = extra ? *extra : DensExtra{};
@@ -961,7 +974,7 @@ void launch_dens(const DevParams& P, const DevGenome* G, const Carried& cur, con
         const bool prune = search == 1;
 #define MG_DENSW_CASE(F)                                                                          \
     case F:                                                                                       \
-        k_dens_warp<F><<<blocks, warps * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,        \
+        k_dens_warp<F><<<blocks, warps * 32, smem, st>>>(P, MG_DENS_GENOME_ARG, cur.pos, conc_in, conc_out, \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.counters + 3,   \
