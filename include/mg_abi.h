@@ -443,7 +443,8 @@ mg_status mg_write_points_vtp(const char* dir, int32_t frame, const mg_points* p
 /* A batch steps many independent systems together (each keeps its own particles, grid,
  * parameters and genome): one CUDA graph launch per step advances every member, the members'
  * kernels running concurrently.  Members must live on one device, must not be profiling, and
- * must outlive the batch; their own streams wait for the batch's steps. */
+ * must outlive the batch; their own streams wait for the batch's steps.  Changes to a member's
+ * parameters, genome or options apply from the next batch step (its steps are captured anew). */
 typedef struct mg_batch_s* mg_batch;
 mg_status mg_batch_create(const mg_handle* members, uint32_t count, mg_batch* out);
 mg_status mg_batch_destroy(mg_batch b);

@@ -52,6 +52,9 @@ struct mg_system {
     DevParams P{};
     DevGenome* dG = nullptr;
     DevGenome hG{};  // host copy of *dG (the warp density pass takes the genome as a parameter)
+    // incremented whenever the captured steps go stale (parameters, genome, options): batches
+    // that hold this handle's steps rebuild theirs
+    uint64_t graph_epoch = 0;
     uint32_t cap = 0;
     void* arena = nullptr;
     size_t arena_bytes = 0;
@@ -292,6 +295,7 @@ mg_status upload_genome(mg_system* h) {
 }
 
 void clear_graphs(mg_system* h) {
+    h->graph_epoch++;
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
     for (auto& kv : h->io_graphs) cudaGraphExecDestroy(kv.second);
@@ -2022,7 +2026,10 @@ mg_status mg_batch_destroy(mg_batch b) {
 
 static mg_status batch_graph(mg_batch b, uint32_t flags, cudaGraphExec_t* out) {
     std::string key = std::to_string(flags) + ":";
-    for (mg_system* h : b->hs) key += (char)('0' + 2 * h->cur + h->conc_cur);
+    for (mg_system* h : b->hs) {
+        key += (char)('0' + 2 * h->cur + h->conc_cur);
+        key += std::to_string(h->graph_epoch) + ",";  // a member changed since: capture anew
+    }
     auto it = b->graphs.find(key);
     if (it != b->graphs.end()) {
         for (mg_system* h : b->hs) advance_state(h, flags);
