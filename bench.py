@@ -187,6 +187,26 @@ def cpu_reference(steps: int, warmup: int, threads: int):
     return d.n * steps / dt, used, dt
 
 
+def fp64_section(d, steps: int = 2):
+    """Each FP32 field of the GPU result after `steps` steps of the workload against the FP64
+    oracle (the checker) run from the same inputs; particles matched by id."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+    import morphogenesis_gb300 as mg
+
+    g = mg.FluidSystem(d.params, d.genome, d.n)
+    g.TransferToCL(d.arrays)
+    g.Run(steps)
+    o64 = orc.Oracle(d.params, d.genome, d.n, 64)
+    o64.upload_all(d.arrays)
+    o64.step(steps)
+    rep = orc.fp64_error_report(g.download, o64)
+    g.close()
+    o64.close()
+    return {"steps": steps, "against": "FP64 oracle, same inputs, particles matched by id",
+            "fields": rep}
+
+
 def surrogate_section(args, peak_tflops):
     """Learned morphogen surrogate at 1,048,576 particles: trained on 2^24 (state, increment)
     pairs captured from plain runs under 8 seeds, then compared with the plain morphogen stage
@@ -473,6 +493,9 @@ def main():
         cpu = {"value": cval, "unit": UNIT, "cores": used, "kind": "port",
                "sample": f"{args.cpu_steps} steps of the same 1,048,576-particle workload ({cdt:.1f} s)"}
     fs.close()
+    fp64 = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        fp64 = fp64_section(d, 2)
 
     sur = None
     large = None
@@ -509,6 +532,7 @@ def main():
                               "frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak},
             "kernels_ms_per_launch": {k: v[1] / v[0] for k, v in prof.items()},
             "cpu_baseline": cpu,
+            "fp64_error": fp64,
             "surrogate": sur,
             "batch": batch,
             "large": large,

@@ -6,11 +6,15 @@
  * (src/host_CUDA.cpp, src/fluid_system.cpp), used by tests/, by smoke() and by the
  * CPU-baseline leg of bench.py as the checker.  It is never linked into the product.
  *
- * Parity status: UNPINNED by the reference itself.  The reference ships no tests, no golden
- * vectors and no fixtures that parse with its own readers, and its compute path does not
- * build here (fluid_system_cuda.cu needs <CL/cl.h>; the OpenCL host needs jsoncpp/VTK/an ICD).
- * The restatement is pinned instead by known-answer tests hand-derived from the reference
- * formulas (tests/golden/).
+ * Parity status: pinned by the reference's own kernels.  The reference ships no tests or golden
+ * vectors and its compute path does not build as a program here (fluid_system_cuda.cu needs
+ * <CL/cl.h>; the OpenCL host needs jsoncpp/VTK/an ICD), but its insertParticles,
+ * countingSortFull, computePressure, computeForce, computeDiffusion and advanceParticles compile
+ * as host C++ against stand-ins for the OpenCL/CUDA headers (oracle/ref_harness.cpp, built into
+ * oracle/_ref/).  The tests compare this restatement with them stage by stage (bit-exact except
+ * the force sums, D2) and keep their outputs as golden vectors (tests/golden/ref_pins.json).
+ * The gene reaction (D3) and bond re-forming (D5, D12) differ from the reference by design and
+ * are pinned by known-answer tests hand-derived from the reference formulas (tests/golden/).
  *
  * The same source builds twice: MGO_REAL=float (liboracle_f32, expression order of the
  * reference kernels, no FMA contraction) and MGO_REAL=double (liboracle_f64, the "FP64 host

@@ -1,9 +1,13 @@
 """ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, and
-only as the checker or the timed CPU reference.  Parity status: unpinned by the reference
-(it ships no tests or golden vectors and its compute path does not build); pinned by the
-hand-derived known-answer tests in tests/golden/.
+only as the checker or the timed CPU reference.  Parity status: pinned by the reference's own
+kernels.  RefKernels runs the reference's insertParticles, countingSortFull, computePressure,
+computeForce, computeDiffusion and advanceParticles compiled as host C++ from the reference
+sources (oracle/ref_harness.cpp); tests/test_ref_pin.py compares the oracle with them stage by
+stage, and tests/golden/ref_pins.json holds their outputs for machines without the sources.
+The gene reaction (D3) and the remodelling decisions (D5, D12) are pinned by the hand-derived
+known-answer tests in tests/golden/ only.
 """
 from __future__ import annotations
 
@@ -184,3 +188,111 @@ class Oracle:
 
 def set_threads(n: int, bits: int = 32) -> int:
     return lib(bits).mgo_set_threads(n)
+
+
+FP64_FIELDS = {"FPOS": A.FPOS, "FVEL": A.FVEL, "FVEVAL": A.FVEVAL, "FFORCE": A.FFORCE,
+               "FPRESS": A.FPRESS, "FDENSITY": A.FDENSITY, "FCONC": A.FCONC}
+
+
+def fp64_error_report(download, o64: "Oracle") -> dict:
+    """Per-field error of an FP32 result against the FP64 oracle run of the same steps.
+
+    `download(buf)` returns the FP32 result's buffer in the reference layout (GPU or FP32
+    oracle); `o64` is an Oracle built with bits=64 that ran the same steps from the same
+    inputs.  Particles are matched by FPARTICLE_ID, so a particle binned differently in double
+    precision is still compared with itself.  Per field (fields written by computePressure,
+    computeForce and advanceParticles, fluid_system_cuda.cu:620-712, 3167-3358, 3470-3614, and
+    FCONC by computeDiffusion/computeGeneAction): rel_l2 = |x - y|_2 / |y|_2, rel_max =
+    max|x - y| / max|y|, rel_median = median |x - y| / (|y| + 1e-6 max|y|).  The w word of the
+    float4 fields is not compared.
+    """
+    ida = np.asarray(download(A.FPARTICLE_ID))
+    idb = o64.download(A.FPARTICLE_ID)
+    pa = np.argsort(ida, kind="stable")
+    pb = np.argsort(idb, kind="stable")
+    if not np.array_equal(ida[pa], idb[pb]):
+        raise AssertionError("the FP32 result and the FP64 oracle hold different particles")
+    out = {}
+    for name, buf in FP64_FIELDS.items():
+        x = np.asarray(download(buf), np.float64)[pa]
+        y = o64.download_f64(buf)[pb]
+        if x.ndim == 2 and x.shape[1] == 4:
+            x, y = x[:, :3], y[:, :3]
+        d = np.abs(x - y)
+        s = float(np.abs(y).max()) if y.size else 0.0
+        ny = float(np.linalg.norm(y))
+        out[name] = {"rel_l2": float(np.linalg.norm(x - y) / ny) if ny > 0 else float(np.linalg.norm(x - y)),
+                     "rel_max": float(d.max() / s) if s > 0 else float(d.max()),
+                     "rel_median": float(np.median(d / (np.abs(y) + 1e-6 * s))) if s > 0 else float(np.median(d))}
+    return out
+
+
+REF_LIB = HERE / "_ref" / "libmg_ref.so"
+REF_SRC = Path("/root/reference/Morphogenesis/src")
+
+
+def build_ref() -> bool:
+    """Builds the pinning harness (the reference's kernels as host C++, oracle/ref_harness.cpp)
+    when the reference sources are present; returns whether the library exists."""
+    if (REF_SRC / "fluid_system_cuda.cu").exists():
+        r = subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_SRC={REF_SRC}"],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference harness build failed:\n" + r.stdout + r.stderr)
+    return REF_LIB.exists()
+
+
+class RefKernels:
+    """The reference's own insertParticles, countingSortFull, computePressure, computeForce,
+    computeDiffusion and advanceParticles run serially on the host (oracle/ref_harness.cpp),
+    with the buffer exchange of Oracle.  One instance at a time (the kernels use globals)."""
+
+    _lib = None
+
+    def __init__(self, params: A.FParams, genome: A.Genome, max_points: int):
+        if RefKernels._lib is None:
+            L = C.CDLL(str(REF_LIB))
+            for name, res, args in (
+                    ("mgr_create", C.c_int, [C.POINTER(A.FParams), C.POINTER(A.Genome), C.c_uint32]),
+                    ("mgr_import", C.c_int, [C.c_int32, C.c_void_p, C.c_size_t]),
+                    ("mgr_export", C.c_int, [C.c_int32, C.c_void_p, C.c_size_t]),
+                    ("mgr_insert", None, []), ("mgr_scan", None, []), ("mgr_sort", None, []),
+                    ("mgr_pressure", None, []), ("mgr_force", None, [C.c_int]),
+                    ("mgr_diffusion", None, []),
+                    ("mgr_advance", None, [C.c_float, C.c_float, C.c_float])):
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            RefKernels._lib = L
+        self.L = RefKernels._lib
+        self.n = max_points
+        self.cells = params.grid_total
+        self.params = params
+        self.L.mgr_create(C.byref(params), C.byref(genome), max_points)
+
+    def upload(self, buf: int, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr)
+        if self.L.mgr_import(buf, a.ctypes.data, a.nbytes):
+            raise RuntimeError(f"mgr_import({buf}) failed")
+
+    def upload_all(self, arrays: dict) -> None:
+        for k, v in arrays.items():
+            self.upload(k, v)
+
+    def download(self, buf: int) -> np.ndarray:
+        dt, shape = buffer_shape(buf, self.n, self.cells)
+        out = np.empty(shape, dt)
+        if self.L.mgr_export(buf, out.ctypes.data, out.nbytes):
+            raise RuntimeError(f"mgr_export({buf}) failed")
+        return out
+
+    def insert(self): self.L.mgr_insert()
+    def prefix_sum(self): self.L.mgr_scan()
+    def sort(self): self.L.mgr_sort()
+    def pressure(self): self.L.mgr_pressure()
+    def force(self, freeze: bool = False): self.L.mgr_force(int(freeze))
+    def diffusion(self): self.L.mgr_diffusion()
+
+    def advance(self, time: float):
+        p = self.params
+        self.L.mgr_advance(time, p.dt, p.psimscale)
