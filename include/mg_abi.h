@@ -452,6 +452,17 @@ mg_status mg_batch_step(mg_batch b, uint32_t nsteps, uint32_t flags);
 /* nsteps batch steps, device time of the whole run (CUDA events on the batch stream) */
 mg_status mg_batch_time_steps(mg_batch b, uint32_t nsteps, uint32_t flags, float* ms);
 
+/* ---- failure-detection self-test (no counterpart in the reference) ------------------------- */
+/* Runs one bounded device-side wait against a flag that nothing sets, on buffers of its own,
+ * and reports whether the wait gave up as designed.  which = 0: the prefix sum's look-back
+ * (a scan whose first tile is never launched); which = 1: the surrogate inference's
+ * tensor-core completion wait (an inference CTA whose MMAs are withheld; the CTA then frees
+ * its tensor memory).  spin_limit: polls before giving up (1 .. 1048576).  Returns
+ * MG_ERR_DEVICE_TIMEOUT when the wait gave up (the expected result, the same status a step
+ * returns when one of these waits runs out), MG_OK if it did not, MG_ERR_CUDA on a CUDA error.
+ * The CUDA context stays usable either way.  Uses the current device and synchronises. */
+mg_status mg_selftest_bounded_wait(int32_t which, uint32_t spin_limit);
+
 /* ---- allocation-free prefix sum (no counterpart in the reference) ------------------------ */
 /* Largest n mg_prefix_sum_noalloc accepts: 16384 tiles of 4096 elements. */
 #define MG_NOALLOC_SCAN_MAX 67108864ull
@@ -466,7 +477,9 @@ mg_status mg_batch_time_steps(mg_batch b, uint32_t nsteps, uint32_t flags, float
  *   n                0 .. MG_NOALLOC_SCAN_MAX; larger n is rejected with MG_ERR_INVALID_ARG
  *   total            optional device uint32 receiving the sum of all n counts
  *   error            optional device uint32 the caller has zeroed; bit 0 is set if a bounded
- *                    look-back wait gave up (the offsets are then invalid)
+ *                    look-back wait gave up (the offsets are then invalid).  With error NULL such
+ *                    a timeout goes unreported: the call still returns MG_OK (it does not wait for
+ *                    the scan), so pass an error word wherever a timeout must be detected
  *   stream           a cudaStream_t passed as void* (NULL: the default stream); the call is
  *                    asynchronous on it and uses the current device
  * The first call on each device looks up the scratch address (a one-time set-up); make that

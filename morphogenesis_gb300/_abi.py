@@ -48,6 +48,8 @@ P_COUNT = P_B3 + MLP_OUT
 NORM_COUNT = 2 * MLP_IN + 2 * MLP_OUT
 
 MG_OK = 0
+MG_OK, MG_ERR_INVALID_ARG, MG_ERR_OOM, MG_ERR_GRID_OVERFLOW, MG_ERR_LIST_OVERFLOW = 0, 1, 2, 3, 4
+MG_ERR_DEVICE_TIMEOUT, MG_ERR_CUDA, MG_ERR_UNSUPPORTED, MG_ERR_INCONSISTENT = 5, 6, 7, 8
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "GRID_OVERFLOW", 4: "LIST_OVERFLOW",
                 5: "DEVICE_TIMEOUT", 6: "CUDA_ERROR", 7: "UNSUPPORTED", 8: "INCONSISTENT"}
 
@@ -212,6 +214,7 @@ SIGNATURES = [
     ("mg_batch_step", C.c_int, [H, C.c_uint32, C.c_uint32]),
     ("mg_batch_time_steps", C.c_int, [H, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]),
     ("mg_prefix_sum_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("mg_selftest_bounded_wait", C.c_int, [C.c_int32, C.c_uint32]),
 ]
 
 _lib = None

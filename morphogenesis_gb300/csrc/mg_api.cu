@@ -115,6 +115,9 @@ struct mg_batch_s {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     std::map<std::string, cudaGraphExec_t> graphs;
+    // members' capture epochs the cached graphs were made for: when one changes, every cached
+    // graph holds stale parameters or genomes and is destroyed
+    std::vector<uint64_t> epochs;
     std::string err;
 };
 
@@ -721,6 +724,12 @@ void advance_state(mg_system* h, uint32_t flags) {
     h->cur = 1 - h->cur;
     h->conc_cur = 1 - conc0;
     if (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)) h->conc_cur = conc0;
+}
+
+// The inverse of advance_state (a step whose graph was not launched).
+void undo_state(mg_system* h, uint32_t flags) {
+    h->cur = 1 - h->cur;
+    if (!(flags & (MG_STEP_GENES | MG_STEP_SURROGATE))) h->conc_cur = 1 - h->conc_cur;
 }
 
 // Bookkeeping of a handle after nsteps graph steps (the same as run_steps does).
@@ -1991,7 +2000,31 @@ mg_status mg_set_tuning(mg_handle h, const int32_t* choice) {
     return MG_OK;
 }
 
+// ---- failure-detection self-test ---------------------------------------------------------------
+mg_status mg_selftest_bounded_wait(int32_t which, uint32_t spin_limit) {
+    if ((which != 0 && which != 1) || spin_limit == 0 || spin_limit > (1u << 20))
+        return fail(nullptr, MG_ERR_INVALID_ARG, "mg_selftest_bounded_wait: which must be 0 or 1, spin_limit 1 .. 1048576");
+    cudaStream_t st = nullptr;
+    MG_CUDA(nullptr, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    uint32_t bits = 0;
+    cudaError_t e = which == 0 ? mg::scan_selftest_wait_timeout(spin_limit, &bits, st)
+                               : mg::mlp_selftest_wait_timeout(spin_limit, &bits, st);
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "mg_selftest_bounded_wait");
+    const uint32_t expect = which == 0 ? (uint32_t)ERR_SCAN_TIMEOUT : (uint32_t)mg::MLP_ERR_MBAR_TIMEOUT;
+    if (bits & expect)
+        return fail(nullptr, MG_ERR_DEVICE_TIMEOUT,
+                    which == 0 ? "self-test: prefix-sum look-back gave up waiting (bounded spin)"
+                               : "self-test: tensor-core completion wait gave up (bounded spin)");
+    return MG_OK;
+}
+
 // ---- batched instances -----------------------------------------------------------------------
+static void batch_clear_graphs(mg_batch b) {
+    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+}
+
 mg_status mg_batch_create(const mg_handle* hs, uint32_t count, mg_batch* out) {
     if (!hs || !out || count == 0) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_batch_create: bad arguments");
     for (uint32_t k = 0; k < count; k++) {
@@ -2017,7 +2050,7 @@ mg_status mg_batch_create(const mg_handle* hs, uint32_t count, mg_batch* out) {
 mg_status mg_batch_destroy(mg_batch b) {
     if (!b) return MG_OK;
     cudaStreamSynchronize(b->stream);
-    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    batch_clear_graphs(b);
     cudaEventDestroy(b->done);
     cudaStreamDestroy(b->stream);
     delete b;
@@ -2025,11 +2058,14 @@ mg_status mg_batch_destroy(mg_batch b) {
 }
 
 static mg_status batch_graph(mg_batch b, uint32_t flags, cudaGraphExec_t* out) {
-    std::string key = std::to_string(flags) + ":";
-    for (mg_system* h : b->hs) {
-        key += (char)('0' + 2 * h->cur + h->conc_cur);
-        key += std::to_string(h->graph_epoch) + ",";  // a member changed since: capture anew
+    std::vector<uint64_t> epochs;
+    for (mg_system* h : b->hs) epochs.push_back(h->graph_epoch);
+    if (epochs != b->epochs) {  // a member changed since the cached graphs were captured
+        batch_clear_graphs(b);
+        b->epochs = epochs;
     }
+    std::string key = std::to_string(flags) + ":";
+    for (mg_system* h : b->hs) key += (char)('0' + 2 * h->cur + h->conc_cur);
     auto it = b->graphs.find(key);
     if (it != b->graphs.end()) {
         for (mg_system* h : b->hs) advance_state(h, flags);
@@ -2044,6 +2080,14 @@ static mg_status batch_graph(mg_batch b, uint32_t flags, cudaGraphExec_t* out) {
     // particles take 11x the time of 64; groups of 32 were fastest among 16-256).
     cudaGraphNode_t join = nullptr;
     std::vector<cudaGraphNode_t> group;
+    std::vector<std::pair<int, int>> state0;  // members' buffer states before the capture
+    for (mg_system* h : b->hs) state0.emplace_back(h->cur, h->conc_cur);
+    auto restore = [&] {
+        for (size_t k = 0; k < b->hs.size(); k++) {
+            b->hs[k]->cur = state0[k].first;
+            b->hs[k]->conc_cur = state0[k].second;
+        }
+    };
     size_t m = 0;
     for (mg_system* h : b->hs) {
         if (group.size() == (size_t)MG_BATCH_GROUP) {
@@ -2051,6 +2095,7 @@ static mg_status batch_graph(mg_batch b, uint32_t flags, cudaGraphExec_t* out) {
             cudaError_t e = cudaGraphAddEmptyNode(&j, bg, group.data(), group.size());
             if (e != cudaSuccess) {
                 cudaGraphDestroy(bg);
+                restore();
                 return cuda_fail(nullptr, e, "batch group join");
             }
             join = j;
@@ -2073,13 +2118,17 @@ static mg_status batch_graph(mg_batch b, uint32_t flags, cudaGraphExec_t* out) {
         if (g) cudaGraphDestroy(g);
         if (e != cudaSuccess) {
             cudaGraphDestroy(bg);
+            restore();
             return cuda_fail(h, e, "batch step capture");
         }
     }
     cudaGraphExec_t ge = nullptr;
     cudaError_t e = cudaGraphInstantiate(&ge, bg, 0);
     cudaGraphDestroy(bg);
-    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGraphInstantiate (batch)");
+    if (e != cudaSuccess) {
+        restore();
+        return cuda_fail(nullptr, e, "cudaGraphInstantiate (batch)");
+    }
     b->graphs[key] = ge;
     *out = ge;
     return MG_OK;
@@ -2100,12 +2149,18 @@ static mg_status batch_run(mg_batch b, uint32_t nsteps, uint32_t flags, float* m
         MG_CUDA(nullptr, cudaEventRecord(a, b->stream));
     }
     mg_status st = MG_OK;
+    uint32_t launched = 0;  // steps whose graph was launched
     for (uint32_t s = 0; s < nsteps && st == MG_OK; s++) {
         cudaGraphExec_t ge = nullptr;
         st = batch_graph(b, flags, &ge);
         if (st == MG_OK) {
             cudaError_t e = cudaGraphLaunch(ge, b->stream);
-            if (e != cudaSuccess) st = cuda_fail(nullptr, e, "cudaGraphLaunch (batch)");
+            if (e != cudaSuccess) {
+                st = cuda_fail(nullptr, e, "cudaGraphLaunch (batch)");
+                for (mg_system* h : b->hs) undo_state(h, flags);  // the step did not run
+            } else {
+                launched++;
+            }
         }
     }
     if (ms) {
@@ -2121,7 +2176,7 @@ static mg_status batch_run(mg_batch b, uint32_t nsteps, uint32_t flags, float* m
     cudaEventRecord(b->done, b->stream);
     for (mg_system* h : b->hs) {
         cudaStreamWaitEvent(h->stream, b->done, 0);
-        after_steps(h, nsteps, flags);
+        if (launched) after_steps(h, launched, flags);
     }
     if (st != MG_OK) return st;
     for (mg_system* h : b->hs) {

@@ -160,6 +160,8 @@ void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, boo
 void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long long* status,
                  uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st);
 size_t scan_status_words(uint32_t n);
+// failure-detection self-tests: a bounded wait on a flag nothing sets (see the definitions)
+cudaError_t scan_selftest_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, cudaStream_t st);
 void launch_place(const DevParams& P, const Scratch& s, cudaStream_t st);
 // subcounts: also count each cell's 2x2x2 sub-cells (for the per-lane fine-cell search)
 void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, bool subcounts,

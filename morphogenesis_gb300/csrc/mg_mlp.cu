@@ -311,8 +311,8 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar_saddr) {
 }
 
 // Bounded parity wait; returns false when the wait gave up.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar_saddr, uint32_t parity) {
-    for (uint32_t it = 0; it < MBAR_SPIN_LIMIT; it++) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar_saddr, uint32_t parity, uint32_t limit) {
+    for (uint32_t it = 0; it < limit; it++) {
         uint32_t done = 0;
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -440,7 +440,9 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
     const float* __restrict__ conc_plain, float* conc_out, uint32_t* __restrict__ genes,
     const uint32_t* __restrict__ nactive_p, uint32_t ntotal_override, const uint32_t* __restrict__ step_p,
     uint32_t judge_period, uint32_t judge_stride, float threshold, uint32_t* __restrict__ stats,
-    uint32_t* __restrict__ err) {
+    uint32_t* __restrict__ err, uint32_t spin_limit, uint32_t withhold) {
+    // spin_limit bounds every completion wait; withhold != 0 (failure-detection self-test
+    // only) issues no MMA, so the first wait runs out
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
@@ -511,11 +513,11 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         tc_fence_before();
         group_sync(g);
         tc_fence_after();
-        if (gtid == 0) {
+        if (gtid == 0 && !withhold) {
             issue_layer(tmem, act, S.w1, MLP_IN, MLP_H);
             mma_commit(mbar);
         }
-        ok = group_and(g, mbar_wait(mbar, phase));
+        ok = group_and(g, mbar_wait(mbar, phase, spin_limit));
         phase ^= 1u;
         if (!ok) break;
         tc_fence_after();
@@ -536,11 +538,11 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         tc_fence_before();
         group_sync(g);
         tc_fence_after();
-        if (gtid == 0) {
+        if (gtid == 0 && !withhold) {
             issue_layer(tmem, act, S.w2, MLP_H, MLP_H);
             mma_commit(mbar);
         }
-        ok = group_and(g, mbar_wait(mbar, phase));
+        ok = group_and(g, mbar_wait(mbar, phase, spin_limit));
         phase ^= 1u;
         if (!ok) break;
         tc_fence_after();
@@ -560,11 +562,11 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         tc_fence_before();
         group_sync(g);
         tc_fence_after();
-        if (gtid == 0) {
+        if (gtid == 0 && !withhold) {
             issue_layer(tmem, act, S.w3, MLP_H, MLP_OUT);
             mma_commit(mbar);
         }
-        ok = group_and(g, mbar_wait(mbar, phase));
+        ok = group_and(g, mbar_wait(mbar, phase, spin_limit));
         phase ^= 1u;
         if (!ok) break;
         tc_fence_after();
@@ -635,7 +637,7 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         // before the tensor memory is released
         if (gtid == 0) {
             atomicOr(err, MLP_ERR_MBAR_TIMEOUT);
-            mbar_wait(mbar, phase ^ 1u);
+            mbar_wait(mbar, phase ^ 1u, spin_limit);
         }
     }
     tc_fence_before();
@@ -933,7 +935,40 @@ void launch_mlp_infer(const Mlp* m, const bf16* feat, const float* feat_scale, c
     k_mlp_infer<<<num_sms, INF_THREADS, sizeof(InferSmem), st>>>(
         m->inf, feat, feat_scale, conc_in, conc_plain, conc_out, genes, nactive, n_override, step,
         period, stride,
-        threshold, stats, err);
+        threshold, stats, err, MBAR_SPIN_LIMIT, 0u);
+}
+
+// Failure-detection self-test of the tensor-core completion wait: one inference CTA over one
+// tile whose MMAs are withheld, so its mbarrier is never arrived on and the wait runs out
+// after spin_limit polls; the CTA then records MLP_ERR_MBAR_TIMEOUT, frees its tensor memory
+// and returns.  Returns the kernel's error bits; everything it touches is its own.
+cudaError_t mlp_selftest_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, cudaStream_t st) {
+    Mlp m;
+    std::memset(&m, 0, sizeof(m));
+    cudaError_t e = mlp_init_attributes();
+    if (e == cudaSuccess) e = mlp_alloc(&m, 1, st);
+    bf16* feat = nullptr;
+    float* conc = nullptr;
+    uint32_t* err = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&feat, sizeof(bf16) * 128 * MLP_IN);
+    if (e == cudaSuccess) e = cudaMalloc(&conc, sizeof(float) * 2 * 128 * NTF);
+    if (e == cudaSuccess) e = cudaMalloc(&err, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(feat, 0, sizeof(bf16) * 128 * MLP_IN, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(conc, 0, sizeof(float) * 2 * 128 * NTF, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) {
+        k_mlp_infer<<<1, INF_THREADS, sizeof(InferSmem), st>>>(
+            m.inf, feat, nullptr, conc, nullptr, conc + 128 * NTF, nullptr, nullptr, 128u, nullptr,
+            0u, 0u, 0.f, nullptr, err, spin_limit, 1u);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(err_bits, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(feat);
+    cudaFree(conc);
+    cudaFree(err);
+    mlp_free(&m);
+    return e;
 }
 
 }  // namespace mg

@@ -101,6 +101,8 @@ inline uint64_t mix_seed(uint64_t seed, int step) {
 cudaError_t mlp_init_attributes();
 cudaError_t mlp_alloc(Mlp* m, uint64_t seed, cudaStream_t st);
 void mlp_free(Mlp* m);
+// failure-detection self-test: the completion wait of an inference CTA whose MMAs are withheld
+cudaError_t mlp_selftest_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, cudaStream_t st);
 cudaError_t mlp_set_params(Mlp* m, const float* host);
 cudaError_t mlp_get_params(Mlp* m, float* host);
 cudaError_t mlp_set_norm(Mlp* m, const float* host);

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
                                                        uint32_t* __restrict__ out, uint32_t n,
                                                        unsigned long long* status,
                                                        uint32_t* ticket, uint32_t* total,
-                                                       uint32_t* err) {
+                                                       uint32_t* err, uint32_t spin_limit) {
     __shared__ uint32_t s_tile, s_prefix;
     __shared__ uint32_t s_warp[SCAN_THREADS / 32];
     if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
                 const int stop = inclusive ? __ffs(inclusive) - 1 : 31;  // last lane to sum
                 const unsigned needed = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
                 if (unready & needed) {
-                    if (++spins > SPIN_LIMIT) {
+                    if (++spins > spin_limit) {
                         if (lane == 0) atomicOr(err, ERR_SCAN_TIMEOUT);
                         break;
                     }
@@ -219,7 +219,37 @@ void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long lo
                  uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st) {
     uint32_t tiles = (uint32_t)scan_status_words(n);
     if (tiles == 0) return;
-    k_scan<<<tiles, SCAN_THREADS, 0, st>>>(in, out, n, status, ticket, total, err);
+    k_scan<<<tiles, SCAN_THREADS, 0, st>>>(in, out, n, status, ticket, total, err, SPIN_LIMIT);
+}
+
+// Failure-detection self-test of the look-back wait: a scan of 8 tiles whose first tile is
+// never launched (the ticket starts at 1 and 7 blocks run), so its status word stays
+// unpublished and every other tile's wait runs out after spin_limit polls.  Returns the
+// kernel's error bits (ERR_SCAN_TIMEOUT expected); everything it touches is its own.
+cudaError_t scan_selftest_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, cudaStream_t st) {
+    const uint32_t tiles = 8, n = tiles * SCAN_TILE;
+    uint32_t *counts = nullptr, *offsets = nullptr, *words = nullptr;
+    unsigned long long* status = nullptr;
+    cudaError_t e = cudaMalloc(&counts, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&offsets, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&status, sizeof(unsigned long long) * tiles);
+    if (e == cudaSuccess) e = cudaMalloc(&words, sizeof(uint32_t) * 2);  // ticket, error
+    if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * n, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, sizeof(unsigned long long) * tiles, st);
+    const uint32_t init[2] = {1u, 0u};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(words, init, sizeof init, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        k_scan<<<tiles - 1, SCAN_THREADS, 0, st>>>(counts, offsets, n, status, words, nullptr,
+                                                   words + 1, spin_limit);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(err_bits, words + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(counts);
+    cudaFree(offsets);
+    cudaFree(status);
+    cudaFree(words);
+    return e;
 }
 
 // ---- place ----------------------------------------------------------------------------------

@@ -48,6 +48,40 @@ def test_batch_equals_members_stepped_alone(built):
     b.close()
 
 
+def test_batch_follows_member_changes(built):
+    """Members whose genome, parameters or options change between batch steps: the batch steps
+    them with the new values (its steps are captured anew), bit-equal to twins stepped alone
+    with the same changes."""
+    ds = [instance(k) for k in range(4)]
+    alone, batched = [], []
+    for d in ds:
+        for lst in (alone, batched):
+            fs = mg.FluidSystem(d.params, d.genome, d.n)
+            fs.TransferToCL(d.arrays)
+            lst.append(fs)
+    b = mg.Batch(batched)
+    b.Run(4)
+    for fs in alone:
+        fs.Run(4)
+    g = demo.make_genome(seed=77, diffusion=demo.diffusion_rate("R", 0.15))
+    p = ds[1].params
+    p.pintstiff = 1.7
+    for group in (alone, batched):
+        group[0].UpdateGenome(g)
+        group[1].UpdateParams(p)
+        group[2].set_option(A.OPT_NEIGHBOR_SEARCH, 0)
+        group[3].SetParam(A.PVISC, 0.35)
+    b.Run(6)
+    for fs in alone:
+        fs.Run(6)
+    for k, (x, y) in enumerate(zip(alone, batched)):
+        for buf in BUFS:
+            assert np.array_equal(x.download(buf).view(np.uint32), y.download(buf).view(np.uint32)), \
+                f"instance {k} buffer {buf} after a change between batch steps"
+    b.Run(2)  # no change since: the recaptured graphs are reused
+    b.close()
+
+
 def test_batch_rejects_duplicates(built):
     d = instance(0)
     fs = mg.FluidSystem(d.params, d.genome, d.n)

@@ -77,6 +77,26 @@ def test_noalloc_scan_ragged_sizes(built, n):
         assert int(err.item()) == 0
 
 
+def test_noalloc_scan_allocates_nothing(built):
+    """Free device memory is the same before and after repeated calls (buffers made first)."""
+    torch = pytest.importorskip("torch")
+    lib = A.load()
+    n = 3 * 4096 + 5
+    counts = np.arange(n, dtype=np.uint32) % 7
+    dc = _dev(torch, counts)
+    out = torch.empty_like(dc)
+    total = torch.zeros(1, dtype=torch.int32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert _scan(lib, torch, dc, out, total, err) == 0  # first call: one-time scratch lookup
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(8):
+        assert _scan(lib, torch, dc, out, total, err) == 0, lib.mg_last_error(None)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"
+
+
 def test_noalloc_scan_limits(built):
     torch = pytest.importorskip("torch")
     lib = A.load()
