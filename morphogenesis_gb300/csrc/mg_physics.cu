@@ -37,11 +37,6 @@ namespace mg {
 #define MG_DENS_MIN_BLOCKS 3
 #endif
 constexpr int DENS_WARPS = MG_DENS_WARPS;  // warps per block of the warp-cooperative pass
-#ifndef MG_DENS_UNROLL
-#define MG_DENS_UNROLL 4
-#endif
-// survivors tested per iteration of the list-building loop
-constexpr int DENS_UNROLL = MG_DENS_UNROLL;
 // rows of a lane's neighbour list in shared memory: the list appends are branch-free (every
 // survivor is written at the next free row, only hits advance it), so one spare row takes the
 // writes past a full list
@@ -149,13 +144,17 @@ __device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], c
         if (uniform) {
             const float a = dif[0] * cc;
 #if MG_F32X2
-            // cj - cur as cj + (-1) * cur: one rounding of the exact difference, as the subtraction
-            const float2 m1 = make_float2(-1.f, -1.f);
+            // cj - cur as cj + (-1) * cur: one rounding of the exact difference, as the
+            // subtraction; then the product and the sum as packed operations with the numeric
+            // behaviour of __fmul_rn / __fadd_rn per component (never merged into a fused
+            // multiply-add), so each species keeps the reference's two roundings
+            const float2 m1 = make_float2(-1.f, -1.f), a2 = make_float2(a, a);
 #pragma unroll
             for (int t = 0; t < NTF; t += 2) {
                 const float2 d = __ffma2_rn(make_float2(cur[t], cur[t + 1]), m1, make_float2(cj[t], cj[t + 1]));
-                nc[t] += a * d.x;
-                nc[t + 1] += a * d.y;
+                const float2 r = __fadd2_rn(make_float2(nc[t], nc[t + 1]), __fmul2_rn(a2, d));
+                nc[t] = r.x;
+                nc[t + 1] = r.y;
             }
 #else
 #pragma unroll
@@ -494,15 +493,26 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
     uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p,
     const uint32_t* __restrict__ work, uint32_t* __restrict__ ovf, uint32_t* __restrict__ ovf_count,
-    DensExtra X, bool prune) {
+    DensExtra X, bool prune, VerletBufs V) {
     // prune: the positions are those of the last sort, so a window cell whose geometric box
-    // misses the group's box holds no candidate; after positions moved, every cell is walked
+    // misses the group's box holds no candidate; after positions moved, every cell is walked.
+    // V.flag: with Verlet lists this launch runs only when the lists are to be rebuilt
+    // (k_dens_vlist serves the other steps); it then searches with the build radius and
+    // records every lane's list.
     using F = DF<FLAGS>;
 #if MG_DENS_GENOME_BY_VALUE
     const DevGenome* __restrict__ G = &Gv;  // the parameter itself: reads go to the constant bank
 #endif
+    const bool vbuild = V.flag != nullptr;
+    if (vbuild && *V.flag == 0u) return;
+    if (vbuild && blockIdx.x == 0 && threadIdx.x == 0) V.flag[1] += 1u;  // builds so far
     extern __shared__ uint32_t s_list[];  // [warps of the block][NL_CAP][32]
-    __shared__ float4 s_sp[DENS_WARPS][32];  // staged survivors: x, y, z, sorted index (bits)
+    // staged survivors, one array per coordinate so that four consecutive survivors' x (y, z,
+    // sorted index) are one 128-bit load and pairs of them feed packed f32x2 operations
+    __shared__ __align__(16) float s_sx[DENS_WARPS][32];
+    __shared__ __align__(16) float s_sy[DENS_WARPS][32];
+    __shared__ __align__(16) float s_sz[DENS_WARPS][32];
+    __shared__ __align__(16) uint32_t s_sq[DENS_WARPS][32];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     uint32_t* my = s_list + (size_t)w * NL_ROWS * 32 + lane;
     // Lane k of the grid takes the k-th entry of the processing order, so a warp holds
@@ -519,8 +529,12 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     float R2 = 1.f;
     if (F::DENS) R2 = fmaxf(R2, P.r2);
     if (F::DIFF || F::MEAN) R2 = fmaxf(R2, P.r2diff);
+    if (vbuild) R2 = P.vl_r2;  // every term's radius plus the skin
     const float Rf = sqrtf(R2) * 1.0001f + 1e-3f;  // conservative prefilter radius
     const float R2s = R2 * 1.000004f;               // list threshold for the fused distance
+    // a list hit needs d > dmin: other particles at distance 0 are no neighbours now, but a
+    // Verlet list keeps them (and the particle itself, which the exact test drops) for later steps
+    const float dmin = vbuild ? -1.f : 0.f;
     const float INF = __int_as_float(0x7f800000);
     const int g = P.gsrch;
     const int BIG = 1 << 30;
@@ -595,44 +609,56 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                     const unsigned ball = __ballot_sync(0xffffffffu, surv);
                     if (surv) {
                         const uint32_t slot = (uint32_t)__popc(ball & ((1u << lane) - 1u));
-                        s_sp[w][slot] = make_float4(qp.x, qp.y, qp.z, __uint_as_float(off + kk));
+                        s_sx[w][slot] = qp.x;
+                        s_sy[w][slot] = qp.y;
+                        s_sz[w][slot] = qp.z;
+                        s_sq[w][slot] = off + kk;
                     }
                     __syncwarp();
                     const int ns = __popc(ball);
                     if (inw) {
                         // Membership uses a fused-multiply-add distance with a slack of a few
                         // ulps, so the list is a superset of the neighbours; the exact test is
-                        // made again when the list is evaluated.  DENS_UNROLL survivors per
-                        // iteration keep independent dependency chains in flight; every
-                        // survivor is written at the lane's next free row and only hits advance
-                        // it (no divergent branch; a full list writes to the spare row).
+                        // made again when the list is evaluated.  Four survivors per iteration,
+                        // their distances two at a time in packed f32x2 operations (the same
+                        // fused expression per component as approx_dsq); every survivor is
+                        // written at the lane's next free row and only hits advance it (no
+                        // divergent branch; a full list writes to the spare row).
+                        const float2 m1 = make_float2(-1.f, -1.f);
+                        const float2 px = make_float2(ip.x, ip.x), py = make_float2(ip.y, ip.y),
+                                     pz = make_float2(ip.z, ip.z);
                         int tt = 0;
-                        for (; tt + DENS_UNROLL <= ns; tt += DENS_UNROLL) {
-                            float d[DENS_UNROLL];
-                            uint32_t qi[DENS_UNROLL];
+                        for (; tt + 4 <= ns; tt += 4) {
+                            const float4 X = *reinterpret_cast<const float4*>(&s_sx[w][tt]);
+                            const float4 Y = *reinterpret_cast<const float4*>(&s_sy[w][tt]);
+                            const float4 Z = *reinterpret_cast<const float4*>(&s_sz[w][tt]);
+                            const uint4 Q = *reinterpret_cast<const uint4*>(&s_sq[w][tt]);
+                            float2 dx = __ffma2_rn(make_float2(X.x, X.y), m1, px);
+                            float2 dy = __ffma2_rn(make_float2(Y.x, Y.y), m1, py);
+                            float2 dz = __ffma2_rn(make_float2(Z.x, Z.y), m1, pz);
+                            const float2 d01 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+                            dx = __ffma2_rn(make_float2(X.z, X.w), m1, px);
+                            dy = __ffma2_rn(make_float2(Y.z, Y.w), m1, py);
+                            dz = __ffma2_rn(make_float2(Z.z, Z.w), m1, pz);
+                            const float2 d23 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+                            const float d[4] = {d01.x, d01.y, d23.x, d23.y};
+                            const uint32_t qi[4] = {Q.x, Q.y, Q.z, Q.w};
 #pragma unroll
-                            for (int u = 0; u < DENS_UNROLL; u++) {
-                                const float4 sp = s_sp[w][tt + u];
-                                d[u] = approx_dsq(ip, sp);
-                                qi[u] = __float_as_uint(sp.w);
-                            }
-#pragma unroll
-                            for (int u = 0; u < DENS_UNROLL; u++) {
-                                const bool hit = d[u] < R2s && d[u] > 0.f;
+                            for (int u = 0; u < 4; u++) {
+                                const bool hit = d[u] < R2s && d[u] > dmin;
                                 my[min(n, (uint32_t)NL_CAP) * 32] = qi[u] | mark;
                                 mark = hit ? 0u : mark;
                                 n += hit ? 1u : 0u;
                             }
                         }
                         for (; tt < ns; tt++) {
-                            const float4 sp = s_sp[w][tt];
+                            const float4 sp = make_float4(s_sx[w][tt], s_sy[w][tt], s_sz[w][tt], 0.f);
                             const float d = approx_dsq(ip, sp);
-                            const bool hit = d < R2s && d > 0.f;
-                            my[min(n, (uint32_t)NL_CAP) * 32] = __float_as_uint(sp.w) | mark;
+                            const bool hit = d < R2s && d > dmin;
+                            my[min(n, (uint32_t)NL_CAP) * 32] = s_sq[w][tt] | mark;
                             mark = hit ? 0u : mark;
                             n += hit ? 1u : 0u;
                         }
-
                     }
                     __syncwarp();
                 }
@@ -640,6 +666,17 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
         }
     }
     if (!act) return;
+    if (vbuild) {  // the lane's Verlet list: its entries' cold slots, in canonical order
+        const uint32_t id = V.origin[p];
+        if (n > (uint32_t)VL_ROW) {
+            V.cnt[id] = UNDEF;  // searched every step until the next build
+        } else {
+            uint32_t* row = V.row + (size_t)id * VL_ROW;
+            for (uint32_t j = 0; j < n; j++) row[j] = V.origin[my[j * 32] & ~LIST_CELL_START];
+            V.cnt[id] = n;
+        }
+        V.xref[id] = ip;
+    }
     if (n > (uint32_t)NL_CAP) {
         // more neighbours than the list holds (dense clumps): the overflow pass takes it
         ovf[atomicAdd(ovf_count, 1u)] = p;
@@ -648,6 +685,83 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     }
     dens_list_finish<FLAGS>(P, G, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,
                             fcount, X, k);
+}
+
+// ---- Verlet-list kernel -------------------------------------------------------------------
+// The steps between list builds.  A lane's row holds the cold slots of every particle that was
+// within the build radius (every neighbour radius plus the skin) when the list was built, and
+// no particle has moved half the skin since (k_advance checks), so the row holds every
+// particle now within the neighbour radii.  The slots are mapped to current sorted indices,
+// put in ascending order (the canonical order: sorted index order is cell order, then in-cell
+// order), the first entry of each cell is flagged, and dens_list_finish evaluates the list with
+// the exact tests, exactly as after a search: the results are the same bits.  A row whose
+// order changed (a particle changed cells) is written back in the new order, so rows stay
+// nearly sorted and the insertion sort stays linear.
+template <int FLAGS>
+__global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_vlist(
+    DevParams P, MG_DENS_GENOME_PARAM, const float4* __restrict__ pos,
+    const float* __restrict__ conc_in, float* __restrict__ conc_out,
+    const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
+    float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
+    uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p,
+    const uint32_t* __restrict__ work, uint32_t* __restrict__ ovf, uint32_t* __restrict__ ovf_count,
+    DensExtra X, VerletBufs V) {
+#if MG_DENS_GENOME_BY_VALUE
+    const DevGenome* __restrict__ G = &Gv;
+#endif
+    if (*V.flag != 0u) return;  // this step builds the lists (k_dens_warp)
+    extern __shared__ uint32_t s_list[];  // [warps of the block][NL_ROWS][32]
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    uint32_t* my = s_list + (size_t)w * NL_ROWS * 32 + lane;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= *nactive_p) return;
+    const uint32_t p = work[k];
+    const uint32_t id = V.origin[p];
+    const uint32_t n = V.cnt[id];
+    if (n > (uint32_t)VL_ROW) {  // no list (it overflowed at the build): the overflow pass searches
+        ovf[atomicAdd(ovf_count, 1u)] = p;
+        if (X.hlist) X.hcount[k] = UNDEF;
+        return;
+    }
+    uint32_t* row = V.row + (size_t)id * VL_ROW;
+    uint32_t m = 0;
+    bool moved = false;
+    for (uint32_t j = 0; j < n; j += 4) {
+        const uint4 e4 = *reinterpret_cast<const uint4*>(row + j);
+        const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (j + u >= n) break;
+            const uint32_t q = V.pos_of[e[u]];
+            if (q == UNDEF) {  // left the grid
+                moved = true;
+                continue;
+            }
+            uint32_t i = m;
+            while (i > 0 && my[(i - 1) * 32] > q) {
+                my[i * 32] = my[(i - 1) * 32];
+                i--;
+            }
+            moved |= i != m;
+            my[i * 32] = q;
+            m++;
+        }
+    }
+    uint32_t prev = UNDEF;
+    for (uint32_t j = 0; j < m; j++) {
+        const uint32_t q = my[j * 32];
+        const uint32_t c = scell[q];
+        if (c != prev) {
+            my[j * 32] = q | LIST_CELL_START;
+            prev = c;
+        }
+    }
+    if (moved) {
+        for (uint32_t j = 0; j < m; j++) row[j] = V.origin[my[j * 32] & ~LIST_CELL_START];
+        V.cnt[id] = m;
+    }
+    dens_list_finish<FLAGS>(P, G, p, pos[p], m, my, pos, conc_in, conc_out, genes, press, invdens,
+                            flist, fcount, X, k);
 }
 
 // ---- per-lane fine-cell search ----------------------------------------------------------------
@@ -810,10 +924,12 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
     uint32_t* __restrict__ fcount, const uint32_t* __restrict__ ovf,
-    const uint32_t* __restrict__ ovf_count, DensExtra X, bool prune) {
+    const uint32_t* __restrict__ ovf_count, DensExtra X, bool prune, uint32_t* vflag) {
     // prune: positions are those of the last sort, so a window cell whose geometric box misses
-    // the particle's search box holds no neighbour
+    // the particle's search box holds no neighbour.  vflag: the Verlet rebuild flag, which the
+    // two kernels before this one have read; the lists are current from here on
     using F = DF<FLAGS>;
+    if (vflag && blockIdx.x == 0 && threadIdx.x == 0) *vflag = 0u;
     constexpr bool CONC = F::DIFF || F::MEAN;
     __shared__ float4 s_cj[256 / 32][OVF_SEG][NTF / 4];  // concentrations of the segment's hits
     __shared__ float s_d[256 / 32][OVF_SEG];
@@ -956,7 +1072,9 @@ cudaError_t physics_init() {
     if (e == cudaSuccess)                                                                       \
         e = cudaFuncSetAttribute(k_dens_warp<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
     if (e == cudaSuccess)                                                                       \
-        e = cudaFuncSetAttribute(k_dens_fine<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = cudaFuncSetAttribute(k_dens_fine<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
+    if (e == cudaSuccess)                                                                       \
+        e = cudaFuncSetAttribute(k_dens_vlist<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     MG_DENS_FLAG_SETS(MG_ATTR)
 #undef MG_ATTR
     return e;
@@ -972,6 +1090,12 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
     if ((search == 1 || search == 3) && (flags & (1 | 2 | 8 | 16))) {
         uint32_t blocks = (P.cap + warps * 32 - 1) / (warps * 32);
         const bool prune = search == 1;
+        // Verlet lists at sort-time positions (search 1): the search runs only on build steps,
+        // the list kernel on the others; after positions moved since the sort (search 3) the
+        // search runs alone
+        VerletBufs V{};
+        if (P.verlet && search == 1)
+            V = VerletBufs{s.vrow, s.vcnt, s.xref, s.pos_of, cur.origin, s.counters + VL_FLAG};
 #define MG_DENSW_CASE(F)                                                                          \
     case F:                                                                                       \
         k_dens_warp<F><<<blocks, warps * 32, smem, st>>>(P, MG_DENS_GENOME_ARG, cur.pos, conc_in, conc_out, \
@@ -979,12 +1103,18 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.counters + 3,   \
                                                              s.work, s.ovf, s.counters + 6, X,    \
-                                                             prune);                              \
+                                                             prune, V);                           \
+        if (V.flag)                                                                               \
+            k_dens_vlist<F><<<blocks, warps * 32, smem, st>>>(P, MG_DENS_GENOME_ARG, cur.pos, conc_in, \
+                                                              conc_out, cur.genes, s.scell,      \
+                                                              s.press, s.invdens, s.flist,       \
+                                                              s.fcount, s.counters + 3, s.work,  \
+                                                              s.ovf, s.counters + 6, X, V);      \
         k_dens_ovf<F><<<(uint32_t)num_sms * 4, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out,    \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.ovf,            \
-                                                             s.counters + 6, X, prune);           \
+                                                             s.counters + 6, X, prune, V.flag);   \
         return;
         cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
         switch (flags) { MG_DENS_FLAG_SETS(MG_DENSW_CASE) default: break; }
@@ -1003,7 +1133,7 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.ovf,            \
-                                                             s.counters + 6, X, true);            \
+                                                             s.counters + 6, X, true, nullptr);   \
         return;
         cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
         switch (flags) { MG_DENS_FLAG_SETS(MG_DENSF_CASE) default: break; }
@@ -1297,7 +1427,10 @@ template <bool APPLY_BRK, bool SPECIAL>
 __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
                                                  const float4* __restrict__ force,
                                                  const uint32_t* __restrict__ brk,
-                                                 uint32_t* __restrict__ counters) {
+                                                 uint32_t* __restrict__ counters,
+                                                 const float4* __restrict__ xref) {
+    // xref (Verlet lists in use): positions at the last list build, by cold slot; a particle
+    // now more than half the skin away from it sets the rebuild flag
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t step = counters[5];
     const float time = *time_slot(counters, step);
@@ -1339,17 +1472,28 @@ __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
     const float dt = P.dt;
     const float vnx = ax * dt + vel.x, vny = ay * dt + vel.y, vnz = az * dt + vel.z;
     const uint32_t special = SPECIAL ? (C.genes[p] >> 11) & 3u : 0u;  // bit 0: gene 11, bit 1: gene 12
+    float4 np = pos;  // the new position
     if (special == 0) {
         C.veval[p] = make_float4((vel.x + vnx) * 0.5f, (vel.y + vny) * 0.5f, (vel.z + vnz) * 0.5f, ve.w);
         C.vel[p] = make_float4(vnx, vny, vnz, vel.w);
-        C.pos[p] = make_float4(pos.x + vnx * dt, pos.y + vny * dt, pos.z + vnz * dt, pos.w);
+        np = make_float4(pos.x + vnx * dt, pos.y + vny * dt, pos.z + vnz * dt, pos.w);
+        C.pos[p] = np;
     } else if (special == 2u) {
         // externalActuation (cuda:3617-3691): the previous state, z displaced by
         // actuation_factor * sin(time / (actuation_period * dt))
         const float ph = time / (P.actuation_period * dt);
-        C.pos[p] = make_float4(pos.x, pos.y, pos.z + P.actuation_factor * mg_sin_cw(ph), pos.w);
+        np = make_float4(pos.x, pos.y, pos.z + P.actuation_factor * mg_sin_cw(ph), pos.w);
+        C.pos[p] = np;
     }
     // fixedParticles (cuda:3694-3705, after the actuation): the previous state is kept
+    if (xref) {
+        const uint32_t id = C.origin[p];
+        if (id < P.cap) {
+            const float4 r = xref[id];
+            const float dx = np.x - r.x, dy = np.y - r.y, dz = np.z - r.z;
+            if (!(dx * dx + dy * dy + dz * dz <= P.vl_move2)) counters[VL_FLAG] = 1u;
+        }
+    }
     if (APPLY_BRK) {
         const uint32_t br = brk[p];
         if (br) apply_breaks(C.bond, P.cap, p, br);
@@ -1359,14 +1503,15 @@ __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_brk,
                     cudaStream_t st, bool special) {
     uint32_t blocks = (P.cap + 255) / 256;
+    const float4* xref = P.verlet ? s.xref : nullptr;
     if (apply_brk && special)
-        k_advance<true, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+        k_advance<true, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters, xref);
     else if (apply_brk)
-        k_advance<true, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+        k_advance<true, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters, xref);
     else if (special)
-        k_advance<false, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+        k_advance<false, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters, xref);
     else
-        k_advance<false, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+        k_advance<false, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters, xref);
 }
 
 }  // namespace mg
