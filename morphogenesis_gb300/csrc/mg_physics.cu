@@ -717,7 +717,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_vl
     if (k >= *nactive_p) return;
     const uint32_t p = work[k];
     const uint32_t id = V.origin[p];
-    const uint32_t n = V.cnt[id];
+    const uint32_t n = id < P.cap ? V.cnt[id] : UNDEF;
     if (n > (uint32_t)VL_ROW) {  // no list (it overflowed at the build): the overflow pass searches
         ovf[atomicAdd(ovf_count, 1u)] = p;
         if (X.hlist) X.hcount[k] = UNDEF;
@@ -732,7 +732,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_vl
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             if (j + u >= n) break;
-            const uint32_t q = V.pos_of[e[u]];
+            const uint32_t q = e[u] < P.cap ? V.pos_of[e[u]] : UNDEF;
             if (q == UNDEF) {  // left the grid
                 moved = true;
                 continue;
