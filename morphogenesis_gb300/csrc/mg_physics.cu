@@ -145,16 +145,15 @@ __device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], c
             const float a = dif[0] * cc;
 #if MG_F32X2
             // cj - cur as cj + (-1) * cur: one rounding of the exact difference, as the
-            // subtraction; then the product and the sum as packed operations with the numeric
-            // behaviour of __fmul_rn / __fadd_rn per component (never merged into a fused
-            // multiply-add), so each species keeps the reference's two roundings
-            const float2 m1 = make_float2(-1.f, -1.f), a2 = make_float2(a, a);
+            // subtraction.  The product and the sum stay scalar: packed as __fmul2_rn feeding
+            // __fadd2_rn they gave other bits than the two roundings of the reference (measured
+            // against the oracle), i.e. they were merged into a fused multiply-add.
+            const float2 m1 = make_float2(-1.f, -1.f);
 #pragma unroll
             for (int t = 0; t < NTF; t += 2) {
                 const float2 d = __ffma2_rn(make_float2(cur[t], cur[t + 1]), m1, make_float2(cj[t], cj[t + 1]));
-                const float2 r = __fadd2_rn(make_float2(nc[t], nc[t + 1]), __fmul2_rn(a2, d));
-                nc[t] = r.x;
-                nc[t + 1] = r.y;
+                nc[t] += a * d.x;
+                nc[t + 1] += a * d.y;
             }
 #else
 #pragma unroll
