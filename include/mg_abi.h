@@ -316,21 +316,9 @@ enum mg_option {
      * length, modulus and damping kept from the slot (default); 1 = makeBond's elastin defaults
      * from the genome (param[0]: elastLim, default rest length, modulus, damping,
      * fluid_system_cuda.cu:1573-1593) */
-    MG_OPT_HEAL_PARAMS = 2,
-    /* Verlet lists for the warp-cooperative search: 1 (default) keeps, per particle, the
-     * particles within the search radius plus a skin from the last list build, and the steps
-     * in between evaluate those lists instead of searching; the lists are rebuilt once any
-     * particle has moved half the skin since the build (checked by the integration and after
-     * every position upload).  Used with the 27-cell window when a grid cell is at least the
-     * search radius plus the skin; 0 searches every step.  Results are identical. */
-    MG_OPT_VERLET = 3,
-    /* skin of the Verlet lists in thousandths of the search radius (1..500, default 75) */
-    MG_OPT_VERLET_SKIN = 4
+    MG_OPT_HEAL_PARAMS = 2
 };
 mg_status mg_set_option(mg_handle h, int32_t option, int32_t value);
-/* Number of Verlet-list builds the density passes of this handle have made (MG_OPT_VERLET);
- * synchronises the handle's stream.  No counterpart in the reference (it searches every step). */
-mg_status mg_neighbor_list_builds(mg_handle h, uint32_t* builds);
 
 /* ---- launch-shape autotuner ------------------------------------------------------------------ */
 /* Launch shape of the density pass: {warps per block (4 or 8), search groups (0: a cell and the

@@ -311,12 +311,6 @@ class FluidSystem:
                                                   flags, C.byref(bp), C.byref(bc)))
         return bp.value, bc.value
 
-    def neighbor_list_builds(self) -> int:
-        """Verlet-list builds the density passes have made so far (MG_OPT_VERLET)."""
-        n = A.C.c_uint32()
-        self._check(self.lib.mg_neighbor_list_builds(self.h, A.C.byref(n)))
-        return int(n.value)
-
     def kernel_launches(self) -> int:
         return int(self.lib.mg_kernel_launches(self.h))
 

@@ -37,8 +37,6 @@ STEP_DEFAULT = STEP_PHYSICS | STEP_GENES
 
 OPT_NEIGHBOR_SEARCH = 1
 OPT_HEAL_PARAMS = 2
-OPT_VERLET = 3
-OPT_VERLET_SKIN = 4
 MLP_IN, MLP_H, MLP_OUT = 48, 128, 16
 P_W1 = 0
 P_B1 = P_W1 + MLP_H * MLP_IN
@@ -217,7 +215,6 @@ SIGNATURES = [
     ("mg_batch_time_steps", C.c_int, [H, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]),
     ("mg_prefix_sum_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mg_selftest_bounded_wait", C.c_int, [C.c_int32, C.c_uint32]),
-    ("mg_neighbor_list_builds", C.c_int, [H, C.POINTER(C.c_uint32)]),
 ]
 
 _lib = None

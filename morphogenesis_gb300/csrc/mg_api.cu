@@ -77,8 +77,6 @@ struct mg_system {
     uint32_t* hmem = nullptr;   // re-forming candidates recorded by the density pass: count [cap]
                                 // then list [NL_CAP][cap] (allocated with the first remodelling step)
     int search = 1;             // density pass search: 0 direct walk, 1 warp-cooperative
-    int verlet_opt = 1;         // Verlet lists for the warp-cooperative search (MG_OPT_VERLET)
-    int verlet_skin = 75;       // their skin in thousandths of the search radius (MG_OPT_VERLET_SKIN)
     float time = 0.f;
     std::string err;
     std::map<uint64_t, cudaGraphExec_t> graphs;
@@ -203,28 +201,6 @@ void derive(DevParams& D, const mg_fparams& p, uint32_t cap) {
     D.group_mode = 0;
     D.sub_bits = 2;
     D.cells = (uint32_t)p.grid_total;
-}
-
-// Verlet lists of the warp-cooperative density pass: used when the option is on, the window is
-// the 27-cell one and a grid cell is at least the build radius on every axis (so everything
-// within the build radius of a particle lies in its window).  The build radius is the largest
-// radius of any neighbour term (density r2, diffusion r2 / ss^2, fluid force 1) plus the skin;
-// lists are rebuilt once a particle has moved half the skin since the build.  The margins
-// cover the rounding of the fused distance that picks list entries and of the displacement test.
-void set_verlet(mg_system* h) {
-    DevParams& D = h->P;
-    const double R = std::sqrt(std::max(1.0, std::max((double)D.r2, (double)D.r2diff)));
-    const double skin = R * h->verlet_skin / 1000.0;
-    bool ok = h->verlet_opt != 0 && D.gsrch == 3 && skin > 0.0;
-    for (int k = 0; k < 3; k++) ok = ok && (double)D.gcell[k] >= (R + skin) * 1.001;
-    D.verlet = ok ? 1 : 0;
-    D.vl_r2 = (float)((R + skin) * (R + skin) * 1.00002);
-    D.vl_move2 = (float)(0.25 * skin * skin * 0.9999);
-}
-
-// The lists are rebuilt at the next density pass (parameters changed, state restored).
-void verlet_invalidate(mg_system* h) {
-    cudaMemsetAsync(h->s.counters + VL_FLAG, 1, sizeof(uint32_t), h->stream);
 }
 
 mg_status check_params(mg_system* h, const mg_fparams* p) {
@@ -587,8 +563,6 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
             }
         if (motion_up) cudaEventRecord(ev[6], B);
         cudaStreamWaitEvent(st, ev[1], 0);
-        for (uint32_t k = 0; k < io->nin; k++)
-            if (io->in[k].buf_id == MG_FPOS) launch_verlet_check(h->P, h->set[h->cur], h->s, st);
     }
     enqueue_insert_rank(h, prof);
     if (up) cudaStreamWaitEvent(st, ev[2], 0);
@@ -643,9 +617,8 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
 
 int kernels_per_step(const mg_system* h, uint32_t flags) {
     int n = 6;  // insert, scan, place, cellsort, cellsort_big, gather
-    // density pass (+ its overflow pass with the warp search, + the Verlet-list kernel)
-    if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE))
-        n += h->search ? (h->search == 1 && h->P.verlet ? 3 : 2) : 1;
+    // density pass (+ its overflow pass with the warp search)
+    if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE)) n += h->search ? 2 : 1;
     if (flags & MG_STEP_SURROGATE) n += 1;
     if (flags & MG_STEP_PHYSICS) n += 3;  // force (two kernels), advance
     if (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) n += (flags & MG_STEP_PHYSICS) ? 4 : 3;
@@ -980,7 +953,6 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     h->cap = max_points;
     h->time = params->time;
     derive(h->P, *params, max_points);
-    set_verlet(h);
     cudaError_t e = cudaGetDevice(&h->device);
     if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaGetDevice"); }
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
@@ -1040,10 +1012,6 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     plan.push_back({(void**)&h->s.scan_status, 8 * (tiles + 1)});
     plan.push_back({(void**)&h->s.counters, 64});
     plan.push_back({(void**)&h->s.big_list, 4 * (size_t)BIG_LIST_CAP});
-    plan.push_back({(void**)&h->s.vrow, 4 * (size_t)VL_ROW * n});
-    plan.push_back({(void**)&h->s.vcnt, 4 * n});
-    plan.push_back({(void**)&h->s.xref, 16 * n});
-    plan.push_back({(void**)&h->s.pos_of, 4 * n});
     plan.push_back({(void**)&h->dG, sizeof(DevGenome)});
     size_t total = 0;
     for (auto& pr : plan) total += align_up(pr.second);
@@ -1064,7 +1032,6 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     launch_init_set(max_points, h->set[1], h->stream);
     uint32_t init_counters[16] = {0};
     init_counters[3] = max_points;  // every slot counts as active until the first sort
-    init_counters[VL_FLAG] = 1u;    // the first density pass builds the Verlet lists
     std::memcpy(&init_counters[7], &params->time, 4);  // device time, both parity slots
     std::memcpy(&init_counters[8], &params->time, 4);
     cudaMemcpyAsync(h->s.counters, init_counters, sizeof(init_counters), cudaMemcpyHostToDevice, h->stream);
@@ -1124,8 +1091,6 @@ mg_status mg_update_params(mg_handle h, const mg_fparams* p) {
     h->P.dens_warps = old.dens_warps;
     h->P.group_mode = old.group_mode;
     h->P.sub_bits = old.sub_bits;
-    set_verlet(h);
-    verlet_invalidate(h);
     clear_graphs(h);
     // the device copy of the time (both parity slots)
     const uint32_t t2[2] = {*reinterpret_cast<const uint32_t*>(&p->time), *reinterpret_cast<const uint32_t*>(&p->time)};
@@ -1237,7 +1202,6 @@ static mg_status enqueue_upload(mg_handle h, int32_t id, const void* host, size_
     }
     if (dst) {
         MG_CUDA(h, cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, st));
-        if (id == MG_FPOS) launch_verlet_check(h->P, c, h->s, st);
         return MG_OK;
     }
     mg_status s2 = ensure_staging(h, bytes);
@@ -1604,27 +1568,11 @@ mg_status mg_set_option(mg_handle h, int32_t option, int32_t value) {
         if (value == 2 && h->search != 2 && h->phase == PHASE_SORTED) h->phase = PHASE_UNSORTED;
         h->search = value;
         h->flist_valid = false;
-        verlet_invalidate(h);
         clear_graphs(h);
         return MG_OK;
     case MG_OPT_HEAL_PARAMS:
         if (value < 0 || value > 1) return fail(h, MG_ERR_INVALID_ARG, "heal parameters are 0 or 1");
         h->P.heal_params = value;
-        clear_graphs(h);
-        return MG_OK;
-    case MG_OPT_VERLET:
-        if (value < 0 || value > 1) return fail(h, MG_ERR_INVALID_ARG, "Verlet lists are 0 or 1");
-        h->verlet_opt = value;
-        set_verlet(h);
-        verlet_invalidate(h);
-        clear_graphs(h);
-        return MG_OK;
-    case MG_OPT_VERLET_SKIN:
-        if (value < 1 || value > 500)
-            return fail(h, MG_ERR_INVALID_ARG, "Verlet skin is 1..500 thousandths of the search radius");
-        h->verlet_skin = value;
-        set_verlet(h);
-        verlet_invalidate(h);
         clear_graphs(h);
         return MG_OK;
     default:
@@ -2031,13 +1979,6 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
     if (choice) { choice[0] = pick.warps; choice[1] = pick.group; choice[2] = pick.sub; choice[3] = pick.search; }
     if (ms_per_step) *ms_per_step = best / (float)steps;
     return check_device(h);
-}
-
-mg_status mg_neighbor_list_builds(mg_handle h, uint32_t* builds) {
-    if (!h || !builds) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
-    mg_status st = MG_OK;
-    *builds = read_word(h, h->s.counters + VL_FLAG + 1, &st);
-    return st;
 }
 
 mg_status mg_get_tuning(mg_handle h, int32_t* choice) {

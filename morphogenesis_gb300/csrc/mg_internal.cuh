@@ -42,8 +42,6 @@ constexpr uint32_t SPIN_LIMIT = 1u << 22; // bounded look-back polls
 #endif
 constexpr int NL_CAP = MG_NL_CAP;  // per-lane neighbour list of the warp-cooperative density pass
 constexpr int FL_CAP = 32;  // fluid-force neighbours (dsq < 1) recorded per particle
-constexpr int VL_ROW = NL_CAP;  // entries of a Verlet list row (a lane's list holds them all)
-constexpr int VL_FLAG = 9;      // counters[VL_FLAG]: Verlet rebuild flag
 constexpr int MLP_FEATURES = 48;
 constexpr int PROP_K = 8;  // proposals a particle keeps for ranking (more: it walks its window)  // surrogate inputs: conc[16], neighbour-mean conc[16], gene bits[16]
 
@@ -73,12 +71,6 @@ struct DevParams {
     // its row, 1: one cell), sub-cell bits per axis of the processing order (1 or 2)
     int dens_warps, group_mode, sub_bits;
     int full_epi;  // per-gene FEPIGEN words carried (countdowns, activation lists) instead of bits
-    // Verlet neighbour lists of the warp-cooperative density pass (0: search every step):
-    // vl_r2 the squared build radius (the largest radius of any neighbour term plus the skin,
-    // with a margin for rounding), vl_move2 the squared displacement since the build past which
-    // the lists are rebuilt (below half the skin, with the same margin)
-    int verlet;
-    float vl_r2, vl_move2;
     int heal_params;  // healed bonds: 0 rest length = distance (D5), 1 makeBond's genome defaults
     uint32_t cap;
     uint32_t cells;
@@ -149,9 +141,7 @@ struct Scratch {
     uint32_t* counters; // [0] scan tile ticket, [1] big-cell list length, [2] error word,
                         // [3] nactive, [5] step counter (incremented by insert),
                         // [6] density-pass overflow queue length, [7], [8] simulation time
-                        // (float bits, slot = step counter parity), [9] Verlet rebuild flag
-                        // (nonzero: the next density pass builds the lists), [10] Verlet
-                        // list builds so far
+                        // (float bits, slot = step counter parity)
     uint32_t* ovf;      // [cap] particles whose neighbours overflow a lane's list
     uint8_t* freemask;  // [cap] remodelling: free incoming slots
     uint32_t* prop_cnt;   // [cap] remodelling: proposals received
@@ -159,15 +149,6 @@ struct Scratch {
     uint32_t* prop;     // [cap] remodelling: proposed partner
     float* propd;       // [cap] remodelling: its squared distance
     uint32_t* big_list; // [BIG_LIST_CAP] cells that need the block-level ordering
-    // Verlet neighbour lists, indexed by the particle's cold slot (`origin`, which the sort
-    // does not move): the slots of the particles within the build radius at the last build
-    // ([cap][VL_ROW], ascending sorted index as of the last step that used the row), their
-    // number (UNDEF: more than the row holds, the particle is searched every step), the
-    // position at the build, and the current sorted index of each slot (UNDEF once dropped)
-    uint32_t* vrow;
-    uint32_t* vcnt;
-    float4* xref;
-    uint32_t* pos_of;
 };
 
 // ---- launchers (all on one stream; no host synchronisation inside) ----------------------
@@ -182,8 +163,6 @@ size_t scan_status_words(uint32_t n);
 // failure-detection self-tests: a bounded wait on a flag nothing sets (see the definitions)
 cudaError_t scan_selftest_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, cudaStream_t st);
 void launch_place(const DevParams& P, const Scratch& s, cudaStream_t st);
-// after positions were written from the host: rebuild the Verlet lists if they no longer hold
-void launch_verlet_check(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
 // subcounts: also count each cell's 2x2x2 sub-cells (for the per-lane fine-cell search)
 void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, bool subcounts,
                      cudaStream_t st);
@@ -217,16 +196,6 @@ struct DensExtra {
     // number (0xFFFFFFFF: not recorded, the particle overflowed)
     uint32_t* hlist;
     uint32_t* hcount;
-};
-// Verlet lists of the density pass (Scratch::vrow ...) for one launch; flag null: no lists (the
-// warp search runs alone, e.g. when positions moved since the sort)
-struct VerletBufs {
-    uint32_t* row;
-    uint32_t* cnt;
-    float4* xref;
-    const uint32_t* pos_of;
-    const uint32_t* origin;  // cold slot of each sorted particle (the rows' key)
-    uint32_t* flag;
 };
 // G: the genome in device memory; Gh: its host copy, passed by value to the warp search so
 // its uniform reads go through the constant cache

@@ -492,19 +492,13 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
     uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p,
     const uint32_t* __restrict__ work, uint32_t* __restrict__ ovf, uint32_t* __restrict__ ovf_count,
-    DensExtra X, bool prune, VerletBufs V) {
+    DensExtra X, bool prune) {
     // prune: the positions are those of the last sort, so a window cell whose geometric box
-    // misses the group's box holds no candidate; after positions moved, every cell is walked.
-    // V.flag: with Verlet lists this launch runs only when the lists are to be rebuilt
-    // (k_dens_vlist serves the other steps); it then searches with the build radius and
-    // records every lane's list.
+    // misses the group's box holds no candidate; after positions moved, every cell is walked
     using F = DF<FLAGS>;
 #if MG_DENS_GENOME_BY_VALUE
     const DevGenome* __restrict__ G = &Gv;  // the parameter itself: reads go to the constant bank
 #endif
-    const bool vbuild = V.flag != nullptr;
-    if (vbuild && *V.flag == 0u) return;
-    if (vbuild && blockIdx.x == 0 && threadIdx.x == 0) V.flag[1] += 1u;  // builds so far
     extern __shared__ uint32_t s_list[];  // [warps of the block][NL_CAP][32]
     // staged survivors, one array per coordinate so that four consecutive survivors' x (y, z,
     // sorted index) are one 128-bit load and pairs of them feed packed f32x2 operations
@@ -528,12 +522,8 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     float R2 = 1.f;
     if (F::DENS) R2 = fmaxf(R2, P.r2);
     if (F::DIFF || F::MEAN) R2 = fmaxf(R2, P.r2diff);
-    if (vbuild) R2 = P.vl_r2;  // every term's radius plus the skin
     const float Rf = sqrtf(R2) * 1.0001f + 1e-3f;  // conservative prefilter radius
     const float R2s = R2 * 1.000004f;               // list threshold for the fused distance
-    // a list hit needs d > dmin: other particles at distance 0 are no neighbours now, but a
-    // Verlet list keeps them (and the particle itself, which the exact test drops) for later steps
-    const float dmin = vbuild ? -1.f : 0.f;
     const float INF = __int_as_float(0x7f800000);
     const int g = P.gsrch;
     const int BIG = 1 << 30;
@@ -620,9 +610,9 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                         // ulps, so the list is a superset of the neighbours; the exact test is
                         // made again when the list is evaluated.  Four survivors per iteration,
                         // their distances two at a time in packed f32x2 operations (the same
-                        // fused expression per component as approx_dsq); every survivor is
-                        // written at the lane's next free row and only hits advance it (no
-                        // divergent branch; a full list writes to the spare row).
+                        // fused expression per component as approx_dsq: list membership only);
+                        // every survivor is written at the lane's next free row and only hits
+                        // advance it (no divergent branch; a full list writes to the spare row).
                         const float2 m1 = make_float2(-1.f, -1.f);
                         const float2 px = make_float2(ip.x, ip.x), py = make_float2(ip.y, ip.y),
                                      pz = make_float2(ip.z, ip.z);
@@ -644,7 +634,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                             const uint32_t qi[4] = {Q.x, Q.y, Q.z, Q.w};
 #pragma unroll
                             for (int u = 0; u < 4; u++) {
-                                const bool hit = d[u] < R2s && d[u] > dmin;
+                                const bool hit = d[u] < R2s && d[u] > 0.f;
                                 my[min(n, (uint32_t)NL_CAP) * 32] = qi[u] | mark;
                                 mark = hit ? 0u : mark;
                                 n += hit ? 1u : 0u;
@@ -653,7 +643,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                         for (; tt < ns; tt++) {
                             const float4 sp = make_float4(s_sx[w][tt], s_sy[w][tt], s_sz[w][tt], 0.f);
                             const float d = approx_dsq(ip, sp);
-                            const bool hit = d < R2s && d > dmin;
+                            const bool hit = d < R2s && d > 0.f;
                             my[min(n, (uint32_t)NL_CAP) * 32] = s_sq[w][tt] | mark;
                             mark = hit ? 0u : mark;
                             n += hit ? 1u : 0u;
@@ -665,17 +655,6 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
         }
     }
     if (!act) return;
-    if (vbuild) {  // the lane's Verlet list: its entries' cold slots, in canonical order
-        const uint32_t id = V.origin[p];
-        if (n > (uint32_t)VL_ROW) {
-            V.cnt[id] = UNDEF;  // searched every step until the next build
-        } else {
-            uint32_t* row = V.row + (size_t)id * VL_ROW;
-            for (uint32_t j = 0; j < n; j++) row[j] = V.origin[my[j * 32] & ~LIST_CELL_START];
-            V.cnt[id] = n;
-        }
-        V.xref[id] = ip;
-    }
     if (n > (uint32_t)NL_CAP) {
         // more neighbours than the list holds (dense clumps): the overflow pass takes it
         ovf[atomicAdd(ovf_count, 1u)] = p;
@@ -684,83 +663,6 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     }
     dens_list_finish<FLAGS>(P, G, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,
                             fcount, X, k);
-}
-
-// ---- Verlet-list kernel -------------------------------------------------------------------
-// The steps between list builds.  A lane's row holds the cold slots of every particle that was
-// within the build radius (every neighbour radius plus the skin) when the list was built, and
-// no particle has moved half the skin since (k_advance checks), so the row holds every
-// particle now within the neighbour radii.  The slots are mapped to current sorted indices,
-// put in ascending order (the canonical order: sorted index order is cell order, then in-cell
-// order), the first entry of each cell is flagged, and dens_list_finish evaluates the list with
-// the exact tests, exactly as after a search: the results are the same bits.  A row whose
-// order changed (a particle changed cells) is written back in the new order, so rows stay
-// nearly sorted and the insertion sort stays linear.
-template <int FLAGS>
-__global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_vlist(
-    DevParams P, MG_DENS_GENOME_PARAM, const float4* __restrict__ pos,
-    const float* __restrict__ conc_in, float* __restrict__ conc_out,
-    const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
-    float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
-    uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p,
-    const uint32_t* __restrict__ work, uint32_t* __restrict__ ovf, uint32_t* __restrict__ ovf_count,
-    DensExtra X, VerletBufs V) {
-#if MG_DENS_GENOME_BY_VALUE
-    const DevGenome* __restrict__ G = &Gv;
-#endif
-    if (*V.flag != 0u) return;  // this step builds the lists (k_dens_warp)
-    extern __shared__ uint32_t s_list[];  // [warps of the block][NL_ROWS][32]
-    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
-    uint32_t* my = s_list + (size_t)w * NL_ROWS * 32 + lane;
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= *nactive_p) return;
-    const uint32_t p = work[k];
-    const uint32_t id = V.origin[p];
-    const uint32_t n = id < P.cap ? V.cnt[id] : UNDEF;
-    if (n > (uint32_t)VL_ROW) {  // no list (it overflowed at the build): the overflow pass searches
-        ovf[atomicAdd(ovf_count, 1u)] = p;
-        if (X.hlist) X.hcount[k] = UNDEF;
-        return;
-    }
-    uint32_t* row = V.row + (size_t)id * VL_ROW;
-    uint32_t m = 0;
-    bool moved = false;
-    for (uint32_t j = 0; j < n; j += 4) {
-        const uint4 e4 = *reinterpret_cast<const uint4*>(row + j);
-        const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            if (j + u >= n) break;
-            const uint32_t q = e[u] < P.cap ? V.pos_of[e[u]] : UNDEF;
-            if (q == UNDEF) {  // left the grid
-                moved = true;
-                continue;
-            }
-            uint32_t i = m;
-            while (i > 0 && my[(i - 1) * 32] > q) {
-                my[i * 32] = my[(i - 1) * 32];
-                i--;
-            }
-            moved |= i != m;
-            my[i * 32] = q;
-            m++;
-        }
-    }
-    uint32_t prev = UNDEF;
-    for (uint32_t j = 0; j < m; j++) {
-        const uint32_t q = my[j * 32];
-        const uint32_t c = scell[q];
-        if (c != prev) {
-            my[j * 32] = q | LIST_CELL_START;
-            prev = c;
-        }
-    }
-    if (moved) {
-        for (uint32_t j = 0; j < m; j++) row[j] = V.origin[my[j * 32] & ~LIST_CELL_START];
-        V.cnt[id] = m;
-    }
-    dens_list_finish<FLAGS>(P, G, p, pos[p], m, my, pos, conc_in, conc_out, genes, press, invdens,
-                            flist, fcount, X, k);
 }
 
 // ---- per-lane fine-cell search ----------------------------------------------------------------
@@ -923,12 +825,10 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
     uint32_t* __restrict__ fcount, const uint32_t* __restrict__ ovf,
-    const uint32_t* __restrict__ ovf_count, DensExtra X, bool prune, uint32_t* vflag) {
+    const uint32_t* __restrict__ ovf_count, DensExtra X, bool prune) {
     // prune: positions are those of the last sort, so a window cell whose geometric box misses
-    // the particle's search box holds no neighbour.  vflag: the Verlet rebuild flag, which the
-    // two kernels before this one have read; the lists are current from here on
+    // the particle's search box holds no neighbour
     using F = DF<FLAGS>;
-    if (vflag && blockIdx.x == 0 && threadIdx.x == 0) *vflag = 0u;
     constexpr bool CONC = F::DIFF || F::MEAN;
     __shared__ float4 s_cj[256 / 32][OVF_SEG][NTF / 4];  // concentrations of the segment's hits
     __shared__ float s_d[256 / 32][OVF_SEG];
@@ -1071,9 +971,7 @@ cudaError_t physics_init() {
     if (e == cudaSuccess)                                                                       \
         e = cudaFuncSetAttribute(k_dens_warp<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
     if (e == cudaSuccess)                                                                       \
-        e = cudaFuncSetAttribute(k_dens_fine<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
-    if (e == cudaSuccess)                                                                       \
-        e = cudaFuncSetAttribute(k_dens_vlist<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = cudaFuncSetAttribute(k_dens_fine<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     MG_DENS_FLAG_SETS(MG_ATTR)
 #undef MG_ATTR
     return e;
@@ -1089,12 +987,6 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
     if ((search == 1 || search == 3) && (flags & (1 | 2 | 8 | 16))) {
         uint32_t blocks = (P.cap + warps * 32 - 1) / (warps * 32);
         const bool prune = search == 1;
-        // Verlet lists at sort-time positions (search 1): the search runs only on build steps,
-        // the list kernel on the others; after positions moved since the sort (search 3) the
-        // search runs alone
-        VerletBufs V{};
-        if (P.verlet && search == 1)
-            V = VerletBufs{s.vrow, s.vcnt, s.xref, s.pos_of, cur.origin, s.counters + VL_FLAG};
 #define MG_DENSW_CASE(F)                                                                          \
     case F:                                                                                       \
         k_dens_warp<F><<<blocks, warps * 32, smem, st>>>(P, MG_DENS_GENOME_ARG, cur.pos, conc_in, conc_out, \
@@ -1102,18 +994,12 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.counters + 3,   \
                                                              s.work, s.ovf, s.counters + 6, X,    \
-                                                             prune, V);                           \
-        if (V.flag)                                                                               \
-            k_dens_vlist<F><<<blocks, warps * 32, smem, st>>>(P, MG_DENS_GENOME_ARG, cur.pos, conc_in, \
-                                                              conc_out, cur.genes, s.scell,      \
-                                                              s.press, s.invdens, s.flist,       \
-                                                              s.fcount, s.counters + 3, s.work,  \
-                                                              s.ovf, s.counters + 6, X, V);      \
+                                                             prune);                              \
         k_dens_ovf<F><<<(uint32_t)num_sms * 4, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out,    \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.ovf,            \
-                                                             s.counters + 6, X, prune, V.flag);   \
+                                                             s.counters + 6, X, prune);           \
         return;
         cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
         switch (flags) { MG_DENS_FLAG_SETS(MG_DENSW_CASE) default: break; }
@@ -1132,7 +1018,7 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.ovf,            \
-                                                             s.counters + 6, X, true, nullptr);   \
+                                                             s.counters + 6, X, true);            \
         return;
         cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
         switch (flags) { MG_DENS_FLAG_SETS(MG_DENSF_CASE) default: break; }
@@ -1426,10 +1312,7 @@ template <bool APPLY_BRK, bool SPECIAL>
 __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
                                                  const float4* __restrict__ force,
                                                  const uint32_t* __restrict__ brk,
-                                                 uint32_t* __restrict__ counters,
-                                                 const float4* __restrict__ xref) {
-    // xref (Verlet lists in use): positions at the last list build, by cold slot; a particle
-    // now more than half the skin away from it sets the rebuild flag
+                                                 uint32_t* __restrict__ counters) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t step = counters[5];
     const float time = *time_slot(counters, step);
@@ -1471,28 +1354,17 @@ __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
     const float dt = P.dt;
     const float vnx = ax * dt + vel.x, vny = ay * dt + vel.y, vnz = az * dt + vel.z;
     const uint32_t special = SPECIAL ? (C.genes[p] >> 11) & 3u : 0u;  // bit 0: gene 11, bit 1: gene 12
-    float4 np = pos;  // the new position
     if (special == 0) {
         C.veval[p] = make_float4((vel.x + vnx) * 0.5f, (vel.y + vny) * 0.5f, (vel.z + vnz) * 0.5f, ve.w);
         C.vel[p] = make_float4(vnx, vny, vnz, vel.w);
-        np = make_float4(pos.x + vnx * dt, pos.y + vny * dt, pos.z + vnz * dt, pos.w);
-        C.pos[p] = np;
+        C.pos[p] = make_float4(pos.x + vnx * dt, pos.y + vny * dt, pos.z + vnz * dt, pos.w);
     } else if (special == 2u) {
         // externalActuation (cuda:3617-3691): the previous state, z displaced by
         // actuation_factor * sin(time / (actuation_period * dt))
         const float ph = time / (P.actuation_period * dt);
-        np = make_float4(pos.x, pos.y, pos.z + P.actuation_factor * mg_sin_cw(ph), pos.w);
-        C.pos[p] = np;
+        C.pos[p] = make_float4(pos.x, pos.y, pos.z + P.actuation_factor * mg_sin_cw(ph), pos.w);
     }
     // fixedParticles (cuda:3694-3705, after the actuation): the previous state is kept
-    if (xref) {
-        const uint32_t id = C.origin[p];
-        if (id < P.cap) {
-            const float4 r = xref[id];
-            const float dx = np.x - r.x, dy = np.y - r.y, dz = np.z - r.z;
-            if (!(dx * dx + dy * dy + dz * dz <= P.vl_move2)) counters[VL_FLAG] = 1u;
-        }
-    }
     if (APPLY_BRK) {
         const uint32_t br = brk[p];
         if (br) apply_breaks(C.bond, P.cap, p, br);
@@ -1502,15 +1374,14 @@ __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_brk,
                     cudaStream_t st, bool special) {
     uint32_t blocks = (P.cap + 255) / 256;
-    const float4* xref = P.verlet ? s.xref : nullptr;
     if (apply_brk && special)
-        k_advance<true, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters, xref);
+        k_advance<true, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
     else if (apply_brk)
-        k_advance<true, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters, xref);
+        k_advance<true, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
     else if (special)
-        k_advance<false, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters, xref);
+        k_advance<false, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
     else
-        k_advance<false, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters, xref);
+        k_advance<false, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
 }
 
 }  // namespace mg

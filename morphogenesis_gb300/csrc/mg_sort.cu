@@ -81,9 +81,7 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
                                                 uint32_t* __restrict__ newidx,
                                                 uint32_t* __restrict__ count,
                                                 uint8_t* __restrict__ sub,
-                                                uint32_t* __restrict__ step, bool warp_order,
-                                                const uint32_t* __restrict__ origin,
-                                                uint32_t* __restrict__ pos_of) {
+                                                uint32_t* __restrict__ step, bool warp_order) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) *step += 1u;  // step counter read by the later kernels of this step
     bool in = i < P.cap;
@@ -94,11 +92,6 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
         cell[i] = c;
         newidx[i] = UNDEF;  // overwritten by the cell sort for particles inside the window
         if (c != UNDEF) sub[i] = (uint8_t)sub_of(P, pi, warp_order);
-        // a particle leaving the grid leaves the Verlet lists' index map (the gather maps the others)
-        if (c == UNDEF && pos_of) {
-            const uint32_t id = origin[i];
-            if (id < P.cap) pos_of[id] = UNDEF;
-        }
     }
     bool valid = in && c != UNDEF;
     unsigned active = __ballot_sync(0xffffffffu, valid);
@@ -117,39 +110,7 @@ void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, boo
                    cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
     k_insert<<<blocks, 256, 0, st>>>(P, cur.pos, s.cell, s.arank, s.newidx, s.count, s.sub,
-                                      s.counters + 5, warp_order, cur.origin,
-                                      P.verlet ? s.pos_of : nullptr);
-}
-
-// ---- Verlet lists after a position upload ----------------------------------------------------
-// Positions written from the host: a particle now more than half the skin away from its
-// position at the last list build, or a parked slot given a position inside the grid (it joins
-// at the next sort and is in no list), sets the rebuild flag.  Positions the host wrote back
-// unchanged keep the lists.
-__global__ void __launch_bounds__(256) k_verlet_check(DevParams P, const float4* __restrict__ pos,
-                                                      const uint32_t* __restrict__ origin,
-                                                      const float4* __restrict__ xref,
-                                                      uint32_t* __restrict__ counters) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P.cap) return;
-    const float4 x = pos[p];
-    if (p >= counters[3]) {
-        if (cell_of(P, x) != UNDEF) counters[VL_FLAG] = 1u;
-        return;
-    }
-    const uint32_t id = origin[p];
-    if (id >= P.cap) {
-        counters[VL_FLAG] = 1u;
-        return;
-    }
-    const float4 r = xref[id];
-    const float dx = x.x - r.x, dy = x.y - r.y, dz = x.z - r.z;
-    if (!(dx * dx + dy * dy + dz * dz <= P.vl_move2)) counters[VL_FLAG] = 1u;
-}
-
-void launch_verlet_check(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st) {
-    if (!P.verlet) return;
-    k_verlet_check<<<(P.cap + 255) / 256, 256, 0, st>>>(P, cur.pos, cur.origin, s.xref, s.counters);
+                                      s.counters + 5, warp_order);
 }
 
 // ---- single-pass scan (decoupled look-back) ------------------------------------------------
@@ -479,7 +440,7 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
                                                 float* __restrict__ invdens,
                                                 float4* __restrict__ force,
                                                 const uint32_t* __restrict__ nactive_p,
-                                                int parts, uint32_t* __restrict__ pos_of) {
+                                                int parts) {
     // parts: GATHER_CORE (positions, bonds, genes, origins, cells; the scratch of parked slots),
     // GATHER_CONC (concentrations), GATHER_MOTION (velocities, incoming-bond table)
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -512,10 +473,8 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
             } else {
                 D.genes[p] = __ldg(S.genes + i);
             }
-            const uint32_t id = __ldg(S.origin + i);
-            D.origin[p] = id;
+            D.origin[p] = __ldg(S.origin + i);
             scell[p] = __ldg(cell + i);
-            if (pos_of && id < cap) pos_of[id] = p;  // the Verlet lists' index map
         }
         if (parts & GATHER_MOTION) {
             D.vel[p] = __ldg(S.vel + i);
@@ -570,8 +529,7 @@ void launch_gather(const DevParams& P, const Carried& src, const float* src_conc
                    int parts) {
     uint32_t blocks = (P.cap + 255) / 256;
     k_gather<<<blocks, 256, 0, st>>>(P, src, src_conc, dst, dst_conc, s.sorted, s.newidx, s.cell,
-                                      s.scell, s.press, s.invdens, s.force, s.counters + 3, parts,
-                                      P.verlet ? s.pos_of : nullptr);
+                                      s.scell, s.press, s.invdens, s.force, s.counters + 3, parts);
 }
 
 }  // namespace mg
