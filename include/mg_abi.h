@@ -19,7 +19,8 @@
  *   FAGE/FCOLOR/FGCELL/FGNDX/FBIN/FPARTICLE_ID/FMASS_RADIUS/FNERVEIDX  uint32[N]
  *   FELASTIDX                uint32[N][6][9]        (words 1-4 and 6-7 are float bits)
  *   FPARTICLEIDX             uint32[N][12]          ((particle, bond) pairs of incoming bonds)
- *   FCONC                    float[N][16]           (device layout used by the kernels)
+ *   FCONC                    float[N][16]           (device layout used by the kernels; or
+ *                                                   float[16][N], getConc's, with MG_OPT_CONC_LAYOUT)
  *   FEPIGEN                  uint32[16][N]          ([gene][particle])
  *   FBIN_COUNT/FBIN_OFFSET   uint32[grid_total]
  *   FBIN_COUNT_ACTIVE_GENES/FBIN_OFFSET_ACTIVE_GENES  uint32[16][grid_total]
@@ -316,7 +317,12 @@ enum mg_option {
      * length, modulus and damping kept from the slot (default); 1 = makeBond's elastin defaults
      * from the genome (param[0]: elastLim, default rest length, modulus, damping,
      * fluid_system_cuda.cu:1573-1593) */
-    MG_OPT_HEAL_PARAMS = 2
+    MG_OPT_HEAL_PARAMS = 2,
+    /* layout of FCONC in mg_upload / mg_download / mg_step_io: 0 = float[N][16], the rows the
+     * kernels read (FCONC[p*16+tf], fluid_system_cuda.cu:739, 3097; default); 1 = float[16][N],
+     * the reference host's own buffer (getConc(tf) = FCONC + tf*mMaxPoints, fluid_system.h:574),
+     * transposed on the device */
+    MG_OPT_CONC_LAYOUT = 3
 };
 mg_status mg_set_option(mg_handle h, int32_t option, int32_t value);
 

@@ -151,15 +151,21 @@ class FluidSystem:
         return p
 
     # -- transfer -------------------------------------------------------------------------------
-    def upload(self, buf: int, arr: np.ndarray) -> None:
+    def _buf_shape(self, buf: int):
         dt, shape = _shape(buf, self.max_points, self.cells)
+        if buf == A.FCONC and getattr(self, "conc_species_major", False):
+            shape = (A.NUM_TF, self.max_points)  # getConc's layout (MG_OPT_CONC_LAYOUT 1)
+        return dt, shape
+
+    def upload(self, buf: int, arr: np.ndarray) -> None:
+        dt, shape = self._buf_shape(buf)
         a = np.ascontiguousarray(arr, dtype=dt)
         if a.shape != shape:
             raise ValueError(f"buffer {buf}: expected shape {shape}, got {a.shape}")
         self._check(self.lib.mg_upload(self.h, buf, a.ctypes.data, a.nbytes))
 
     def download(self, buf: int, out: np.ndarray | None = None) -> np.ndarray:
-        dt, shape = _shape(buf, self.max_points, self.cells)
+        dt, shape = self._buf_shape(buf)
         if out is None:
             out = np.empty(shape, dt)
         self._check(self.lib.mg_download(self.h, buf, out.ctypes.data, out.nbytes))
@@ -262,6 +268,8 @@ class FluidSystem:
 
     def set_option(self, option: int, value: int) -> None:
         self._check(self.lib.mg_set_option(self.h, int(option), int(value)))
+        if option == A.OPT_CONC_LAYOUT:
+            self.conc_species_major = bool(value)
 
     def autotune(self, steps: int = 5, flags: int = A.STEP_DEFAULT) -> dict:
         """Times the density pass's launch shapes on the current state (restored after each

@@ -77,6 +77,7 @@ struct mg_system {
     uint32_t* hmem = nullptr;   // re-forming candidates recorded by the density pass: count [cap]
                                 // then list [NL_CAP][cap] (allocated with the first remodelling step)
     int search = 1;             // density pass search: 0 direct walk, 1 warp-cooperative
+    int conc_species_major = 0; // FCONC exchanged as [16][N] (MG_OPT_CONC_LAYOUT 1)
     float time = 0.f;
     std::string err;
     std::map<uint64_t, cudaGraphExec_t> graphs;
@@ -455,7 +456,7 @@ void* direct_buffer(mg_system* h, int32_t id, bool upload) {
     case MG_FPRESS: return h->s.press;
     case MG_FDENSITY: return h->s.invdens;
     case MG_FPARTICLEIDX: return c.pidx;
-    case MG_FCONC: return conc_of(h, h->conc_cur);
+    case MG_FCONC: return h->conc_species_major ? nullptr : conc_of(h, h->conc_cur);
     case MG_FBIN_COUNT: return upload ? nullptr : h->s.count;
     case MG_FBIN_OFFSET: return upload ? nullptr : h->s.offset;
     default: return nullptr;
@@ -1180,7 +1181,7 @@ static mg_status enqueue_upload(mg_handle h, int32_t id, const void* host, size_
     case MG_FPRESS: dst = h->s.press; break;
     case MG_FDENSITY: dst = h->s.invdens; break;
     case MG_FPARTICLEIDX: dst = c.pidx; break;
-    case MG_FCONC: dst = conc_of(h, h->conc_cur); break;
+    case MG_FCONC: dst = h->conc_species_major ? nullptr : conc_of(h, h->conc_cur); break;
     case MG_FGCELL: case MG_FGNDX: return MG_OK;  // recomputed by insert
     default: break;
     }
@@ -1208,7 +1209,9 @@ static mg_status enqueue_upload(mg_handle h, int32_t id, const void* host, size_
     if (s2 != MG_OK) return s2;
     MG_CUDA(h, cudaMemcpyAsync(h->staging, host, bytes, cudaMemcpyHostToDevice, st));
     const uint32_t* sref = (const uint32_t*)h->staging;
-    if (id == MG_FELASTIDX) {
+    if (id == MG_FCONC) {  // species-major host layout
+        launch_conc_transpose(h->cap, (const float*)sref, conc_of(h, h->conc_cur), false, st);
+    } else if (id == MG_FELASTIDX) {
         launch_import_bonds(h->P, sref, c, h->cold, st);
         h->brk_pending = false;
     } else if (id == MG_FEPIGEN) {
@@ -1244,12 +1247,19 @@ static mg_status enqueue_download(mg_handle h, int32_t id, void* host, size_t by
     case MG_FPRESS: src = h->s.press; break;
     case MG_FDENSITY: src = h->s.invdens; break;
     case MG_FPARTICLEIDX: src = c.pidx; break;
-    case MG_FCONC: src = conc_of(h, h->conc_cur); break;
+    case MG_FCONC: src = h->conc_species_major ? nullptr : conc_of(h, h->conc_cur); break;
     case MG_FBIN_COUNT: src = h->s.count; break;
     case MG_FBIN_OFFSET: src = h->s.offset; break;
     default: break;
     }
     if (id == MG_FEPIGEN && h->P.full_epi) src = c.epi;
+    if (id == MG_FCONC && h->conc_species_major) {
+        mg_status s2 = ensure_staging(h, bytes);
+        if (s2 != MG_OK) return s2;
+        launch_conc_transpose(h->cap, conc_of(h, h->conc_cur), (float*)h->staging, true, st);
+        MG_CUDA(h, cudaMemcpyAsync(host, h->staging, bytes, cudaMemcpyDeviceToHost, st));
+        return MG_OK;
+    }
     if (src) {
         MG_CUDA(h, cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, st));
         return MG_OK;
@@ -1574,6 +1584,10 @@ mg_status mg_set_option(mg_handle h, int32_t option, int32_t value) {
         if (value < 0 || value > 1) return fail(h, MG_ERR_INVALID_ARG, "heal parameters are 0 or 1");
         h->P.heal_params = value;
         clear_graphs(h);
+        return MG_OK;
+    case MG_OPT_CONC_LAYOUT:
+        if (value < 0 || value > 1) return fail(h, MG_ERR_INVALID_ARG, "FCONC layout is 0 or 1");
+        h->conc_species_major = value;
         return MG_OK;
     default:
         return fail(h, MG_ERR_INVALID_ARG, "unknown option " + std::to_string(option));

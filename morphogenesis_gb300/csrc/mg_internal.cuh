@@ -229,6 +229,9 @@ void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bo
                     cudaStream_t st, bool special = false);
 
 // ---- import/export between the reference layouts and the device layout -------------------
+// FCONC rows [cap][16] <-> species-major [16][cap]
+void launch_conc_transpose(uint32_t cap, const float* src, float* dst, bool to_species_major,
+                           cudaStream_t st);
 void launch_import_bonds(const DevParams& P, const uint32_t* ref, const Carried& cur,
                          const Cold& cold, cudaStream_t st);
 void launch_export_bonds(const DevParams& P, const Carried& cur, const Cold& cold,

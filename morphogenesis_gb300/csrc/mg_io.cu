@@ -179,6 +179,36 @@ void launch_export_grid_index(const DevParams& P, const Scratch& s, int which, i
                                                             s.scell, s.offset, s.counters + 3, ref);
 }
 
+// FCONC between the device's particle-major rows [N][16] and the species-major layout a
+// reference host keeps (getConc(tf) = FCONC + tf * mMaxPoints, fluid_system.h:574): a 32 x 16
+// tile through shared memory so that both sides are read and written coalesced.
+__global__ void k_conc_transpose(uint32_t cap, const float* __restrict__ src, float* __restrict__ dst,
+                                 int to_species_major) {
+    __shared__ float tile[32][NTF + 1];
+    const uint32_t p0 = blockIdx.x * 32u;
+    const uint32_t tx = threadIdx.x & 31u, ty = threadIdx.x >> 5;  // 32 x 16 threads
+    if (to_species_major) {
+        for (uint32_t k = threadIdx.x; k < 32u * NTF; k += blockDim.x) {  // rows in
+            const uint32_t r = k / NTF, t = k % NTF;
+            if (p0 + r < cap) tile[r][t] = src[(size_t)(p0 + r) * NTF + t];
+        }
+        __syncthreads();
+        if (p0 + tx < cap) dst[(size_t)ty * cap + p0 + tx] = tile[tx][ty];  // species rows out
+    } else {
+        if (p0 + tx < cap) tile[tx][ty] = src[(size_t)ty * cap + p0 + tx];
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < 32u * NTF; k += blockDim.x) {
+            const uint32_t r = k / NTF, t = k % NTF;
+            if (p0 + r < cap) dst[(size_t)(p0 + r) * NTF + t] = tile[r][t];
+        }
+    }
+}
+
+void launch_conc_transpose(uint32_t cap, const float* src, float* dst, bool to_species_major,
+                           cudaStream_t st) {
+    k_conc_transpose<<<(cap + 31) / 32, 32 * NTF, 0, st>>>(cap, src, dst, to_species_major ? 1 : 0);
+}
+
 __global__ void k_fill_u32(uint32_t* p, uint32_t v, size_t n) {
     size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) p[k] = v;
