@@ -359,6 +359,7 @@ def batch_section(args):
     r = np.random.default_rng(2)
     counts = np.exp(r.uniform(np.log(1024), np.log(65536), args.batch_instances))
     members = []
+    demos = []
     total = 0
     t0 = time.perf_counter()
     for k, c in enumerate(counts):
@@ -368,8 +369,17 @@ def batch_section(args):
         fs = mg.FluidSystem(d.params, d.genome, d.n)
         fs.TransferToCL(d.arrays)
         members.append(fs)
+        demos.append(d)
         total += d.n
     build_s = time.perf_counter() - t0
+    # packed: every instance in one system, one kernel launch per stage
+    pk = mg.Packed([d.params for d in demos], [d.genome for d in demos], [d.n for d in demos])
+    pk.TransferToCL(pk.concat([d.arrays for d in demos]))
+    del demos
+    pk.Run(3)
+    ms_packed = pk.time_steps(args.batch_steps)
+    packed_launches = pk.kernel_launches()
+    pk.close()
     for fs in members:  # warm: graphs captured, caches hot
         fs.Run(3)
     b = mg.Batch(members)
@@ -381,13 +391,19 @@ def batch_section(args):
     out = {"instances": len(members), "particles": total, "steps": args.batch_steps,
            "particles_min": int(min(m.max_points for m in members)),
            "particles_max": int(max(m.max_points for m in members)),
-           "batched_ms": ms_batch, "sequential_ms": ms_seq,
+           "packed_ms": ms_packed, "batched_ms": ms_batch, "sequential_ms": ms_seq,
+           "packed_particle_steps_s": total * args.batch_steps / (ms_packed / 1e3),
            "batched_particle_steps_s": total * args.batch_steps / (ms_batch / 1e3),
            "sequential_particle_steps_s": total * args.batch_steps / (ms_seq / 1e3),
-           "speedup": ms_seq / ms_batch, "setup_s": build_s,
-           "design": "one CUDA graph launch per step holding every instance's step graph, in "
-                     "groups of 32 independent branches joined before the next group (instances "
-                     "keep their own arenas, grids and genomes)"}
+           "speedup_packed_vs_sequential": ms_seq / ms_packed, "speedup": ms_seq / ms_batch,
+           "packed_kernel_launches_per_step": packed_launches / (args.batch_steps + 3),
+           "setup_s": build_s,
+           "design": {"packed": "every instance in one system (mg_create_packed): one kernel launch "
+                                "per stage over all instances' particles, instance slabs stacked in a "
+                                "shared grid, each instance in its own frame with its own box, grid, "
+                                "stiffness and genome",
+                      "batched": "one CUDA graph launch per step holding every instance's step graph, "
+                                 "in groups of 32 independent branches joined before the next group"}}
     b.close()
     for fs in members:
         fs.close()

@@ -445,6 +445,24 @@ mg_status mg_write_points_vtp(const char* dir, int32_t frame, const mg_points* p
                               const float* veval, const float* force, const float* press,
                               const float* invdens, const float volmin[3], const float volmax[3]);
 
+/* ---- packed instances (parameter sweeps in one system) ------------------------------------------
+ * n_inst independent tissues advanced as one system: every stage is one kernel launch over all
+ * instances' particles.  Instance k keeps its own parameters' box, grid (origin, resolution;
+ * the cell size is shared), intstiff and genome, and its own coordinate frame, so each instance
+ * evaluates exactly what it evaluates as a system of its own (same bits); the other
+ * parameters must be equal.  Its cells are a slab of a shared grid (slabs stacked along y), so
+ * after each sort its particles are one contiguous segment of the sorted order
+ * (mg_instance_ranges).  Buffers are exchanged like a single system of sum(max_points)
+ * particles: instance 0's particles first, bond partners and incoming-bond entries as indices
+ * into that concatenation; FGCELL / FBIN_* refer to the shared grid.  Steps take
+ * MG_STEP_PHYSICS / GENES / FREEZE (no surrogate, remodelling or special particles);
+ * parameters and genomes are fixed at creation.  The reference runs a sweep as separate jobs
+ * (src/slurm/Morphogenesis_param_sweep.slurm; axes in src/SpecfileBatchGenerator.cpp:87-192). */
+mg_status mg_create_packed(const mg_fparams* params, const mg_genome* genomes,
+                           const uint32_t* max_points, uint32_t n_inst, mg_handle* out);
+/* Sorted-index segment [first[k], first[k] + count[k]) of instance k after the last sort. */
+mg_status mg_instance_ranges(mg_handle h, uint32_t* first, uint32_t* count);
+
 /* ---- batched instances (parameter sweeps) --------------------------------------------------- */
 /* A batch steps many independent systems together (each keeps its own particles, grid,
  * parameters and genome): one CUDA graph launch per step advances every member, the members'

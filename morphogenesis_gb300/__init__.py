@@ -378,3 +378,81 @@ class Batch:
         except Exception:
             pass
 
+
+
+# buffers whose entries are particle indices of the same system (shifted when instances are packed)
+_INDEX_WORDS = {A.FELASTIDX: (A.BOND_DATA, (0,), 9), A.FPARTICLEIDX: (12, (0,), 2)}
+
+
+class Packed(FluidSystem):
+    """Independent tissues advanced as one system (mg_create_packed): every stage is one kernel
+    launch over all instances' particles, each instance keeping its own box, grid, stiffness,
+    genome and coordinate frame (so it computes exactly what it computes alone).  Buffers are
+    exchanged as one system of sum(counts) particles, instance 0's first (`concat` builds them
+    from per-instance arrays, `split` cuts a downloaded buffer back into instances).  The
+    reference runs such a sweep as separate jobs (src/slurm/Morphogenesis_param_sweep.slurm)."""
+
+    def __init__(self, params_list, genome_list, counts):
+        self.lib = load()
+        k = len(params_list)
+        if k == 0 or len(genome_list) != k or len(counts) != k:
+            raise ValueError("one parameter set, genome and particle count per instance")
+        self.counts = [int(c) for c in counts]
+        self.offsets = np.concatenate([[0], np.cumsum(self.counts)]).astype(np.int64)
+        self.params = params_list[0]
+        self.genome = genome_list[0]
+        self.max_points = int(self.offsets[-1])
+        P = (A.FParams * k)(*params_list)
+        G = (A.Genome * k)(*genome_list)
+        cnt = (C.c_uint32 * k)(*self.counts)
+        h = C.c_void_p()
+        self._check(self.lib.mg_create_packed(P, G, cnt, k, C.byref(h)), None)
+        self.h = h
+        self.cells = int(self.GetParams().grid_total)
+
+    def concat(self, arrays_list) -> dict:
+        """Per-instance arrays in the reference layouts -> one dict for TransferToCL: rows
+        stacked in instance order (FEPIGEN along its particle axis), bond partners and incoming
+        entries shifted by the instance's first slot (no-partner values kept)."""
+        out = {}
+        for buf in arrays_list[0]:
+            parts = []
+            for j, arrs in enumerate(arrays_list):
+                a = np.array(arrs[buf], copy=True)
+                if buf in _INDEX_WORDS:
+                    width, cols, stride = _INDEX_WORDS[buf]
+                    v = a.reshape(self.counts[j], -1)
+                    for c0 in cols:
+                        col = v[:, c0::stride]
+                        valid = col < self.counts[j]
+                        col[valid] += np.uint32(self.offsets[j])
+                        col[~valid] = A.NO_PARTNER
+                        v[:, c0::stride] = col
+                parts.append(a)
+            axis = 1 if buf == A.FEPIGEN else 0
+            out[buf] = np.ascontiguousarray(np.concatenate(parts, axis=axis))
+        return out
+
+    def ranges(self):
+        """Sorted-index segment (first, count) of every instance after the last sort."""
+        k = len(self.counts)
+        first, count = (C.c_uint32 * k)(), (C.c_uint32 * k)()
+        self._check(self.lib.mg_instance_ranges(self.h, first, count))
+        return [(int(first[j]), int(count[j])) for j in range(k)]
+
+    def split(self, buf: int, arr: np.ndarray | None = None) -> list:
+        """A downloaded buffer cut into the instances' sorted segments, indices made local."""
+        a = self.download(buf) if arr is None else arr
+        out = []
+        for (f, c) in self.ranges():
+            part = np.array(a[:, f:f + c] if buf == A.FEPIGEN else a[f:f + c], copy=True)
+            if buf in _INDEX_WORDS:
+                width, cols, stride = _INDEX_WORDS[buf]
+                v = part.reshape(c, -1)
+                for c0 in cols:
+                    col = v[:, c0::stride]
+                    inside = (col >= f) & (col < f + c)
+                    col[inside] -= np.uint32(f)
+                    v[:, c0::stride] = col
+            out.append(part)
+        return out

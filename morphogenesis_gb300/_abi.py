@@ -216,6 +216,9 @@ SIGNATURES = [
     ("mg_batch_time_steps", C.c_int, [H, C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]),
     ("mg_prefix_sum_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mg_selftest_bounded_wait", C.c_int, [C.c_int32, C.c_uint32]),
+    ("mg_create_packed", C.c_int, [C.POINTER(FParams), C.POINTER(Genome), C.POINTER(C.c_uint32), C.c_uint32,
+                                   C.POINTER(H)]),
+    ("mg_instance_ranges", C.c_int, [H, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
 ]
 
 _lib = None

@@ -7,6 +7,7 @@
 // (fluid_system.cpp:1919-2014).  Where the reference calls clFinish after every kernel and
 // reads counts back to the host every sort, the whole step here is one CUDA graph with the
 // active particle count kept on the device.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -101,6 +102,12 @@ struct mg_system {
     uint32_t* sur_stats = nullptr;   // [0] judged, [1] handed over, [2] worst relative error bits
     uint32_t judge_period = 10, judge_stride = 64;
     float judge_threshold = 1e-3f;
+    // packed instances (mg_create_packed): per-instance frames, genomes and particle counts
+    uint32_t n_inst = 0;
+    InstParams* d_inst = nullptr;       // [n_inst] in the arena
+    DevGenome* d_genomes = nullptr;     // [n_inst] in the arena
+    std::vector<InstParams> inst;       // host copy
+    std::vector<uint32_t> inst_count;   // particles per instance (slots in upload order)
 };
 
 struct mg_mlp_s {
@@ -225,6 +232,8 @@ void clear_graphs(mg_system* h);
 // (countdowns and activation lists), initialised from the current gene bits.
 mg_status enable_full_epi(mg_system* h) {
     if (h->P.full_epi) return MG_OK;
+    if (h->P.n_inst)
+        return fail(h, MG_ERR_UNSUPPORTED, "packed instances keep gene bits only (no FEPIGEN countdowns or activation lists)");
     const size_t words = (size_t)NG * h->cap;
     cudaError_t e = cudaMalloc(&h->epi_mem, 2 * words * sizeof(uint32_t));
     if (e != cudaSuccess) {
@@ -241,10 +250,10 @@ mg_status enable_full_epi(mg_system* h) {
     return MG_OK;
 }
 
-mg_status upload_genome(mg_system* h) {
-    DevGenome g;
+// The device form of a genome (rates and weights as float, sparse lists compacted); an empty
+// string when it is valid, else the reason.
+std::string make_dev_genome(const mg_genome& G, DevGenome& g) {
     std::memset(&g, 0, sizeof(g));
-    const mg_genome& G = h->genome;
     for (int a = 0; a < NG; a++)
         for (int t = 0; t < NTF; t++) g.sens[a][t] = G.sensitivity[a][t];
     for (int t = 0; t < NTF; t++) {
@@ -253,11 +262,11 @@ mg_status upload_genome(mg_system* h) {
     }
     for (int a = 0; a < NG; a++) {
         int ns = (int)G.secrete[a][2 * NTF];
-        if (ns < 0 || ns > NTF) return fail(h, MG_ERR_INVALID_ARG, "secrete list count out of range");
+        if (ns < 0 || ns > NTF) return "secrete list count out of range";
         int k = 0;
         for (int j = 0; j < ns; j++) {
             int tf = (int)G.secrete[a][2 * j];
-            if (tf < 0 || tf >= NTF) return fail(h, MG_ERR_INVALID_ARG, "secrete list names a species out of range");
+            if (tf < 0 || tf >= NTF) return "secrete list names a species out of range";
             g.sec_tf[a][k] = tf;
             g.sec_rate[a][k] = G.secrete[a][2 * j + 1];
             k++;
@@ -281,16 +290,29 @@ mg_status upload_genome(mg_system* h) {
         for (int k = 0; k < 8; k++) g.tanh_p[t][k] = G.tanh_param[t][k];
         for (int k = 0; k < 12; k++) g.bparam[t][k] = G.param[t][k];
     }
+    int uniform = g.diff[0] != 0.f;
+    for (int t = 1; t < NTF; t++) uniform &= g.diff[t] == g.diff[0];
+    g.uniform = uniform;
+    return std::string();
+}
+
+bool has_activations(const DevGenome& g) {
     bool activations = false;
     for (int a = 0; a < NG; a++) activations |= g.nact[a] > 0;
-    if (activations) {  // activations change FEPIGEN words: keep the full state
+    return activations;
+}
+
+mg_status upload_genome(mg_system* h) {
+    DevGenome g;
+    const std::string why = make_dev_genome(h->genome, g);
+    if (!why.empty()) return fail(h, MG_ERR_INVALID_ARG, why);
+    if (has_activations(g)) {  // activations change FEPIGEN words: keep the full state
+        if (h->P.n_inst) return fail(h, MG_ERR_UNSUPPORTED, "packed instances take genomes without activation lists");
         mg_status st = enable_full_epi(h);
         if (st != MG_OK) return st;
     }
-    int uniform = g.diff[0] != 0.f;
-    for (int t = 1; t < NTF; t++) uniform &= g.diff[t] == g.diff[0];
-    if (h->P.uniform_diff != uniform) clear_graphs(h);
-    h->P.uniform_diff = uniform;
+    if (h->P.uniform_diff != g.uniform) clear_graphs(h);
+    h->P.uniform_diff = g.uniform;
     h->hG = g;
     clear_graphs(h);  // captured density launches hold the genome by value
     MG_CUDA(h, cudaMemcpyAsync(h->dG, &g, sizeof(g), cudaMemcpyHostToDevice, h->stream));
@@ -747,7 +769,18 @@ void after_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
     h->drifted = (flags & MG_STEP_PHYSICS) != 0;
 }
 
+// Packed instances step physics and the plain morphogen stage (the batched sweep); the
+// surrogate, remodelling and special particles run on single systems.
+mg_status packed_flags_ok(mg_system* h, uint32_t flags) {
+    if (h->n_inst && (flags & (MG_STEP_SURROGATE | MG_STEP_REMODEL | MG_STEP_BOND_CHANGES | MG_STEP_SPECIAL)))
+        return fail(h, MG_ERR_UNSUPPORTED,
+                    "packed instances step physics and the plain morphogen stage only (no surrogate, "
+                    "remodelling or special particles)");
+    return MG_OK;
+}
+
 mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
+    if (mg_status st0 = packed_flags_ok(h, flags)) return st0;
     if ((flags & MG_STEP_SURROGATE) && !h->sur)
         return fail(h, MG_ERR_INVALID_ARG, "surrogate step without an attached network (mg_set_surrogate)");
     if ((flags & MG_STEP_SURROGATE) && h->P.full_epi)
@@ -939,8 +972,10 @@ mg_status mg_setup_grid(mg_fparams* p, const float vol_min[3], const float vol_m
     return MG_OK;
 }
 
-mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t max_points,
-                    mg_handle* out) {
+// A system of max_points particles; n_inst > 0 adds the tables of packed instances (their
+// frames, genomes and the per-particle instance ids), which mg_create_packed fills.
+static mg_status create_system(const mg_fparams* params, const mg_genome* genome, uint32_t max_points,
+                               uint32_t n_inst, mg_handle* out) {
     if (!out) return fail(nullptr, MG_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
     mg_status st = check_params(nullptr, params);
@@ -978,6 +1013,11 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
         plan.push_back({(void**)&c.conc, 64 * n});
         plan.push_back({(void**)&c.genes, 4 * n});
         plan.push_back({(void**)&c.origin, 4 * n});
+        if (n_inst) plan.push_back({(void**)&c.iid, 4 * n});
+    }
+    if (n_inst) {
+        plan.push_back({(void**)&h->d_inst, sizeof(InstParams) * (size_t)n_inst});
+        plan.push_back({(void**)&h->d_genomes, sizeof(DevGenome) * (size_t)n_inst});
     }
     plan.push_back({(void**)&h->cold.age, 4 * n});
     plan.push_back({(void**)&h->cold.color, 4 * n});
@@ -1050,6 +1090,129 @@ mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t 
     return MG_OK;
 }
 
+mg_status mg_create(const mg_fparams* params, const mg_genome* genome, uint32_t max_points,
+                    mg_handle* out) {
+    return create_system(params, genome, max_points, 0, out);
+}
+
+// ---- packed instances --------------------------------------------------------------------------
+mg_status mg_create_packed(const mg_fparams* params, const mg_genome* genomes,
+                           const uint32_t* max_points, uint32_t n_inst, mg_handle* out) {
+    if (!out || !params || !genomes || !max_points || n_inst == 0)
+        return fail(nullptr, MG_ERR_INVALID_ARG, "mg_create_packed: bad arguments");
+    *out = nullptr;
+    const mg_fparams& a = params[0];
+    uint64_t cap = 0;
+    long long rx = 0, ry = 0, rz = 0;
+    for (uint32_t k = 0; k < n_inst; k++) {
+        const mg_fparams& q = params[k];
+        mg_status st = check_params(nullptr, &q);
+        if (st != MG_OK) return st;
+        if (max_points[k] == 0) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_create_packed: an instance has no particles");
+        cap += max_points[k];
+        // everything but the stiffness, the box and the grid's placement and size is shared
+        const bool same = q.psimscale == a.psimscale && q.psmoothradius == a.psmoothradius &&
+            q.pradius == a.pradius && q.pmass == a.pmass && q.prest_dens == a.prest_dens &&
+            q.pextstiff == a.pextstiff && q.pvisc == a.pvisc && q.psurface_t == a.psurface_t &&
+            q.pdamp == a.pdamp && q.pforce_min == a.pforce_min && q.pforce_max == a.pforce_max &&
+            q.pforce_freq == a.pforce_freq && q.pground_slope == a.pground_slope &&
+            q.pgravity[0] == a.pgravity[0] && q.pgravity[1] == a.pgravity[1] && q.pgravity[2] == a.pgravity[2] &&
+            q.paccel_limit == a.paccel_limit && q.pvel_limit == a.pvel_limit &&
+            q.actuation_factor == a.actuation_factor && q.actuation_period == a.actuation_period &&
+            q.grid_delta[0] == a.grid_delta[0] && q.grid_delta[1] == a.grid_delta[1] &&
+            q.grid_delta[2] == a.grid_delta[2] && q.grid_srch == 3 && q.dt == a.dt &&
+            q.time == a.time && q.freeze == a.freeze;
+        if (!same)
+            return fail(nullptr, MG_ERR_INVALID_ARG,
+                        "mg_create_packed: instance " + std::to_string(k) +
+                            " differs from instance 0 in more than its stiffness, box and grid "
+                            "(27-cell window and equal cell size required)");
+        rx = std::max<long long>(rx, q.grid_res[0]);
+        rz = std::max<long long>(rz, q.grid_res[2]);
+        ry += q.grid_res[1];
+    }
+    if (cap >= 0x80000000ull) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_create_packed: more than 2^31 particles");
+    if (rx * ry * rz > 0x7fffffffLL) return fail(nullptr, MG_ERR_INVALID_ARG, "mg_create_packed: shared grid above 2^31 cells");
+    // the shared grid: instance slabs stacked along y, x and z as wide as the widest instance
+    mg_fparams g = a;
+    g.grid_res[0] = (int32_t)rx;
+    g.grid_res[1] = (int32_t)ry;
+    g.grid_res[2] = (int32_t)rz;
+    g.grid_total = (int32_t)(rx * ry * rz);
+    for (int d = 0; d < 3; d++) {
+        g.grid_size[d] = (float)g.grid_res[d] / a.grid_delta[d];
+        g.grid_max[d] = g.grid_min[d] + g.grid_size[d];
+    }
+    mg_handle h = nullptr;
+    mg_status st = create_system(&g, &genomes[0], (uint32_t)cap, n_inst, &h);
+    if (st != MG_OK) return st;
+    h->n_inst = n_inst;
+    h->inst.resize(n_inst);
+    h->inst_count.assign(max_points, max_points + n_inst);
+    std::vector<DevGenome> dg(n_inst);
+    int ybase = 0;
+    for (uint32_t k = 0; k < n_inst; k++) {
+        const mg_fparams& q = params[k];
+        InstParams& I = h->inst[k];
+        std::memset(&I, 0, sizeof(I));
+        for (int d = 0; d < 3; d++) {
+            I.gmin[d] = q.grid_min[d];
+            I.gdelta[d] = q.grid_delta[d];
+            I.gcell[d] = 1.f / q.grid_delta[d];
+            I.res[d] = q.grid_res[d];
+            I.scanmax[d] = q.grid_res[d] - q.grid_srch;
+            I.bmin[d] = q.pboundmin[d];
+            I.bmax[d] = q.pboundmax[d];
+        }
+        I.ybase = ybase;
+        I.frame_y = (float)((double)q.grid_min[1] - (double)ybase / (double)q.grid_delta[1]);
+        I.istiff = q.pintstiff;
+        ybase += q.grid_res[1];
+        const std::string why = make_dev_genome(genomes[k], dg[k]);
+        if (!why.empty() || has_activations(dg[k])) {
+            mg_destroy(h);
+            return fail(nullptr, MG_ERR_INVALID_ARG,
+                        "mg_create_packed: genome " + std::to_string(k) + ": " +
+                            (why.empty() ? std::string("activation lists are not supported") : why));
+        }
+    }
+    // the instance of every slot, in upload order (instance 0's particles first)
+    std::vector<uint32_t> iid((size_t)cap);
+    size_t o = 0;
+    for (uint32_t k = 0; k < n_inst; k++)
+        for (uint32_t j = 0; j < max_points[k]; j++) iid[o++] = k;
+    cudaStream_t s0 = h->stream;
+    cudaError_t e = cudaMemcpyAsync(h->d_inst, h->inst.data(), sizeof(InstParams) * n_inst, cudaMemcpyHostToDevice, s0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_genomes, dg.data(), sizeof(DevGenome) * n_inst, cudaMemcpyHostToDevice, s0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->set[h->cur].iid, iid.data(), 4 * cap, cudaMemcpyHostToDevice, s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->set[1 - h->cur].iid, 0xFF, 4 * cap, s0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
+    if (e != cudaSuccess) {
+        mg_destroy(h);
+        return cuda_fail(nullptr, e, "mg_create_packed");
+    }
+    h->P.inst = h->d_inst;
+    h->P.genomes = h->d_genomes;
+    h->P.n_inst = (int)n_inst;
+    clear_graphs(h);
+    *out = h;
+    return MG_OK;
+}
+
+mg_status mg_instance_ranges(mg_handle h, uint32_t* first, uint32_t* count) {
+    if (!h || !first || !count) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    if (!h->n_inst) return fail(h, MG_ERR_INVALID_ARG, "mg_instance_ranges: not a packed system");
+    if (!h->ever_sorted) return fail(h, MG_ERR_INVALID_ARG, "mg_instance_ranges: the particles have not been sorted");
+    mg_status st = MG_OK;
+    const uint32_t nact = read_word(h, h->s.counters + 3, &st);
+    for (uint32_t k = 0; k < h->n_inst && st == MG_OK; k++) {
+        const size_t cell0 = (size_t)h->inst[k].ybase * (size_t)h->P.res[2] * (size_t)h->P.res[0];
+        first[k] = read_word(h, h->s.offset + cell0, &st);
+    }
+    for (uint32_t k = 0; k < h->n_inst; k++) count[k] = (k + 1 < h->n_inst ? first[k + 1] : nact) - first[k];
+    return st;
+}
+
 mg_status mg_destroy(mg_handle h) {
     if (!h) return MG_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -1074,6 +1237,7 @@ mg_status mg_destroy(mg_handle h) {
 
 mg_status mg_update_params(mg_handle h, const mg_fparams* p) {
     if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    if (h->n_inst) return fail(h, MG_ERR_UNSUPPORTED, "packed instances keep the parameters they were created with");
     mg_status st = check_params(h, p);
     if (st != MG_OK) return st;
     if (p->grid_total != h->params.grid_total)
@@ -1102,6 +1266,7 @@ mg_status mg_update_params(mg_handle h, const mg_fparams* p) {
 
 mg_status mg_update_genome(mg_handle h, const mg_genome* g) {
     if (!h || !g) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    if (h->n_inst) return fail(h, MG_ERR_UNSUPPORTED, "packed instances keep the genomes they were created with");
     mg_genome saved = h->genome;
     h->genome = *g;
     mg_status st = upload_genome(h);
@@ -1325,6 +1490,7 @@ mg_status mg_step_io(mg_handle h, const mg_io* in, uint32_t nin, uint32_t nsteps
                      const mg_io* out, uint32_t nout) {
     if (!h || (nin && !in) || (nout && !out)) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
     if (h->profile) return fail(h, MG_ERR_INVALID_ARG, "mg_step_io: profiling is on");
+    if (mg_status st0 = packed_flags_ok(h, flags)) return st0;
     // Plain-copy buffers with the right sizes in page-locked host memory: the copies go into the
     // steps' graphs, overlapped with the first step (uploads) and the last (downloads).
     // Anything else goes the sequential way below.
@@ -1394,7 +1560,7 @@ mg_status mg_get_counts(mg_handle h, uint32_t* num_points, uint32_t* active_poin
     uint32_t n = read_word(h, h->s.counters + 3, &st);
     if (st != MG_OK) return st;
     uint32_t a = n;
-    if (h->ever_sorted || h->phase == PHASE_INSERTED) {
+    if (!h->n_inst && (h->ever_sorted || h->phase == PHASE_INSERTED)) {
         const DevParams& P = h->P;
         long long corner = ((long long)P.scanmax[1] * P.res[2] + P.scanmax[2]) * P.res[0] + P.scanmax[0];
         if (corner >= 0 && corner < (long long)P.cells) a = read_word(h, h->s.offset + corner, &st);
@@ -1480,6 +1646,7 @@ mg_status mg_advance(mg_handle h) {
 }
 
 mg_status mg_run_remodelling(mg_handle h) {
+    if (h && h->n_inst) return packed_flags_ok(h, MG_STEP_REMODEL);
     mg_status st = need_sorted(h);
     if (st != MG_OK) return st;
     launch_remodel(h->P, h->dG, h->set[h->cur], h->cold, h->s, h->changes_valid, !h->drifted, nullptr,
@@ -1488,6 +1655,7 @@ mg_status mg_run_remodelling(mg_handle h) {
 }
 
 mg_status mg_compute_bond_changes(mg_handle h, uint32_t steps_per_inner_loop) {
+    if (h && h->n_inst) return packed_flags_ok(h, MG_STEP_BOND_CHANGES);
     mg_status st = need_sorted(h);
     if (st != MG_OK) return st;
     if (steps_per_inner_loop == 0) return fail(h, MG_ERR_INVALID_ARG, "steps_per_InnerPhysicalLoop is 0");
@@ -1571,6 +1739,8 @@ mg_status mg_set_option(mg_handle h, int32_t option, int32_t value) {
     switch (option) {
     case MG_OPT_NEIGHBOR_SEARCH:
         if (value < 0 || value > 2) return fail(h, MG_ERR_INVALID_ARG, "neighbour search is 0, 1 or 2");
+        if (h->n_inst && value != 1)
+            return fail(h, MG_ERR_UNSUPPORTED, "packed instances use the warp-cooperative search (1)");
         if (value == 2 && h->P.gsrch != 3)
             return fail(h, MG_ERR_UNSUPPORTED, "the fine-cell search needs the 27-cell window (gsrch 3)");
         if (value == 2) h->P.sub_bits = 1;  // its sub-cells are the 2x2x2 halves of a cell
@@ -1817,6 +1987,7 @@ mg_status mg_dataset_read(mg_dataset d, uint64_t first, uint32_t n, float* x, fl
 
 mg_status mg_dataset_capture(mg_dataset d, mg_handle h, uint32_t flags) {
     if (!d || !h) return fail(h, MG_ERR_INVALID_ARG, "mg_dataset_capture: NULL argument");
+    if (h->n_inst) return packed_flags_ok(h, MG_STEP_SURROGATE);
     if (d->size + h->cap > d->capacity) return fail(h, MG_ERR_LIST_OVERFLOW, "mg_dataset_capture: dataset full");
     enqueue_insert_rank(h, false);
     enqueue_gather(h, false);
@@ -1863,6 +2034,7 @@ mg_status mg_mlp_train(mg_mlp m, mg_dataset d, uint32_t steps, uint32_t batch, f
 mg_status mg_set_surrogate(mg_handle h, mg_mlp m, uint32_t judge_period, uint32_t judge_stride,
                            float threshold) {
     if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    if (h->n_inst && m) return packed_flags_ok(h, MG_STEP_SURROGATE);
     clear_graphs(h);
     if (!m) {
         h->sur = nullptr;
@@ -1950,7 +2122,7 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
         st = fail(h, MG_ERR_CUDA, "mg_autotune: events");
     for (const Cand& c : cands) {
         if (st != MG_OK) break;
-        if (c.search == 2 && !fine_ok) continue;
+        if (c.search == 2 && (!fine_ok || h->n_inst)) continue;
         h->search = c.search;
         h->P.dens_warps = c.warps;
         h->P.group_mode = c.group;
@@ -2012,6 +2184,8 @@ mg_status mg_set_tuning(mg_handle h, const int32_t* choice) {
                     "tuning: warps 4 or 8, group mode 0 or 1, sub-cell bits 1 or 2, search 0-2");
     if (choice[3] == 2 && (choice[2] != 1 || h->P.gsrch != 3))
         return fail(h, MG_ERR_INVALID_ARG, "the fine-cell search needs sub-cell bits 1 and gsrch 3");
+    if (h->n_inst && choice[3] != 1)
+        return fail(h, MG_ERR_UNSUPPORTED, "packed instances use the warp-cooperative search (1)");
     if (choice[3] == 2 && (h->search != 2 || h->P.sub_bits != 1) && h->phase == PHASE_SORTED)
         h->phase = PHASE_UNSORTED;  // the fine-cell search needs a sort made for it
     h->P.dens_warps = choice[0];

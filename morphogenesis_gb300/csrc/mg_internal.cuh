@@ -53,6 +53,21 @@ enum : uint32_t {
 };
 
 // Simulation parameters passed by value to every kernel (constant bank).
+// Packed instances (independent tissues advanced as one system, mg_create_packed): the frame
+// and the per-instance physics of instance k.  Every instance keeps its own coordinates and its
+// own grid geometry (origin, cell size, resolution, scan limits); its cells are placed in a
+// slab of the shared grid starting at row y = ybase, with the same x and z indices, so that its
+// particles sort into one contiguous segment and every kernel evaluates exactly the
+// expressions it evaluates for the instance alone.
+struct InstParams {
+    float gmin[3], gdelta[3], gcell[3];
+    int res[3], scanmax[3];
+    int ybase;
+    float frame_y;  // y of the shared grid's row 0 in this instance's frame (gmin.y - ybase * cell)
+    float istiff;
+    float bmin[3], bmax[3];
+};
+
 struct DevParams {
     float gmin[3], gdelta[3];
     float gcell[3];  // 1 / gdelta: a grid cell's extent per axis
@@ -74,6 +89,11 @@ struct DevParams {
     int heal_params;  // healed bonds: 0 rest length = distance (D5), 1 makeBond's genome defaults
     uint32_t cap;
     uint32_t cells;
+    // packed instances (null / 0 for a single system): per-instance frames and physics,
+    // per-instance genomes
+    const InstParams* inst;
+    const struct DevGenome* genomes;
+    int n_inst;
 };
 
 // Genome in device memory (float-widened, compacted sparse lists).
@@ -91,6 +111,7 @@ struct DevGenome {
     float tanh_p[3][8];   // bond remodelling tanh parameters per bond type (l_a..l_d, s_a..s_d)
     float bparam[3][12];  // bond parameters per bond type (elastLim = 8, default rest length,
                           // modulus, damping = 9, 10, 11)
+    int uniform;          // all 16 diffusion rates equal and nonzero
 };
 
 struct Carried {
@@ -103,6 +124,7 @@ struct Carried {
     uint32_t* genes;
     uint32_t* origin;
     uint32_t* epi;  // [16][cap] FEPIGEN words when the full epigenetic state is kept, else null
+    uint32_t* iid;  // packed instances: the particle's instance (UNDEF for parked slots), else null
 };
 
 struct Cold {
@@ -196,6 +218,7 @@ struct DensExtra {
     // number (0xFFFFFFFF: not recorded, the particle overflowed)
     uint32_t* hlist;
     uint32_t* hcount;
+    const uint32_t* iid;       // packed instances: instance of each sorted particle, else null
 };
 // G: the genome in device memory; Gh: its host copy, passed by value to the warp search so
 // its uniform reads go through the constant cache

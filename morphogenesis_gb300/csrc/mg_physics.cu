@@ -285,7 +285,7 @@ __device__ __forceinline__ void dens_epilogue(const DevParams& P, const DevGenom
     if (F::DENS) {
         sum = sum * P.pmass * P.wc2;
         if (sum == 0.f) sum = 1.f;
-        press[p] = (sum - P.rest) * P.istiff;
+        press[p] = (sum - P.rest) * (X.iid ? P.inst[X.iid[p]].istiff : P.istiff);
         invdens[p] = 1.f / sum;
     }
     const uint32_t gene_word = (F::GENE || F::MEAN || F::JUDGE) ? genes[p] : 0u;
@@ -471,7 +471,7 @@ __device__ __forceinline__ void dens_list_finish(
             if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
             if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
                 conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2,
-                                             P.uniform_diff != 0, true);
+                                             G->uniform != 0, true);
                 mcnt++;
                 if (X.hlist) X.hlist[(size_t)nh++ * P.cap + slot] = q;  // nh <= n <= NL_CAP
             }
@@ -559,6 +559,9 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
         // non-empty ones are then taken in order.
         const int ncx = wx1 - wx0 + 1, ncz = wz1 - wz0 + 1;
         const int ncell = ncx * ncz * (wy1 - wy0 + 1);
+        // packed instances: the group's instance, whose frame places its cells (a group's cells
+        // belong to one instance)
+        const uint32_t ginst = X.iid ? X.iid[__shfl_sync(0xffffffffu, p, leader)] : UNDEF;
         for (int cb = 0; cb < ncell; cb += 32) {
             const int t = cb + (int)lane;
             uint32_t tcnt = 0, toff = 0, tpos = 0;  // tpos: the cell's offsets in the window
@@ -566,7 +569,8 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                 const int ox = t % ncx, oz = (t / ncx) % ncz, oy = t / (ncx * ncz);
                 tpos = (uint32_t)ox | ((uint32_t)oy << 8) | ((uint32_t)oz << 16);
                 const int cx = wx0 + ox, cz = wz0 + oz, cy = wy0 + oy;
-                if (!prune || cell_meets_box(P, cx, cy, cz, tx0 - Rf, tx1 + Rf, ty0 - Rf, ty1 + Rf, tz0 - Rf, tz1 + Rf)) {
+                if (!prune || cell_meets_box(ginst != UNDEF ? frame_of(P, ginst) : frame_of(P), cx, cy, cz,
+                                             tx0 - Rf, tx1 + Rf, ty0 - Rf, ty1 + Rf, tz0 - Rf, tz1 + Rf)) {
                     const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
                     tcnt = count[cell];
                     if (tcnt) toff = offset[cell];
@@ -661,7 +665,9 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
         if (X.hlist) X.hcount[k] = UNDEF;
         return;
     }
-    dens_list_finish<FLAGS>(P, G, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,
+    // packed instances: the particle's own genome
+    const DevGenome* __restrict__ Gl = X.iid ? P.genomes + X.iid[p] : G;
+    dens_list_finish<FLAGS>(P, Gl, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,
                             fcount, X, k);
 }
 
@@ -819,7 +825,7 @@ __device__ __forceinline__ void ovf_apply(const DevParams& P, uint32_t p, uint32
 
 template <int FLAGS>
 __global__ void __launch_bounds__(256, 1) k_dens_ovf(
-    DevParams P, const DevGenome* __restrict__ G, const float4* __restrict__ pos,
+    DevParams P, const DevGenome* __restrict__ G0, const float4* __restrict__ pos,
     const float* __restrict__ conc_in, float* __restrict__ conc_out,
     const uint32_t* __restrict__ genes, const uint32_t* __restrict__ scell,
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
@@ -846,6 +852,8 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
     for (uint32_t e = gw; e < nq; e += nw) {
         const uint32_t p = ovf[e];
         const float4 ip = pos[p];
+        const DevGenome* __restrict__ G = X.iid ? P.genomes + X.iid[p] : G0;
+        const CellFrame frame = X.iid ? frame_of(P, X.iid[p]) : frame_of(P);
         const float cur_t = (F::DIFF || F::GENE || F::MEAN) ? conc_in[(size_t)p * NTF + t] : 0.f;
         const float dif_t = F::DIFF ? G->diff[t] : 0.f;
         const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
@@ -864,7 +872,7 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
                 const int cx = (int)(cellc % (uint32_t)P.res[0]);
                 const int cz = (int)((cellc / (uint32_t)P.res[0]) % (uint32_t)P.res[2]);
                 const int cy = (int)(cellc / ((uint32_t)P.res[0] * (uint32_t)P.res[2]));
-                if (!prune || cell_meets_box(P, cx, cy, cz, ip.x - Rf, ip.x + Rf, ip.y - Rf, ip.y + Rf,
+                if (!prune || cell_meets_box(frame, cx, cy, cz, ip.x - Rf, ip.x + Rf, ip.y - Rf, ip.y + Rf,
                                              ip.z - Rf, ip.z + Rf)) {
                     cnt = count[cellc];
                     if (cnt) off = offset[cellc];
@@ -982,6 +990,7 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
                  cudaStream_t st, const DensExtra* extra) {
     DensExtra X = extra ? *extra : DensExtra{};
     X.epi = P.full_epi ? cur.epi : nullptr;
+    X.iid = cur.iid;
     const int warps = (P.dens_warps >= 1 && P.dens_warps <= DENS_WARPS) ? P.dens_warps : DENS_WARPS;
     const size_t smem = (size_t)warps * NL_ROWS * 32 * sizeof(uint32_t);
     if ((search == 1 || search == 3) && (flags & (1 | 2 | 8 | 16))) {
@@ -1319,22 +1328,25 @@ __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
     if (p == 0) *time_slot(counters, step + 1u) = time + P.dt;  // AdvanceTime (fluid_system.cpp:2016)
     if (p >= counters[3]) return;
     const float4 pos = C.pos[p], ve = C.veval[p], f = force[p];
+    // the walls: the system's box, or a packed instance's own
+    const float* bmin = C.iid ? P.inst[C.iid[p]].bmin : P.bmin;
+    const float* bmax = C.iid ? P.inst[C.iid[p]].bmax : P.bmax;
     float ax = f.x, ay = f.y, az = f.z;
     float diff;
-    diff = P.pr - (pos.y - (P.bmin[1] + (pos.x - P.bmin[0]) * P.slope));
+    diff = P.pr - (pos.y - (bmin[1] + (pos.x - bmin[0]) * P.slope));
     wall(ax, ay, az, diff, -P.slope, P.one_minus_slope, 0.f, P.estiff, P.damp, ve);
-    diff = P.pr - (P.bmax[1] - pos.y);
+    diff = P.pr - (bmax[1] - pos.y);
     wall(ax, ay, az, diff, 0.f, -1.f, 0.f, P.estiff, P.damp, ve);
-    diff = P.pr - (pos.x - P.bmin[0]);
+    diff = P.pr - (pos.x - bmin[0]);
     wall(ax, ay, az, diff, 1.f, 0.f, 0.f, P.xmin_stiff, P.damp, ve);
-    diff = P.pr - (P.bmax[0] - pos.x);
+    diff = P.pr - (bmax[0] - pos.x);
     wall(ax, ay, az, diff, -1.f, 0.f, 0.f, P.xmax_stiff, P.damp, ve);
-    diff = P.pr - (pos.z - P.bmin[2]);
+    diff = P.pr - (pos.z - bmin[2]);
     wall(ax, ay, az, diff, 0.f, 0.f, 1.f, P.estiff, P.damp, ve);
-    diff = P.pr - (P.bmax[2] - pos.z);
+    diff = P.pr - (bmax[2] - pos.z);
     wall(ax, ay, az, diff, 0.f, 0.f, -1.f, P.estiff, P.damp, ve);
     {
-        const float dx = P.bmax[0] - pos.x, dy = P.bmax[1] - pos.y, dz = P.bmax[2] - pos.z;
+        const float dx = bmax[0] - pos.x, dy = bmax[1] - pos.y, dz = bmax[2] - pos.z;
         diff = 2.f * P.pr - (dx + dy + dz);
         wall(ax, ay, az, diff, 1.f, 1.f, 1.f, P.estiff, P.damp, ve);
     }

@@ -44,6 +44,23 @@ __device__ __forceinline__ uint32_t cell_of(const DevParams& P, float4 p) {
     return (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
 }
 
+// The same for a particle of a packed system: its instance's grid in its instance's frame,
+// placed in the instance's slab of the shared grid (rows ybase ..).
+__device__ __forceinline__ uint32_t cell_of(const DevParams& P, float4 p, const uint32_t* iid, uint32_t i) {
+    if (!iid) return cell_of(P, p);
+    const uint32_t k = iid[i];
+    if (k >= (uint32_t)P.n_inst) return UNDEF;
+    const InstParams& I = P.inst[k];
+    float gx = (p.x - I.gmin[0]) * I.gdelta[0];
+    float gy = (p.y - I.gmin[1]) * I.gdelta[1];
+    float gz = (p.z - I.gmin[2]) * I.gdelta[2];
+    if (!(gx >= 1.0f && gx < (float)(I.scanmax[0] + 1))) return UNDEF;
+    if (!(gy >= 1.0f && gy < (float)(I.scanmax[1] + 1))) return UNDEF;
+    if (!(gz >= 1.0f && gz < (float)(I.scanmax[2] + 1))) return UNDEF;
+    int cx = (int)gx, cy = (int)gy + I.ybase, cz = (int)gz;
+    return (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
+}
+
 // Morton code of the sub-cell holding a position inside its cell: 2^sub_bits sub-cells per axis
 // (sub_bits 1 or 2) from the fractional part of the cell coordinate.  Only the density pass's
 // processing order uses it, never a result.
@@ -53,9 +70,12 @@ __device__ __forceinline__ uint32_t cell_of(const DevParams& P, float4 p) {
 // compact as a Morton half-cell (MG_SUB_ORDER 0 keeps Morton codes with the y and z
 // coordinates mirrored in odd-x cells).  Without it, Morton codes (bit a = level-0 half of axis
 // a, bit 3 + a = level-1), which the per-lane fine-cell search reads as positions.
-__device__ __forceinline__ uint32_t sub_of(const DevParams& P, float4 p, bool warp_order) {
-    const float g[3] = {(p.x - P.gmin[0]) * P.gdelta[0], (p.y - P.gmin[1]) * P.gdelta[1],
-                        (p.z - P.gmin[2]) * P.gdelta[2]};
+__device__ __forceinline__ uint32_t sub_of(const DevParams& P, float4 p, bool warp_order,
+                                           const InstParams* I = nullptr) {
+    const float* gmin = I ? I->gmin : P.gmin;
+    const float* gdelta = I ? I->gdelta : P.gdelta;
+    const float g[3] = {(p.x - gmin[0]) * gdelta[0], (p.y - gmin[1]) * gdelta[1],
+                        (p.z - gmin[2]) * gdelta[2]};
     const int nsub = 1 << P.sub_bits;
     int q[3];
 #pragma unroll
@@ -81,17 +101,18 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
                                                 uint32_t* __restrict__ newidx,
                                                 uint32_t* __restrict__ count,
                                                 uint8_t* __restrict__ sub,
-                                                uint32_t* __restrict__ step, bool warp_order) {
+                                                uint32_t* __restrict__ step, bool warp_order,
+                                                const uint32_t* __restrict__ iid) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) *step += 1u;  // step counter read by the later kernels of this step
     bool in = i < P.cap;
     uint32_t c = UNDEF;
     if (in) {
         const float4 pi = pos[i];
-        c = cell_of(P, pi);
+        c = cell_of(P, pi, iid, i);
         cell[i] = c;
         newidx[i] = UNDEF;  // overwritten by the cell sort for particles inside the window
-        if (c != UNDEF) sub[i] = (uint8_t)sub_of(P, pi, warp_order);
+        if (c != UNDEF) sub[i] = (uint8_t)sub_of(P, pi, warp_order, iid ? P.inst + iid[i] : nullptr);
     }
     bool valid = in && c != UNDEF;
     unsigned active = __ballot_sync(0xffffffffu, valid);
@@ -110,7 +131,7 @@ void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, boo
                    cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
     k_insert<<<blocks, 256, 0, st>>>(P, cur.pos, s.cell, s.arank, s.newidx, s.count, s.sub,
-                                      s.counters + 5, warp_order);
+                                      s.counters + 5, warp_order, cur.iid);
 }
 
 // ---- single-pass scan (decoupled look-back) ------------------------------------------------
@@ -474,6 +495,7 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
                 D.genes[p] = __ldg(S.genes + i);
             }
             D.origin[p] = __ldg(S.origin + i);
+            if (S.iid) D.iid[p] = __ldg(S.iid + i);
             scell[p] = __ldg(cell + i);
         }
         if (parts & GATHER_MOTION) {
@@ -504,6 +526,7 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
             if (P.full_epi)
                 for (int g = 0; g < NG; g++) D.epi[(size_t)g * cap + p] = 0u;
             D.origin[p] = UNDEF;
+            if (D.iid) D.iid[p] = UNDEF;
             scell[p] = UNDEF;
             press[p] = 0.f;
             invdens[p] = 0.f;
