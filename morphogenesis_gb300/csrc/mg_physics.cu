@@ -483,7 +483,9 @@ __device__ __forceinline__ void dens_list_finish(
     dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press, invdens, X);
 }
 
-template <int FLAGS>
+// PACKED: packed instances (each particle's frame, genome and stiffness from its instance);
+// a separate instantiation so that a single system keeps its genome in the constant bank.
+template <int FLAGS, bool PACKED = false>
 __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_warp(
     DevParams P, MG_DENS_GENOME_PARAM, const float4* __restrict__ pos,
     const float* __restrict__ conc_in, float* __restrict__ conc_out,
@@ -561,7 +563,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
         const int ncell = ncx * ncz * (wy1 - wy0 + 1);
         // packed instances: the group's instance, whose frame places its cells (a group's cells
         // belong to one instance)
-        const uint32_t ginst = X.iid ? X.iid[__shfl_sync(0xffffffffu, p, leader)] : UNDEF;
+        const uint32_t ginst = PACKED ? X.iid[__shfl_sync(0xffffffffu, p, leader)] : UNDEF;
         for (int cb = 0; cb < ncell; cb += 32) {
             const int t = cb + (int)lane;
             uint32_t tcnt = 0, toff = 0, tpos = 0;  // tpos: the cell's offsets in the window
@@ -569,7 +571,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                 const int ox = t % ncx, oz = (t / ncx) % ncz, oy = t / (ncx * ncz);
                 tpos = (uint32_t)ox | ((uint32_t)oy << 8) | ((uint32_t)oz << 16);
                 const int cx = wx0 + ox, cz = wz0 + oz, cy = wy0 + oy;
-                if (!prune || cell_meets_box(ginst != UNDEF ? frame_of(P, ginst) : frame_of(P), cx, cy, cz,
+                if (!prune || cell_meets_box(PACKED ? frame_of(P, ginst) : frame_of(P), cx, cy, cz,
                                              tx0 - Rf, tx1 + Rf, ty0 - Rf, ty1 + Rf, tz0 - Rf, tz1 + Rf)) {
                     const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
                     tcnt = count[cell];
@@ -665,10 +667,12 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
         if (X.hlist) X.hcount[k] = UNDEF;
         return;
     }
-    // packed instances: the particle's own genome
-    const DevGenome* __restrict__ Gl = X.iid ? P.genomes + X.iid[p] : G;
-    dens_list_finish<FLAGS>(P, Gl, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,
-                            fcount, X, k);
+    if (PACKED)  // the particle's own genome
+        dens_list_finish<FLAGS>(P, P.genomes + X.iid[p], p, ip, n, my, pos, conc_in, conc_out, genes,
+                                press, invdens, flist, fcount, X, k);
+    else
+        dens_list_finish<FLAGS>(P, G, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,
+                                fcount, X, k);
 }
 
 // ---- per-lane fine-cell search ----------------------------------------------------------------
@@ -823,7 +827,7 @@ __device__ __forceinline__ void ovf_apply(const DevParams& P, uint32_t p, uint32
     __syncwarp();
 }
 
-template <int FLAGS>
+template <int FLAGS, bool PACKED = false>
 __global__ void __launch_bounds__(256, 1) k_dens_ovf(
     DevParams P, const DevGenome* __restrict__ G0, const float4* __restrict__ pos,
     const float* __restrict__ conc_in, float* __restrict__ conc_out,
@@ -852,8 +856,8 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
     for (uint32_t e = gw; e < nq; e += nw) {
         const uint32_t p = ovf[e];
         const float4 ip = pos[p];
-        const DevGenome* __restrict__ G = X.iid ? P.genomes + X.iid[p] : G0;
-        const CellFrame frame = X.iid ? frame_of(P, X.iid[p]) : frame_of(P);
+        const DevGenome* __restrict__ G = PACKED ? P.genomes + X.iid[p] : G0;
+        const CellFrame frame = PACKED ? frame_of(P, X.iid[p]) : frame_of(P);
         const float cur_t = (F::DIFF || F::GENE || F::MEAN) ? conc_in[(size_t)p * NTF + t] : 0.f;
         const float dif_t = F::DIFF ? G->diff[t] : 0.f;
         const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
@@ -971,6 +975,8 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
 // The per-lane lists take 48 KB of dynamic shared memory next to the static survivor buffers,
 // above the 48 KB a launch gets without opting in.
 #define MG_DENS_FLAG_SETS(M) M(1) M(2) M(3) M(5) M(6) M(7) M(9) M(23) M(46) M(47)
+// the flag sets of packed instances (physics and the plain morphogen stage)
+#define MG_DENS_PACKED_SETS(M) M(1) M(2) M(3) M(5) M(6) M(7)
 
 cudaError_t physics_init() {
     const int smem = DENS_WARPS * NL_ROWS * 32 * (int)sizeof(uint32_t);
@@ -982,6 +988,11 @@ cudaError_t physics_init() {
         e = cudaFuncSetAttribute(k_dens_fine<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     MG_DENS_FLAG_SETS(MG_ATTR)
 #undef MG_ATTR
+#define MG_ATTR_PACKED(F)                                                                       \
+    if (e == cudaSuccess)                                                                       \
+        e = cudaFuncSetAttribute(k_dens_warp<F, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    MG_DENS_PACKED_SETS(MG_ATTR_PACKED)
+#undef MG_ATTR_PACKED
     return e;
 }
 
@@ -996,23 +1007,31 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
     if ((search == 1 || search == 3) && (flags & (1 | 2 | 8 | 16))) {
         uint32_t blocks = (P.cap + warps * 32 - 1) / (warps * 32);
         const bool prune = search == 1;
-#define MG_DENSW_CASE(F)                                                                          \
+#define MG_DENSW_CASE_P(F, PK)                                                                    \
     case F:                                                                                       \
-        k_dens_warp<F><<<blocks, warps * 32, smem, st>>>(P, MG_DENS_GENOME_ARG, cur.pos, conc_in, conc_out, \
+        k_dens_warp<F, PK><<<blocks, warps * 32, smem, st>>>(P, MG_DENS_GENOME_ARG, cur.pos, conc_in, conc_out, \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.counters + 3,   \
                                                              s.work, s.ovf, s.counters + 6, X,    \
                                                              prune);                              \
-        k_dens_ovf<F><<<(uint32_t)num_sms * 4, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out,    \
+        k_dens_ovf<F, PK><<<(uint32_t)num_sms * 4, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out, \
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, s.press, s.invdens,        \
                                                              s.flist, s.fcount, s.ovf,            \
                                                              s.counters + 6, X, prune);           \
         return;
+#define MG_DENSW_CASE(F) MG_DENSW_CASE_P(F, false)
+#define MG_DENSW_CASE_PACKED(F) MG_DENSW_CASE_P(F, true)
         cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
-        switch (flags) { MG_DENS_FLAG_SETS(MG_DENSW_CASE) default: break; }
+        if (cur.iid) {
+            switch (flags) { MG_DENS_PACKED_SETS(MG_DENSW_CASE_PACKED) default: break; }
+        } else {
+            switch (flags) { MG_DENS_FLAG_SETS(MG_DENSW_CASE) default: break; }
+        }
 #undef MG_DENSW_CASE
+#undef MG_DENSW_CASE_PACKED
+#undef MG_DENSW_CASE_P
     }
     if (search == 2 && (flags & (1 | 2 | 8 | 16))) {
         uint32_t blocks = (P.cap + warps * 32 - 1) / (warps * 32);
