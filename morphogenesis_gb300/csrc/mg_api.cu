@@ -179,6 +179,11 @@ void derive(DevParams& D, const mg_fparams& p, uint32_t cap) {
     D.nadj = (1 * p.grid_res[2] + 1) * p.grid_res[0] + 1;
     D.gsrch = p.grid_srch;
     D.sr = p.psmoothradius;
+    {
+        int ex = 0;
+        const float m = std::frexp(p.psmoothradius, &ex);  // sr = m * 2^ex, m in [0.5, 1)
+        D.sr_inv_exact = (m == 0.5f && std::isfinite(p.psmoothradius)) ? 1.0f / p.psmoothradius : 0.0f;
+    }
     D.r2 = p.psmoothradius * p.psmoothradius;
     D.d2 = p.psimscale * p.psimscale;
     D.r2diff = D.r2 / D.d2;  // computeDiffusion: r2 = fparam.r2 / d2 (cuda:3032)

@@ -43,9 +43,11 @@ constexpr int DENS_WARPS = MG_DENS_WARPS;  // warps per block of the warp-cooper
 constexpr int NL_ROWS = NL_CAP + 1;
 
 // ---- per-neighbour terms ---------------------------------------------------------------
-__device__ __forceinline__ float wendland_term(float dsq, float sr) {
+// sr_inv_exact: 1 / sr when sr is a power of two, where the quotient r / sr is the product
+// r * (1 / sr) exactly (a scaling by a power of two, rounded once either way); else 0
+__device__ __forceinline__ float wendland_term(float dsq, float sr, float sr_inv_exact) {
     const float r = sqrtf(dsq);
-    const float qq = r / sr;
+    const float qq = sr_inv_exact != 0.f ? r * sr_inv_exact : r / sr;
     float b = 1.f - qq;
     b *= b;
     b *= b;
@@ -145,15 +147,19 @@ __device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], c
             const float a = dif[0] * cc;
 #if MG_F32X2
             // cj - cur as cj + (-1) * cur: one rounding of the exact difference, as the
-            // subtraction.  The product and the sum stay scalar: packed as __fmul2_rn feeding
-            // __fadd2_rn they gave other bits than the two roundings of the reference (measured
-            // against the oracle), i.e. they were merged into a fused multiply-add.
-            const float2 m1 = make_float2(-1.f, -1.f);
+            // subtraction; product and sum two species at a time.
+            const float2 m1 = make_float2(-1.f, -1.f), a2 = make_float2(a, a);
 #pragma unroll
             for (int t = 0; t < NTF; t += 2) {
                 const float2 d = __ffma2_rn(make_float2(cur[t], cur[t + 1]), m1, make_float2(cj[t], cj[t + 1]));
-                nc[t] += a * d.x;
-                nc[t + 1] += a * d.y;
+                // the product, then the sum, each rounded: the empty asm hands the compiler a
+                // product it cannot see through, so it cannot merge the two into a fused
+                // multiply-add (which it did with the packed forms alone)
+                float2 pr = __fmul2_rn(a2, d);
+                asm("" : "+f"(pr.x), "+f"(pr.y));
+                const float2 r = __fadd2_rn(make_float2(nc[t], nc[t + 1]), pr);
+                nc[t] = r.x;
+                nc[t + 1] = r.y;
             }
 #else
 #pragma unroll
@@ -219,7 +225,7 @@ __device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint
                 fmark = 0u;
                 nf++;
             }
-            if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
+            if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr, P.sr_inv_exact);
             if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
                 conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc, q, (P.r2diff - dsq) * P.d2,
                                              false, diffuse);
@@ -468,7 +474,7 @@ __device__ __forceinline__ void dens_list_finish(
                 fmark = 0u;
                 nf++;
             }
-            if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr);
+            if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr, P.sr_inv_exact);
             if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
                 conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2,
                                              G->uniform != 0, true);
@@ -816,7 +822,7 @@ __device__ __forceinline__ void ovf_apply(const DevParams& P, uint32_t p, uint32
             fmark = 0u;
             nf++;
         }
-        if (F::DENS && d < P.r2) part += wendland_term(d, P.sr);
+        if (F::DENS && d < P.r2) part += wendland_term(d, P.sr, P.sr_inv_exact);
         if ((F::DIFF || F::MEAN) && d < P.r2diff) {
             const float cj = reinterpret_cast<const float*>(scj[h])[t];
             if (F::MEAN) ms_t += cj;
