@@ -147,19 +147,15 @@ __device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], c
             const float a = dif[0] * cc;
 #if MG_F32X2
             // cj - cur as cj + (-1) * cur: one rounding of the exact difference, as the
-            // subtraction; product and sum two species at a time.
-            const float2 m1 = make_float2(-1.f, -1.f), a2 = make_float2(a, a);
+            // subtraction.  The product and the sum stay scalar: the packed __fmul2_rn and
+            // __fadd2_rn gave other bits than __fmul_rn / __fadd_rn on random operands (45% of
+            // pairs, measured), with or without a barrier between them.
+            const float2 m1 = make_float2(-1.f, -1.f);
 #pragma unroll
             for (int t = 0; t < NTF; t += 2) {
                 const float2 d = __ffma2_rn(make_float2(cur[t], cur[t + 1]), m1, make_float2(cj[t], cj[t + 1]));
-                // the product, then the sum, each rounded: the empty asm hands the compiler a
-                // product it cannot see through, so it cannot merge the two into a fused
-                // multiply-add (which it did with the packed forms alone)
-                float2 pr = __fmul2_rn(a2, d);
-                asm("" : "+f"(pr.x), "+f"(pr.y));
-                const float2 r = __fadd2_rn(make_float2(nc[t], nc[t + 1]), pr);
-                nc[t] = r.x;
-                nc[t + 1] = r.y;
+                nc[t] += a * d.x;
+                nc[t + 1] += a * d.y;
             }
 #else
 #pragma unroll
