@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--sur-steps", type=int, default=1000, help="in-loop surrogate evaluation steps")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-instances section")
     ap.add_argument("--no-large", action="store_true", help="skip the 16.8M-particle section")
+    ap.add_argument("--no-param-l", action="store_true",
+                    help="skip the plain step in the literal parameterisation (L)")
     ap.add_argument("--large-steps", type=int, default=200)
     ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--batch-instances", type=int, default=256)
@@ -205,6 +207,34 @@ def fp64_section(d, steps: int = 2):
     o64.close()
     return {"steps": steps, "against": "FP64 oracle, same inputs, particles matched by id",
             "fields": rep}
+
+
+def param_l_section(args, peak_gbs):
+    """The plain full step of the same 1,048,576-particle lattice in the literal
+    parameterisation (L: h = 0.01 sim units, sim scale 0.005, the reference's hard-coded
+    force radius and (sr - r)^3 kernel), timed like the headline (R) run."""
+    import morphogenesis_gb300 as mg
+    from morphogenesis_gb300 import _abi as A
+    from morphogenesis_gb300 import demo
+
+    d = demo.make_block(DIMS, "L", seed=0)
+    fs = mg.FluidSystem(d.params, d.genome, d.n)
+    fs.TransferToCL(d.arrays)
+    flags = A.STEP_DEFAULT
+    fs.Run(max(args.warmup, 3), flags)
+    tune = fs.autotune(10, flags)
+    fs.synchronize()
+    ms = fs.time_steps(args.steps, flags)
+    cells = int(d.params.grid_total)
+    bpp, bpc = fs.algorithmic_bytes(None, flags)
+    step_bytes = bpp * d.n + bpc * cells
+    per_step_s = ms / args.steps / 1e3
+    fs.close()
+    return {"workload": f"plain full step, {d.n:,} particles (128x64x128 lattice), parameterisation L",
+            "steps": args.steps, "ms_per_step": ms / args.steps,
+            "particle_steps_s": d.n / per_step_s,
+            "step_roofline_frac": step_bytes / per_step_s / 1e9 / peak_gbs,
+            "launch_shape": {k: v for k, v in tune.items() if k != "ms_per_step"}}
 
 
 def surrogate_section(args, peak_tflops):
@@ -513,6 +543,10 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         fp64 = fp64_section(d, 2)
 
+    param_l = None
+    if rank == 0 and not args.no_param_l:
+        param_l = param_l_section(args, peak)
+
     sur = None
     large = None
     if rank == 0 and not args.no_surrogate:
@@ -534,7 +568,7 @@ def main():
                        "parameterisation": PARAM, "particles_per_gpu": n, "cells": cells,
                        "l2": f"inputs larger than L2: step state {step_bytes / 1e9:.2f} GB/step",
                        "parallelism": f"replicas x{world}",
-                       "density_launch_shape": {k: tune[k] for k in ("dens_warps", "group_mode", "sub_bits", "search")}},
+                       "launch_shape": {k: v for k, v in tune.items() if k != "ms_per_step"}},
             "clocks": clk,
             "gpu_launches": int(launches),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
@@ -549,6 +583,7 @@ def main():
             "kernels_ms_per_launch": {k: v[1] / v[0] for k, v in prof.items()},
             "cpu_baseline": cpu,
             "fp64_error": fp64,
+            "parameterisation_L": param_l,
             "surrogate": sur,
             "batch": batch,
             "large": large,

@@ -333,9 +333,16 @@ mg_status mg_set_option(mg_handle h, int32_t option, int32_t value);
  * Results are identical for every choice. */
 mg_status mg_get_tuning(mg_handle h, int32_t choice[4]);
 mg_status mg_set_tuning(mg_handle h, const int32_t choice[4]);
-/* Times every launch shape over `steps` plain steps (flags: physics/genes only) on the
- * handle's current state, restoring the state after each trial, and keeps the fastest (the
- * default shape unless another is more than 3% faster).
+/* Threads per block of the force pass (k_force and k_force_in), the gather (the sort's
+ * permutation of the carried state) and integration: {force, gather, advance}, each 128, 256
+ * (the default) or 512.  Results are identical for every choice. */
+mg_status mg_get_block_sizes(mg_handle h, int32_t threads[3]);
+mg_status mg_set_block_sizes(mg_handle h, const int32_t threads[3]);
+/* Times every density-pass launch shape over `steps` plain steps (flags: physics/genes only)
+ * on the handle's current state, restoring the state after each trial, and keeps the fastest
+ * (the default shape unless another is more than 3% faster); then, with that shape, the block
+ * sizes of the force, gather and advance passes one at a time, by the same rule (read them
+ * with mg_get_block_sizes).  choice receives the density shape as mg_get_tuning gives it.
  * Needs a free device allocation the size of the handle's arena for the snapshot. */
 mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t choice[4],
                       float* ms_per_step);

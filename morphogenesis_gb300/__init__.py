@@ -272,13 +272,26 @@ class FluidSystem:
             self.conc_species_major = bool(value)
 
     def autotune(self, steps: int = 5, flags: int = A.STEP_DEFAULT) -> dict:
-        """Times the density pass's launch shapes on the current state (restored after each
-        trial) and keeps the fastest; returns the choice and its ms per step."""
+        """Times the density pass's launch shapes, then the force, gather and advance block
+        sizes, on the current state (restored after each trial) and keeps the fastest;
+        returns the choice and its ms per step."""
         ch = (C.c_int32 * 4)()
         ms = C.c_float()
         self._check(self.lib.mg_autotune(self.h, steps, flags, ch, C.byref(ms)))
+        f, g, a = self.block_sizes()
         return {"dens_warps": ch[0], "group_mode": ch[1], "sub_bits": ch[2], "search": ch[3],
+                "force_threads": f, "gather_threads": g, "advance_threads": a,
                 "ms_per_step": ms.value}
+
+    def block_sizes(self) -> tuple[int, int, int]:
+        """Threads per block of the (force, gather, advance) passes."""
+        t = (C.c_int32 * 3)()
+        self._check(self.lib.mg_get_block_sizes(self.h, t))
+        return tuple(t)
+
+    def set_block_sizes(self, force: int, gather: int, advance: int) -> None:
+        t = (C.c_int32 * 3)(force, gather, advance)
+        self._check(self.lib.mg_set_block_sizes(self.h, t))
 
     def device_bytes(self) -> tuple[int, int]:
         """(arena bytes, all device bytes the handle holds now)."""

@@ -209,6 +209,8 @@ SIGNATURES = [
     ("mg_device_bytes", C.c_int, [H, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     ("mg_get_tuning", C.c_int, [H, C.POINTER(C.c_int32)]),
     ("mg_set_tuning", C.c_int, [H, C.POINTER(C.c_int32)]),
+    ("mg_get_block_sizes", C.c_int, [H, C.POINTER(C.c_int32)]),
+    ("mg_set_block_sizes", C.c_int, [H, C.POINTER(C.c_int32)]),
     ("mg_autotune", C.c_int, [H, C.c_uint32, C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
     ("mg_batch_create", C.c_int, [C.POINTER(H), C.c_uint32, C.POINTER(H)]),
     ("mg_batch_destroy", C.c_int, [H]),

@@ -213,6 +213,7 @@ void derive(DevParams& D, const mg_fparams& p, uint32_t cap) {
     D.dens_warps = 8;
     D.group_mode = 0;
     D.sub_bits = 2;
+    D.force_threads = D.gather_threads = D.advance_threads = 256;
     D.cells = (uint32_t)p.grid_total;
 }
 
@@ -1261,6 +1262,9 @@ mg_status mg_update_params(mg_handle h, const mg_fparams* p) {
     h->P.dens_warps = old.dens_warps;
     h->P.group_mode = old.group_mode;
     h->P.sub_bits = old.sub_bits;
+    h->P.force_threads = old.force_threads;
+    h->P.gather_threads = old.gather_threads;
+    h->P.advance_threads = old.advance_threads;
     clear_graphs(h);
     // the device copy of the time (both parity slots)
     const uint32_t t2[2] = {*reinterpret_cast<const uint32_t*>(&p->time), *reinterpret_cast<const uint32_t*>(&p->time)};
@@ -2089,9 +2093,11 @@ mg_status mg_device_bytes(mg_handle h, size_t* arena, size_t* total) {
 }
 
 // ---- autotuner --------------------------------------------------------------------------------
-// Times the density pass's launch shapes on the handle's own state: each candidate runs
-// `steps` graph steps from a snapshot of the whole arena, which is restored afterwards, so
-// tuning leaves the simulation where it was.  Results do not depend on the choice.
+// Times launch shapes on the handle's own state: each candidate runs `steps` graph steps from a
+// snapshot of the whole arena, which is restored afterwards, so tuning leaves the simulation
+// where it was.  First the density pass's shape (warps per block, search groups, sub-cell
+// bits, search), then, one pass at a time with that shape, the block sizes of the force,
+// gather and advance passes.  Results do not depend on the choice.
 mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choice, float* ms_per_step) {
     if (!h || steps == 0) return fail(h, MG_ERR_INVALID_ARG, "mg_autotune: bad arguments");
     if (flags & (MG_STEP_SURROGATE | MG_STEP_REMODEL))
@@ -2116,15 +2122,32 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
     mg_status st = MG_OK;
     cudaError_t e = cudaMemcpyAsync(snap, h->arena, h->arena_bytes, cudaMemcpyDeviceToDevice, h->stream);
     if (e != cudaSuccess) st = cuda_fail(h, e, "mg_autotune snapshot");
+    cudaEvent_t a = nullptr, z = nullptr;
+    if (st == MG_OK && (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&z) != cudaSuccess))
+        st = fail(h, MG_ERR_CUDA, "mg_autotune: events");
+    // one trial of the shape in h->P / h->search: two warm steps capture the graphs of both
+    // buffer parities, then the timed run, each from the snapshot
+    auto trial = [&](float* t) -> mg_status {
+        clear_graphs(h);
+        cudaError_t e2;
+        if ((e2 = restore()) != cudaSuccess) return cuda_fail(h, e2, "mg_autotune restore");
+        mg_status s2 = run_steps(h, 2, flags);
+        if (s2 != MG_OK) return s2;
+        if ((e2 = restore()) != cudaSuccess) return cuda_fail(h, e2, "mg_autotune restore");
+        cudaEventRecord(a, h->stream);
+        if ((s2 = run_steps(h, steps, flags)) != MG_OK) return s2;
+        cudaEventRecord(z, h->stream);
+        cudaEventSynchronize(z);
+        *t = 0.f;
+        cudaEventElapsedTime(t, a, z);
+        return MG_OK;
+    };
     struct Cand { int warps, group, sub, search; };
     const bool fine_ok = h->P.gsrch == 3;
     const Cand cands[] = {{8, 0, 2, 1}, {8, 1, 2, 1}, {8, 0, 1, 1}, {8, 1, 1, 1}, {4, 0, 2, 1},
                           {4, 1, 2, 1}, {4, 0, 1, 1}, {4, 1, 1, 1}, {8, 0, 1, 2}, {4, 0, 1, 2}};
     float best = 0.f;
     Cand pick = cands[0];
-    cudaEvent_t a = nullptr, z = nullptr;
-    if (st == MG_OK && (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&z) != cudaSuccess))
-        st = fail(h, MG_ERR_CUDA, "mg_autotune: events");
     for (const Cand& c : cands) {
         if (st != MG_OK) break;
         if (c.search == 2 && (!fine_ok || h->n_inst)) continue;
@@ -2132,21 +2155,33 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
         h->P.dens_warps = c.warps;
         h->P.group_mode = c.group;
         h->P.sub_bits = c.sub;
-        clear_graphs(h);
-        // two warm steps capture the graphs of both buffer parities, then the timed run
-        if ((e = restore()) != cudaSuccess) { st = cuda_fail(h, e, "mg_autotune restore"); break; }
-        if ((st = run_steps(h, 2, flags)) != MG_OK) break;
-        if ((e = restore()) != cudaSuccess) { st = cuda_fail(h, e, "mg_autotune restore"); break; }
-        cudaEventRecord(a, h->stream);
-        if ((st = run_steps(h, steps, flags)) != MG_OK) break;
-        cudaEventRecord(z, h->stream);
-        cudaEventSynchronize(z);
         float t = 0.f;
-        cudaEventElapsedTime(&t, a, z);
+        if ((st = trial(&t)) != MG_OK) break;
         // the first candidate (the default shape) stays unless another beats the best by 3%:
         // on fresh states several shapes time within noise, and the default holds up best as
         // the tissue evolves
         if (&c == cands || t < best * 0.97f) { best = t; pick = c; }
+    }
+    // block sizes of the one-particle-per-thread passes, one pass at a time, the density
+    // shape fixed at its pick (its time with 256-thread blocks is the time to beat)
+    int threads[3] = {P0.force_threads, P0.gather_threads, P0.advance_threads};
+    if (st == MG_OK) {
+        h->search = pick.search;
+        h->P.dens_warps = pick.warps;
+        h->P.group_mode = pick.group;
+        h->P.sub_bits = pick.sub;
+        int* slot[3] = {&h->P.force_threads, &h->P.gather_threads, &h->P.advance_threads};
+        for (int k = 0; k < 3 && st == MG_OK; k++) {
+            const int keep = *slot[k];
+            for (int nt : {128, 256, 512}) {
+                if (nt == keep) continue;
+                *slot[k] = nt;
+                float t = 0.f;
+                if ((st = trial(&t)) != MG_OK) break;
+                if (t < best * 0.97f) { best = t; threads[k] = nt; }
+            }
+            *slot[k] = threads[k];
+        }
     }
     if (a) cudaEventDestroy(a);
     if (z) cudaEventDestroy(z);
@@ -2157,6 +2192,9 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
         h->P.group_mode = pick.group;
         h->P.sub_bits = pick.sub;
         h->search = pick.search;
+        h->P.force_threads = threads[0];
+        h->P.gather_threads = threads[1];
+        h->P.advance_threads = threads[2];
     }
     clear_graphs(h);
     e = restore();
@@ -2170,6 +2208,26 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
     if (choice) { choice[0] = pick.warps; choice[1] = pick.group; choice[2] = pick.sub; choice[3] = pick.search; }
     if (ms_per_step) *ms_per_step = best / (float)steps;
     return check_device(h);
+}
+
+mg_status mg_get_block_sizes(mg_handle h, int32_t* threads) {
+    if (!h || !threads) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    threads[0] = h->P.force_threads;
+    threads[1] = h->P.gather_threads;
+    threads[2] = h->P.advance_threads;
+    return MG_OK;
+}
+
+mg_status mg_set_block_sizes(mg_handle h, const int32_t* threads) {
+    if (!h || !threads) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    for (int k = 0; k < 3; k++)
+        if (threads[k] != 128 && threads[k] != 256 && threads[k] != 512)
+            return fail(h, MG_ERR_INVALID_ARG, "block sizes: 128, 256 or 512 threads");
+    h->P.force_threads = threads[0];
+    h->P.gather_threads = threads[1];
+    h->P.advance_threads = threads[2];
+    clear_graphs(h);
+    return MG_OK;
 }
 
 mg_status mg_get_tuning(mg_handle h, int32_t* choice) {

@@ -68,6 +68,9 @@ struct InstParams {
     float bmin[3], bmax[3];
 };
 
+// Largest block of the one-particle-per-thread passes the launch shape may pick.
+constexpr int MG_PLAIN_MAX_THREADS = 512;
+
 struct DevParams {
     float gmin[3], gdelta[3];
     float gcell[3];  // 1 / gdelta: a grid cell's extent per axis
@@ -87,6 +90,9 @@ struct DevParams {
     // picks them by timing): warps per block, search groups (0: a cell and the next cell of
     // its row, 1: one cell), sub-cell bits per axis of the processing order (1 or 2)
     int dens_warps, group_mode, sub_bits;
+    // threads per block of the one-particle-per-thread passes (128, 256 or 512; mg_autotune
+    // picks them by timing): force (k_force and k_force_in), gather, advance
+    int force_threads, gather_threads, advance_threads;
     int full_epi;  // per-gene FEPIGEN words carried (countdowns, activation lists) instead of bits
     int heal_params;  // healed bonds: 0 rest length = distance (D5), 1 makeBond's genome defaults
     uint32_t cap;

@@ -13,9 +13,7 @@
 // word) lives in one fixed file-scope device array, so the input is limited to
 // MG_NOALLOC_SCAN_MAX elements (16384 tiles, 128 KiB of scratch per device).  All calls on one
 // device share that array: calls whose scans may overlap in time race on it.
-#include <atomic>
 #include <cstdio>
-#include <mutex>
 
 #include "../../include/mg_abi.h"
 #include "mg_internal.cuh"
@@ -32,39 +30,18 @@ static_assert((uint64_t)NOALLOC_TILES * SCAN_TILE == MG_NOALLOC_SCAN_MAX,
 // high 32 bits the error word used when the caller passes none.
 static __device__ __align__(256) unsigned long long g_scan_scratch[NOALLOC_TILES + 1];
 
-constexpr int MAX_DEVICES = 64;
-std::atomic<unsigned long long*> g_scratch_ptr[MAX_DEVICES];
-std::mutex g_setup_lock;
-
-// The scratch address on the current device, looked up on the first call made with that
-// device current.
+// The scratch address in the current device's context.  It is looked up on every call (a host
+// lookup, no device work): a cached address would outlive a cudaDeviceReset, after which the
+// module and its scratch are loaded again at another address.
 mg_status scratch_of_current_device(unsigned long long** out) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
+    unsigned long long* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&p, g_scan_scratch);
+    if (e != cudaSuccess || !p) {
         char msg[160];
-        std::snprintf(msg, sizeof msg, "mg_prefix_sum_noalloc: cudaGetDevice: %s",
+        std::snprintf(msg, sizeof msg,
+                      "mg_prefix_sum_noalloc: cudaGetSymbolAddress of the scratch: %s",
                       cudaGetErrorString(e));
         return record_thread_error(MG_ERR_CUDA, msg);
-    }
-    if (dev < 0 || dev >= MAX_DEVICES)
-        return record_thread_error(MG_ERR_UNSUPPORTED,
-                                   "mg_prefix_sum_noalloc: device ordinal above 63");
-    unsigned long long* p = g_scratch_ptr[dev].load(std::memory_order_acquire);
-    if (!p) {
-        std::lock_guard<std::mutex> lock(g_setup_lock);
-        p = g_scratch_ptr[dev].load(std::memory_order_acquire);
-        if (!p) {
-            e = cudaGetSymbolAddress((void**)&p, g_scan_scratch);
-            if (e != cudaSuccess || !p) {
-                char msg[160];
-                std::snprintf(msg, sizeof msg,
-                              "mg_prefix_sum_noalloc: cudaGetSymbolAddress of the scratch on "
-                              "device %d: %s", dev, cudaGetErrorString(e));
-                return record_thread_error(MG_ERR_CUDA, msg);
-            }
-            g_scratch_ptr[dev].store(p, std::memory_order_release);
-        }
     }
     *out = p;
     return MG_OK;

@@ -1128,7 +1128,7 @@ __device__ __forceinline__ void fluid_term(const DevParams& P, float4 ip, float4
     cz = cz + (pz + vz);
 }
 
-__global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
+__global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force(DevParams P, Carried C,
                                                const uint32_t* __restrict__ scell,
                                                const uint32_t* __restrict__ count,
                                                const uint32_t* __restrict__ offset,
@@ -1240,7 +1240,7 @@ __global__ void __launch_bounds__(256) k_force(DevParams P, Carried C,
 // atomicAdd at cuda:3311-3313), added to the first kernel's sum.  An owner's stored term is the
 // one its own-bond loop evaluated for this particle as partner: the same arguments, the same
 // bits as evaluating it here.
-__global__ void __launch_bounds__(256) k_force_in(uint32_t cap, const uint32_t* __restrict__ pidx,
+__global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force_in(uint32_t cap, const uint32_t* __restrict__ pidx,
                                                   const float4* __restrict__ bterm,
                                                   float4* __restrict__ force,
                                                   const uint32_t* __restrict__ nactive_p) {
@@ -1275,10 +1275,10 @@ __global__ void __launch_bounds__(256) k_force_in(uint32_t cap, const uint32_t* 
 
 void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool use_list,
                   cudaStream_t st) {
-    uint32_t blocks = (P.cap + 255) / 256;
-    k_force<<<blocks, 256, 0, st>>>(P, cur, s.scell, s.count, s.offset, s.press, s.invdens, s.flist,
+    const uint32_t nt = (uint32_t)P.force_threads, blocks = (P.cap + nt - 1) / nt;
+    k_force<<<blocks, nt, 0, st>>>(P, cur, s.scell, s.count, s.offset, s.press, s.invdens, s.flist,
                                     s.fcount, use_list ? 1 : 0, s.force, s.bterm, s.brk, s.counters + 3);
-    k_force_in<<<blocks, 256, 0, st>>>(P.cap, cur.pidx, s.bterm, s.force, s.counters + 3);
+    k_force_in<<<blocks, nt, 0, st>>>(P.cap, cur.pidx, s.bterm, s.force, s.counters + 3);
 }
 
 // Broken bonds get rest length 0 (cuda:3315-3317).  The force kernel records the breaks in
@@ -1339,7 +1339,7 @@ __device__ __forceinline__ float* time_slot(uint32_t* counters, uint32_t step) {
 }
 
 template <bool APPLY_BRK, bool SPECIAL>
-__global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
+__global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_advance(DevParams P, Carried C,
                                                  const float4* __restrict__ force,
                                                  const uint32_t* __restrict__ brk,
                                                  uint32_t* __restrict__ counters) {
@@ -1406,15 +1406,15 @@ __global__ void __launch_bounds__(256) k_advance(DevParams P, Carried C,
 
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_brk,
                     cudaStream_t st, bool special) {
-    uint32_t blocks = (P.cap + 255) / 256;
+    const uint32_t nt = (uint32_t)P.advance_threads, blocks = (P.cap + nt - 1) / nt;
     if (apply_brk && special)
-        k_advance<true, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+        k_advance<true, true><<<blocks, nt, 0, st>>>(P, cur, s.force, s.brk, s.counters);
     else if (apply_brk)
-        k_advance<true, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+        k_advance<true, false><<<blocks, nt, 0, st>>>(P, cur, s.force, s.brk, s.counters);
     else if (special)
-        k_advance<false, true><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+        k_advance<false, true><<<blocks, nt, 0, st>>>(P, cur, s.force, s.brk, s.counters);
     else
-        k_advance<false, false><<<blocks, 256, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+        k_advance<false, false><<<blocks, nt, 0, st>>>(P, cur, s.force, s.brk, s.counters);
 }
 
 }  // namespace mg

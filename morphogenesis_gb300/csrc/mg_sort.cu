@@ -450,7 +450,7 @@ __device__ __forceinline__ uint32_t remap(uint32_t j, uint32_t cap, const uint32
     return j < cap ? __ldg(newidx + j) : NO_PARTNER;
 }
 
-__global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
+__global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Carried S,
                                                 const float* __restrict__ sconc, Carried D,
                                                 float* __restrict__ dconc,
                                                 const uint32_t* __restrict__ sorted,
@@ -550,8 +550,8 @@ __global__ void __launch_bounds__(256) k_gather(DevParams P, Carried S,
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st,
                    int parts) {
-    uint32_t blocks = (P.cap + 255) / 256;
-    k_gather<<<blocks, 256, 0, st>>>(P, src, src_conc, dst, dst_conc, s.sorted, s.newidx, s.cell,
+    const uint32_t nt = (uint32_t)P.gather_threads, blocks = (P.cap + nt - 1) / nt;
+    k_gather<<<blocks, nt, 0, st>>>(P, src, src_conc, dst, dst_conc, s.sorted, s.newidx, s.cell,
                                       s.scell, s.press, s.invdens, s.force, s.counters + 3, parts);
 }
 

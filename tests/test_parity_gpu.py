@@ -470,6 +470,18 @@ def test_launch_shapes_give_identical_results(built):
         for b, w in want.items():
             assert np.array_equal(fs.download(b).view(np.uint32), w), f"shape {shape} buffer {b}"
         fs.close()
+    # block sizes of the force, gather and advance passes
+    for threads in ((128, 512, 128), (512, 128, 512)):
+        fs = mg.FluidSystem(d.params, d.genome, d.n)
+        fs.TransferToCL(d.arrays)
+        fs.set_block_sizes(*threads)
+        assert fs.block_sizes() == threads
+        fs.Run(30)
+        for b, w in want.items():
+            assert np.array_equal(fs.download(b).view(np.uint32), w), f"block sizes {threads} buffer {b}"
+        with pytest.raises(A.MgError):
+            fs.set_block_sizes(64, 256, 256)
+        fs.close()
     # the autotuner restores the state it tunes on
     fs = mg.FluidSystem(d.params, d.genome, d.n)
     fs.TransferToCL(d.arrays)
@@ -477,6 +489,7 @@ def test_launch_shapes_give_identical_results(built):
     before = fs.download(A.FPOS).copy()
     res = fs.autotune(3)
     assert fs.tuning() == (res["dens_warps"], res["group_mode"], res["sub_bits"], res["search"])
+    assert fs.block_sizes() == (res["force_threads"], res["gather_threads"], res["advance_threads"])
     assert np.array_equal(fs.download(A.FPOS), before)
     fs.Run(20)
     for b, w in want.items():
