@@ -488,7 +488,9 @@ mg_status mg_batch_time_steps(mg_batch b, uint32_t nsteps, uint32_t flags, float
  * and reports whether the wait gave up as designed.  which = 0: the prefix sum's look-back
  * (a scan whose first tile is never launched); which = 1: the surrogate inference's
  * tensor-core completion wait (an inference CTA whose MMAs are withheld; the CTA then frees
- * its tensor memory).  spin_limit: polls before giving up (1 .. 1048576).  Returns
+ * its tensor memory); which = 2: the training GEMM's completion wait (a GEMM CTA whose MMAs are
+ * withheld; mg_mlp_train and mg_mlp_gradients return MG_ERR_DEVICE_TIMEOUT when such a wait
+ * runs out).  spin_limit: polls before giving up (1 .. 1048576).  Returns
  * MG_ERR_DEVICE_TIMEOUT when the wait gave up (the expected result, the same status a step
  * returns when one of these waits runs out), MG_OK if it did not, MG_ERR_CUDA on a CUDA error.
  * The CUDA context stays usable either way.  Uses the current device and synchronises. */

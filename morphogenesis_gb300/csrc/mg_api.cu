@@ -1850,7 +1850,14 @@ mg_status mg_algorithmic_bytes(mg_handle h, const char* kernel, uint32_t flags,
 }
 
 // ---- learned morphogen surrogate ------------------------------------------------------------
-static mg_status mlp_fail(cudaError_t e, const char* where) { return cuda_fail(nullptr, e, where); }
+static mg_status mlp_fail(cudaError_t e, const char* where) {
+    if (e == cudaErrorTimeout) {
+        char msg[200];
+        std::snprintf(msg, sizeof msg, "%s: a tensor-core completion wait gave up (bounded spin)", where);
+        return fail(nullptr, MG_ERR_DEVICE_TIMEOUT, msg);
+    }
+    return cuda_fail(nullptr, e, where);
+}
 
 mg_status mg_mlp_create(uint64_t seed, mg_mlp* out) {
     if (!out) return fail(nullptr, MG_ERR_INVALID_ARG, "out is NULL");
@@ -2262,20 +2269,22 @@ mg_status mg_set_tuning(mg_handle h, const int32_t* choice) {
 
 // ---- failure-detection self-test ---------------------------------------------------------------
 mg_status mg_selftest_bounded_wait(int32_t which, uint32_t spin_limit) {
-    if ((which != 0 && which != 1) || spin_limit == 0 || spin_limit > (1u << 20))
-        return fail(nullptr, MG_ERR_INVALID_ARG, "mg_selftest_bounded_wait: which must be 0 or 1, spin_limit 1 .. 1048576");
+    if (which < 0 || which > 2 || spin_limit == 0 || spin_limit > (1u << 20))
+        return fail(nullptr, MG_ERR_INVALID_ARG, "mg_selftest_bounded_wait: which must be 0, 1 or 2, spin_limit 1 .. 1048576");
     cudaStream_t st = nullptr;
     MG_CUDA(nullptr, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     uint32_t bits = 0;
     cudaError_t e = which == 0 ? mg::scan_selftest_wait_timeout(spin_limit, &bits, st)
-                               : mg::mlp_selftest_wait_timeout(spin_limit, &bits, st);
+                  : which == 1 ? mg::mlp_selftest_wait_timeout(spin_limit, &bits, st)
+                               : mg::mlp_selftest_gemm_wait_timeout(spin_limit, &bits, st);
     cudaStreamDestroy(st);
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "mg_selftest_bounded_wait");
     const uint32_t expect = which == 0 ? (uint32_t)ERR_SCAN_TIMEOUT : (uint32_t)mg::MLP_ERR_MBAR_TIMEOUT;
-    if (bits & expect)
-        return fail(nullptr, MG_ERR_DEVICE_TIMEOUT,
-                    which == 0 ? "self-test: prefix-sum look-back gave up waiting (bounded spin)"
-                               : "self-test: tensor-core completion wait gave up (bounded spin)");
+    static const char* const what[3] = {
+        "self-test: prefix-sum look-back gave up waiting (bounded spin)",
+        "self-test: tensor-core completion wait gave up (bounded spin)",
+        "self-test: training-GEMM completion wait gave up (bounded spin)"};
+    if (bits & expect) return fail(nullptr, MG_ERR_DEVICE_TIMEOUT, what[which]);
     return MG_OK;
 }
 

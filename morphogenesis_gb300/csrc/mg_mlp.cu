@@ -1,7 +1,8 @@
 // mg_mlp.cu - training and inference kernels of the learned reaction surrogate (row a12).
 //
-// Training: BF16 tensor-core GEMMs (mma.sync.m16n8k16, FP32 accumulate) for the forward and
-// backward products, elementwise bias/GELU/loss kernels and Adam on FP32 master weights.
+// Training: BF16 GEMMs on 5th-generation tensor cores (tcgen05.mma, FP32 accumulators in
+// tensor memory, split-K for the weight gradients) for the forward and backward products,
+// elementwise bias/GELU/loss kernels and Adam on FP32 master weights.
 // Inference (inside the simulation step): one persistent kernel per SM that runs the three
 // layers on 5th-generation tensor cores -- tcgen05.mma with operands in shared memory
 // (K-major core-matrix layout, no swizzle) and FP32 accumulators in tensor memory, read back
@@ -20,100 +21,6 @@
 namespace mg {
 
 using bf16 = __nv_bfloat16;
-
-// =============================================================================================
-// Training GEMM: C (+)= A * B with mma.sync.m16n8k16 (bf16 in, fp32 accumulate)
-// =============================================================================================
-constexpr int GBM = 64, GBN = 64, GBK = 32, GPAD = 8;
-
-__device__ __forceinline__ uint32_t ld_pair(const bf16* p) {
-    return *reinterpret_cast<const uint32_t*>(p);
-}
-
-__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], const uint32_t (&a)[4],
-                                               const uint32_t (&b)[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-        "{%8,%9}, {%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf16* __restrict__ A,
-                                                   long sam, long sak, const bf16* __restrict__ B,
-                                                   long sbk, long sbn, float* __restrict__ C,
-                                                   long ldc, int split) {
-    __shared__ __align__(16) bf16 As[GBM][GBK + GPAD];
-    __shared__ __align__(16) bf16 Bs[GBN][GBK + GPAD];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-    const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
-    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-    const int per = ((K + split - 1) / split + GBK - 1) / GBK * GBK;
-    const int kb = blockIdx.z * per, ke = min(K, kb + per);
-    float acc[2][4][4];
-#pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-#pragma unroll
-            for (int r = 0; r < 4; r++) acc[i][j][r] = 0.f;
-    const bf16 zero = __float2bfloat16(0.f);
-    for (int k0 = kb; k0 < ke; k0 += GBK) {
-        for (int e = tid; e < GBM * GBK; e += 128) {
-            const int mm = e / GBK, kk = e % GBK, gm = m0 + mm, gk = k0 + kk;
-            As[mm][kk] = (gm < M && gk < ke) ? A[(long)gm * sam + (long)gk * sak] : zero;
-        }
-        for (int e = tid; e < GBN * GBK; e += 128) {
-            const int nn = e / GBK, kk = e % GBK, gn = n0 + nn, gk = k0 + kk;
-            Bs[nn][kk] = (gn < N && gk < ke) ? B[(long)gk * sbk + (long)gn * sbn] : zero;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < GBK; kk += 16) {
-            uint32_t a[2][4], b[4][2];
-#pragma unroll
-            for (int mt = 0; mt < 2; mt++) {
-                const int r = wm + mt * 16 + g;
-                a[mt][0] = ld_pair(&As[r][kk + 2 * t]);
-                a[mt][1] = ld_pair(&As[r + 8][kk + 2 * t]);
-                a[mt][2] = ld_pair(&As[r][kk + 2 * t + 8]);
-                a[mt][3] = ld_pair(&As[r + 8][kk + 2 * t + 8]);
-            }
-#pragma unroll
-            for (int nt = 0; nt < 4; nt++) {
-                const int c = wn + nt * 8 + g;
-                b[nt][0] = ld_pair(&Bs[c][kk + 2 * t]);
-                b[nt][1] = ld_pair(&Bs[c][kk + 2 * t + 8]);
-            }
-#pragma unroll
-            for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-                for (int nt = 0; nt < 4; nt++) mma_bf16_16816(acc[mt][nt], a[mt], b[nt]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-        for (int nt = 0; nt < 4; nt++) {
-            const int r = m0 + wm + mt * 16 + g, c = n0 + wn + nt * 8 + 2 * t;
-            const float v[4] = {acc[mt][nt][0], acc[mt][nt][1], acc[mt][nt][2], acc[mt][nt][3]};
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int rr = r + (q >= 2 ? 8 : 0), cc = c + (q & 1);
-                if (rr < M && cc < N) {
-                    if (split > 1) atomicAdd(&C[(long)rr * ldc + cc], v[q]);
-                    else C[(long)rr * ldc + cc] = v[q];
-                }
-            }
-        }
-}
-
-void launch_gemm_bf16(int M, int N, int K, const bf16* A, long sam, long sak, const bf16* B,
-                      long sbk, long sbn, float* C, long ldc, int split, cudaStream_t st) {
-    dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM, split);
-    k_gemm_bf16<<<grid, 128, 0, st>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, split);
-}
 
 // =============================================================================================
 // Training elementwise kernels
@@ -430,6 +337,236 @@ __device__ __forceinline__ bool group_and(uint32_t g, bool v) {
     return out != 0;
 }
 
+// =============================================================================================
+// Training GEMM on tcgen05: C (+)= sum_k A(m, k) B(n, k), BF16 operands, FP32 accumulators
+// =============================================================================================
+// A(m, k) = A.p[m * A.s_row + k * A.s_k], B(n, k) = B.p[n * B.s_row + k * B.s_k], C(m, n) at
+// C[m * scm + n * scn].  One CTA of 128 threads computes a 128 x nt tile (nt = the tile's
+// columns rounded up to 16, at most 128) over one K range of a split-K grid (atomicAdd into C
+// when split > 1).  The threads stage 64-wide K chunks of both operands into shared memory in
+// the K-major core-matrix layout (transposing 8 x 8 blocks in registers when the operand is
+// contiguous along its rows rather than along K), double-buffered: one elected thread issues
+// the chunk's four tcgen05.mma (M 128, K 16 each) and commits them to the buffer's mbarrier
+// while the others stage the next chunk.  The accumulator lives in 128 TMEM columns; warp w
+// reads lanes 32w..32w+31 (rows) back with tcgen05.ld.  Every mbarrier wait is bounded: on
+// timeout the CTA records MLP_ERR_MBAR_TIMEOUT, waits (bounded) for its MMAs in flight, frees
+// its tensor memory and returns.
+constexpr int TG_BM = 128, TG_BN = 128, TG_BK = 64, TG_THREADS = 128;
+constexpr uint32_t TG_TMEM_COLS = 128;
+
+struct GemmOperand {
+    const bf16* p;
+    long s_row, s_k;
+    int mode;  // 1: K contiguous (16-byte loads), 0: rows contiguous (8 x 8 transposes), -1: scalar
+};
+
+struct GemmSmem {
+    bf16 a[2][TG_BM * TG_BK];  // 16 KB per buffer
+    bf16 b[2][TG_BN * TG_BK];  // 16 KB per buffer
+    unsigned long long mbar[2];
+    uint32_t tmem_base;
+};
+
+__device__ __forceinline__ bf16 gemm_elem(const GemmOperand& o, int r, int k, int rows, int kend) {
+    return (r < rows && k < kend) ? o.p[(long)r * o.s_row + (long)k * o.s_k] : __float2bfloat16(0.f);
+}
+
+// Rows [row0, row0 + nrows) x K [k0, k0 + TG_BK) of an operand into a core-matrix tile; zeros
+// at rows >= rows_lim and at k >= kend.
+__device__ __forceinline__ void gemm_stage(bf16* tile, const GemmOperand& o, int row0, int rows_lim,
+                                           int nrows, int k0, int kend, int tid) {
+    if (o.mode == 1) {
+        for (int idx = tid; idx < nrows * (TG_BK / 8); idx += TG_THREADS) {
+            const int r = idx >> 3, kq = (idx & 7) * 8, gr = row0 + r, gk = k0 + kq;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (gr < rows_lim) {
+                if (gk + 8 <= kend) {
+                    v = *reinterpret_cast<const uint4*>(o.p + (long)gr * o.s_row + gk);
+                } else {
+                    bf16 e[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) e[j] = gemm_elem(o, gr, gk + j, rows_lim, kend);
+                    v = *reinterpret_cast<uint4*>(e);
+                }
+            }
+            *reinterpret_cast<uint4*>(tile + core_offset(r, kq, TG_BK)) = v;
+        }
+    } else if (o.mode == 0) {
+        // one 8 x 8 block (one core matrix) per thread and pass: eight 16-byte loads along the
+        // rows, one per k, transposed into eight 16-byte rows along k
+        for (int idx = tid; idx < (nrows / 8) * (TG_BK / 8); idx += TG_THREADS) {
+            const int r0 = (idx >> 3) * 8, kq = (idx & 7) * 8, gr0 = row0 + r0;
+            uint32_t w[8][4];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int gk = k0 + kq + j;
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (gk < kend) {
+                    if (gr0 + 8 <= rows_lim) {
+                        v = *reinterpret_cast<const uint4*>(o.p + (long)gk * o.s_k + gr0);
+                    } else {
+                        bf16 e[8];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) e[i] = gemm_elem(o, gr0 + i, gk, rows_lim, kend);
+                        v = *reinterpret_cast<uint4*>(e);
+                    }
+                }
+                w[j][0] = v.x; w[j][1] = v.y; w[j][2] = v.z; w[j][3] = v.w;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                // row i: element i of each k, two k per 32-bit word (the lower k in the low half)
+                const uint32_t sel = (i & 1) ? 0x7632u : 0x5410u;
+                uint4 out;
+                out.x = __byte_perm(w[0][i >> 1], w[1][i >> 1], sel);
+                out.y = __byte_perm(w[2][i >> 1], w[3][i >> 1], sel);
+                out.z = __byte_perm(w[4][i >> 1], w[5][i >> 1], sel);
+                out.w = __byte_perm(w[6][i >> 1], w[7][i >> 1], sel);
+                *reinterpret_cast<uint4*>(tile + core_offset(r0 + i, kq, TG_BK)) = out;
+            }
+        }
+    } else {
+        for (int idx = tid; idx < nrows * TG_BK; idx += TG_THREADS) {
+            const int r = idx / TG_BK, k = idx % TG_BK;
+            tile[core_offset(r, k, TG_BK)] = gemm_elem(o, row0 + r, k0 + k, rows_lim, kend);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(TG_THREADS) k_gemm_tc(int M, int N, int K, GemmOperand A, GemmOperand B,
+                                                        float* __restrict__ C, long scm, long scn, int split,
+                                                        uint32_t* __restrict__ err, uint32_t spin_limit,
+                                                        uint32_t withhold) {
+    // withhold != 0 (failure-detection self-test only) issues no MMA, so a wait runs out
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    GemmSmem& S = *reinterpret_cast<GemmSmem*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * TG_BM, n0 = blockIdx.x * TG_BN;
+    const int ncols = min(TG_BN, N - n0);
+    const uint32_t nt = (uint32_t)((ncols + 15) & ~15);
+    const int per = ((K + split - 1) / split + TG_BK - 1) / TG_BK * TG_BK;
+    const int kb = blockIdx.z * per, ke = min(K, kb + per);
+    const int nchunks = ke > kb ? (ke - kb + TG_BK - 1) / TG_BK : 0;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&S.mbar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&S.mbar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         smem_u32(&S.tmem_base)),
+                     "r"(TG_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+    bool ok = true;
+    int issued = 0;  // chunks committed (thread 0)
+    for (int c = 0; c < nchunks; c++) {
+        const int buf = c & 1;
+        if (c >= 2) {  // the MMAs of chunk c - 2 have finished reading this buffer
+            ok = __syncthreads_and(mbar_wait(smem_u32(&S.mbar[buf]), ((c - 2) >> 1) & 1, spin_limit));
+            if (!ok) break;
+            tc_fence_after();
+        }
+        const int k0 = kb + c * TG_BK;
+        gemm_stage(S.a[buf], A, m0, M, TG_BM, k0, ke, tid);
+        gemm_stage(S.b[buf], B, n0, N, (int)nt, k0, ke, tid);
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0 && !withhold) {
+            const uint32_t sa = smem_u32(S.a[buf]), sb = smem_u32(S.b[buf]);
+            const uint32_t sbo = (TG_BK >> 3) * 128u;  // next group of 8 rows
+            const uint32_t idesc = idesc_bf16(TG_BM, nt);
+#pragma unroll
+            for (uint32_t s = 0; s < TG_BK / 16; s++)
+                mma_f16_ss(tmem, smem_desc(sa + s * 256u, 128u, sbo), smem_desc(sb + s * 256u, 128u, sbo),
+                           idesc, (c > 0 || s > 0) ? 1u : 0u);
+            mma_commit(smem_u32(&S.mbar[buf]));
+            issued = c + 1;
+        }
+    }
+    if (ok && nchunks > 0) {
+        // the last two chunks (the earlier ones were waited for in the loop)
+        const int l = nchunks - 1;
+        bool w = mbar_wait(smem_u32(&S.mbar[l & 1]), (l >> 1) & 1, spin_limit);
+        if (w && l > 0) w = mbar_wait(smem_u32(&S.mbar[(l - 1) & 1]), ((l - 1) >> 1) & 1, spin_limit);
+        ok = __syncthreads_and(w);
+        if (ok) {
+            tc_fence_after();
+            const int gm = m0 + warp * 32 + lane;
+            const uint32_t taddr = tmem + (((uint32_t)warp * 32u) << 16);
+            const bool vec = split == 1 && scn == 1 && (scm & 3) == 0 &&
+                             ((reinterpret_cast<uintptr_t>(C) & 15u) == 0) && ((n0 & 3) == 0);
+            for (uint32_t c0 = 0; c0 < nt; c0 += 16) {
+                float v[16];
+                tmem_ld16(taddr + c0, v);
+                if (gm < M) {
+                    const int nb = n0 + (int)c0;
+                    float* row = C + (long)gm * scm;
+                    if (vec && (int)c0 + 16 <= ncols) {
+                        float4* o = reinterpret_cast<float4*>(row + nb);
+#pragma unroll
+                        for (int q = 0; q < 4; q++) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; j++) {
+                            if ((int)c0 + j < ncols) {
+                                float* d = row + (long)(nb + j) * scn;
+                                if (split > 1) atomicAdd(d, v[j]);
+                                else *d = v[j];
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (!ok && tid == 0) {
+        atomicOr(err, MLP_ERR_MBAR_TIMEOUT);
+        if (issued > 0)  // one more bounded wait for the MMAs in flight before the TMEM is freed
+            mbar_wait(smem_u32(&S.mbar[(issued - 1) & 1]), ((issued - 1) >> 1) & 1, spin_limit);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(S.tmem_base),
+                     "r"(TG_TMEM_COLS)
+                     : "memory");
+}
+
+GemmOperand gemm_operand(const bf16* p, long s_row, long s_k) {
+    const bool aligned = (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
+    int mode = -1;
+    if (aligned && s_k == 1 && s_row % 8 == 0) mode = 1;
+    else if (aligned && s_row == 1 && s_k % 8 == 0) mode = 0;
+    return GemmOperand{p, s_row, s_k, mode};
+}
+
+// C(m, n) (+)= sum_k A(m, k) B(k, n) with A(m, k) = A[m*sam + k*sak], B(k, n) = B[k*sbk + n*sbn]
+// (bf16), C(m, n) at C[m*ldc + n] (fp32).  K split over gridDim.z with atomic accumulation
+// when split > 1 (C must then be zeroed first).  A product with fewer than 64 rows runs
+// transposed (C^T = B^T A^T) so that the 128-row MMA tile is filled by the longer side.
+void launch_gemm_bf16(int M, int N, int K, const bf16* A, long sam, long sak, const bf16* B,
+                      long sbk, long sbn, float* C, long ldc, int split, uint32_t* err, cudaStream_t st,
+                      uint32_t withhold = 0) {
+    GemmOperand a = gemm_operand(A, sam, sak), b = gemm_operand(B, sbn, sbk);
+    long scm = ldc, scn = 1;
+    if (M < 64 && N > M) {
+        std::swap(a, b);
+        std::swap(M, N);
+        std::swap(scm, scn);
+    }
+    dim3 grid((N + TG_BN - 1) / TG_BN, (M + TG_BM - 1) / TG_BM, split);
+    k_gemm_tc<<<grid, TG_THREADS, sizeof(GemmSmem), st>>>(M, N, K, a, b, C, scm, scn, split, err,
+                                                          MBAR_SPIN_LIMIT, withhold);
+}
+
 // Surrogate step: for each particle p < nactive, conc_out[p] = conc_in[p] + s_p * MLP(features[p])
 // (s_p the particle's input scale, 1 without feat_scale).  Particles under judgement (sampled
 // this step) or already handed to the plain method (bit 31 of their gene word) compare against /
@@ -675,6 +812,8 @@ inline uint32_t blocks(size_t n, int t = 256) { return (uint32_t)((n + t - 1) / 
 }  // namespace
 
 cudaError_t mlp_init_attributes() {
+    MLP_TRY(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(GemmSmem)));
     return cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)sizeof(InferSmem));
 }
@@ -688,6 +827,8 @@ cudaError_t mlp_alloc(Mlp* m, uint64_t seed, cudaStream_t st) {
     m->adam_v = m->adam_m + P_COUNT;
     MLP_TRY(cudaMalloc(&m->wb, sizeof(bf16) * P_COUNT));
     MLP_TRY(cudaMalloc(&m->norm, sizeof(float) * NORM_COUNT));
+    MLP_TRY(cudaMalloc(&m->err, sizeof(uint32_t)));
+    MLP_TRY(cudaMemsetAsync(m->err, 0, sizeof(uint32_t), st));
     const size_t inf_bytes = sizeof(bf16) * (MLP_H * MLP_IN + MLP_H * MLP_H + MLP_OUT * MLP_H) +
                              sizeof(float) * (2 * MLP_H + MLP_OUT);
     MLP_TRY(cudaMalloc(&m->inf_mem, inf_bytes));
@@ -725,6 +866,7 @@ void mlp_free(Mlp* m) {
     cudaFree(m->params);
     cudaFree(m->wb);
     cudaFree(m->norm);
+    cudaFree(m->err);
     cudaFree(m->inf_mem);
     cudaFree(m->ws);
     std::memset(m, 0, sizeof(*m));
@@ -817,6 +959,14 @@ cudaError_t mlp_fit_norm(Mlp* m, const float* dx, const float* dy, uint64_t rows
 
 namespace {
 
+// The training GEMMs' error bits: a completion wait that gave up reads as cudaErrorTimeout.
+cudaError_t check_err(Mlp* m) {
+    uint32_t bits = 0;
+    MLP_TRY(cudaMemcpyAsync(&bits, m->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, m->st));
+    MLP_TRY(cudaStreamSynchronize(m->st));
+    return bits ? cudaErrorTimeout : cudaSuccess;
+}
+
 struct Workspace {
     bf16 *X, *H1, *H2, *dY16, *dZ16;
     float *Y, *Z1, *Z2, *Z3, *dY32, *dH, *dZ32;
@@ -857,29 +1007,30 @@ void fwd_bwd(Mlp* m, const Workspace& w, uint32_t B) {
     const bf16* W1 = m->wb + P_W1;
     const bf16* W2 = m->wb + P_W2;
     const bf16* W3 = m->wb + P_W3;
-    const int split = (int)std::max<uint32_t>(1u, std::min<uint32_t>(64u, B / 1024u));
-    launch_gemm_bf16(B, MLP_H, MLP_IN, w.X, MLP_IN, 1, W1, 1, MLP_IN, w.Z1, MLP_H, 1, st);
+    // weight gradients reduce over the batch: split K into ranges of at least 512 rows
+    const int split = (int)std::max<uint32_t>(1u, std::min<uint32_t>(128u, B / 512u));
+    launch_gemm_bf16(B, MLP_H, MLP_IN, w.X, MLP_IN, 1, W1, 1, MLP_IN, w.Z1, MLP_H, 1, m->err, st);
     k_bias_act<<<blocks((size_t)B * MLP_H), 256, 0, st>>>(w.Z1, m->params + P_B1, MLP_H, (size_t)B * MLP_H, w.H1);
-    launch_gemm_bf16(B, MLP_H, MLP_H, w.H1, MLP_H, 1, W2, 1, MLP_H, w.Z2, MLP_H, 1, st);
+    launch_gemm_bf16(B, MLP_H, MLP_H, w.H1, MLP_H, 1, W2, 1, MLP_H, w.Z2, MLP_H, 1, m->err, st);
     k_bias_act<<<blocks((size_t)B * MLP_H), 256, 0, st>>>(w.Z2, m->params + P_B2, MLP_H, (size_t)B * MLP_H, w.H2);
-    launch_gemm_bf16(B, MLP_OUT, MLP_H, w.H2, MLP_H, 1, W3, 1, MLP_H, w.Z3, MLP_OUT, 1, st);
+    launch_gemm_bf16(B, MLP_OUT, MLP_H, w.H2, MLP_H, 1, W3, 1, MLP_H, w.Z3, MLP_OUT, 1, m->err, st);
     k_bias_act<<<blocks((size_t)B * MLP_OUT), 256, 0, st>>>(w.Z3, m->params + P_B3, MLP_OUT, (size_t)B * MLP_OUT, nullptr);
     cudaMemsetAsync(w.loss, 0, sizeof(double), st);
     k_out_grad<<<blocks((size_t)B * MLP_OUT), 256, 0, st>>>(w.Z3, w.Y, (size_t)B * MLP_OUT,
                                                           1.f / ((float)B * MLP_OUT), w.dY16, w.dY32, w.loss);
     cudaMemsetAsync(m->grads, 0, 4ull * P_COUNT, st);
     // layer 3
-    launch_gemm_bf16(MLP_OUT, MLP_H, B, w.dY16, 1, MLP_OUT, w.H2, MLP_H, 1, m->grads + P_W3, MLP_H, split, st);
+    launch_gemm_bf16(MLP_OUT, MLP_H, B, w.dY16, 1, MLP_OUT, w.H2, MLP_H, 1, m->grads + P_W3, MLP_H, split, m->err, st);
     k_colsum<<<MLP_OUT, 256, 0, st>>>(w.dY32, B, MLP_OUT, m->grads + P_B3);
-    launch_gemm_bf16(B, MLP_H, MLP_OUT, w.dY16, MLP_OUT, 1, W3, MLP_H, 1, w.dH, MLP_H, 1, st);
+    launch_gemm_bf16(B, MLP_H, MLP_OUT, w.dY16, MLP_OUT, 1, W3, MLP_H, 1, w.dH, MLP_H, 1, m->err, st);
     k_act_grad<<<blocks((size_t)B * MLP_H), 256, 0, st>>>(w.dH, w.Z2, (size_t)B * MLP_H, w.dZ16, w.dZ32);
     // layer 2
-    launch_gemm_bf16(MLP_H, MLP_H, B, w.dZ16, 1, MLP_H, w.H1, MLP_H, 1, m->grads + P_W2, MLP_H, split, st);
+    launch_gemm_bf16(MLP_H, MLP_H, B, w.dZ16, 1, MLP_H, w.H1, MLP_H, 1, m->grads + P_W2, MLP_H, split, m->err, st);
     k_colsum<<<MLP_H, 256, 0, st>>>(w.dZ32, B, MLP_H, m->grads + P_B2);
-    launch_gemm_bf16(B, MLP_H, MLP_H, w.dZ16, MLP_H, 1, W2, MLP_H, 1, w.dH, MLP_H, 1, st);
+    launch_gemm_bf16(B, MLP_H, MLP_H, w.dZ16, MLP_H, 1, W2, MLP_H, 1, w.dH, MLP_H, 1, m->err, st);
     k_act_grad<<<blocks((size_t)B * MLP_H), 256, 0, st>>>(w.dH, w.Z1, (size_t)B * MLP_H, w.dZ16, w.dZ32);
     // layer 1
-    launch_gemm_bf16(MLP_H, MLP_IN, B, w.dZ16, 1, MLP_H, w.X, MLP_IN, 1, m->grads + P_W1, MLP_IN, split, st);
+    launch_gemm_bf16(MLP_H, MLP_IN, B, w.dZ16, 1, MLP_H, w.X, MLP_IN, 1, m->grads + P_W1, MLP_IN, split, m->err, st);
     k_colsum<<<MLP_H, 256, 0, st>>>(w.dZ32, B, MLP_H, m->grads + P_B1);
 }
 
@@ -890,6 +1041,7 @@ cudaError_t mlp_train(Mlp* m, const float* dx, const float* dy, uint64_t rows, u
     if (rows == 0 || B == 0) return cudaErrorInvalidValue;
     Workspace w;
     MLP_TRY(workspace(m, B, &w));
+    MLP_TRY(cudaMemsetAsync(m->err, 0, sizeof(uint32_t), m->st));
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     for (uint32_t s = 0; s < steps; s++) {
         k_make_batch<<<blocks(B), 256, 0, m->st>>>(dx, dy, rows, B, mix_seed(seed, m->adam_t), m->norm,
@@ -909,6 +1061,7 @@ cudaError_t mlp_train(Mlp* m, const float* dx, const float* dy, uint64_t rows, u
         }
     }
     MLP_TRY(cudaGetLastError());
+    MLP_TRY(check_err(m));
     return mlp_refresh_inference(m);
 }
 
@@ -916,9 +1069,11 @@ cudaError_t mlp_grad(Mlp* m, const float* dx, const float* dy, uint32_t n, float
                      double* loss) {
     Workspace w;
     MLP_TRY(workspace(m, n, &w));
+    MLP_TRY(cudaMemsetAsync(m->err, 0, sizeof(uint32_t), m->st));
     k_make_batch<<<blocks(n), 256, 0, m->st>>>(dx, dy, n, n, 0, m->norm, w.X, w.Y, 1);
     fwd_bwd(m, w, n);
     MLP_TRY(cudaGetLastError());
+    MLP_TRY(check_err(m));
     MLP_TRY(cudaMemcpyAsync(grads_host, m->grads, 4ull * P_COUNT, cudaMemcpyDeviceToHost, m->st));
     double l = 0;
     MLP_TRY(cudaMemcpyAsync(&l, w.loss, sizeof(double), cudaMemcpyDeviceToHost, m->st));
@@ -968,6 +1123,37 @@ cudaError_t mlp_selftest_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, c
     cudaFree(conc);
     cudaFree(err);
     mlp_free(&m);
+    return e;
+}
+
+// Failure-detection self-test of the training GEMM's completion waits: one CTA of a 128 x 16 x
+// 192 product whose MMAs are withheld, so the wait for the first chunk's buffer runs out after
+// spin_limit polls; the CTA records MLP_ERR_MBAR_TIMEOUT, frees its tensor memory and returns.
+cudaError_t mlp_selftest_gemm_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, cudaStream_t st) {
+    const int M = 128, N = 16, K = 192;
+    bf16 *a = nullptr, *b = nullptr;
+    float* c = nullptr;
+    uint32_t* err = nullptr;
+    cudaError_t e = mlp_init_attributes();
+    if (e == cudaSuccess) e = cudaMalloc(&a, sizeof(bf16) * M * K);
+    if (e == cudaSuccess) e = cudaMalloc(&b, sizeof(bf16) * N * K);
+    if (e == cudaSuccess) e = cudaMalloc(&c, sizeof(float) * M * N);
+    if (e == cudaSuccess) e = cudaMalloc(&err, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(a, 0, sizeof(bf16) * M * K, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b, 0, sizeof(bf16) * N * K, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) {
+        const GemmOperand ga = gemm_operand(a, K, 1), gb = gemm_operand(b, K, 1);
+        k_gemm_tc<<<dim3(1, 1, 1), TG_THREADS, sizeof(GemmSmem), st>>>(M, N, K, ga, gb, c, N, 1, 1, err,
+                                                                       spin_limit, 1u);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(err_bits, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(a);
+    cudaFree(b);
+    cudaFree(c);
+    cudaFree(err);
     return e;
 }
 

@@ -62,14 +62,6 @@ __device__ __forceinline__ float gelu_grad(float x) {
     return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * GELU_K0 * (1.0f + 3.0f * GELU_K1 * x * x);
 }
 
-// ---- training (mma.sync) ----------------------------------------------------------------
-// C[M x N] (fp32, row stride ldc) (+)= A[M x K] * B[K x N]; A(m,k) = A[m*sam + k*sak],
-// B(k,n) = B[k*sbk + n*sbn], all bf16.  K split over gridDim.z with atomic accumulation when
-// split > 1 (C must then be zeroed first).
-void launch_gemm_bf16(int M, int N, int K, const __nv_bfloat16* A, long sam, long sak,
-                      const __nv_bfloat16* B, long sbk, long sbn, float* C, long ldc, int split,
-                      cudaStream_t st);
-
 // ---- inference (tcgen05) --------------------------------------------------------------
 // Error bits raised by the inference kernel.
 enum : uint32_t { MLP_ERR_MBAR_TIMEOUT = 1u << 8 };
@@ -86,6 +78,7 @@ struct Mlp {
     float* adam_v;
     __nv_bfloat16* wb;
     float* norm;
+    uint32_t* err;  // MLP_ERR_* bits of the training GEMMs (bounded completion waits)
     InferWeights inf;
     void* inf_mem;
     void* ws;
@@ -103,6 +96,8 @@ cudaError_t mlp_alloc(Mlp* m, uint64_t seed, cudaStream_t st);
 void mlp_free(Mlp* m);
 // failure-detection self-test: the completion wait of an inference CTA whose MMAs are withheld
 cudaError_t mlp_selftest_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, cudaStream_t st);
+// failure-detection self-test: the completion wait of a training-GEMM CTA whose MMAs are withheld
+cudaError_t mlp_selftest_gemm_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, cudaStream_t st);
 cudaError_t mlp_set_params(Mlp* m, const float* host);
 cudaError_t mlp_get_params(Mlp* m, float* host);
 cudaError_t mlp_set_norm(Mlp* m, const float* host);

@@ -7,6 +7,7 @@ with the CUDA context still usable (a plain step afterwards matches the oracle).
   that is never published.
 * The surrogate inference's tensor-core completion wait: an inference CTA whose MMAs are
   withheld, so its mbarrier is never arrived on; the CTA frees its tensor memory and returns.
+* The training GEMM's completion wait, the same way (a GEMM CTA with its MMAs withheld).
 """
 import time
 
@@ -20,7 +21,7 @@ from morphogenesis_gb300 import demo
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("which", [0, 1], ids=["scan-look-back", "mlp-completion"])
+@pytest.mark.parametrize("which", [0, 1, 2], ids=["scan-look-back", "mlp-completion", "gemm-completion"])
 def test_wait_gives_up_and_reports_timeout(built, which):
     lib = A.load()
     t0 = time.perf_counter()
@@ -35,7 +36,7 @@ def test_context_usable_after_timeouts(built):
     import morphogenesis_gb300 as mg
 
     lib = A.load()
-    for which in (0, 1):
+    for which in (0, 1, 2):
         assert lib.mg_selftest_bounded_wait(which, 200) == A.MG_ERR_DEVICE_TIMEOUT
     d = demo.make_block(8, "R", seed=0)
     g = mg.FluidSystem(d.params, d.genome, d.n)

@@ -47,8 +47,10 @@ def net(built):
     return m
 
 
-def test_gradients_match_cpu_reference(net):
-    x, y = random_batch(512, 7)
+@pytest.mark.parametrize("n", [512, 3000])
+def test_gradients_match_cpu_reference(net, n):
+    # 3000 rows: a ragged last 128-row tile and five split-K ranges in the weight gradients
+    x, y = random_batch(n, 7)
     g, loss = net.gradients(x, y)
     gr, lr = mlp_ref.grads(net.params(), net.norm(), x, y)
     assert abs(loss - lr) <= 1e-4 * abs(lr) + 1e-9
