@@ -265,8 +265,12 @@ def surrogate_section(args, peak_tflops):
     m.fit_normalization(ds)
     t0 = time.perf_counter()
     curve = m.train(ds, args.train_steps, batch=65536, lr=1e-3, seed=1)
+    train_s = time.perf_counter() - t0
+    # forward, data-gradient and weight-gradient products: 3 x 2 x batch x 24,576 FLOP per step
+    gemm_flop = 3 * 2 * 65536 * (48 * 128 + 128 * 128 + 128 * 16)
     out["train"] = {"steps": args.train_steps, "batch": 65536, "lr": 1e-3,
-                    "seconds": time.perf_counter() - t0,
+                    "seconds": train_s,
+                    "gemm_tflops_whole_step": gemm_flop * args.train_steps / train_s / 1e12,
                     "loss_first": float(curve[:10].mean()), "loss_last": float(curve[-50:].mean())}
     ds.close()
 
@@ -321,8 +325,14 @@ def surrogate_section(args, peak_tflops):
         fs.synchronize()
     ms_plain = plain.time_steps(K, A.STEP_DEFAULT)
     ms_sur = sur.time_steps(K, A.STEP_DEFAULT | A.STEP_SURROGATE)
+    ms_phys = plain.time_steps(K, A.STEP_PHYSICS)
     out["full_step"] = {"plain_particle_steps_s": n * K / (ms_plain / 1e3),
-                        "surrogate_particle_steps_s": n * K / (ms_sur / 1e3)}
+                        "surrogate_particle_steps_s": n * K / (ms_sur / 1e3),
+                        "physics_only_particle_steps_s": n * K / (ms_phys / 1e3)}
+    # the morphogen stage as the full step's cost over physics alone, in both forms
+    d_plain, d_sur = (ms_plain - ms_phys) / K, (ms_sur - ms_phys) / K
+    out["morphogen_stage_in_step"] = {"plain_ms": d_plain, "surrogate_ms": d_sur,
+                                      "speedup": d_plain / d_sur if d_sur > 0 else None}
     plain.close()
     sur.close()
 
