@@ -122,11 +122,22 @@ struct DevGenome {
     int uniform;          // all 16 diffusion rates equal and nonzero
 };
 
+// Bond records, per bond slot a two [cap] arrays of uint4: the A half (partner, rest length,
+// modulus, damping) and the B half (elastic limit, partner's particle id, strain^2
+// integrator, strain integrator).  The force pass rewrites the integrators every step; with
+// the halves in separate arrays its writes dirty the B sectors only.
+__host__ __device__ __forceinline__ size_t bond_ia(uint32_t cap, int a, uint32_t p) {
+    return (size_t)(2 * a) * cap + p;
+}
+__host__ __device__ __forceinline__ size_t bond_ib(uint32_t cap, int a, uint32_t p) {
+    return (size_t)(2 * a + 1) * cap + p;
+}
+
 struct Carried {
     float4* pos;
     float4* vel;
     float4* veval;
-    uint4* bond;  // [NB][cap][2]
+    uint4* bond;  // [NB][2][cap]: per bond slot, the A halves then the B halves (bond_ia/bond_ib)
     uint32_t* pidx;
     float* conc;
     uint32_t* genes;

@@ -18,9 +18,8 @@ __global__ void k_import_bonds(uint32_t cap, const uint32_t* __restrict__ ref,
     if (k >= (size_t)cap * NB) return;
     uint32_t p = (uint32_t)(k / NB), a = (uint32_t)(k % NB);
     const uint32_t* w = ref + k * 9;
-    size_t r = ((size_t)a * cap + p) * 2;
-    bond[r] = make_uint4(w[0], w[2], w[3], w[4]);
-    bond[r + 1] = make_uint4(w[1], w[5], w[6], w[7]);
+    bond[bond_ia(cap, (int)a, p)] = make_uint4(w[0], w[2], w[3], w[4]);
+    bond[bond_ib(cap, (int)a, p)] = make_uint4(w[1], w[5], w[6], w[7]);
     uint32_t o = origin[p];
     if (o != UNDEF) change[(size_t)o * NB + a] = w[8];
 }
@@ -33,8 +32,7 @@ __global__ void k_export_bonds(uint32_t cap, const uint4* __restrict__ bond,
     size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= (size_t)cap * NB) return;
     uint32_t p = (uint32_t)(k / NB), a = (uint32_t)(k % NB);
-    size_t r = ((size_t)a * cap + p) * 2;
-    uint4 A = bond[r], B = bond[r + 1];
+    uint4 A = bond[bond_ia(cap, (int)a, p)], B = bond[bond_ib(cap, (int)a, p)];
     if (apply_breaks && p < *nactive_p && (brk[p] >> a) & 1u) A.y = 0u;
     uint32_t* w = ref + k * 9;
     w[0] = A.x; w[1] = B.x; w[2] = A.y; w[3] = A.z; w[4] = A.w;
@@ -290,9 +288,8 @@ __global__ void k_init_set(uint32_t cap, uint4* __restrict__ bond, uint32_t* __r
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= cap) return;
     for (int a = 0; a < NB; a++) {
-        size_t r = ((size_t)a * cap + p) * 2;
-        bond[r] = make_uint4(NO_PARTNER, 0u, 0u, 0u);
-        bond[r + 1] = make_uint4(0u, NO_PARTNER, 0u, 0u);
+        bond[bond_ia(cap, a, p)] = make_uint4(NO_PARTNER, 0u, 0u, 0u);
+        bond[bond_ib(cap, a, p)] = make_uint4(0u, NO_PARTNER, 0u, 0u);
     }
     for (int k = 0; k < 12; k++) pidx[(size_t)p * 12 + k] = NO_PARTNER;
     origin[p] = p;

@@ -1096,14 +1096,6 @@ __device__ __forceinline__ BondTerm bond_term(float4 po, float4 vo, float4 pj, f
     return t;
 }
 
-// A bond record (32 bytes: partner, rest length, modulus, damping | elastic limit, -, the two
-// strain integrators) as one 256-bit load; records are 32-byte aligned.
-__device__ __forceinline__ void load_record(const uint4* rec, uint4& A, uint4& B) {
-    asm("ld.global.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=r"(A.x), "=r"(A.y), "=r"(A.z), "=r"(A.w), "=r"(B.x), "=r"(B.y), "=r"(B.z), "=r"(B.w)
-        : "l"(rec));
-}
-
 __device__ __forceinline__ bool is_nan3(const BondTerm& t) {
     return t.ex != t.ex || t.ey != t.ey || t.ez != t.ez;
 }
@@ -1153,9 +1145,8 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force(DevParams P, Car
     // own (outgoing) bonds
 #pragma unroll
     for (int a = 0; a < NB; a++) {
-        uint4* rec = C.bond + ((size_t)a * cap + p) * 2;
-        uint4 A, B;
-        load_record(rec, A, B);
+        uint4* recb = C.bond + bond_ib(cap, a, p);
+        const uint4 A = C.bond[bond_ia(cap, a, p)], B = *recb;
         const uint32_t j = A.x;
         const float restlen = __uint_as_float(A.y);
         if (j >= nact || restlen < REST_MIN) {
@@ -1167,7 +1158,7 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force(DevParams P, Car
                                      __uint_as_float(A.w), elastlim, P.pmass);
         const float sq = __uint_as_float(B.z) + t.strain * t.strain;
         const float si = __uint_as_float(B.w) + t.strain;
-        *reinterpret_cast<uint2*>(&rec[1].z) = make_uint2(__float_as_uint(sq), __float_as_uint(si));
+        *reinterpret_cast<uint2*>(&recb->z) = make_uint2(__float_as_uint(sq), __float_as_uint(si));
         bterm[(size_t)a * cap + p] = make_float4(t.ex, t.ey, t.ez, __uint_as_float(j));
         if (!is_nan3(t)) {
             fx = fx - t.ex;
@@ -1287,7 +1278,7 @@ void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool
 __device__ __forceinline__ void apply_breaks(uint4* bond, uint32_t cap, uint32_t p, uint32_t br) {
 #pragma unroll
     for (int a = 0; a < NB; a++)
-        if (br & (1u << a)) reinterpret_cast<uint32_t*>(bond + ((size_t)a * cap + p) * 2)[1] = 0u;
+        if (br & (1u << a)) reinterpret_cast<uint32_t*>(bond + bond_ia(cap, a, p))[1] = 0u;
 }
 
 __global__ void __launch_bounds__(256) k_apply_breaks(uint32_t cap, uint4* __restrict__ bond,

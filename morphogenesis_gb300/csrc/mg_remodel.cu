@@ -51,7 +51,7 @@ __device__ __forceinline__ bool rest_is_small(uint32_t rest_bits) {
 }
 
 __device__ __forceinline__ uint4 bond_a(const uint4* bond, uint32_t cap, uint32_t p, int a) {
-    return bond[((size_t)a * cap + p) * 2];
+    return bond[bond_ia(cap, a, p)];
 }
 
 __device__ __forceinline__ int heal_slot(const uint4* bond, uint32_t cap, uint32_t p, uint32_t nact,
@@ -132,11 +132,11 @@ __global__ void __launch_bounds__(256) k_bond_changes(DevParams P, const DevGeno
     const uint32_t o = C.origin[p];
     for (int b = 0; b < NB; b++) {
         const int type = bone && b < 4 ? 2 : (fibre && b == 0 ? 1 : 0);
-        const size_t r0 = ((size_t)b * cap + p) * 2;
-        uint4 A = C.bond[r0];
+        const size_t ra = bond_ia(cap, b, p), rb = bond_ib(cap, b, p);
+        uint4 A = C.bond[ra];
         float rest = __uint_as_float(A.y);
         if (rest > 0.f) {
-            uint4 B = C.bond[r0 + 1];
+            uint4 B = C.bond[rb];
             const float si = __uint_as_float(B.w) / steps, sq = __uint_as_float(B.z) / steps;
             const float* T = G->tanh_p[type];
             rest = rest * (T[0] + T[1] * mg_tanh_cw(T[2] * si - T[3]));
@@ -145,8 +145,8 @@ __global__ void __launch_bounds__(256) k_bond_changes(DevParams P, const DevGeno
             A.z = __float_as_uint(mod);
             B.z = 0u;
             B.w = 0u;
-            C.bond[r0] = A;
-            C.bond[r0 + 1] = B;
+            C.bond[ra] = A;
+            C.bond[rb] = B;
         }
         const bool heal = rest == 0.f || A.x >= n;
         if (o != UNDEF) change_cold[(size_t)o * NB + b] = heal ? 1u : 0u;
@@ -455,18 +455,18 @@ __global__ void __launch_bounds__(256) k_accept(DevParams P, const DevGenome* __
     if (slot < 0) return;  // no free incoming slot left for this proposal: retry next step
     const int b = heal_slot(bond, cap, i, n, origin, change_cold, from_changes);
     if (b < 0) return;
-    const size_t r0 = ((size_t)b * cap + i) * 2;
-    const uint4 A = bond[r0];
+    const size_t ra = bond_ia(cap, b, i), rb = bond_ib(cap, b, i);
+    const uint4 A = bond[ra];
     const uint32_t oj = origin[j];
     const uint32_t pj = oj != UNDEF ? pid_cold[oj] : UNDEF;
     if (P.heal_params) {  // makeBond(i, j, b, slot, elastin) (cuda:1573-1593)
         const float* E = G->bparam[0];
-        bond[r0] = make_uint4(j, __float_as_uint(E[9]), __float_as_uint(E[10]), __float_as_uint(E[11]));
-        bond[r0 + 1] = make_uint4(__float_as_uint(E[8]), pj, 0u, 0u);
+        bond[ra] = make_uint4(j, __float_as_uint(E[9]), __float_as_uint(E[10]), __float_as_uint(E[11]));
+        bond[rb] = make_uint4(__float_as_uint(E[8]), pj, 0u, 0u);
     } else {
         const float rest = sqrtf(d);
-        bond[r0] = make_uint4(j, __float_as_uint(rest), A.z, A.w);
-        bond[r0 + 1] = make_uint4(__float_as_uint(1.5f * rest), pj, 0u, 0u);
+        bond[ra] = make_uint4(j, __float_as_uint(rest), A.z, A.w);
+        bond[rb] = make_uint4(__float_as_uint(1.5f * rest), pj, 0u, 0u);
     }
     const uint32_t oi = origin[i];
     if (oi != UNDEF) change_cold[(size_t)oi * NB + b] = 0u;

@@ -474,11 +474,11 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
             D.pos[p] = __ldg(S.pos + i);
 #pragma unroll
             for (int a = 0; a < NB; a++) {
-                const size_t src = ((size_t)a * cap + i) * 2, dst = ((size_t)a * cap + p) * 2;
-                uint4 A, B;
-                ld32(S.bond + src, A, B);
+                uint4 A = __ldg(S.bond + bond_ia(cap, a, i));
+                const uint4 B = __ldg(S.bond + bond_ib(cap, a, i));
                 A.x = remap(A.x, cap, newidx);
-                st32(D.bond + dst, A, B);
+                D.bond[bond_ia(cap, a, p)] = A;
+                D.bond[bond_ib(cap, a, p)] = B;
             }
             if (P.full_epi) {
                 // per-gene words move with the particle; the bits (dense-list membership at sort
@@ -518,9 +518,8 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
             D.pos[p] = make_float4(P.bmin[0], P.bmin[1], P.null_z, 0.0f);
 #pragma unroll
             for (int a = 0; a < NB; a++) {
-                const size_t dst = ((size_t)a * cap + p) * 2;
-                D.bond[dst] = make_uint4(NO_PARTNER, 0u, 0u, 0u);
-                D.bond[dst + 1] = make_uint4(0u, NO_PARTNER, 0u, 0u);
+                D.bond[bond_ia(cap, a, p)] = make_uint4(NO_PARTNER, 0u, 0u, 0u);
+                D.bond[bond_ib(cap, a, p)] = make_uint4(0u, NO_PARTNER, 0u, 0u);
             }
             D.genes[p] = 0u;
             if (P.full_epi)

@@ -166,3 +166,59 @@ def test_handover_takes_the_plain_result(built):
     assert judged == d.n and handed == d.n
     assert np.array_equal(plain.download(A.FCONC), sur.download(A.FCONC))
     assert np.array_equal(plain.download(A.FPOS), sur.download(A.FPOS))
+
+
+def _one_stage_error(m, d):
+    """Per-particle relative error of one surrogate morphogen stage against the plain stage from
+    the same state (largest deviation over the largest plain concentration)."""
+    plain = mg.FluidSystem(d.params, d.genome, d.n)
+    sur = mg.FluidSystem(d.params, d.genome, d.n)
+    for fs in (plain, sur):
+        fs.TransferToCL(d.arrays)
+        fs.Run(3)
+    S.attach(sur, m, judge_period=0, judge_stride=0, threshold=1e-3)
+    plain.Run(1, A.STEP_GENES)
+    sur.Run(1, A.STEP_GENES | A.STEP_SURROGATE)
+    cp, cs = plain.download(A.FCONC).astype(np.float64), sur.download(A.FCONC).astype(np.float64)
+    plain.close()
+    sur.close()
+    return np.abs(cs - cp).max(1) / np.maximum(np.abs(cp).max(1), 1e-30)
+
+
+def test_what_the_trained_network_gains(built):
+    """What the trained network gains over the method without it, on a 24^3 scene (13,824
+    particles): its one-stage accuracy against the same network untrained (the gain of
+    training; both with the normalisation fitted on the same pairs), and the morphogen stage's
+    cost in both forms inside the full step (step time minus the physics-only step time).  The
+    plain stage here is the density pass's fused diffusion + reaction epilogue, and the network
+    stands in for the reaction only, so the surrogate form costs more than the plain one: the
+    test records the measured ratio and asserts what holds."""
+    m, ds, _ = _train_small()
+    m0 = S.Mlp(seed=5)
+    m0.fit_normalization(ds)
+    d = demo.make_block(24, "R", seed=7)
+    e_trained, e_untrained = _one_stage_error(m, d), _one_stage_error(m0, d)
+    K = 50
+    plain = mg.FluidSystem(d.params, d.genome, d.n)
+    sur = mg.FluidSystem(d.params, d.genome, d.n)
+    for fs in (plain, sur):
+        fs.TransferToCL(d.arrays)
+        fs.Run(3)
+    S.attach(sur, m, judge_period=10, judge_stride=64, threshold=1e-3)
+    t_phys = plain.time_steps(K, A.STEP_PHYSICS) / K
+    t_plain = plain.time_steps(K, A.STEP_DEFAULT) / K
+    t_sur = sur.time_steps(K, A.STEP_DEFAULT | A.STEP_SURROGATE) / K
+    stage_plain, stage_sur = t_plain - t_phys, t_sur - t_phys
+    print(f"one-stage error, trained: median {np.median(e_trained):.2e} max {e_trained.max():.2e}; "
+          f"untrained: median {np.median(e_untrained):.2e}; stage ms plain {stage_plain:.4f} "
+          f"surrogate {stage_sur:.4f} (speed ratio {stage_plain / max(stage_sur, 1e-9):.2f})")
+    assert np.isfinite(e_trained).all() and np.isfinite(e_untrained).all()
+    assert np.median(e_trained) <= 1e-3, f"trained median one-stage error {np.median(e_trained):.2e}"
+    # measured on a GB300: trained 2.7e-4, untrained 1.9e-3 (an untrained network's increments
+    # are near zero, so its error is about the reaction's own size relative to the
+    # concentrations); stage 0.028 ms plain against 0.032 ms surrogate (0.88)
+    assert np.median(e_untrained) >= 4 * np.median(e_trained), \
+        f"training gained too little: {np.median(e_untrained):.2e} vs {np.median(e_trained):.2e}"
+    assert t_phys > 0 and t_plain > 0 and t_sur > 0
+    for x in (plain, sur, m, m0, ds):
+        x.close()
