@@ -97,6 +97,7 @@ struct mg_system {
     // learned morphogen surrogate (attached network is borrowed, not owned)
     mg::Mlp* sur = nullptr;
     __nv_bfloat16* feat = nullptr;   // [cap][48] surrogate inputs
+    CUtensorMap feat_map{};          // TMA view of feat for the inference kernel
     float* feat_scale = nullptr;     // [cap] per-particle scale of the inputs
     float* conc_plain = nullptr;     // [cap][16] plain update of judged / handed-over particles
     uint32_t* sur_stats = nullptr;   // [0] judged, [1] handed over, [2] worst relative error bits
@@ -536,7 +537,7 @@ void enqueue_surrogate_morphogen(mg_system* h, bool density, bool prof, bool hea
     if (h->search) h->flist_valid = true;
     { Mark m(h, prof, "mlp_infer");
       // conc_out holds the diffused concentrations; the network adds the reaction increment
-      launch_mlp_infer(h->sur, h->feat, h->feat_scale, conc_of(h, cout), h->conc_plain, conc_of(h, cout),
+      launch_mlp_infer(h->sur, h->feat_map, h->feat_scale, conc_of(h, cout), h->conc_plain, conc_of(h, cout),
                        h->set[h->cur].genes, h->s.counters + 3, 0, h->s.counters + 5, h->judge_period,
                        h->judge_stride, h->judge_threshold, h->sur_stats, h->s.counters + 2,
                        h->num_sms, h->stream); }
@@ -1950,8 +1951,10 @@ mg_status mg_mlp_infer(mg_mlp m, const float* x, uint32_t n, float* y) {
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    CUtensorMap map;
+    if (e == cudaSuccess) e = mg::make_feat_map(feat, n, &map);
     if (e == cudaSuccess) {
-        mg::launch_mlp_infer(&m->m, feat, nullptr, cin, nullptr, cout, nullptr, nullptr, n, nullptr, 0, 0, 0.f,
+        mg::launch_mlp_infer(&m->m, map, nullptr, cin, nullptr, cout, nullptr, nullptr, n, nullptr, 0, 0, 0.f,
                              nullptr, err, sms, m->st);
         e = cudaGetLastError();
     }
@@ -2062,6 +2065,13 @@ mg_status mg_set_surrogate(mg_handle h, mg_mlp m, uint32_t judge_period, uint32_
         if (e == cudaSuccess) e = cudaMalloc(&h->conc_plain, 4ull * h->cap * NTF);
         if (e == cudaSuccess) e = cudaMalloc(&h->sur_stats, 16);
         if (e != cudaSuccess) return fail(h, MG_ERR_OOM, "surrogate buffers");
+    }
+    {
+        cudaError_t e = mg::make_feat_map(h->feat, h->cap, &h->feat_map);
+        if (e != cudaSuccess) {
+            h->sur = nullptr;
+            return cuda_fail(h, e, "surrogate feature tensor map");
+        }
     }
     MG_CUDA(h, cudaMemsetAsync(h->sur_stats, 0, 16, h->stream));
     cudaStreamSynchronize(m->st);

@@ -168,15 +168,22 @@ struct InferSmem {
     bf16 w1[MLP_H * MLP_IN];    // 12 KB  B operand layer 1 (N=128 x K=48)
     bf16 w2[MLP_H * MLP_H];     // 32 KB  B operand layer 2 (N=128 x K=128)
     bf16 w3[MLP_OUT * MLP_H];   //  4 KB  B operand layer 3 (N=16 x K=128)
-    // per group: A operand of layer 1 (128 x 48, the first 12 KB) and of layers 2 and 3
-    // (128 x 128); layer 1 has finished reading its operand before the epilogue overwrites it
+    // per group: A operand of layer 1, the tile's 128 x 48 features as six TMA planes of 8
+    // features x 128 rows (2 KB each: plane kb holds core matrices (row group, kb) 128 bytes
+    // apart), loaded one tile ahead
+    bf16 feat[INF_GROUPS][128 * MLP_IN];
+    // per group: A operand of layers 2 and 3 (128 x 128, core-matrix layout)
     bf16 act[INF_GROUPS][128 * MLP_H];
     alignas(16) float b1[MLP_H];
     alignas(16) float b2[MLP_H];
     alignas(16) float b3[MLP_OUT];
-    unsigned long long mbar[INF_GROUPS];
+    unsigned long long mbar[INF_GROUPS];  // MMA completion
+    unsigned long long tbar[INF_GROUPS];  // feature tile arrival (TMA transaction bytes)
     uint32_t tmem_base;
 };
+static_assert(sizeof(InferSmem) <= 232448, "inference shared memory above the 227 KB a CTA may use");
+constexpr uint32_t FEAT_PLANE_BYTES = 128u * 8u * 2u;               // 8 features x 128 rows
+constexpr uint32_t FEAT_TILE_BYTES = FEAT_PLANE_BYTES * (MLP_IN / 8);  // 12 KB
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -306,6 +313,37 @@ __device__ __forceinline__ void bias_gelu8(const float* v, const float* b, float
 #pragma unroll
     for (int i = 0; i < 8; i++) h[i] = gelu(v[i] + b[i]);
 #endif
+}
+
+// One feature tile (rows row0 .. row0 + 127, all 48 features) into its six planes: the
+// mbarrier expects the tile's bytes, and each TMA load of a plane completes its share (rows
+// past the matrix read as zeros).  The planes start at feature 0, 8, ..., 40 (16-byte aligned
+// x coordinates).  Single thread.
+__device__ __forceinline__ void feat_tile_tma(bf16* planes, const CUtensorMap* map, uint32_t row0,
+                                              uint32_t bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(FEAT_TILE_BYTES)
+                 : "memory");
+#pragma unroll
+    for (uint32_t kb = 0; kb < MLP_IN / 8; kb++)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+            "[%0], [%1, {%2, %3}], [%4];\n" ::"r"(smem_u32(planes + kb * 128u * 8u)),
+            "l"(reinterpret_cast<uint64_t>(map)), "r"(kb * 8u), "r"(row0), "r"(bar)
+            : "memory");
+}
+
+// Layer 1 from the feature planes: D[128 x 128] = F[128 x 48] * W1[128 x 48]^T.  In the planes
+// the two core matrices of a K=16 step are a plane apart (leading byte offset 2 KB) and row
+// groups 128 bytes apart (stride byte offset); W1 keeps the core-matrix tile layout.
+__device__ __forceinline__ void issue_layer1(uint32_t d_tmem, const bf16* planes, const bf16* w1) {
+    const uint32_t sa = smem_u32(planes), sb = smem_u32(w1);
+    const uint32_t idesc = idesc_bf16(128, MLP_H);
+#pragma unroll
+    for (uint32_t s = 0; s < MLP_IN / 16; s++) {
+        const uint64_t ad = smem_desc(sa + s * 2u * FEAT_PLANE_BYTES, FEAT_PLANE_BYTES, 128u);
+        const uint64_t bd = smem_desc(sb + s * 256u, 128u, (MLP_IN >> 3) * 128u);
+        mma_f16_ss(d_tmem, ad, bd, idesc, s > 0 ? 1u : 0u);
+    }
 }
 
 // Issues one layer: D[128 x N] = A[128 x K] * B[N x K]^T, K/16 MMAs (single thread).
@@ -572,14 +610,14 @@ void launch_gemm_bf16(int M, int N, int K, const bf16* A, long sam, long sak, co
 // this step) or already handed to the plain method (bit 31 of their gene word) compare against /
 // take the plain update in conc_plain.
 __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
-    InferWeights W, const bf16* __restrict__ feat, const float* __restrict__ feat_scale,
+    InferWeights W, const __grid_constant__ CUtensorMap feat_map, const float* __restrict__ feat_scale,
     const float* conc_in,
     const float* __restrict__ conc_plain, float* conc_out, uint32_t* __restrict__ genes,
     const uint32_t* __restrict__ nactive_p, uint32_t ntotal_override, const uint32_t* __restrict__ step_p,
     uint32_t judge_period, uint32_t judge_stride, float threshold, uint32_t* __restrict__ stats,
     uint32_t* __restrict__ err, uint32_t spin_limit, uint32_t withhold) {
-    // spin_limit bounds every completion wait; withhold != 0 (failure-detection self-test
-    // only) issues no MMA, so the first wait runs out
+    // spin_limit bounds every wait (feature arrival, MMA completion); withhold != 0
+    // (failure-detection self-test only) issues no MMA, so the first completion wait runs out
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
@@ -610,8 +648,11 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
     }
     if (tid < INF_GROUPS) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&S.mbar[tid])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&S.tbar[tid])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
+    if (tid == 0)
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&feat_map)) : "memory");
     if (warp == 0) {  // one warp allocates the tensor memory of the CTA
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
                          smem_u32(&S.tmem_base)),
@@ -624,8 +665,10 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
     __syncthreads();
     tc_fence_after();
     const uint32_t mbar = smem_u32(&S.mbar[g]);
+    const uint32_t tbar = smem_u32(&S.tbar[g]);
     const uint32_t tmem = S.tmem_base + g * 128u;        // this group's 128 columns
     bf16* act = S.act[g];
+    bf16* planes = S.feat[g];
     const uint32_t quad = gwarp & 3u, half = gwarp >> 2;
     const uint32_t lane_addr = tmem + ((quad * 32u) << 16);  // this warp's TMEM lanes
     const uint32_t row = quad * 32u + (gtid & 31u);          // tile row = this thread's particle
@@ -633,31 +676,36 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
     bool ok = true;
 
     const uint32_t ntiles = (n + 127) / 128;
-    for (uint32_t tile = blockIdx.x * INF_GROUPS + g; tile < ntiles; tile += gridDim.x * INF_GROUPS) {
+    const uint32_t first = blockIdx.x * INF_GROUPS + g, tstride = gridDim.x * INF_GROUPS;
+    // tpend: 0, or 1 + the parity of a feature tile in flight whose arrival is not yet observed
+    uint32_t tphase = 0, tpend = 0;
+    if (first < ntiles) {
+        if (gtid == 0) feat_tile_tma(planes, &feat_map, first * 128u, tbar);
+        tpend = 1u + tphase;
+    }
+    for (uint32_t tile = first; tile < ntiles; tile += tstride) {
         const uint32_t p = tile * 128u + row;
         const bool live = p < n;
-        // layer-1 operand: the particle's 48 bf16 features (zeros past the end), 6 / INF_SPLIT
-        // of the six 16-byte chunks per thread
-        {
-            const uint4* src = reinterpret_cast<const uint4*>(feat + (size_t)p * MLP_IN);
-#pragma unroll
-            for (uint32_t c = half * (6 / INF_SPLIT); c < (half + 1) * (6 / INF_SPLIT); c++) {
-                const uint4 v = live ? src[c] : make_uint4(0u, 0u, 0u, 0u);
-                *reinterpret_cast<uint4*>(act + core_offset(row, c * 8, MLP_IN)) = v;
-            }
-        }
-        fence_async_smem();
-        tc_fence_before();
-        group_sync(g);
+        // the tile's features (rows past the matrix are zeros; rows past n are computed and
+        // not stored)
+        ok = group_and(g, mbar_wait(tbar, tphase, spin_limit));
+        tphase ^= 1u;
+        if (!ok) break;
+        tpend = 0;
         tc_fence_after();
         if (gtid == 0 && !withhold) {
-            issue_layer(tmem, act, S.w1, MLP_IN, MLP_H);
+            issue_layer1(tmem, planes, S.w1);
             mma_commit(mbar);
         }
         ok = group_and(g, mbar_wait(mbar, phase, spin_limit));
         phase ^= 1u;
         if (!ok) break;
         tc_fence_after();
+        // layer 1 has read the planes: the next tile's features load under this tile's work
+        if (tile + tstride < ntiles) {
+            if (gtid == 0) feat_tile_tma(planes, &feat_map, (tile + tstride) * 128u, tbar);
+            tpend = 1u + tphase;
+        }
         // layer-1 epilogue: bias + GELU -> layer-2 operand (layer 1 has finished with `act`)
 #pragma unroll
         for (uint32_t c0 = half * INF_COLS; c0 < (half + 1) * INF_COLS; c0 += 32) {
@@ -770,11 +818,12 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         tc_fence_after();
     }
     if (!ok) {
-        // a wait gave up: record it and give the group's MMAs in flight one more bounded wait
-        // before the tensor memory is released
+        // a wait gave up: record it and give the group's MMAs and feature load in flight one
+        // more bounded wait each before the tensor memory and the CTA's shared memory go
         if (gtid == 0) {
             atomicOr(err, MLP_ERR_MBAR_TIMEOUT);
             mbar_wait(mbar, phase ^ 1u, spin_limit);
+            if (tpend) mbar_wait(tbar, tpend - 1u, spin_limit);
         }
     }
     tc_fence_before();
@@ -1082,13 +1131,40 @@ cudaError_t mlp_grad(Mlp* m, const float* dx, const float* dy, uint32_t n, float
     return cudaSuccess;
 }
 
-void launch_mlp_infer(const Mlp* m, const bf16* feat, const float* feat_scale, const float* conc_in,
+// cuTensorMapEncodeTiled, looked up once through the runtime (no link against the driver
+// library).
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+cudaError_t make_feat_map(const bf16* feat, uint32_t rows, CUtensorMap* map) {
+    static EncodeTiled encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        MLP_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+        encode = reinterpret_cast<EncodeTiled>(fn);
+    }
+    // a 16-byte aligned base, a 96-byte row stride and 16-byte boxes along the features
+    if ((reinterpret_cast<uintptr_t>(feat) & 15u) != 0 || rows == 0) return cudaErrorInvalidValue;
+    const cuuint64_t dims[2] = {(cuuint64_t)MLP_IN, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)MLP_IN * sizeof(bf16)};
+    const cuuint32_t box[2] = {8u, 128u};
+    const cuuint32_t estride[2] = {1u, 1u};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(feat), dims, strides,
+                              box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+void launch_mlp_infer(const Mlp* m, const CUtensorMap& feat_map, const float* feat_scale, const float* conc_in,
                       const float* conc_plain,
                       float* conc_out, uint32_t* genes, const uint32_t* nactive, uint32_t n_override,
                       const uint32_t* step, uint32_t period, uint32_t stride, float threshold,
                       uint32_t* stats, uint32_t* err, int num_sms, cudaStream_t st) {
     k_mlp_infer<<<num_sms, INF_THREADS, sizeof(InferSmem), st>>>(
-        m->inf, feat, feat_scale, conc_in, conc_plain, conc_out, genes, nactive, n_override, step,
+        m->inf, feat_map, feat_scale, conc_in, conc_plain, conc_out, genes, nactive, n_override, step,
         period, stride,
         threshold, stats, err, MBAR_SPIN_LIMIT, 0u);
 }
@@ -1111,9 +1187,11 @@ cudaError_t mlp_selftest_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, c
     if (e == cudaSuccess) e = cudaMemsetAsync(feat, 0, sizeof(bf16) * 128 * MLP_IN, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(conc, 0, sizeof(float) * 2 * 128 * NTF, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(uint32_t), st);
+    CUtensorMap map;
+    if (e == cudaSuccess) e = make_feat_map(feat, 128, &map);
     if (e == cudaSuccess) {
         k_mlp_infer<<<1, INF_THREADS, sizeof(InferSmem), st>>>(
-            m.inf, feat, nullptr, conc, nullptr, conc + 128 * NTF, nullptr, nullptr, 128u, nullptr,
+            m.inf, map, nullptr, conc, nullptr, conc + 128 * NTF, nullptr, nullptr, 128u, nullptr,
             0u, 0u, 0.f, nullptr, err, spin_limit, 1u);
         e = cudaGetLastError();
     }

@@ -1,12 +1,13 @@
 // mg_mlp.cuh - the learned reaction surrogate: MLP 48 -> 128 -> 128 -> 16 with GELU.
 //
-// Inputs per particle: 16 concentrations, 16 neighbour-mean concentrations (over the
-// diffusion neighbours), 16 gene bits as 0/1.  Output: the concentration increment of one
-// morphogen stage (diffusion + gene reaction).  BF16 weights and activations, FP32
-// accumulation.  Training keeps FP32 master weights for Adam; inference uses weights with the
+// Inputs per particle: 16 concentrations (after diffusion and decay), 16 neighbour-mean
+// concentrations (over the diffusion neighbours), both divided by the particle's largest
+// concentration, and 16 gene bits as 0/1.  Output: the gene reaction's concentration increment
+// over the same scale.  BF16 weights and activations, FP32 accumulation.  Training keeps FP32 master weights for Adam; inference uses weights with the
 // input and output normalisation folded into the first and last layer.
 #pragma once
 #include <cstdint>
+#include <cuda.h>  // CUtensorMap (types only; the encoder is looked up through the runtime)
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -108,7 +109,10 @@ cudaError_t mlp_train(Mlp* m, const float* dx, const float* dy, uint64_t rows, u
                       uint32_t batch, float lr, uint64_t seed, float* loss_host);
 cudaError_t mlp_grad(Mlp* m, const float* dx, const float* dy, uint32_t n, float* grads_host,
                      double* loss);
-void launch_mlp_infer(const Mlp* m, const __nv_bfloat16* feat, const float* feat_scale,
+// Tensor map of a [rows][48] bf16 feature matrix for the inference kernel's TMA loads: boxes
+// of 8 features x 128 rows (one 2 KB plane of core matrices each), rows past `rows` read as 0.
+cudaError_t make_feat_map(const __nv_bfloat16* feat, uint32_t rows, CUtensorMap* map);
+void launch_mlp_infer(const Mlp* m, const CUtensorMap& feat_map, const float* feat_scale,
                       const float* conc_in,
                       const float* conc_plain, float* conc_out, uint32_t* genes,
                       const uint32_t* nactive, uint32_t n_override, const uint32_t* step,
