@@ -692,6 +692,11 @@ __global__ void __launch_bounds__(INF_THREADS, 1) k_mlp_infer(
         tphase ^= 1u;
         if (!ok) break;
         tpend = 0;
+        // the output step's reads of this particle, towards L2 while the three layers run
+        if (half == 0 && live) {
+            asm volatile("prefetch.global.L2 [%0];\n" ::"l"(conc_in + (size_t)p * NTF));
+            if (genes) asm volatile("prefetch.global.L2 [%0];\n" ::"l"(genes + p));
+        }
         tc_fence_after();
         if (gtid == 0 && !withhold) {
             issue_layer1(tmem, planes, S.w1);
