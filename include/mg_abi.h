@@ -322,7 +322,13 @@ enum mg_option {
      * kernels read (FCONC[p*16+tf], fluid_system_cuda.cu:739, 3097; default); 1 = float[16][N],
      * the reference host's own buffer (getConc(tf) = FCONC + tf*mMaxPoints, fluid_system.h:574),
      * transposed on the device */
-    MG_OPT_CONC_LAYOUT = 3
+    MG_OPT_CONC_LAYOUT = 3,
+    /* steps between re-origins (0 = never; default 64): the bond records and cold fields are
+     * kept by each particle's origin slot so that the sort does not move them; a re-origin sort
+     * renumbers the origins to the sorted order (one step that moves them), after which the
+     * force pass reads a warp's bond records from contiguous slots.  The first step after an
+     * upload of FPOS re-origins too.  Results are identical for every period. */
+    MG_OPT_REORIGIN_PERIOD = 4
 };
 mg_status mg_set_option(mg_handle h, int32_t option, int32_t value);
 

@@ -38,6 +38,7 @@ STEP_DEFAULT = STEP_PHYSICS | STEP_GENES
 OPT_NEIGHBOR_SEARCH = 1
 OPT_HEAL_PARAMS = 2
 OPT_CONC_LAYOUT = 3
+OPT_REORIGIN_PERIOD = 4
 MLP_IN, MLP_H, MLP_OUT = 48, 128, 16
 P_W1 = 0
 P_B1 = P_W1 + MLP_H * MLP_IN

@@ -62,7 +62,14 @@ struct mg_system {
     Carried set[2]{};
     int cur = 0;
     int conc_cur = 0;
-    Cold cold{};
+    Cold cold{};      // the current origin space (cold fields, bond records)
+    Cold cold_alt{};  // the other one, which a re-origin moves the records into
+    int osp = 0;      // which of the two is current (part of the captured graphs' keys)
+    // re-origin: every `reorigin_period` plain steps (and at the first after an upload of
+    // positions) the sort renumbers origins to the sorted order, so that the force pass reads
+    // the bond records of a warp's particles from contiguous slots; 0 = never
+    uint32_t reorigin_period = 64, since_reorigin = 0;
+    bool reorigin_due = true;
     Scratch s{};
     void* staging = nullptr;
     size_t staging_bytes = 0;
@@ -423,17 +430,33 @@ void enqueue_insert_rank(mg_system* h, bool prof) {
     { Mark m(h, prof, "cellsort"); launch_cellsort(P, h->s, h->num_sms, h->search == 2, st); }
 }
 
+// Internal step flag (never a caller's): this step's sort renumbers the origins.
+constexpr uint32_t STEP_REORIGIN = 1u << 31;
+
+// After a re-origin gather: the other origin space becomes the current one.
+void swap_ospace(mg_system* h) {
+    std::swap(h->cold, h->cold_alt);
+    for (Carried& c : h->set) {
+        c.bond = h->cold.bond;
+        c.partner = h->cold.partner;
+    }
+    h->osp ^= 1;
+}
+
 // conc_ready / motion_ready: the concentrations / the velocities and incoming-bond table arrive
 // later (uploads still in flight).  The rest is moved first, the concentrations after the
 // stream has waited for conc_ready; the motion part is left to flush_motion, which the step
 // calls before its force pass (nothing before it reads those fields).
 void enqueue_gather(mg_system* h, bool prof, cudaEvent_t conc_ready = nullptr,
-                    cudaEvent_t motion_ready = nullptr) {
+                    cudaEvent_t motion_ready = nullptr, bool reorigin = false) {
     int src = h->cur, dst = 1 - h->cur;
     int csrc = h->conc_cur, cdst = 1 - h->conc_cur;
     { Mark m(h, prof, "gather");
-      const int first = GATHER_CORE | (conc_ready ? 0 : GATHER_CONC) | (motion_ready ? 0 : GATHER_MOTION);
-      launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream, first);
+      const int first = GATHER_CORE | (conc_ready ? 0 : GATHER_CONC) | (motion_ready ? 0 : GATHER_MOTION) |
+                        (reorigin ? GATHER_REORIGIN : 0);
+      launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream, first,
+                    &h->cold, &h->cold_alt);
+      if (reorigin) swap_ospace(h);
       if (conc_ready) {
           cudaStreamWaitEvent(h->stream, conc_ready, 0);
           launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream,
@@ -596,7 +619,8 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
     }
     enqueue_insert_rank(h, prof);
     if (up) cudaStreamWaitEvent(st, ev[2], 0);
-    enqueue_gather(h, prof, conc_up ? ev[5] : nullptr, motion_up ? ev[6] : nullptr);
+    enqueue_gather(h, prof, conc_up ? ev[5] : nullptr, motion_up ? ev[6] : nullptr,
+                   (flags & STEP_REORIGIN) != 0);
     const bool remodel = (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) != 0;
     const bool heal_list = heal_from_density(h, flags);
     if (flags & MG_STEP_SURROGATE) {
@@ -657,7 +681,8 @@ int kernels_per_step(const mg_system* h, uint32_t flags) {
 }
 
 mg_status get_graph(mg_system* h, uint32_t flags, cudaGraphExec_t* out) {
-    uint64_t key = ((uint64_t)flags << 8) | ((uint64_t)h->cur << 1) | (uint64_t)h->conc_cur;
+    uint64_t key = ((uint64_t)flags << 8) | ((uint64_t)h->osp << 2) | ((uint64_t)h->cur << 1) |
+                   (uint64_t)h->conc_cur;
     auto it = h->graphs.find(key);
     int cur0 = h->cur, conc0 = h->conc_cur;
     if (it != h->graphs.end()) {
@@ -666,6 +691,7 @@ mg_status get_graph(mg_system* h, uint32_t flags, cudaGraphExec_t* out) {
         h->cur = 1 - cur0;
         h->conc_cur = 1 - conc0;
         if (flags & (MG_STEP_GENES | MG_STEP_SURROGATE)) h->conc_cur = conc0;
+        if (flags & STEP_REORIGIN) swap_ospace(h);
         return MG_OK;
     }
     DevParams saved = h->P;
@@ -701,7 +727,8 @@ bool host_pinned(const void* ptr) {
 // Graph of one step with its host exchange folded in (cached by flags, buffer state and the
 // exchange list: host addresses are part of the captured copies).
 mg_status get_io_graph(mg_system* h, uint32_t flags, const IoPlan& io, cudaGraphExec_t* out) {
-    std::string key = std::to_string(flags) + "/" + std::to_string(h->cur) + "/" + std::to_string(h->conc_cur);
+    std::string key = std::to_string(flags) + "/" + std::to_string(h->cur) + "/" + std::to_string(h->conc_cur) +
+                      "/" + std::to_string(h->osp);
     char buf[96];
     for (uint32_t k = 0; k < io.nin; k++) {
         std::snprintf(buf, sizeof buf, "/i%d:%p:%zu", io.in[k].buf_id, io.in[k].host, io.in[k].bytes);
@@ -795,18 +822,22 @@ mg_status run_steps(mg_system* h, uint32_t nsteps, uint32_t flags) {
                     "the surrogate step needs gene states 0 / INT_MAX without activation lists "
                     "(the network replaces the reaction and would skip the epigenetic countdowns)");
     for (uint32_t s = 0; s < nsteps; s++) {
+        const bool reo = h->reorigin_period && (h->reorigin_due || h->since_reorigin + 1 >= h->reorigin_period);
+        const uint32_t fs = flags | (reo ? STEP_REORIGIN : 0u);
         if (h->profile) {
             DevParams saved = h->P;
             if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
             prepare_step(h, flags);
-            enqueue_step(h, flags, true);
+            enqueue_step(h, fs, true);
             h->P = saved;
         } else {
             cudaGraphExec_t ge = nullptr;
-            mg_status st = get_graph(h, flags, &ge);
+            mg_status st = get_graph(h, fs, &ge);
             if (st != MG_OK) return st;
             MG_CUDA(h, cudaGraphLaunch(ge, h->stream));
         }
+        h->since_reorigin = reo ? 0u : h->since_reorigin + 1;
+        if (reo) h->reorigin_due = false;
         h->launches += (uint64_t)kernels_per_step(h, flags);
         if (flags & MG_STEP_PHYSICS) h->time = h->time + h->P.dt;
     }
@@ -1015,7 +1046,6 @@ static mg_status create_system(const mg_fparams* params, const mg_genome* genome
         plan.push_back({(void**)&c.pos, 16 * n});
         plan.push_back({(void**)&c.vel, 16 * n});
         plan.push_back({(void**)&c.veval, 16 * n});
-        plan.push_back({(void**)&c.bond, 32 * NB * n});
         plan.push_back({(void**)&c.pidx, 48 * n});
         plan.push_back({(void**)&c.conc, 64 * n});
         plan.push_back({(void**)&c.genes, 4 * n});
@@ -1026,12 +1056,17 @@ static mg_status create_system(const mg_fparams* params, const mg_genome* genome
         plan.push_back({(void**)&h->d_inst, sizeof(InstParams) * (size_t)n_inst});
         plan.push_back({(void**)&h->d_genomes, sizeof(DevGenome) * (size_t)n_inst});
     }
-    plan.push_back({(void**)&h->cold.age, 4 * n});
-    plan.push_back({(void**)&h->cold.color, 4 * n});
-    plan.push_back({(void**)&h->cold.pid, 4 * n});
-    plan.push_back({(void**)&h->cold.mass_radius, 4 * n});
-    plan.push_back({(void**)&h->cold.nerve, 4 * n});
-    plan.push_back({(void**)&h->cold.change, 4 * NB * n});
+    // the two origin spaces (cold fields and bond records; the carried sets share the current)
+    for (Cold* c : {&h->cold, &h->cold_alt}) {
+        plan.push_back({(void**)&c->bond, 32 * NB * n});
+        plan.push_back({(void**)&c->partner, 4 * NB * n});
+        plan.push_back({(void**)&c->age, 4 * n});
+        plan.push_back({(void**)&c->color, 4 * n});
+        plan.push_back({(void**)&c->pid, 4 * n});
+        plan.push_back({(void**)&c->mass_radius, 4 * n});
+        plan.push_back({(void**)&c->nerve, 4 * n});
+        plan.push_back({(void**)&c->change, 4 * NB * n});
+    }
     plan.push_back({(void**)&h->s.cell, 4 * n});
     plan.push_back({(void**)&h->s.arank, 4 * n});
     plan.push_back({(void**)&h->s.order, 4 * n});
@@ -1074,6 +1109,10 @@ static mg_status create_system(const mg_fparams* params, const mg_genome* genome
     for (auto& pr : plan) {
         *pr.first = base;
         base += align_up(pr.second);
+    }
+    for (Carried& c : h->set) {
+        c.bond = h->cold.bond;
+        c.partner = h->cold.partner;
     }
     cudaMemsetAsync(h->arena, 0, total, h->stream);
     launch_init_set(max_points, h->set[0], h->stream);
@@ -1347,7 +1386,10 @@ static mg_status enqueue_upload(mg_handle h, int32_t id, const void* host, size_
     Carried& c = h->set[h->cur];
     void* dst = nullptr;
     h->flist_valid = false;
-    if (id == MG_FPOS) h->drifted = true;  // positions no longer those the cells were built from
+    if (id == MG_FPOS) {
+        h->drifted = true;        // positions no longer those the cells were built from
+        h->reorigin_due = true;   // and the upload order is no guide to the sorted order
+    }
     switch (id) {
     case MG_FPOS: dst = c.pos; break;
     case MG_FVEL: dst = c.vel; break;
@@ -1769,6 +1811,10 @@ mg_status mg_set_option(mg_handle h, int32_t option, int32_t value) {
         if (value < 0 || value > 1) return fail(h, MG_ERR_INVALID_ARG, "FCONC layout is 0 or 1");
         h->conc_species_major = value;
         return MG_OK;
+    case MG_OPT_REORIGIN_PERIOD:
+        if (value < 0) return fail(h, MG_ERR_INVALID_ARG, "re-origin period is 0 (never) or more steps");
+        h->reorigin_period = (uint32_t)value;
+        return MG_OK;
     default:
         return fail(h, MG_ERR_INVALID_ARG, "unknown option " + std::to_string(option));
     }
@@ -2127,13 +2173,23 @@ mg_status mg_autotune(mg_handle h, uint32_t steps, uint32_t flags, int32_t* choi
         cudaGetLastError();
         return fail(h, MG_ERR_OOM, "mg_autotune: no room for a snapshot of the arena");
     }
-    struct Host { int cur, conc_cur, phase; bool ever_sorted, brk_pending, flist_valid; float time; uint64_t launches; };
-    const Host saved{h->cur, h->conc_cur, h->phase, h->ever_sorted, h->brk_pending, h->flist_valid, h->time, h->launches};
+    struct Host {
+        int cur, conc_cur, phase, osp;
+        bool ever_sorted, brk_pending, flist_valid, reorigin_due;
+        float time;
+        uint64_t launches;
+        uint32_t since_reorigin;
+    };
+    const Host saved{h->cur, h->conc_cur, h->phase, h->osp, h->ever_sorted, h->brk_pending, h->flist_valid,
+                     h->reorigin_due, h->time, h->launches, h->since_reorigin};
     const DevParams P0 = h->P;
     auto restore = [&]() -> cudaError_t {
         h->cur = saved.cur; h->conc_cur = saved.conc_cur; h->phase = saved.phase;
         h->ever_sorted = saved.ever_sorted; h->brk_pending = saved.brk_pending;
         h->flist_valid = saved.flist_valid; h->time = saved.time; h->launches = saved.launches;
+        if (h->osp != saved.osp) swap_ospace(h);
+        h->reorigin_due = saved.reorigin_due;
+        h->since_reorigin = saved.since_reorigin;
         return cudaMemcpyAsync(h->arena, snap, h->arena_bytes, cudaMemcpyDeviceToDevice, h->stream);
     };
     mg_status st = MG_OK;
@@ -2344,7 +2400,7 @@ static mg_status batch_graph(mg_batch b, uint32_t flags, cudaGraphExec_t* out) {
         b->epochs = epochs;
     }
     std::string key = std::to_string(flags) + ":";
-    for (mg_system* h : b->hs) key += (char)('0' + 2 * h->cur + h->conc_cur);
+    for (mg_system* h : b->hs) key += (char)('0' + 4 * h->osp + 2 * h->cur + h->conc_cur);
     auto it = b->graphs.find(key);
     if (it != b->graphs.end()) {
         for (mg_system* h : b->hs) advance_state(h, flags);

@@ -122,22 +122,31 @@ struct DevGenome {
     int uniform;          // all 16 diffusion rates equal and nonzero
 };
 
-// Bond records, per bond slot a two [cap] arrays of uint4: the A half (partner, rest length,
-// modulus, damping) and the B half (elastic limit, partner's particle id, strain^2
-// integrator, strain integrator).  The force pass rewrites the integrators every step; with
-// the halves in separate arrays its writes dirty the B sectors only.
-__host__ __device__ __forceinline__ size_t bond_ia(uint32_t cap, int a, uint32_t p) {
-    return (size_t)(2 * a) * cap + p;
+// Bond records are kept by particle origin (the slot a particle was uploaded to), not in sorted
+// order, so the sort does not move them: per bond slot two [cap] arrays of uint4, the A half
+// (-, rest length, modulus, damping) and the B half (elastic limit, partner's particle id,
+// strain^2 integrator, strain integrator), and one [cap] array of partners, each the partner's
+// current sorted index (the sort remaps it in place).  The force pass rewrites the integrators
+// every step; with the halves in separate arrays its writes dirty the B sectors only.
+// o: the particle's origin.
+__host__ __device__ __forceinline__ size_t bond_ia(uint32_t cap, int a, uint32_t o) {
+    return (size_t)(2 * a) * cap + o;
 }
-__host__ __device__ __forceinline__ size_t bond_ib(uint32_t cap, int a, uint32_t p) {
-    return (size_t)(2 * a + 1) * cap + p;
+__host__ __device__ __forceinline__ size_t bond_ib(uint32_t cap, int a, uint32_t o) {
+    return (size_t)(2 * a + 1) * cap + o;
+}
+__host__ __device__ __forceinline__ size_t bond_ip(uint32_t cap, int a, uint32_t o) {
+    return (size_t)a * cap + o;
 }
 
 struct Carried {
     float4* pos;
     float4* vel;
     float4* veval;
-    uint4* bond;  // [NB][2][cap]: per bond slot, the A halves then the B halves (bond_ia/bond_ib)
+    // bond records by origin (bond_ia / bond_ib / bond_ip), shared by both sets: the sort moves
+    // only the origins and remaps the partners in place
+    uint4* bond;        // [NB][2][cap]: per bond slot, the A halves then the B halves
+    uint32_t* partner;  // [NB][cap]: the partner's sorted index (NO_PARTNER: none)
     uint32_t* pidx;
     float* conc;
     uint32_t* genes;
@@ -146,6 +155,8 @@ struct Carried {
     uint32_t* iid;  // packed instances: the particle's instance (UNDEF for parked slots), else null
 };
 
+// Everything kept by origin: the cold fields and the bond records (the carried sets' bond and
+// partner pointers are this space's).
 struct Cold {
     uint32_t* age;
     uint32_t* color;
@@ -153,6 +164,8 @@ struct Cold {
     uint32_t* mass_radius;
     uint32_t* nerve;
     uint32_t* change;  // [cap][NB]
+    uint4* bond;        // [NB][2][cap] (bond_ia / bond_ib)
+    uint32_t* partner;  // [NB][cap] (bond_ip)
 };
 
 struct Scratch {
@@ -209,10 +222,12 @@ void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, bool sub
                      cudaStream_t st);
 // parts of the carried state a gather moves (the three make the whole state): positions,
 // bonds, genes, origins and cells; concentrations; velocities and the incoming-bond table
-enum : int { GATHER_CORE = 1, GATHER_CONC = 2, GATHER_MOTION = 4, GATHER_ALL = 7 };
+// GATHER_REORIGIN (with GATHER_CORE): the particles' origins become their sorted indices,
+// their cold fields and bond records move from space `cs` to space `cd` accordingly.
+enum : int { GATHER_CORE = 1, GATHER_CONC = 2, GATHER_MOTION = 4, GATHER_ALL = 7, GATHER_REORIGIN = 8 };
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st,
-                   int parts = GATHER_ALL);
+                   int parts = GATHER_ALL, const Cold* cs = nullptr, const Cold* cd = nullptr);
 // flags: 1 density/pressure, 2 diffusion, 4 gene reaction
 // flags: 1 density, 2 diffusion, 4 gene reaction, 8 surrogate features, 16 capture of
 // training pairs, 32 judge (plain update of sampled / handed-over particles into conc_plain).

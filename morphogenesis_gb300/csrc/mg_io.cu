@@ -10,21 +10,26 @@ constexpr uint32_t EPIGEN_ACTIVE = 2147483647u;
 static inline uint32_t blocks_for(size_t n) { return (uint32_t)((n + 255) / 256); }
 
 // FELASTIDX word order: [0]partner [1]elastlim [2]restlen [3]modulus [4]damping [5]pid
-// [6]strain^2 integrator [7]strain integrator [8]change type (fluid.h:73, 155).
+// [6]strain^2 integrator [7]strain integrator [8]change type (fluid.h:73, 155).  The records
+// live at the particle's origin; a slot without one (a particle dropped from the grid) keeps
+// nothing, like the cold fields, and reads back as no bond.
 __global__ void k_import_bonds(uint32_t cap, const uint32_t* __restrict__ ref,
-                               uint4* __restrict__ bond, const uint32_t* __restrict__ origin,
-                               uint32_t* __restrict__ change) {
+                               uint4* __restrict__ bond, uint32_t* __restrict__ partner,
+                               const uint32_t* __restrict__ origin, uint32_t* __restrict__ change) {
     size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= (size_t)cap * NB) return;
     uint32_t p = (uint32_t)(k / NB), a = (uint32_t)(k % NB);
     const uint32_t* w = ref + k * 9;
-    bond[bond_ia(cap, (int)a, p)] = make_uint4(w[0], w[2], w[3], w[4]);
-    bond[bond_ib(cap, (int)a, p)] = make_uint4(w[1], w[5], w[6], w[7]);
-    uint32_t o = origin[p];
-    if (o != UNDEF) change[(size_t)o * NB + a] = w[8];
+    const uint32_t o = origin[p];
+    if (o == UNDEF) return;
+    bond[bond_ia(cap, (int)a, o)] = make_uint4(0u, w[2], w[3], w[4]);
+    bond[bond_ib(cap, (int)a, o)] = make_uint4(w[1], w[5], w[6], w[7]);
+    partner[bond_ip(cap, (int)a, o)] = w[0];
+    change[(size_t)o * NB + a] = w[8];
 }
 
 __global__ void k_export_bonds(uint32_t cap, const uint4* __restrict__ bond,
+                               const uint32_t* __restrict__ partner,
                                const uint32_t* __restrict__ origin,
                                const uint32_t* __restrict__ change,
                                const uint32_t* __restrict__ brk, int apply_breaks,
@@ -32,25 +37,30 @@ __global__ void k_export_bonds(uint32_t cap, const uint4* __restrict__ bond,
     size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= (size_t)cap * NB) return;
     uint32_t p = (uint32_t)(k / NB), a = (uint32_t)(k % NB);
-    uint4 A = bond[bond_ia(cap, (int)a, p)], B = bond[bond_ib(cap, (int)a, p)];
+    const uint32_t o = origin[p];
+    uint4 A = make_uint4(NO_PARTNER, 0u, 0u, 0u), B = make_uint4(0u, NO_PARTNER, 0u, 0u);
+    if (o != UNDEF) {  // else a parked slot: no bond
+        A = bond[bond_ia(cap, (int)a, o)];
+        B = bond[bond_ib(cap, (int)a, o)];
+        A.x = partner[bond_ip(cap, (int)a, o)];
+    }
     if (apply_breaks && p < *nactive_p && (brk[p] >> a) & 1u) A.y = 0u;
     uint32_t* w = ref + k * 9;
     w[0] = A.x; w[1] = B.x; w[2] = A.y; w[3] = A.z; w[4] = A.w;
     w[5] = B.y; w[6] = B.z; w[7] = B.w;
-    uint32_t o = origin[p];
     w[8] = o != UNDEF ? change[(size_t)o * NB + a] : 0u;
 }
 
 void launch_import_bonds(const DevParams& P, const uint32_t* ref, const Carried& cur,
                          const Cold& cold, cudaStream_t st) {
     size_t n = (size_t)P.cap * NB;
-    k_import_bonds<<<blocks_for(n), 256, 0, st>>>(P.cap, ref, cur.bond, cur.origin, cold.change);
+    k_import_bonds<<<blocks_for(n), 256, 0, st>>>(P.cap, ref, cur.bond, cur.partner, cur.origin, cold.change);
 }
 
 void launch_export_bonds(const DevParams& P, const Carried& cur, const Cold& cold,
                          const Scratch& s, bool apply_breaks, uint32_t* ref, cudaStream_t st) {
     size_t n = (size_t)P.cap * NB;
-    k_export_bonds<<<blocks_for(n), 256, 0, st>>>(P.cap, cur.bond, cur.origin, cold.change, s.brk,
+    k_export_bonds<<<blocks_for(n), 256, 0, st>>>(P.cap, cur.bond, cur.partner, cur.origin, cold.change, s.brk,
                                                    apply_breaks ? 1 : 0, s.counters + 3, ref);
 }
 
@@ -283,20 +293,21 @@ void launch_gene_lists(const DevParams& P, const Carried& cur, const Scratch& s,
 namespace mg {
 
 // Fresh carried set: no bonds, no incoming bonds, identity origin.
-__global__ void k_init_set(uint32_t cap, uint4* __restrict__ bond, uint32_t* __restrict__ pidx,
-                           uint32_t* __restrict__ origin) {
+__global__ void k_init_set(uint32_t cap, uint4* __restrict__ bond, uint32_t* __restrict__ partner,
+                           uint32_t* __restrict__ pidx, uint32_t* __restrict__ origin) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= cap) return;
-    for (int a = 0; a < NB; a++) {
-        bond[bond_ia(cap, a, p)] = make_uint4(NO_PARTNER, 0u, 0u, 0u);
+    for (int a = 0; a < NB; a++) {  // slot p is origin p
+        bond[bond_ia(cap, a, p)] = make_uint4(0u, 0u, 0u, 0u);
         bond[bond_ib(cap, a, p)] = make_uint4(0u, NO_PARTNER, 0u, 0u);
+        partner[bond_ip(cap, a, p)] = NO_PARTNER;
     }
     for (int k = 0; k < 12; k++) pidx[(size_t)p * 12 + k] = NO_PARTNER;
     origin[p] = p;
 }
 
 void launch_init_set(uint32_t cap, const Carried& c, cudaStream_t st) {
-    k_init_set<<<blocks_for(cap), 256, 0, st>>>(cap, c.bond, c.pidx, c.origin);
+    k_init_set<<<blocks_for(cap), 256, 0, st>>>(cap, c.bond, c.partner, c.pidx, c.origin);
 }
 
 }  // namespace mg

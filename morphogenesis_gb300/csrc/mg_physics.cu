@@ -1140,14 +1140,19 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force(DevParams P, Car
     if (p >= nact) return;
     const uint32_t cap = P.cap;
     const float4 ip = C.pos[p], iv = C.veval[p];
+    // the bond records' slot; a particle without an origin (a slot that was parked and given a
+    // position again by an upload) has no bonds
+    const uint32_t o0 = C.origin[p];
+    const bool has_rec = o0 != UNDEF;
+    const uint32_t o = has_rec ? o0 : 0u;
     float fx = 0.f, fy = 0.f, fz = 0.f;
     uint32_t br = 0;
     // own (outgoing) bonds
 #pragma unroll
     for (int a = 0; a < NB; a++) {
-        uint4* recb = C.bond + bond_ib(cap, a, p);
-        const uint4 A = C.bond[bond_ia(cap, a, p)], B = *recb;
-        const uint32_t j = A.x;
+        uint4* recb = C.bond + bond_ib(cap, a, o);
+        const uint4 A = C.bond[bond_ia(cap, a, o)], B = *recb;
+        const uint32_t j = has_rec ? C.partner[bond_ip(cap, a, o)] : NO_PARTNER;
         const float restlen = __uint_as_float(A.y);
         if (j >= nact || restlen < REST_MIN) {
             bterm[(size_t)a * cap + p] = make_float4(0.f, 0.f, 0.f, __uint_as_float(UNDEF));
@@ -1275,24 +1280,26 @@ void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool
 // Broken bonds get rest length 0 (cuda:3315-3317).  The force kernel records the breaks in
 // brk[] instead of writing the rest length, because other threads of the same kernel read
 // that rest length for their incoming-bond reactions.
-__device__ __forceinline__ void apply_breaks(uint4* bond, uint32_t cap, uint32_t p, uint32_t br) {
+// Rest length 0 on the bonds that broke (o: the particle's origin, where its records live).
+__device__ __forceinline__ void apply_breaks(uint4* bond, uint32_t cap, uint32_t o, uint32_t br) {
 #pragma unroll
     for (int a = 0; a < NB; a++)
-        if (br & (1u << a)) reinterpret_cast<uint32_t*>(bond + bond_ia(cap, a, p))[1] = 0u;
+        if (br & (1u << a)) reinterpret_cast<uint32_t*>(bond + bond_ia(cap, a, o))[1] = 0u;
 }
 
 __global__ void __launch_bounds__(256) k_apply_breaks(uint32_t cap, uint4* __restrict__ bond,
+                                                      const uint32_t* __restrict__ origin,
                                                       const uint32_t* __restrict__ brk,
                                                       const uint32_t* __restrict__ nactive_p) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= *nactive_p) return;
-    const uint32_t br = brk[p];
-    if (br) apply_breaks(bond, cap, p, br);
+    const uint32_t br = brk[p], o = origin[p];
+    if (br && o != UNDEF) apply_breaks(bond, cap, o, br);
 }
 
 void launch_apply_breaks(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
-    k_apply_breaks<<<blocks, 256, 0, st>>>(P.cap, cur.bond, s.brk, s.counters + 3);
+    k_apply_breaks<<<blocks, 256, 0, st>>>(P.cap, cur.bond, cur.origin, s.brk, s.counters + 3);
 }
 
 // ---- advance -----------------------------------------------------------------------------
@@ -1391,7 +1398,7 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_advance(DevParams P, C
     // fixedParticles (cuda:3694-3705, after the actuation): the previous state is kept
     if (APPLY_BRK) {
         const uint32_t br = brk[p];
-        if (br) apply_breaks(C.bond, P.cap, p, br);
+        if (br && C.origin[p] != UNDEF) apply_breaks(C.bond, P.cap, C.origin[p], br);
     }
 }
 

@@ -50,21 +50,24 @@ __device__ __forceinline__ bool rest_is_small(uint32_t rest_bits) {
     return __uint_as_float(rest_bits) < __int_as_float(0x30897060);
 }
 
-__device__ __forceinline__ uint4 bond_a(const uint4* bond, uint32_t cap, uint32_t p, int a) {
-    return bond[bond_ia(cap, a, p)];
+// Rest length bits and partner of bond slot a of the particle with origin o (its records'
+// slot).
+__device__ __forceinline__ uint32_t bond_rest(const uint4* bond, uint32_t cap, uint32_t o, int a) {
+    return reinterpret_cast<const uint32_t*>(bond + bond_ia(cap, a, o))[1];
 }
 
-__device__ __forceinline__ int heal_slot(const uint4* bond, uint32_t cap, uint32_t p, uint32_t nact,
-                                         const uint32_t* origin, const uint32_t* change,
-                                         bool from_changes) {
-    const uint32_t o = from_changes ? origin[p] : UNDEF;
+__device__ __forceinline__ int heal_slot(const uint4* bond, const uint32_t* partner, uint32_t cap,
+                                         uint32_t p, uint32_t nact, const uint32_t* origin,
+                                         const uint32_t* change, bool from_changes) {
+    const uint32_t o = origin[p];
+    if (o == UNDEF) return -1;
 #pragma unroll
     for (int a = 0; a < NB; a++) {
-        const uint4 A = bond_a(bond, cap, p, a);
+        const uint32_t rest = bond_rest(bond, cap, o, a), j = partner[bond_ip(cap, a, o)];
         if (from_changes) {
-            const uint32_t w = o != UNDEF ? change[(size_t)o * NB + a] : 0u;
-            if ((w & 1u) && (__uint_as_float(A.y) == 0.f || A.x >= nact)) return a;
-        } else if (A.x < nact && rest_is_small(A.y)) {
+            const uint32_t w = change[(size_t)o * NB + a];
+            if ((w & 1u) && (__uint_as_float(rest) == 0.f || j >= nact)) return a;
+        } else if (j < nact && rest_is_small(rest)) {
             return a;
         }
     }
@@ -129,10 +132,11 @@ __global__ void __launch_bounds__(256) k_bond_changes(DevParams P, const DevGeno
         bone = (bits >> 9) & 1u;
         fibre = ((bits >> 6) & 1u) || ((bits >> 7) & 1u) || ((bits >> 10) & 1u);
     }
-    const uint32_t o = C.origin[p];
+    const uint32_t o = C.origin[p];  // the bond records' slot
+    if (o == UNDEF) return;
     for (int b = 0; b < NB; b++) {
         const int type = bone && b < 4 ? 2 : (fibre && b == 0 ? 1 : 0);
-        const size_t ra = bond_ia(cap, b, p), rb = bond_ib(cap, b, p);
+        const size_t ra = bond_ia((uint32_t)cap, b, o), rb = bond_ib((uint32_t)cap, b, o);
         uint4 A = C.bond[ra];
         float rest = __uint_as_float(A.y);
         if (rest > 0.f) {
@@ -148,8 +152,8 @@ __global__ void __launch_bounds__(256) k_bond_changes(DevParams P, const DevGeno
             C.bond[ra] = A;
             C.bond[rb] = B;
         }
-        const bool heal = rest == 0.f || A.x >= n;
-        if (o != UNDEF) change_cold[(size_t)o * NB + b] = heal ? 1u : 0u;
+        const bool heal = rest == 0.f || C.partner[bond_ip((uint32_t)cap, b, o)] >= n;
+        change_cold[(size_t)o * NB + b] = heal ? 1u : 0u;
         if (heal) break;
     }
 }
@@ -219,6 +223,7 @@ __global__ void __launch_bounds__(256) k_change_lists(uint32_t cap, uint32_t cel
 }
 
 __global__ void __launch_bounds__(256) k_free_slots(uint32_t cap, const uint4* __restrict__ bond,
+                                                    const uint32_t* __restrict__ partner,
                                                     const uint32_t* __restrict__ pidx,
                                                     const uint32_t* __restrict__ origin,
                                                     const uint32_t* __restrict__ pid_cold,
@@ -238,8 +243,9 @@ __global__ void __launch_bounds__(256) k_free_slots(uint32_t cap, const uint4* _
         const uint32_t k = pidx[(size_t)j * 12 + 2 * s], bk = pidx[(size_t)j * 12 + 2 * s + 1];
         bool live = false;
         if (k < n && bk < (uint32_t)NB) {
-            const uint4 A = bond_a(bond, cap, k, (int)bk);
-            live = A.x == j && !rest_is_small(A.y);
+            const uint32_t ok = origin[k];
+            live = ok != UNDEF && partner[bond_ip(cap, (int)bk, ok)] == j &&
+                   !rest_is_small(bond_rest(bond, cap, ok, (int)bk));
         }
         if (!live) m |= 1u << s;
     }
@@ -257,7 +263,8 @@ __global__ void __launch_bounds__(256) k_free_slots(uint32_t cap, const uint4* _
 constexpr int PROPOSE_WARPS = 8;
 __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
     DevParams P, const float4* __restrict__ pos, const uint4* __restrict__ bond,
-    const uint32_t* __restrict__ origin, const uint32_t* __restrict__ pid_cold,
+    const uint32_t* __restrict__ partner, const uint32_t* __restrict__ origin,
+    const uint32_t* __restrict__ pid_cold,
     const uint32_t* __restrict__ scell, const uint32_t* __restrict__ count,
     const uint32_t* __restrict__ offset, const uint8_t* __restrict__ freemask,
     const uint32_t* __restrict__ nactive_p, const uint32_t* __restrict__ change, bool from_changes,
@@ -276,11 +283,12 @@ __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
         prop[i] = UNDEF;
         propd[i] = 0.f;
     }
-    const bool wants = act && heal_slot(bond, cap, i, n, origin, change, from_changes) >= 0;
+    const bool wants = act && heal_slot(bond, partner, cap, i, n, origin, change, from_changes) >= 0;
     if (!__any_sync(0xffffffffu, wants)) return;
     uint32_t partners[NB];
+    const uint32_t oi = wants ? origin[i] : UNDEF;
 #pragma unroll
-    for (int a = 0; a < NB; a++) partners[a] = wants ? bond_a(bond, cap, i, a).x : UNDEF;
+    for (int a = 0; a < NB; a++) partners[a] = wants ? partner[bond_ip(cap, a, oi)] : UNDEF;
     const float INF = __int_as_float(0x7f800000);
     const float4 ip = wants ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     float best = 0.f;
@@ -401,6 +409,7 @@ __global__ void __launch_bounds__(PROPOSE_WARPS * 32) k_propose_warp(
 
 __global__ void __launch_bounds__(256) k_accept(DevParams P, const DevGenome* __restrict__ G,
                                                 uint4* __restrict__ bond,
+                                                uint32_t* __restrict__ partner,
                                                 uint32_t* __restrict__ pidx,
                                                 const uint32_t* __restrict__ origin,
                                                 const uint32_t* __restrict__ pid_cold,
@@ -453,23 +462,24 @@ __global__ void __launch_bounds__(256) k_accept(DevParams P, const DevGenome* __
             else r--;
         }
     if (slot < 0) return;  // no free incoming slot left for this proposal: retry next step
-    const int b = heal_slot(bond, cap, i, n, origin, change_cold, from_changes);
+    const int b = heal_slot(bond, partner, cap, i, n, origin, change_cold, from_changes);
     if (b < 0) return;
-    const size_t ra = bond_ia(cap, b, i), rb = bond_ib(cap, b, i);
+    const uint32_t oi = origin[i];  // i's bond records' slot (valid: heal_slot found one)
+    const size_t ra = bond_ia(cap, b, oi), rb = bond_ib(cap, b, oi);
     const uint4 A = bond[ra];
     const uint32_t oj = origin[j];
     const uint32_t pj = oj != UNDEF ? pid_cold[oj] : UNDEF;
     if (P.heal_params) {  // makeBond(i, j, b, slot, elastin) (cuda:1573-1593)
         const float* E = G->bparam[0];
-        bond[ra] = make_uint4(j, __float_as_uint(E[9]), __float_as_uint(E[10]), __float_as_uint(E[11]));
+        bond[ra] = make_uint4(0u, __float_as_uint(E[9]), __float_as_uint(E[10]), __float_as_uint(E[11]));
         bond[rb] = make_uint4(__float_as_uint(E[8]), pj, 0u, 0u);
     } else {
         const float rest = sqrtf(d);
-        bond[ra] = make_uint4(j, __float_as_uint(rest), A.z, A.w);
+        bond[ra] = make_uint4(0u, __float_as_uint(rest), A.z, A.w);
         bond[rb] = make_uint4(__float_as_uint(1.5f * rest), pj, 0u, 0u);
     }
-    const uint32_t oi = origin[i];
-    if (oi != UNDEF) change_cold[(size_t)oi * NB + b] = 0u;
+    partner[bond_ip(cap, b, oi)] = j;
+    change_cold[(size_t)oi * NB + b] = 0u;
     pidx[(size_t)j * 12 + 2 * slot] = i;
     pidx[(size_t)j * 12 + 2 * slot + 1] = (uint32_t)b;
 }
@@ -480,15 +490,15 @@ void launch_remodel(const DevParams& P, const DevGenome* G, const Carried& cur, 
                     const Scratch& s, bool from_changes, bool prune, const uint32_t* hcount,
                     const uint32_t* hlist, cudaStream_t st) {
     const uint32_t blocks = (P.cap + 255) / 256;
-    k_free_slots<<<blocks, 256, 0, st>>>(P.cap, cur.bond, cur.pidx, cur.origin, cold.pid, s.counters + 3,
+    k_free_slots<<<blocks, 256, 0, st>>>(P.cap, cur.bond, cur.partner, cur.pidx, cur.origin, cold.pid, s.counters + 3,
                                          s.freemask);
     cudaMemsetAsync(s.prop_cnt, 0, sizeof(uint32_t) * P.cap, st);
     const uint32_t wblocks = (P.cap + PROPOSE_WARPS * 32 - 1) / (PROPOSE_WARPS * 32);
     k_propose_warp<<<wblocks, PROPOSE_WARPS * 32, 0, st>>>(
-        P, cur.pos, cur.bond, cur.origin, cold.pid, s.scell, s.count, s.offset, s.freemask,
+        P, cur.pos, cur.bond, cur.partner, cur.origin, cold.pid, s.scell, s.count, s.offset, s.freemask,
         s.counters + 3, cold.change, from_changes, s.work, prune, hcount, hlist, s.prop, s.propd,
         s.prop_cnt, s.prop_list);
-    k_accept<<<blocks, 256, 0, st>>>(P, G, cur.bond, cur.pidx, cur.origin, cold.pid, cold.change,
+    k_accept<<<blocks, 256, 0, st>>>(P, G, cur.bond, cur.partner, cur.pidx, cur.origin, cold.pid, cold.change,
                                      s.scell, s.count, s.offset, s.freemask, s.prop, s.propd,
                                      s.counters + 3, from_changes, s.prop_cnt, s.prop_list);
 }

@@ -15,9 +15,10 @@
 //              cells <= 256 particles; block tier <= 8192, ordered stream compaction above),
 //              which yields sorted[] (sorted -> old) and newidx[] (old -> sorted), and the
 //              density pass's processing order work[];
-//   gather   : every carried field is gathered through sorted[], bond partners and incoming
-//              bond owners are remapped through newidx[] (in up to three kernels when parts
-//              of the state are still being uploaded).
+//   gather   : every carried field is gathered through sorted[]; the bond records stay at the
+//              particles' origins, their partners and the incoming-bond owners are remapped
+//              through newidx[] (in up to three kernels when parts of the state are still
+//              being uploaded).
 #include <cuda/atomic>
 #include <cfloat>
 #include "mg_internal.cuh"
@@ -461,25 +462,27 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
                                                 float* __restrict__ invdens,
                                                 float4* __restrict__ force,
                                                 const uint32_t* __restrict__ nactive_p,
-                                                int parts) {
-    // parts: GATHER_CORE (positions, bonds, genes, origins, cells; the scratch of parked slots),
-    // GATHER_CONC (concentrations), GATHER_MOTION (velocities, incoming-bond table)
+                                                int parts, Cold cs, Cold cd) {
+    // parts: GATHER_CORE (positions, genes, origins, cells, the bond partners; the scratch of
+    // parked slots), GATHER_CONC (concentrations), GATHER_MOTION (velocities, incoming-bond
+    // table).  The bond records stay at their origins; only their partners change, to this
+    // sort's indices, in place.
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t cap = P.cap;
     if (p >= cap) return;
+    if ((parts & GATHER_CORE) && !(parts & GATHER_REORIGIN)) {
+#pragma unroll
+        for (int a = 0; a < NB; a++) {  // slot p read as an origin
+            uint32_t* q = D.partner + bond_ip(cap, a, p);
+            *q = remap(*q, cap, newidx);
+        }
+    }
     const uint32_t nact = *nactive_p;
     if (p < nact) {
         const uint32_t i = sorted[p];
         if (parts & GATHER_CORE) {
             D.pos[p] = __ldg(S.pos + i);
-#pragma unroll
-            for (int a = 0; a < NB; a++) {
-                uint4 A = __ldg(S.bond + bond_ia(cap, a, i));
-                const uint4 B = __ldg(S.bond + bond_ib(cap, a, i));
-                A.x = remap(A.x, cap, newidx);
-                D.bond[bond_ia(cap, a, p)] = A;
-                D.bond[bond_ib(cap, a, p)] = B;
-            }
+
             if (P.full_epi) {
                 // per-gene words move with the particle; the bits (dense-list membership at sort
                 // time, FEPIGEN > 0) are taken from them
@@ -494,7 +497,28 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
             } else {
                 D.genes[p] = __ldg(S.genes + i);
             }
-            D.origin[p] = __ldg(S.origin + i);
+            const uint32_t o = __ldg(S.origin + i);
+            if (parts & GATHER_REORIGIN) {
+                // the particle's records move to slot p of the other space, and p becomes its
+                // origin (a particle without records keeps none)
+                if (o != UNDEF) {
+                    cd.age[p] = __ldg(cs.age + o);
+                    cd.color[p] = __ldg(cs.color + o);
+                    cd.pid[p] = __ldg(cs.pid + o);
+                    cd.mass_radius[p] = __ldg(cs.mass_radius + o);
+                    cd.nerve[p] = __ldg(cs.nerve + o);
+#pragma unroll
+                    for (int a = 0; a < NB; a++) {
+                        cd.change[(size_t)p * NB + a] = __ldg(cs.change + (size_t)o * NB + a);
+                        cd.bond[bond_ia(cap, a, p)] = __ldg(cs.bond + bond_ia(cap, a, o));
+                        cd.bond[bond_ib(cap, a, p)] = __ldg(cs.bond + bond_ib(cap, a, o));
+                        cd.partner[bond_ip(cap, a, p)] = remap(__ldg(cs.partner + bond_ip(cap, a, o)), cap, newidx);
+                    }
+                }
+                D.origin[p] = o != UNDEF ? p : UNDEF;
+            } else {
+                D.origin[p] = o;
+            }
             if (S.iid) D.iid[p] = __ldg(S.iid + i);
             scell[p] = __ldg(cell + i);
         }
@@ -516,11 +540,7 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
         // parked null particle (out-of-grid parking of advanceParticles, cuda:3474-3477)
         if (parts & GATHER_CORE) {
             D.pos[p] = make_float4(P.bmin[0], P.bmin[1], P.null_z, 0.0f);
-#pragma unroll
-            for (int a = 0; a < NB; a++) {
-                D.bond[bond_ia(cap, a, p)] = make_uint4(NO_PARTNER, 0u, 0u, 0u);
-                D.bond[bond_ib(cap, a, p)] = make_uint4(0u, NO_PARTNER, 0u, 0u);
-            }
+
             D.genes[p] = 0u;
             if (P.full_epi)
                 for (int g = 0; g < NG; g++) D.epi[(size_t)g * cap + p] = 0u;
@@ -548,10 +568,12 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
 
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st,
-                   int parts) {
+                   int parts, const Cold* cs, const Cold* cd) {
     const uint32_t nt = (uint32_t)P.gather_threads, blocks = (P.cap + nt - 1) / nt;
+    if ((parts & GATHER_REORIGIN) && (!cs || !cd || !(parts & GATHER_CORE))) parts &= ~GATHER_REORIGIN;
     k_gather<<<blocks, nt, 0, st>>>(P, src, src_conc, dst, dst_conc, s.sorted, s.newidx, s.cell,
-                                      s.scell, s.press, s.invdens, s.force, s.counters + 3, parts);
+                                      s.scell, s.press, s.invdens, s.force, s.counters + 3, parts,
+                                      cs ? *cs : Cold{}, cd ? *cd : Cold{});
 }
 
 }  // namespace mg

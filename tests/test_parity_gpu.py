@@ -470,6 +470,18 @@ def test_launch_shapes_give_identical_results(built):
         for b, w in want.items():
             assert np.array_equal(fs.download(b).view(np.uint32), w), f"shape {shape} buffer {b}"
         fs.close()
+    # re-origin periods (bond records and cold fields renumbered to the sorted order): never,
+    # every step, every third step
+    for period in (0, 1, 3):
+        fs = mg.FluidSystem(d.params, d.genome, d.n)
+        fs.TransferToCL(d.arrays)
+        fs.set_option(A.OPT_REORIGIN_PERIOD, period)
+        fs.Run(30)
+        for b, w in want.items():
+            assert np.array_equal(fs.download(b).view(np.uint32), w), f"re-origin period {period} buffer {b}"
+        for b in (A.FAGE, A.FCOLOR, A.FPARTICLE_ID, A.FMASS_RADIUS, A.FNERVEIDX):
+            assert np.array_equal(fs.download(b), ref.download(b)), f"re-origin period {period} buffer {b}"
+        fs.close()
     # block sizes of the force, gather and advance passes
     for threads in ((128, 512, 128), (512, 128, 512)):
         fs = mg.FluidSystem(d.params, d.genome, d.n)
