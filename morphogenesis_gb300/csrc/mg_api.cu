@@ -698,15 +698,28 @@ mg_status get_graph(mg_system* h, uint32_t flags, cudaGraphExec_t* out) {
     if (flags & MG_STEP_FREEZE) h->P.freeze = 1;
     cudaGraph_t g = nullptr;
     prepare_step(h, flags);
+    const int osp0 = h->osp;
+    // a step that is not launched leaves the buffer state where it was
+    auto unwind = [&]() {
+        h->cur = cur0;
+        h->conc_cur = conc0;
+        if (h->osp != osp0) swap_ospace(h);
+    };
     MG_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     enqueue_step(h, flags, false);
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     h->P = saved;
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+    if (e != cudaSuccess) {
+        unwind();
+        return cuda_fail(h, e, "cudaStreamEndCapture");
+    }
     cudaGraphExec_t ge = nullptr;
     e = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    if (e != cudaSuccess) {
+        unwind();
+        return cuda_fail(h, e, "cudaGraphInstantiate");
+    }
     h->graphs[key] = ge;
     *out = ge;
     return MG_OK;
