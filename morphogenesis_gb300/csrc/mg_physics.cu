@@ -181,6 +181,20 @@ struct DF {
                           CAPTURE = FLAGS & 16, JUDGE = FLAGS & 32, MEAN = FEAT || CAPTURE;
 };
 
+// Slots past the active particles (parked: dropped from the grid) keep their concentrations
+// through the morphogen stage, which writes the other buffer: their rows are copied across
+// (the reference's per-particle loops skip them and leave them as they are).
+template <int FLAGS>
+__device__ __forceinline__ void park_conc(const float* conc_in, float* conc_out, uint32_t k,
+                                          uint32_t nact, uint32_t cap) {
+    using F = DF<FLAGS>;
+    if ((F::DIFF || F::GENE || F::MEAN) && k >= nact && k < cap) {
+        float v[NTF];
+        load_row16(conc_in + (size_t)k * NTF, v);
+        store_row16(conc_out + (size_t)k * NTF, v);
+    }
+}
+
 __device__ __forceinline__ bool judged_lane(const DensExtra& X, uint32_t p, uint32_t gene_word) {
     if ((gene_word >> 31) & 1u) return true;  // handed to the plain method for good
     if (!X.judge_period || !X.judge_stride) return false;
@@ -409,7 +423,10 @@ __global__ void __launch_bounds__(256) k_dens(DevParams P, const DevGenome* __re
                                               const uint32_t* __restrict__ nactive_p, DensExtra X) {
     using F = DF<FLAGS>;
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= *nactive_p) return;
+    if (p >= *nactive_p) {
+        park_conc<FLAGS>(conc_in, conc_out, p, *nactive_p, P.cap);
+        return;
+    }
     float cur[NTF], nc[NTF], ms[NTF];
     load_conc<FLAGS>(G, conc_in, p, cur);
     const float* dif = G->diff;  // the species' rates, read from the genome where used
@@ -516,6 +533,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     // particles of one compact sub-region of a cell; results go to the particle's sorted slot.
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = k < *nactive_p;
+    if (!act) park_conc<FLAGS>(conc_in, conc_out, k, *nactive_p, P.cap);
     if (!__any_sync(0xffffffffu, act)) return;
     const uint32_t p = act ? work[k] : 0u;
 
@@ -699,7 +717,10 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_fi
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     uint32_t* my = s_list + (size_t)w * NL_CAP * 32 + lane;
     const uint32_t k0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k0 >= *nactive_p) return;
+    if (k0 >= *nactive_p) {
+        park_conc<FLAGS>(conc_in, conc_out, k0, *nactive_p, P.cap);
+        return;
+    }
     const uint32_t p = work[k0];
     const float4 ip = pos[p];
     float R2 = 1.f;

@@ -179,6 +179,26 @@ def test_edge_empty_ragged_and_dropped(built):
     g, o = pair(d, d.n)
     g.Run(2); o.step(2)
     compare(g, o)
+    # parked slots given in-grid positions again by an upload of FPOS come back without bonds
+    # (their records were dropped with them) and step identically; every re-origin period
+    d = demo.make_block(6, "R", seed=7)
+    d.arrays[A.FPOS][::7, 0] = -1e4
+    g, o = pair(d, d.n)
+    g.Run(2); o.step(2)
+    nact = g.counts()[0]
+    assert nact < d.n
+    back = g.download(A.FPOS)
+    live = back[:nact, :3]
+    back[nact:, :3] = live[: d.n - nact] + np.float32(0.37)
+    for period in (0, 1, 64):
+        g2, o2 = pair(d, d.n)
+        g2.set_option(A.OPT_REORIGIN_PERIOD, period)
+        g2.Run(2); o2.step(2)
+        g2.upload(A.FPOS, back); o2.upload(A.FPOS, back)
+        g2.Run(3); o2.step(3)
+        assert g2.counts()[0] == o2.counts()[0] > nact
+        compare(g2, o2)
+        g2.close(); o2.close()
 
 
 @pytest.mark.parametrize("count", [300, 9000])
