@@ -447,13 +447,15 @@ void swap_ospace(mg_system* h) {
 // later (uploads still in flight).  The rest is moved first, the concentrations after the
 // stream has waited for conc_ready; the motion part is left to flush_motion, which the step
 // calls before its force pass (nothing before it reads those fields).
+// scratch: the step does not compute pressure, density and forces again after this sort, so
+// the sort moves the first two and zeroes the forces as countingSortFull does.
 void enqueue_gather(mg_system* h, bool prof, cudaEvent_t conc_ready = nullptr,
-                    cudaEvent_t motion_ready = nullptr, bool reorigin = false) {
+                    cudaEvent_t motion_ready = nullptr, bool reorigin = false, bool scratch = true) {
     int src = h->cur, dst = 1 - h->cur;
     int csrc = h->conc_cur, cdst = 1 - h->conc_cur;
     { Mark m(h, prof, "gather");
       const int first = GATHER_CORE | (conc_ready ? 0 : GATHER_CONC) | (motion_ready ? 0 : GATHER_MOTION) |
-                        (reorigin ? GATHER_REORIGIN : 0);
+                        (reorigin ? GATHER_REORIGIN : 0) | (scratch ? GATHER_SCRATCH : 0);
       launch_gather(h->P, h->set[src], conc_of(h, csrc), h->set[dst], conc_of(h, cdst), h->s, h->stream, first,
                     &h->cold, &h->cold_alt);
       if (reorigin) swap_ospace(h);
@@ -505,8 +507,8 @@ void* direct_buffer(mg_system* h, int32_t id, bool upload) {
     case MG_FVEL: return c.vel;
     case MG_FVEVAL: return c.veval;
     case MG_FFORCE: return h->s.force;
-    case MG_FPRESS: return h->s.press;
-    case MG_FDENSITY: return h->s.invdens;
+    case MG_FPRESS: return c.press;
+    case MG_FDENSITY: return c.invdens;
     case MG_FPARTICLEIDX: return c.pidx;
     case MG_FCONC: return h->conc_species_major ? nullptr : conc_of(h, h->conc_cur);
     case MG_FBIN_COUNT: return upload ? nullptr : h->s.count;
@@ -620,7 +622,7 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
     enqueue_insert_rank(h, prof);
     if (up) cudaStreamWaitEvent(st, ev[2], 0);
     enqueue_gather(h, prof, conc_up ? ev[5] : nullptr, motion_up ? ev[6] : nullptr,
-                   (flags & STEP_REORIGIN) != 0);
+                   (flags & STEP_REORIGIN) != 0, (flags & MG_STEP_PHYSICS) == 0);
     const bool remodel = (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) != 0;
     const bool heal_list = heal_from_density(h, flags);
     if (flags & MG_STEP_SURROGATE) {
@@ -1060,6 +1062,8 @@ static mg_status create_system(const mg_fparams* params, const mg_genome* genome
         plan.push_back({(void**)&c.vel, 16 * n});
         plan.push_back({(void**)&c.veval, 16 * n});
         plan.push_back({(void**)&c.pidx, 48 * n});
+        plan.push_back({(void**)&c.press, 4 * n});
+        plan.push_back({(void**)&c.invdens, 4 * n});
         plan.push_back({(void**)&c.conc, 64 * n});
         plan.push_back({(void**)&c.genes, 4 * n});
         plan.push_back({(void**)&c.origin, 4 * n});
@@ -1096,8 +1100,6 @@ static mg_status create_system(const mg_fparams* params, const mg_genome* genome
     plan.push_back({(void**)&h->s.propd, 4 * n});
     plan.push_back({(void**)&h->s.newidx, 4 * n});
     plan.push_back({(void**)&h->s.scell, 4 * n});
-    plan.push_back({(void**)&h->s.press, 4 * n});
-    plan.push_back({(void**)&h->s.invdens, 4 * n});
     plan.push_back({(void**)&h->s.force, 16 * n});
     plan.push_back({(void**)&h->s.bterm, 16 * (size_t)NB * n});
     plan.push_back({(void**)&h->s.brk, 4 * n});
@@ -1408,8 +1410,8 @@ static mg_status enqueue_upload(mg_handle h, int32_t id, const void* host, size_
     case MG_FVEL: dst = c.vel; break;
     case MG_FVEVAL: dst = c.veval; break;
     case MG_FFORCE: dst = h->s.force; break;
-    case MG_FPRESS: dst = h->s.press; break;
-    case MG_FDENSITY: dst = h->s.invdens; break;
+    case MG_FPRESS: dst = c.press; break;
+    case MG_FDENSITY: dst = c.invdens; break;
     case MG_FPARTICLEIDX: dst = c.pidx; break;
     case MG_FCONC: dst = h->conc_species_major ? nullptr : conc_of(h, h->conc_cur); break;
     case MG_FGCELL: case MG_FGNDX: return MG_OK;  // recomputed by insert
@@ -1474,8 +1476,8 @@ static mg_status enqueue_download(mg_handle h, int32_t id, void* host, size_t by
     case MG_FVEL: src = c.vel; break;
     case MG_FVEVAL: src = c.veval; break;
     case MG_FFORCE: src = h->s.force; break;
-    case MG_FPRESS: src = h->s.press; break;
-    case MG_FDENSITY: src = h->s.invdens; break;
+    case MG_FPRESS: src = c.press; break;
+    case MG_FDENSITY: src = c.invdens; break;
     case MG_FPARTICLEIDX: src = c.pidx; break;
     case MG_FCONC: src = h->conc_species_major ? nullptr : conc_of(h, h->conc_cur); break;
     case MG_FBIN_COUNT: src = h->s.count; break;

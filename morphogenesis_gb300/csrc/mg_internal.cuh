@@ -153,6 +153,10 @@ struct Carried {
     uint32_t* origin;
     uint32_t* epi;  // [16][cap] FEPIGEN words when the full epigenetic state is kept, else null
     uint32_t* iid;  // packed instances: the particle's instance (UNDEF for parked slots), else null
+    // pressure and 1/density: written by the density pass; a sort permutes them (and zeroes
+    // the forces) as countingSortFull does, when the step does not compute them again
+    float* press;
+    float* invdens;
 };
 
 // Everything kept by origin: the cold fields and the bond records (the carried sets' bond and
@@ -181,8 +185,6 @@ struct Scratch {
                                  // (8 bits each) of cells below WARP_CELL_MAX particles
     uint32_t* newidx;   // newidx[i] = sorted index of pre-sort particle i (UNDEF if dropped)
     uint32_t* scell;    // cell of sorted particle p
-    float* press;
-    float* invdens;
     float4* force;
     float4* bterm;      // [NB][cap] each own bond's acceleration on its partner in the last force
                         // pass (x, y, z; w = the partner's index bits, UNDEF when not evaluated)
@@ -224,7 +226,10 @@ void launch_cellsort(const DevParams& P, const Scratch& s, int num_sms, bool sub
 // bonds, genes, origins and cells; concentrations; velocities and the incoming-bond table
 // GATHER_REORIGIN (with GATHER_CORE): the particles' origins become their sorted indices,
 // their cold fields and bond records move from space `cs` to space `cd` accordingly.
-enum : int { GATHER_CORE = 1, GATHER_CONC = 2, GATHER_MOTION = 4, GATHER_ALL = 7, GATHER_REORIGIN = 8 };
+// GATHER_SCRATCH: pressure and 1/density moved with the particles and the forces zeroed, as
+// countingSortFull does (cuda:219-221); steps whose density and force passes rewrite them skip it.
+enum : int { GATHER_CORE = 1, GATHER_CONC = 2, GATHER_MOTION = 4, GATHER_ALL = 7, GATHER_REORIGIN = 8,
+             GATHER_SCRATCH = 16 };
 void launch_gather(const DevParams& P, const Carried& src, const float* src_conc,
                    const Carried& dst, float* dst_conc, const Scratch& s, cudaStream_t st,
                    int parts = GATHER_ALL, const Cold* cs = nullptr, const Cold* cd = nullptr);

@@ -1034,13 +1034,13 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
     case F:                                                                                       \
         k_dens_warp<F, PK><<<blocks, warps * 32, smem, st>>>(P, MG_DENS_GENOME_ARG, cur.pos, conc_in, conc_out, \
                                                              cur.genes, s.scell, s.count,         \
-                                                             s.offset, s.press, s.invdens,        \
+                                                             s.offset, cur.press, cur.invdens,        \
                                                              s.flist, s.fcount, s.counters + 3,   \
                                                              s.work, s.ovf, s.counters + 6, X,    \
                                                              prune);                              \
         k_dens_ovf<F, PK><<<(uint32_t)num_sms * 4, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out, \
                                                              cur.genes, s.scell, s.count,         \
-                                                             s.offset, s.press, s.invdens,        \
+                                                             s.offset, cur.press, cur.invdens,        \
                                                              s.flist, s.fcount, s.ovf,            \
                                                              s.counters + 6, X, prune);           \
         return;
@@ -1062,12 +1062,12 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
     case F:                                                                                       \
         k_dens_fine<F><<<blocks, warps * 32, smem, st>>>(P, G, cur.pos, conc_in, conc_out,        \
                                                          cur.genes, s.scell, s.count, s.offset,   \
-                                                         s.subcnt, s.press, s.invdens, s.flist,   \
+                                                         s.subcnt, cur.press, cur.invdens, s.flist,   \
                                                          s.fcount, s.counters + 3, s.work, s.ovf, \
                                                          s.counters + 6, X);                      \
         k_dens_ovf<F><<<(uint32_t)num_sms * 4, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out,    \
                                                              cur.genes, s.scell, s.count,         \
-                                                             s.offset, s.press, s.invdens,        \
+                                                             s.offset, cur.press, cur.invdens,        \
                                                              s.flist, s.fcount, s.ovf,            \
                                                              s.counters + 6, X, true);            \
         return;
@@ -1079,7 +1079,7 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
 #define MG_DENS_CASE(F)                                                                        \
     case F:                                                                                    \
         k_dens<F><<<blocks, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out, cur.genes, s.scell, \
-                                          s.count, s.offset, s.press, s.invdens,              \
+                                          s.count, s.offset, cur.press, cur.invdens,              \
                                           s.counters + 3, X);                                  \
         return;
     switch (flags) { MG_DENS_FLAG_SETS(MG_DENS_CASE) MG_DENS_CASE(4) default: break; }
@@ -1293,7 +1293,7 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force_in(uint32_t cap,
 void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool use_list,
                   cudaStream_t st) {
     const uint32_t nt = (uint32_t)P.force_threads, blocks = (P.cap + nt - 1) / nt;
-    k_force<<<blocks, nt, 0, st>>>(P, cur, s.scell, s.count, s.offset, s.press, s.invdens, s.flist,
+    k_force<<<blocks, nt, 0, st>>>(P, cur, s.scell, s.count, s.offset, cur.press, cur.invdens, s.flist,
                                     s.fcount, use_list ? 1 : 0, s.force, s.bterm, s.brk, s.counters + 3);
     k_force_in<<<blocks, nt, 0, st>>>(P.cap, cur.pidx, s.bterm, s.force, s.counters + 3);
 }

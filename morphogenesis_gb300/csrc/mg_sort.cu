@@ -458,8 +458,6 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
                                                 const uint32_t* __restrict__ newidx,
                                                 const uint32_t* __restrict__ cell,
                                                 uint32_t* __restrict__ scell,
-                                                float* __restrict__ press,
-                                                float* __restrict__ invdens,
                                                 float4* __restrict__ force,
                                                 const uint32_t* __restrict__ nactive_p,
                                                 int parts, Cold cs, Cold cd) {
@@ -522,6 +520,11 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
             if (S.iid) D.iid[p] = __ldg(S.iid + i);
             scell[p] = __ldg(cell + i);
         }
+        if (parts & GATHER_SCRATCH) {  // countingSortFull's FPRESS / FDENSITY copy, FFORCE = 0
+            D.press[p] = __ldg(S.press + i);
+            D.invdens[p] = __ldg(S.invdens + i);
+            force[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         if (parts & GATHER_MOTION) {
             D.vel[p] = __ldg(S.vel + i);
             D.veval[p] = __ldg(S.veval + i);
@@ -547,8 +550,8 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
             D.origin[p] = UNDEF;
             if (D.iid) D.iid[p] = UNDEF;
             scell[p] = UNDEF;
-            press[p] = 0.f;
-            invdens[p] = 0.f;
+            D.press[p] = 0.f;
+            D.invdens[p] = 0.f;
             force[p] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         if (parts & GATHER_MOTION) {
@@ -572,7 +575,7 @@ void launch_gather(const DevParams& P, const Carried& src, const float* src_conc
     const uint32_t nt = (uint32_t)P.gather_threads, blocks = (P.cap + nt - 1) / nt;
     if ((parts & GATHER_REORIGIN) && (!cs || !cd || !(parts & GATHER_CORE))) parts &= ~GATHER_REORIGIN;
     k_gather<<<blocks, nt, 0, st>>>(P, src, src_conc, dst, dst_conc, s.sorted, s.newidx, s.cell,
-                                      s.scell, s.press, s.invdens, s.force, s.counters + 3, parts,
+                                      s.scell, s.force, s.counters + 3, parts,
                                       cs ? *cs : Cold{}, cd ? *cd : Cold{});
 }
 
