@@ -101,3 +101,98 @@ def test_random_operation_sequences(built, seed):
         assert np.isfinite(g.download(A.FPOS)[: g.counts()[0], :3]).all() or box <= 0
     g.close()
     o.close()
+
+
+CHANGE_BUFS = [A.FBIN_COUNT_CHANGES, A.FBIN_OFFSET_CHANGES, A.FDENSE_LIST_LENGTHS_CHANGES,
+               A.FDENSE_LISTS_CHANGES]
+
+
+def moving_tissue(seed):
+    """A breakable, moving block, mostly living, with tissue genes (tendon, muscle, bone,
+    elastic ligament) at random."""
+    d = demo.make_block(7, "R", seed=seed, breakable=True)
+    r = np.random.default_rng(seed)
+    v = r.uniform(-30, 30, (d.n, 4)).astype(np.float32)
+    v[:, 3] = 0
+    d.arrays[A.FVEL] = v
+    d.arrays[A.FVEVAL] = v.copy()
+    ep = d.arrays[A.FEPIGEN]
+    ep[2] = np.where(r.random(d.n) < 0.8, A.EPIGEN_ACTIVE, 0)
+    for gene, share in ((6, 0.2), (7, 0.2), (9, 0.2), (10, 0.1)):
+        ep[gene] = np.where(r.random(d.n) < share, A.EPIGEN_ACTIVE, 0)
+    return d
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_random_sequences_with_remodelling(built, seed):
+    """Remodelling tissues: steps with bond changes and heal, the Run2 loop's pieces
+    (PhysicalSort, InnerPhysicalLoop, GeneAction, Remodelling), uploads of FELASTIDX that break
+    or remove bonds, of FEPIGEN with countdowns (the full epigenetic state), ZeroVel; every
+    buffer and the change lists against the oracle after each operation."""
+    import morphogenesis_gb300 as mg
+
+    r = np.random.default_rng(2000 + seed)
+    d = moving_tissue(seed)
+    g = mg.FluidSystem(d.params, d.genome, d.n)
+    o = orc.Oracle(d.params, d.genome, d.n)
+    g.TransferToCL(d.arrays)
+    o.upload_all(d.arrays)
+    log = []
+    g.Run(1)
+    o.step(1)
+    for k in range(8):
+        op = int(r.integers(0, 7))
+        if op == 0:
+            n = int(r.integers(1, 4))
+            fl = [A.STEP_DEFAULT | A.STEP_BOND_CHANGES, A.STEP_DEFAULT | A.STEP_REMODEL,
+                  A.STEP_PHYSICS | A.STEP_REMODEL][int(r.integers(0, 3))]
+            g.Run(n, fl)
+            o.step(n, fl)
+            log.append(f"run {n} flags {fl}")
+        elif op == 1:
+            inner = int(r.integers(1, 4))
+            g.Run2PhysicalSort()
+            o.insert(); o.prefix_sum(); o.sort()
+            for _ in range(inner):
+                g.Run2InnerPhysicalLoop()
+                o.pressure(); o.force(); o.advance()
+            g.Run2GeneAction()
+            o.diffusion(); o.genes()
+            g.Run2Remodelling(inner)
+            o.bond_changes(inner); o.remodel()
+            log.append(f"run2 cycle {inner}")
+        elif op == 2:
+            e0 = g.download(A.FELASTIDX)
+            e = e0.reshape(-1, 6, 9)  # a view of e0: [particle][bond][word]
+            pick = r.random(e.shape[:2])
+            e[pick < 0.05, 2] = np.float32(0).view(np.uint32)        # rest length 0: broken
+            e[(pick >= 0.05) & (pick < 0.08), 0] = A.NO_PARTNER       # no partner
+            g.upload(A.FELASTIDX, e0)
+            o.upload(A.FELASTIDX, e0)
+            log.append("upload FELASTIDX")
+        elif op == 3:
+            ep = g.download(A.FEPIGEN)
+            pick = r.random(ep.shape)
+            ep[pick < 0.05] = r.integers(1, 6, ep.shape)[pick < 0.05].astype(np.uint32)
+            g.upload(A.FEPIGEN, ep)
+            o.upload(A.FEPIGEN, ep)
+            log.append("upload FEPIGEN")
+        elif op == 4:
+            g.ZeroVelCL()
+            z = np.zeros((d.n, 4), np.float32)
+            o.upload(A.FVEL, z)
+            o.upload(A.FVEVAL, z)
+            log.append("zero velocities")
+        elif op == 5:
+            g.Run(2)
+            o.step(2)
+            log.append("run 2")
+        else:
+            g.set_option(A.OPT_REORIGIN_PERIOD, int(r.choice([0, 1, 3])))
+            log.append("re-origin period")
+        what = f"seed {seed}, after " + "; ".join(log)
+        check(g, o, what)
+        for b in CHANGE_BUFS:
+            assert np.array_equal(g.download(b), o.download(b)), f"{what}: change buffer {b}"
+    g.close()
+    o.close()
