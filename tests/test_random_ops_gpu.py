@@ -196,3 +196,75 @@ def test_random_sequences_with_remodelling(built, seed):
             assert np.array_equal(g.download(b), o.download(b)), f"{what}: change buffer {b}"
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_random_sequences_packed_instances(built, seed):
+    """Packed instances against the same tissues as systems of their own under random steps
+    (physics, genes only, both, frozen bonds), position nudges and drops applied to both, and
+    re-origin periods: every instance's sorted segment bit for bit equal to its own system's
+    active particles after each operation."""
+    import morphogenesis_gb300 as mg
+
+    r = np.random.default_rng(3000 + seed)
+    ds = []
+    for k in range(4):
+        side = int(r.integers(4, 9))
+        g0 = demo.make_genome(seed=40 + k, diffusion=demo.diffusion_rate("R", float(r.uniform(0.05, 0.2))))
+        ds.append(demo.make_block(side, "R", seed=seed * 10 + k, genome=g0,
+                                  intstiff=float(r.uniform(0.5, 2.0)), breakable=bool(k % 2)))
+    pk = mg.Packed([d.params for d in ds], [d.genome for d in ds], [d.n for d in ds])
+    pk.TransferToCL(pk.concat([d.arrays for d in ds]))
+    alone = []
+    for d in ds:
+        fs = mg.FluidSystem(d.params, d.genome, d.n)
+        fs.TransferToCL(d.arrays)
+        alone.append(fs)
+    bufs = (A.FPOS, A.FVEL, A.FVEVAL, A.FFORCE, A.FPRESS, A.FDENSITY, A.FCONC, A.FELASTIDX,
+            A.FPARTICLEIDX, A.FPARTICLE_ID, A.FEPIGEN)
+    log = []
+    pk.Run(1)
+    for fs in alone:
+        fs.Run(1)
+    for step in range(6):
+        op = int(r.integers(0, 4))
+        if op <= 1:
+            n = int(r.integers(1, 4))
+            fl = FLAGS[int(r.integers(0, 4))]
+            pk.Run(n, fl)
+            for fs in alone:
+                fs.Run(n, fl)
+            log.append(f"run {n} flags {fl}")
+        elif op == 2:
+            drop = bool(r.integers(0, 2))
+            ppos = pk.download(A.FPOS)
+            for (f, c), fs in zip(pk.ranges(), alone):
+                apos = fs.download(A.FPOS)
+                sel = np.nonzero(r.random(c) < (0.08 if drop else 0.2))[0]
+                if drop:
+                    apos[sel, 0] = np.float32(-1e4)
+                else:
+                    apos[sel, :3] += r.uniform(-0.2, 0.2, (len(sel), 3)).astype(np.float32)
+                ppos[f + sel] = apos[sel]
+                fs.upload(A.FPOS, apos)
+            pk.upload(A.FPOS, ppos)
+            log.append("drop" if drop else "nudge")
+        else:
+            period = int(r.choice([0, 1, 64]))
+            pk.set_option(A.OPT_REORIGIN_PERIOD, period)
+            for fs in alone:
+                fs.set_option(A.OPT_REORIGIN_PERIOD, int(r.choice([0, 1, 64])))
+            log.append("re-origin periods")
+        what = f"seed {seed}, after " + "; ".join(log)
+        ranges = pk.ranges()
+        for b in bufs:
+            parts = pk.split(b)
+            for k, fs in enumerate(alone):
+                x, y = bits(parts[k]), bits(fs.download(b))
+                c = ranges[k][1]
+                assert fs.counts()[0] == c, f"{what}: instance {k} holds {fs.counts()[0]} particles alone, {c} packed"
+                y = y[:, :c] if b == A.FEPIGEN else y[:c]
+                assert np.array_equal(x, y), f"{what}: instance {k}, buffer {b}"
+    pk.close()
+    for fs in alone:
+        fs.close()
