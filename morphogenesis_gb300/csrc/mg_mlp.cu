@@ -1143,14 +1143,17 @@ using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, 
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 cudaError_t make_feat_map(const bf16* feat, uint32_t rows, CUtensorMap* map) {
-    static EncodeTiled encode = nullptr;
-    if (!encode) {
+    // looked up once (a function-local static: initialised by one thread, seen by all)
+    static const EncodeTiled encode = []() -> EncodeTiled {
         void* fn = nullptr;
         cudaDriverEntryPointQueryResult q{};
-        MLP_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
-        if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
-        encode = reinterpret_cast<EncodeTiled>(fn);
-    }
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return reinterpret_cast<EncodeTiled>(fn);
+    }();
+    if (!encode) return cudaErrorNotSupported;
     // a 16-byte aligned base, a 96-byte row stride and 16-byte boxes along the features
     if ((reinterpret_cast<uintptr_t>(feat) & 15u) != 0 || rows == 0) return cudaErrorInvalidValue;
     const cuuint64_t dims[2] = {(cuuint64_t)MLP_IN, (cuuint64_t)rows};
