@@ -450,20 +450,32 @@ def batch_section(args):
     return out
 
 
+def workload_config(world: int) -> dict:
+    """The workload's description, the same in both arms' JSON lines."""
+    from morphogenesis_gb300 import demo
+
+    n = DIMS[0] * DIMS[1] * DIMS[2]
+    p = demo.make_params(DIMS, PARAM)
+    cells = int(p.grid_total)
+    return {"workload": "plain full step, 1,048,576 particles (128x64x128 lattice), grid 132^3, gsrch 3",
+            "parameterisation": PARAM, "particles_per_gpu": n, "cells": cells,
+            "l2": "inputs larger than L2: step state 1.40 GB/step",
+            "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     steps = max(1, args.steps if args.steps <= 20 else 20)
-    warm = min(args.warmup, 1)
+    warm = max(args.warmup, 3)  # as the GPU arm
     value, used, dt = cpu_reference(steps, warm, threads)
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded jittered 128x64x128 lattice, 6 bonds/particle, 16 species, 16 gene bits",
-        "config": {"workload": "plain full step, 1,048,576 particles (128x64x128 lattice), grid 132^3, gsrch 3",
-                   "parameterisation": PARAM},
+        "config": workload_config(world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port",
                          "sample": f"{steps} steps of the 1,048,576-particle workload after {warm} warm-up"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -574,11 +586,8 @@ def main():
             "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded jittered 128x64x128 lattice, 6 bonds/particle, 16 species, 16 gene bits",
-            "config": {"workload": "plain full step, 1,048,576 particles (128x64x128 lattice), grid 132^3, gsrch 3",
-                       "parameterisation": PARAM, "particles_per_gpu": n, "cells": cells,
-                       "l2": f"inputs larger than L2: step state {step_bytes / 1e9:.2f} GB/step",
-                       "parallelism": f"replicas x{world}",
-                       "launch_shape": {k: v for k, v in tune.items() if k != "ms_per_step"}},
+            "config": workload_config(world),
+            "launch_shape": {k: v for k, v in tune.items() if k != "ms_per_step"},
             "clocks": clk,
             "gpu_launches": int(launches),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
