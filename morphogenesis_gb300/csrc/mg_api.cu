@@ -7,6 +7,7 @@
 // (fluid_system.cpp:1919-2014).  Where the reference calls clFinish after every kernel and
 // reads counts back to the host every sort, the whole step here is one CUDA graph with the
 // active particle count kept on the device.
+#include <nvtx3/nvToolsExt.h>
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -383,12 +384,23 @@ int prof_slot(mg_system* h, const char* name) {
     return (int)h->prof.size() - 1;
 }
 
+// An NVTX range around a host entry point or, in profiling mode, a stage's launches (named by
+// the stage); a tool such as Nsight Systems or `ncu --nvtx` sees them, otherwise they cost a
+// check of the NVTX dispatch table.
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
+
 struct Mark {
     mg_system* h;
     bool on;
     ProfMark m{};
     Mark(mg_system* h_, bool on_, const char* name) : h(h_), on(on_) {
         if (!on) return;
+        nvtxRangePushA(name);
         m.slot = prof_slot(h, name);
         cudaEventCreate(&m.a);
         cudaEventCreate(&m.b);
@@ -398,6 +410,7 @@ struct Mark {
         if (!on) return;
         cudaEventRecord(m.b, h->stream);
         h->marks.push_back(m);
+        nvtxRangePop();
     }
 };
 
@@ -1556,6 +1569,7 @@ mg_status mg_download(mg_handle h, int32_t id, void* host, size_t bytes) {
 mg_status mg_step_io(mg_handle h, const mg_io* in, uint32_t nin, uint32_t nsteps, uint32_t flags,
                      const mg_io* out, uint32_t nout) {
     if (!h || (nin && !in) || (nout && !out)) return fail(h, MG_ERR_INVALID_ARG, "NULL argument");
+    Range r("mg_step_io");
     if (h->profile) return fail(h, MG_ERR_INVALID_ARG, "mg_step_io: profiling is on");
     if (mg_status st0 = packed_flags_ok(h, flags)) return st0;
     // Plain-copy buffers with the right sizes in page-locked host memory: the copies go into the
@@ -1773,6 +1787,7 @@ mg_status mg_run_gene_action(mg_handle h) {
 
 mg_status mg_step(mg_handle h, uint32_t nsteps, uint32_t flags) {
     if (!h) return fail(nullptr, MG_ERR_INVALID_ARG, "handle is NULL");
+    Range r("mg_step");
     mg_status st = run_steps(h, nsteps, flags);
     if (st != MG_OK) return st;
     return check_device(h);
