@@ -6,7 +6,8 @@ import os
 from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
-LIB_PATH = PKG / "_build" / "libmg_gb300.so"
+# MG_BUILD_DIR: load a variant built there (morphogenesis_gb300/build.py), else the product build
+LIB_PATH = PKG / os.environ.get("MG_BUILD_DIR", "_build") / "libmg_gb300.so"
 
 BONDS_PER_PARTICLE = 6
 DATA_PER_BOND = 9

@@ -15,7 +15,9 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
-OUT = PKG / "_build"
+# MG_BUILD_DIR (environment, a directory name inside the package) builds a variant elsewhere,
+# e.g. the bounds-checking library (MG_NVCC_EXTRA=-DMG_BOUNDS_CHECK=1) next to the product one
+OUT = PKG / os.environ.get("MG_BUILD_DIR", "_build")
 LIB = OUT / "libmg_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

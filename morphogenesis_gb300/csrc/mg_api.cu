@@ -369,6 +369,8 @@ mg_status check_device(mg_system* h) {
         return fail(h, MG_ERR_GRID_OVERFLOW, "more than 65536 grid cells hold over 256 particles");
     if (err & mg::MLP_ERR_MBAR_TIMEOUT)
         return fail(h, MG_ERR_DEVICE_TIMEOUT, "surrogate inference: tensor-core completion wait gave up (bounded spin)");
+    if (err & ERR_INDEX)
+        return fail(h, MG_ERR_CUDA, "an index past its buffer (bounds-checking build): a kernel read a corrupt index");
     if (err & ERR_EPIGEN_VALUE)
         return fail(h, MG_ERR_UNSUPPORTED,
                     "FEPIGEN values other than 0 and INT_MAX (epigenetic countdowns) are not "
@@ -1142,6 +1144,7 @@ static mg_status create_system(const mg_fparams* params, const mg_genome* genome
         c.bond = h->cold.bond;
         c.partner = h->cold.partner;
     }
+    h->P.err = h->s.counters + 2;
     cudaMemsetAsync(h->arena, 0, total, h->stream);
     launch_init_set(max_points, h->set[0], h->stream);
     launch_init_set(max_points, h->set[1], h->stream);
@@ -1333,6 +1336,7 @@ mg_status mg_update_params(mg_handle h, const mg_fparams* p) {
     h->P.force_threads = old.force_threads;
     h->P.gather_threads = old.gather_threads;
     h->P.advance_threads = old.advance_threads;
+    h->P.err = old.err;
     clear_graphs(h);
     // the device copy of the time (both parity slots)
     const uint32_t t2[2] = {*reinterpret_cast<const uint32_t*>(&p->time), *reinterpret_cast<const uint32_t*>(&p->time)};

@@ -50,7 +50,12 @@ enum : uint32_t {
     ERR_SCAN_TIMEOUT = 1u << 0,
     ERR_BIG_LIST_OVERFLOW = 1u << 1,
     ERR_EPIGEN_VALUE = 1u << 2,
+    ERR_INDEX = 1u << 3,  // a data-dependent index past its buffer (bounds-checking builds)
 };
+
+#ifndef MG_BOUNDS_CHECK
+#define MG_BOUNDS_CHECK 0
+#endif
 
 // Simulation parameters passed by value to every kernel (constant bank).
 // Packed instances (independent tissues advanced as one system, mg_create_packed): the frame
@@ -102,7 +107,25 @@ struct DevParams {
     const InstParams* inst;
     const struct DevGenome* genomes;
     int n_inst;
+    uint32_t* err;  // the device error word (where bounds-checking builds record ERR_INDEX)
 };
+
+// Bounds-checking builds (MG_BOUNDS_CHECK=1): a data-dependent index at or past its bound sets
+// ERR_INDEX in the error word and is replaced by one inside the buffer, so the access stays in
+// bounds and the host reports the error after the step.  Other builds return the index as it is.
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t checked(const DevParams& P, uint32_t i, uint32_t bound) {
+#if MG_BOUNDS_CHECK
+    if (i >= bound) {
+        if (P.err) atomicOr(P.err, (uint32_t)ERR_INDEX);
+        return bound ? bound - 1u : 0u;
+    }
+#endif
+    (void)P;
+    (void)bound;
+    return i;
+}
+#endif
 
 // Genome in device memory (float-widened, compacted sparse lists).
 struct DevGenome {

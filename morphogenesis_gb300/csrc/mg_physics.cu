@@ -471,7 +471,7 @@ __device__ __forceinline__ void dens_list_finish(
         uint32_t nf = 0, nh = 0, fmark = 0u;
         for (uint32_t k = 0; k < n; k++) {
             const uint32_t e = my[k * 32];
-            const uint32_t q = e & ~LIST_CELL_START;
+            const uint32_t q = checked(P, e & ~LIST_CELL_START, P.cap);
             const float4 jp = pos[q];
             if (e & LIST_CELL_START) {  // first neighbour of the next cell:
                 if (F::DENS) {          // flush the previous cell's partial sum
@@ -535,7 +535,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     const bool act = k < *nactive_p;
     if (!act) park_conc<FLAGS>(conc_in, conc_out, k, *nactive_p, P.cap);
     if (!__any_sync(0xffffffffu, act)) return;
-    const uint32_t p = act ? work[k] : 0u;
+    const uint32_t p = act ? checked(P, work[k], P.cap) : 0u;
 
     const float4 ip = act ? pos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
     const uint32_t pcell = act ? scell[p] : 0u;
@@ -593,7 +593,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                 const int cx = wx0 + ox, cz = wz0 + oz, cy = wy0 + oy;
                 if (!prune || cell_meets_box(PACKED ? frame_of(P, ginst) : frame_of(P), cx, cy, cz,
                                              tx0 - Rf, tx1 + Rf, ty0 - Rf, ty1 + Rf, tz0 - Rf, tz1 + Rf)) {
-                    const uint32_t cell = (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx);
+                    const uint32_t cell = checked(P, (uint32_t)((cy * P.res[2] + cz) * P.res[0] + cx), P.cells);
                     tcnt = count[cell];
                     if (tcnt) toff = offset[cell];
                 }
@@ -614,7 +614,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                 for (uint32_t base = 0; base < cnt; base += 32) {
                     const uint32_t kk = base + lane;
                     const bool valid = kk < cnt;
-                    const float4 qp = valid ? pos[off + kk] : make_float4(INF, INF, INF, 0.f);
+                    const float4 qp = valid ? pos[checked(P, off + kk, P.cap)] : make_float4(INF, INF, INF, 0.f);
                     // survivors: candidates within Rf of the span (the span's box with rounded
                     // edges and corners); every lane's neighbour is one, as the lane lies in it
                     const float ex = fmaxf(0.f, fmaxf(tx0 - qp.x, qp.x - tx1));
@@ -1163,7 +1163,7 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force(DevParams P, Car
     const float4 ip = C.pos[p], iv = C.veval[p];
     // the bond records' slot; a particle without an origin (a slot that was parked and given a
     // position again by an upload) has no bonds
-    const uint32_t o0 = C.origin[p];
+    const uint32_t o0 = C.origin[p] == UNDEF ? UNDEF : checked(P, C.origin[p], cap);
     const bool has_rec = o0 != UNDEF;
     const uint32_t o = has_rec ? o0 : 0u;
     float fx = 0.f, fy = 0.f, fz = 0.f;
@@ -1215,14 +1215,14 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force(DevParams P, Car
             // two neighbours per iteration, so their gathers are in flight together
             for (; k + 2 <= nf; k += 2) {
                 const uint32_t e0 = flist[(size_t)k * cap + p], e1 = flist[(size_t)(k + 1) * cap + p];
-                const uint32_t q0 = e0 & ~FLIST_CELL_START, q1 = e1 & ~FLIST_CELL_START;
+                const uint32_t q0 = checked(P, e0 & ~FLIST_CELL_START, cap), q1 = checked(P, e1 & ~FLIST_CELL_START, cap);
                 const float4 jp0 = C.pos[q0], jp1 = C.pos[q1], jv0 = C.veval[q0], jv1 = C.veval[q1];
                 const float pr0 = press[q0], pr1 = press[q1], dn0 = invdens[q0], dn1 = invdens[q1];
                 term(e0, jp0, jv0, pr0, dn0);
                 term(e1, jp1, jv1, pr1, dn1);
             }
             if (k < nf) {
-                const uint32_t e = flist[(size_t)k * cap + p], q = e & ~FLIST_CELL_START;
+                const uint32_t e = flist[(size_t)k * cap + p], q = checked(P, e & ~FLIST_CELL_START, cap);
                 term(e, C.pos[q], C.veval[q], press[q], invdens[q]);
             }
             sx = sx + cx; sy = sy + cy; sz = sz + cz;

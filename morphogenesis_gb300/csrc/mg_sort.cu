@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
     }
     const uint32_t nact = *nactive_p;
     if (p < nact) {
-        const uint32_t i = sorted[p];
+        const uint32_t i = checked(P, sorted[p], cap);
         if (parts & GATHER_CORE) {
             D.pos[p] = __ldg(S.pos + i);
 
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
             } else {
                 D.genes[p] = __ldg(S.genes + i);
             }
-            const uint32_t o = __ldg(S.origin + i);
+            const uint32_t o0 = __ldg(S.origin + i), o = o0 == UNDEF ? UNDEF : checked(P, o0, cap);
             if (parts & GATHER_REORIGIN) {
                 // the particle's records move to slot p of the other space, and p becomes its
                 // origin (a particle without records keeps none)
