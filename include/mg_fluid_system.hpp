@@ -193,6 +193,23 @@ class FluidSystem {
     // the legacy Run() order, nsteps steps (one sort per step)
     void Run(uint32_t nsteps = 1, uint32_t flags = MG_STEP_DEFAULT) { check(mg_step(h_, nsteps, flags), "Run"); }
 
+    // ---- tuning (results are identical for every choice) ---------------------------------------
+    // Times the launch shapes and block sizes over `steps` steps of the current state (restored
+    // afterwards) and keeps the fastest; returns its ms per step.  Call after TransferToCL.
+    float Autotune(uint32_t steps = 5, uint32_t flags = MG_STEP_DEFAULT) {
+        int32_t choice[4];
+        float ms = 0.f;
+        check(mg_autotune(h_, steps, flags, choice, &ms), "Autotune");
+        return ms;
+    }
+    // threads per block of the force, gather and advance passes: 128, 256 or 512 each
+    void SetBlockSizes(int32_t force, int32_t gather, int32_t advance) {
+        const int32_t t[3] = {force, gather, advance};
+        check(mg_set_block_sizes(h_, t), "SetBlockSizes");
+    }
+    // MG_OPT_* (include/mg_abi.h)
+    void SetOption(int32_t option, int32_t value) { check(mg_set_option(h_, option, value), "SetOption"); }
+
    private:
     static constexpr int kHostBufs[] = {MG_FPOS, MG_FVEL, MG_FVEVAL, MG_FFORCE, MG_FPRESS, MG_FDENSITY,
                                         MG_FAGE, MG_FCOLOR, MG_FELASTIDX, MG_FPARTICLEIDX, MG_FPARTICLE_ID,

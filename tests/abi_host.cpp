@@ -1,6 +1,7 @@
 // abi_host.cpp - a compiled C++ host on include/mg_fluid_system.hpp (the FluidSystem-style
 // façade over mg_abi.h), driving the reference's calling sequence: FluidSetupCL, FluidParamCL,
-// UpdateGenome, AllocateParticles, buffers filled through the host mirrors, TransferToCL, one
+// UpdateGenome, AllocateParticles, buffers filled through the host mirrors, TransferToCL, the
+// tuning calls (re-origin period, block sizes, autotune: none may change a result), one
 // Run2 cycle (Run2PhysicalSort, Run2InnerPhysicalLoop, Run2GeneAction), `steps` legacy steps,
 // TransferFromCL.  Built and run by tests/test_cpp_host.py, which compares what it writes with
 // the same sequence run through the Python binding.
@@ -84,6 +85,10 @@ int main(int argc, char** argv) {
         // the species-major accessor sees species tf of particle i where the reference's does
         if (fs.getConc(3)[5] != reinterpret_cast<const float*>(fs.mcpu(MG_FCONC))[3 * n + 5]) return 3;
         fs.TransferToCL();
+        // tuning changes no result: the run below must match the Python binding's defaults
+        fs.SetOption(MG_OPT_REORIGIN_PERIOD, 3);
+        fs.SetBlockSizes(512, 128, 256);
+        if (!(fs.Autotune(2) > 0.f)) return 5;
         fs.Run2PhysicalSort();
         fs.Run2InnerPhysicalLoop();
         fs.Run2GeneAction();
