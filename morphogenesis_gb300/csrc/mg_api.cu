@@ -192,6 +192,7 @@ void derive(DevParams& D, const mg_fparams& p, uint32_t cap) {
         int ex = 0;
         const float m = std::frexp(p.psmoothradius, &ex);  // sr = m * 2^ex, m in [0.5, 1)
         D.sr_inv_exact = (m == 0.5f && std::isfinite(p.psmoothradius)) ? 1.0f / p.psmoothradius : 0.0f;
+        D.unit = 1.0f;
     }
     D.r2 = p.psmoothradius * p.psmoothradius;
     D.d2 = p.psimscale * p.psimscale;

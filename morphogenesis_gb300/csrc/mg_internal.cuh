@@ -85,6 +85,9 @@ struct DevParams {
     float sr, r2, r2diff, d2, pmass, rest, istiff, wc2, surf;
     // 1 / sr when sr is a power of two (then r / sr == r * (1 / sr) exactly), else 0
     float sr_inv_exact;
+    // 1.0, read at run time: a unit multiplier the compiler cannot fold (the packed diffusion
+    // sums are written as p * unit + nc so that they are not fused with the product p)
+    float unit;
     float pr, bmin[3], bmax[3], estiff, damp, xmin_stiff, xmax_stiff, slope, one_minus_slope;
     float grav[3], AL, AL2, VL, VL2, vl_factor, dt;
     float actuation_factor, actuation_period;

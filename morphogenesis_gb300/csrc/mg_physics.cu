@@ -59,7 +59,8 @@ __device__ __forceinline__ float wendland_term(float dsq, float sr, float sr_inv
 constexpr uint32_t FLIST_CELL_START = 0x80000000u;
 
 // Build switches kept for measuring each choice against its plain form (both forms give the
-// same bits): 256-bit concentration rows, packed f32x2 species differences.
+// same bits): 256-bit concentration rows, packed f32x2 diffusion terms (MG_F32X2 1: the species
+// differences; 2: also the products and the sums, each as a fused operation rounding once).
 #ifndef MG_ROW_V8
 #define MG_ROW_V8 1
 #endif
@@ -74,7 +75,7 @@ constexpr uint32_t FLIST_CELL_START = 0x80000000u;
 #define MG_DENS_GENOME_ARG G
 #endif
 #ifndef MG_F32X2
-#define MG_F32X2 1
+#define MG_F32X2 2
 #endif
 // A particle's 16 concentrations as two 256-bit loads: a gather of rows from 32 lanes then
 // costs the L1 two accesses per row instead of four.  Rows are 64 bytes in buffers aligned to
@@ -120,7 +121,7 @@ __device__ __forceinline__ void store_row16(float* row, const float (&v)[NTF]) {
 template <bool DIFF, bool MEAN>
 __device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], const float* __restrict__ dif,
                                            const float (&cur)[NTF], const float* conc, uint32_t q,
-                                           float cc, bool uniform, bool diffuse) {
+                                           float cc, bool uniform, bool diffuse, float unit) {
     if (!DIFF && !MEAN) return;
     float cj[NTF];
     load_row16(conc + (size_t)q * NTF, cj);
@@ -147,16 +148,35 @@ __device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], c
             const float a = dif[0] * cc;
 #if MG_F32X2
             // cj - cur as cj + (-1) * cur: one rounding of the exact difference, as the
-            // subtraction.  The product and the sum stay scalar: the packed __fmul2_rn and
-            // __fadd2_rn gave other bits than __fmul_rn / __fadd_rn on random operands (45% of
-            // pairs, measured), with or without a barrier between them.
+            // subtraction.  The packed __fmul2_rn and __fadd2_rn gave other bits than
+            // __fmul_rn / __fadd_rn on random operands (45% of pairs, measured), with or without
+            // a barrier between them, so the product and the sum are never written that way.
             const float2 m1 = make_float2(-1.f, -1.f);
+#if MG_F32X2 >= 2
+            // ... and the product and the sum as fused operations that round once each:
+            // a * d + (-0) is the product a * d rounded (for every d, zeros' signs included),
+            // p * unit + nc the sum p + nc rounded.  Three packed operations per species pair.
+            // With a literal 1 for the unit the compiler fused the two into a * d + nc (one
+            // rounding), even when written as inline fma.rn.f32x2; a unit read at run time it
+            // cannot fold, and the probe of both forms on random operands (zeros, subnormals,
+            // wide exponents) gave the scalar bits in every case.
+            const float2 a2 = make_float2(a, a), one = make_float2(unit, unit), nz = make_float2(-0.f, -0.f);
+#pragma unroll
+            for (int t = 0; t < NTF; t += 2) {
+                const float2 d = __ffma2_rn(make_float2(cur[t], cur[t + 1]), m1, make_float2(cj[t], cj[t + 1]));
+                const float2 pr = __ffma2_rn(a2, d, nz);
+                const float2 s = __ffma2_rn(pr, one, make_float2(nc[t], nc[t + 1]));
+                nc[t] = s.x;
+                nc[t + 1] = s.y;
+            }
+#else
 #pragma unroll
             for (int t = 0; t < NTF; t += 2) {
                 const float2 d = __ffma2_rn(make_float2(cur[t], cur[t + 1]), m1, make_float2(cj[t], cj[t + 1]));
                 nc[t] += a * d.x;
                 nc[t + 1] += a * d.y;
             }
+#endif
 #else
 #pragma unroll
             for (int t = 0; t < NTF; t++) nc[t] += a * (cj[t] - cur[t]);
@@ -238,7 +258,7 @@ __device__ __forceinline__ float dens_direct(const DevParams& P, float4 ip, uint
             if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr, P.sr_inv_exact);
             if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
                 conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc, q, (P.r2diff - dsq) * P.d2,
-                                             false, diffuse);
+                                             false, diffuse, P.unit);
                 mcnt++;
             }
         }
@@ -490,7 +510,7 @@ __device__ __forceinline__ void dens_list_finish(
             if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr, P.sr_inv_exact);
             if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
                 conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2,
-                                             G->uniform != 0, true);
+                                             G->uniform != 0, true, P.unit);
                 mcnt++;
                 if (X.hlist) X.hlist[(size_t)nh++ * P.cap + slot] = q;  // nh <= n <= NL_CAP
             }
