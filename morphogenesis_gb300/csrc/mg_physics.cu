@@ -38,9 +38,12 @@ namespace mg {
 #endif
 constexpr int DENS_WARPS = MG_DENS_WARPS;  // warps per block of the warp-cooperative pass
 // rows of a lane's neighbour list in shared memory: the list appends are branch-free (every
-// survivor is written at the next free row, only hits advance it), so one spare row takes the
-// writes past a full list
-constexpr int NL_ROWS = NL_CAP + 1;
+// survivor is written at the next free row, only hits advance it); a batch of four survivors
+// starts at row min(n, NL_CAP), so three spare rows take the writes past a full list
+#ifndef MG_DENS_WP
+#define MG_DENS_WP 1
+#endif
+constexpr int NL_ROWS = NL_CAP + (MG_DENS_WP ? 4 : 1);
 
 // ---- per-neighbour terms ---------------------------------------------------------------
 // sr_inv_exact: 1 / sr when sr is a power of two, where the quotient r / sr is the product
@@ -678,6 +681,20 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                             const float2 d23 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
                             const float d[4] = {d01.x, d01.y, d23.x, d23.y};
                             const uint32_t qi[4] = {Q.x, Q.y, Q.z, Q.w};
+#if MG_DENS_WP
+                            // the batch's row pointer advances by a row per hit; the hits are
+                            // counted from it once per batch
+                            uint32_t* const wp0 = my + min(n, (uint32_t)NL_CAP) * 32;
+                            uint32_t* wp = wp0;
+#pragma unroll
+                            for (int u = 0; u < 4; u++) {
+                                const bool hit = d[u] < R2s && d[u] > 0.f;
+                                *wp = qi[u] | mark;
+                                mark = hit ? 0u : mark;
+                                wp += hit ? 32 : 0;
+                            }
+                            n += (uint32_t)(wp - wp0) >> 5;
+#else
 #pragma unroll
                             for (int u = 0; u < 4; u++) {
                                 const bool hit = d[u] < R2s && d[u] > 0.f;
@@ -685,6 +702,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                                 mark = hit ? 0u : mark;
                                 n += hit ? 1u : 0u;
                             }
+#endif
                         }
                         for (; tt < ns; tt++) {
                             const float4 sp = make_float4(s_sx[w][tt], s_sy[w][tt], s_sz[w][tt], 0.f);
