@@ -19,8 +19,9 @@
 //    broadcast in ascending order and every lane appends the ones inside its own radius and
 //    window to a per-lane list in shared memory.  The neighbour terms are then evaluated lane
 //    by lane over these lists, so no lane idles through a neighbour that belongs to another
-//    lane.  A lane whose list overflows (more than NL_CAP neighbours) is queued for the
-//    overflow pass, one warp per queued particle.
+//    lane.  A lane whose list overflows (more than NL_CAP neighbours) is then walked by its
+//    whole warp (the overflow walk, one warp per particle); the fine-cell search queues such
+//    particles for the same walk in a second kernel.
 // The density pass also records each particle's fluid-force neighbours (dsq < 1) so the force
 // pass reads a short list instead of searching again.
 #include <cfloat>
@@ -525,6 +526,194 @@ __device__ __forceinline__ void dens_list_finish(
     dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press, invdens, X);
 }
 
+// ---- overflow walk ----------------------------------------------------------------------------
+// Particles with more neighbours than NL_CAP (only in dense clumps), one warp per particle
+// (the warp search's own warp, or k_dens_ovf for the fine-cell search's queue), in two phases
+// that repeat over segments of OVF_SEG hits:
+//  collect : the window cells (in the reference order, 32 at a time, one per lane) form one
+//            stream of candidates; each lane takes one candidate per chunk (its cell found by a
+//            binary search over the cells' running counts), several chunks in flight, and the
+//            hits are compacted in order into shared memory with their distance, window-cell
+//            index and concentrations;
+//  apply   : the hits are taken in that order by every lane: the density partial sum of each
+//            cell, species t (mod 16) of the diffusion and neighbour sums in lane t with the
+//            one-thread walk's expression and order, the force list in lane 0.
+// Lane 0 then runs the common epilogue.
+constexpr int OVF_SEG = 64;
+
+// Takes a segment's hits in order (the apply phase of the overflow pass).
+template <int FLAGS>
+__device__ __forceinline__ void ovf_apply(const DevParams& P, uint32_t p, uint32_t lane, uint32_t t,
+                                          uint32_t* __restrict__ flist, const float* sd,
+                                          const uint32_t* sq, const uint8_t* sc, const float4 (*scj)[NTF / 4],
+                                          uint32_t nh, int& lastcell, uint32_t& fmark, float& sum, float& part,
+                                          uint32_t& nf, float& nc_t, float& ms_t, uint32_t& mcnt,
+                                          float dif_t, float cur_t) {
+    using F = DF<FLAGS>;
+    __syncwarp();
+    for (uint32_t h = 0; h < nh; h++) {
+        const float d = sd[h];
+        const int c = sc[h];
+        if (c != lastcell) {  // first hit of the next cell: flush the previous partial
+            sum += part;
+            part = 0.f;
+            lastcell = c;
+            fmark = FLIST_CELL_START;
+        }
+        if (d < 1.f) {
+            if (lane == 0 && nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = sq[h] | fmark;
+            fmark = 0u;
+            nf++;
+        }
+        if (F::DENS && d < P.r2) part += wendland_term(d, P.sr, P.sr_inv_exact);
+        if ((F::DIFF || F::MEAN) && d < P.r2diff) {
+            const float cj = reinterpret_cast<const float*>(scj[h])[t];
+            if (F::MEAN) ms_t += cj;
+            if (F::DIFF && dif_t != 0.f) nc_t += (dif_t * ((P.r2diff - d) * P.d2)) * (cj - cur_t);
+            mcnt++;
+        }
+    }
+    __syncwarp();
+}
+
+// One queued particle, by the whole warp: s_cj, s_d, s_q and s_c hold a segment of OVF_SEG hits
+// (OVF_SEG * 73 bytes of the warp's own shared memory).
+template <int FLAGS, bool PACKED>
+__device__ __forceinline__ void ovf_particle(
+    const DevParams& P, const DevGenome* __restrict__ G0, uint32_t p, const float4* __restrict__ pos,
+    const float* __restrict__ conc_in, float* __restrict__ conc_out, const uint32_t* __restrict__ genes,
+    const uint32_t* __restrict__ scell, const uint32_t* __restrict__ count,
+    const uint32_t* __restrict__ offset, float* __restrict__ press, float* __restrict__ invdens,
+    uint32_t* __restrict__ flist, uint32_t* __restrict__ fcount, const DensExtra& X, bool prune,
+    float4 (*s_cj)[NTF / 4], float* s_d, uint32_t* s_q, uint8_t* s_c) {
+    // prune: positions are those of the last sort, so a window cell whose geometric box misses
+    // the particle's search box holds no neighbour
+    using F = DF<FLAGS>;
+    constexpr bool CONC = F::DIFF || F::MEAN;
+    const uint32_t lane = threadIdx.x & 31u, t = lane & 15u;
+    float R2 = 1.f;
+    if (F::DENS) R2 = fmaxf(R2, P.r2);
+    if (CONC) R2 = fmaxf(R2, P.r2diff);
+    const float Rf = sqrtf(R2) * 1.0001f + 1e-3f;  // conservative search-box half width
+    const float4 ip = pos[p];
+    const DevGenome* __restrict__ G = PACKED ? P.genomes + X.iid[p] : G0;
+    const CellFrame frame = PACKED ? frame_of(P, X.iid[p]) : frame_of(P);
+    const float cur_t = (F::DIFF || F::GENE || F::MEAN) ? conc_in[(size_t)p * NTF + t] : 0.f;
+    const float dif_t = F::DIFF ? G->diff[t] : 0.f;
+    const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
+    float nc_t = 0.f, ms_t = 0.f, sum = 0.f, part = 0.f;
+    uint32_t mcnt = 0, nf = 0;
+    int lastcell = -1;
+    uint32_t fmark = 0u;
+    const uint32_t base = scell[p] - (uint32_t)P.nadj;
+    uint32_t nh = 0;  // hits of the current segment
+    for (int cg = 0; cg < P.adjcnt; cg += 32) {
+        // this group's window cells: count, offset and running start, one per lane
+        const int ci = cg + (int)lane;
+        uint32_t cnt = 0, off = 0;
+        if (ci < P.adjcnt) {
+            const uint32_t cellc = base + (uint32_t)P.adj[ci];
+            const int cx = (int)(cellc % (uint32_t)P.res[0]);
+            const int cz = (int)((cellc / (uint32_t)P.res[0]) % (uint32_t)P.res[2]);
+            const int cy = (int)(cellc / ((uint32_t)P.res[0] * (uint32_t)P.res[2]));
+            if (!prune || cell_meets_box(frame, cx, cy, cz, ip.x - Rf, ip.x + Rf, ip.y - Rf, ip.y + Rf,
+                                         ip.z - Rf, ip.z + Rf)) {
+                cnt = count[cellc];
+                if (cnt) off = offset[cellc];
+            }
+        }
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int dd = 1; dd < 32; dd <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, dd);
+            if ((int)lane >= dd) incl += v;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t start = incl - cnt;
+        for (uint32_t b0 = 0; b0 < total; b0 += 128) {
+            // four chunks of 32 candidates in flight
+            float dq[4];
+            uint32_t qq[4], cc[4];
+            bool hit[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t k = b0 + (uint32_t)u * 32u + lane;
+                hit[u] = false;
+                dq[u] = 0.f;
+                qq[u] = 0u;
+                cc[u] = 0u;
+                // the cell holding candidate k: the last lane whose start is <= k
+                uint32_t lo = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const uint32_t st = __shfl_sync(0xffffffffu, start, (int)(lo + step) & 31);
+                    if (lo + step < 32 && st <= k) lo += step;
+                }
+                if (k < total) {
+                    const uint32_t sl = __shfl_sync(0xffffffffu, start, (int)lo);
+                    const uint32_t ol = __shfl_sync(0xffffffffu, off, (int)lo);
+                    qq[u] = ol + (k - sl);
+                    cc[u] = (uint32_t)cg + lo;
+                } else {
+                    __shfl_sync(0xffffffffu, start, (int)lo);
+                    __shfl_sync(0xffffffffu, off, (int)lo);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t k = b0 + (uint32_t)u * 32u + lane;
+                if (k < total) {
+                    const float4 jp = pos[qq[u]];
+                    const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+                    dq[u] = dx * dx + dy * dy + dz * dz;
+                    hit[u] = dq[u] < R2 && dq[u] > 0.f;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const unsigned ball = __ballot_sync(0xffffffffu, hit[u]);
+                const uint32_t nb = (uint32_t)__popc(ball);
+                if (nh + nb > (uint32_t)OVF_SEG) {  // segment full: take what it holds
+                    ovf_apply<FLAGS>(P, p, lane, t, flist, s_d, s_q, s_c, s_cj, nh,
+                                     lastcell, fmark, sum, part, nf, nc_t, ms_t, mcnt, dif_t, cur_t);
+                    nh = 0;
+                }
+                if (hit[u]) {
+                    const uint32_t slot = nh + (uint32_t)__popc(ball & ((1u << lane) - 1u));
+                    s_d[slot] = dq[u];
+                    s_q[slot] = qq[u];
+                    s_c[slot] = (uint8_t)cc[u];
+                    if (CONC && dq[u] < P.r2diff) {
+                        const float4* c4 = reinterpret_cast<const float4*>(conc_in + (size_t)qq[u] * NTF);
+#pragma unroll
+                        for (int k4 = 0; k4 < NTF / 4; k4++) s_cj[slot][k4] = c4[k4];
+                    }
+                }
+                nh += nb;
+            }
+        }
+    }
+    ovf_apply<FLAGS>(P, p, lane, t, flist, s_d, s_q, s_c, s_cj, nh, lastcell,
+                     fmark, sum, part, nf, nc_t, ms_t, mcnt, dif_t, cur_t);
+    if (F::DENS) sum += part;
+    float cur[NTF], nc[NTF], ms[NTF];
+#pragma unroll
+    for (int k = 0; k < NTF; k++) {
+        cur[k] = __shfl_sync(0xffffffffu, cur_t, k);
+        nc[k] = __shfl_sync(0xffffffffu, nc_t, k);
+        ms[k] = __shfl_sync(0xffffffffu, ms_t, k);
+    }
+    if (lane == 0) {
+        fcount[p] = nf;
+        dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press,
+                             invdens, X);
+    }
+    __syncwarp();
+}
+
+// Bytes of a warp's shared memory that ovf_particle takes.
+constexpr size_t OVF_SMEM = (size_t)OVF_SEG * (NTF * sizeof(float) + sizeof(float) + sizeof(uint32_t) + 1);
+
 // PACKED: packed instances (each particle's frame, genome and stiffness from its instance);
 // a separate instantiation so that a single system keeps its genome in the constant bank.
 template <int FLAGS, bool PACKED = false>
@@ -535,15 +724,15 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ offset,
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
     uint32_t* __restrict__ fcount, const uint32_t* __restrict__ nactive_p,
-    const uint32_t* __restrict__ work, uint32_t* __restrict__ ovf, uint32_t* __restrict__ ovf_count,
-    DensExtra X, bool prune) {
+    const uint32_t* __restrict__ work, DensExtra X, bool prune) {
     // prune: the positions are those of the last sort, so a window cell whose geometric box
     // misses the group's box holds no candidate; after positions moved, every cell is walked
     using F = DF<FLAGS>;
 #if MG_DENS_GENOME_BY_VALUE
     const DevGenome* __restrict__ G = &Gv;  // the parameter itself: reads go to the constant bank
 #endif
-    extern __shared__ uint32_t s_list[];  // [warps of the block][NL_CAP][32]
+    extern __shared__ __align__(16) uint32_t s_list[];  // [warps of the block][NL_ROWS][32]
+    static_assert(OVF_SMEM <= (size_t)NL_ROWS * 32 * sizeof(uint32_t), "overflow segment in a warp's list rows");
     // staged survivors, one array per coordinate so that four consecutive survivors' x (y, z,
     // sorted index) are one 128-bit load and pairs of them feed packed f32x2 operations
     __shared__ __align__(16) float s_sx[DENS_WARPS][32];
@@ -718,19 +907,33 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
             }
         }
     }
-    if (!act) return;
-    if (n > (uint32_t)NL_CAP) {
-        // more neighbours than the list holds (dense clumps): the overflow pass takes it
-        ovf[atomicAdd(ovf_count, 1u)] = p;
-        if (X.hlist) X.hcount[k] = UNDEF;
-        return;
+    const bool over = act && n > (uint32_t)NL_CAP;
+    if (act && !over) {
+        if (PACKED)  // the particle's own genome
+            dens_list_finish<FLAGS>(P, P.genomes + X.iid[p], p, ip, n, my, pos, conc_in, conc_out, genes,
+                                    press, invdens, flist, fcount, X, k);
+        else
+            dens_list_finish<FLAGS>(P, G, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens,
+                                    flist, fcount, X, k);
     }
-    if (PACKED)  // the particle's own genome
-        dens_list_finish<FLAGS>(P, P.genomes + X.iid[p], p, ip, n, my, pos, conc_in, conc_out, genes,
-                                press, invdens, flist, fcount, X, k);
-    else
-        dens_list_finish<FLAGS>(P, G, p, ip, n, my, pos, conc_in, conc_out, genes, press, invdens, flist,
-                                fcount, X, k);
+    // Lanes with more neighbours than the list holds (dense clumps): the warp takes them one at a
+    // time with the overflow walk, its list rows (read by now) holding the segments' hits.
+    unsigned ob = __ballot_sync(0xffffffffu, over);
+    if (!ob) return;
+    __syncwarp();
+    uint8_t* const scratch = reinterpret_cast<uint8_t*>(s_list + (size_t)w * NL_ROWS * 32);
+    float4 (*const o_cj)[NTF / 4] = reinterpret_cast<float4 (*)[NTF / 4]>(scratch);
+    float* const o_d = reinterpret_cast<float*>(scratch + OVF_SEG * NTF * sizeof(float));
+    uint32_t* const o_q = reinterpret_cast<uint32_t*>(scratch + OVF_SEG * (NTF + 1) * sizeof(float));
+    uint8_t* const o_c = scratch + OVF_SEG * (NTF + 2) * sizeof(float);
+    while (ob) {
+        const int src = __ffs(ob) - 1;
+        ob &= ob - 1;
+        ovf_particle<FLAGS, PACKED>(P, G, __shfl_sync(0xffffffffu, p, src), pos, conc_in, conc_out, genes,
+                                    scell, count, offset, press, invdens, flist, fcount, X, prune, o_cj,
+                                    o_d, o_q, o_c);
+    }
+    if (over && X.hlist) X.hcount[k] = UNDEF;  // the re-forming search walks its cells again
 }
 
 // ---- per-lane fine-cell search ----------------------------------------------------------------
@@ -839,55 +1042,6 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_fi
                             fcount, X, k0);
 }
 
-// ---- overflow pass ----------------------------------------------------------------------------
-// Particles queued by the searches (more neighbours than NL_CAP, only in dense clumps), one
-// warp per particle, in two phases that repeat over segments of OVF_SEG hits:
-//  collect : the window cells (in the reference order, 32 at a time, one per lane) form one
-//            stream of candidates; each lane takes one candidate per chunk (its cell found by a
-//            binary search over the cells' running counts), several chunks in flight, and the
-//            hits are compacted in order into shared memory with their distance, window-cell
-//            index and concentrations;
-//  apply   : the hits are taken in that order by every lane: the density partial sum of each
-//            cell, species t (mod 16) of the diffusion and neighbour sums in lane t with the
-//            one-thread walk's expression and order, the force list in lane 0.
-// Lane 0 then runs the common epilogue.
-constexpr int OVF_SEG = 64;
-
-// Takes a segment's hits in order (the apply phase of the overflow pass).
-template <int FLAGS>
-__device__ __forceinline__ void ovf_apply(const DevParams& P, uint32_t p, uint32_t lane, uint32_t t,
-                                          uint32_t* __restrict__ flist, const float* sd,
-                                          const uint32_t* sq, const uint8_t* sc, const float4 (*scj)[NTF / 4],
-                                          uint32_t nh, int& lastcell, uint32_t& fmark, float& sum, float& part,
-                                          uint32_t& nf, float& nc_t, float& ms_t, uint32_t& mcnt,
-                                          float dif_t, float cur_t) {
-    using F = DF<FLAGS>;
-    __syncwarp();
-    for (uint32_t h = 0; h < nh; h++) {
-        const float d = sd[h];
-        const int c = sc[h];
-        if (c != lastcell) {  // first hit of the next cell: flush the previous partial
-            sum += part;
-            part = 0.f;
-            lastcell = c;
-            fmark = FLIST_CELL_START;
-        }
-        if (d < 1.f) {
-            if (lane == 0 && nf < (uint32_t)FL_CAP) flist[(size_t)nf * P.cap + p] = sq[h] | fmark;
-            fmark = 0u;
-            nf++;
-        }
-        if (F::DENS && d < P.r2) part += wendland_term(d, P.sr, P.sr_inv_exact);
-        if ((F::DIFF || F::MEAN) && d < P.r2diff) {
-            const float cj = reinterpret_cast<const float*>(scj[h])[t];
-            if (F::MEAN) ms_t += cj;
-            if (F::DIFF && dif_t != 0.f) nc_t += (dif_t * ((P.r2diff - d) * P.d2)) * (cj - cur_t);
-            mcnt++;
-        }
-    }
-    __syncwarp();
-}
-
 template <int FLAGS, bool PACKED = false>
 __global__ void __launch_bounds__(256, 1) k_dens_ovf(
     DevParams P, const DevGenome* __restrict__ G0, const float4* __restrict__ pos,
@@ -897,140 +1051,19 @@ __global__ void __launch_bounds__(256, 1) k_dens_ovf(
     float* __restrict__ press, float* __restrict__ invdens, uint32_t* __restrict__ flist,
     uint32_t* __restrict__ fcount, const uint32_t* __restrict__ ovf,
     const uint32_t* __restrict__ ovf_count, DensExtra X, bool prune) {
-    // prune: positions are those of the last sort, so a window cell whose geometric box misses
-    // the particle's search box holds no neighbour
-    using F = DF<FLAGS>;
-    constexpr bool CONC = F::DIFF || F::MEAN;
     __shared__ float4 s_cj[256 / 32][OVF_SEG][NTF / 4];  // concentrations of the segment's hits
     __shared__ float s_d[256 / 32][OVF_SEG];
     __shared__ uint32_t s_q[256 / 32][OVF_SEG];
     __shared__ uint8_t s_c[256 / 32][OVF_SEG];
-    const uint32_t lane = threadIdx.x & 31u, t = lane & 15u, wl = threadIdx.x >> 5;
+    const uint32_t wl = threadIdx.x >> 5;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     uint32_t nq = *ovf_count;
     if (nq > P.cap) nq = P.cap;
-    float R2 = 1.f;
-    if (F::DENS) R2 = fmaxf(R2, P.r2);
-    if (CONC) R2 = fmaxf(R2, P.r2diff);
-    const float Rf = sqrtf(R2) * 1.0001f + 1e-3f;  // conservative search-box half width
-    for (uint32_t e = gw; e < nq; e += nw) {
-        const uint32_t p = ovf[e];
-        const float4 ip = pos[p];
-        const DevGenome* __restrict__ G = PACKED ? P.genomes + X.iid[p] : G0;
-        const CellFrame frame = PACKED ? frame_of(P, X.iid[p]) : frame_of(P);
-        const float cur_t = (F::DIFF || F::GENE || F::MEAN) ? conc_in[(size_t)p * NTF + t] : 0.f;
-        const float dif_t = F::DIFF ? G->diff[t] : 0.f;
-        const bool plain = !F::JUDGE || judged_lane(X, p, genes[p]);
-        float nc_t = 0.f, ms_t = 0.f, sum = 0.f, part = 0.f;
-        uint32_t mcnt = 0, nf = 0;
-        int lastcell = -1;
-        uint32_t fmark = 0u;
-        const uint32_t base = scell[p] - (uint32_t)P.nadj;
-        uint32_t nh = 0;  // hits of the current segment
-        for (int cg = 0; cg < P.adjcnt; cg += 32) {
-            // this group's window cells: count, offset and running start, one per lane
-            const int ci = cg + (int)lane;
-            uint32_t cnt = 0, off = 0;
-            if (ci < P.adjcnt) {
-                const uint32_t cellc = base + (uint32_t)P.adj[ci];
-                const int cx = (int)(cellc % (uint32_t)P.res[0]);
-                const int cz = (int)((cellc / (uint32_t)P.res[0]) % (uint32_t)P.res[2]);
-                const int cy = (int)(cellc / ((uint32_t)P.res[0] * (uint32_t)P.res[2]));
-                if (!prune || cell_meets_box(frame, cx, cy, cz, ip.x - Rf, ip.x + Rf, ip.y - Rf, ip.y + Rf,
-                                             ip.z - Rf, ip.z + Rf)) {
-                    cnt = count[cellc];
-                    if (cnt) off = offset[cellc];
-                }
-            }
-            uint32_t incl = cnt;
-#pragma unroll
-            for (int dd = 1; dd < 32; dd <<= 1) {
-                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, dd);
-                if ((int)lane >= dd) incl += v;
-            }
-            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-            const uint32_t start = incl - cnt;
-            for (uint32_t b0 = 0; b0 < total; b0 += 128) {
-                // four chunks of 32 candidates in flight
-                float dq[4];
-                uint32_t qq[4], cc[4];
-                bool hit[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const uint32_t k = b0 + (uint32_t)u * 32u + lane;
-                    hit[u] = false;
-                    dq[u] = 0.f;
-                    qq[u] = 0u;
-                    cc[u] = 0u;
-                    // the cell holding candidate k: the last lane whose start is <= k
-                    uint32_t lo = 0;
-#pragma unroll
-                    for (int step = 16; step > 0; step >>= 1) {
-                        const uint32_t st = __shfl_sync(0xffffffffu, start, (int)(lo + step) & 31);
-                        if (lo + step < 32 && st <= k) lo += step;
-                    }
-                    if (k < total) {
-                        const uint32_t sl = __shfl_sync(0xffffffffu, start, (int)lo);
-                        const uint32_t ol = __shfl_sync(0xffffffffu, off, (int)lo);
-                        qq[u] = ol + (k - sl);
-                        cc[u] = (uint32_t)cg + lo;
-                    } else {
-                        __shfl_sync(0xffffffffu, start, (int)lo);
-                        __shfl_sync(0xffffffffu, off, (int)lo);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const uint32_t k = b0 + (uint32_t)u * 32u + lane;
-                    if (k < total) {
-                        const float4 jp = pos[qq[u]];
-                        const float dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
-                        dq[u] = dx * dx + dy * dy + dz * dz;
-                        hit[u] = dq[u] < R2 && dq[u] > 0.f;
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const unsigned ball = __ballot_sync(0xffffffffu, hit[u]);
-                    const uint32_t nb = (uint32_t)__popc(ball);
-                    if (nh + nb > (uint32_t)OVF_SEG) {  // segment full: take what it holds
-                        ovf_apply<FLAGS>(P, p, lane, t, flist, s_d[wl], s_q[wl], s_c[wl], s_cj[wl], nh,
-                                         lastcell, fmark, sum, part, nf, nc_t, ms_t, mcnt, dif_t, cur_t);
-                        nh = 0;
-                    }
-                    if (hit[u]) {
-                        const uint32_t slot = nh + (uint32_t)__popc(ball & ((1u << lane) - 1u));
-                        s_d[wl][slot] = dq[u];
-                        s_q[wl][slot] = qq[u];
-                        s_c[wl][slot] = (uint8_t)cc[u];
-                        if (CONC && dq[u] < P.r2diff) {
-                            const float4* c4 = reinterpret_cast<const float4*>(conc_in + (size_t)qq[u] * NTF);
-#pragma unroll
-                            for (int k4 = 0; k4 < NTF / 4; k4++) s_cj[wl][slot][k4] = c4[k4];
-                        }
-                    }
-                    nh += nb;
-                }
-            }
-        }
-        ovf_apply<FLAGS>(P, p, lane, t, flist, s_d[wl], s_q[wl], s_c[wl], s_cj[wl], nh, lastcell,
-                         fmark, sum, part, nf, nc_t, ms_t, mcnt, dif_t, cur_t);
-        if (F::DENS) sum += part;
-        float cur[NTF], nc[NTF], ms[NTF];
-#pragma unroll
-        for (int k = 0; k < NTF; k++) {
-            cur[k] = __shfl_sync(0xffffffffu, cur_t, k);
-            nc[k] = __shfl_sync(0xffffffffu, nc_t, k);
-            ms[k] = __shfl_sync(0xffffffffu, ms_t, k);
-        }
-        if (lane == 0) {
-            fcount[p] = nf;
-            dens_epilogue<FLAGS>(P, G, p, sum, nc, ms, mcnt, cur, plain, genes, conc_out, press,
-                                 invdens, X);
-        }
-        __syncwarp();
-    }
+    for (uint32_t e = gw; e < nq; e += nw)
+        ovf_particle<FLAGS, PACKED>(P, G0, ovf[e], pos, conc_in, conc_out, genes, scell, count, offset,
+                                    press, invdens, flist, fcount, X, prune, s_cj[wl], s_d[wl], s_q[wl],
+                                    s_c[wl]);
 }
 
 // The per-lane lists take 48 KB of dynamic shared memory next to the static survivor buffers,
@@ -1074,17 +1107,10 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
                                                              cur.genes, s.scell, s.count,         \
                                                              s.offset, cur.press, cur.invdens,        \
                                                              s.flist, s.fcount, s.counters + 3,   \
-                                                             s.work, s.ovf, s.counters + 6, X,    \
-                                                             prune);                              \
-        k_dens_ovf<F, PK><<<(uint32_t)num_sms * 4, 256, 0, st>>>(P, G, cur.pos, conc_in, conc_out, \
-                                                             cur.genes, s.scell, s.count,         \
-                                                             s.offset, cur.press, cur.invdens,        \
-                                                             s.flist, s.fcount, s.ovf,            \
-                                                             s.counters + 6, X, prune);           \
+                                                             s.work, X, prune);                   \
         return;
 #define MG_DENSW_CASE(F) MG_DENSW_CASE_P(F, false)
 #define MG_DENSW_CASE_PACKED(F) MG_DENSW_CASE_P(F, true)
-        cudaMemsetAsync(s.counters + 6, 0, sizeof(uint32_t), st);
         if (cur.iid) {
             switch (flags) { MG_DENS_PACKED_SETS(MG_DENSW_CASE_PACKED) default: break; }
         } else {
