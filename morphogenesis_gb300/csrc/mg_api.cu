@@ -436,9 +436,7 @@ float* conc_of(mg_system* h, int k) { return h->set[k].conc; }
 void enqueue_insert_rank(mg_system* h, bool prof) {
     const DevParams& P = h->P;
     cudaStream_t st = h->stream;
-    cudaMemsetAsync(h->s.count, 0, sizeof(uint32_t) * P.cells, st);
-    cudaMemsetAsync(h->s.scan_status, 0, sizeof(unsigned long long) * scan_status_words(P.cells), st);
-    cudaMemsetAsync(h->s.counters, 0, 2 * sizeof(uint32_t), st);
+    launch_clear_bins(P, h->s, h->num_sms, st);
     { Mark m(h, prof, "insert"); launch_insert(P, h->set[h->cur], h->s, h->search != 2, st); }
     { Mark m(h, prof, "scan"); launch_scan(h->s.count, h->s.offset, P.cells, h->s.scan_status,
                                            h->s.counters, h->s.counters + 3, h->s.counters + 2, st); }

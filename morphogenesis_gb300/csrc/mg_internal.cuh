@@ -237,6 +237,7 @@ struct Scratch {
 cudaError_t physics_init();  // per-kernel attributes, once per device before the first launch
 // warp_order: sub-cell codes ordered for the warp-cooperative searches (x-first slabs); false
 // gives the Morton codes the per-lane fine-cell search reads as positions
+void launch_clear_bins(const DevParams& P, const Scratch& s, int num_sms, cudaStream_t st);
 void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, bool warp_order,
                    cudaStream_t st);
 void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long long* status,

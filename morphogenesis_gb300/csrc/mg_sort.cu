@@ -128,6 +128,25 @@ __global__ void __launch_bounds__(256) k_insert(DevParams P, const float4* __res
     }
 }
 
+// Zeroes the bin counts, the scan's tile status words and the sort's first two counters
+// before the bin pass: one kernel instead of three memsets.
+__global__ void __launch_bounds__(256) k_clear_bins(uint32_t* __restrict__ count, uint32_t cells,
+                                                    unsigned long long* __restrict__ status,
+                                                    uint32_t nstatus, uint32_t* __restrict__ counters) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    const uint32_t n4 = cells / 4u;  // count is 256-byte aligned
+    uint4* c4 = reinterpret_cast<uint4*>(count);
+    for (uint32_t k = i; k < n4; k += stride) c4[k] = make_uint4(0u, 0u, 0u, 0u);
+    for (uint32_t k = n4 * 4u + i; k < cells; k += stride) count[k] = 0u;
+    for (uint32_t k = i; k < nstatus; k += stride) status[k] = 0ull;
+    if (i < 2u) counters[i] = 0u;
+}
+
+void launch_clear_bins(const DevParams& P, const Scratch& s, int num_sms, cudaStream_t st) {
+    k_clear_bins<<<(uint32_t)num_sms * 4u, 256, 0, st>>>(s.count, P.cells, s.scan_status,
+                                                        (uint32_t)scan_status_words(P.cells), s.counters);
+}
+
 void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, bool warp_order,
                    cudaStream_t st) {
     uint32_t blocks = (P.cap + 255) / 256;
