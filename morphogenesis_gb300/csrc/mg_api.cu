@@ -659,8 +659,12 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
             }
     if (early) cudaEventRecord(ev[4], A);
     flush_motion(h, prof);
+    // without remodelling the integration follows the force pass and adds the incoming-bond
+    // reactions itself (one kernel fewer)
+    const bool in_advance = !remodel;
     if (flags & MG_STEP_PHYSICS) {
-        { Mark m(h, prof, "force"); launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream); }
+        { Mark m(h, prof, "force");
+          launch_force(h->P, h->set[h->cur], h->s, h->flist_valid, h->stream, in_advance); }
     }
     if (remodel) {  // Run2Remodelling, after the gene action and before AdvanceCL
         Mark m(h, prof, "remodel");
@@ -673,7 +677,8 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
     }
     if (flags & MG_STEP_PHYSICS) {
         { Mark m(h, prof, "advance");
-          launch_advance(h->P, h->set[h->cur], h->s, !remodel, h->stream, (flags & MG_STEP_SPECIAL) != 0); }
+          launch_advance(h->P, h->set[h->cur], h->s, !remodel, h->stream, (flags & MG_STEP_SPECIAL) != 0,
+                         in_advance); }
         h->flist_valid = false;
     }
     if (io) {
@@ -686,11 +691,13 @@ void enqueue_step(mg_system* h, uint32_t flags, bool prof, const IoPlan* io = nu
 }
 
 int kernels_per_step(const mg_system* h, uint32_t flags) {
-    int n = 6;  // insert, scan, place, cellsort, cellsort_big, gather
-    // density pass (+ its overflow pass with the warp search)
-    if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE)) n += h->search ? 2 : 1;
+    int n = 7;  // clear, insert, scan, place, cellsort, cellsort_big, gather
+    // density pass (+ its overflow pass with the fine-cell search)
+    if (flags & (MG_STEP_PHYSICS | MG_STEP_GENES | MG_STEP_SURROGATE)) n += h->search == 2 ? 2 : 1;
     if (flags & MG_STEP_SURROGATE) n += 1;
-    if (flags & MG_STEP_PHYSICS) n += 3;  // force (two kernels), advance
+    const bool remodel = (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) != 0;
+    // force (two kernels, the second folded into the integration without remodelling), advance
+    if (flags & MG_STEP_PHYSICS) n += remodel ? 3 : 2;
     if (flags & (MG_STEP_REMODEL | MG_STEP_BOND_CHANGES)) n += (flags & MG_STEP_PHYSICS) ? 4 : 3;
     if (flags & MG_STEP_BOND_CHANGES) n += 1;
     return n;

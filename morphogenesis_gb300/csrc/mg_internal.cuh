@@ -292,8 +292,10 @@ void launch_dens(const DevParams& P, const DevGenome* G, const DevGenome& Gh, co
                  float* conc_out, const Scratch& s, int flags, int search, int num_sms,
                  cudaStream_t st, const DensExtra* extra = nullptr);
 
+// incoming_in_advance: the integration follows directly and adds the incoming-bond reactions
+// itself (launch_advance with incoming), so k_force_in is not launched
 void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool use_list,
-                  cudaStream_t st);
+                  cudaStream_t st, bool incoming_in_advance = false);
 void launch_apply_breaks(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st);
 // re-forming of broken bonds on the sorted state, breaks already applied (D5)
 // computeBondChanges over the living particles; steps = steps_per_InnerPhysicalLoop
@@ -313,9 +315,11 @@ void launch_change_lists(const DevParams& P, const Carried& cur, const Cold& col
 void launch_remodel(const DevParams& P, const DevGenome* G, const Carried& cur, const Cold& cold,
                     const Scratch& s, bool from_changes, bool prune, const uint32_t* hcount,
                     const uint32_t* hlist, cudaStream_t st);
-// special: externalActuation / fixedParticles for genes 12 / 11 (SpecialParticlesCL)
+// special: externalActuation / fixedParticles for genes 12 / 11 (SpecialParticlesCL);
+// incoming: add the incoming-bond reactions to the force first (after launch_force with
+// incoming_in_advance)
 void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_breaks,
-                    cudaStream_t st, bool special = false);
+                    cudaStream_t st, bool special = false, bool incoming = false);
 
 // ---- import/export between the reference layouts and the device layout -------------------
 // FCONC rows [cap][16] <-> species-major [16][cap]

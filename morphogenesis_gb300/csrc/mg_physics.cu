@@ -1320,14 +1320,11 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force(DevParams P, Car
 // Second force kernel: the reactions of incoming bonds, in slot order (the gather form of the
 // atomicAdd at cuda:3311-3313), added to the first kernel's sum.  An owner's stored term is the
 // one its own-bond loop evaluated for this particle as partner: the same arguments, the same
-// bits as evaluating it here.
-__global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force_in(uint32_t cap, const uint32_t* __restrict__ pidx,
-                                                  const float4* __restrict__ bterm,
-                                                  float4* __restrict__ force,
-                                                  const uint32_t* __restrict__ nactive_p) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nact = *nactive_p;
-    if (p >= nact) return;
+// bits as evaluating it here.  Run by k_force_in, or at the top of the integration when it
+// follows the force pass directly.
+__device__ __forceinline__ float4 add_incoming(uint32_t cap, const uint32_t* __restrict__ pidx,
+                                               const float4* __restrict__ bterm,
+                                               const float4* __restrict__ force, uint32_t p, uint32_t nact) {
     const uint4* pi = reinterpret_cast<const uint4*>(pidx + (size_t)p * 12);
     uint32_t in[12];
 #pragma unroll
@@ -1351,15 +1348,25 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force_in(uint32_t cap,
         f.y = f.y + t[b].y;
         f.z = f.z + t[b].z;
     }
-    force[p] = f;
+    return f;
+}
+
+__global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force_in(uint32_t cap, const uint32_t* __restrict__ pidx,
+                                                  const float4* __restrict__ bterm,
+                                                  float4* __restrict__ force,
+                                                  const uint32_t* __restrict__ nactive_p) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nact = *nactive_p;
+    if (p >= nact) return;
+    force[p] = add_incoming(cap, pidx, bterm, force, p, nact);
 }
 
 void launch_force(const DevParams& P, const Carried& cur, const Scratch& s, bool use_list,
-                  cudaStream_t st) {
+                  cudaStream_t st, bool incoming_in_advance) {
     const uint32_t nt = (uint32_t)P.force_threads, blocks = (P.cap + nt - 1) / nt;
     k_force<<<blocks, nt, 0, st>>>(P, cur, s.scell, s.count, s.offset, cur.press, cur.invdens, s.flist,
                                     s.fcount, use_list ? 1 : 0, s.force, s.bterm, s.brk, s.counters + 3);
-    k_force_in<<<blocks, nt, 0, st>>>(P.cap, cur.pidx, s.bterm, s.force, s.counters + 3);
+    if (!incoming_in_advance) k_force_in<<<blocks, nt, 0, st>>>(P.cap, cur.pidx, s.bterm, s.force, s.counters + 3);
 }
 
 // Broken bonds get rest length 0 (cuda:3315-3317).  The force kernel records the breaks in
@@ -1421,17 +1428,28 @@ __device__ __forceinline__ float* time_slot(uint32_t* counters, uint32_t step) {
     return reinterpret_cast<float*>(counters + 7 + (step & 1u));
 }
 
-template <bool APPLY_BRK, bool SPECIAL>
+// IN: the force pass left the incoming-bond reactions to this kernel (k_force_in's sum, written
+// back to the force buffer, then integrated).
+template <bool APPLY_BRK, bool SPECIAL, bool IN>
 __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_advance(DevParams P, Carried C,
-                                                 const float4* __restrict__ force,
+                                                 float4* __restrict__ force,
+                                                 const float4* __restrict__ bterm,
                                                  const uint32_t* __restrict__ brk,
                                                  uint32_t* __restrict__ counters) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t step = counters[5];
     const float time = *time_slot(counters, step);
     if (p == 0) *time_slot(counters, step + 1u) = time + P.dt;  // AdvanceTime (fluid_system.cpp:2016)
-    if (p >= counters[3]) return;
-    const float4 pos = C.pos[p], ve = C.veval[p], f = force[p];
+    const uint32_t nact = counters[3];
+    if (p >= nact) return;
+    float4 f;
+    if (IN) {
+        f = add_incoming(P.cap, C.pidx, bterm, force, p, nact);
+        force[p] = f;
+    } else {
+        f = force[p];
+    }
+    const float4 pos = C.pos[p], ve = C.veval[p];
     // the walls: the system's box, or a packed instance's own
     const float* bmin = C.iid ? P.inst[C.iid[p]].bmin : P.bmin;
     const float* bmax = C.iid ? P.inst[C.iid[p]].bmax : P.bmax;
@@ -1487,17 +1505,26 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_advance(DevParams P, C
     }
 }
 
-void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_brk,
-                    cudaStream_t st, bool special) {
+template <bool APPLY_BRK, bool SPECIAL>
+static void launch_advance_as(const DevParams& P, const Carried& cur, const Scratch& s, cudaStream_t st,
+                              bool incoming) {
     const uint32_t nt = (uint32_t)P.advance_threads, blocks = (P.cap + nt - 1) / nt;
-    if (apply_brk && special)
-        k_advance<true, true><<<blocks, nt, 0, st>>>(P, cur, s.force, s.brk, s.counters);
-    else if (apply_brk)
-        k_advance<true, false><<<blocks, nt, 0, st>>>(P, cur, s.force, s.brk, s.counters);
-    else if (special)
-        k_advance<false, true><<<blocks, nt, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+    if (incoming)
+        k_advance<APPLY_BRK, SPECIAL, true><<<blocks, nt, 0, st>>>(P, cur, s.force, s.bterm, s.brk, s.counters);
     else
-        k_advance<false, false><<<blocks, nt, 0, st>>>(P, cur, s.force, s.brk, s.counters);
+        k_advance<APPLY_BRK, SPECIAL, false><<<blocks, nt, 0, st>>>(P, cur, s.force, s.bterm, s.brk, s.counters);
+}
+
+void launch_advance(const DevParams& P, const Carried& cur, const Scratch& s, bool apply_brk,
+                    cudaStream_t st, bool special, bool incoming) {
+    if (apply_brk && special)
+        launch_advance_as<true, true>(P, cur, s, st, incoming);
+    else if (apply_brk)
+        launch_advance_as<true, false>(P, cur, s, st, incoming);
+    else if (special)
+        launch_advance_as<false, true>(P, cur, s, st, incoming);
+    else
+        launch_advance_as<false, false>(P, cur, s, st, incoming);
 }
 
 }  // namespace mg
