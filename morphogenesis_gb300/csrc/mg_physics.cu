@@ -41,10 +41,7 @@ constexpr int DENS_WARPS = MG_DENS_WARPS;  // warps per block of the warp-cooper
 // rows of a lane's neighbour list in shared memory: the list appends are branch-free (every
 // survivor is written at the next free row, only hits advance it); a batch of four survivors
 // starts at row min(n, NL_CAP), so three spare rows take the writes past a full list
-#ifndef MG_DENS_WP
-#define MG_DENS_WP 1
-#endif
-constexpr int NL_ROWS = NL_CAP + (MG_DENS_WP ? 4 : 1);
+constexpr int NL_ROWS = NL_CAP + 4;
 
 // ---- per-neighbour terms ---------------------------------------------------------------
 // sr_inv_exact: 1 / sr when sr is a power of two, where the quotient r / sr is the product
@@ -850,7 +847,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                         // their distances two at a time in packed f32x2 operations (the same
                         // fused expression per component as approx_dsq: list membership only);
                         // every survivor is written at the lane's next free row and only hits
-                        // advance it (no divergent branch; a full list writes to the spare row).
+                        // advance it (no divergent branch; a full list writes to a spare row).
                         const float2 m1 = make_float2(-1.f, -1.f);
                         const float2 px = make_float2(ip.x, ip.x), py = make_float2(ip.y, ip.y),
                                      pz = make_float2(ip.z, ip.z);
@@ -870,7 +867,6 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                             const float2 d23 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
                             const float d[4] = {d01.x, d01.y, d23.x, d23.y};
                             const uint32_t qi[4] = {Q.x, Q.y, Q.z, Q.w};
-#if MG_DENS_WP
                             // the batch's row pointer advances by a row per hit; the hits are
                             // counted from it once per batch
                             uint32_t* const wp0 = my + min(n, (uint32_t)NL_CAP) * 32;
@@ -883,15 +879,6 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                                 wp += hit ? 32 : 0;
                             }
                             n += (uint32_t)(wp - wp0) >> 5;
-#else
-#pragma unroll
-                            for (int u = 0; u < 4; u++) {
-                                const bool hit = d[u] < R2s && d[u] > 0.f;
-                                my[min(n, (uint32_t)NL_CAP) * 32] = qi[u] | mark;
-                                mark = hit ? 0u : mark;
-                                n += hit ? 1u : 0u;
-                            }
-#endif
                         }
                         for (; tt < ns; tt++) {
                             const float4 sp = make_float4(s_sx[w][tt], s_sy[w][tt], s_sz[w][tt], 0.f);
