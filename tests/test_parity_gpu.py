@@ -211,8 +211,8 @@ def test_crowded_cell_orders(built, count):
     g, o = pair(d, n)
     g.Run(1, A.STEP_GENES); o.step(1, A.STEP_GENES)
     compare(g, o, bufs_float=[A.FPOS, A.FCONC])
-    # a full step: every particle of the crowded cell overflows its list and takes the overflow
-    # pass (density, diffusion and the fluid-force list)
+    # a full step: every particle of the crowded cell overflows its list and is walked by its
+    # warp (density, diffusion and the fluid-force list)
     g1, o1 = pair(d, n)
     g1.Run(1, A.STEP_DEFAULT); o1.step(1, A.STEP_DEFAULT)
     assert compare(g1, o1), "crowded cell: full step differs from the oracle"
