@@ -538,7 +538,7 @@ __device__ __forceinline__ void dens_list_finish(
 // Lane 0 then runs the common epilogue.
 constexpr int OVF_SEG = 64;
 
-// Takes a segment's hits in order (the apply phase of the overflow pass).
+// Takes a segment's hits in order (the apply phase of the overflow walk).
 template <int FLAGS>
 __device__ __forceinline__ void ovf_apply(const DevParams& P, uint32_t p, uint32_t lane, uint32_t t,
                                           uint32_t* __restrict__ flist, const float* sd,
