@@ -120,12 +120,10 @@ __device__ __forceinline__ void store_row16(float* row, const float (&v)[NTF]) {
 // neighbour sum (ms, when MEAN).  (dif[t] * cc) * (cq[t] - cur[t]) is the reference term; with
 // one common nonzero rate the product dif[t] * cc is the same value for every species.
 template <bool DIFF, bool MEAN>
-__device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], const float* __restrict__ dif,
-                                           const float (&cur)[NTF], const float* conc, uint32_t q,
-                                           float cc, bool uniform, bool diffuse, float unit) {
+__device__ __forceinline__ void conc_terms_row(float (&nc)[NTF], float (&ms)[NTF], const float* __restrict__ dif,
+                                               const float (&cur)[NTF], const float (&cj)[NTF],
+                                               float cc, bool uniform, bool diffuse, float unit) {
     if (!DIFF && !MEAN) return;
-    float cj[NTF];
-    load_row16(conc + (size_t)q * NTF, cj);
 #if MG_F32X2
     // Packed pairs of species (f32x2: two IEEE single operations, each rounded as the scalar
     // one) where no product feeds a sum: the compiler may fuse a packed multiply into the packed
@@ -188,6 +186,17 @@ __device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], c
                 if (dif[t] != 0.f) nc[t] += (dif[t] * cc) * (cj[t] - cur[t]);
         }
     }
+}
+
+// The same, loading neighbour q's row first.
+template <bool DIFF, bool MEAN>
+__device__ __forceinline__ void conc_terms(float (&nc)[NTF], float (&ms)[NTF], const float* __restrict__ dif,
+                                           const float (&cur)[NTF], const float* conc, uint32_t q,
+                                           float cc, bool uniform, bool diffuse, float unit) {
+    if (!DIFF && !MEAN) return;
+    float cj[NTF];
+    load_row16(conc + (size_t)q * NTF, cj);
+    conc_terms_row<DIFF, MEAN>(nc, ms, dif, cur, cj, cc, uniform, diffuse, unit);
 }
 
 
@@ -493,6 +502,10 @@ __device__ __forceinline__ void dens_list_finish(
         for (uint32_t k = 0; k < n; k++) {
             const uint32_t e = my[k * 32];
             const uint32_t q = checked(P, e & ~LIST_CELL_START, P.cap);
+            // the neighbour's row is loaded with its position (both depend on q alone), so the
+            // two loads overlap; entries beyond the diffusion radius leave it unused
+            float cj[NTF];
+            if (F::DIFF || F::MEAN) load_row16(conc_in + (size_t)q * NTF, cj);
             const float4 jp = pos[q];
             if (e & LIST_CELL_START) {  // first neighbour of the next cell:
                 if (F::DENS) {          // flush the previous cell's partial sum
@@ -510,8 +523,8 @@ __device__ __forceinline__ void dens_list_finish(
             }
             if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr, P.sr_inv_exact);
             if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
-                conc_terms<F::DIFF, F::MEAN>(nc, ms, dif, cur, conc_in, q, (P.r2diff - dsq) * P.d2,
-                                             G->uniform != 0, true, P.unit);
+                conc_terms_row<F::DIFF, F::MEAN>(nc, ms, dif, cur, cj, (P.r2diff - dsq) * P.d2,
+                                                 G->uniform != 0, true, P.unit);
                 mcnt++;
                 if (X.hlist) X.hlist[(size_t)nh++ * P.cap + slot] = q;  // nh <= n <= NL_CAP
             }
@@ -846,8 +859,9 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                         // made again when the list is evaluated.  Four survivors per iteration,
                         // their distances two at a time in packed f32x2 operations (the same
                         // fused expression per component as approx_dsq: list membership only);
-                        // every survivor is written at the lane's next free row and only hits
-                        // advance it (no divergent branch; a full list writes to a spare row).
+                        // a hit is written at the lane's next free row by a predicated store
+                        // (no divergent branch, no shared-memory store for the misses; a full
+                        // list writes to a spare row).
                         const float2 m1 = make_float2(-1.f, -1.f);
                         const float2 px = make_float2(ip.x, ip.x), py = make_float2(ip.y, ip.y),
                                      pz = make_float2(ip.z, ip.z);
@@ -874,7 +888,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
 #pragma unroll
                             for (int u = 0; u < 4; u++) {
                                 const bool hit = d[u] < R2s && d[u] > 0.f;
-                                *wp = qi[u] | mark;
+                                if (hit) *wp = qi[u] | mark;
                                 mark = hit ? 0u : mark;
                                 wp += hit ? 32 : 0;
                             }
@@ -884,7 +898,7 @@ __global__ void __launch_bounds__(DENS_WARPS * 32, MG_DENS_MIN_BLOCKS) k_dens_wa
                             const float4 sp = make_float4(s_sx[w][tt], s_sy[w][tt], s_sz[w][tt], 0.f);
                             const float d = approx_dsq(ip, sp);
                             const bool hit = d < R2s && d > 0.f;
-                            my[min(n, (uint32_t)NL_CAP) * 32] = s_sq[w][tt] | mark;
+                            if (hit) my[min(n, (uint32_t)NL_CAP) * 32] = s_sq[w][tt] | mark;
                             mark = hit ? 0u : mark;
                             n += hit ? 1u : 0u;
                         }
