@@ -503,9 +503,11 @@ __device__ __forceinline__ void dens_list_finish(
             const uint32_t e = my[k * 32];
             const uint32_t q = checked(P, e & ~LIST_CELL_START, P.cap);
             // the neighbour's row is loaded with its position (both depend on q alone), so the
-            // two loads overlap; entries beyond the diffusion radius leave it unused
+            // two loads overlap; entries beyond the diffusion radius leave it unused.  Not in
+            // the surrogate's forms, whose 16 neighbour sums leave no registers for it (spills)
+            constexpr bool EARLY = F::DIFF && !F::MEAN;
             float cj[NTF];
-            if (F::DIFF || F::MEAN) load_row16(conc_in + (size_t)q * NTF, cj);
+            if (EARLY) load_row16(conc_in + (size_t)q * NTF, cj);
             const float4 jp = pos[q];
             if (e & LIST_CELL_START) {  // first neighbour of the next cell:
                 if (F::DENS) {          // flush the previous cell's partial sum
@@ -523,6 +525,7 @@ __device__ __forceinline__ void dens_list_finish(
             }
             if (F::DENS && dsq < P.r2 && dsq > 0.f) part += wendland_term(dsq, P.sr, P.sr_inv_exact);
             if ((F::DIFF || F::MEAN) && dsq < P.r2diff && dsq > 0.f) {
+                if (!EARLY) load_row16(conc_in + (size_t)q * NTF, cj);
                 conc_terms_row<F::DIFF, F::MEAN>(nc, ms, dif, cur, cj, (P.r2diff - dsq) * P.d2,
                                                  G->uniform != 0, true, P.unit);
                 mcnt++;
