@@ -1280,9 +1280,15 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_force(DevParams P, Car
                 fluid_term(P, ip, iv, ipress, idens, jp, jv, jpress, jdens, dsq, dx, dy, dz, cx, cy, cz);
             };
             uint32_t k = 0;
-            // two neighbours per iteration, so their gathers are in flight together
+            // two neighbours per iteration, so their gathers are in flight together, and the
+            // next two list entries loaded one iteration ahead
+            uint32_t e0n = nf >= 2 ? flist[p] : 0u, e1n = nf >= 2 ? flist[(size_t)cap + p] : 0u;
             for (; k + 2 <= nf; k += 2) {
-                const uint32_t e0 = flist[(size_t)k * cap + p], e1 = flist[(size_t)(k + 1) * cap + p];
+                const uint32_t e0 = e0n, e1 = e1n;
+                if (k + 4 <= nf) {
+                    e0n = flist[(size_t)(k + 2) * cap + p];
+                    e1n = flist[(size_t)(k + 3) * cap + p];
+                }
                 const uint32_t q0 = checked(P, e0 & ~FLIST_CELL_START, cap), q1 = checked(P, e1 & ~FLIST_CELL_START, cap);
                 const float4 jp0 = C.pos[q0], jp1 = C.pos[q1], jv0 = C.veval[q0], jv1 = C.veval[q1];
                 const float pr0 = press[q0], pr1 = press[q1], dn0 = invdens[q0], dn1 = invdens[q1];
