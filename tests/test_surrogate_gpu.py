@@ -146,8 +146,9 @@ def test_training_and_judged_surrogate_step(built):
     judged, handed, worst = S.stats(sur)
     assert judged == d.n // 8 or judged == (d.n + 7) // 8
     assert handed <= judged
-    # particles handed over carry the plain result exactly
-    assert np.median(rel) < 1e-2, f"median relative error {np.median(rel)}"
+    # particles handed over carry the plain result exactly; the others are within the
+    # configuration's 1e-3 (the same network measured 2.7e-4 median on this scene)
+    assert np.median(rel) < 1e-3, f"median relative error {np.median(rel)}"
     assert np.isfinite(cs).all()
     _ = c0
 
