@@ -33,6 +33,10 @@ constexpr uint32_t NO_PARTNER = 0xFFFFFFFFu;
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;                      // per thread
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS; // 4096 cells per tile
+// The step's scans take 64 items per thread (16,384 cells per tile): with every tile of the
+// grid in flight at once, a tile's look-back reads its predecessors' status 32 at a time until
+// it meets an inclusive prefix, so fewer, larger tiles shorten the longest look-back.
+constexpr int WIDE_SCAN_ITEMS = 64;
 constexpr int WARP_CELL_MAX = 256;   // cells up to this size are ordered by one warp
 constexpr int BLOCK_CELL_MAX = 8192; // up to this by one block in shared memory
 constexpr uint32_t BIG_LIST_CAP = 1u << 16;
@@ -240,8 +244,12 @@ cudaError_t physics_init();  // per-kernel attributes, once per device before th
 void launch_clear_bins(const DevParams& P, const Scratch& s, int num_sms, cudaStream_t st);
 void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, bool warp_order,
                    cudaStream_t st);
+// narrow: tiles of SCAN_TILE cells (the allocation-free scan's fixed scratch is sized for
+// them), else of SCAN_THREADS * WIDE_SCAN_ITEMS
 void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long long* status,
-                 uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st);
+                 uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st,
+                 bool narrow = false);
+// status words of a scan of n cells (of the narrow tiles: enough for either)
 size_t scan_status_words(uint32_t n);
 // failure-detection self-tests: a bounded wait on a flag nothing sets (see the definitions)
 cudaError_t scan_selftest_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, cudaStream_t st);

@@ -76,7 +76,7 @@ extern "C" mg_status mg_prefix_sum_noalloc(const uint32_t* counts, uint32_t* off
     if (e == cudaSuccess && n > 0) {
         uint32_t* ticket = (uint32_t*)(scratch + NOALLOC_TILES);
         launch_scan(counts, offsets, (uint32_t)n, scratch, ticket, total,
-                    error ? error : ticket + 1, st);
+                    error ? error : ticket + 1, st, /*narrow=*/true);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) {

@@ -162,6 +162,7 @@ void launch_insert(const DevParams& P, const Carried& cur, const Scratch& s, boo
 // ERR_SCAN_TIMEOUT when it gives up.
 size_t scan_status_words(uint32_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
 
+template <int ITEMS>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restrict__ in,
                                                        uint32_t* __restrict__ out, uint32_t n,
                                                        unsigned long long* status,
@@ -172,14 +173,15 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
     if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
-    const uint32_t ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    constexpr uint32_t TILE = SCAN_THREADS * ITEMS;
+    const uint32_t ntiles = (n + TILE - 1) / TILE;
     const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-    const uint32_t per_warp = SCAN_TILE / (SCAN_THREADS / 32);
-    const uint32_t wbase = tile * SCAN_TILE + warp * per_warp;
-    uint32_t vals[SCAN_ITEMS];
+    const uint32_t per_warp = TILE / (SCAN_THREADS / 32);
+    const uint32_t wbase = tile * TILE + warp * per_warp;
+    uint32_t vals[ITEMS];
     uint32_t run = 0;
 #pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; k++) {
+    for (int k = 0; k < ITEMS; k++) {
         uint32_t idx = wbase + k * 32 + lane;
         uint32_t v = idx < n ? in[idx] : 0u;
         uint32_t x = v;
@@ -250,17 +252,24 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
     __syncthreads();
     const uint32_t pre = s_prefix + s_warp[warp];
 #pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; k++) {
+    for (int k = 0; k < ITEMS; k++) {
         uint32_t idx = wbase + k * 32 + lane;
         if (idx < n) out[idx] = pre + vals[k];
     }
 }
 
 void launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, unsigned long long* status,
-                 uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st) {
-    uint32_t tiles = (uint32_t)scan_status_words(n);
-    if (tiles == 0) return;
-    k_scan<<<tiles, SCAN_THREADS, 0, st>>>(in, out, n, status, ticket, total, err, SPIN_LIMIT);
+                 uint32_t* ticket, uint32_t* total, uint32_t* err, cudaStream_t st, bool narrow) {
+    if (n == 0) return;
+    if (narrow) {
+        const uint32_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+        k_scan<SCAN_ITEMS><<<tiles, SCAN_THREADS, 0, st>>>(in, out, n, status, ticket, total, err, SPIN_LIMIT);
+    } else {
+        constexpr uint32_t WIDE_TILE = SCAN_THREADS * WIDE_SCAN_ITEMS;
+        const uint32_t tiles = (n + WIDE_TILE - 1) / WIDE_TILE;
+        k_scan<WIDE_SCAN_ITEMS><<<tiles, SCAN_THREADS, 0, st>>>(in, out, n, status, ticket, total, err,
+                                                                 SPIN_LIMIT);
+    }
 }
 
 // Failure-detection self-test of the look-back wait: a scan of 8 tiles whose first tile is
@@ -280,7 +289,7 @@ cudaError_t scan_selftest_wait_timeout(uint32_t spin_limit, uint32_t* err_bits, 
     const uint32_t init[2] = {1u, 0u};
     if (e == cudaSuccess) e = cudaMemcpyAsync(words, init, sizeof init, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        k_scan<<<tiles - 1, SCAN_THREADS, 0, st>>>(counts, offsets, n, status, words, nullptr,
+        k_scan<SCAN_ITEMS><<<tiles - 1, SCAN_THREADS, 0, st>>>(counts, offsets, n, status, words, nullptr,
                                                    words + 1, spin_limit);
         e = cudaGetLastError();
     }
