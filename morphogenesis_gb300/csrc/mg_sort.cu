@@ -497,11 +497,16 @@ __global__ void __launch_bounds__(MG_PLAIN_MAX_THREADS) k_gather(DevParams P, Ca
     const uint32_t cap = P.cap;
     if (p >= cap) return;
     if ((parts & GATHER_CORE) && !(parts & GATHER_REORIGIN)) {
+        // slot p read as an origin: the six partners loaded first, then remapped and stored
+        // (a store may alias the next slot's load as far as the compiler knows, which would
+        // otherwise keep each slot's two loads waiting for the previous slot's store)
+        uint32_t j[NB];
 #pragma unroll
-        for (int a = 0; a < NB; a++) {  // slot p read as an origin
-            uint32_t* q = D.partner + bond_ip(cap, a, p);
-            *q = remap(*q, cap, newidx);
-        }
+        for (int a = 0; a < NB; a++) j[a] = D.partner[bond_ip(cap, a, p)];
+#pragma unroll
+        for (int a = 0; a < NB; a++) j[a] = remap(j[a], cap, newidx);
+#pragma unroll
+        for (int a = 0; a < NB; a++) D.partner[bond_ip(cap, a, p)] = j[a];
     }
     const uint32_t nact = *nactive_p;
     if (p < nact) {
