@@ -521,8 +521,10 @@ mg_status mg_selftest_bounded_wait(int32_t which, uint32_t spin_limit);
  *                    the scan), so pass an error word wherever a timeout must be detected
  *   stream           a cudaStream_t passed as void* (NULL: the default stream); the call is
  *                    asynchronous on it and uses the current device
- * The first call on each device looks up the scratch address (a one-time set-up); make that
- * first call, with the device current, before any stream capture begins.  Calls on one device
+ * Every call looks up the scratch's address on the current device (cudaGetSymbolAddress, a
+ * host-side lookup that allocates nothing, so a device reset cannot leave a stale address);
+ * a device's first call may load the library's device code, so make that first call, with
+ * the device current, before any stream capture begins.  Calls on one device
  * share the scratch: calls whose scans can overlap in time (different streams without
  * ordering, or several host threads at once) race and give wrong offsets; order them. */
 mg_status mg_prefix_sum_noalloc(const uint32_t* counts, uint32_t* offsets, uint64_t n,

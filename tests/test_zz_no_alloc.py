@@ -87,7 +87,7 @@ def test_noalloc_scan_allocates_nothing(built):
     out = torch.empty_like(dc)
     total = torch.zeros(1, dtype=torch.int32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
-    assert _scan(lib, torch, dc, out, total, err) == 0  # first call: one-time scratch lookup
+    assert _scan(lib, torch, dc, out, total, err) == 0  # warm-up: the device code is loaded
     torch.cuda.synchronize()
     free0, _ = torch.cuda.mem_get_info()
     for _ in range(8):
